@@ -1,0 +1,253 @@
+/*
+ * mcx.h - C ABI of the GB300 transport + per-cell balance library (libmcx.so).
+ *
+ * This is the drop-in boundary for the MOCASSIN iteration hot path.  Every
+ * entry point below replaces one loop (or one set-up routine) of the Fortran
+ * reference; the reference routine it replaces is cited beside it as
+ * path:line inside the MOCASSIN source tree (source/...).  A Fortran driver
+ * binds these through ISO_C_BINDING; Python binds them through ctypes.
+ *
+ * Conventions
+ *  - Plain C types only: pointers, sizes, int32/int64/float/double.
+ *  - Arrays crossing the boundary use the reference's Fortran layout:
+ *      per-cell x per-frequency arrays  A(0:nCells, 1:nbins)  -> [nbins][nCells+1]
+ *        (cell index fastest, exactly the column-major memory of the Fortran array)
+ *      ionDen(0:nCells, 1:nElementsUsed, 1:nstages)           -> [nstages][nElemUsed][nCells+1]
+ *      active(1:nx,1:ny,1:nz)                                 -> [nz][ny][nx] (x fastest)
+ *  - Every function returns an int status (MCX_OK == 0).  The library never
+ *    exits the process (the reference calls `stop`); the message of the last
+ *    failure is returned by mcx_last_error / mcx_setup_last_error.
+ *  - A context (mcx_ctx) owns device memory, one CUDA stream and the
+ *    device-resident copies of the tables and grid state.  One context per
+ *    host thread / rank; there is no global mutable state.
+ */
+#ifndef MCX_H
+#define MCX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define MCX_OK              0
+#define MCX_ERR_INPUT       1   /* invalid argument / input deck           */
+#define MCX_ERR_IO          2   /* data or input file missing / unreadable */
+#define MCX_ERR_CUDA        3   /* CUDA runtime error                       */
+#define MCX_ERR_NOMEM       4   /* allocation failure                       */
+#define MCX_ERR_STATE       5   /* call out of order (e.g. no grid loaded)  */
+#define MCX_ERR_STEP_LIMIT  6   /* a packet hit the reference's step limits */
+#define MCX_ERR_TIMEOUT     7   /* a bounded device wait gave up            */
+#define MCX_ERR_INTERNAL    8
+
+/* ------------------------------------------------------------- array ids */
+/* Ids used by mcx_setup_get / mcx_setup_set / mcx_get / mcx_put. */
+enum mcx_array_id {
+    MCX_ARR_NU = 1,          /* float [nbins]        nuArray [Ryd]                */
+    MCX_ARR_WIDFLX,          /* float [nbins]        widFlx  [Ryd]                */
+    MCX_ARR_XSEC,            /* float [nxsec]        xSecArray                    */
+    MCX_ARR_SRC_CDF,         /* float [nbins]        inSpectrumProbDen(1,:)       */
+    MCX_ARR_KN_SIGMA_T,      /* float [nbins]        KNsigmaT                     */
+    MCX_ARR_KN_CDF,          /* float [180][nbins]   KNsigmaArray(nbins,180)      */
+    MCX_ARR_PCOMP,           /* float [180][nbins]   PcompArray(nbins,180)        */
+    MCX_ARR_XAXIS,           /* float [nx]                                        */
+    MCX_ARR_YAXIS,           /* float [ny]                                        */
+    MCX_ARR_ZAXIS,           /* float [nz]                                        */
+    MCX_ARR_ACTIVE,          /* int32 [nz][ny][nx]   active(nx,ny,nz)             */
+    MCX_ARR_HDEN,            /* float [nCells+1]                                  */
+    MCX_ARR_TE,              /* float [nCells+1]                                  */
+    MCX_ARR_NE,              /* float [nCells+1]                                  */
+    MCX_ARR_TEOLD,           /* float [nCells+1]                                  */
+    MCX_ARR_NEOLD,           /* float [nCells+1]                                  */
+    MCX_ARR_IONDEN,          /* float [nstages][nElemUsed][nCells+1]              */
+    MCX_ARR_OPACITY,         /* float [nbins][nCells+1]  opacity(0:C,1:B)         */
+    MCX_ARR_RECPDF,          /* float [nbins][nCells+1]  recPDF(0:C,1:B)          */
+    MCX_ARR_TOTAL_LINES,     /* float [nCells+1]         totalLines(0:C)          */
+    MCX_ARR_JSTE,            /* double[nbins][nCells+1]  Jste(0:C,1:B)            */
+    MCX_ARR_ESCAPED,         /* double[nbins+1][nCells+1] escapedPackets(0:C,0:B,0) */
+    MCX_ARR_VOLUME,          /* float [nCells+1]      getVolume per active cell    */
+    MCX_ARR_ELEM_ABUN,       /* float [30]            elemAbun(1,1:30)             */
+    MCX_ARR_GAUNT_TE,        /* float [nCells+1]      Te at which the ff Gaunt factor
+                                                      was last tabulated, per cell  */
+    MCX_ARR_SCAOPAC,         /* float [nbins][nCells+1] dust scaOpac(0:C,1:B)      */
+    MCX_ARR_DUSTPDF,         /* float [nbins][nCells+1] dustPDF(0:C,1:B)           */
+    MCX_ARR_NDUST,           /* float [nCells+1]                                   */
+    MCX_ARR_LG_CONVERGED,    /* int32 [nCells+1]                                   */
+    MCX_ARR_H_EST,           /* double[nbins][nCells+1] H(0:C,1:B) (radPress only) */
+    MCX_ARR_COUNT_
+};
+
+/* Set-up-only tables (mcx_setup_get only). */
+#define MCX_SARR_POINTERS      1001  /* int32[32]: HlevXSecP(1), HlevNuP(1), HeISingXSecP(1), HeIlevNuP(1),
+                                        HeIIXSecP(1), HeIIlevNuP(1), bremsXSecP, lymanP, KshellLimitP,
+                                        secIonP, cRecoilHP, cRecoilHeP, xrayP, BjumpP, 0...          */
+#define MCX_SARR_ELEMENT_P     1002  /* int32[30][30][7][3] elementP(elem,ion,shell,k) at [elem-1][ion-1][shell-1][k-1] */
+#define MCX_SARR_N_SHELLS      1003  /* int32[30][30] nShells(elem,ion)                                */
+#define MCX_SARR_ELEM_XREF     1004  /* int32[30] elementXref                                           */
+#define MCX_SARR_ION_EDGE      1005  /* float[nEdges] ionEdge (sorted)                                  */
+#define MCX_SARR_COMXSEC_H     1006  /* float[nbins] comXSecH                                           */
+#define MCX_SARR_COMXSEC_C     1007  /* float[nbins] comXSecC                                           */
+#define MCX_SARR_XSEC_RECOIL   1008  /* float[nbins] xSecRecoil                                         */
+
+/* -------------------------------------------------------------- set-up */
+/* Host-side model built from an input deck.  Replaces readInput
+ * (source/set_input_mod.f90:12-708), initCartesianGrid
+ * (source/grid_mod.f90:21-608), initXSecArray (source/ph_mod.f90:204-517),
+ * setContinuum/setProbDen (source/continuum_mod.f90:33-504), fillGrid /
+ * setMotherGrid (source/grid_mod.f90:651-1832) and setStarPosition
+ * (source/grid_mod.f90:3690-3790). */
+typedef struct mcx_setup mcx_setup;
+
+/* Frequency-mesh modes. */
+#define MCX_MESH_REFERENCE  0   /* exactly the reference's choice (fill() mesh for nuMax > 25) */
+#define MCX_MESH_LOG_EDGES  1   /* the reference's nuMax <= 25 construction (log mesh with the
+                                   H series edges and ionisation thresholds inserted) forced at
+                                   the deck's nbins for any nuMax                               */
+
+typedef struct mcx_setup_opts {
+    int32_t mesh_mode;          /* MCX_MESH_*                                        */
+    int32_t reserved[7];
+} mcx_setup_opts;
+
+typedef struct mcx_setup_info {
+    int32_t nx, ny, nz;
+    int32_t n_cells;            /* active cells (ids 1..n_cells; 0 = inactive)        */
+    int32_t nbins;
+    int32_t n_xsec;             /* length of xSecArray                                */
+    int32_t n_elem_used;        /* nElementsUsed                                      */
+    int32_t nstages;
+    int32_t symmetric_xyz, lg_gas, lg_dust, lg_compton;
+    int32_t star_idx[3];        /* starIndeces(1,1:3), 1-based, -1 outside the grid    */
+    int32_t lyman_p;            /* lymanP (1-based)                                   */
+    int64_t n_photons;          /* nPhotons(1)                                        */
+    int32_t max_iterate_mc;
+    int32_t n_species, n_sizes;
+    float   star_pos[3];        /* starPosition(1) [cm]                               */
+    float   r_out, r_in;        /* R_out, R_in [cm]                                   */
+    float   l_star;             /* Lstar(1) [e36 erg/s]                               */
+    float   l_phot;             /* LPhot [e36 phot/s]                                 */
+    float   ion_edge1;          /* ionEdge(1) [Ryd]                                   */
+    float   te_start;
+    float   min_convergence;    /* minConvergence [%]                                 */
+    float   xhi_limit;          /* XHILimit                                           */
+    int32_t reserved[8];
+} mcx_setup_info;
+
+int  mcx_setup_from_input(const char* input_file, const char* data_dir,
+                          const mcx_setup_opts* opts, mcx_setup** out);
+void mcx_setup_free(mcx_setup* s);
+int  mcx_setup_info_get(const mcx_setup* s, mcx_setup_info* info);
+/* Copy an array out of / into the set-up (sizes in bytes must match exactly). */
+int  mcx_setup_get(const mcx_setup* s, int32_t array_id, void* dst, size_t nbytes);
+/* Number of elements of a set-up array (for MCX_SARR_ION_EDGE and the others). */
+int  mcx_setup_len(const mcx_setup* s, int32_t array_id, int64_t* count);
+int  mcx_setup_set(mcx_setup* s, int32_t array_id, const void* src, size_t nbytes);
+/* Message of the last set-up failure of this thread. */
+const char* mcx_setup_last_error(void);
+
+/* ---------------------------------------------------------- device context */
+typedef struct mcx_ctx mcx_ctx;
+
+int  mcx_ctx_create(int32_t device, mcx_ctx** out);
+void mcx_ctx_destroy(mcx_ctx* ctx);
+int  mcx_last_error(const mcx_ctx* ctx, char* buf, size_t len);
+int  mcx_sync(mcx_ctx* ctx);
+
+/* Upload tables and the grid state of a set-up to the device (once per model). */
+int  mcx_load(mcx_ctx* ctx, const mcx_setup* s);
+
+/* Download / upload a device-resident array in the Fortran layout given above.
+ * `host` must hold exactly `nbytes`; this is how a Fortran driver exchanges
+ * state with the library between phases. */
+int  mcx_get(mcx_ctx* ctx, int32_t array_id, void* host, size_t nbytes);
+int  mcx_put(mcx_ctx* ctx, int32_t array_id, const void* host, size_t nbytes);
+
+/* Raw device pointer of a context array (for zero-copy callers). */
+int  mcx_device_ptr(mcx_ctx* ctx, int32_t array_id, void** dptr);
+
+/* ------------------------------------------------------- phase: opacity */
+/* Per-cell opacity kappa(nu): free-free + sum of bound-free x-sections times
+ * ion densities + Klein-Nishina electron scattering.  Replaces the
+ * ionizationDriver loop of iterateMC (source/iteration_mod.f90:112-192) and
+ * ionizationDriver/BoltGaunt/getGauntFF/eDenSum/addOpacity
+ * (source/ionization_mod.f90:26-477), including the skip rule for cells whose
+ * Te and Ne changed by less than 0.5 % (source/iteration_mod.f90:131-149). */
+typedef struct mcx_phase_opts {
+    int32_t n_iterate_mc;       /* nIterateMC (1-based); the skip rule applies when > 1 */
+    int32_t reserved[7];
+} mcx_phase_opts;
+
+typedef struct mcx_phase_stats {
+    int64_t cells_computed;
+    int64_t cells_skipped;
+    float   kernel_ms;          /* CUDA-event time of the phase's kernels            */
+    float   reserved_f[3];
+    int64_t reserved[4];
+} mcx_phase_stats;
+
+int  mcx_opacity(mcx_ctx* ctx, const mcx_phase_opts* opts, mcx_phase_stats* stats);
+
+/* ------------------------------------------------------ phase: transport */
+/* Monte Carlo transport of n packets from source iStar, accumulating the
+ * path-length estimator of the mean intensity J_nu (Jste) and the escape
+ * tally.  Replaces energyPacketDriver / energyPacketRun / newPhotonPacket /
+ * initPhotonPacket / getNu2 / pathSegment / comptonScatter
+ * (source/photon_mod.f90:28-416, 418-741, 744-896, 928-972, 976-1756,
+ * 1758-4085, 6805-6848) for a single mother grid without plane-parallel
+ * illumination.  Packet k (0-based, global id counter_base + k) draws its
+ * random numbers from its own Philox4x32-10 stream keyed by `seed`, so the
+ * result does not depend on scheduling and ranks can shard packets by
+ * counter range. */
+#define MCX_PREC_FP32_GEOM  0   /* FP32 packet geometry / tau, FP64 J accumulation */
+#define MCX_PREC_FP64       1   /* FP64 everywhere (the plain path)                */
+
+typedef struct mcx_transport_opts {
+    int32_t istar;              /* 1-based source index                                */
+    int32_t precision;          /* MCX_PREC_*                                          */
+    int64_t n_packets;          /* packets of this call                                */
+    uint64_t seed;              /* Philox key                                          */
+    uint64_t counter_base;      /* global id of the first packet of this call          */
+    int64_t n_photons_norm;     /* nPhotons(iStar) used for deltaE = Lstar/nPhotons;
+                                   0 means n_packets                                   */
+    int32_t zero_estimators;    /* 1: clear Jste/escaped before transporting           */
+    int32_t block_size;         /* 0 = library default                                 */
+    int32_t grid_mult;          /* persistent blocks per SM; 0 = library default        */
+    int32_t chunk;              /* packets handed out per queue grab; 0 = default       */
+    int32_t reserved[4];
+} mcx_transport_opts;
+
+typedef struct mcx_transport_stats {
+    int64_t crossings;          /* cell-wall crossings (estimator updates of a full segment) */
+    int64_t interactions;       /* in-cell interactions (estimator update of a partial segment) */
+    int64_t absorptions;        /* absorbed and re-emitted as diffuse / dustEmi packets      */
+    int64_t scatterings;        /* Compton or dust scatterings                               */
+    int64_t escaped;            /* packets that left the grid / R_out                         */
+    int64_t line_escapes;       /* diffuse packets emitted as (untransported) line photons    */
+    int64_t trapped;            /* histories that hit recursionLimit / safeLimit              */
+    int64_t emissions;          /* frequency draws from a CDF (source + re-emission)          */
+    double  q_phot;             /* Qphot (e36 photons/s above 1 Ryd emitted by the source)    */
+    float   kernel_ms;          /* CUDA-event time of the transport kernel                    */
+    float   reserved_f[3];
+    int64_t reserved[4];
+} mcx_transport_stats;
+
+int  mcx_transport(mcx_ctx* ctx, const mcx_transport_opts* opts, mcx_transport_stats* stats);
+
+/* J normalisation after all sources: Jste *= 1e-9 and /8 in octant mode;
+ * escaped /8 in octant mode (source/iteration_mod.f90:1002-1031). */
+int  mcx_normalize_j(mcx_ctx* ctx);
+
+/* ------------------------------------------------------------- timing */
+/* CUDA events on the context stream (for callers that time a group of calls). */
+int  mcx_timer_start(mcx_ctx* ctx);
+int  mcx_timer_stop(mcx_ctx* ctx, float* ms);
+
+/* ------------------------------------------------------------- version */
+const char* mcx_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MCX_H */

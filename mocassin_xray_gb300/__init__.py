@@ -1,0 +1,7 @@
+"""GB300-native (sm_103a) MOCASSIN iteration hot path: Monte Carlo transport
+of photon packets and the per-cell opacity / balance phases, behind the C ABI
+of libmcx.so (include/mcx.h)."""
+from . import abi, configs
+from .model import Context, Setup
+
+__all__ = ["abi", "configs", "Context", "Setup"]

@@ -1,0 +1,130 @@
+"""ctypes binding of libmcx.so (the C ABI declared in include/mcx.h).
+
+This is the Python side of the drop-in boundary: the same entry points a
+Fortran driver binds through ISO_C_BINDING.  Loading fails loudly when the
+library has not been built; there is no fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "libmcx.so"
+
+MCX_OK = 0
+ERRORS = {1: "MCX_ERR_INPUT", 2: "MCX_ERR_IO", 3: "MCX_ERR_CUDA", 4: "MCX_ERR_NOMEM", 5: "MCX_ERR_STATE",
+          6: "MCX_ERR_STEP_LIMIT", 7: "MCX_ERR_TIMEOUT", 8: "MCX_ERR_INTERNAL"}
+
+# array ids (enum mcx_array_id)
+(ARR_NU, ARR_WIDFLX, ARR_XSEC, ARR_SRC_CDF, ARR_KN_SIGMA_T, ARR_KN_CDF, ARR_PCOMP, ARR_XAXIS, ARR_YAXIS,
+ ARR_ZAXIS, ARR_ACTIVE, ARR_HDEN, ARR_TE, ARR_NE, ARR_TEOLD, ARR_NEOLD, ARR_IONDEN, ARR_OPACITY, ARR_RECPDF,
+ ARR_TOTAL_LINES, ARR_JSTE, ARR_ESCAPED, ARR_VOLUME, ARR_ELEM_ABUN, ARR_GAUNT_TE, ARR_SCAOPAC, ARR_DUSTPDF,
+ ARR_NDUST, ARR_LG_CONVERGED, ARR_H_EST) = range(1, 31)
+SARR_POINTERS, SARR_ELEMENT_P, SARR_N_SHELLS, SARR_ELEM_XREF, SARR_ION_EDGE, SARR_COMXSEC_H, \
+    SARR_COMXSEC_C, SARR_XSEC_RECOIL = range(1001, 1009)
+
+MESH_REFERENCE, MESH_LOG_EDGES = 0, 1
+PREC_FP32_GEOM, PREC_FP64 = 0, 1
+
+
+class SetupOpts(C.Structure):
+    _fields_ = [("mesh_mode", C.c_int32), ("reserved", C.c_int32 * 7)]
+
+
+class SetupInfo(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("n_cells", C.c_int32),
+                ("nbins", C.c_int32), ("n_xsec", C.c_int32), ("n_elem_used", C.c_int32), ("nstages", C.c_int32),
+                ("symmetric_xyz", C.c_int32), ("lg_gas", C.c_int32), ("lg_dust", C.c_int32),
+                ("lg_compton", C.c_int32), ("star_idx", C.c_int32 * 3), ("lyman_p", C.c_int32),
+                ("n_photons", C.c_int64), ("max_iterate_mc", C.c_int32), ("n_species", C.c_int32),
+                ("n_sizes", C.c_int32), ("star_pos", C.c_float * 3), ("r_out", C.c_float), ("r_in", C.c_float),
+                ("l_star", C.c_float), ("l_phot", C.c_float), ("ion_edge1", C.c_float), ("te_start", C.c_float),
+                ("min_convergence", C.c_float), ("xhi_limit", C.c_float), ("reserved", C.c_int32 * 8)]
+
+
+class PhaseOpts(C.Structure):
+    _fields_ = [("n_iterate_mc", C.c_int32), ("reserved", C.c_int32 * 7)]
+
+
+class PhaseStats(C.Structure):
+    _fields_ = [("cells_computed", C.c_int64), ("cells_skipped", C.c_int64), ("kernel_ms", C.c_float),
+                ("reserved_f", C.c_float * 3), ("reserved", C.c_int64 * 4)]
+
+
+class TransportOpts(C.Structure):
+    _fields_ = [("istar", C.c_int32), ("precision", C.c_int32), ("n_packets", C.c_int64), ("seed", C.c_uint64),
+                ("counter_base", C.c_uint64), ("n_photons_norm", C.c_int64), ("zero_estimators", C.c_int32),
+                ("block_size", C.c_int32), ("grid_mult", C.c_int32), ("chunk", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
+
+
+class TransportStats(C.Structure):
+    _fields_ = [("crossings", C.c_int64), ("interactions", C.c_int64), ("absorptions", C.c_int64),
+                ("scatterings", C.c_int64), ("escaped", C.c_int64), ("line_escapes", C.c_int64),
+                ("trapped", C.c_int64), ("emissions", C.c_int64), ("q_phot", C.c_double), ("kernel_ms", C.c_float),
+                ("reserved_f", C.c_float * 3), ("reserved", C.c_int64 * 4)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("reserved")}
+
+
+# exported symbols and their signatures: (name, restype, argtypes)
+_P = C.c_void_p
+SIGNATURES = [
+    ("mcx_setup_from_input", C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(SetupOpts), C.POINTER(_P)]),
+    ("mcx_setup_free", None, [_P]),
+    ("mcx_setup_info_get", C.c_int, [_P, C.POINTER(SetupInfo)]),
+    ("mcx_setup_get", C.c_int, [_P, C.c_int32, _P, C.c_size_t]),
+    ("mcx_setup_len", C.c_int, [_P, C.c_int32, C.POINTER(C.c_int64)]),
+    ("mcx_setup_set", C.c_int, [_P, C.c_int32, _P, C.c_size_t]),
+    ("mcx_setup_last_error", C.c_char_p, []),
+    ("mcx_ctx_create", C.c_int, [C.c_int32, C.POINTER(_P)]),
+    ("mcx_ctx_destroy", None, [_P]),
+    ("mcx_last_error", C.c_int, [_P, C.c_char_p, C.c_size_t]),
+    ("mcx_sync", C.c_int, [_P]),
+    ("mcx_load", C.c_int, [_P, _P]),
+    ("mcx_get", C.c_int, [_P, C.c_int32, _P, C.c_size_t]),
+    ("mcx_put", C.c_int, [_P, C.c_int32, _P, C.c_size_t]),
+    ("mcx_device_ptr", C.c_int, [_P, C.c_int32, C.POINTER(_P)]),
+    ("mcx_opacity", C.c_int, [_P, C.POINTER(PhaseOpts), C.POINTER(PhaseStats)]),
+    ("mcx_transport", C.c_int, [_P, C.POINTER(TransportOpts), C.POINTER(TransportStats)]),
+    ("mcx_normalize_j", C.c_int, [_P]),
+    ("mcx_timer_start", C.c_int, [_P]),
+    ("mcx_timer_stop", C.c_int, [_P, C.POINTER(C.c_float)]),
+    ("mcx_version", C.c_char_p, []),
+]
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """The loaded libmcx.so; raises if it is missing (no fallback path exists)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+        l = C.CDLL(str(LIB_PATH))
+        for name, res, args in SIGNATURES:
+            f = getattr(l, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = l
+    return _lib
+
+
+class McxError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def check_setup(rc: int) -> None:
+    if rc != MCX_OK:
+        raise McxError(rc, lib().mcx_setup_last_error().decode())
+
+
+def as_ptr(a: np.ndarray) -> C.c_void_p:
+    assert a.flags["C_CONTIGUOUS"]
+    return C.c_void_p(a.ctypes.data)

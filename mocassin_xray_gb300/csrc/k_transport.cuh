@@ -1,0 +1,487 @@
+// k_transport.cuh - persistent Monte Carlo packet-transport kernel.
+//
+// GB300 design: one thread owns one packet history; a warp keeps all 32 lanes
+// busy by refilling idle lanes from a device work queue with one
+// warp-aggregated atomic per refill.  Each loop iteration advances every lane
+// by one event (an emission, or one cell step of pathSegment), so the lanes of
+// a warp stay on the same code path.  Packet geometry and optical depth run in
+// the template precision R (float: the production path; double: the plain
+// FP64 path); the mean-intensity estimator J_nu is accumulated with FP64
+// atomics into the Fortran-layout array Jste[nu][cell].  The source spectrum
+// CDF, the frequency mesh and the axes are staged in shared memory.
+//
+// Physics follows the reference routine by routine (single mother grid, no
+// plane-parallel illumination):
+//   energyPacketDriver/energyPacketRun   source/photon_mod.f90:28-741
+//   initPhotonPacket / getNu2            source/photon_mod.f90:744-972
+//   newPhotonPacket                      source/photon_mod.f90:976-1756
+//   pathSegment                          source/photon_mod.f90:1758-4085
+//   comptonScatter                       source/photon_mod.f90:6805-6848
+// Packet k of a call (global id counter_base + k) draws its uniforms from its
+// own Philox4x32-10 stream, so a history does not depend on scheduling.
+// Jste(0,:), the dump row the reference fills for inactive cells and never
+// reads, is not accumulated.
+#pragma once
+#include "mcx_device.cuh"
+
+namespace mcx {
+
+enum : int { PT_STELLAR = 0, PT_DIFFUSE = 1, PT_DUSTEMI = 2 };
+enum : int { ST_IDLE = 0, ST_EMIT = 1, ST_STEP = 2, ST_DONE = 3 };
+
+constexpr int kSafeLimit = 500000;        // pathSegment (source/photon_mod.f90:1873-1878)
+constexpr int kRecursionLimit = 100000;   // recursionLimit (source/constants_mod.f90:70)
+
+template <typename R> struct RMath;
+template <> struct RMath<float> {
+  static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+  static __device__ __forceinline__ float log_(float x) { return logf(x); }
+  static __device__ __forceinline__ float cos_(float x) { return cosf(x); }
+  static __device__ __forceinline__ float sin_(float x) { return sinf(x); }
+  static __device__ __forceinline__ float abs_(float x) { return fabsf(x); }
+  static __device__ __forceinline__ float min_(float a, float b) { return fminf(a, b); }
+};
+template <> struct RMath<double> {
+  static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+  static __device__ __forceinline__ double log_(double x) { return log(x); }
+  static __device__ __forceinline__ double cos_(double x) { return cos(x); }
+  static __device__ __forceinline__ double sin_(double x) { return sin(x); }
+  static __device__ __forceinline__ double abs_(double x) { return fabs(x); }
+  static __device__ __forceinline__ double min_(double a, double b) { return fmin(a, b); }
+};
+
+template <typename R>
+struct Packet {
+  R x, y, z, vx, vy, vz;
+  R nu, absTau, passProb;
+  int xP, yP, zP, nuP, origin;
+  int type, lgStellar, nEmit, nStep;
+  PacketRng rng;
+};
+
+struct LocalCounters {
+  unsigned long long crossings = 0, interactions = 0, absorptions = 0, scatterings = 0;
+  unsigned long long escaped = 0, lineEscapes = 0, trapped = 0, emissions = 0, errors = 0;
+  double qPhot = 0.;
+};
+
+template <typename R>
+struct TransportShared {
+  const float* X; const float* Y; const float* Z;
+  const float* nu; const float* cdf;
+};
+
+__device__ __forceinline__ int activeAt(const DevGrid& g, int i, int j, int k) {
+  return __ldg(g.active + (size_t)(i - 1) + (size_t)g.nx * ((size_t)(j - 1) + (size_t)g.ny * (size_t)(k - 1)));
+}
+
+// getNu2 on a monotone CDF: the reference's linear scan "last i with u >= cdf(i)"
+// equals the count of leading entries <= u, found here by bisection.
+template <typename R>
+__device__ __forceinline__ int sampleCDF(const float* cdf, int len, int nbins, R u) {
+  int lo = 0, hi = len < nbins ? len : nbins;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (u >= (R)cdf[mid]) lo = mid + 1; else hi = mid;
+  }
+  int nuP = lo < 1 ? 1 : lo;
+  if (nuP < nbins) ++nuP;
+  return nuP;
+}
+
+template <typename R>
+__device__ __forceinline__ R draw(Packet<R>& p) { return uniformFrom<R>(p.rng.next()); }
+
+// initPhotonPacket (source/photon_mod.f90:744-896): position, frequency, an
+// isotropic direction (re-drawn while a component is exactly zero) and the
+// octant fold for stellar packets.
+template <typename R>
+__device__ __forceinline__ void initPacket(const DevGrid& g, const TransportShared<R>& sh, Packet<R>& p, int nuP,
+                                           bool line, bool stellar, int xP, int yP, int zP) {
+  using M = RMath<R>;
+  p.nuP = nuP;
+  p.lgStellar = stellar;
+  p.nu = line ? R(0) : (R)sh.nu[nuP - 1];
+  p.xP = xP; p.yP = yP; p.zP = zP;
+  for (int rep = 0; rep < 1000000; ++rep) {
+    R r1 = draw(p);
+    R w = R(2) * r1 - R(1);
+    R t = M::sqrt_(R(1) - w * w);
+    R r2 = draw(p);
+    R ang = R(3.141592654) * (R(2) * r2 - R(1));
+    p.vx = t * M::cos_(ang); p.vy = t * M::sin_(ang); p.vz = w;
+    if (p.vx != R(0) && p.vy != R(0) && p.vz != R(0)) break;
+  }
+  if (g.symmetric && stellar) {
+    if (p.vx < R(0)) p.vx = -p.vx;
+    if (p.vy < R(0)) p.vy = -p.vy;
+    if (p.vz < R(0)) p.vz = -p.vz;
+  }
+  p.origin = (xP > 0 && yP > 0 && zP > 0) ? activeAt(g, xP, yP, zP) : 0;
+}
+
+template <typename R>
+__device__ __forceinline__ void escapeTally(const DevGrid& g, const DevTransportOut& out, const Packet<R>& p,
+                                            double deltaE, LocalCounters& lc) {
+  atomicAdd(out.escaped + (size_t)p.origin + ((size_t)g.nCells + 1) * (size_t)p.nuP, deltaE);
+  ++lc.escaped;
+}
+
+template <typename R>
+__device__ __forceinline__ void deposit(const DevGrid& g, const DevTransportOut& out, int cell, int nuP, R dl,
+                                        R dV, R deltaE, R costheta) {
+  if (cell <= 0) return;
+  size_t idx = (size_t)cell + ((size_t)g.nCells + 1) * (size_t)(nuP - 1);
+  atomicAdd(out.jste + idx, (double)(dl * deltaE / dV));
+  if (out.hEst) atomicAdd(out.hEst + idx, (double)((dl * deltaE) * costheta / dV));
+}
+
+// locate (source/interpolation_mod.f90:49-106) on the frequency mesh
+template <typename R>
+__device__ __forceinline__ int locateNu(const float* xa, int n, R x) {
+  if (x > (R)xa[n - 1]) return n;
+  if (x < (R)xa[0]) return 0;
+  int jlow = 0, jup = n + 1;
+  for (int it = 0; it < 64; ++it) {
+    if (jup - jlow < 1) break;
+    int jm = (jup + jlow) >> 1;
+    R v = (R)xa[jm - 1];
+    if (v == x) return jm;
+    if (x > v) { if (jlow == jm) break; jlow = jm; } else jup = jm;
+  }
+  return jlow;
+}
+
+// comptonScatter (source/photon_mod.f90:6805-6848)
+template <typename R>
+__device__ __forceinline__ void comptonScatter(const DevGrid& g, const TransportShared<R>& sh, Packet<R>& p) {
+  using M = RMath<R>;
+  const float* row = g.KNcdfT + (size_t)(p.nuP - 1) * 180;
+  int th = sampleCDF<R>(row, 180, g.nbins, draw(p));
+  R newTheta = (R)th * R(3.141592654) / R(180);
+  R u = draw(p);
+  R w = R(2) * u - R(1);
+  R t = M::sqrt_(R(1) - w * w);
+  p.vx = t * M::cos_(newTheta);
+  p.vy = t * M::sin_(newTheta);
+  p.vz = w;
+  int thc = th > 180 ? 180 : th;
+  R newNu = p.nu * (R)__ldg(g.PcompT + (size_t)(p.nuP - 1) * 180 + (thc - 1));
+  int newNuP = locateNu<R>(sh.nu, g.nbins, newNu);
+  if (newNuP < 1) newNuP = 1;
+  p.nu = newNu;
+  p.nuP = newNuP;
+}
+
+// Volume of cell `cell` in the geometry precision.
+template <typename R> __device__ __forceinline__ R cellVolume(const DevGrid& g, int cell);
+template <> __device__ __forceinline__ float cellVolume<float>(const DevGrid& g, int cell) { return __ldg(g.volF + cell); }
+template <> __device__ __forceinline__ double cellVolume<double>(const DevGrid& g, int cell) { return __ldg(g.volD + cell); }
+
+// energyPacketRun + newPhotonPacket: create the packet of history step p.type
+// at (p.x,p.y,p.z; p.xP,p.yP,p.zP).  Returns the next state.
+template <typename R>
+__device__ int emitPacket(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,
+                          const TransportShared<R>& sh, Packet<R>& p, double deltaE, LocalCounters& lc) {
+  using M = RMath<R>;
+  if (p.nEmit >= kRecursionLimit) { ++lc.trapped; return ST_IDLE; }
+  ++p.nEmit;
+  bool line = false;
+  if (p.type == PT_STELLAR) {
+    int nuP = sampleCDF<R>(sh.cdf, g.nbins, g.nbins, draw(p));
+    ++lc.emissions;
+    p.x = (R)g.starPos[0]; p.y = (R)g.starPos[1]; p.z = (R)g.starPos[2];
+    initPacket<R>(g, sh, p, nuP, false, true, g.starIdx[0], g.starIdx[1], g.starIdx[2]);
+    if (p.nu >= R(1)) lc.qPhot += deltaE / (2.1799153e-11 * (double)p.nu);
+  } else {
+    if (p.xP < 1 || p.xP > g.nx || p.yP < 1 || p.yP > g.ny || p.zP < 1 || p.zP > g.nz) { ++lc.errors; return ST_IDLE; }
+    int cell = activeAt(g, p.xP, p.yP, p.zP);
+    if (cell <= 0) { ++lc.errors; return ST_IDLE; }
+    if (p.type == PT_DIFFUSE) {
+      R rnd = R(1) - draw(p);
+      if (rnd <= (R)__ldg(in.totalLines + cell)) {
+        initPacket<R>(g, sh, p, 0, true, false, p.xP, p.yP, p.zP);
+        line = true;
+      } else {
+        int nuP = sampleCDF<R>(in.recCDFT + (size_t)cell * g.nbins, g.nbins, g.nbins, draw(p));
+        ++lc.emissions;
+        initPacket<R>(g, sh, p, nuP, false, false, p.xP, p.yP, p.zP);
+      }
+    } else {
+      int nuP = sampleCDF<R>(in.dustCDFT + (size_t)cell * g.nbins, g.nbins, g.nbins, draw(p));
+      ++lc.emissions;
+      initPacket<R>(g, sh, p, nuP, false, false, p.xP, p.yP, p.zP);
+    }
+  }
+  if (line) {
+    ++lc.lineEscapes;
+    if (p.nEmit >= kRecursionLimit) ++lc.trapped;
+    return ST_IDLE;
+  }
+  if (!g.lgDust && p.nu < (R)g.ionEdge1) {
+    escapeTally<R>(g, out, p, deltaE, lc);
+    if (p.nEmit >= kRecursionLimit) ++lc.trapped;
+    return ST_IDLE;
+  }
+  // pathSegment entry (source/photon_mod.f90:1813-1878)
+  if (p.xP <= 0 || p.xP > g.nx || p.yP <= 0 || p.yP > g.ny || p.zP <= 0 || p.zP > g.nz) { ++lc.errors; return ST_IDLE; }
+  p.absTau = R(0);
+  p.passProb = -M::log_(R(1) - draw(p));
+  p.nStep = 0;
+  return ST_STEP;
+}
+
+// One iteration of pathSegment's main loop (source/photon_mod.f90:1880-4036).
+template <typename R>
+__device__ int stepPacket(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,
+                          const TransportShared<R>& sh, Packet<R>& p, R deltaER, double deltaE, LocalCounters& lc) {
+  using M = RMath<R>;
+  const int nx = g.nx, ny = g.ny, nz = g.nz;
+  const float* X = sh.X; const float* Y = sh.Y; const float* Z = sh.Z;
+#define AXR(A, i) ((R)(A)[(i) - 1])
+  if (++p.nStep > kSafeLimit) { ++lc.trapped; if (p.nEmit >= kRecursionLimit) ++lc.trapped; return ST_IDLE; }
+  int xP = p.xP, yP = p.yP, zP = p.zP;
+  if (xP < 1 || xP > nx || yP < 1 || yP > ny || zP < 1 || zP > nz) { ++lc.errors; return ST_IDLE; }
+  R rx = p.x, ry = p.y, rz = p.z, vx = p.vx, vy = p.vy, vz = p.vz;
+
+  // wall-snap heuristics (source/photon_mod.f90:1882-1919), signed divisor as in the reference
+  if (xP < nx) { R m = (AXR(X, xP) + AXR(X, xP + 1)) / R(2); if (vx > R(0) && M::abs_(rx - m) / m < R(2.e-2)) xP = xP + 1; }
+  if (xP > 1)  { R m = (AXR(X, xP) + AXR(X, xP - 1)) / R(2); if (vx < R(0) && M::abs_(rx - m) / m < R(2.e-2)) xP = xP - 1; }
+  if (yP < ny) { R m = (AXR(Y, yP) + AXR(Y, yP + 1)) / R(2); if (vy > R(0) && M::abs_(ry - m) / m < R(2.e-2)) yP = yP + 1; }
+  if (yP > 1)  { R m = (AXR(Y, yP) + AXR(Y, yP - 1)) / R(2); if (vy < R(0) && M::abs_(ry - m) / m < R(2.e-2)) yP = yP - 1; }
+  if (zP < nz) { R m = (AXR(Z, zP) + AXR(Z, zP + 1)) / R(2); if (vz > R(0) && M::abs_(rz - m) / m < R(2.e-2)) zP = zP + 1; }
+  if (zP > 1)  { R m = (AXR(Z, zP) + AXR(Z, zP - 1)) / R(2); if (vz < R(0) && M::abs_(rz - m) / m < R(2.e-2)) zP = zP - 1; }
+
+  // distances from the walls (source/photon_mod.f90:1933-2084); with one
+  // mother grid the reference's inner loop runs exactly once
+  if (g.symmetric) {
+    if (rx <= AXR(X, 1)) { if (vx < R(0)) vx = -vx; rx = AXR(X, 1); }
+    if (ry <= AXR(Y, 1)) { if (vy < R(0)) vy = -vy; ry = AXR(Y, 1); }
+    if (rz <= AXR(Z, 1)) { if (vz < R(0)) vz = -vz; rz = AXR(Z, 1); }
+  }
+  R dSx, dSy, dSz;
+  bool lost = false;
+  if (vx > R(0)) {
+    if (xP < nx) { dSx = ((AXR(X, xP + 1) + AXR(X, xP)) / R(2) - rx) / vx;
+                   if (M::abs_(dSx) < R(1.e-5)) { rx = (AXR(X, xP + 1) + AXR(X, xP)) / R(2); xP = xP + 1; } }
+    else { dSx = (AXR(X, nx) - rx) / vx; if (M::abs_(dSx) < R(1.e-5)) { rx = AXR(X, nx); lost = true; } }
+  } else if (vx < R(0)) {
+    if (xP > 1) { dSx = ((AXR(X, xP) + AXR(X, xP - 1)) / R(2) - rx) / vx;
+                  if (M::abs_(dSx) < R(1.e-5)) { rx = (AXR(X, xP) + AXR(X, xP - 1)) / R(2); xP = xP - 1; } }
+    else { dSx = (AXR(X, 1) - rx) / vx; if (M::abs_(dSx) < R(1.e-5)) rx = AXR(X, 1); }
+  } else dSx = AXR(X, nx);
+  if (lost) { if (p.nEmit >= kRecursionLimit) ++lc.trapped; return ST_IDLE; }
+  if (vy > R(0)) {
+    if (yP < ny) { dSy = ((AXR(Y, yP + 1) + AXR(Y, yP)) / R(2) - ry) / vy;
+                   if (M::abs_(dSy) < R(1.e-5)) { ry = (AXR(Y, yP + 1) + AXR(Y, yP)) / R(2); yP = yP + 1; } }
+    else { dSy = (AXR(Y, ny) - ry) / vy; if (M::abs_(dSy) < R(1.e-5)) { ry = AXR(Y, ny); lost = true; } }
+  } else if (vy < R(0)) {
+    if (yP > 1) { dSy = ((AXR(Y, yP) + AXR(Y, yP - 1)) / R(2) - ry) / vy;
+                  if (M::abs_(dSy) < R(1.e-5)) { ry = (AXR(Y, yP) + AXR(Y, yP - 1)) / R(2); yP = yP - 1; } }
+    else { dSy = (AXR(Y, 1) - ry) / vy; if (M::abs_(dSy) < R(1.e-5)) ry = AXR(Y, 1); }
+  } else dSy = AXR(Y, ny);
+  if (lost) { if (p.nEmit >= kRecursionLimit) ++lc.trapped; return ST_IDLE; }
+  if (vz > R(0)) {
+    if (zP < nz) { dSz = ((AXR(Z, zP + 1) + AXR(Z, zP)) / R(2) - rz) / vz;
+                   if (M::abs_(dSz) < R(1.e-5)) { rz = (AXR(Z, zP + 1) + AXR(Z, zP)) / R(2); zP = zP + 1; } }
+    else { dSz = (AXR(Z, nz) - rz) / vz; if (M::abs_(dSz) < R(1.e-5)) { rz = AXR(Z, nz); lost = true; } }
+  } else if (vz < R(0)) {
+    if (zP > 1) { dSz = ((AXR(Z, zP) + AXR(Z, zP - 1)) / R(2) - rz) / vz;
+                  if (M::abs_(dSz) < R(1.e-5)) { rz = (AXR(Z, zP) + AXR(Z, zP - 1)) / R(2); zP = zP - 1; } }
+    else { dSz = (AXR(Z, 1) - rz) / vz; if (M::abs_(dSz) < R(1.e-5)) rz = AXR(Z, 1); }
+  } else dSz = AXR(Z, nz);
+  if (lost) { if (p.nEmit >= kRecursionLimit) ++lc.trapped; return ST_IDLE; }
+  if (xP > nx || xP < 1 || yP > ny || yP < 1 || zP > nz || zP < 1) { ++lc.errors; return ST_IDLE; }
+
+  // nearest wall (source/photon_mod.f90:2087-2137)
+  if (M::abs_(dSx) < R(1.e-5)) dSx = AXR(X, nx);
+  if (M::abs_(dSy) < R(1.e-5)) dSy = AXR(Y, ny);
+  if (M::abs_(dSz) < R(1.e-5)) dSz = AXR(Z, nz);
+  dSx = M::abs_(dSx); dSy = M::abs_(dSy); dSz = M::abs_(dSz);
+  R dS;
+  if (dSx <= R(0)) dS = M::min_(dSy, dSz);
+  else if (dSy <= R(0)) dS = M::min_(dSx, dSz);
+  else if (dSz <= R(0)) dS = M::min_(dSx, dSy);
+  else { dS = M::min_(dSx, dSy); dS = M::min_(dS, dSz); }
+  if (!(dS > R(0))) { ++lc.errors; return ST_IDLE; }
+
+  const int cell = activeAt(g, xP, yP, zP);
+  const size_t C1 = (size_t)g.nCells + 1;
+  const R kap = (R)__ldg(in.opacity + (size_t)cell + C1 * (size_t)(p.nuP - 1));
+  const R tauCell = dS * kap;
+  const R dV = cell > 0 ? cellVolume<R>(g, cell) : R(1);
+  R costheta = R(1);
+  if (g.radPress && !(rx == R(0) && ry == R(0) && rz == R(0))) {
+    costheta = ((rx * vx) + (ry * vy) + (rz * vz)) /
+               (R(1.e10) * M::sqrt_((rx / R(1.e10)) * (rx / R(1.e10)) + (ry / R(1.e10)) * (ry / R(1.e10)) +
+                                    (rz / R(1.e10)) * (rz / R(1.e10))));
+  }
+
+  int next = ST_STEP;
+  if ((p.absTau + tauCell > p.passProb) && cell > 0) {
+    // interaction within the cell (source/photon_mod.f90:2244-2700)
+    R dlLoc = (p.passProb - p.absTau) / kap;
+    rx = rx + dlLoc * vx; ry = ry + dlLoc * vy; rz = rz + dlLoc * vz;
+    if (g.symmetric) {
+      if (rx <= AXR(X, 1)) { if (vx < R(0)) vx = -vx; rx = AXR(X, 1); }
+      if (ry <= AXR(Y, 1)) { if (vy < R(0)) vy = -vy; ry = AXR(Y, 1); }
+      if (rz <= AXR(Z, 1)) { if (vz < R(0)) vz = -vz; rz = AXR(Z, 1); }
+    }
+    deposit<R>(g, out, cell, p.nuP, dlLoc, dV, deltaER, costheta);
+    ++lc.interactions;
+    R rad = M::sqrt_((rx / R(1.e10)) * (rx / R(1.e10)) + (ry / R(1.e10)) * (ry / R(1.e10)) +
+                     (rz / R(1.e10)) * (rz / R(1.e10))) * R(1.e10);
+    if (rad >= (R)g.rOut && g.rOut > 0.f) {
+      escapeTally<R>(g, out, p, deltaE, lc);
+      if (p.nEmit >= kRecursionLimit) ++lc.trapped;
+      return ST_IDLE;
+    }
+    if (g.lgDust) {
+      R probSca = (R)__ldg(in.scaOpac + (size_t)cell + C1 * (size_t)(p.nuP - 1)) / kap;
+      R rnd = R(1) - draw(p);
+      if (rnd > probSca) {
+        ++lc.absorptions;
+        p.type = g.lgGas ? PT_DIFFUSE : PT_DUSTEMI;
+        next = ST_EMIT;
+      } else {
+        ++lc.scatterings;
+        initPacket<R>(g, sh, p, p.nuP, false, false, xP, yP, zP);
+        vx = p.vx; vy = p.vy; vz = p.vz;
+        p.absTau = R(0);
+        p.passProb = -M::log_(R(1) - draw(p));
+      }
+    } else {
+      R probSca = g.lgCompton ? (R)__ldg(g.KNsigmaT + p.nuP - 1) * (R)__ldg(in.ne + cell) / kap : R(0);
+      R rnd = R(1) - draw(p);
+      if (rnd <= probSca) {
+        ++lc.scatterings;
+        comptonScatter<R>(g, sh, p);
+        p.origin = cell;
+        vx = p.vx; vy = p.vy; vz = p.vz;
+        p.absTau = R(0);
+        p.passProb = -M::log_(R(1) - draw(p));
+      } else {
+        ++lc.absorptions;
+        p.type = PT_DIFFUSE;
+        next = ST_EMIT;
+      }
+    }
+  } else {
+    // the packet crosses the cell (source/photon_mod.f90:2703-2881)
+    deposit<R>(g, out, cell, p.nuP, dS, dV, deltaER, costheta);
+    ++lc.crossings;
+    p.absTau = p.absTau + tauCell;
+    rx = rx + dS * vx; ry = ry + dS * vy; rz = rz + dS * vz;
+    if (dS == dSx && vx > R(0)) xP = xP + 1;
+    else if (dS == dSx && vx < R(0)) xP = xP - 1;
+    else if (dS == dSy && vy > R(0)) yP = yP + 1;
+    else if (dS == dSy && vy < R(0)) yP = yP - 1;
+    else if (dS == dSz && vz > R(0)) zP = zP + 1;
+    else if (dS == dSz && vz < R(0)) zP = zP - 1;
+    bool esc = false;
+    if (!g.symmetric) {
+      // full-grid escape (source/photon_mod.f90:2884-3244)
+      if (ry < AXR(Y, 1) || yP < 1) esc = true;
+      if (ry > AXR(Y, ny) || yP > ny) esc = true;
+      if (rx <= AXR(X, 1) || xP < 1) esc = true;
+      if (rx >= AXR(X, nx) || xP > nx) esc = true;
+      if (rz <= AXR(Z, 1) || zP < 1) esc = true;
+      if (rz >= AXR(Z, nz) || zP > nz) esc = true;
+    }
+    // grid boundary and mirror planes (source/photon_mod.f90:3607-3890)
+    if (!esc && ((!g.symmetric && (rx <= AXR(X, 1) || ry <= AXR(Y, 1) || rz <= AXR(Z, 1))) ||
+                 rx >= AXR(X, nx) || ry >= AXR(Y, ny) || rz >= AXR(Z, nz) || xP > nx || yP > ny || zP > nz))
+      esc = true;
+    if (esc) {
+      escapeTally<R>(g, out, p, deltaE, lc);
+      if (p.nEmit >= kRecursionLimit) ++lc.trapped;
+      return ST_IDLE;
+    }
+    if (g.symmetric) {
+      if (rx <= AXR(X, 1) || xP < 1) { if (vx < R(0)) vx = -vx; xP = 1; rx = AXR(X, 1); }
+      if (ry <= AXR(Y, 1) || yP < 1) { if (vy < R(0)) vy = -vy; yP = 1; ry = AXR(Y, 1); }
+      if (rz <= AXR(Z, 1) || zP < 1) { if (vz < R(0)) vz = -vz; zP = 1; rz = AXR(Z, 1); }
+    }
+  }
+  // source/photon_mod.f90:3951-4036
+  if (next == ST_STEP && (xP > nx || yP > ny || zP > nz)) {
+    escapeTally<R>(g, out, p, deltaE, lc);
+    if (p.nEmit >= kRecursionLimit) ++lc.trapped;
+    return ST_IDLE;
+  }
+  p.x = rx; p.y = ry; p.z = rz; p.vx = vx; p.vy = vy; p.vz = vz;
+  p.xP = xP; p.yP = yP; p.zP = zP;
+  return next;
+#undef AXR
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256)
+transportKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportCounters* cnt,
+                uint64_t seed, uint64_t base, unsigned long long n, double deltaE) {
+  extern __shared__ float smem[];
+  float* sX = smem;
+  float* sY = sX + g.nx;
+  float* sZ = sY + g.ny;
+  float* sNu = sZ + g.nz;
+  float* sCdf = sNu + g.nbins;
+  for (int i = threadIdx.x; i < g.nx; i += blockDim.x) sX[i] = g.xAxis[i];
+  for (int i = threadIdx.x; i < g.ny; i += blockDim.x) sY[i] = g.yAxis[i];
+  for (int i = threadIdx.x; i < g.nz; i += blockDim.x) sZ[i] = g.zAxis[i];
+  for (int i = threadIdx.x; i < g.nbins; i += blockDim.x) { sNu[i] = g.nu[i]; sCdf[i] = g.srcCDF[i]; }
+  __syncthreads();
+  TransportShared<R> sh{sX, sY, sZ, sNu, sCdf};
+
+  const unsigned FULL = 0xffffffffu;
+  const unsigned lane = threadIdx.x & 31u;
+  const R deltaER = (R)deltaE;
+  LocalCounters lc;
+  Packet<R> p;
+  p.nEmit = 0; p.nStep = 0;
+  int state = ST_IDLE;
+
+  for (;;) {
+    const unsigned need = __ballot_sync(FULL, state == ST_IDLE);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long first = 0;
+      if ((int)lane == leader) first = atomicAdd(&cnt->queue, (unsigned long long)__popc(need));
+      first = __shfl_sync(FULL, first, leader);
+      if (state == ST_IDLE) {
+        const unsigned long long id = first + (unsigned long long)__popc(need & ((1u << lane) - 1u));
+        if (id < n) {
+          p.rng.init(seed, base + id);
+          p.type = PT_STELLAR;
+          p.nEmit = 0;
+          state = ST_EMIT;
+        } else {
+          state = ST_DONE;
+        }
+      }
+    }
+    if (__ballot_sync(FULL, state != ST_DONE) == 0u) break;
+    if (state == ST_EMIT) state = emitPacket<R>(g, in, out, sh, p, deltaE, lc);
+    else if (state == ST_STEP) state = stepPacket<R>(g, in, out, sh, p, deltaER, deltaE, lc);
+  }
+
+  // one atomic per counter per warp
+  auto wsum = [&](unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+    return v;
+  };
+  unsigned long long v;
+  v = wsum(lc.crossings);    if (lane == 0 && v) atomicAdd(&cnt->crossings, v);
+  v = wsum(lc.interactions); if (lane == 0 && v) atomicAdd(&cnt->interactions, v);
+  v = wsum(lc.absorptions);  if (lane == 0 && v) atomicAdd(&cnt->absorptions, v);
+  v = wsum(lc.scatterings);  if (lane == 0 && v) atomicAdd(&cnt->scatterings, v);
+  v = wsum(lc.escaped);      if (lane == 0 && v) atomicAdd(&cnt->escaped, v);
+  v = wsum(lc.lineEscapes);  if (lane == 0 && v) atomicAdd(&cnt->lineEscapes, v);
+  v = wsum(lc.trapped);      if (lane == 0 && v) atomicAdd(&cnt->trapped, v);
+  v = wsum(lc.emissions);    if (lane == 0 && v) atomicAdd(&cnt->emissions, v);
+  v = wsum(lc.errors);       if (lane == 0 && v) atomicAdd(&cnt->errors, v);
+  double q = lc.qPhot;
+  for (int o = 16; o > 0; o >>= 1) q += __shfl_down_sync(FULL, q, o);
+  if (lane == 0 && q != 0.) atomicAdd(&cnt->qPhot, q);
+}
+
+}  // namespace mcx

@@ -1,0 +1,18 @@
+// k_transport_f64.cu - double-geometry instantiation of the transport kernel.
+#include "k_transport.cuh"
+#include "k_transport_launch.h"
+
+namespace mcx {
+
+cudaError_t launchTransportF64(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,
+                               DevTransportCounters* cnt, uint64_t seed, uint64_t base, unsigned long long n,
+                               double deltaE, const TransportLaunch& L, cudaStream_t s) {
+  transportKernel<double><<<L.blocks, L.threads, L.smem, s>>>(g, in, out, cnt, seed, base, n, deltaE);
+  return cudaGetLastError();
+}
+
+cudaError_t transportOccupancyF64(int threads, size_t smem, int* blocksPerSM) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, transportKernel<double>, threads, smem);
+}
+
+}  // namespace mcx

@@ -1,0 +1,788 @@
+// mcx_api.cu - the C ABI of libmcx.so (declared in include/mcx.h): set-up
+// objects, device contexts, array exchange in the reference's Fortran layout
+// and the phase entry points (opacity, transport, J normalisation).
+#include "../../include/mcx.h"
+#include "k_opacity.cuh"
+#include "k_transport_launch.h"
+#include "mcx_device.cuh"
+#include "setup_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+using namespace mcx;
+
+// ------------------------------------------------------------------ set-up
+struct mcx_setup {
+  Setup s;
+};
+
+namespace {
+thread_local std::string g_setupError;
+
+template <typename T>
+int copyOut(const std::vector<T>& v, void* dst, size_t nbytes) {
+  if (nbytes != v.size() * sizeof(T)) {
+    g_setupError = "mcx_setup_get: size mismatch (expected " + std::to_string(v.size() * sizeof(T)) + " bytes)";
+    return MCX_ERR_INPUT;
+  }
+  if (nbytes) std::memcpy(dst, v.data(), nbytes);
+  return MCX_OK;
+}
+template <typename T>
+int copyIn(std::vector<T>& v, const void* src, size_t nbytes) {
+  if (nbytes != v.size() * sizeof(T)) {
+    g_setupError = "mcx_setup_set: size mismatch (expected " + std::to_string(v.size() * sizeof(T)) + " bytes)";
+    return MCX_ERR_INPUT;
+  }
+  if (nbytes) std::memcpy(v.data(), src, nbytes);
+  return MCX_OK;
+}
+
+// Cell volume in FP64 with the operation order of getVolume
+// (source/grid_mod.f90:2887-2986) evaluated in double.
+double volumeD(const Setup& s, int xP, int yP, int zP) {
+  auto A = [](const std::vector<float>& a, int i) { return (double)a[i - 1]; };
+  const bool sym = s.p.lgSymmetricXYZ;
+  double dx = 0., dy = 0., dz = 0.;
+  if (xP > 1 && xP < s.nx) dx = std::fabs(A(s.xAxis, xP + 1) - A(s.xAxis, xP - 1)) / 2.;
+  else if (xP == 1) dx = sym ? std::fabs(A(s.xAxis, 2) - A(s.xAxis, 1)) / 2. : std::fabs(A(s.xAxis, 2) - A(s.xAxis, 1));
+  else if (xP == s.nx) dx = std::fabs(A(s.xAxis, xP) - A(s.xAxis, xP - 1));
+  if (yP > 1 && yP < s.ny) dy = std::fabs(A(s.yAxis, yP + 1) - A(s.yAxis, yP - 1)) / 2.;
+  else if (yP == 1) dy = sym ? std::fabs(A(s.yAxis, 2) - A(s.yAxis, 1)) / 2. : std::fabs(A(s.yAxis, 2) - A(s.yAxis, 1));
+  else if (yP == s.ny) dy = std::fabs(A(s.yAxis, yP) - A(s.yAxis, yP - 1));
+  if (zP > 1 && zP < s.nz) dz = std::fabs(A(s.zAxis, zP + 1) - A(s.zAxis, zP - 1)) / 2.;
+  else if (zP == 1) dz = sym ? std::fabs(A(s.zAxis, 2) - A(s.zAxis, 1)) / 2. : std::fabs(A(s.zAxis, 2) - A(s.zAxis, 1));
+  else if (zP == s.nz) dz = std::fabs(A(s.zAxis, zP) - A(s.zAxis, zP - 1));
+  dx = dx / 1.e15; dy = dy / 1.e15; dz = dz / 1.e15;
+  return dx * dy * dz;
+}
+}  // namespace
+
+extern "C" int mcx_setup_from_input(const char* input_file, const char* data_dir, const mcx_setup_opts* opts,
+                                    mcx_setup** out) {
+  if (!input_file || !data_dir || !out) { g_setupError = "mcx_setup_from_input: null argument"; return MCX_ERR_INPUT; }
+  *out = nullptr;
+  auto* m = new (std::nothrow) mcx_setup();
+  if (!m) { g_setupError = "mcx_setup_from_input: out of memory"; return MCX_ERR_NOMEM; }
+  try {
+    buildSetup(m->s, input_file, data_dir, opts ? opts->mesh_mode : 0);
+  } catch (const std::exception& e) {
+    g_setupError = e.what();
+    delete m;
+    std::string w = g_setupError;
+    return (w.find("can't open") != std::string::npos || w.find("truncated") != std::string::npos) ? MCX_ERR_IO
+                                                                                                 : MCX_ERR_INPUT;
+  }
+  *out = m;
+  return MCX_OK;
+}
+
+extern "C" void mcx_setup_free(mcx_setup* s) { delete s; }
+
+extern "C" const char* mcx_setup_last_error(void) { return g_setupError.c_str(); }
+
+extern "C" int mcx_setup_info_get(const mcx_setup* m, mcx_setup_info* info) {
+  if (!m || !info) { g_setupError = "mcx_setup_info_get: null argument"; return MCX_ERR_INPUT; }
+  const Setup& s = m->s;
+  std::memset(info, 0, sizeof(*info));
+  info->nx = s.nx; info->ny = s.ny; info->nz = s.nz;
+  info->n_cells = s.nCells;
+  info->nbins = s.nbins;
+  info->n_xsec = (int32_t)s.xSec.size();
+  info->n_elem_used = s.nElemUsed;
+  info->nstages = s.p.nstages;
+  info->symmetric_xyz = s.p.lgSymmetricXYZ;
+  info->lg_gas = s.p.lgGas; info->lg_dust = s.p.lgDust; info->lg_compton = s.p.lgCompton;
+  for (int d = 0; d < 3; ++d) { info->star_idx[d] = s.starIdx[d]; info->star_pos[d] = s.starPos[d]; }
+  info->lyman_p = s.lymanP;
+  info->n_photons = s.p.nPhotons;
+  info->max_iterate_mc = s.p.maxIterateMC;
+  info->r_out = s.p.R_out; info->r_in = s.p.R_in;
+  info->l_star = s.LStar; info->l_phot = s.LPhot;
+  info->ion_edge1 = s.ionEdge.empty() ? 0.f : s.ionEdge[0];
+  info->te_start = s.p.TeStart;
+  info->min_convergence = s.p.minConvergence;
+  info->xhi_limit = s.p.XHILimit;
+  return MCX_OK;
+}
+
+
+static std::vector<int32_t> packedPointers(const Setup& s) {
+  std::vector<int32_t> p(32, 0);
+  p[0] = s.HlevXSecP[0]; p[1] = s.HlevNuP[0]; p[2] = s.HeISingXSecP[0]; p[3] = s.HeIlevNuP[0];
+  p[4] = s.HeIIXSecP[0]; p[5] = s.HeIIlevNuP[0]; p[6] = s.bremsXSecP; p[7] = s.lymanP;
+  p[8] = s.KshellLimitP; p[9] = s.secIonP; p[10] = s.cRecoilHP; p[11] = s.cRecoilHeP;
+  p[12] = s.xrayP; p[13] = s.BjumpP;
+  return p;
+}
+
+extern "C" int mcx_setup_get(const mcx_setup* m, int32_t id, void* dst, size_t nbytes) {
+  if (!m || (!dst && nbytes)) { g_setupError = "mcx_setup_get: null argument"; return MCX_ERR_INPUT; }
+  const Setup& s = m->s;
+  switch (id) {
+    case MCX_ARR_NU: return copyOut(s.nu, dst, nbytes);
+    case MCX_ARR_WIDFLX: return copyOut(s.widFlx, dst, nbytes);
+    case MCX_ARR_XSEC: return copyOut(s.xSec, dst, nbytes);
+    case MCX_ARR_SRC_CDF: return copyOut(s.srcCDF, dst, nbytes);
+    case MCX_ARR_KN_SIGMA_T: return copyOut(s.KNsigmaT, dst, nbytes);
+    case MCX_ARR_KN_CDF: return copyOut(s.KNcdf, dst, nbytes);
+    case MCX_ARR_PCOMP: return copyOut(s.Pcomp, dst, nbytes);
+    case MCX_ARR_XAXIS: return copyOut(s.xAxis, dst, nbytes);
+    case MCX_ARR_YAXIS: return copyOut(s.yAxis, dst, nbytes);
+    case MCX_ARR_ZAXIS: return copyOut(s.zAxis, dst, nbytes);
+    case MCX_ARR_ACTIVE: return copyOut(s.active, dst, nbytes);
+    case MCX_ARR_HDEN: return copyOut(s.Hden, dst, nbytes);
+    case MCX_ARR_TE: return copyOut(s.Te, dst, nbytes);
+    case MCX_ARR_NE: return copyOut(s.Ne, dst, nbytes);
+    case MCX_ARR_TEOLD: return copyOut(s.TeOld, dst, nbytes);
+    case MCX_ARR_NEOLD: return copyOut(s.NeOld, dst, nbytes);
+    case MCX_ARR_IONDEN: return copyOut(s.ionDen, dst, nbytes);
+    case MCX_ARR_VOLUME: return copyOut(s.volume, dst, nbytes);
+    case MCX_ARR_NDUST: return copyOut(s.Ndust, dst, nbytes);
+    case MCX_ARR_ELEM_ABUN: {
+      std::vector<float> v(s.elemAbun, s.elemAbun + kNElements);
+      return copyOut(v, dst, nbytes);
+    }
+    case MCX_SARR_POINTERS: return copyOut(packedPointers(s), dst, nbytes);
+    case MCX_SARR_ELEMENT_P: {
+      std::vector<int32_t> v(&s.elementP[0][0][0][0], &s.elementP[0][0][0][0] + 30 * 30 * 7 * 3);
+      return copyOut(v, dst, nbytes);
+    }
+    case MCX_SARR_N_SHELLS: {
+      std::vector<int32_t> v(&s.nShells[0][0], &s.nShells[0][0] + 30 * 30);
+      return copyOut(v, dst, nbytes);
+    }
+    case MCX_SARR_ELEM_XREF: {
+      std::vector<int32_t> v(s.elemXref, s.elemXref + kNElements);
+      return copyOut(v, dst, nbytes);
+    }
+    case MCX_SARR_ION_EDGE: return copyOut(s.ionEdge, dst, nbytes);
+    case MCX_SARR_COMXSEC_H: return copyOut(s.comXSecH, dst, nbytes);
+    case MCX_SARR_COMXSEC_C: return copyOut(s.comXSecC, dst, nbytes);
+    case MCX_SARR_XSEC_RECOIL: return copyOut(s.xSecRecoil, dst, nbytes);
+    default: g_setupError = "mcx_setup_get: unknown array id " + std::to_string(id); return MCX_ERR_INPUT;
+  }
+}
+
+extern "C" int mcx_setup_len(const mcx_setup* m, int32_t id, int64_t* count) {
+  if (!m || !count) { g_setupError = "mcx_setup_len: null argument"; return MCX_ERR_INPUT; }
+  const Setup& s = m->s;
+  const int64_t C1 = (int64_t)s.nCells + 1, nb = s.nbins;
+  switch (id) {
+    case MCX_ARR_NU: case MCX_ARR_WIDFLX: case MCX_ARR_SRC_CDF: case MCX_ARR_KN_SIGMA_T:
+    case MCX_SARR_COMXSEC_H: case MCX_SARR_COMXSEC_C: case MCX_SARR_XSEC_RECOIL: *count = nb; break;
+    case MCX_ARR_XSEC: *count = (int64_t)s.xSec.size(); break;
+    case MCX_ARR_KN_CDF: case MCX_ARR_PCOMP: *count = 180 * nb; break;
+    case MCX_ARR_XAXIS: *count = s.nx; break;
+    case MCX_ARR_YAXIS: *count = s.ny; break;
+    case MCX_ARR_ZAXIS: *count = s.nz; break;
+    case MCX_ARR_ACTIVE: *count = (int64_t)s.active.size(); break;
+    case MCX_ARR_HDEN: case MCX_ARR_TE: case MCX_ARR_NE: case MCX_ARR_TEOLD: case MCX_ARR_NEOLD:
+    case MCX_ARR_VOLUME: case MCX_ARR_NDUST: *count = C1; break;
+    case MCX_ARR_IONDEN: *count = (int64_t)s.ionDen.size(); break;
+    case MCX_ARR_ELEM_ABUN: case MCX_SARR_ELEM_XREF: *count = 30; break;
+    case MCX_SARR_POINTERS: *count = 32; break;
+    case MCX_SARR_ELEMENT_P: *count = 30 * 30 * 7 * 3; break;
+    case MCX_SARR_N_SHELLS: *count = 30 * 30; break;
+    case MCX_SARR_ION_EDGE: *count = (int64_t)s.ionEdge.size(); break;
+    default: g_setupError = "mcx_setup_len: unknown array id " + std::to_string(id); return MCX_ERR_INPUT;
+  }
+  return MCX_OK;
+}
+
+extern "C" int mcx_setup_set(mcx_setup* m, int32_t id, const void* src, size_t nbytes) {
+  if (!m || (!src && nbytes)) { g_setupError = "mcx_setup_set: null argument"; return MCX_ERR_INPUT; }
+  Setup& s = m->s;
+  switch (id) {
+    case MCX_ARR_HDEN: return copyIn(s.Hden, src, nbytes);
+    case MCX_ARR_TE: return copyIn(s.Te, src, nbytes);
+    case MCX_ARR_NE: return copyIn(s.Ne, src, nbytes);
+    case MCX_ARR_TEOLD: return copyIn(s.TeOld, src, nbytes);
+    case MCX_ARR_NEOLD: return copyIn(s.NeOld, src, nbytes);
+    case MCX_ARR_IONDEN: return copyIn(s.ionDen, src, nbytes);
+    case MCX_ARR_SRC_CDF: return copyIn(s.srcCDF, src, nbytes);
+    default: g_setupError = "mcx_setup_set: array id " + std::to_string(id) + " is not settable"; return MCX_ERR_INPUT;
+  }
+}
+
+// ------------------------------------------------------------------ context
+namespace {
+
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  ~DBuf() { if (p) cudaFree(p); }
+  cudaError_t alloc(size_t count) {
+    if (p) { cudaFree(p); p = nullptr; n = 0; }
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc((void**)&p, count * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+}  // namespace
+
+struct mcx_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, tev0 = nullptr, tev1 = nullptr;
+  std::string err;
+  bool loaded = false;
+  int numSMs = 0;
+
+  // model sizes and flags
+  int nx = 0, ny = 0, nz = 0, nCells = 0, nbins = 0, nstages = 0, nElemUsed = 0, nXsec = 0;
+  bool symmetric = false, lgDust = false, lgGas = false, lgCompton = false, radPress = false;
+  float lStar = 0.f, ionEdge1 = 0.f, rOut = 0.f;
+  int64_t nPhotons = 0;
+  int starIdx[3] = {0, 0, 0};
+  float starPos[3] = {0.f, 0.f, 0.f};
+  std::vector<int32_t> activeHost;
+  float gauntTeOld = -1.f;   // BoltGaunt's saved TeOld2
+
+  // tables
+  DBuf<float> nu, log10nu, xsec, KNsigmaT, KNcdfT, PcompT, srcCDF, xAxis, yAxis, zAxis, volF;
+  DBuf<double> volD;
+  DBuf<int32_t> active;
+  DBuf<int32_t> csrStart, slotPlane;
+  DBuf<int2> csrTerm;
+  DBuf<float> slotAbun, slotFFWeight;
+  int nSlots = 0, bremsP0 = 0;
+  // state
+  DBuf<float> hden, te, ne, teOld, neOld, ionDen, ndust;
+  // phase arrays
+  DBuf<float> opacity, recPDF, recCDFT, totalLines, scaOpac, dustPDF, dustCDFT;
+  DBuf<double> jste, escaped, hEst;
+  // scratch
+  DBuf<float> gauntTe;
+  DBuf<uint8_t> computeMask;
+  DBuf<DevTransportCounters> counters;
+  bool haveOpacity = false, haveRecPDF = false, haveDustPDF = false;
+};
+
+namespace {
+
+int fail(mcx_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cudaFail(mcx_ctx* c, cudaError_t e, const char* what) {
+  return fail(c, MCX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call, what)                                   \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return cudaFail(c, e_, what); \
+  } while (0)
+
+__global__ void transposeKernel(const float* __restrict__ in, float* __restrict__ out, int rows, int cols) {
+  // in: [rows][cols] -> out: [cols][rows]
+  __shared__ float tile[32][33];
+  int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    int r = by + j, cc = bx + threadIdx.x;
+    if (r < rows && cc < cols) tile[j][threadIdx.x] = in[(size_t)r * cols + cc];
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    int r = bx + j, cc = by + threadIdx.x;
+    if (r < cols && cc < rows) out[(size_t)r * rows + cc] = tile[threadIdx.x][j];
+  }
+}
+
+cudaError_t transpose(const float* in, float* out, int rows, int cols, cudaStream_t s) {
+  dim3 b(32, 8), g((cols + 31) / 32, (rows + 31) / 32);
+  transposeKernel<<<g, b, 0, s>>>(in, out, rows, cols);
+  return cudaGetLastError();
+}
+
+// j = (j * mul) / div, two roundings as in source/iteration_mod.f90:1002-1031
+__global__ void scaleJKernel(double* j, size_t n, double mul, double div) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (; i < n; i += stride) {
+    double v = j[i] * mul;
+    if (div != 1.) v = v / div;
+    j[i] = v;
+  }
+}
+
+template <typename T>
+cudaError_t upload(DBuf<T>& b, const std::vector<T>& v) {
+  cudaError_t e = b.alloc(v.size());
+  if (e != cudaSuccess) return e;
+  if (v.empty()) return cudaSuccess;
+  return cudaMemcpy(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+}  // namespace
+
+extern "C" int mcx_ctx_create(int32_t device, mcx_ctx** out) {
+  if (!out) return MCX_ERR_INPUT;
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n <= device || device < 0) {
+    g_setupError = std::string("mcx_ctx_create: no CUDA device ") + std::to_string(device) + ": " +
+                   (e != cudaSuccess ? cudaGetErrorString(e) : "device index out of range");
+    return MCX_ERR_CUDA;
+  }
+  auto* c = new (std::nothrow) mcx_ctx();
+  if (!c) return MCX_ERR_NOMEM;
+  c->device = device;
+  if ((e = cudaSetDevice(device)) != cudaSuccess || (e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreate(&c->ev0)) != cudaSuccess || (e = cudaEventCreate(&c->ev1)) != cudaSuccess ||
+      (e = cudaEventCreate(&c->tev0)) != cudaSuccess || (e = cudaEventCreate(&c->tev1)) != cudaSuccess) {
+    g_setupError = std::string("mcx_ctx_create: ") + cudaGetErrorString(e);
+    delete c;
+    return MCX_ERR_CUDA;
+  }
+  cudaDeviceGetAttribute(&c->numSMs, cudaDevAttrMultiProcessorCount, device);
+  *out = c;
+  return MCX_OK;
+}
+
+extern "C" void mcx_ctx_destroy(mcx_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->tev0) cudaEventDestroy(c->tev0);
+  if (c->tev1) cudaEventDestroy(c->tev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+extern "C" int mcx_last_error(const mcx_ctx* c, char* buf, size_t len) {
+  if (!buf || len == 0) return MCX_ERR_INPUT;
+  const std::string& m = c ? c->err : g_setupError;
+  std::snprintf(buf, len, "%s", m.c_str());
+  return MCX_OK;
+}
+
+extern "C" int mcx_sync(mcx_ctx* c) {
+  if (!c) return MCX_ERR_INPUT;
+  CK(cudaStreamSynchronize(c->stream), "mcx_sync");
+  return MCX_OK;
+}
+
+// Build the opacity kernel's per-bin CSR list of bound-free terms in the
+// summation order of addOpacity (source/ionization_mod.f90:375-390).
+static void buildOpacityTables(const Setup& s, std::vector<int32_t>& csrStart, std::vector<int2>& csrTerm,
+                               std::vector<int32_t>& slotPlane, std::vector<float>& slotAbun,
+                               std::vector<float>& slotFF) {
+  const int nb = s.nbins, S = s.p.nstages, E = std::max(s.nElemUsed, 1);
+  int slotOf[31][32];
+  for (auto& r : slotOf) for (auto& x : r) x = -1;
+  auto slot = [&](int n, int ion) {
+    if (slotOf[n][ion] >= 0) return slotOf[n][ion];
+    int id = (int)slotPlane.size();
+    slotOf[n][ion] = id;
+    int xr = s.elemXref[n - 1];
+    slotPlane.push_back((xr - 1) + E * (ion - 1));
+    slotAbun.push_back(s.elemAbun[n - 1]);
+    // free-free electron sum: density(2,2) + sum_{n>=3} i^2 density(n,i+1)
+    float w = 0.f;
+    if (n == 2 && ion == 2) w = 1.f;
+    else if (n >= 3 && ion >= 2 && ion - 1 <= std::min(n, S - 1)) w = (float)((ion - 1) * (ion - 1));
+    slotFF.push_back(w);
+    return id;
+  };
+  // all slots of ions with a filled density, in element order, so that every
+  // free-free contributor has a slot
+  for (int n = 1; n <= 30; ++n) {
+    if (!s.elemOn[n - 1]) continue;
+    for (int i = 1; i <= std::min(n, S); ++i) slot(n, i);
+  }
+  struct Range { int lo, hi, k, slot; };
+  std::vector<Range> ranges;
+  auto inOpacity = [&](int xSecP, int lo, int hi, int sl) {
+    int iup = std::min(hi, nb);
+    iup = std::max(lo, iup);
+    ranges.push_back({lo, iup, xSecP - lo, sl});
+  };
+  if (s.elemOn[0]) inOpacity(s.HlevXSecP[0], s.HlevNuP[0], nb, slot(1, 1));
+  if (s.elemOn[1]) {
+    inOpacity(s.HeISingXSecP[0], s.HeIlevNuP[0], nb, slot(2, 1));
+    inOpacity(s.HeIIXSecP[0], s.HeIIlevNuP[0], nb, slot(2, 2));
+  }
+  for (int n = 3; n <= 30; ++n) {
+    if (!s.elemOn[n - 1]) continue;
+    for (int ion = 1; ion <= std::min(n, S); ++ion)
+      for (int sh = 1; sh <= s.nShells[n - 1][ion - 1]; ++sh) {
+        const int* P = s.elementP[n - 1][ion - 1][sh - 1];
+        inOpacity(P[2], P[0], P[1], slot(n, ion));
+      }
+  }
+  std::vector<std::vector<int2>> per(nb + 1);
+  for (const auto& r : ranges)
+    for (int i = std::max(r.lo, 1); i <= std::min(r.hi, nb); ++i) per[i].push_back(make_int2(r.k, r.slot));
+  csrStart.assign(nb + 1, 0);
+  csrTerm.clear();
+  for (int i = 1; i <= nb; ++i) {
+    csrStart[i - 1] = (int32_t)csrTerm.size();
+    csrTerm.insert(csrTerm.end(), per[i].begin(), per[i].end());
+  }
+  csrStart[nb] = (int32_t)csrTerm.size();
+}
+
+extern "C" int mcx_load(mcx_ctx* c, const mcx_setup* m) {
+  if (!c || !m) return fail(c, MCX_ERR_INPUT, "mcx_load: null argument");
+  const Setup& s = m->s;
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  c->loaded = false;
+  c->nx = s.nx; c->ny = s.ny; c->nz = s.nz; c->nCells = s.nCells; c->nbins = s.nbins;
+  c->nstages = s.p.nstages; c->nElemUsed = std::max(s.nElemUsed, 1); c->nXsec = (int)s.xSec.size();
+  c->symmetric = s.p.lgSymmetricXYZ; c->lgDust = s.p.lgDust; c->lgGas = s.p.lgGas;
+  c->lgCompton = s.p.lgCompton; c->radPress = s.p.lgRadPress;
+  c->lStar = s.LStar; c->ionEdge1 = s.ionEdge.empty() ? 0.f : s.ionEdge[0]; c->rOut = s.p.R_out;
+  c->nPhotons = s.p.nPhotons;
+  for (int d = 0; d < 3; ++d) { c->starIdx[d] = s.starIdx[d]; c->starPos[d] = s.starPos[d]; }
+  c->gauntTeOld = -1.f;
+  // validate what the kernels index with
+  for (int32_t a : s.active)
+    if (a < 0 || a > s.nCells) return fail(c, MCX_ERR_INPUT, "mcx_load: active() holds ids outside [0, nCells] (sub-grids are not supported)");
+  if (s.nbins < 2 || s.nCells < 1) return fail(c, MCX_ERR_INPUT, "mcx_load: empty grid or frequency mesh");
+  if (s.starIdx[0] < 1 || s.starIdx[0] > s.nx || s.starIdx[1] < 1 || s.starIdx[1] > s.ny || s.starIdx[2] < 1 || s.starIdx[2] > s.nz)
+    return fail(c, MCX_ERR_INPUT, "mcx_load: the source must lie inside the grid");
+  c->activeHost = s.active;
+
+  const int nb = s.nbins;
+  const size_t C1 = (size_t)s.nCells + 1;
+  std::vector<float> l10(nb);
+  for (int i = 0; i < nb; ++i) l10[i] = log10f(s.nu[i]);
+  std::vector<float> knT((size_t)nb * 180), pcT((size_t)nb * 180);
+  for (int i = 0; i < nb; ++i)
+    for (int j = 0; j < 180; ++j) {
+      knT[(size_t)i * 180 + j] = s.KNcdf[(size_t)j * nb + i];
+      pcT[(size_t)i * 180 + j] = s.Pcomp[(size_t)j * nb + i];
+    }
+  std::vector<double> vd(C1, 1.0);
+  std::vector<float> vf(C1, 1.f);
+  for (int i = 1; i <= s.nx; ++i)
+    for (int j = 1; j <= s.ny; ++j)
+      for (int k = 1; k <= s.nz; ++k) {
+        int cell = s.activeAt(i, j, k);
+        if (cell > 0) { vd[cell] = volumeD(s, i, j, k); vf[cell] = s.volume[cell]; }
+      }
+  CK(upload(c->nu, s.nu), "upload nu");
+  CK(upload(c->log10nu, l10), "upload log10nu");
+  CK(upload(c->xsec, s.xSec.empty() ? std::vector<float>(1, 0.f) : s.xSec), "upload xsec");
+  CK(upload(c->KNsigmaT, s.KNsigmaT), "upload KNsigmaT");
+  CK(upload(c->KNcdfT, knT), "upload KN cdf");
+  CK(upload(c->PcompT, pcT), "upload Pcomp");
+  CK(upload(c->srcCDF, s.srcCDF), "upload srcCDF");
+  CK(upload(c->xAxis, s.xAxis), "upload xAxis");
+  CK(upload(c->yAxis, s.yAxis), "upload yAxis");
+  CK(upload(c->zAxis, s.zAxis), "upload zAxis");
+  CK(upload(c->active, s.active), "upload active");
+  CK(upload(c->volD, vd), "upload volume");
+  CK(upload(c->volF, vf), "upload volume");
+  std::vector<int32_t> cs, sp;
+  std::vector<int2> ct;
+  std::vector<float> sa, sf;
+  buildOpacityTables(s, cs, ct, sp, sa, sf);
+  c->nSlots = (int)sp.size();
+  c->bremsP0 = s.bremsXSecP - 1;
+  CK(upload(c->csrStart, cs), "upload csr");
+  CK(upload(c->csrTerm, ct.empty() ? std::vector<int2>(1, make_int2(0, 0)) : ct), "upload csr");
+  CK(upload(c->slotPlane, sp.empty() ? std::vector<int32_t>(1, 0) : sp), "upload slots");
+  CK(upload(c->slotAbun, sa.empty() ? std::vector<float>(1, 0.f) : sa), "upload slots");
+  CK(upload(c->slotFFWeight, sf.empty() ? std::vector<float>(1, 0.f) : sf), "upload slots");
+  CK(upload(c->hden, s.Hden), "upload Hden");
+  CK(upload(c->te, s.Te), "upload Te");
+  CK(upload(c->ne, s.Ne), "upload Ne");
+  CK(upload(c->teOld, s.TeOld), "upload TeOld");
+  CK(upload(c->neOld, s.NeOld), "upload NeOld");
+  CK(upload(c->ionDen, s.ionDen), "upload ionDen");
+  CK(upload(c->ndust, s.Ndust), "upload Ndust");
+  CK(c->opacity.alloc(C1 * nb), "alloc opacity");
+  CK(c->recPDF.alloc(C1 * nb), "alloc recPDF");
+  CK(c->recCDFT.alloc(C1 * nb), "alloc recCDF");
+  CK(c->totalLines.alloc(C1), "alloc totalLines");
+  CK(c->jste.alloc(C1 * nb), "alloc Jste");
+  CK(c->escaped.alloc(C1 * (nb + 1)), "alloc escaped");
+  if (c->radPress) CK(c->hEst.alloc(C1 * nb), "alloc H");
+  if (c->lgDust) {
+    CK(c->scaOpac.alloc(C1 * nb), "alloc scaOpac");
+    CK(c->dustPDF.alloc(C1 * nb), "alloc dustPDF");
+    CK(c->dustCDFT.alloc(C1 * nb), "alloc dustCDF");
+  }
+  CK(c->gauntTe.alloc(C1), "alloc gauntTe");
+  CK(c->computeMask.alloc(C1), "alloc mask");
+  CK(c->counters.alloc(1), "alloc counters");
+  CK(cudaMemset(c->opacity.p, 0, c->opacity.bytes()), "memset");
+  CK(cudaMemset(c->recPDF.p, 0, c->recPDF.bytes()), "memset");
+  CK(cudaMemset(c->recCDFT.p, 0, c->recCDFT.bytes()), "memset");
+  CK(cudaMemset(c->totalLines.p, 0, c->totalLines.bytes()), "memset");
+  CK(cudaMemset(c->jste.p, 0, c->jste.bytes()), "memset");
+  CK(cudaMemset(c->escaped.p, 0, c->escaped.bytes()), "memset");
+  if (c->hEst.p) CK(cudaMemset(c->hEst.p, 0, c->hEst.bytes()), "memset");
+  if (c->scaOpac.p) CK(cudaMemset(c->scaOpac.p, 0, c->scaOpac.bytes()), "memset");
+  CK(cudaDeviceSynchronize(), "mcx_load");
+  c->haveOpacity = c->haveRecPDF = c->haveDustPDF = false;
+  c->loaded = true;
+  return MCX_OK;
+}
+
+namespace {
+
+struct ArrView {
+  void* dev;
+  size_t bytes;
+};
+
+ArrView viewOf(mcx_ctx* c, int id) {
+  switch (id) {
+    case MCX_ARR_NU: return {c->nu.p, c->nu.bytes()};
+    case MCX_ARR_XSEC: return {c->xsec.p, c->xsec.bytes()};
+    case MCX_ARR_SRC_CDF: return {c->srcCDF.p, c->srcCDF.bytes()};
+    case MCX_ARR_KN_SIGMA_T: return {c->KNsigmaT.p, c->KNsigmaT.bytes()};
+    case MCX_ARR_XAXIS: return {c->xAxis.p, c->xAxis.bytes()};
+    case MCX_ARR_YAXIS: return {c->yAxis.p, c->yAxis.bytes()};
+    case MCX_ARR_ZAXIS: return {c->zAxis.p, c->zAxis.bytes()};
+    case MCX_ARR_ACTIVE: return {c->active.p, c->active.bytes()};
+    case MCX_ARR_HDEN: return {c->hden.p, c->hden.bytes()};
+    case MCX_ARR_TE: return {c->te.p, c->te.bytes()};
+    case MCX_ARR_NE: return {c->ne.p, c->ne.bytes()};
+    case MCX_ARR_TEOLD: return {c->teOld.p, c->teOld.bytes()};
+    case MCX_ARR_NEOLD: return {c->neOld.p, c->neOld.bytes()};
+    case MCX_ARR_IONDEN: return {c->ionDen.p, c->ionDen.bytes()};
+    case MCX_ARR_OPACITY: return {c->opacity.p, c->opacity.bytes()};
+    case MCX_ARR_RECPDF: return {c->recPDF.p, c->recPDF.bytes()};
+    case MCX_ARR_TOTAL_LINES: return {c->totalLines.p, c->totalLines.bytes()};
+    case MCX_ARR_JSTE: return {c->jste.p, c->jste.bytes()};
+    case MCX_ARR_ESCAPED: return {c->escaped.p, c->escaped.bytes()};
+    case MCX_ARR_VOLUME: return {c->volF.p, c->volF.bytes()};
+    case MCX_ARR_GAUNT_TE: return {c->gauntTe.p, c->gauntTe.bytes()};
+    case MCX_ARR_SCAOPAC: return {c->scaOpac.p, c->scaOpac.bytes()};
+    case MCX_ARR_DUSTPDF: return {c->dustPDF.p, c->dustPDF.bytes()};
+    case MCX_ARR_NDUST: return {c->ndust.p, c->ndust.bytes()};
+    case MCX_ARR_H_EST: return {c->hEst.p, c->hEst.bytes()};
+    default: return {nullptr, 0};
+  }
+}
+
+}  // namespace
+
+extern "C" int mcx_get(mcx_ctx* c, int32_t id, void* host, size_t nbytes) {
+  if (!c || (!host && nbytes)) return fail(c, MCX_ERR_INPUT, "mcx_get: null argument");
+  if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_get: no model loaded");
+  ArrView v = viewOf(c, id);
+  if (!v.dev) return fail(c, MCX_ERR_INPUT, "mcx_get: array id " + std::to_string(id) + " is not held by the context");
+  if (v.bytes != nbytes) return fail(c, MCX_ERR_INPUT, "mcx_get: size mismatch, expected " + std::to_string(v.bytes) + " bytes");
+  CK(cudaMemcpyAsync(host, v.dev, nbytes, cudaMemcpyDeviceToHost, c->stream), "mcx_get");
+  CK(cudaStreamSynchronize(c->stream), "mcx_get");
+  return MCX_OK;
+}
+
+extern "C" int mcx_put(mcx_ctx* c, int32_t id, const void* host, size_t nbytes) {
+  if (!c || (!host && nbytes)) return fail(c, MCX_ERR_INPUT, "mcx_put: null argument");
+  if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_put: no model loaded");
+  switch (id) {
+    case MCX_ARR_NU: case MCX_ARR_XSEC: case MCX_ARR_XAXIS: case MCX_ARR_YAXIS: case MCX_ARR_ZAXIS:
+    case MCX_ARR_ACTIVE: case MCX_ARR_VOLUME: case MCX_ARR_GAUNT_TE:
+      return fail(c, MCX_ERR_INPUT, "mcx_put: geometry and tables are set by mcx_load");
+    default: break;
+  }
+  ArrView v = viewOf(c, id);
+  if (!v.dev) return fail(c, MCX_ERR_INPUT, "mcx_put: array id " + std::to_string(id) + " is not held by the context");
+  if (v.bytes != nbytes) return fail(c, MCX_ERR_INPUT, "mcx_put: size mismatch, expected " + std::to_string(v.bytes) + " bytes");
+  CK(cudaMemcpyAsync(v.dev, host, nbytes, cudaMemcpyHostToDevice, c->stream), "mcx_put");
+  const int C1 = c->nCells + 1;
+  if (id == MCX_ARR_RECPDF) { CK(transpose(c->recPDF.p, c->recCDFT.p, c->nbins, C1, c->stream), "transpose recPDF"); c->haveRecPDF = true; }
+  if (id == MCX_ARR_DUSTPDF) { CK(transpose(c->dustPDF.p, c->dustCDFT.p, c->nbins, C1, c->stream), "transpose dustPDF"); c->haveDustPDF = true; }
+  if (id == MCX_ARR_OPACITY) c->haveOpacity = true;
+  CK(cudaStreamSynchronize(c->stream), "mcx_put");
+  return MCX_OK;
+}
+
+extern "C" int mcx_device_ptr(mcx_ctx* c, int32_t id, void** dptr) {
+  if (!c || !dptr) return fail(c, MCX_ERR_INPUT, "mcx_device_ptr: null argument");
+  if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_device_ptr: no model loaded");
+  ArrView v = viewOf(c, id);
+  if (!v.dev) return fail(c, MCX_ERR_INPUT, "mcx_device_ptr: unknown array id");
+  *dptr = v.dev;
+  return MCX_OK;
+}
+
+// ------------------------------------------------------------ opacity phase
+extern "C" int mcx_opacity(mcx_ctx* c, const mcx_phase_opts* opts, mcx_phase_stats* stats) {
+  if (!c) return MCX_ERR_INPUT;
+  if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_opacity: no model loaded");
+  if (!c->lgGas) return fail(c, MCX_ERR_STATE, "mcx_opacity: the grid holds no gas");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  const int it = opts ? opts->n_iterate_mc : 1;
+  const size_t C1 = (size_t)c->nCells + 1;
+  // the skip rule and the Gaunt cache are sequential host logic over four
+  // per-cell arrays (source/iteration_mod.f90:131-149, source/ionization_mod.f90:171-175)
+  std::vector<float> te(C1), ne(C1), teOld(C1), neOld(C1), gte(C1, 0.f);
+  std::vector<uint8_t> mask(C1, 0);
+  CK(cudaMemcpyAsync(te.data(), c->te.p, C1 * 4, cudaMemcpyDeviceToHost, c->stream), "d2h Te");
+  CK(cudaMemcpyAsync(ne.data(), c->ne.p, C1 * 4, cudaMemcpyDeviceToHost, c->stream), "d2h Ne");
+  CK(cudaMemcpyAsync(teOld.data(), c->teOld.p, C1 * 4, cudaMemcpyDeviceToHost, c->stream), "d2h TeOld");
+  CK(cudaMemcpyAsync(neOld.data(), c->neOld.p, C1 * 4, cudaMemcpyDeviceToHost, c->stream), "d2h NeOld");
+  CK(cudaStreamSynchronize(c->stream), "mcx_opacity");
+  int64_t computed = 0, skipped = 0;
+  for (int i = 1; i <= c->nx; ++i)
+    for (int j = 1; j <= c->ny; ++j)
+      for (int k = 1; k <= c->nz; ++k) {
+        int cell = c->activeHost[(size_t)(i - 1) + (size_t)c->nx * ((size_t)(j - 1) + (size_t)c->ny * (size_t)(k - 1))];
+        if (cell <= 0) continue;
+        bool skip = it > 1 && (std::fabs(te[cell] - teOld[cell]) / teOld[cell]) < 0.005f &&
+                    (std::fabs(ne[cell] - neOld[cell]) / neOld[cell]) < 0.005f;
+        if (skip) { ++skipped; continue; }
+        mask[cell] = 1;
+        ++computed;
+        if (std::fabs(1.f - c->gauntTeOld / te[cell]) > 0.10f) c->gauntTeOld = te[cell];
+        gte[cell] = c->gauntTeOld;
+      }
+  CK(cudaMemcpyAsync(c->computeMask.p, mask.data(), C1, cudaMemcpyHostToDevice, c->stream), "h2d mask");
+  CK(cudaMemcpyAsync(c->gauntTe.p, gte.data(), C1 * 4, cudaMemcpyHostToDevice, c->stream), "h2d gauntTe");
+  OpacityDev t{};
+  t.nbins = c->nbins; t.nCells = c->nCells; t.nXsec = c->nXsec; t.lgCompton = c->lgCompton;
+  t.nSlots = c->nSlots; t.bremsP0 = c->bremsP0;
+  t.nu = c->nu.p; t.log10nu = c->log10nu.p; t.xsec = c->xsec.p; t.KNsigmaT = c->KNsigmaT.p;
+  t.csrStart = c->csrStart.p; t.csrTerm = c->csrTerm.p;
+  t.slotPlane = c->slotPlane.p; t.slotAbun = c->slotAbun.p; t.slotFFWeight = c->slotFFWeight.p;
+  CK(cudaEventRecord(c->ev0, c->stream), "event");
+  CK(launchOpacity(t, c->hden.p, c->te.p, c->ne.p, c->ionDen.p, c->gauntTe.p, c->computeMask.p, c->opacity.p, c->stream),
+     "opacity kernel");
+  CK(cudaEventRecord(c->ev1, c->stream), "event");
+  CK(cudaStreamSynchronize(c->stream), "mcx_opacity");
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->cells_computed = computed;
+    stats->cells_skipped = skipped;
+    cudaEventElapsedTime(&stats->kernel_ms, c->ev0, c->ev1);
+  }
+  c->haveOpacity = true;
+  return MCX_OK;
+}
+
+// ---------------------------------------------------------- transport phase
+extern "C" int mcx_transport(mcx_ctx* c, const mcx_transport_opts* o, mcx_transport_stats* stats) {
+  if (!c || !o) return fail(c, MCX_ERR_INPUT, "mcx_transport: null argument");
+  if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_transport: no model loaded");
+  if (o->istar != 1) return fail(c, MCX_ERR_INPUT, "mcx_transport: only source 1 is supported");
+  if (o->n_packets < 0) return fail(c, MCX_ERR_INPUT, "mcx_transport: negative packet count");
+  if (!c->haveOpacity) return fail(c, MCX_ERR_STATE, "mcx_transport: no opacity (call mcx_opacity or mcx_put(MCX_ARR_OPACITY))");
+  if (c->lgGas && !c->haveRecPDF) return fail(c, MCX_ERR_STATE, "mcx_transport: no re-emission CDF (recPDF)");
+  if (c->lgDust && !c->lgGas && !c->haveDustPDF) return fail(c, MCX_ERR_STATE, "mcx_transport: no dust emission CDF");
+  if (o->precision != MCX_PREC_FP32_GEOM && o->precision != MCX_PREC_FP64)
+    return fail(c, MCX_ERR_INPUT, "mcx_transport: unknown precision");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  const int64_t norm = o->n_photons_norm > 0 ? o->n_photons_norm : o->n_packets;
+  const double deltaE = norm > 0 ? (double)c->lStar / (double)norm : 0.;
+  if (o->zero_estimators) {
+    CK(cudaMemsetAsync(c->jste.p, 0, c->jste.bytes(), c->stream), "memset Jste");
+    CK(cudaMemsetAsync(c->escaped.p, 0, c->escaped.bytes(), c->stream), "memset escaped");
+    if (c->hEst.p) CK(cudaMemsetAsync(c->hEst.p, 0, c->hEst.bytes(), c->stream), "memset H");
+  }
+  CK(cudaMemsetAsync(c->counters.p, 0, sizeof(DevTransportCounters), c->stream), "memset counters");
+
+  DevGrid g{};
+  g.nx = c->nx; g.ny = c->ny; g.nz = c->nz; g.nCells = c->nCells; g.nbins = c->nbins;
+  g.symmetric = c->symmetric; g.lgDust = c->lgDust; g.lgGas = c->lgGas; g.lgCompton = c->lgCompton;
+  g.radPress = c->radPress;
+  for (int d = 0; d < 3; ++d) { g.starIdx[d] = c->starIdx[d]; g.starPos[d] = c->starPos[d]; }
+  g.ionEdge1 = c->ionEdge1; g.rOut = c->rOut;
+  g.xAxis = c->xAxis.p; g.yAxis = c->yAxis.p; g.zAxis = c->zAxis.p; g.active = c->active.p;
+  g.nu = c->nu.p; g.srcCDF = c->srcCDF.p; g.KNsigmaT = c->KNsigmaT.p; g.KNcdfT = c->KNcdfT.p;
+  g.PcompT = c->PcompT.p; g.volD = c->volD.p; g.volF = c->volF.p;
+  DevTransportIn in{};
+  in.opacity = c->opacity.p; in.scaOpac = c->scaOpac.p; in.recCDFT = c->recCDFT.p; in.dustCDFT = c->dustCDFT.p;
+  in.totalLines = c->totalLines.p; in.ne = c->ne.p;
+  DevTransportOut out{};
+  out.jste = c->jste.p; out.escaped = c->escaped.p; out.hEst = c->hEst.p;
+
+  TransportLaunch L{};
+  L.threads = o->block_size > 0 ? o->block_size : 256;
+  if (L.threads % 32 != 0 || L.threads > 256) return fail(c, MCX_ERR_INPUT, "mcx_transport: block_size must be a multiple of 32 up to 256");
+  L.smem = (size_t)(c->nx + c->ny + c->nz + 2 * c->nbins) * sizeof(float);
+  int perSM = 0;
+  CK(transportOccupancy(o->precision == MCX_PREC_FP64, L.threads, L.smem, &perSM), "occupancy");
+  if (perSM < 1) perSM = 1;
+  int mult = o->grid_mult > 0 ? std::min(o->grid_mult, perSM) : perSM;
+  L.blocks = c->numSMs * mult;
+  const unsigned long long n = (unsigned long long)o->n_packets;
+  if (n > 0) {
+    const unsigned long long maxBlocks = (n + L.threads - 1) / L.threads;
+    if ((unsigned long long)L.blocks > maxBlocks) L.blocks = (int)maxBlocks;
+  }
+  CK(cudaEventRecord(c->ev0, c->stream), "event");
+  if (n > 0) {
+    cudaError_t e = (o->precision == MCX_PREC_FP64)
+                        ? launchTransportF64(g, in, out, c->counters.p, o->seed, o->counter_base, n, deltaE, L, c->stream)
+                        : launchTransportF32(g, in, out, c->counters.p, o->seed, o->counter_base, n, deltaE, L, c->stream);
+    if (e != cudaSuccess) return cudaFail(c, e, "transport kernel");
+  }
+  CK(cudaEventRecord(c->ev1, c->stream), "event");
+  DevTransportCounters h{};
+  CK(cudaMemcpyAsync(&h, c->counters.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream), "d2h counters");
+  CK(cudaStreamSynchronize(c->stream), "mcx_transport");
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->crossings = (int64_t)h.crossings;
+    stats->interactions = (int64_t)h.interactions;
+    stats->absorptions = (int64_t)h.absorptions;
+    stats->scatterings = (int64_t)h.scatterings;
+    stats->escaped = (int64_t)h.escaped;
+    stats->line_escapes = (int64_t)h.lineEscapes;
+    stats->trapped = (int64_t)h.trapped;
+    stats->emissions = (int64_t)h.emissions;
+    stats->q_phot = h.qPhot;
+    cudaEventElapsedTime(&stats->kernel_ms, c->ev0, c->ev1);
+  }
+  if (h.errors)
+    return fail(c, MCX_ERR_INTERNAL,
+                "mcx_transport: " + std::to_string(h.errors) + " packet(s) reached a state where the reference stops");
+  return MCX_OK;
+}
+
+extern "C" int mcx_normalize_j(mcx_ctx* c) {
+  if (!c) return MCX_ERR_INPUT;
+  if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_normalize_j: no model loaded");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  const double div = c->symmetric ? 8. : 1.;
+  int blocks = c->numSMs * 4;
+  scaleJKernel<<<blocks, 256, 0, c->stream>>>(c->jste.p, c->jste.n, 1.e-9, div);
+  CK(cudaGetLastError(), "scale J");
+  if (div != 1.) {
+    scaleJKernel<<<blocks, 256, 0, c->stream>>>(c->escaped.p, c->escaped.n, 1., div);
+    CK(cudaGetLastError(), "scale escaped");
+  }
+  CK(cudaStreamSynchronize(c->stream), "mcx_normalize_j");
+  return MCX_OK;
+}
+
+extern "C" int mcx_timer_start(mcx_ctx* c) {
+  if (!c) return MCX_ERR_INPUT;
+  CK(cudaEventRecord(c->tev0, c->stream), "timer");
+  return MCX_OK;
+}
+
+extern "C" int mcx_timer_stop(mcx_ctx* c, float* ms) {
+  if (!c || !ms) return MCX_ERR_INPUT;
+  CK(cudaEventRecord(c->tev1, c->stream), "timer");
+  CK(cudaEventSynchronize(c->tev1), "timer");
+  CK(cudaEventElapsedTime(ms, c->tev0, c->tev1), "timer");
+  return MCX_OK;
+}
+
+extern "C" const char* mcx_version(void) { return "mcx 0.1 (sm_103a)"; }

@@ -1,0 +1,104 @@
+// mcx_device.cuh - device-side data structures and helpers shared by the
+// transport, opacity and balance kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mcx {
+
+// Frequency-independent grid description, passed by value to kernels.
+struct DevGrid {
+  int32_t nx, ny, nz, nCells, nbins;
+  int32_t symmetric, lgDust, lgGas, lgCompton, radPress;
+  int32_t starIdx[3];
+  float starPos[3];
+  float ionEdge1, rOut;
+  const float* xAxis;        // [nx]
+  const float* yAxis;        // [ny]
+  const float* zAxis;        // [nz]
+  const int32_t* active;     // [nz][ny][nx]
+  const float* nu;           // [nbins]
+  const float* srcCDF;       // [nbins]
+  const float* KNsigmaT;     // [nbins]
+  const float* KNcdfT;       // [nbins][180]  (theta fastest, one row per frequency)
+  const float* PcompT;       // [nbins][180]
+  const double* volD;        // [nCells+1] cell volume [e45 cm^3] (FP64)
+  const float* volF;         // [nCells+1] the same in FP32
+};
+
+// Per-cell fields the transport reads.
+struct DevTransportIn {
+  const float* opacity;      // [nbins][C+1]
+  const float* scaOpac;      // [nbins][C+1] or null
+  const float* recCDFT;      // [C+1][nbins]  re-emission CDF rows (frequency fastest)
+  const float* dustCDFT;     // [C+1][nbins]  dust emission CDF rows or null
+  const float* totalLines;   // [C+1]
+  const float* ne;           // [C+1]
+};
+
+struct DevTransportOut {
+  double* jste;              // [nbins][C+1]
+  double* escaped;           // [nbins+1][C+1]
+  double* hEst;              // [nbins][C+1] or null
+};
+
+// Counters accumulated by the transport kernel (device scratch).
+struct DevTransportCounters {
+  unsigned long long crossings, interactions, absorptions, scatterings;
+  unsigned long long escaped, lineEscapes, trapped, emissions;
+  unsigned long long errors;
+  unsigned long long queue;            // work-queue head (next packet index)
+  double qPhot;
+  unsigned long long pad[5];
+};
+
+// Philox4x32-10 (Salmon et al., SC'11), round constants of the published algorithm.
+__host__ __device__ inline void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                              uint32_t k0, uint32_t k1, uint32_t out[4]) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+#ifdef __CUDA_ARCH__
+    uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
+    uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+#else
+    uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+    uint32_t lo0 = (uint32_t)p0, hi0 = (uint32_t)(p0 >> 32), lo1 = (uint32_t)p1, hi1 = (uint32_t)(p1 >> 32);
+#endif
+    uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    if (r < 9) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+// Per-packet counter-based stream: draw k of packet pid is word k%4 of
+// philox(key, (pid_lo, pid_hi, k/4, k>>34)).
+struct PacketRng {
+  uint32_t k0, k1, p0, p1;
+  uint32_t buf[4];
+  uint32_t k;        // draws taken so far (histories never take 2^32 draws)
+
+  __device__ __forceinline__ void init(uint64_t seed, uint64_t pid) {
+    k0 = (uint32_t)seed; k1 = (uint32_t)(seed >> 32);
+    p0 = (uint32_t)pid; p1 = (uint32_t)(pid >> 32);
+    k = 0;
+  }
+  __device__ __forceinline__ uint32_t next() {
+    if ((k & 3u) == 0) philox4x32_10(p0, p1, k >> 2, 0u, k0, k1, buf);
+    uint32_t x;
+    switch (k & 3u) { case 0: x = buf[0]; break; case 1: x = buf[1]; break; case 2: x = buf[2]; break; default: x = buf[3]; }
+    ++k;
+    return x;
+  }
+};
+
+// Uniform in (0,1) in the geometry precision R.
+template <typename R> __device__ __forceinline__ R uniformFrom(uint32_t x);
+template <> __device__ __forceinline__ double uniformFrom<double>(uint32_t x) {
+  return ((double)x + 0.5) * (1.0 / 4294967296.0);
+}
+template <> __device__ __forceinline__ float uniformFrom<float>(uint32_t x) {
+  return ((float)(x >> 8) + 0.5f) * 5.9604644775390625e-08f;
+}
+
+}  // namespace mcx

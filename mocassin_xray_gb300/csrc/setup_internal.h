@@ -1,0 +1,116 @@
+// setup_internal.h - host-side model of one nebula: parsed input deck, frequency
+// mesh, cross-section tables, source spectrum and the initial grid state.
+// Built by setup.cpp; consumed by mcx_api.cu (upload to the device).
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace mcx {
+
+constexpr int kNElements = 30;      // nElements (source/constants_mod.f90:62)
+constexpr int kNHlevel = 10;        // nHlevel
+constexpr int kNHeIlevel = 9;       // nHeIlevel
+constexpr int kNHeIIlevel = 9;      // nHeIIlevel
+constexpr int kNAngles = 180;       // Compton theta bins (source/ph_mod.f90:1889)
+
+// Parsed input deck (keyword grammar of source/set_input_mod.f90:140-500,
+// defaults of :33-117).
+struct Params {
+  bool lgBadnell = true, lgCompton = true, lgRadPress = false;
+  bool lgHdenConstant = false, lgDfile = false, lgDlaw = false;
+  bool lgDust = false, lgDustConstant = false, lgGas = true;
+  bool lgSymmetricXYZ = false, lg1D = false, lgPlaneIonization = false;
+  bool lgAutoPackets = false, lgTalk = false, lgOutput = false;
+  bool lgMdMg = false, lgMdMh = false, lgDustScattering = true;
+  int nx = 30, ny = 30, nz = 30;
+  int maxIterateMC = 30, nbins = 600, nstages = 17;
+  int64_t nPhotons = 0;
+  int64_t maxPhotons = 0;
+  float convIncPercent = 0.f, nPhotIncrease = 0.f, convWriteGrid = 0.f;
+  float minConvergence = 95.f;
+  float Hdensity = 0.f, fillingFactor = 1.f;
+  float densityLaw[3] = {0.f, 0.f, 0.f};
+  float LPhot = 0.f, LStar = 0.f, TStellar = 0.f;
+  float nuMax = 15.f, nuMin = 1.001e-5f;
+  float Rnx = -1.f, Rny = -1.f, Rnz = -1.f, R_in = -1.f, R_out = 0.f;
+  float TeStart = 10000.f, XHILimit = 0.05f;
+  float NdustValue = 0.f, MdMgValue = 0.f;
+  float pwlIndex = 0.f, pwlMin = 0.f, pwlMax = 0.f;
+  float starPos[3] = {0.f, 0.f, 0.f};
+  bool haveStarPos = false, haveLStar = false, haveTStellar = false;
+  bool haveContShape = false, haveNPhotons = false, haveAbundance = false;
+  std::string contShape;          // "blackbody" | "powerlaw"
+  std::string densityFile, abundanceFile, NdustFile;
+  std::string dustFile[2];
+  std::string baseDir;            // directory the deck's relative paths are resolved against
+};
+
+struct Setup {
+  Params p;
+  std::string dataDir;
+  int meshMode = 0;
+
+  // composition (source/composition_mod.f90:10-70)
+  float elemAbun[kNElements] = {};
+  bool elemOn[kNElements] = {};
+  int elemXref[kNElements] = {};   // 1-based index among used elements, 0 if off
+  int nElemUsed = 0;
+
+  // Verner fits (source/ph_mod.f90:523-573): ph1(6,30,30,7), ph2(7,30,30)
+  float ph1[7][kNElements][kNElements][6] = {};   // [shell][ne][nz][i]
+  float ph2[kNElements][kNElements][7] = {};       // [ne][nz][i]
+
+  // frequency mesh
+  int nbins = 0;
+  std::vector<float> nu, widFlx;
+  std::vector<float> ionEdge;                        // sorted, nEdges entries
+
+  // mesh pointers (1-based like the reference)
+  int lymanP = 0, KshellLimitP = 0, secIonP = 0, cRecoilHP = 0, cRecoilHeP = 0;
+  int xrayP = 0, BjumpP = 0;
+  int HlevNuP[kNHlevel + 1] = {}, HeIlevNuP[kNHeIlevel + 1] = {}, HeIIlevNuP[kNHeIIlevel + 1] = {};
+  float HlevEn[kNHlevel + 1] = {}, HeIlevEn[kNHeIlevel + 1] = {}, HeIIlevEn[kNHeIIlevel + 1] = {};
+  int nShells[kNElements][kNElements] = {};          // [elem-1][ion-1]
+  int elementP[kNElements][kNElements][7][3] = {};   // [elem-1][ion-1][shell-1][k]
+
+  // cross sections (source/ph_mod.f90:204-517)
+  std::vector<float> xSec;                           // xSecArray (0-based storage, 1-based pointers)
+  int HlevXSecP[kNHlevel] = {}, HeISingXSecP[kNHeIlevel] = {}, HeIIXSecP[kNHeIIlevel] = {};
+  int bremsXSecP = 0;
+
+  // Compton tables (source/ph_mod.f90:1883-1924, :370-410)
+  std::vector<float> KNsigmaT;                       // [nbins]
+  std::vector<float> KNcdf, Pcomp;                   // [180][nbins] (frequency fastest)
+  std::vector<float> comXSecH, comXSecC, xSecRecoil; // [nbins]
+
+  // source spectrum (source/continuum_mod.f90:33-504)
+  std::vector<double> inSpectrumErg, inSpectrumPhot;
+  std::vector<float> srcCDF;                         // inSpectrumProbDen(1,:)
+  double normConstantErg = 0., normConstantPhot = 0.;
+  float LStar = 0.f, LPhot = 0.f, RStar = 0.f;
+
+  // grid
+  int nx = 0, ny = 0, nz = 0, nCells = 0;
+  std::vector<float> xAxis, yAxis, zAxis;
+  std::vector<int32_t> active;                       // [nz][ny][nx]
+  std::vector<float> Hden, Te, Ne, TeOld, NeOld;     // [nCells+1]
+  std::vector<float> ionDen;                         // [nstages][nElemUsed][nCells+1]
+  std::vector<float> volume;                         // [nCells+1]
+  std::vector<float> Ndust;                          // [nCells+1]
+  int starIdx[3] = {-1, -1, -1};
+  float starPos[3] = {0.f, 0.f, 0.f};
+
+  inline int activeAt(int i, int j, int k) const {   // 1-based Fortran indices
+    return active[(size_t)(i - 1) + (size_t)nx * ((size_t)(j - 1) + (size_t)ny * (size_t)(k - 1))];
+  }
+};
+
+// Builds a Setup from an input deck; throws std::runtime_error with a message.
+void buildSetup(Setup& s, const std::string& inputFile, const std::string& dataDir, int meshMode);
+
+// Bisection locate of source/interpolation_mod.f90:49-106 (1-based result:
+// 0 below range, n above range, the matched index on an exact hit).
+int locate(const float* xa, int n, float x);
+
+}  // namespace mcx

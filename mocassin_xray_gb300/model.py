@@ -1,0 +1,155 @@
+"""Host-side Python mirror of the reference's set-up and iteration phases,
+calling libmcx.so through its C ABI.
+
+``Setup`` is the model built from an input deck (readInput / initCartesianGrid
+/ initXSecArray / setContinuum / fillGrid of the reference).  ``Context`` holds
+the device-resident copy and runs the phases of one MC iteration the way
+iterateMC (source/iteration_mod.f90:32-1497) sequences them.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import abi
+from .abi import lib
+
+
+class Setup:
+    def __init__(self, input_file: str | Path, data_dir: str | Path, mesh_mode: int = abi.MESH_REFERENCE):
+        opts = abi.SetupOpts(mesh_mode=mesh_mode)
+        h = C.c_void_p()
+        abi.check_setup(lib().mcx_setup_from_input(str(input_file).encode(), str(data_dir).encode(),
+                                                   C.byref(opts), C.byref(h)))
+        self._h = h
+        info = abi.SetupInfo()
+        abi.check_setup(lib().mcx_setup_info_get(h, C.byref(info)))
+        self.info = info
+
+    def close(self) -> None:
+        if self._h:
+            lib().mcx_setup_free(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    # sizes
+    @property
+    def n_cells(self) -> int:
+        return self.info.n_cells
+
+    @property
+    def nbins(self) -> int:
+        return self.info.nbins
+
+    _DT = {abi.ARR_ACTIVE: np.int32, abi.SARR_POINTERS: np.int32, abi.SARR_ELEMENT_P: np.int32,
+           abi.SARR_N_SHELLS: np.int32, abi.SARR_ELEM_XREF: np.int32}
+
+    def get(self, arr_id: int) -> np.ndarray:
+        n = C.c_int64()
+        abi.check_setup(lib().mcx_setup_len(self._h, arr_id, C.byref(n)))
+        a = np.empty(n.value, dtype=self._DT.get(arr_id, np.float32))
+        abi.check_setup(lib().mcx_setup_get(self._h, arr_id, abi.as_ptr(a), a.nbytes))
+        return a
+
+    def set(self, arr_id: int, a: np.ndarray) -> None:
+        a = np.ascontiguousarray(a, dtype=self._DT.get(arr_id, np.float32))
+        abi.check_setup(lib().mcx_setup_set(self._h, arr_id, abi.as_ptr(a), a.nbytes))
+
+
+class Context:
+    """One device context (libmcx's mcx_ctx) holding one loaded model."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        rc = lib().mcx_ctx_create(device, C.byref(h))
+        if rc != abi.MCX_OK:
+            raise abi.McxError(rc, lib().mcx_setup_last_error().decode())
+        self._h = h
+        self.setup: Setup | None = None
+
+    def close(self) -> None:
+        if self._h:
+            lib().mcx_ctx_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc: int) -> None:
+        if rc != abi.MCX_OK:
+            buf = C.create_string_buffer(1024)
+            lib().mcx_last_error(self._h, buf, 1024)
+            raise abi.McxError(rc, buf.value.decode())
+
+    def load(self, setup: Setup) -> None:
+        self._check(lib().mcx_load(self._h, setup.handle))
+        self.setup = setup
+
+    def _shape(self, arr_id: int) -> tuple[tuple, type]:
+        s = self.setup.info
+        C1, nb = s.n_cells + 1, s.nbins
+        f32, f64 = np.float32, np.float64
+        shapes = {
+            abi.ARR_OPACITY: ((nb, C1), f32), abi.ARR_RECPDF: ((nb, C1), f32), abi.ARR_SCAOPAC: ((nb, C1), f32),
+            abi.ARR_DUSTPDF: ((nb, C1), f32), abi.ARR_JSTE: ((nb, C1), f64), abi.ARR_H_EST: ((nb, C1), f64),
+            abi.ARR_ESCAPED: ((nb + 1, C1), f64), abi.ARR_TOTAL_LINES: ((C1,), f32), abi.ARR_HDEN: ((C1,), f32),
+            abi.ARR_TE: ((C1,), f32), abi.ARR_NE: ((C1,), f32), abi.ARR_TEOLD: ((C1,), f32),
+            abi.ARR_NEOLD: ((C1,), f32), abi.ARR_VOLUME: ((C1,), f32), abi.ARR_GAUNT_TE: ((C1,), f32),
+            abi.ARR_NDUST: ((C1,), f32),
+            abi.ARR_IONDEN: ((s.nstages, max(s.n_elem_used, 1), C1), f32),
+        }
+        return shapes[arr_id]
+
+    def get(self, arr_id: int) -> np.ndarray:
+        shape, dt = self._shape(arr_id)
+        a = np.empty(shape, dtype=dt)
+        self._check(lib().mcx_get(self._h, arr_id, abi.as_ptr(a), a.nbytes))
+        return a
+
+    def put(self, arr_id: int, a: np.ndarray) -> None:
+        shape, dt = self._shape(arr_id)
+        a = np.ascontiguousarray(a, dtype=dt).reshape(shape)
+        self._check(lib().mcx_put(self._h, arr_id, abi.as_ptr(a), a.nbytes))
+
+    def opacity(self, n_iterate_mc: int = 1) -> abi.PhaseStats:
+        st = abi.PhaseStats()
+        o = abi.PhaseOpts(n_iterate_mc=n_iterate_mc)
+        self._check(lib().mcx_opacity(self._h, C.byref(o), C.byref(st)))
+        return st
+
+    def transport(self, n_packets: int, seed: int = 0, counter_base: int = 0, precision: int = abi.PREC_FP32_GEOM,
+                  zero: bool = True, n_photons_norm: int = 0, block_size: int = 0, grid_mult: int = 0) -> abi.TransportStats:
+        o = abi.TransportOpts(istar=1, precision=precision, n_packets=n_packets, seed=seed, counter_base=counter_base,
+                              n_photons_norm=n_photons_norm, zero_estimators=1 if zero else 0,
+                              block_size=block_size, grid_mult=grid_mult)
+        st = abi.TransportStats()
+        self._check(lib().mcx_transport(self._h, C.byref(o), C.byref(st)))
+        return st
+
+    def normalize_j(self) -> None:
+        self._check(lib().mcx_normalize_j(self._h))
+
+    def sync(self) -> None:
+        self._check(lib().mcx_sync(self._h))
+
+    def timer_start(self) -> None:
+        self._check(lib().mcx_timer_start(self._h))
+
+    def timer_stop(self) -> float:
+        ms = C.c_float()
+        self._check(lib().mcx_timer_stop(self._h, C.byref(ms)))
+        return ms.value

@@ -1,0 +1,191 @@
+"""ctypes binding of the CPU oracle (oracle/_build/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: the FP64 restatement of the reference that the
+GB300 kernels are checked against, and the timed CPU baseline.  Only tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline / reference arm use it.
+Parity unpinned against the reference's own outputs (the reference ships no
+tests or golden outputs and cannot be compiled without a Fortran compiler);
+pinned by analytic known-answer tests and the Philox4x32-10 published vectors.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "liboracle.so"
+
+
+def build() -> Path:
+    r = subprocess.run(["make", "-s", "-C", str(HERE)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+    return LIB_PATH
+
+
+_P = C.c_void_p
+_f = C.POINTER(C.c_float)
+_i = C.POINTER(C.c_int32)
+_d = C.POINTER(C.c_double)
+
+
+class TransportIn(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("n_cells", C.c_int32), ("nbins", C.c_int32),
+                ("symmetric_xyz", C.c_int32), ("lg_dust", C.c_int32), ("lg_gas", C.c_int32),
+                ("lg_compton", C.c_int32), ("rad_press", C.c_int32),
+                ("x_axis", _P), ("y_axis", _P), ("z_axis", _P), ("active", _P), ("nu", _P), ("src_cdf", _P),
+                ("kn_sigma_t", _P), ("kn_cdf", _P), ("pcomp", _P), ("opacity", _P), ("sca_opac", _P),
+                ("rec_pdf", _P), ("dust_pdf", _P), ("total_lines", _P), ("ne", _P),
+                ("ion_edge1", C.c_float), ("r_out", C.c_float), ("star_pos", C.c_float * 3),
+                ("star_idx", C.c_int32 * 3), ("delta_e", C.c_double)]
+
+
+class TransportOut(C.Structure):
+    _fields_ = [("jste", _P), ("escaped", _P), ("h_est", _P)]
+
+
+class TransportStats(C.Structure):
+    _fields_ = [("crossings", C.c_int64), ("interactions", C.c_int64), ("absorptions", C.c_int64),
+                ("scatterings", C.c_int64), ("escaped", C.c_int64), ("line_escapes", C.c_int64),
+                ("trapped", C.c_int64), ("emissions", C.c_int64), ("q_phot", C.c_double), ("error", C.c_int32),
+                ("pad", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+
+
+class OpacityIn(C.Structure):
+    _fields_ = [("n_cells", C.c_int32), ("nbins", C.c_int32), ("nstages", C.c_int32), ("n_elem_used", C.c_int32),
+                ("lg_compton", C.c_int32), ("n_xsec", C.c_int32), ("nu", _P), ("xsec", _P), ("kn_sigma_t", _P),
+                ("ptr", _P), ("elem_abun", _P), ("elem_xref", _P), ("n_shells", _P), ("element_p", _P),
+                ("hden", _P), ("te", _P), ("ne", _P), ("ionden", _P), ("gaunt_te", _P), ("compute", _P)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            build()
+        l = C.CDLL(str(LIB_PATH))
+        l.orc_philox4x32_10.argtypes = [_P, _P, _P]
+        l.orc_philox4x32_10.restype = None
+        l.orc_transport.argtypes = [C.POINTER(TransportIn), C.c_uint64, C.c_uint64, C.c_int64, C.c_int32,
+                                    C.POINTER(TransportOut), C.POINTER(TransportStats)]
+        l.orc_transport.restype = C.c_int
+        l.orc_opacity.argtypes = [C.POINTER(OpacityIn), _P]
+        l.orc_opacity.restype = C.c_int
+        l.orc_gaunt_ff.argtypes = [C.c_double, C.c_double, _P, C.c_int32, _P]
+        l.orc_gaunt_ff.restype = None
+        l.orc_gaunt_cache.argtypes = [C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, C.POINTER(C.c_float), _P]
+        l.orc_gaunt_cache.restype = None
+        _lib = l
+    return _lib
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def philox(ctr, key) -> np.ndarray:
+    c = np.ascontiguousarray(ctr, dtype=np.uint32)
+    k = np.ascontiguousarray(key, dtype=np.uint32)
+    out = np.zeros(4, dtype=np.uint32)
+    lib().orc_philox4x32_10(_p(c), _p(k), _p(out))
+    return out
+
+
+def gaunt_ff(z: float, log10te: float, nu: np.ndarray) -> np.ndarray:
+    nu = np.ascontiguousarray(nu, dtype=np.float32)
+    g = np.zeros(nu.size, dtype=np.float64)
+    lib().orc_gaunt_ff(z, log10te, _p(nu), nu.size, _p(g))
+    return g
+
+
+def gaunt_cache(nx, ny, nz, active, te, compute, te_old: float) -> tuple[np.ndarray, float]:
+    active = np.ascontiguousarray(active, dtype=np.int32)
+    te = np.ascontiguousarray(te, dtype=np.float32)
+    compute = np.ascontiguousarray(compute, dtype=np.uint8)
+    out = np.zeros(te.size, dtype=np.float32)
+    t = C.c_float(te_old)
+    lib().orc_gaunt_cache(nx, ny, nz, _p(active), _p(te), _p(compute), C.byref(t), _p(out))
+    return out, t.value
+
+
+def opacity(setup, te=None, ne=None, ionden=None, hden=None, gaunt_te=None, compute=None, out=None) -> np.ndarray:
+    """Oracle opacity for a mocassin_xray_gb300.Setup (arrays default to the set-up's state)."""
+    from mocassin_xray_gb300 import abi
+    i = setup.info
+    C1, nb = i.n_cells + 1, i.nbins
+    arrs = dict(
+        nu=setup.get(abi.ARR_NU), xsec=setup.get(abi.ARR_XSEC), kn=setup.get(abi.ARR_KN_SIGMA_T),
+        ptr=setup.get(abi.SARR_POINTERS), abun=setup.get(abi.ARR_ELEM_ABUN), xref=setup.get(abi.SARR_ELEM_XREF),
+        nsh=setup.get(abi.SARR_N_SHELLS), ep=setup.get(abi.SARR_ELEMENT_P),
+        hden=np.ascontiguousarray(hden if hden is not None else setup.get(abi.ARR_HDEN), dtype=np.float32),
+        te=np.ascontiguousarray(te if te is not None else setup.get(abi.ARR_TE), dtype=np.float32),
+        ne=np.ascontiguousarray(ne if ne is not None else setup.get(abi.ARR_NE), dtype=np.float32),
+        ion=np.ascontiguousarray(ionden if ionden is not None else setup.get(abi.ARR_IONDEN), dtype=np.float32),
+    )
+    if compute is None:
+        compute = np.ones(C1, dtype=np.uint8)
+        compute[0] = 0
+    compute = np.ascontiguousarray(compute, dtype=np.uint8)
+    if gaunt_te is None:
+        gaunt_te, _ = gaunt_cache(i.nx, i.ny, i.nz, setup.get(abi.ARR_ACTIVE), arrs["te"], compute, -1.0)
+    gaunt_te = np.ascontiguousarray(gaunt_te, dtype=np.float32)
+    if out is None:
+        out = np.zeros((nb, C1), dtype=np.float32)
+    s = OpacityIn(n_cells=i.n_cells, nbins=nb, nstages=i.nstages, n_elem_used=max(i.n_elem_used, 1),
+                  lg_compton=i.lg_compton, n_xsec=arrs["xsec"].size, nu=_p(arrs["nu"]), xsec=_p(arrs["xsec"]),
+                  kn_sigma_t=_p(arrs["kn"]), ptr=_p(arrs["ptr"]), elem_abun=_p(arrs["abun"]),
+                  elem_xref=_p(arrs["xref"]), n_shells=_p(arrs["nsh"]), element_p=_p(arrs["ep"]),
+                  hden=_p(arrs["hden"]), te=_p(arrs["te"]), ne=_p(arrs["ne"]), ionden=_p(arrs["ion"]),
+                  gaunt_te=_p(gaunt_te), compute=_p(compute))
+    rc = lib().orc_opacity(C.byref(s), _p(out))
+    if rc != 0:
+        raise RuntimeError(f"orc_opacity failed: {rc}")
+    return out
+
+
+def transport(setup, opacity_arr, rec_pdf, total_lines, ne=None, n: int = 1000, seed: int = 0,
+              counter_base: int = 0, nthreads: int = 1, n_photons_norm: int = 0,
+              sca_opac=None, dust_pdf=None):
+    """Oracle transport of packets [counter_base, counter_base+n); returns (Jste, escaped, stats)."""
+    from mocassin_xray_gb300 import abi
+    i = setup.info
+    C1, nb = i.n_cells + 1, i.nbins
+    keep = dict(
+        x=setup.get(abi.ARR_XAXIS), y=setup.get(abi.ARR_YAXIS), z=setup.get(abi.ARR_ZAXIS),
+        act=setup.get(abi.ARR_ACTIVE), nu=setup.get(abi.ARR_NU), cdf=setup.get(abi.ARR_SRC_CDF),
+        kn=setup.get(abi.ARR_KN_SIGMA_T), kncdf=setup.get(abi.ARR_KN_CDF), pc=setup.get(abi.ARR_PCOMP),
+        op=np.ascontiguousarray(opacity_arr, dtype=np.float32),
+        rec=np.ascontiguousarray(rec_pdf, dtype=np.float32),
+        tl=np.ascontiguousarray(total_lines, dtype=np.float32),
+        ne=np.ascontiguousarray(ne if ne is not None else setup.get(abi.ARR_NE), dtype=np.float32),
+        sca=None if sca_opac is None else np.ascontiguousarray(sca_opac, dtype=np.float32),
+        dust=None if dust_pdf is None else np.ascontiguousarray(dust_pdf, dtype=np.float32),
+    )
+    norm = n_photons_norm if n_photons_norm > 0 else n
+    s = TransportIn(nx=i.nx, ny=i.ny, nz=i.nz, n_cells=i.n_cells, nbins=nb, symmetric_xyz=i.symmetric_xyz,
+                    lg_dust=i.lg_dust, lg_gas=i.lg_gas, lg_compton=i.lg_compton, rad_press=0,
+                    x_axis=_p(keep["x"]), y_axis=_p(keep["y"]), z_axis=_p(keep["z"]), active=_p(keep["act"]),
+                    nu=_p(keep["nu"]), src_cdf=_p(keep["cdf"]), kn_sigma_t=_p(keep["kn"]),
+                    kn_cdf=_p(keep["kncdf"]), pcomp=_p(keep["pc"]), opacity=_p(keep["op"]),
+                    sca_opac=_p(keep["sca"]), rec_pdf=_p(keep["rec"]), dust_pdf=_p(keep["dust"]),
+                    total_lines=_p(keep["tl"]), ne=_p(keep["ne"]), ion_edge1=i.ion_edge1, r_out=i.r_out,
+                    delta_e=float(np.float32(i.l_star)) / norm)
+    s.star_pos[:] = list(i.star_pos)
+    s.star_idx[:] = list(i.star_idx)
+    j = np.zeros((nb, C1), dtype=np.float64)
+    e = np.zeros((nb + 1, C1), dtype=np.float64)
+    o = TransportOut(jste=_p(j), escaped=_p(e), h_est=None)
+    st = TransportStats()
+    rc = lib().orc_transport(C.byref(s), seed, counter_base, n, nthreads, C.byref(o), C.byref(st))
+    if rc != 0:
+        raise RuntimeError(f"orc_transport failed: {rc}")
+    return j, e, st

@@ -1,0 +1,130 @@
+/*
+ * oracle.h - CPU FP64 restatement of the MOCASSIN iteration hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GB300
+ * kernels of libmcx.so and the timed CPU baseline of bench.py; nothing in the
+ * product links, loads or calls it.  It restates the Fortran reference
+ * (rwesson/mocassin_xray, "MOCASSIN 2007 Version 3") routine by routine; each
+ * function cites the reference file:line it follows.
+ *
+ * Parity status: the reference has no tests, golden vectors or fixtures, and
+ * it cannot be compiled here or on the GPU hosts (no Fortran compiler), so
+ * this restatement is pinned only by analytic known-answer tests and by the
+ * published Philox4x32-10 known-answer vectors: parity unpinned against the
+ * reference's own outputs.
+ *
+ * Arrays use the reference's Fortran layouts:
+ *   [nbins][nCells+1] for A(0:nCells,1:nbins), [nz][ny][nx] for active(nx,ny,nz).
+ */
+#ifndef MCX_ORACLE_H
+#define MCX_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ RNG */
+/* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).  Packet p draws its
+ * k-th uniform from block k/4, word k%4 of philox(key=(seed_lo,seed_hi),
+ * ctr=(p_lo, p_hi, k/4, 0)). */
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+/* ------------------------------------------------------------ transport */
+typedef struct orc_transport_in {
+    int32_t nx, ny, nz, n_cells, nbins;
+    int32_t symmetric_xyz, lg_dust, lg_gas, lg_compton, rad_press;
+    const float* x_axis;        /* [nx] */
+    const float* y_axis;        /* [ny] */
+    const float* z_axis;        /* [nz] */
+    const int32_t* active;      /* [nz][ny][nx] */
+    const float* nu;            /* [nbins] nuArray */
+    const float* src_cdf;       /* [nbins] inSpectrumProbDen(iStar,:) */
+    const float* kn_sigma_t;    /* [nbins] */
+    const float* kn_cdf;        /* [180][nbins] */
+    const float* pcomp;         /* [180][nbins] */
+    const float* opacity;       /* [nbins][C+1] */
+    const float* sca_opac;      /* [nbins][C+1] or NULL (dust) */
+    const float* rec_pdf;       /* [nbins][C+1] */
+    const float* dust_pdf;      /* [nbins][C+1] or NULL (dust only) */
+    const float* total_lines;   /* [C+1] */
+    const float* ne;            /* [C+1] */
+    float ion_edge1;            /* ionEdge(1) */
+    float r_out;                /* R_out */
+    float star_pos[3];
+    int32_t star_idx[3];        /* 1-based */
+    double delta_e;             /* Lstar/nPhotons */
+} orc_transport_in;
+
+typedef struct orc_transport_out {
+    double* jste;               /* [nbins][C+1], accumulated (not cleared) */
+    double* escaped;            /* [nbins+1][C+1], accumulated */
+    double* h_est;              /* [nbins][C+1] or NULL */
+} orc_transport_out;
+
+typedef struct orc_transport_stats {
+    int64_t crossings, interactions, absorptions, scatterings;
+    int64_t escaped, line_escapes, trapped, emissions;
+    double q_phot;
+    int32_t error;              /* 0 ok; 1 insane state (the reference `stop`s) */
+    int32_t pad;
+} orc_transport_stats;
+
+/* Transport packets [counter_base, counter_base + n) from the stellar source.
+ * Returns 0 or a nonzero error code.  `nthreads` > 1 splits the packets over
+ * OpenMP-free POSIX threads with private estimator copies summed at the end. */
+int orc_transport(const orc_transport_in* in, uint64_t seed, uint64_t counter_base, int64_t n,
+                  int32_t nthreads, orc_transport_out* out, orc_transport_stats* stats);
+
+/* Volume [e45 cm^3] of cell (xP,yP,zP), 1-based (getVolume, source/grid_mod.f90:2887-2986). */
+double orc_cell_volume(const orc_transport_in* in, int32_t xP, int32_t yP, int32_t zP);
+
+
+/* -------------------------------------------------------------- opacity */
+/* Packed set-up pointers (1-based like the reference), see mcx_setup_get(MCX_ARR_POINTERS). */
+enum {
+    ORC_P_HLEVXSECP1 = 0, ORC_P_HLEVNUP1, ORC_P_HEISINGXSECP1, ORC_P_HEILEVNUP1,
+    ORC_P_HEIIXSECP1, ORC_P_HEIILEVNUP1, ORC_P_BREMSXSECP, ORC_P_LYMANP, ORC_P_COUNT_ = 32
+};
+
+typedef struct orc_opacity_in {
+    int32_t n_cells, nbins, nstages, n_elem_used, lg_compton, n_xsec;
+    const float* nu;            /* [nbins] */
+    const float* xsec;          /* [n_xsec] xSecArray */
+    const float* kn_sigma_t;    /* [nbins] */
+    const int32_t* ptr;         /* [32] packed pointers (ORC_P_*) */
+    const float* elem_abun;     /* [30] */
+    const int32_t* elem_xref;   /* [30] 1-based, 0 = element off */
+    const int32_t* n_shells;    /* [30][30]  nShells(elem,ion) at [elem-1][ion-1] */
+    const int32_t* element_p;   /* [30][30][7][3] elementP(elem,ion,shell,k) */
+    const float* hden;          /* [C+1] */
+    const float* te;            /* [C+1] */
+    const float* ne;            /* [C+1] */
+    const float* ionden;        /* [nstages][n_elem_used][C+1] */
+    const float* gaunt_te;      /* [C+1] Te at which gauntFF was tabulated for the cell */
+    const uint8_t* compute;     /* [C+1] 1 = recompute the cell, 0 = keep (skip rule) */
+} orc_opacity_in;
+
+/* ionizationDriver/BoltGaunt/getGauntFF/eDenSum/addOpacity
+ * (source/ionization_mod.f90:26-477) for every cell with compute[c] = 1;
+ * writes opacity[nu][c] (Fortran layout); other cells are left untouched. */
+int orc_opacity(const orc_opacity_in* in, float* opacity);
+
+/* Hummer (1988) free-free Gaunt factor fit of getGauntFF
+ * (source/ionization_mod.f90:196-334) at log10(Z) = z, log10(Te) and n frequencies. */
+void orc_gaunt_ff(double z, double log10te, const float* nu, int32_t n, double* g);
+
+/* The reference tabulates gauntFF only when Te moved by more than 10 % since
+ * the last tabulation (BoltGaunt, source/ionization_mod.f90:136-178), a cache
+ * shared by all cells in processing order (i, j, k nested, k fastest).  This
+ * replays that cache: for each active cell in processing order with
+ * compute[c] = 1 it updates *te_old (the saved TeOld2; start at -1) and writes
+ * the tabulation temperature to gaunt_te[c]. */
+void orc_gaunt_cache(int32_t nx, int32_t ny, int32_t nz, const int32_t* active, const float* te,
+                     const uint8_t* compute, float* te_old, float* gaunt_te);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,111 @@
+"""Parity of the GB300 transport kernels with the FP64 oracle.
+
+Packet k draws from the same Philox stream in both, so the FP64 plain path
+follows the oracle's histories step for step: the estimators agree to
+rounding (the libm of the GPU and of the host differ in the last bit of
+log/cos/sin, which moves interaction points by ~1e-16 relative).  The
+production FP32-geometry path follows the same histories except where a
+float rounding flips a discrete decision; it is checked statistically.
+"""
+import numpy as np
+import pytest
+
+from conftest import synthetic_recpdf
+from mocassin_xray_gb300 import abi, configs, Context, Setup
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(decks, data_dir, oracle_lib, name):
+    s = Setup(decks[name], data_dir)
+    op = oracle_lib.opacity(s)
+    rec = synthetic_recpdf(s.get(abi.ARR_NU), s.n_cells)
+    tl = np.full(s.n_cells + 1, 0.3, np.float32)
+    ctx = Context(0)
+    ctx.load(s)
+    ctx.put(abi.ARR_OPACITY, op)
+    ctx.put(abi.ARR_RECPDF, rec)
+    ctx.put(abi.ARR_TOTAL_LINES, tl)
+    return s, op, rec, tl, ctx
+
+
+@pytest.mark.parametrize("name", ["h_small", "lognormal_small"])
+def test_fp64_transport_matches_oracle(decks, data_dir, oracle_lib, name):
+    s, op, rec, tl, ctx = _case(decks, data_dir, oracle_lib, name)
+    n, seed = 20000, 1234
+    st = ctx.transport(n, seed=seed, precision=abi.PREC_FP64)
+    j = ctx.get(abi.ARR_JSTE)
+    esc = ctx.get(abi.ARR_ESCAPED)
+    jo, eo, so = oracle_lib.transport(s, op, rec, tl, n=n, seed=seed, nthreads=4)
+    assert so.error == 0
+    # identical histories: identical event counts (a rare last-bit flip may move one event)
+    for k in ("crossings", "interactions", "absorptions", "scatterings", "escaped", "line_escapes", "emissions"):
+        assert abs(getattr(st, k) - getattr(so, k)) <= max(2, 1e-4 * getattr(so, k)), k
+    assert st.trapped == 0
+    # estimator totals to rounding, per-cell/per-bin entries to rounding for all but a few
+    assert j.sum() == pytest.approx(jo.sum(), rel=1e-9)
+    assert esc.sum() == pytest.approx(eo.sum(), rel=1e-9)
+    rel = np.abs(j - jo) / np.maximum(np.abs(jo), 1e-300)
+    bad = (rel > 1e-9) & (jo > 0)
+    assert bad.sum() <= 1e-3 * (jo > 0).sum()
+    assert st.q_phot == pytest.approx(so.q_phot, rel=1e-9)
+    ctx.close()
+
+
+@pytest.mark.parametrize("name", ["h_small", "lognormal_small"])
+def test_fp32_transport_statistics(decks, data_dir, oracle_lib, name):
+    s, op, rec, tl, ctx = _case(decks, data_dir, oracle_lib, name)
+    n, seed = 40000, 99
+    st = ctx.transport(n, seed=seed, precision=abi.PREC_FP32_GEOM)
+    j = ctx.get(abi.ARR_JSTE)
+    esc = ctx.get(abi.ARR_ESCAPED)
+    jo, eo, so = oracle_lib.transport(s, op, rec, tl, n=n, seed=seed, nthreads=4)
+    # energy is conserved exactly by the bookkeeping
+    de = float(np.float32(s.info.l_star)) / n
+    assert esc.sum() + st.line_escapes * de == pytest.approx(float(np.float32(s.info.l_star)), rel=1e-9)
+    assert st.escaped + st.line_escapes == n
+    # same random integers, FP32 geometry: the histories mostly coincide
+    assert st.crossings == pytest.approx(so.crossings, rel=2e-3)
+    assert st.absorptions == pytest.approx(so.absorptions, rel=5e-3, abs=5)
+    # J integrated over frequency per cell agrees within 1 % where the oracle's MC noise is small
+    jc, joc = j[:, 1:].sum(0), jo[:, 1:].sum(0)
+    hit = joc > np.percentile(joc, 50)
+    assert np.median(np.abs(jc[hit] / joc[hit] - 1)) < 1e-3
+    assert jc.sum() == pytest.approx(joc.sum(), rel=2e-3)
+    ctx.close()
+
+
+def test_transport_sharding_composes(decks, data_dir, oracle_lib):
+    """Two calls over packet ranges [0,n/2) and [n/2,n) accumulate the same
+    estimators as one call over [0,n) (how ranks shard packets)."""
+    s, op, rec, tl, ctx = _case(decks, data_dir, oracle_lib, "h_small")
+    n = 10000
+    ctx.transport(n, seed=5, precision=abi.PREC_FP64)
+    j_all = ctx.get(abi.ARR_JSTE)
+    ctx.transport(n // 2, seed=5, precision=abi.PREC_FP64, n_photons_norm=n)
+    ctx.transport(n // 2, seed=5, counter_base=n // 2, precision=abi.PREC_FP64, n_photons_norm=n, zero=False)
+    j_two = ctx.get(abi.ARR_JSTE)
+    np.testing.assert_allclose(j_two, j_all, rtol=1e-11, atol=1e-300)
+    ctx.close()
+
+
+def test_normalize_j(decks, data_dir, oracle_lib):
+    s, op, rec, tl, ctx = _case(decks, data_dir, oracle_lib, "h_small")
+    ctx.transport(2000, seed=1, precision=abi.PREC_FP64)
+    j = ctx.get(abi.ARR_JSTE)
+    ctx.normalize_j()
+    jn = ctx.get(abi.ARR_JSTE)
+    # octant mode: (J * 1e-9) / 8  (source/iteration_mod.f90:1002-1031)
+    np.testing.assert_array_equal(jn, (j * 1e-9) / 8.0)
+    ctx.close()
+
+
+def test_block_shapes_give_identical_results(decks, data_dir, oracle_lib):
+    """Scheduling (block size, blocks per SM) does not change any history."""
+    s, op, rec, tl, ctx = _case(decks, data_dir, oracle_lib, "lognormal_small")
+    ctx.transport(8000, seed=2, precision=abi.PREC_FP64, block_size=256)
+    j1 = ctx.get(abi.ARR_JSTE)
+    ctx.transport(8000, seed=2, precision=abi.PREC_FP64, block_size=64, grid_mult=1)
+    j2 = ctx.get(abi.ARR_JSTE)
+    np.testing.assert_allclose(j2, j1, rtol=1e-11, atol=1e-300)
+    ctx.close()
