@@ -239,6 +239,63 @@ int  mcx_transport(mcx_ctx* ctx, const mcx_transport_opts* opts, mcx_transport_s
  * escaped /8 in octant mode (source/iteration_mod.f90:1002-1031). */
 int  mcx_normalize_j(mcx_ctx* ctx);
 
+
+/* ------------------------------------------- transport without allocation */
+/* No counterpart in the reference.  Some callers cannot allocate device
+ * memory themselves: a Fortran or C host that receives device buffers from a
+ * framework's own pool, or code that runs where cudaMalloc is not allowed
+ * while other work holds the device.  This entry point runs the same transport
+ * kernel as mcx_transport but allocates nothing: the caller passes every input
+ * and output as a device pointer, and the kernel's scratch (work-queue head and
+ * counters, the per-cell volumes, the re-emission CDF rows and the Compton
+ * tables transposed for sampling) lives in one file-scope __device__ array of
+ * MCX_NOALLOC_SCRATCH_BYTES that every GPU loading libmcx.so holds until the
+ * process exits.  Problems whose scratch would exceed it are rejected with
+ * MCX_ERR_INPUT.
+ *  - The first call on a device looks up that array's device address
+ *    (cudaGetSymbolAddress) with the device current; make that first call
+ *    before any stream capture.
+ *  - Every call shares the one array: calls whose work overlaps on the GPU
+ *    (different streams or threads at the same time) race on it.  The entry
+ *    point clears the counters each call and rewrites the rest.
+ *  - Gas only (no dust), single mother grid, source 1, arrays in the Fortran
+ *    layouts given at the top of this header. */
+#define MCX_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
+
+typedef struct mcx_noalloc_transport_args {
+    int32_t nx, ny, nz, n_cells, nbins;
+    int32_t symmetric_xyz, lg_compton, precision;  /* precision: MCX_PREC_* */
+    int32_t star_idx[3];        /* 1-based                                   */
+    int32_t zero_estimators;    /* 1: clear jste/escaped first               */
+    float   star_pos[3];
+    float   ion_edge1, r_out;
+    int32_t pad0;
+    double  delta_e;            /* Lstar / nPhotons                          */
+    int64_t n_packets;
+    uint64_t seed, counter_base;
+    /* device pointers, caller-owned */
+    const float*   x_axis;      /* [nx]                                     */
+    const float*   y_axis;      /* [ny]                                     */
+    const float*   z_axis;      /* [nz]                                     */
+    const int32_t* active;      /* [nz][ny][nx]                             */
+    const float*   nu;          /* [nbins]                                  */
+    const float*   src_cdf;     /* [nbins]                                  */
+    const float*   kn_sigma_t;  /* [nbins]                                  */
+    const float*   kn_cdf;      /* [180][nbins] KNsigmaArray(nbins,180)     */
+    const float*   pcomp;       /* [180][nbins] PcompArray(nbins,180)       */
+    const float*   opacity;     /* [nbins][C+1]                             */
+    const float*   rec_pdf;     /* [nbins][C+1]                             */
+    const float*   total_lines; /* [C+1]                                    */
+    const float*   ne;          /* [C+1]                                    */
+    double*        jste;        /* [nbins][C+1]   accumulated               */
+    double*        escaped;     /* [nbins+1][C+1] accumulated               */
+    void*          stream;      /* cudaStream_t; NULL = legacy default stream */
+} mcx_noalloc_transport_args;
+
+int  mcx_transport_noalloc(const mcx_noalloc_transport_args* args, mcx_transport_stats* stats);
+/* Message of the last mcx_transport_noalloc failure of this thread. */
+const char* mcx_noalloc_last_error(void);
+
 /* ------------------------------------------------------------- timing */
 /* CUDA events on the context stream (for callers that time a group of calls). */
 int  mcx_timer_start(mcx_ctx* ctx);

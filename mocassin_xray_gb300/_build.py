@@ -44,6 +44,7 @@ def build_lib(verbose: bool = False) -> Path:
         ("k_opacity.cu", []),
         ("k_transport_f32.cu", []),
         ("k_transport_f64.cu", ["--fmad=false"]),
+        ("mcx_noalloc.cu", []),
     ]
     cmds = []
     objs = []

@@ -70,6 +70,22 @@ class TransportStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("reserved")}
 
 
+class NoallocTransportArgs(C.Structure):
+    """mcx_noalloc_transport_args: every buffer is a caller-owned device pointer."""
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("n_cells", C.c_int32),
+                ("nbins", C.c_int32), ("symmetric_xyz", C.c_int32), ("lg_compton", C.c_int32),
+                ("precision", C.c_int32), ("star_idx", C.c_int32 * 3), ("zero_estimators", C.c_int32),
+                ("star_pos", C.c_float * 3), ("ion_edge1", C.c_float), ("r_out", C.c_float), ("pad0", C.c_int32),
+                ("delta_e", C.c_double), ("n_packets", C.c_int64), ("seed", C.c_uint64), ("counter_base", C.c_uint64),
+                ("x_axis", C.c_void_p), ("y_axis", C.c_void_p), ("z_axis", C.c_void_p), ("active", C.c_void_p),
+                ("nu", C.c_void_p), ("src_cdf", C.c_void_p), ("kn_sigma_t", C.c_void_p), ("kn_cdf", C.c_void_p),
+                ("pcomp", C.c_void_p), ("opacity", C.c_void_p), ("rec_pdf", C.c_void_p),
+                ("total_lines", C.c_void_p), ("ne", C.c_void_p), ("jste", C.c_void_p), ("escaped", C.c_void_p),
+                ("stream", C.c_void_p)]
+
+
+NOALLOC_SCRATCH_BYTES = 64 * 1024 * 1024
+
 # exported symbols and their signatures: (name, restype, argtypes)
 _P = C.c_void_p
 SIGNATURES = [
@@ -94,6 +110,8 @@ SIGNATURES = [
     ("mcx_timer_start", C.c_int, [_P]),
     ("mcx_timer_stop", C.c_int, [_P, C.POINTER(C.c_float)]),
     ("mcx_version", C.c_char_p, []),
+    ("mcx_transport_noalloc", C.c_int, [C.POINTER(NoallocTransportArgs), C.POINTER(TransportStats)]),
+    ("mcx_noalloc_last_error", C.c_char_p, []),
 ]
 
 _lib = None
