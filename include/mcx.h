@@ -90,6 +90,23 @@ enum mcx_array_id {
 #define MCX_SARR_COMXSEC_H     1006  /* float[nbins] comXSecH                                           */
 #define MCX_SARR_COMXSEC_C     1007  /* float[nbins] comXSecC                                           */
 #define MCX_SARR_XSEC_RECOIL   1008  /* float[nbins] xSecRecoil                                         */
+/* emission tables (read once from data/) */
+#define MCX_SARR_EM_DIMS       1009  /* int32[16]: nTk, nlimHI, nlimHeI, nlimHeII, nFbHeavy, nHydroFiles,
+                                        j2TsP, HeIILymanP(1:4), 0...                                   */
+#define MCX_SARR_EM_TK         1010  /* float[nTk]                                                      */
+#define MCX_SARR_EM_EDGE_P     1011  /* int32[3][32]                                                    */
+#define MCX_SARR_EM_LOG_GAMMA  1012  /* float[3][nTk][32]                                               */
+#define MCX_SARR_EM_FB_HEAVY   1013  /* int32[nFbHeavy][7]                                              */
+#define MCX_SARR_EM_HYDRO_MAP  1014  /* int32[9][12]                                                    */
+#define MCX_SARR_EM_HYDRO_DENS 1015  /* float[nHydroFiles][13]                                          */
+#define MCX_SARR_EM_HYDRO_LINES 1016 /* float[nHydroFiles][13][14][8]                                   */
+#define MCX_SARR_EM_HYDRO_TEMPS 1017 /* float[12]                                                       */
+#define MCX_SARR_EM_HB_COEFF   1018  /* float[2][9][4]                                                  */
+#define MCX_SARR_EM_RB_EDGE    1019  /* float[2][3][26]                                                 */
+#define MCX_SARR_EM_R2A_EDGE   1020  /* float[3][18]                                                    */
+#define MCX_SARR_EM_HEI_REC    1021  /* float[34][3][4]                                                 */
+#define MCX_SARR_EM_HEI_2PHOT  1022  /* float[2][41]                                                    */
+#define MCX_SARR_EM_HEII_LYMAN 1023  /* float[2][4] ratios, frequencies                                 */
 
 /* -------------------------------------------------------------- set-up */
 /* Host-side model built from an input deck.  Replaces readInput
@@ -188,6 +205,19 @@ typedef struct mcx_phase_stats {
 } mcx_phase_stats;
 
 int  mcx_opacity(mcx_ctx* ctx, const mcx_phase_opts* opts, mcx_phase_stats* stats);
+
+/* ------------------------------------------------------- phase: emission */
+/* Per-cell diffuse emission: the re-emission CDF recPDF(cell,:) (H, He and
+ * heavy-ion free-bound + free-free continua, two-photon continua, the He I
+ * 2^3S and He II Lyman lines) and the fraction of non-ionising line photons
+ * totalLines(cell) (hydrogenic and He I recombination lines, plus forbidden
+ * lines when heavy ions have atomic data).  Replaces the emissionDriver loop of
+ * iterateMC (source/iteration_mod.f90:279-623) and emissionDriver / fb_ff /
+ * twoPhoton / RecLinesEmission / setDiffusePDF (source/emission_mod.f90:36-252,
+ * :336-1151, :1528-1919), with the same skip rule as the opacity phase.  The
+ * free-free Gaunt factors are those last tabulated by mcx_opacity, as in the
+ * reference, so mcx_opacity must have run at least once. */
+int  mcx_emission(mcx_ctx* ctx, const mcx_phase_opts* opts, mcx_phase_stats* stats);
 
 /* ------------------------------------------------------ phase: transport */
 /* Monte Carlo transport of n packets from source iStar, accumulating the

@@ -40,6 +40,8 @@ def build_lib(verbose: bool = False) -> Path:
     common = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", str(INCLUDE), "-I", str(CSRC)]
     units = [
         ("setup.cpp", ["-x", "cu"]),
+        ("setup_emission.cpp", ["-x", "cu"]),
+        ("k_emission.cu", []),
         ("mcx_api.cu", []),
         ("k_opacity.cu", []),
         ("k_transport_f32.cu", []),

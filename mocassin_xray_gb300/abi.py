@@ -24,6 +24,11 @@ ERRORS = {1: "MCX_ERR_INPUT", 2: "MCX_ERR_IO", 3: "MCX_ERR_CUDA", 4: "MCX_ERR_NO
  ARR_NDUST, ARR_LG_CONVERGED, ARR_H_EST) = range(1, 31)
 SARR_POINTERS, SARR_ELEMENT_P, SARR_N_SHELLS, SARR_ELEM_XREF, SARR_ION_EDGE, SARR_COMXSEC_H, \
     SARR_COMXSEC_C, SARR_XSEC_RECOIL = range(1001, 1009)
+(SARR_EM_DIMS, SARR_EM_TK, SARR_EM_EDGE_P, SARR_EM_LOG_GAMMA, SARR_EM_FB_HEAVY, SARR_EM_HYDRO_MAP,
+ SARR_EM_HYDRO_DENS, SARR_EM_HYDRO_LINES, SARR_EM_HYDRO_TEMPS, SARR_EM_HB_COEFF, SARR_EM_RB_EDGE,
+ SARR_EM_R2A_EDGE, SARR_EM_HEI_REC, SARR_EM_HEI_2PHOT, SARR_EM_HEII_LYMAN) = range(1009, 1024)
+INT_SARR = {SARR_POINTERS, SARR_ELEMENT_P, SARR_N_SHELLS, SARR_ELEM_XREF, SARR_EM_DIMS, SARR_EM_EDGE_P,
+            SARR_EM_FB_HEAVY, SARR_EM_HYDRO_MAP}
 
 MESH_REFERENCE, MESH_LOG_EDGES = 0, 1
 PREC_FP32_GEOM, PREC_FP64 = 0, 1
@@ -105,6 +110,7 @@ SIGNATURES = [
     ("mcx_put", C.c_int, [_P, C.c_int32, _P, C.c_size_t]),
     ("mcx_device_ptr", C.c_int, [_P, C.c_int32, C.POINTER(_P)]),
     ("mcx_opacity", C.c_int, [_P, C.POINTER(PhaseOpts), C.POINTER(PhaseStats)]),
+    ("mcx_emission", C.c_int, [_P, C.POINTER(PhaseOpts), C.POINTER(PhaseStats)]),
     ("mcx_transport", C.c_int, [_P, C.POINTER(TransportOpts), C.POINTER(TransportStats)]),
     ("mcx_normalize_j", C.c_int, [_P]),
     ("mcx_timer_start", C.c_int, [_P]),

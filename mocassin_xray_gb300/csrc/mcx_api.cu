@@ -2,6 +2,7 @@
 // objects, device contexts, array exchange in the reference's Fortran layout
 // and the phase entry points (opacity, transport, J normalisation).
 #include "../../include/mcx.h"
+#include "k_emission.cuh"
 #include "k_opacity.cuh"
 #include "k_transport_launch.h"
 #include "mcx_device.cuh"
@@ -169,6 +170,28 @@ extern "C" int mcx_setup_get(const mcx_setup* m, int32_t id, void* dst, size_t n
     case MCX_SARR_COMXSEC_H: return copyOut(s.comXSecH, dst, nbytes);
     case MCX_SARR_COMXSEC_C: return copyOut(s.comXSecC, dst, nbytes);
     case MCX_SARR_XSEC_RECOIL: return copyOut(s.xSecRecoil, dst, nbytes);
+    case MCX_SARR_EM_DIMS: {
+      const EmissionTables& em = s.em;
+      std::vector<int32_t> v(16, 0);
+      v[0] = em.nTk; v[1] = em.nlim[0]; v[2] = em.nlim[1]; v[3] = em.nlim[2];
+      v[4] = (int32_t)(em.fbHeavy.size() / 7); v[5] = em.nHydroFiles; v[6] = em.j2TsP;
+      for (int k = 0; k < 4; ++k) v[7 + k] = em.HeIILymanP[k];
+      return copyOut(v, dst, nbytes);
+    }
+    case MCX_SARR_EM_TK: return copyOut(s.em.tk, dst, nbytes);
+    case MCX_SARR_EM_EDGE_P: return copyOut(s.em.edgeP, dst, nbytes);
+    case MCX_SARR_EM_LOG_GAMMA: return copyOut(s.em.logGamma, dst, nbytes);
+    case MCX_SARR_EM_FB_HEAVY: return copyOut(s.em.fbHeavy, dst, nbytes);
+    case MCX_SARR_EM_HYDRO_MAP: return copyOut(s.em.hydroFileMap, dst, nbytes);
+    case MCX_SARR_EM_HYDRO_DENS: return copyOut(s.em.hydroDens, dst, nbytes);
+    case MCX_SARR_EM_HYDRO_LINES: return copyOut(s.em.hydroLines, dst, nbytes);
+    case MCX_SARR_EM_HYDRO_TEMPS: return copyOut(std::vector<float>(s.em.hydroLinesTemps, s.em.hydroLinesTemps + 12), dst, nbytes);
+    case MCX_SARR_EM_HB_COEFF: return copyOut(std::vector<float>(&s.em.HbCoeff[0][0][0], &s.em.HbCoeff[0][0][0] + 72), dst, nbytes);
+    case MCX_SARR_EM_RB_EDGE: return copyOut(std::vector<float>(&s.em.rbEdge[0][0][0], &s.em.rbEdge[0][0][0] + 156), dst, nbytes);
+    case MCX_SARR_EM_R2A_EDGE: return copyOut(std::vector<float>(&s.em.r2aEdge[0][0], &s.em.r2aEdge[0][0] + 54), dst, nbytes);
+    case MCX_SARR_EM_HEI_REC: return copyOut(std::vector<float>(&s.em.HeIrec[0][0][0], &s.em.HeIrec[0][0][0] + 408), dst, nbytes);
+    case MCX_SARR_EM_HEI_2PHOT: return copyOut(std::vector<float>(&s.em.HeI2phot[0][0], &s.em.HeI2phot[0][0] + 82), dst, nbytes);
+    case MCX_SARR_EM_HEII_LYMAN: return copyOut(std::vector<float>(&s.em.HeIILyman[0][0], &s.em.HeIILyman[0][0] + 8), dst, nbytes);
     default: g_setupError = "mcx_setup_get: unknown array id " + std::to_string(id); return MCX_ERR_INPUT;
   }
 }
@@ -194,6 +217,22 @@ extern "C" int mcx_setup_len(const mcx_setup* m, int32_t id, int64_t* count) {
     case MCX_SARR_ELEMENT_P: *count = 30 * 30 * 7 * 3; break;
     case MCX_SARR_N_SHELLS: *count = 30 * 30; break;
     case MCX_SARR_ION_EDGE: *count = (int64_t)s.ionEdge.size(); break;
+    case MCX_SARR_EM_DIMS: *count = 16; break;
+    case MCX_SARR_EM_TK: *count = (int64_t)s.em.tk.size(); break;
+    case MCX_SARR_EM_EDGE_P: *count = (int64_t)s.em.edgeP.size(); break;
+    case MCX_SARR_EM_LOG_GAMMA: *count = (int64_t)s.em.logGamma.size(); break;
+    case MCX_SARR_EM_FB_HEAVY: *count = (int64_t)s.em.fbHeavy.size(); break;
+    case MCX_SARR_EM_HYDRO_MAP: *count = (int64_t)s.em.hydroFileMap.size(); break;
+    case MCX_SARR_EM_HYDRO_DENS: *count = (int64_t)s.em.hydroDens.size(); break;
+    case MCX_SARR_EM_HYDRO_LINES: *count = (int64_t)s.em.hydroLines.size(); break;
+    case MCX_SARR_EM_HYDRO_TEMPS: *count = 12; break;
+    case MCX_SARR_EM_HB_COEFF: *count = 72; break;
+    case MCX_SARR_EM_RB_EDGE: *count = 156; break;
+    case MCX_SARR_EM_R2A_EDGE: *count = 54; break;
+    case MCX_SARR_EM_HEI_REC: *count = 408; break;
+    case MCX_SARR_EM_HEI_2PHOT: *count = 82; break;
+    case MCX_SARR_EM_HEII_LYMAN: *count = 8; break;
+
     default: g_setupError = "mcx_setup_len: unknown array id " + std::to_string(id); return MCX_ERR_INPUT;
   }
   return MCX_OK;
@@ -269,6 +308,7 @@ struct mcx_ctx {
   DBuf<float> gauntTe;
   DBuf<uint8_t> computeMask;
   DBuf<DevTransportCounters> counters;
+  std::unique_ptr<EmissionData> emission;
   bool haveOpacity = false, haveRecPDF = false, haveDustPDF = false;
 };
 
@@ -534,6 +574,11 @@ extern "C" int mcx_load(mcx_ctx* c, const mcx_setup* m) {
   CK(cudaMemset(c->escaped.p, 0, c->escaped.bytes()), "memset");
   if (c->hEst.p) CK(cudaMemset(c->hEst.p, 0, c->hEst.bytes()), "memset");
   if (c->scaOpac.p) CK(cudaMemset(c->scaOpac.p, 0, c->scaOpac.bytes()), "memset");
+  c->emission.reset();
+  if (c->lgGas) {
+    std::string em = emissionDataCreate(s, c->emission);
+    if (!em.empty()) return fail(c, MCX_ERR_INPUT, "mcx_load: " + em);
+  }
   CK(cudaDeviceSynchronize(), "mcx_load");
   c->haveOpacity = c->haveRecPDF = c->haveDustPDF = false;
   c->loaded = true;
@@ -622,6 +667,60 @@ extern "C" int mcx_device_ptr(mcx_ctx* c, int32_t id, void** dptr) {
 }
 
 // ------------------------------------------------------------ opacity phase
+// Skip rule of the opacity and emission loops (source/iteration_mod.f90:131-149,
+// :340-356): for nIterateMC > 1, cells whose Te and Ne moved by less than 0.5 %
+// keep last iteration's values.  Computed on the host from the device state.
+static int skipMask(mcx_ctx* c, int it, std::vector<float>& te, std::vector<uint8_t>& mask, int64_t& computed,
+                    int64_t& skipped) {
+  const size_t C1 = (size_t)c->nCells + 1;
+  std::vector<float> ne(C1), teOld(C1), neOld(C1);
+  te.assign(C1, 0.f);
+  mask.assign(C1, 0);
+  CK(cudaMemcpyAsync(te.data(), c->te.p, C1 * 4, cudaMemcpyDeviceToHost, c->stream), "d2h Te");
+  CK(cudaMemcpyAsync(ne.data(), c->ne.p, C1 * 4, cudaMemcpyDeviceToHost, c->stream), "d2h Ne");
+  CK(cudaMemcpyAsync(teOld.data(), c->teOld.p, C1 * 4, cudaMemcpyDeviceToHost, c->stream), "d2h TeOld");
+  CK(cudaMemcpyAsync(neOld.data(), c->neOld.p, C1 * 4, cudaMemcpyDeviceToHost, c->stream), "d2h NeOld");
+  CK(cudaStreamSynchronize(c->stream), "skip rule");
+  computed = skipped = 0;
+  for (size_t cell = 1; cell < C1; ++cell) {
+    bool skip = it > 1 && (std::fabs(te[cell] - teOld[cell]) / teOld[cell]) < 0.005f &&
+                (std::fabs(ne[cell] - neOld[cell]) / neOld[cell]) < 0.005f;
+    if (skip) ++skipped; else { mask[cell] = 1; ++computed; }
+  }
+  return MCX_OK;
+}
+
+extern "C" int mcx_emission(mcx_ctx* c, const mcx_phase_opts* opts, mcx_phase_stats* stats) {
+  if (!c) return MCX_ERR_INPUT;
+  if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_emission: no model loaded");
+  if (!c->lgGas || !c->emission) return fail(c, MCX_ERR_STATE, "mcx_emission: the grid holds no gas");
+  if (c->gauntTeOld <= 0.f) return fail(c, MCX_ERR_STATE, "mcx_emission: run mcx_opacity first (its Gaunt factors are reused)");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  const int it = opts ? opts->n_iterate_mc : 1;
+  std::vector<float> te;
+  std::vector<uint8_t> mask;
+  int64_t computed = 0, skipped = 0;
+  int rc = skipMask(c, it, te, mask, computed, skipped);
+  if (rc != MCX_OK) return rc;
+  const size_t C1 = (size_t)c->nCells + 1;
+  CK(cudaMemcpyAsync(c->computeMask.p, mask.data(), C1, cudaMemcpyHostToDevice, c->stream), "h2d mask");
+  CK(cudaEventRecord(c->ev0, c->stream), "event");
+  CK(launchEmissionGaunt(c->emission->dev, c->gauntTeOld, c->stream), "emission gaunt");
+  CK(launchEmission(c->emission->dev, c->te.p, c->ne.p, c->ionDen.p, c->computeMask.p, nullptr, c->recPDF.p,
+                    c->totalLines.p, c->stream), "emission kernel");
+  CK(transpose(c->recPDF.p, c->recCDFT.p, c->nbins, (int)C1, c->stream), "transpose recPDF");
+  CK(cudaEventRecord(c->ev1, c->stream), "event");
+  CK(cudaStreamSynchronize(c->stream), "mcx_emission");
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->cells_computed = computed;
+    stats->cells_skipped = skipped;
+    cudaEventElapsedTime(&stats->kernel_ms, c->ev0, c->ev1);
+  }
+  c->haveRecPDF = true;
+  return MCX_OK;
+}
+
 extern "C" int mcx_opacity(mcx_ctx* c, const mcx_phase_opts* opts, mcx_phase_stats* stats) {
   if (!c) return MCX_ERR_INPUT;
   if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_opacity: no model loaded");

@@ -335,31 +335,6 @@ float phFitHIon(float x, int n, float z) {
   return (float)(std::pow(10.0, v) / ((double)z * z));
 }
 
-// getOuterShell (source/hydro_mod.f90:89-180)
-void getOuterShell(int z, int nElec, int& outShell, int& g0, int& g1) {
-  static const int ss[30] = {1,1,2,2,3,3,3,3,3,3,4,4,5,5,5,5,5,5,6,6,6,6,6,6,6,6,6,6,7,7};
-  static const int gl[30] = {2,1,2,1,6,9,4,9,6,1,2,1,6,9,4,9,6,1,2,1,10,21,28,7,6,25,28,21,2,1};
-  static const int glhigh[12] = {10,21,28,25,6,25,28,21,10,1,2,1};   // indices 19..30
-  if (z > 30) fail("getOuterShell: atomic number out of range");
-  if (nElec < 1 || nElec > z) fail("getOuterShell: number of electrons out of range");
-  outShell = ss[nElec - 1];
-  if (z == nElec && z > 18) outShell = 7;
-  if (z == nElec + 1 && (z == 20 || z == 21 || z == 22 || z == 25 || z == 26)) outShell = 7;
-  g0 = gl[nElec - 1];
-  g1 = (nElec == 1) ? 1 : gl[nElec - 2];
-  if (z > 20 && nElec >= 19 && (z - nElec) >= 1) {
-    g0 = glhigh[nElec - 19];
-    g1 = (nElec == 19) ? gl[nElec - 2] : glhigh[nElec - 20];
-  }
-  if (z == nElec) {
-    if (z > 20 && nElec >= 21) g1 = glhigh[nElec - 20];
-    switch (z) { case 21: g1 = 15; break; case 22: g1 = 28; break; case 25: g1 = 7; break; case 26: g1 = 30; break; default: break; }
-  }
-  if (z - nElec == 1) {
-    switch (z) { case 21: g0 = 15; break; case 22: g0 = 28; break; case 25: g0 = 7; break; case 26: g0 = 30; break; default: break; }
-  }
-}
-
 // ------------------------------------------------------------ frequency mesh
 // fill (source/grid_mod.f90:610-648), single precision as in the reference.
 void fillSeg(float enlo, float enhi, float resolv, int& n0, std::vector<float>& nu, std::vector<float>& wid, int nbinsMax) {
@@ -889,6 +864,32 @@ void setStarPosition(Setup& s) {
 
 }  // namespace
 
+// getOuterShell (source/hydro_mod.f90:89-180)
+void getOuterShell(int z, int nElec, int& outShell, int& g0, int& g1) {
+  static const int ss[30] = {1,1,2,2,3,3,3,3,3,3,4,4,5,5,5,5,5,5,6,6,6,6,6,6,6,6,6,6,7,7};
+  static const int gl[30] = {2,1,2,1,6,9,4,9,6,1,2,1,6,9,4,9,6,1,2,1,10,21,28,7,6,25,28,21,2,1};
+  static const int glhigh[12] = {10,21,28,25,6,25,28,21,10,1,2,1};   // indices 19..30
+  if (z > 30) fail("getOuterShell: atomic number out of range");
+  if (nElec < 1 || nElec > z) fail("getOuterShell: number of electrons out of range");
+  outShell = ss[nElec - 1];
+  if (z == nElec && z > 18) outShell = 7;
+  if (z == nElec + 1 && (z == 20 || z == 21 || z == 22 || z == 25 || z == 26)) outShell = 7;
+  g0 = gl[nElec - 1];
+  g1 = (nElec == 1) ? 1 : gl[nElec - 2];
+  if (z > 20 && nElec >= 19 && (z - nElec) >= 1) {
+    g0 = glhigh[nElec - 19];
+    g1 = (nElec == 19) ? gl[nElec - 2] : glhigh[nElec - 20];
+  }
+  if (z == nElec) {
+    if (z > 20 && nElec >= 21) g1 = glhigh[nElec - 20];
+    switch (z) { case 21: g1 = 15; break; case 22: g1 = 28; break; case 25: g1 = 7; break; case 26: g1 = 30; break; default: break; }
+  }
+  if (z - nElec == 1) {
+    switch (z) { case 21: g0 = 15; break; case 22: g0 = 28; break; case 25: g0 = 7; break; case 26: g0 = 30; break; default: break; }
+  }
+}
+
+
 int locate(const float* xa, int n, float x) {
   if (x > xa[n - 1]) return n;
   if (x < xa[0]) return 0;
@@ -926,6 +927,7 @@ void buildSetup(Setup& s, const std::string& inputFile, const std::string& dataD
   buildMesh(s);
   if (s.p.lgGas) initXSecArray(s);
   else fail("initXSecArray: dust x sections are outside this build's scope");
+  if (s.p.lgGas) buildEmissionTables(s);
   setContinuum(s);
   fillGrid(s);
   setStarPosition(s);

@@ -46,8 +46,38 @@ struct Params {
   std::string baseDir;            // directory the deck's relative paths are resolved against
 };
 
+// Tables of the emission phase (source/emission_mod.f90:336-1919), read once.
+struct EmissionTables {
+  // continuum emission coefficients gamma(nu, T) at the series edges (initGammaCont,
+  // source/ph_mod.f90:31-200): [3] = HI, HeI, HeII
+  int nTk = 0;
+  int nlim[3] = {0, 0, 0};
+  std::vector<float> tk;                 // [nTk]
+  std::vector<int32_t> edgeP;            // [3][32] 1-based bins
+  std::vector<float> logGamma;           // [3][nTk][32]
+  // heavy-element free-bound terms (fb_ff, source/emission_mod.f90:550-614):
+  // {elem, ion, IPnuP, highNuP, xSecP, g0, g1}
+  std::vector<int32_t> fbHeavy;
+  // hydrogenic recombination lines (RecLinesEmission, source/emission_mod.f90:856-1151)
+  int nHydroFiles = 0;
+  std::vector<int32_t> hydroFileMap;     // [9][12] file index for (izp, itemp)
+  std::vector<int32_t> hydroNDens;       // [nFiles]
+  std::vector<float> hydroDens;          // [nFiles][13]
+  std::vector<float> hydroLines;         // [nFiles][13][14][8]  (iup 2..15, ilow 1..8)
+  float HbCoeff[2][9][4] = {};           // HbACoeff, HbBCoeff (data/gaussfitHb.dat)
+  float rbEdge[2][3][26] = {};           // data/r1bEdge.dat, data/r2bEdge.dat
+  float r2aEdge[3][18] = {};             // data/r2aEdge.dat
+  float hydroLinesTemps[12] = {};
+  float HeIrec[34][3][4] = {};           // HeIrecLineCoeff (coefficient 1 scaled by 1e25)
+  float HeI2phot[2][41] = {};            // y, Ay (data/HeI2phot.dat)
+  float HeIILyman[2][4] = {};            // ratio, nu (data/r2a0100old.dat)
+  int32_t HeIILymanP[4] = {};            // locate(nuArray, nu)
+  int32_t j2TsP = 0;                     // locate(nuArray, 1.45673)
+};
+
 struct Setup {
   Params p;
+  EmissionTables em;
   std::string dataDir;
   int meshMode = 0;
 
@@ -105,6 +135,12 @@ struct Setup {
     return active[(size_t)(i - 1) + (size_t)nx * ((size_t)(j - 1) + (size_t)ny * (size_t)(k - 1))];
   }
 };
+
+// Outer shell and ground statistical weights of (z, nElec) (getOuterShell, source/hydro_mod.f90:89-180).
+void getOuterShell(int z, int nElec, int& outShell, int& g0, int& g1);
+
+// Reads the emission-phase tables (after the mesh and cross sections exist).
+void buildEmissionTables(Setup& s);
 
 // Builds a Setup from an input deck; throws std::runtime_error with a message.
 void buildSetup(Setup& s, const std::string& inputFile, const std::string& dataDir, int meshMode);

@@ -52,8 +52,7 @@ class Setup:
     def nbins(self) -> int:
         return self.info.nbins
 
-    _DT = {abi.ARR_ACTIVE: np.int32, abi.SARR_POINTERS: np.int32, abi.SARR_ELEMENT_P: np.int32,
-           abi.SARR_N_SHELLS: np.int32, abi.SARR_ELEM_XREF: np.int32}
+    _DT = {abi.ARR_ACTIVE: np.int32, **{k: np.int32 for k in abi.INT_SARR}}
 
     def get(self, arr_id: int) -> np.ndarray:
         n = C.c_int64()
@@ -129,6 +128,12 @@ class Context:
         st = abi.PhaseStats()
         o = abi.PhaseOpts(n_iterate_mc=n_iterate_mc)
         self._check(lib().mcx_opacity(self._h, C.byref(o), C.byref(st)))
+        return st
+
+    def emission(self, n_iterate_mc: int = 1) -> abi.PhaseStats:
+        st = abi.PhaseStats()
+        o = abi.PhaseOpts(n_iterate_mc=n_iterate_mc)
+        self._check(lib().mcx_emission(self._h, C.byref(o), C.byref(st)))
         return st
 
     def transport(self, n_packets: int, seed: int = 0, counter_base: int = 0, precision: int = abi.PREC_FP32_GEOM,

@@ -10,6 +10,7 @@ pinned by analytic known-answer tests and the Philox4x32-10 published vectors.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import subprocess
 from pathlib import Path
 
@@ -64,6 +65,18 @@ class OpacityIn(C.Structure):
                 ("hden", _P), ("te", _P), ("ne", _P), ("ionden", _P), ("gaunt_te", _P), ("compute", _P)]
 
 
+class EmissionIn(C.Structure):
+    _fields_ = [("n_cells", C.c_int32), ("nbins", C.c_int32), ("nstages", C.c_int32), ("n_elem_used", C.c_int32),
+                ("n_xsec", C.c_int32), ("n_fb_heavy", C.c_int32), ("n_tk", C.c_int32), ("nlim", C.c_int32 * 3),
+                ("j2ts_p", C.c_int32), ("heii_lyman_p", C.c_int32 * 4),
+                ("nu", _P), ("widflx", _P), ("xsec", _P), ("ptr", _P), ("elem_abun", _P), ("elem_xref", _P),
+                ("tk", _P), ("gamma_edge_p", _P), ("log_gamma", _P), ("fb_heavy", _P), ("gaunt_ff", _P),
+                ("gaunt_ff_heii", _P), ("hei2phot", _P), ("heii_lyman", _P), ("hydro_file_map", _P),
+                ("hydro_dens", _P), ("hydro_lines", _P), ("hydro_temps", _P), ("hb_coeff", _P), ("rb_edge", _P),
+                ("r2a_edge", _P), ("hei_rec", _P), ("te", _P), ("ne", _P), ("ionden", _P), ("for_lines", _P),
+                ("compute", _P)]
+
+
 _lib = None
 
 
@@ -84,6 +97,8 @@ def lib() -> C.CDLL:
         l.orc_gaunt_ff.restype = None
         l.orc_gaunt_cache.argtypes = [C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, C.POINTER(C.c_float), _P]
         l.orc_gaunt_cache.restype = None
+        l.orc_emission.argtypes = [C.POINTER(EmissionIn), _P, _P]
+        l.orc_emission.restype = C.c_int
         _lib = l
     return _lib
 
@@ -189,3 +204,56 @@ def transport(setup, opacity_arr, rec_pdf, total_lines, ne=None, n: int = 1000, 
     if rc != 0:
         raise RuntimeError(f"orc_transport failed: {rc}")
     return j, e, st
+
+
+def emission(setup, gaunt_te: float, te=None, ne=None, ionden=None, compute=None, for_lines=None,
+             rec_pdf=None, total_lines=None):
+    """Oracle emission phase for a mocassin_xray_gb300.Setup: returns (recPDF [nbins][C+1], totalLines [C+1]).
+    `gaunt_te` is the temperature of the last Gaunt tabulation of the opacity phase."""
+    from mocassin_xray_gb300 import abi
+    i = setup.info
+    C1, nb = i.n_cells + 1, i.nbins
+    dims = setup.get(abi.SARR_EM_DIMS)
+    k = dict(
+        nu=setup.get(abi.ARR_NU), wid=setup.get(abi.ARR_WIDFLX), xsec=setup.get(abi.ARR_XSEC),
+        ptr=setup.get(abi.SARR_POINTERS), abun=setup.get(abi.ARR_ELEM_ABUN), xref=setup.get(abi.SARR_ELEM_XREF),
+        tk=setup.get(abi.SARR_EM_TK), edge=setup.get(abi.SARR_EM_EDGE_P), lg=setup.get(abi.SARR_EM_LOG_GAMMA),
+        fb=setup.get(abi.SARR_EM_FB_HEAVY), h2=setup.get(abi.SARR_EM_HEI_2PHOT),
+        ly=np.ascontiguousarray(setup.get(abi.SARR_EM_HEII_LYMAN)[:4]),
+        hmap=setup.get(abi.SARR_EM_HYDRO_MAP), hdens=setup.get(abi.SARR_EM_HYDRO_DENS),
+        hlines=setup.get(abi.SARR_EM_HYDRO_LINES), htemps=setup.get(abi.SARR_EM_HYDRO_TEMPS),
+        hb=setup.get(abi.SARR_EM_HB_COEFF), rb=setup.get(abi.SARR_EM_RB_EDGE), r2a=setup.get(abi.SARR_EM_R2A_EDGE),
+        heirec=setup.get(abi.SARR_EM_HEI_REC),
+        te=np.ascontiguousarray(te if te is not None else setup.get(abi.ARR_TE), dtype=np.float32),
+        ne=np.ascontiguousarray(ne if ne is not None else setup.get(abi.ARR_NE), dtype=np.float32),
+        ion=np.ascontiguousarray(ionden if ionden is not None else setup.get(abi.ARR_IONDEN), dtype=np.float32),
+    )
+    nu = k["nu"]
+    k["g1"] = gaunt_ff(0.0, math.log10(gaunt_te), nu).astype(np.float32)
+    k["g2"] = gaunt_ff(0.30103, math.log10(gaunt_te), nu).astype(np.float32)
+    fl = None if for_lines is None else np.ascontiguousarray(for_lines, dtype=np.float32)
+    if compute is None:
+        compute = np.ones(C1, dtype=np.uint8)
+        compute[0] = 0
+    compute = np.ascontiguousarray(compute, dtype=np.uint8)
+    if rec_pdf is None:
+        rec_pdf = np.zeros((nb, C1), dtype=np.float32)
+    if total_lines is None:
+        total_lines = np.zeros(C1, dtype=np.float32)
+    s = EmissionIn(n_cells=i.n_cells, nbins=nb, nstages=i.nstages, n_elem_used=max(i.n_elem_used, 1),
+                   n_xsec=k["xsec"].size, n_fb_heavy=int(dims[4]), n_tk=int(dims[0]), j2ts_p=int(dims[6]))
+    s.nlim[:] = [int(x) for x in dims[1:4]]
+    s.heii_lyman_p[:] = [int(x) for x in dims[7:11]]
+    for f, key in (("nu", "nu"), ("widflx", "wid"), ("xsec", "xsec"), ("ptr", "ptr"), ("elem_abun", "abun"),
+                   ("elem_xref", "xref"), ("tk", "tk"), ("gamma_edge_p", "edge"), ("log_gamma", "lg"),
+                   ("fb_heavy", "fb"), ("gaunt_ff", "g1"), ("gaunt_ff_heii", "g2"), ("hei2phot", "h2"),
+                   ("heii_lyman", "ly"), ("hydro_file_map", "hmap"), ("hydro_dens", "hdens"),
+                   ("hydro_lines", "hlines"), ("hydro_temps", "htemps"), ("hb_coeff", "hb"), ("rb_edge", "rb"),
+                   ("r2a_edge", "r2a"), ("hei_rec", "heirec"), ("te", "te"), ("ne", "ne"), ("ionden", "ion")):
+        setattr(s, f, _p(k[key]))
+    s.for_lines = _p(fl)
+    s.compute = _p(compute)
+    rc = lib().orc_emission(C.byref(s), _p(rec_pdf), _p(total_lines))
+    if rc != 0:
+        raise RuntimeError(f"orc_emission failed: {rc}")
+    return rec_pdf, total_lines

@@ -124,6 +124,46 @@ void orc_gaunt_ff(double z, double log10te, const float* nu, int32_t n, double* 
 void orc_gaunt_cache(int32_t nx, int32_t ny, int32_t nz, const int32_t* active, const float* te,
                      const uint8_t* compute, float* te_old, float* gaunt_te);
 
+/* ------------------------------------------------------------- emission */
+typedef struct orc_emission_in {
+    int32_t n_cells, nbins, nstages, n_elem_used, n_xsec, n_fb_heavy;
+    int32_t n_tk, nlim[3];
+    int32_t j2ts_p;             /* locate(nuArray, 1.45673) */
+    int32_t heii_lyman_p[4];
+    const float* nu;            /* [nbins] */
+    const float* widflx;        /* [nbins] */
+    const float* xsec;          /* [n_xsec] */
+    const int32_t* ptr;         /* [32] packed pointers (ORC_P_*) */
+    const float* elem_abun;     /* [30] */
+    const int32_t* elem_xref;   /* [30] */
+    const float* tk;            /* [n_tk] */
+    const int32_t* gamma_edge_p;/* [3][32] */
+    const float* log_gamma;     /* [3][n_tk][32] */
+    const int32_t* fb_heavy;    /* [n_fb_heavy][7] elem, ion, IPnuP, highNuP, xSecP, g0, g1 */
+    const float* gaunt_ff;      /* [nbins] gauntFF as last tabulated by the opacity phase */
+    const float* gaunt_ff_heii; /* [nbins] gauntFFHeII */
+    const float* hei2phot;      /* [2][41] y, Ay */
+    const float* heii_lyman;    /* [4] ratios */
+    const int32_t* hydro_file_map; /* [9][12] */
+    const float* hydro_dens;    /* [nFiles][13] */
+    const float* hydro_lines;   /* [nFiles][13][14][8] */
+    const float* hydro_temps;   /* [12] */
+    const float* hb_coeff;      /* [2][9][4] */
+    const float* rb_edge;       /* [2][3][26] */
+    const float* r2a_edge;      /* [3][18] */
+    const float* hei_rec;       /* [34][3][4] */
+    const float* te;            /* [C+1] */
+    const float* ne;            /* [C+1] */
+    const float* ionden;        /* [nstages][n_elem_used][C+1] */
+    const float* for_lines;     /* [C+1] forbidden-line total per cell, or NULL */
+    const uint8_t* compute;     /* [C+1] */
+} orc_emission_in;
+
+/* emissionDriver for gas without dust: writes recPDF[nu][c] and totalLines[c]
+ * for the cells with compute[c] = 1.  Returns 0, or 4 when the frequency mesh
+ * is too coarse between two gamma edges (the reference stops there). */
+int orc_emission(const orc_emission_in* in, float* rec_pdf, float* total_lines);
+
 #ifdef __cplusplus
 }
 #endif
