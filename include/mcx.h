@@ -76,6 +76,9 @@ enum mcx_array_id {
     MCX_ARR_NDUST,           /* float [nCells+1]                                   */
     MCX_ARR_LG_CONVERGED,    /* int32 [nCells+1]                                   */
     MCX_ARR_H_EST,           /* double[nbins][nCells+1] H(0:C,1:B) (radPress only) */
+    MCX_ARR_LG_BLACK,        /* int32 [nCells+1] lgBlack: no photon hit in the last balance */
+    MCX_ARR_N_ITER_T,        /* int32 [nCells+1] T-iterations of the last balance (0 = not updated) */
+    MCX_ARR_FOR_LINES,       /* float [nCells+1] forbidden-line total of the last emission phase */
     MCX_ARR_COUNT_
 };
 
@@ -107,6 +110,26 @@ enum mcx_array_id {
 #define MCX_SARR_EM_HEI_REC    1021  /* float[34][3][4]                                                 */
 #define MCX_SARR_EM_HEI_2PHOT  1022  /* float[2][41]                                                    */
 #define MCX_SARR_EM_HEII_LYMAN 1023  /* float[2][4] ratios, frequencies                                 */
+/* balance tables (source/hydro_mod.f90:13-53, :334-418, :676-764; source/update_mod.f90:3094-3305) */
+#define MCX_SARR_CION_CF       1024  /* float[30][30][5] CF(i,elem,nElec) at [elem-1][nElec-1][i-1]     */
+#define MCX_SARR_CION_THERM    1025  /* float[30][30] cionTherm(elem,ion)                               */
+#define MCX_SARR_NAUGER        1026  /* int32[30][30][10] nauger(elem,ion,shell)                        */
+#define MCX_SARR_AUGER         1027  /* float[30][30][10][10] auger(elem,ion,shell,nelec)               */
+#define MCX_SARR_RR_BADNELL    1028  /* float[6][30][31] RRbA,B,T0,T1,C,T2 at [k][z-1][n]              */
+#define MCX_SARR_DR_BADNELL_C  1029  /* float[30][31][9] DRbC(idr,z,n) at [z-1][n][idr-1]              */
+#define MCX_SARR_DR_BADNELL_E  1030  /* float[30][31][9] DRbE                                           */
+#define MCX_SARR_RADREC_RREC   1031  /* float[30][30][2] rrec(i,z,n) at [z-1][n-1][i-1]                 */
+#define MCX_SARR_RADREC_RNEW   1032  /* float[30][30][4] rnew(i,z,n)                                    */
+#define MCX_SARR_DIELEC        1033  /* float[nRows][8] dielectronic.dat: elem,n,a,b,c,d,f,g            */
+#define MCX_SARR_ALDRO         1034  /* float[nRows][6] aldrovandi.dat: elem,n,a,b,t0,t1                */
+#define MCX_SARR_OUTER_SHELL   1035  /* int32[30][30][3] getOuterShell(z,nElec): outShell,g0,g1        */
+#define MCX_SARR_ATOM_INDEX    1036  /* int32[30][31] multi-level atom slot of (elem,ion), -1 = no data */
+#define MCX_SARR_ATOM_HDR      1037  /* int32[nAtoms][16] packed atom headers (fields:
+                                        elem, ion, nLev, nTemp, iup2p, recType, nRec, offLogT, offQom,
+                                        offY2, offA, offG, offE, offRec, offAtp, 0)                     */
+#define MCX_SARR_ATOM_DATA     1038  /* double[n] packed atom data: log10 T[nTemp]; qom and its natural-
+                                        spline second derivatives [pair (l<u) row-major][nTemp];
+                                        a(j,i) at [j-1][i-1]; g; e [1/cm]; recombination fits; atp    */
 
 /* -------------------------------------------------------------- set-up */
 /* Host-side model built from an input deck.  Replaces readInput
@@ -218,6 +241,38 @@ int  mcx_opacity(mcx_ctx* ctx, const mcx_phase_opts* opts, mcx_phase_stats* stat
  * free-free Gaunt factors are those last tabulated by mcx_opacity, as in the
  * reference, so mcx_opacity must have run at least once. */
 int  mcx_emission(mcx_ctx* ctx, const mcx_phase_opts* opts, mcx_phase_stats* stats);
+
+/* ------------------------------------------------------- phase: balance */
+/* Per-cell thermal and ionisation balance from the normalised J (Jste after
+ * mcx_normalize_j): the T-iteration of updateCell / iterateT
+ * (source/update_mod.f90:15-482) with calcAlpha (:2298-2413, Badnell or the
+ * radRecFit/dielectronic fits), photoionisation / getPhotoRates
+ * (:3584-3832, :3971-4040), collisionalIonisation (:3552-3582), compton
+ * (:3834-3897), ionBalance (:1575-1992) and thermBalance (:887-1215) with
+ * forLines / equilibrium (:1221-1262; source/emission_mod.f90:2505-3106).
+ * Replaces the updateCell loop of iterateMC (source/iteration_mod.f90:1136-1156):
+ * TeOld/NeOld take Te/Ne first, then Te, Ne, ionDen, lgConverged and lgBlack
+ * are updated on the device.  Gas only; grains are outside this phase. */
+#define MCX_BAL_FP64  0         /* FP64 throughout (the plain path)                    */
+
+typedef struct mcx_balance_opts {
+    int32_t precision;          /* MCX_BAL_*                                            */
+    int32_t max_rounds;         /* T-iteration cap; 0 = 20 (maxIterateT)                */
+    int32_t reserved[6];
+} mcx_balance_opts;
+
+typedef struct mcx_balance_stats {
+    int64_t cells_updated;      /* cells with at least one photon hit                  */
+    int64_t no_hit;             /* grid%noHit                                          */
+    int64_t no_ion_bal;         /* grid%noIonBal: ionBalance reached 15 X-iterations   */
+    int64_t no_te_bal;          /* grid%noTeBal: iterateT reached 20 T-iterations      */
+    int64_t converged;          /* cells with lgConverged = 1                          */
+    int32_t max_iter_t;         /* most T-iterations any cell needed                    */
+    float   kernel_ms;          /* CUDA-event time of the phase                         */
+    int64_t reserved[4];
+} mcx_balance_stats;
+
+int  mcx_balance(mcx_ctx* ctx, const mcx_balance_opts* opts, mcx_balance_stats* stats);
 
 /* ------------------------------------------------------ phase: transport */
 /* Monte Carlo transport of n packets from source iStar, accumulating the

@@ -1,8 +1,8 @@
 """Builds libmcx.so (the CUDA hot path for sm_103a) in-tree.
 
 Every translation unit is compiled in parallel with one -gencode for
-sm_103a; the FP64 transport instantiation is compiled with --fmad=false so
-that its arithmetic rounds operation by operation.
+sm_103a; the FP64 transport and balance code is compiled with --fmad=false
+so that its arithmetic rounds operation by operation.
 """
 from __future__ import annotations
 
@@ -19,6 +19,9 @@ LIB = PKG / "libmcx.so"
 INCLUDE = PKG.parent / "include"
 
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# set-up tables are computed on the host: no FMA contraction, so that x86 and
+# Arm hosts round every operation the same way
+HOST_EXACT = ["-Xcompiler", "-ffp-contract=off"]
 
 
 def _nvcc() -> str:
@@ -39,13 +42,15 @@ def build_lib(verbose: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     common = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", str(INCLUDE), "-I", str(CSRC)]
     units = [
-        ("setup.cpp", ["-x", "cu"]),
-        ("setup_emission.cpp", ["-x", "cu"]),
+        ("setup.cpp", ["-x", "cu", *HOST_EXACT]),
+        ("setup_emission.cpp", ["-x", "cu", *HOST_EXACT]),
+        ("setup_balance.cpp", ["-x", "cu", *HOST_EXACT]),
         ("k_emission.cu", []),
         ("mcx_api.cu", []),
         ("k_opacity.cu", []),
         ("k_transport_f32.cu", []),
         ("k_transport_f64.cu", ["--fmad=false"]),
+        ("k_balance.cu", ["--fmad=false"]),
         ("mcx_noalloc.cu", []),
     ]
     cmds = []

@@ -21,17 +21,25 @@ ERRORS = {1: "MCX_ERR_INPUT", 2: "MCX_ERR_IO", 3: "MCX_ERR_CUDA", 4: "MCX_ERR_NO
 (ARR_NU, ARR_WIDFLX, ARR_XSEC, ARR_SRC_CDF, ARR_KN_SIGMA_T, ARR_KN_CDF, ARR_PCOMP, ARR_XAXIS, ARR_YAXIS,
  ARR_ZAXIS, ARR_ACTIVE, ARR_HDEN, ARR_TE, ARR_NE, ARR_TEOLD, ARR_NEOLD, ARR_IONDEN, ARR_OPACITY, ARR_RECPDF,
  ARR_TOTAL_LINES, ARR_JSTE, ARR_ESCAPED, ARR_VOLUME, ARR_ELEM_ABUN, ARR_GAUNT_TE, ARR_SCAOPAC, ARR_DUSTPDF,
- ARR_NDUST, ARR_LG_CONVERGED, ARR_H_EST) = range(1, 31)
+ ARR_NDUST, ARR_LG_CONVERGED, ARR_H_EST, ARR_LG_BLACK, ARR_N_ITER_T, ARR_FOR_LINES) = range(1, 34)
 SARR_POINTERS, SARR_ELEMENT_P, SARR_N_SHELLS, SARR_ELEM_XREF, SARR_ION_EDGE, SARR_COMXSEC_H, \
     SARR_COMXSEC_C, SARR_XSEC_RECOIL = range(1001, 1009)
 (SARR_EM_DIMS, SARR_EM_TK, SARR_EM_EDGE_P, SARR_EM_LOG_GAMMA, SARR_EM_FB_HEAVY, SARR_EM_HYDRO_MAP,
  SARR_EM_HYDRO_DENS, SARR_EM_HYDRO_LINES, SARR_EM_HYDRO_TEMPS, SARR_EM_HB_COEFF, SARR_EM_RB_EDGE,
  SARR_EM_R2A_EDGE, SARR_EM_HEI_REC, SARR_EM_HEI_2PHOT, SARR_EM_HEII_LYMAN) = range(1009, 1024)
+(SARR_CION_CF, SARR_CION_THERM, SARR_NAUGER, SARR_AUGER, SARR_RR_BADNELL, SARR_DR_BADNELL_C,
+ SARR_DR_BADNELL_E, SARR_RADREC_RREC, SARR_RADREC_RNEW, SARR_DIELEC, SARR_ALDRO, SARR_OUTER_SHELL,
+ SARR_ATOM_INDEX, SARR_ATOM_HDR, SARR_ATOM_DATA) = range(1024, 1039)
 INT_SARR = {SARR_POINTERS, SARR_ELEMENT_P, SARR_N_SHELLS, SARR_ELEM_XREF, SARR_EM_DIMS, SARR_EM_EDGE_P,
-            SARR_EM_FB_HEAVY, SARR_EM_HYDRO_MAP}
+            SARR_EM_FB_HEAVY, SARR_EM_HYDRO_MAP, SARR_NAUGER, SARR_OUTER_SHELL, SARR_ATOM_INDEX, SARR_ATOM_HDR}
+F64_SARR = {SARR_ATOM_DATA}
+# packed atom header fields (MCX_SARR_ATOM_HDR)
+(AT_ELEM, AT_ION, AT_NLEV, AT_NTEMP, AT_IUP2P, AT_RECTYPE, AT_NREC, AT_OFF_LOGT, AT_OFF_QOM, AT_OFF_Y2,
+ AT_OFF_A, AT_OFF_G, AT_OFF_E, AT_OFF_REC, AT_OFF_ATP) = range(15)
 
 MESH_REFERENCE, MESH_LOG_EDGES = 0, 1
 PREC_FP32_GEOM, PREC_FP64 = 0, 1
+BAL_FP64 = 0
 
 
 class SetupOpts(C.Structure):
@@ -47,6 +55,16 @@ class SetupInfo(C.Structure):
                 ("n_sizes", C.c_int32), ("star_pos", C.c_float * 3), ("r_out", C.c_float), ("r_in", C.c_float),
                 ("l_star", C.c_float), ("l_phot", C.c_float), ("ion_edge1", C.c_float), ("te_start", C.c_float),
                 ("min_convergence", C.c_float), ("xhi_limit", C.c_float), ("reserved", C.c_int32 * 8)]
+
+
+class BalanceOpts(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("max_rounds", C.c_int32), ("reserved", C.c_int32 * 6)]
+
+
+class BalanceStats(C.Structure):
+    _fields_ = [("cells_updated", C.c_int64), ("no_hit", C.c_int64), ("no_ion_bal", C.c_int64),
+                ("no_te_bal", C.c_int64), ("converged", C.c_int64), ("max_iter_t", C.c_int32),
+                ("kernel_ms", C.c_float), ("reserved", C.c_int64 * 4)]
 
 
 class PhaseOpts(C.Structure):
@@ -113,6 +131,7 @@ SIGNATURES = [
     ("mcx_emission", C.c_int, [_P, C.POINTER(PhaseOpts), C.POINTER(PhaseStats)]),
     ("mcx_transport", C.c_int, [_P, C.POINTER(TransportOpts), C.POINTER(TransportStats)]),
     ("mcx_normalize_j", C.c_int, [_P]),
+    ("mcx_balance", C.c_int, [_P, C.POINTER(BalanceOpts), C.POINTER(BalanceStats)]),
     ("mcx_timer_start", C.c_int, [_P]),
     ("mcx_timer_stop", C.c_int, [_P, C.POINTER(C.c_float)]),
     ("mcx_version", C.c_char_p, []),

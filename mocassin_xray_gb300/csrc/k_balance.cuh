@@ -1,0 +1,125 @@
+// k_balance.cuh - per-cell balance phase on the device: the T-iteration of
+// updateCell/iterateT (source/update_mod.f90:15-482) for every cell at once.
+//
+// The reference recurses per cell (iterateT calls itself up to maxIterateT =
+// 20 times, ionBalance up to 15 times).  Here every cell advances one
+// T-iteration per round, and a round is three launches over the cells still
+// iterating:
+//   rates   (thread per cell)         calcAlpha, photoionisation, collisional
+//                                     ionisation, compton, ionBalance, and the
+//                                     thermBalance terms that need no atom solve
+//   atoms   (thread per cell and ion) forLines: equilibrium of every ion with
+//                                     data, summed to that ion's line cooling
+//   secant  (thread per cell)         heating - cooling, the bracketing secant
+//                                     step, convergence and the cell's results
+// A J-only pass before the first round integrates the photoionisation rates
+// and Compton sums, which the reference recomputes on every T-iteration from
+// the same J.  All arithmetic is FP64.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+
+namespace mcx {
+
+struct Setup;
+
+// One photoionised shell (elem, ion, shell) of an element that is on.
+struct PhotoShell {
+  int32_t elem, ion, shell;   // Z, stage, shell (1-based)
+  int32_t ipNuP, highNuP;     // IPnuP, highNuP (1-based bins)
+  int32_t xsecP;              // xSecArray pointer (1-based) of the shell (H/He: of the level)
+  int32_t heavy;              // 1: getPhotoRates (elem > 2), 0: the H/He direct sum
+  float yield1;               // auger(elem, ion, shell, 1)
+};
+
+struct BalanceCounters {
+  unsigned long long noHit, noIonBal, noTeBal, converged, updated, maxIterT;
+};
+
+// Device view (by value as a kernel parameter; pointers are device memory).
+struct BalanceDev {
+  int32_t nbins, nCells, nstages, nElemUsed, nShellsTot, nAtoms, nDiel, nAldro;
+  int32_t lgBadnell, lgCompton;
+  int32_t secIonP, cRecoilHP, cRecoilHeP;
+  float xhiLimit;
+  int32_t xref[31];            // elementXref by Z (index 1..30), 0 = off
+  int32_t zOf[31];             // Z of used element e (1-based)
+  float abun[31];              // elemAbun by Z
+  int32_t pairShell0[31 * 32]; // [e-1][ion-1] first PhotoShell of (element e, ion), -1 none
+  int32_t pairNShell[31 * 32];
+  const float* nu;             // [nbins]
+  const float* xsec;
+  const float* xsecRecoil;     // [nbins]
+  const PhotoShell* shells;    // [nShellsTot]
+  const float* CF;             // [30][30][5]
+  const float* cionTherm;      // [30][30]
+  const int32_t* nauger;       // [30][30][10]
+  const float* auger;          // [30][30][10][10]
+  const float* RRb;            // [6][30][31]
+  const float* DRbC;           // [30][31][9]
+  const float* DRbE;
+  const float* rrec;           // [30][30][2]
+  const float* rnew;           // [30][30][4]
+  const float* diel;           // [nDiel][8]
+  const float* aldro;          // [nAldro][6]
+  const int32_t* outer;        // [30][30][3]
+  const int32_t* atomHdr;      // [nAtoms][16]
+  const double* atomData;
+  // per-cell work, [k][C+1] (cell fastest)
+  double* ion;                 // [nstages][nElemUsed]
+  double* alpha;               // [nElemUsed][nstages]
+  double* coll1;               // [nElemUsed][nstages]
+  double* coll2;
+  double* gam;                 // [nShellsTot] photoionisation rate (J integral, + charge exchange)
+  double* heatA;               // [nShellsTot] heating without the secondary-ionisation tail
+  double* heatHi;              // [nShellsTot] tail heating, times heatef
+  double* pi1;                 // [nShellsTot] photoIon(1, ...)
+  double* pi2;                 // [nShellsTot] photoIon(2, ...)
+  double* comp;                // [4] s1, s2, recoil H, recoil He
+  double* te, *ne, *xOld;
+  double* tHigh, *tLow, *resHigh, *resLow;
+  double* heat;                // photoionisation heating
+  double* coolA;               // coolFF + coolRec
+  double* coolHex;             // H collisional excitation
+  double* coolCollH;           // collisional ionisation cooling
+  double* compHeat, *compRecoil, *compCool;   // Compton terms (times Ne where the reference multiplies)
+  double* forSum;              // [nAtoms] forbidden-line cooling of each ion
+  int32_t* nIterT;
+  int8_t* state;               // 0 iterating, 1 done, 2 no photon hit
+  int8_t* ibConv;
+  BalanceCounters* counters;
+};
+
+class BalanceData {
+ public:
+  ~BalanceData();
+  BalanceDev dev{};
+  void* blocks[64] = {};
+  int nBlocks = 0;
+};
+
+// Builds the device tables and the per-cell work arrays of a set-up.
+std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out);
+
+// Grid arrays the balance reads and writes (device memory).
+struct BalanceGrid {
+  const double* jste;          // [nbins][C+1], normalised
+  const float* hden;           // [C+1]
+  float* te, *ne, *ionDen;     // [C+1], [C+1], [nstages][nElemUsed][C+1]
+  int32_t* converged, *black, *nIterT;   // [C+1]
+};
+
+// updateCell for every cell: up to maxRounds T-iterations (the reference's
+// maxIterateT = 20).  Asynchronous on the stream; counters are left in
+// BalanceDev::counters.
+cudaError_t launchBalance(BalanceData& b, const BalanceGrid& g, int maxRounds, cudaStream_t s);
+
+// The forLines line total of every cell (the emission phase's normFor,
+// rec = .true., units of 1e-25 erg/s per gas density) from the grid state.
+cudaError_t launchForLinesEmission(BalanceData& b, const float* te, const float* ne, const float* ionDen,
+                                   const uint8_t* compute, float* forLines, cudaStream_t s);
+
+}  // namespace mcx

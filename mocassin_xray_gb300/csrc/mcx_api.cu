@@ -3,6 +3,7 @@
 // and the phase entry points (opacity, transport, J normalisation).
 #include "../../include/mcx.h"
 #include "k_emission.cuh"
+#include "k_balance.cuh"
 #include "k_opacity.cuh"
 #include "k_transport_launch.h"
 #include "mcx_device.cuh"
@@ -29,6 +30,14 @@ struct mcx_setup {
 namespace {
 thread_local std::string g_setupError;
 
+int copyRaw(const void* src, size_t size, void* dst, size_t nbytes) {
+  if (nbytes != size) {
+    g_setupError = "mcx_setup_get: size mismatch (expected " + std::to_string(size) + " bytes)";
+    return MCX_ERR_INPUT;
+  }
+  std::memcpy(dst, src, nbytes);
+  return MCX_OK;
+}
 template <typename T>
 int copyOut(const std::vector<T>& v, void* dst, size_t nbytes) {
   if (nbytes != v.size() * sizeof(T)) {
@@ -192,6 +201,21 @@ extern "C" int mcx_setup_get(const mcx_setup* m, int32_t id, void* dst, size_t n
     case MCX_SARR_EM_HEI_REC: return copyOut(std::vector<float>(&s.em.HeIrec[0][0][0], &s.em.HeIrec[0][0][0] + 408), dst, nbytes);
     case MCX_SARR_EM_HEI_2PHOT: return copyOut(std::vector<float>(&s.em.HeI2phot[0][0], &s.em.HeI2phot[0][0] + 82), dst, nbytes);
     case MCX_SARR_EM_HEII_LYMAN: return copyOut(std::vector<float>(&s.em.HeIILyman[0][0], &s.em.HeIILyman[0][0] + 8), dst, nbytes);
+    case MCX_SARR_CION_CF: return copyRaw(&s.bal.CF[0][0][0], sizeof(s.bal.CF), dst, nbytes);
+    case MCX_SARR_CION_THERM: return copyRaw(&s.bal.cionTherm[0][0], sizeof(s.bal.cionTherm), dst, nbytes);
+    case MCX_SARR_NAUGER: return copyRaw(&s.bal.nauger[0][0][0], sizeof(s.bal.nauger), dst, nbytes);
+    case MCX_SARR_AUGER: return copyRaw(&s.bal.auger[0][0][0][0], sizeof(s.bal.auger), dst, nbytes);
+    case MCX_SARR_RR_BADNELL: return copyRaw(&s.bal.RRb[0][0][0], sizeof(s.bal.RRb), dst, nbytes);
+    case MCX_SARR_DR_BADNELL_C: return copyRaw(&s.bal.DRbC[0][0][0], sizeof(s.bal.DRbC), dst, nbytes);
+    case MCX_SARR_DR_BADNELL_E: return copyRaw(&s.bal.DRbE[0][0][0], sizeof(s.bal.DRbE), dst, nbytes);
+    case MCX_SARR_RADREC_RREC: return copyRaw(&s.bal.rrec[0][0][0], sizeof(s.bal.rrec), dst, nbytes);
+    case MCX_SARR_RADREC_RNEW: return copyRaw(&s.bal.rnew[0][0][0], sizeof(s.bal.rnew), dst, nbytes);
+    case MCX_SARR_DIELEC: return copyOut(s.bal.diel, dst, nbytes);
+    case MCX_SARR_ALDRO: return copyOut(s.bal.aldro, dst, nbytes);
+    case MCX_SARR_OUTER_SHELL: return copyRaw(&s.bal.outer[0][0][0], sizeof(s.bal.outer), dst, nbytes);
+    case MCX_SARR_ATOM_INDEX: return copyRaw(&s.bal.atomIndex[0][0], sizeof(s.bal.atomIndex), dst, nbytes);
+    case MCX_SARR_ATOM_HDR: return copyOut(s.bal.atomHdr, dst, nbytes);
+    case MCX_SARR_ATOM_DATA: return copyOut(s.bal.atomData, dst, nbytes);
     default: g_setupError = "mcx_setup_get: unknown array id " + std::to_string(id); return MCX_ERR_INPUT;
   }
 }
@@ -232,6 +256,20 @@ extern "C" int mcx_setup_len(const mcx_setup* m, int32_t id, int64_t* count) {
     case MCX_SARR_EM_HEI_REC: *count = 408; break;
     case MCX_SARR_EM_HEI_2PHOT: *count = 82; break;
     case MCX_SARR_EM_HEII_LYMAN: *count = 8; break;
+    case MCX_SARR_CION_CF: *count = 30 * 30 * 5; break;
+    case MCX_SARR_CION_THERM: *count = 30 * 30; break;
+    case MCX_SARR_NAUGER: *count = 30 * 30 * 10; break;
+    case MCX_SARR_AUGER: *count = 30 * 30 * 10 * 10; break;
+    case MCX_SARR_RR_BADNELL: *count = 6 * 30 * 31; break;
+    case MCX_SARR_DR_BADNELL_C: case MCX_SARR_DR_BADNELL_E: *count = 30 * 31 * 9; break;
+    case MCX_SARR_RADREC_RREC: *count = 30 * 30 * 2; break;
+    case MCX_SARR_RADREC_RNEW: *count = 30 * 30 * 4; break;
+    case MCX_SARR_DIELEC: *count = (int64_t)s.bal.diel.size(); break;
+    case MCX_SARR_ALDRO: *count = (int64_t)s.bal.aldro.size(); break;
+    case MCX_SARR_OUTER_SHELL: *count = 30 * 30 * 3; break;
+    case MCX_SARR_ATOM_INDEX: *count = 30 * 31; break;
+    case MCX_SARR_ATOM_HDR: *count = (int64_t)s.bal.atomHdr.size(); break;
+    case MCX_SARR_ATOM_DATA: *count = (int64_t)s.bal.atomData.size(); break;
 
     default: g_setupError = "mcx_setup_len: unknown array id " + std::to_string(id); return MCX_ERR_INPUT;
   }
@@ -309,6 +347,9 @@ struct mcx_ctx {
   DBuf<uint8_t> computeMask;
   DBuf<DevTransportCounters> counters;
   std::unique_ptr<EmissionData> emission;
+  std::unique_ptr<BalanceData> balance;
+  DBuf<int32_t> lgConverged, lgBlack, nIterT;
+  DBuf<float> forLines;
   bool haveOpacity = false, haveRecPDF = false, haveDustPDF = false;
 };
 
@@ -574,10 +615,21 @@ extern "C" int mcx_load(mcx_ctx* c, const mcx_setup* m) {
   CK(cudaMemset(c->escaped.p, 0, c->escaped.bytes()), "memset");
   if (c->hEst.p) CK(cudaMemset(c->hEst.p, 0, c->hEst.bytes()), "memset");
   if (c->scaOpac.p) CK(cudaMemset(c->scaOpac.p, 0, c->scaOpac.bytes()), "memset");
+  CK(c->lgConverged.alloc(C1), "alloc lgConverged");
+  CK(c->lgBlack.alloc(C1), "alloc lgBlack");
+  CK(c->nIterT.alloc(C1), "alloc nIterT");
+  CK(c->forLines.alloc(C1), "alloc forLines");
+  CK(cudaMemset(c->lgConverged.p, 0, c->lgConverged.bytes()), "memset");
+  CK(cudaMemset(c->lgBlack.p, 0, c->lgBlack.bytes()), "memset");
+  CK(cudaMemset(c->nIterT.p, 0, c->nIterT.bytes()), "memset");
+  CK(cudaMemset(c->forLines.p, 0, c->forLines.bytes()), "memset");
   c->emission.reset();
+  c->balance.reset();
   if (c->lgGas) {
     std::string em = emissionDataCreate(s, c->emission);
     if (!em.empty()) return fail(c, MCX_ERR_INPUT, "mcx_load: " + em);
+    std::string bl = balanceDataCreate(s, c->balance);
+    if (!bl.empty()) return fail(c, MCX_ERR_INPUT, "mcx_load: " + bl);
   }
   CK(cudaDeviceSynchronize(), "mcx_load");
   c->haveOpacity = c->haveRecPDF = c->haveDustPDF = false;
@@ -619,6 +671,10 @@ ArrView viewOf(mcx_ctx* c, int id) {
     case MCX_ARR_DUSTPDF: return {c->dustPDF.p, c->dustPDF.bytes()};
     case MCX_ARR_NDUST: return {c->ndust.p, c->ndust.bytes()};
     case MCX_ARR_H_EST: return {c->hEst.p, c->hEst.bytes()};
+    case MCX_ARR_LG_CONVERGED: return {c->lgConverged.p, c->lgConverged.bytes()};
+    case MCX_ARR_LG_BLACK: return {c->lgBlack.p, c->lgBlack.bytes()};
+    case MCX_ARR_N_ITER_T: return {c->nIterT.p, c->nIterT.bytes()};
+    case MCX_ARR_FOR_LINES: return {c->forLines.p, c->forLines.bytes()};
     default: return {nullptr, 0};
   }
 }
@@ -706,7 +762,13 @@ extern "C" int mcx_emission(mcx_ctx* c, const mcx_phase_opts* opts, mcx_phase_st
   CK(cudaMemcpyAsync(c->computeMask.p, mask.data(), C1, cudaMemcpyHostToDevice, c->stream), "h2d mask");
   CK(cudaEventRecord(c->ev0, c->stream), "event");
   CK(launchEmissionGaunt(c->emission->dev, c->gauntTeOld, c->stream), "emission gaunt");
-  CK(launchEmission(c->emission->dev, c->te.p, c->ne.p, c->ionDen.p, c->computeMask.p, nullptr, c->recPDF.p,
+  const float* forLines = nullptr;
+  if (c->balance && c->balance->dev.nAtoms > 0) {
+    CK(launchForLinesEmission(*c->balance, c->te.p, c->ne.p, c->ionDen.p, c->computeMask.p, c->forLines.p, c->stream),
+       "emission forLines");
+    forLines = c->forLines.p;
+  }
+  CK(launchEmission(c->emission->dev, c->te.p, c->ne.p, c->ionDen.p, c->computeMask.p, forLines, c->recPDF.p,
                     c->totalLines.p, c->stream), "emission kernel");
   CK(transpose(c->recPDF.p, c->recCDFT.p, c->nbins, (int)C1, c->stream), "transpose recPDF");
   CK(cudaEventRecord(c->ev1, c->stream), "event");
@@ -867,6 +929,38 @@ extern "C" int mcx_normalize_j(mcx_ctx* c) {
     CK(cudaGetLastError(), "scale escaped");
   }
   CK(cudaStreamSynchronize(c->stream), "mcx_normalize_j");
+  return MCX_OK;
+}
+
+extern "C" int mcx_balance(mcx_ctx* c, const mcx_balance_opts* opts, mcx_balance_stats* stats) {
+  if (!c) return MCX_ERR_INPUT;
+  if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_balance: no model loaded");
+  if (!c->lgGas || !c->balance) return fail(c, MCX_ERR_STATE, "mcx_balance: the grid holds no gas");
+  if (opts && opts->precision != MCX_BAL_FP64) return fail(c, MCX_ERR_INPUT, "mcx_balance: unknown precision");
+  const int rounds = (opts && opts->max_rounds > 0) ? opts->max_rounds : 20;
+  if (rounds > 20) return fail(c, MCX_ERR_INPUT, "mcx_balance: max_rounds above maxIterateT (20)");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  const size_t C1 = (size_t)c->nCells + 1;
+  CK(cudaEventRecord(c->ev0, c->stream), "event");
+  // iterateMC saves the state the skip rule compares against (source/iteration_mod.f90:1136-1139)
+  CK(cudaMemcpyAsync(c->teOld.p, c->te.p, C1 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream), "TeOld");
+  CK(cudaMemcpyAsync(c->neOld.p, c->ne.p, C1 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream), "NeOld");
+  BalanceGrid g{c->jste.p, c->hden.p, c->te.p, c->ne.p, c->ionDen.p, c->lgConverged.p, c->lgBlack.p, c->nIterT.p};
+  CK(launchBalance(*c->balance, g, rounds, c->stream), "balance kernels");
+  CK(cudaEventRecord(c->ev1, c->stream), "event");
+  BalanceCounters h{};
+  CK(cudaMemcpyAsync(&h, c->balance->dev.counters, sizeof(h), cudaMemcpyDeviceToHost, c->stream), "d2h counters");
+  CK(cudaStreamSynchronize(c->stream), "mcx_balance");
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->cells_updated = (int64_t)h.updated;
+    stats->no_hit = (int64_t)h.noHit;
+    stats->no_ion_bal = (int64_t)h.noIonBal;
+    stats->no_te_bal = (int64_t)h.noTeBal;
+    stats->converged = (int64_t)h.converged;
+    stats->max_iter_t = (int32_t)h.maxIterT;
+    cudaEventElapsedTime(&stats->kernel_ms, c->ev0, c->ev1);
+  }
   return MCX_OK;
 }
 

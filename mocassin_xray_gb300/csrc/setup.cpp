@@ -926,8 +926,11 @@ void buildSetup(Setup& s, const std::string& inputFile, const std::string& dataD
   if (s.p.lgGas) computeIonEdges(s);
   buildMesh(s);
   if (s.p.lgGas) initXSecArray(s);
-  else fail("initXSecArray: dust x sections are outside this build's scope");
-  if (s.p.lgGas) buildEmissionTables(s);
+  else fail("initXSecArray: dust x sections are outside this library's scope");
+  if (s.p.lgGas) {
+    buildEmissionTables(s);
+    buildBalanceTables(s);
+  }
   setContinuum(s);
   fillGrid(s);
   setStarPosition(s);

@@ -11,6 +11,7 @@
 // record, takes as many values as it needs across records, and drops the rest
 // of its last record.
 #include "setup_internal.h"
+#include "list_reader.h"
 
 #include <cmath>
 #include <cstdlib>
@@ -23,67 +24,6 @@ namespace mcx {
 namespace {
 
 [[noreturn]] void efail(const std::string& msg) { throw std::runtime_error(msg); }
-
-class ListReader {
- public:
-  explicit ListReader(const std::string& path) : path_(path) {
-    std::ifstream in(path);
-    if (!in) efail("can't open data file " + path);
-    std::string l;
-    while (std::getline(in, l)) lines_.push_back(l);
-  }
-  bool eof() const { return pos_ >= lines_.size(); }
-  // One READ of n numbers (list-directed); returns false at end of file.
-  bool read(int n, std::vector<double>& out) {
-    out.clear();
-    while ((int)out.size() < n) {
-      if (pos_ >= lines_.size()) return false;
-      tokens(lines_[pos_++], out, n);
-    }
-    return true;
-  }
-  std::vector<double> need(int n) {
-    std::vector<double> v;
-    if (!read(n, v)) efail("data file truncated: " + path_);
-    return v;
-  }
-  // One READ of a (possibly quoted) string.
-  std::string readString() {
-    while (pos_ < lines_.size()) {
-      const std::string& l = lines_[pos_++];
-      size_t i = l.find_first_not_of(" \t");
-      if (i == std::string::npos) continue;
-      if (l[i] == '\'' || l[i] == '"') {
-        size_t j = l.find(l[i], i + 1);
-        return l.substr(i + 1, j == std::string::npos ? std::string::npos : j - i - 1);
-      }
-      size_t j = l.find_first_of(" \t,", i);
-      return l.substr(i, j == std::string::npos ? std::string::npos : j - i);
-    }
-    efail("data file truncated: " + path_);
-  }
-
- private:
-  static void tokens(const std::string& l, std::vector<double>& out, int n) {
-    size_t i = 0;
-    while (i < l.size() && (int)out.size() < n) {
-      while (i < l.size() && (l[i] == ' ' || l[i] == '\t' || l[i] == ',' || l[i] == '\r')) ++i;
-      if (i >= l.size() || l[i] == '!' || l[i] == '/') break;
-      size_t j = i;
-      while (j < l.size() && !(l[j] == ' ' || l[j] == '\t' || l[j] == ',' || l[j] == '\r')) ++j;
-      std::string t = l.substr(i, j - i);
-      for (auto& c : t) if (c == 'd' || c == 'D') c = 'e';
-      char* end = nullptr;
-      double v = std::strtod(t.c_str(), &end);
-      if (end == t.c_str()) break;   // non-numeric token ends the useful part of the record
-      out.push_back(v);
-      i = j;
-    }
-  }
-  std::string path_;
-  std::vector<std::string> lines_;
-  size_t pos_ = 0;
-};
 
 std::string baseName(const std::string& f) {
   size_t s = f.find_last_of('/');

@@ -75,9 +75,44 @@ struct EmissionTables {
   int32_t j2TsP = 0;                     // locate(nuArray, 1.45673)
 };
 
+// Packed multi-level atom of one ion (the data equilibrium reads from its ion
+// file, source/emission_mod.f90:2589-2880), header fields per atom:
+enum AtomHdr {
+  kAtElem = 0, kAtIon, kAtNLev, kAtNTemp, kAtIup2p, kAtRecType, kAtNRec, kAtOffLogT,
+  kAtOffQom, kAtOffY2, kAtOffA, kAtOffG, kAtOffE, kAtOffRec, kAtOffAtp, kAtHdrSize = 16
+};
+// recombination-coefficient fits at the end of an ion file
+enum AtomRec { kRecNone = 0, kRecPowerLaw = 1, kRecChianti = 2 };
+constexpr int kRecWidth[3] = {0, 11, 5};   // br,z,a_r(4),a_d(5) | jj,a,b,c,d
+constexpr int kMaxLevels = 30;             // nForLevels (source/constants_mod.f90)
+
+// Tables of the per-cell balance (updateCell and the routines it calls,
+// source/update_mod.f90), read once at set-up.
+struct BalanceTables {
+  float CF[kNElements][kNElements][5] = {};        // cion.dat CF(i,elem,nElec) at [elem-1][nElec-1][i-1]
+  float cionTherm[kNElements][kNElements] = {};    // [elem-1][ion-1]
+  int32_t nauger[kNElements][kNElements][10] = {}; // auger.dat [elem-1][ion-1][shell-1]
+  float auger[kNElements][kNElements][10][10] = {};// [elem-1][ion-1][shell-1][nelec-1]
+  float RRb[6][kNElements][kNElements + 1] = {};   // rrBadnell A,B,T0,T1,C,T2 at [k][z-1][n]
+  float DRbC[kNElements][kNElements + 1][9] = {};  // drBadnell at [z-1][n][idr-1]
+  float DRbE[kNElements][kNElements + 1][9] = {};
+  float rrec[kNElements][kNElements][2] = {};      // radrec.dat at [z-1][n-1][i-1]
+  float rnew[kNElements][kNElements][4] = {};
+  std::vector<float> diel;                         // dielectronic.dat rows: elem,n,a,b,c,d,f,g
+  std::vector<float> aldro;                        // aldrovandi.dat rows: elem,n,a,b,t0,t1
+  int32_t outer[kNElements][kNElements][3] = {};   // getOuterShell(z, nElec): outShell, g0, g1
+  // multi-level atoms of the ions with data (lgDataAvailable)
+  int32_t atomIndex[kNElements][kNElements + 1];   // [elem-1][ion-1] -> atom slot, -1 none
+  std::vector<int32_t> atomHdr;                    // [nAtoms][kAtHdrSize]
+  std::vector<double> atomData;
+  int nAtoms = 0;
+  int maxLev = 0;
+};
+
 struct Setup {
   Params p;
   EmissionTables em;
+  BalanceTables bal;
   std::string dataDir;
   int meshMode = 0;
 
@@ -141,6 +176,9 @@ void getOuterShell(int z, int nElec, int& outShell, int& g0, int& g1);
 
 // Reads the emission-phase tables (after the mesh and cross sections exist).
 void buildEmissionTables(Setup& s);
+
+// Reads the rate tables and the multi-level atoms of the balance phase.
+void buildBalanceTables(Setup& s);
 
 // Builds a Setup from an input deck; throws std::runtime_error with a message.
 void buildSetup(Setup& s, const std::string& inputFile, const std::string& dataDir, int meshMode);

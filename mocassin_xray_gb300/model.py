@@ -52,7 +52,7 @@ class Setup:
     def nbins(self) -> int:
         return self.info.nbins
 
-    _DT = {abi.ARR_ACTIVE: np.int32, **{k: np.int32 for k in abi.INT_SARR}}
+    _DT = {abi.ARR_ACTIVE: np.int32, **{k: np.int32 for k in abi.INT_SARR}, **{k: np.float64 for k in abi.F64_SARR}}
 
     def get(self, arr_id: int) -> np.ndarray:
         n = C.c_int64()
@@ -108,7 +108,8 @@ class Context:
             abi.ARR_ESCAPED: ((nb + 1, C1), f64), abi.ARR_TOTAL_LINES: ((C1,), f32), abi.ARR_HDEN: ((C1,), f32),
             abi.ARR_TE: ((C1,), f32), abi.ARR_NE: ((C1,), f32), abi.ARR_TEOLD: ((C1,), f32),
             abi.ARR_NEOLD: ((C1,), f32), abi.ARR_VOLUME: ((C1,), f32), abi.ARR_GAUNT_TE: ((C1,), f32),
-            abi.ARR_NDUST: ((C1,), f32),
+            abi.ARR_NDUST: ((C1,), f32), abi.ARR_LG_CONVERGED: ((C1,), np.int32),
+            abi.ARR_LG_BLACK: ((C1,), np.int32), abi.ARR_N_ITER_T: ((C1,), np.int32), abi.ARR_FOR_LINES: ((C1,), f32),
             abi.ARR_IONDEN: ((s.nstages, max(s.n_elem_used, 1), C1), f32),
         }
         return shapes[arr_id]
@@ -143,6 +144,13 @@ class Context:
                               block_size=block_size, grid_mult=grid_mult)
         st = abi.TransportStats()
         self._check(lib().mcx_transport(self._h, C.byref(o), C.byref(st)))
+        return st
+
+    def balance(self, max_rounds: int = 0, precision: int = abi.BAL_FP64) -> abi.BalanceStats:
+        """updateCell for every cell (Te, Ne, ionDen, lgConverged) from the normalised J."""
+        o = abi.BalanceOpts(precision=precision, max_rounds=max_rounds)
+        st = abi.BalanceStats()
+        self._check(lib().mcx_balance(self._h, C.byref(o), C.byref(st)))
         return st
 
     def normalize_j(self) -> None:

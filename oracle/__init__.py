@@ -257,3 +257,116 @@ def emission(setup, gaunt_te: float, te=None, ne=None, ionden=None, compute=None
     if rc != 0:
         raise RuntimeError(f"orc_emission failed: {rc}")
     return rec_pdf, total_lines
+
+
+class BalanceIn(C.Structure):
+    _fields_ = [("n_cells", C.c_int32), ("nbins", C.c_int32), ("nstages", C.c_int32), ("n_elem_used", C.c_int32),
+                ("n_xsec", C.c_int32), ("lg_badnell", C.c_int32), ("lg_compton", C.c_int32), ("n_diel", C.c_int32),
+                ("n_aldro", C.c_int32), ("n_atoms", C.c_int32), ("xhi_limit", C.c_float),
+                ("nu", _P), ("xsec", _P), ("ptr", _P), ("xsec_recoil", _P), ("elem_abun", _P), ("elem_xref", _P),
+                ("n_shells", _P), ("element_p", _P), ("cf", _P), ("cion_therm", _P), ("nauger", _P), ("auger", _P),
+                ("rr_badnell", _P), ("dr_c", _P), ("dr_e", _P), ("rrec", _P), ("rnew", _P), ("diel", _P),
+                ("aldro", _P), ("outer", _P), ("atom_index", _P), ("atom_hdr", _P), ("atom_data", _P),
+                ("jste", _P), ("hden", _P)]
+
+
+class BalanceState(C.Structure):
+    _fields_ = [("te", _P), ("ne", _P), ("ionden", _P), ("converged", _P), ("black", _P), ("n_iter_t", _P)]
+
+
+class BalanceStats(C.Structure):
+    _fields_ = [("no_hit", C.c_double), ("no_ion_bal", C.c_double), ("no_te_bal", C.c_double),
+                ("converged", C.c_int64)]
+
+
+def _balance_lib():
+    l = lib()
+    if not getattr(l, "_balance_ready", False):
+        l.orc_balance.argtypes = [C.POINTER(BalanceIn), C.POINTER(BalanceState), C.c_int32, C.POINTER(BalanceStats)]
+        l.orc_balance.restype = C.c_int
+        l.orc_equilibrium.argtypes = [C.POINTER(BalanceIn), C.c_int32, C.c_double, C.c_double, C.c_double, C.c_int32,
+                                      _P, _P]
+        l.orc_equilibrium.restype = C.c_int
+        l.orc_for_lines_emission.argtypes = [C.POINTER(BalanceIn), _P, _P, _P, _P]
+        l.orc_for_lines_emission.restype = C.c_int
+        l._balance_ready = True
+    return l
+
+
+class BalanceTables:
+    """The set-up tables the balance oracle reads, taken from a Setup once."""
+
+    def __init__(self, setup, lg_badnell: bool = True):
+        from mocassin_xray_gb300 import abi
+        i = setup.info
+        g = setup.get
+        self.k = dict(
+            nu=g(abi.ARR_NU), xsec=g(abi.ARR_XSEC), ptr=g(abi.SARR_POINTERS), rec=g(abi.SARR_XSEC_RECOIL),
+            abun=g(abi.ARR_ELEM_ABUN), xref=g(abi.SARR_ELEM_XREF), nsh=g(abi.SARR_N_SHELLS),
+            ep=g(abi.SARR_ELEMENT_P), cf=g(abi.SARR_CION_CF), ct=g(abi.SARR_CION_THERM), na=g(abi.SARR_NAUGER),
+            au=g(abi.SARR_AUGER), rr=g(abi.SARR_RR_BADNELL), drc=g(abi.SARR_DR_BADNELL_C),
+            dre=g(abi.SARR_DR_BADNELL_E), rrec=g(abi.SARR_RADREC_RREC), rnew=g(abi.SARR_RADREC_RNEW),
+            diel=g(abi.SARR_DIELEC), aldro=g(abi.SARR_ALDRO), outer=g(abi.SARR_OUTER_SHELL),
+            aidx=g(abi.SARR_ATOM_INDEX), ahdr=g(abi.SARR_ATOM_HDR), adata=g(abi.SARR_ATOM_DATA),
+            hden=g(abi.ARR_HDEN))
+        k = self.k
+        self.info = i
+        self.s = BalanceIn(n_cells=i.n_cells, nbins=i.nbins, nstages=i.nstages, n_elem_used=max(i.n_elem_used, 1),
+                           n_xsec=k["xsec"].size, lg_badnell=1 if lg_badnell else 0, lg_compton=i.lg_compton,
+                           n_diel=k["diel"].size // 8, n_aldro=k["aldro"].size // 6, n_atoms=k["ahdr"].size // 16,
+                           xhi_limit=i.xhi_limit)
+        for f, key in (("nu", "nu"), ("xsec", "xsec"), ("ptr", "ptr"), ("xsec_recoil", "rec"), ("elem_abun", "abun"),
+                       ("elem_xref", "xref"), ("n_shells", "nsh"), ("element_p", "ep"), ("cf", "cf"),
+                       ("cion_therm", "ct"), ("nauger", "na"), ("auger", "au"), ("rr_badnell", "rr"),
+                       ("dr_c", "drc"), ("dr_e", "dre"), ("rrec", "rrec"), ("rnew", "rnew"), ("diel", "diel"),
+                       ("aldro", "aldro"), ("outer", "outer"), ("atom_index", "aidx"), ("atom_hdr", "ahdr"),
+                       ("atom_data", "adata"), ("hden", "hden")):
+            setattr(self.s, f, _p(k[key]))
+
+    def atom(self, elem: int, ion: int) -> int:
+        return int(self.k["aidx"].reshape(30, 31)[elem - 1, ion - 1])
+
+    def nlev(self, atom: int) -> int:
+        return int(self.k["ahdr"].reshape(-1, 16)[atom, 2])
+
+
+def equilibrium(tables: BalanceTables, atom: int, te: float, ne: float, ion_den_up: float = 0.0, rec: bool = False):
+    """Level populations and line emissivities [lower][upper] of one ion (equilibrium)."""
+    nlev = tables.nlev(atom)
+    n = np.zeros(nlev, dtype=np.float64)
+    em = np.zeros((nlev, nlev), dtype=np.float64)
+    _balance_lib().orc_equilibrium(C.byref(tables.s), atom, te, ne, ion_den_up, 1 if rec else 0, _p(n), _p(em))
+    return n, em
+
+
+def balance(tables: BalanceTables, jste, te, ne, ionden, nthreads: int = 1):
+    """updateCell for every cell: returns (te, ne, ionden, converged, black, n_iter_t, stats)."""
+    i = tables.info
+    C1 = i.n_cells + 1
+    jste = np.ascontiguousarray(jste, dtype=np.float64)
+    te = np.array(te, dtype=np.float32, copy=True)
+    ne = np.array(ne, dtype=np.float32, copy=True)
+    ionden = np.array(ionden, dtype=np.float32, copy=True).reshape(-1)
+    conv = np.zeros(C1, dtype=np.int32)
+    black = np.zeros(C1, dtype=np.int32)
+    nit = np.zeros(C1, dtype=np.int32)
+    tables.s.jste = _p(jste)
+    st = BalanceState(te=_p(te), ne=_p(ne), ionden=_p(ionden), converged=_p(conv), black=_p(black),
+                      n_iter_t=_p(nit))
+    stats = BalanceStats()
+    rc = _balance_lib().orc_balance(C.byref(tables.s), C.byref(st), nthreads, C.byref(stats))
+    tables.s.jste = None
+    if rc != 0:
+        raise RuntimeError(f"orc_balance failed: {rc}")
+    return te, ne, ionden, conv, black, nit, stats
+
+
+def for_lines_emission(tables: BalanceTables, te, ne, ionden) -> np.ndarray:
+    """normFor of each cell: the emission phase's forbidden-line total [1e-25 erg/s per gas density]."""
+    C1 = tables.info.n_cells + 1
+    te = np.ascontiguousarray(te, dtype=np.float32)
+    ne = np.ascontiguousarray(ne, dtype=np.float32)
+    ionden = np.ascontiguousarray(ionden, dtype=np.float32).reshape(-1)
+    out = np.zeros(C1, dtype=np.float64)
+    _balance_lib().orc_for_lines_emission(C.byref(tables.s), _p(te), _p(ne), _p(ionden), _p(out))
+    return out

@@ -164,6 +164,77 @@ typedef struct orc_emission_in {
  * is too coarse between two gamma edges (the reference stops there). */
 int orc_emission(const orc_emission_in* in, float* rec_pdf, float* total_lines);
 
+/* -------------------------------------------------------------- balance */
+/* Packed multi-level atom header fields (mcx_setup_get(MCX_SARR_ATOM_HDR)). */
+enum {
+    ORC_AT_ELEM = 0, ORC_AT_ION, ORC_AT_NLEV, ORC_AT_NTEMP, ORC_AT_IUP2P, ORC_AT_RECTYPE, ORC_AT_NREC,
+    ORC_AT_OFF_LOGT, ORC_AT_OFF_QOM, ORC_AT_OFF_Y2, ORC_AT_OFF_A, ORC_AT_OFF_G, ORC_AT_OFF_E,
+    ORC_AT_OFF_REC, ORC_AT_OFF_ATP, ORC_AT_HDR = 16
+};
+
+typedef struct orc_balance_in {
+    int32_t n_cells, nbins, nstages, n_elem_used, n_xsec;
+    int32_t lg_badnell, lg_compton, n_diel, n_aldro, n_atoms;
+    float xhi_limit;
+    const float* nu;            /* [nbins] */
+    const float* xsec;          /* [n_xsec] xSecArray */
+    const int32_t* ptr;         /* [32] packed pointers */
+    const float* xsec_recoil;   /* [nbins] */
+    const float* elem_abun;     /* [30] */
+    const int32_t* elem_xref;   /* [30] */
+    const int32_t* n_shells;    /* [30][30] */
+    const int32_t* element_p;   /* [30][30][7][3] */
+    const float* cf;            /* [30][30][5] cion.dat CF(i,elem,nElec) */
+    const float* cion_therm;    /* [30][30] */
+    const int32_t* nauger;      /* [30][30][10] */
+    const float* auger;         /* [30][30][10][10] */
+    const float* rr_badnell;    /* [6][30][31] */
+    const float* dr_c;          /* [30][31][9] */
+    const float* dr_e;          /* [30][31][9] */
+    const float* rrec;          /* [30][30][2] */
+    const float* rnew;          /* [30][30][4] */
+    const float* diel;          /* [n_diel][8] */
+    const float* aldro;         /* [n_aldro][6] */
+    const int32_t* outer;       /* [30][30][3] outShell, g0, g1 of (z, nElec) */
+    const int32_t* atom_index;  /* [30][31] */
+    const int32_t* atom_hdr;    /* [n_atoms][16] */
+    const double* atom_data;
+    const double* jste;         /* [nbins][C+1] */
+    const float* hden;          /* [C+1] */
+} orc_balance_in;
+
+typedef struct orc_balance_state {
+    float* te;                  /* [C+1] in/out */
+    float* ne;                  /* [C+1] in/out */
+    float* ionden;              /* [nstages][n_elem_used][C+1] in/out */
+    int32_t* converged;         /* [C+1] out: lgConverged */
+    int32_t* black;             /* [C+1] out: lgBlack (no photon hit) */
+    int32_t* n_iter_t;          /* [C+1] out: T-iterations used (0 = not updated) */
+} orc_balance_state;
+
+typedef struct orc_balance_stats {
+    double no_hit, no_ion_bal, no_te_bal;
+    int64_t converged;
+} orc_balance_stats;
+
+/* updateCell (source/update_mod.f90:15-482) for every active cell: the
+ * T-iteration (iterateT) around calcAlpha, photoionisation, collisional
+ * ionisation, Compton, ionBalance and thermBalance (forLines/equilibrium).
+ * Gas only (no grains).  Returns 0. */
+int orc_balance(const orc_balance_in* in, orc_balance_state* st, int32_t nthreads, orc_balance_stats* stats);
+
+/* equilibrium (source/emission_mod.f90:2505-3007) for atom slot `atom`:
+ * level populations n[nLev] and line emissivities em[i][j] (lower i, upper j,
+ * [nLev][nLev], zero where a(j,i) = 0).  rec selects the recombination term. */
+int orc_equilibrium(const orc_balance_in* in, int32_t atom, double te, double ne, double ion_den_up,
+                    int32_t rec, double* n, double* em);
+
+/* The emission phase's forbidden-line total normFor of each cell
+ * (forLines with rec = .true., source/emission_mod.f90:1481-1524 and
+ * :1780-1795), in its units of 1e-25 erg/s per unit gas density. */
+int orc_for_lines_emission(const orc_balance_in* in, const float* te, const float* ne, const float* ionden,
+                           double* for_lines);
+
 #ifdef __cplusplus
 }
 #endif

@@ -17,7 +17,17 @@ FILES = [
     "HeI2phot.dat",     # HeI two-photon rates
     "hydroLinesFiles.dat", "gaussfitHb.dat", "r1bEdge.dat", "r2bEdge.dat", "r2aEdge.dat",
     "HeIrecLines.dat", "r2a0100old.dat",
+    # balance phase
+    "cion.dat",         # Voronov (1997) collisional ionisation fits and Shull & van Steenberg heating
+    "auger.dat",        # Auger electron yields
+    "rrBadnell.dat", "drBadnell.dat",    # Badnell radiative / dielectronic recombination fits
+    "radrec.dat",       # Verner & Ferland radiative recombination fits
+    "dielectronic.dat", "aldrovandi.dat",  # dielectronic recombination fits
+    "fileNames.dat",    # the multi-level ion file of each (element, stage)
 ]
+
+# elements whose multi-level ion files the committed decks read (C, N, O, Ne, Mg, Si, S, Fe)
+ION_FILE_ELEMENTS = (6, 7, 8, 10, 12, 14, 16, 26)
 
 
 def listed_hydro_files(src_dir: Path) -> list[str]:
@@ -29,11 +39,25 @@ def listed_hydro_files(src_dir: Path) -> list[str]:
             names.append(n)
     return names
 
+def listed_ion_files(src_dir: Path) -> list[str]:
+    """The ion files fileNames.dat names for ION_FILE_ELEMENTS that exist (makeElements's
+    order: elements 3..30, stages 1..min(elem+1, 31), one (A20) record each)."""
+    records = (src_dir / "fileNames.dat").read_text().split("\n")
+    names, k = [], 0
+    for elem in range(3, 31):
+        for _ion in range(1, min(elem + 1, 31) + 1):
+            n = records[k][:20].strip().split("/")[-1]
+            k += 1
+            if elem in ION_FILE_ELEMENTS and n and (src_dir / n).exists() and n not in names:
+                names.append(n)
+    return names
+
+
 def main(src: str) -> None:
     src_dir = Path(src)
     dst = Path(__file__).resolve().parent / "atomic_data"
     dst.mkdir(exist_ok=True)
-    for f in FILES + listed_hydro_files(src_dir):
+    for f in FILES + listed_hydro_files(src_dir) + listed_ion_files(src_dir):
         shutil.copyfile(src_dir / f, dst / f)
         print("copied", f)
 

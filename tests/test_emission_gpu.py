@@ -41,7 +41,8 @@ def test_emission_matches_oracle(decks, data_dir, oracle_lib, name, perturb):
     tl = ctx.get(abi.ARR_TOTAL_LINES)
     compute = np.ones(s.n_cells + 1, np.uint8); compute[0] = 0
     _, te_last = oracle_lib.gaunt_cache(s.info.nx, s.info.ny, s.info.nz, s.get(abi.ARR_ACTIVE), te, compute, -1.0)
-    rec_o, tl_o = oracle_lib.emission(s, te_last, te=te, ne=ne, ionden=np.asarray(ion).reshape(-1))
+    fl = oracle_lib.for_lines_emission(oracle_lib.BalanceTables(s), te, ne, np.asarray(ion).reshape(-1))
+    rec_o, tl_o = oracle_lib.emission(s, te_last, te=te, ne=ne, ionden=np.asarray(ion).reshape(-1), for_lines=fl)
     assert np.all(np.diff(rec[:, 1:], axis=0) >= 0.0)
     assert np.all(rec[-1, 1:] == 1.0)
     np.testing.assert_allclose(rec[:, 1:], rec_o[:, 1:], rtol=0, atol=3e-5)
