@@ -5,11 +5,15 @@
 Workload: the lognormal multi-element nebula (41^3 full grid, H He C N O Ne S,
 n_H = 10^(2+0.5g) with g a seeded Gaussian random field of correlation length
 4 cells, 45 kK blackbody with Q(H) = 2e49 s^-1, 600-bin 1e-4..500 Ryd mesh,
-1e7 packets per iteration).  One step is one pass of the hot path as built:
-per-cell opacity for every cell, Monte Carlo transport of 1e7 stellar packets
-(with their re-emissions) and the J normalisation.  The headline metric is MC
-packets/s; `e2e` is the same through the C ABI with the per-cell state
-uploaded from pinned host memory and Jste read back every step.
+1e7 packets per iteration).  One step is one Monte Carlo iteration of
+iterateMC from the deck's initial state: the opacity and the emission phase
+of every cell, the transport of 1e7 stellar packets with their re-emissions,
+the J normalisation and the balance of every cell (T-iteration, ionisation
+ladder, multi-level atoms).  The production path runs FP32 packet geometry
+with FP64 estimators and the mixed-precision balance; the plain FP64 path is
+timed beside it.  The headline metric is MC packets/s over the whole
+iteration; `e2e` is the same through the C ABI with the per-cell state
+uploaded from pinned host memory and the updated state read back every step.
 
 Under torchrun (N > 1) every rank runs its own replica of the step on its own
 GPU (packets shard with no data-path collective); value = all packets / the
@@ -35,6 +39,10 @@ sys.path.insert(0, str(ROOT))
 DATA_DIR = ROOT / "tests" / "golden" / "atomic_data"
 METRIC = "MC packets/s"
 UNIT = "packets/s"
+# kernels of one step: opacity 1; emission 5 (Gaunt table, forbidden lines per
+# ion and their sum, emissivity, CDF transpose); transport 1; J normalisation
+# 1; balance 63 (J integrals, state load, 20 rounds x (rates, atoms, secant), store)
+KERNELS_PER_STEP = 1 + 5 + 1 + 1 + 63
 
 
 def parse():
@@ -47,6 +55,8 @@ def parse():
     ap.add_argument("--grid", type=int, default=41)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=0, help="packets of the CPU sample (0 = auto)")
+    ap.add_argument("--cpu-cells", type=int, default=0, help="cells of the CPU emission/balance sample (0 = auto)")
+    ap.add_argument("--plain-steps", type=int, default=2, help="steps of the plain FP64 path timed beside")
     return ap.parse_args()
 
 
@@ -83,14 +93,6 @@ def make_deck(grid: int, packets: int) -> Path:
     if not p.exists():
         configs.lognormal_gas(d, n=grid, packets=packets)
     return p
-
-
-def synthetic_rec_cdf(nu: np.ndarray, n_cells: int) -> np.ndarray:
-    """Re-emission CDF used until the emission phase is part of the step."""
-    w = np.where(nu >= 1.0, nu ** 3 * np.exp(-(nu - 1.0) / 0.3), 1e-3 * nu ** 0.5)
-    cdf = np.cumsum(w) / w.sum()
-    cdf[-1] = 1.0
-    return np.repeat(cdf[:, None].astype(np.float32), n_cells + 1, axis=1)
 
 
 class ClockSampler:
@@ -171,24 +173,58 @@ def cpu_threads() -> int:
         return os.cpu_count() or 1
 
 
-def cpu_step(setup, packets_full: int, sample: int, threads: int) -> dict:
-    """One step of the oracle (the reference restated on the host cores): the
-    opacity of every cell, then the transport of `sample` packets; the
-    transport part is linear in packets and is scaled to `packets_full`."""
+def cpu_step(setup, packets_full: int, sample: int, cells: int, threads: int) -> dict:
+    """One iteration of the oracle (the reference restated in C) on the host
+    cores, on a bounded sample: the opacity of every cell; the emission
+    phase and the balance of `cells` evenly spaced cells; the transport of
+    `sample` packets.  Each sampled part is scaled linearly to the full
+    workload (cells, packets)."""
     import oracle
     from mocassin_xray_gb300 import abi
+    C1 = setup.n_cells + 1
+    te, ne, ion = setup.get(abi.ARR_TE), setup.get(abi.ARR_NE), setup.get(abi.ARR_IONDEN)
+    every = max(1, setup.n_cells // max(cells, 1))
+    pick = np.zeros(C1, np.uint8)
+    pick[1::every] = 1
+    n_pick = int(pick.sum())
+    tables = oracle.BalanceTables(setup)
     t0 = time.perf_counter()
-    op = oracle.opacity(setup)
+    comp = np.ones(C1, np.uint8)
+    comp[0] = 0
+    gte, te_last = oracle.gaunt_cache(setup.info.nx, setup.info.ny, setup.info.nz, setup.get(abi.ARR_ACTIVE), te,
+                                      comp, -1.0)
+    op = oracle.opacity(setup, te=te, ne=ne, ionden=ion, gaunt_te=gte)
     t1 = time.perf_counter()
-    rec = synthetic_rec_cdf(setup.get(abi.ARR_NU), setup.n_cells)
-    tl = np.full(setup.n_cells + 1, 0.3, np.float32)
+    fl = oracle.for_lines_emission(tables, te, ne, ion, compute=pick)
+    rec, tl = oracle.emission(setup, te_last, te=te, ne=ne, ionden=ion, for_lines=fl, compute=pick)
     t2 = time.perf_counter()
-    _, _, st = oracle.transport(setup, op, rec, tl, n=sample, seed=1, nthreads=threads,
-                                n_photons_norm=packets_full)
+    # the transport sample runs on the oracle's own tables for the sampled
+    # cells and a recombination-like CDF elsewhere
+    nu = setup.get(abi.ARR_NU)
+    w = np.where(nu >= 1.0, nu ** 3 * np.exp(-(nu - 1.0) / 0.3), 1e-3 * nu ** 0.5)
+    cdf = (np.cumsum(w) / w.sum()).astype(np.float32)
+    cdf[-1] = 1.0
+    rec[:, pick == 0] = cdf[:, None]
+    tl[pick == 0] = np.median(tl[pick == 1])
     t3 = time.perf_counter()
-    t_step = (t1 - t0) + (t3 - t2) * packets_full / sample
-    return {"t_opacity": t1 - t0, "t_transport_sample": t3 - t2, "t_step_extrapolated": t_step,
-            "value": packets_full / t_step, "crossings": st.crossings}
+    j, _, st = oracle.transport(setup, op, rec, tl, ne=ne, n=sample, seed=1, nthreads=threads,
+                                n_photons_norm=packets_full)
+    t4 = time.perf_counter()
+    j *= 1e-9
+    j[:, pick == 0] = 0.0          # unsampled cells are skipped by the balance (no photon hit)
+    oracle.balance(tables, j, te, ne, ion, nthreads=threads)
+    t5 = time.perf_counter()
+    scale_cells = setup.n_cells / n_pick
+    t_step = (t1 - t0) + (t2 - t1) * scale_cells + (t4 - t3) * packets_full / sample + (t5 - t4) * scale_cells
+    return {"t_opacity": t1 - t0, "t_emission_sample": t2 - t1, "t_transport_sample": t4 - t3,
+            "t_balance_sample": t5 - t4, "t_step_extrapolated": t_step, "value": packets_full / t_step,
+            "cells_sampled": n_pick, "crossings": st.crossings}
+
+
+def cpu_sample_text(setup, r: dict, sample: int, packets: int, threads: int) -> str:
+    return (f"per step: opacity of all {setup.n_cells} cells; emission + balance of {r['cells_sampled']} evenly "
+            f"spaced cells scaled to {setup.n_cells}; transport of {sample} packets scaled to {packets}; "
+            f"{threads} threads (reference Fortran not compilable: no Fortran compiler)")
 
 
 def run_reference(args, dist, ws, rank):
@@ -201,9 +237,10 @@ def run_reference(args, dist, ws, rank):
     setup = Setup(deck, DATA_DIR, mesh_mode=abi.MESH_LOG_EDGES)
     threads = cpu_threads()
     sample = args.cpu_sample or 200_000
+    cells = args.cpu_cells or 2000
     res = []
     for i in range(args.warmup + args.steps):
-        r = cpu_step(setup, args.packets, sample, threads)
+        r = cpu_step(setup, args.packets, sample, cells, threads)
         if i >= args.warmup:
             res.append(r)
     t = float(np.mean([r["t_step_extrapolated"] for r in res]))
@@ -214,24 +251,25 @@ def run_reference(args, dist, ws, rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config_dict(args, setup),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"per step: opacity of all {setup.n_cells} cells + transport of {sample} "
-                                   f"packets on {threads} threads, transport time scaled linearly to "
-                                   f"{args.packets} packets (reference Fortran not compilable: no Fortran compiler)"},
+                         "sample": cpu_sample_text(setup, res[-1], sample, args.packets, threads)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cells_balanced_per_s": setup.n_cells / (float(np.mean([r["t_balance_sample"] for r in res]))
+                                                 * setup.n_cells / res[-1]["cells_sampled"]),
     }
     print(json.dumps(line))
 
 
 def config_dict(args, setup) -> dict:
-    return {"workload": "lognormal multi-element nebula, 41^3 full grid, 600-bin mesh, 1e7 packets/step"
+    return {"workload": "lognormal multi-element nebula, 41^3 full grid, 600-bin mesh, 1e7 packets/iteration"
             if args.grid == 41 and args.packets == 10_000_000 else
-            f"lognormal multi-element nebula, {args.grid}^3 grid, {setup.nbins}-bin mesh, {args.packets} packets/step",
+            f"lognormal multi-element nebula, {args.grid}^3 grid, {setup.nbins}-bin mesh, {args.packets} packets/iteration",
+            "step": "one MC iteration from the initial state: opacity, emission, transport, J normalisation, balance",
             "grid": f"{args.grid}^3", "n_cells": setup.n_cells, "nbins": setup.nbins,
             "packets_per_step": args.packets, "elements": "H,He,C,N,O,Ne,S",
             "geometry_precision": "fp32", "estimator_precision": "fp64",
-            "l2": "inputs larger than L2 (Jste fp64 and opacity exceed 129 MB)",
-            "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU",
-            "reemission_cdf": "synthetic (emission phase not yet in the step)"}
+            "balance_precision": "fp32 rates, fp64 level populations / ladder / bracketing",
+            "l2": "inputs larger than L2 (Jste fp64 331 MB, opacity 165 MB)",
+            "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU"}
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -243,20 +281,24 @@ def run_gpu(args, dist, ws, rank, local):
     setup = Setup(deck, DATA_DIR, mesh_mode=abi.MESH_LOG_EDGES)
     ctx = Context(local)
     ctx.load(setup)
+    ctx.state_save()
     C1, nb = setup.n_cells + 1, setup.nbins
-    ctx.put(abi.ARR_RECPDF, synthetic_rec_cdf(setup.get(abi.ARR_NU), setup.n_cells))
-    ctx.put(abi.ARR_TOTAL_LINES, np.full(C1, 0.3, np.float32))
     n = args.packets
     base = rank * n
 
-    def step(i: int):
-        ctx.opacity(1)
-        st = ctx.transport(n, seed=1000 + i, counter_base=base, precision=abi.PREC_FP32_GEOM, zero=True,
-                           n_photons_norm=n)
+    def step(i: int, plain: bool = False):
+        ctx.state_restore()
+        ph = {}
+        ph["opacity"] = ctx.opacity(1).kernel_ms
+        ph["emission"] = ctx.emission(1, precision=abi.PHASE_EXACT if plain else abi.PHASE_MIXED).kernel_ms
+        st = ctx.transport(n, seed=1000 + i, counter_base=base,
+                           precision=abi.PREC_FP64 if plain else abi.PREC_FP32_GEOM, zero=True, n_photons_norm=n)
+        ph["transport"] = st.kernel_ms
         ctx.normalize_j()
-        return st
+        bs = ctx.balance(precision=abi.BAL_FP64 if plain else abi.BAL_MIXED)
+        ph["balance"] = bs.kernel_ms
+        return st, bs, ph
 
-    kernels_per_step = 1 + 1 + 2   # opacity, transport, normalize (J and escaped)
     for i in range(args.warmup):
         step(i)
     ctx.sync()
@@ -273,12 +315,15 @@ def run_gpu(args, dist, ws, rank, local):
     clk = clocks.stop()
     ms_step = max_over_ranks(dist, ms / args.steps)
     value = ws * n / (ms_step / 1e3)
+    phases = {k: float(np.mean([p[k] for _, _, p in stats])) for k in stats[0][2]}
+    bal_ms = phases["balance"]
 
     # roofline of the transport kernel: algorithmic bytes per estimator update
     # (4 B kappa read + 16 B J read-modify-write) plus ceil(log2 B) * 4 B per CDF search
-    upd = np.mean([s.crossings + s.interactions for s in stats])
-    emis = np.mean([s.emissions for s in stats])
-    kms = np.mean([s.kernel_ms for s in stats])
+    tst = [t for t, _, _ in stats]
+    upd = np.mean([s.crossings + s.interactions for s in tst])
+    emis = np.mean([s.emissions for s in tst])
+    kms = np.mean([s.kernel_ms for s in tst])
     alg_bytes = upd * 20.0 + emis * math.ceil(math.log2(nb)) * 4.0
     achieved = alg_bytes / (kms / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
@@ -286,21 +331,35 @@ def run_gpu(args, dist, ws, rank, local):
     traffic = None
     if tr:
         traffic = tr["dram_bytes_per_update"] * upd
-    # e2e: the same step through the C ABI from pinned host memory, Jste read back
+
+    # the plain FP64 path (FP64 geometry, FP64 multi-level atoms and rates) on the same step
+    plain = [step(10_000 + i, plain=True) for i in range(args.plain_steps)] if args.plain_steps > 0 else []
+    plain_ms = float(np.mean([sum(p.values()) for _, _, p in plain])) if plain else None
+
+    # e2e: the same step through the C ABI from pinned host memory, the updated state read back
     te = torch.from_numpy(setup.get(abi.ARR_TE)).pin_memory()
     ne = torch.from_numpy(setup.get(abi.ARR_NE)).pin_memory()
     ion = torch.from_numpy(setup.get(abi.ARR_IONDEN)).pin_memory()
-    jhost = torch.empty((nb, C1), dtype=torch.float64).pin_memory()
+    te_out = torch.empty_like(te).pin_memory()
+    ne_out = torch.empty_like(ne).pin_memory()
+    ion_out = torch.empty_like(ion).pin_memory()
     import ctypes
     lib = abi.lib()
 
     def put(arr_id, t):
         ctx._check(lib.mcx_put(ctx._h, arr_id, ctypes.c_void_p(t.data_ptr()), t.numel() * t.element_size()))
 
+    def get(arr_id, t):
+        ctx._check(lib.mcx_get(ctx._h, arr_id, ctypes.c_void_p(t.data_ptr()), t.numel() * t.element_size()))
+
     def e2e_step(i):
         put(abi.ARR_TE, te); put(abi.ARR_NE, ne); put(abi.ARR_IONDEN, ion)
-        step(i)
-        ctx._check(lib.mcx_get(ctx._h, abi.ARR_JSTE, ctypes.c_void_p(jhost.data_ptr()), jhost.numel() * 8))
+        ctx.opacity(1)
+        ctx.emission(1, precision=abi.PHASE_MIXED)
+        ctx.transport(n, seed=2000 + i, counter_base=base, precision=abi.PREC_FP32_GEOM, zero=True, n_photons_norm=n)
+        ctx.normalize_j()
+        ctx.balance(precision=abi.BAL_MIXED)
+        get(abi.ARR_TE, te_out); get(abi.ARR_NE, ne_out); get(abi.ARR_IONDEN, ion_out)
 
     e2e_step(0)
     barrier(dist)
@@ -312,8 +371,9 @@ def run_gpu(args, dist, ws, rank, local):
     wall_e2e = time.perf_counter() - t0
     ms_e2e_step = max_over_ranks(dist, max(ms_e2e, wall_e2e * 1e3) / args.steps)
     h2d = te.numel() * 4 + ne.numel() * 4 + ion.numel() * 4
-    d2h = jhost.numel() * 8
+    d2h = h2d
 
+    bst = [b for _, b, _ in stats]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -324,8 +384,17 @@ def run_gpu(args, dist, ws, rank, local):
                      "frac": achieved / peak, "traffic": traffic,
                      "kernel": "transportKernel<float>", "peak_kind": peak_kind,
                      "alg_bytes_per_launch": alg_bytes, "kernel_ms": kms},
-        "gpu_launches": kernels_per_step * args.steps,
-        "transport": {k: float(np.mean([getattr(s, k) for s in stats])) for k in
+        "gpu_launches": KERNELS_PER_STEP * args.steps,
+        "phase_ms": phases,
+        "cells_balanced_per_s": setup.n_cells / (bal_ms / 1e3),
+        "balance": {"cells_updated": float(np.mean([b.cells_updated for b in bst])),
+                    "no_te_bal": float(np.mean([b.no_te_bal for b in bst])),
+                    "max_iter_t": int(max(b.max_iter_t for b in bst))},
+        "plain_fp64_gpu": None if plain_ms is None else {
+            "ms_per_step": plain_ms, "value": ws * n / (plain_ms / 1e3),
+            "phase_ms": {k: float(np.mean([p[k] for _, _, p in plain])) for k in plain[0][2]},
+            "speedup_of_production": plain_ms / ms_step},
+        "transport": {k: float(np.mean([getattr(s, k) for s in tst])) for k in
                       ("crossings", "interactions", "absorptions", "scatterings", "escaped", "line_escapes",
                        "emissions", "trapped", "kernel_ms")},
     }
@@ -334,10 +403,10 @@ def run_gpu(args, dist, ws, rank, local):
     if rank == 0 and not args.no_cpu_baseline:
         threads = cpu_threads()
         sample = args.cpu_sample or 200_000
-        cb = cpu_step(setup, n, sample, threads)
+        cells = args.cpu_cells or 2000
+        cb = cpu_step(setup, n, sample, cells, threads)
         line["cpu_baseline"] = {"value": cb["value"], "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"opacity of all {setup.n_cells} cells + transport of {sample} packets "
-                                          f"on {threads} threads, transport time scaled linearly to {n} packets"}
+                                "sample": cpu_sample_text(setup, cb, sample, n, threads)}
     if rank == 0:
         print(json.dumps(line))
     ctx.close()

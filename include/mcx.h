@@ -207,6 +207,13 @@ int  mcx_put(mcx_ctx* ctx, int32_t array_id, const void* host, size_t nbytes);
 /* Raw device pointer of a context array (for zero-copy callers). */
 int  mcx_device_ptr(mcx_ctx* ctx, int32_t array_id, void** dptr);
 
+/* Device-side snapshot of the per-cell gas state (Te, Ne, ionDen, TeOld,
+ * NeOld, lgConverged) and its restoration, stream-ordered with the phases.
+ * No counterpart in the reference, which keeps one grid state; used to rerun
+ * an iteration from the same state (timing, tests, restarts in memory). */
+int  mcx_state_save(mcx_ctx* ctx);
+int  mcx_state_restore(mcx_ctx* ctx);
+
 /* ------------------------------------------------------- phase: opacity */
 /* Per-cell opacity kappa(nu): free-free + sum of bound-free x-sections times
  * ion densities + Klein-Nishina electron scattering.  Replaces the
@@ -214,9 +221,13 @@ int  mcx_device_ptr(mcx_ctx* ctx, int32_t array_id, void** dptr);
  * ionizationDriver/BoltGaunt/getGauntFF/eDenSum/addOpacity
  * (source/ionization_mod.f90:26-477), including the skip rule for cells whose
  * Te and Ne changed by less than 0.5 % (source/iteration_mod.f90:131-149). */
+#define MCX_PHASE_EXACT  0     /* the reference's arithmetic (FP64 multi-level atoms)      */
+#define MCX_PHASE_MIXED  1     /* emission: forbidden lines from the mixed-precision solver */
+
 typedef struct mcx_phase_opts {
     int32_t n_iterate_mc;       /* nIterateMC (1-based); the skip rule applies when > 1 */
-    int32_t reserved[7];
+    int32_t precision;          /* MCX_PHASE_*                                           */
+    int32_t reserved[6];
 } mcx_phase_opts;
 
 typedef struct mcx_phase_stats {
@@ -254,6 +265,9 @@ int  mcx_emission(mcx_ctx* ctx, const mcx_phase_opts* opts, mcx_phase_stats* sta
  * TeOld/NeOld take Te/Ne first, then Te, Ne, ionDen, lgConverged and lgBlack
  * are updated on the device.  Gas only; grains are outside this phase. */
 #define MCX_BAL_FP64  0         /* FP64 throughout (the plain path)                    */
+#define MCX_BAL_MIXED 1         /* FP32 rates, collision strengths and exponentials;
+                                   FP64 level-population LU, ionisation ladder and
+                                   normalisation, electron density, Te bracketing      */
 
 typedef struct mcx_balance_opts {
     int32_t precision;          /* MCX_BAL_*                                            */

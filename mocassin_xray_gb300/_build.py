@@ -50,7 +50,9 @@ def build_lib(verbose: bool = False) -> Path:
         ("k_opacity.cu", []),
         ("k_transport_f32.cu", []),
         ("k_transport_f64.cu", ["--fmad=false"]),
-        ("k_balance.cu", ["--fmad=false"]),
+        ("k_balance.cu", []),
+        ("k_balance_f64.cu", ["--fmad=false"]),
+        ("k_balance_mixed.cu", []),
         ("mcx_noalloc.cu", []),
     ]
     cmds = []

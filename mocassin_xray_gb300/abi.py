@@ -39,7 +39,8 @@ F64_SARR = {SARR_ATOM_DATA}
 
 MESH_REFERENCE, MESH_LOG_EDGES = 0, 1
 PREC_FP32_GEOM, PREC_FP64 = 0, 1
-BAL_FP64 = 0
+BAL_FP64, BAL_MIXED = 0, 1
+PHASE_EXACT, PHASE_MIXED = 0, 1
 
 
 class SetupOpts(C.Structure):
@@ -68,7 +69,7 @@ class BalanceStats(C.Structure):
 
 
 class PhaseOpts(C.Structure):
-    _fields_ = [("n_iterate_mc", C.c_int32), ("reserved", C.c_int32 * 7)]
+    _fields_ = [("n_iterate_mc", C.c_int32), ("precision", C.c_int32), ("reserved", C.c_int32 * 6)]
 
 
 class PhaseStats(C.Structure):
@@ -127,6 +128,8 @@ SIGNATURES = [
     ("mcx_get", C.c_int, [_P, C.c_int32, _P, C.c_size_t]),
     ("mcx_put", C.c_int, [_P, C.c_int32, _P, C.c_size_t]),
     ("mcx_device_ptr", C.c_int, [_P, C.c_int32, C.POINTER(_P)]),
+    ("mcx_state_save", C.c_int, [_P]),
+    ("mcx_state_restore", C.c_int, [_P]),
     ("mcx_opacity", C.c_int, [_P, C.POINTER(PhaseOpts), C.POINTER(PhaseStats)]),
     ("mcx_emission", C.c_int, [_P, C.POINTER(PhaseOpts), C.POINTER(PhaseStats)]),
     ("mcx_transport", C.c_int, [_P, C.POINTER(TransportOpts), C.POINTER(TransportStats)]),

@@ -14,7 +14,8 @@
 //                                     step, convergence and the cell's results
 // A J-only pass before the first round integrates the photoionisation rates
 // and Compton sums, which the reference recomputes on every T-iteration from
-// the same J.  All arithmetic is FP64.
+// the same J.  Two precisions: FP64 throughout, or FP32 rates with FP64 level
+// populations, ionisation ladder and Te bracketing (k_balance_impl.cuh).
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -66,8 +67,10 @@ struct BalanceDev {
   const float* diel;           // [nDiel][8]
   const float* aldro;          // [nAldro][6]
   const int32_t* outer;        // [30][30][3]
+  const float4* chex;          // [31][32] charge-exchange a, b, c, d of (Z, ion), 0 where none
   const int32_t* atomHdr;      // [nAtoms][16]
   const double* atomData;
+  const float* atomDataF;      // the same values in FP32 (mixed precision)
   // per-cell work, [k][C+1] (cell fastest)
   double* ion;                 // [nstages][nElemUsed]
   double* alpha;               // [nElemUsed][nstages]
@@ -112,14 +115,18 @@ struct BalanceGrid {
   int32_t* converged, *black, *nIterT;   // [C+1]
 };
 
+constexpr int kBalFp64 = 0;    // FP64 throughout (the plain path)
+constexpr int kBalMixed = 1;   // FP32 rates / splines / exponentials, FP64 solves and bracketing
+
 // updateCell for every cell: up to maxRounds T-iterations (the reference's
 // maxIterateT = 20).  Asynchronous on the stream; counters are left in
 // BalanceDev::counters.
-cudaError_t launchBalance(BalanceData& b, const BalanceGrid& g, int maxRounds, cudaStream_t s);
+cudaError_t launchBalance(BalanceData& b, const BalanceGrid& g, int maxRounds, int precision, cudaStream_t s);
 
-// The forLines line total of every cell (the emission phase's normFor,
-// rec = .true., units of 1e-25 erg/s per gas density) from the grid state.
+// The forLines line total of every cell with compute[c] = 1 (the emission
+// phase's normFor, rec = .true., units of 1e-25 erg/s per gas density) from
+// the grid state.
 cudaError_t launchForLinesEmission(BalanceData& b, const float* te, const float* ne, const float* ionDen,
-                                   const uint8_t* compute, float* forLines, cudaStream_t s);
+                                   const uint8_t* compute, float* forLines, int precision, cudaStream_t s);
 
 }  // namespace mcx

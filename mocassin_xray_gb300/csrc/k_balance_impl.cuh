@@ -1,0 +1,919 @@
+// k_balance_impl.cuh - device code of the balance phase, compiled twice:
+//   k_balance_f64.cu    real = double, --fmad=false: the plain FP64 path that is
+//                       checked against the oracle operation by operation
+//   k_balance_mixed.cu  real = float: rates, splines and exponentials in FP32
+//                       (the reference's own REAL), while the level-population
+//                       LU solve, the ionisation ladder and its normalisation,
+//                       the electron density and the Te bracketing stay FP64
+// The including file defines MCX_BAL_REAL, MCX_BAL_NS and MCX_BAL_EXACT.
+//
+// Reference routines: updateCell / iterateT (source/update_mod.f90:15-482),
+// calcAlpha (:2298-2413), RRbadnell / DRbadnell (:2415-2450), radRecFit
+// (:3094-3202), dielectronic (:3204-3305), collisionalIonisation
+// (:3552-3582), photoionisation (:3584-3832), compton (:3834-3897),
+// getPhotoRates (:3971-4040), ionBalance (:1575-1992), thermBalance
+// (:887-1215), forLines (:1221-1262), equilibrium / luSlv
+// (source/emission_mod.f90:2505-3106), splint (source/interpolation_mod.f90:286-335).
+#include "k_balance.cuh"
+#include "setup_internal.h"
+
+#include <algorithm>
+
+namespace mcx {
+namespace MCX_BAL_NS {
+
+typedef MCX_BAL_REAL real;
+
+// a default-REAL constant of the reference, at its single-precision value, in
+// the rate precision (RF) or in FP64 (RD)
+#define RF(x) ((real)(x##f))
+#define RD(x) ((double)(x##f))
+
+__device__ __forceinline__ real kBoltz() { return RF(1.380658e-16); }    // constants_mod.f90:18
+__device__ __forceinline__ real kRyd2erg() { return RF(2.1799e-11); }   // constants_mod.f90:20
+__device__ __forceinline__ real kHcRyd() { return RF(2.1799153e-11); }  // update_mod.f90:64
+__device__ __forceinline__ double kXMax() { return RD(0.99999); }       // constants_mod.f90:57
+
+constexpr int kNE = 30;
+// mixed precision: ions with elemAbun * ionDen below this skip the atom solve
+constexpr double kNegligibleIon = 1e-16;
+
+struct CellIdx {
+  int cell, C1;
+};
+
+__device__ __forceinline__ double& ionAt(const BalanceDev& b, const CellIdx& c, int z, int st) {
+  return b.ion[((size_t)(st - 1) * b.nElemUsed + (b.xref[z] - 1)) * c.C1 + c.cell];
+}
+__device__ __forceinline__ size_t pairOff(const BalanceDev& b, const CellIdx& c, int z, int ion) {
+  return ((size_t)(b.xref[z] - 1) * b.nstages + (ion - 1)) * c.C1 + c.cell;
+}
+
+// ------------------------------------------------------------- rate functions
+
+__device__ real rrBadnell(const BalanceDev& b, real te, int elem, int nel) {
+  const float* t = b.RRb;
+  auto RB = [&](int k) { return (real)t[((size_t)k * kNE + (elem - 1)) * (kNE + 1) + nel]; };
+  real A = RB(0), B = RB(1), T0 = RB(2), T1 = RB(3), Cc = RB(4), T2 = RB(5);
+  real bbad = B + Cc * exp(-T2 / te);
+  const real h = (real)0.5, one = (real)1.;
+  return A / (pow(te / T0, h) * pow(one + pow(te / T0, h), one - bbad) * pow(one + pow(te / T1, h), one + bbad));
+}
+
+__device__ real drBadnell(const BalanceDev& b, real te, int elem, int nel) {
+  real dr = 0;
+  const float* E = b.DRbE + ((size_t)(elem - 1) * (kNE + 1) + nel) * 9;
+  const float* Cc = b.DRbC + ((size_t)(elem - 1) * (kNE + 1) + nel) * 9;
+  for (int idr = 0; idr < 9; ++idr)
+    if ((real)E[idr] / te < (real)87.) dr = dr + (real)Cc[idr] * exp(-(real)E[idr] / te);
+  return dr * pow(te, (real)-1.5);
+}
+
+__constant__ float kFeFit[3][10] = {
+    {4.33e-10f, 3.91e-10f, 3.49e-10f, 3.16e-10f, 2.96e-10f, 2.59e-10f, 2.24e-10f, 1.91e-10f, 1.68e-10f, 1.46e-10f},
+    {0.531f, 0.523f, 0.521f, 0.534f, 0.557f, 0.567f, 0.579f, 0.601f, 0.602f, 0.597f},
+    {5.77e-02f, 6.15e-02f, 6.22e-02f, 6.02e-02f, 5.79e-02f, 5.65e-02f, 5.49e-02f, 5.10e-02f, 5.07e-02f, 5.22e-02f}};
+
+__device__ real radRecFit(const BalanceDev& b, real te, int z, int n) {
+  const real one = (real)1.;
+  if ((n <= 3) || (n == 11) || ((z > 5) && (z < 9)) || (z == 10) || ((z == 26) && (n > 11))) {
+    const float* r = b.rnew + ((size_t)(z - 1) * kNE + (n - 1)) * 4;
+    real tt = sqrt(te / (real)r[2]);
+    return (real)r[0] / (tt * pow(tt + one, one - (real)r[1]) * pow(one + sqrt(te / (real)r[3]), one + (real)r[1]));
+  }
+  real tt = te * RF(1.e-4);
+  if ((z == 26) && (n <= 13))
+    return (real)kFeFit[0][n - 4] / pow(tt, (real)kFeFit[1][n - 4] + (real)kFeFit[2][n - 4] * log10(tt));
+  const float* r = b.rrec + ((size_t)(z - 1) * kNE + (n - 1)) * 2;
+  return (real)r[0] / pow(tt, (real)r[1]);
+}
+
+// diRec(elem, ion) of dielectronic: the last row of dielectronic.dat for
+// (elem, ion) whose temperature flag applies, or above 6e4 K the last row of
+// aldrovandi.dat (the whole diRec array is replaced there).
+__device__ real diRecOf(const BalanceDev& b, real te, int elem, int ion) {
+  if (ion > b.nstages) return 0;
+  const real one = (real)1.;
+  if (te > (real)60000.) {
+    real v = 0;
+    for (int r = 0; r < b.nAldro; ++r) {
+      const float* d = b.aldro + (size_t)r * 6;
+      if ((int)d[0] != elem || (int)d[0] - (int)d[1] + 1 != ion) continue;
+      real a = d[2], bb = d[3], t0 = d[4], t1 = d[5];
+      v = a * pow(te, (real)-1.5) * exp(-t0 / te) * (one + bb * exp(-t1 / te));
+    }
+    return v;
+  }
+  real t = te > (real)1000. ? te / (real)10000. : RF(0.1);
+  real v = 0;
+  for (int r = 0; r < b.nDiel; ++r) {
+    const float* d = b.diel + (size_t)r * 8;
+    if ((int)d[0] != elem || (int)d[0] + 1 - (int)d[1] != ion) continue;
+    int g = (int)d[7];
+    bool use = g == 0 || (g == 1 && te < (real)20000.) || (g == 2 && te >= (real)20000.);
+    if (!use) continue;
+    real a = d[2], bb = d[3], cc = d[4], dd = d[5], f = d[6];
+    v = RF(1e-12) * (a / t + bb + cc * t + dd * (t * t)) * pow(t, (real)-1.5) * exp(-f / t);
+  }
+  return v;
+}
+
+__device__ void calcAlpha(const BalanceDev& b, const CellIdx& c, real te) {
+  const int ns = b.nstages;
+  for (int e = 1; e <= b.nElemUsed; ++e) {
+    const int elem = b.zOf[e];
+    const int top = min(ns - 1, elem);
+    for (int ion = 1; ion <= top; ++ion) {
+      real a;
+      if (b.lgBadnell) {
+        int nel = elem - ion;
+        if (nel <= 11) {
+          a = rrBadnell(b, te, elem, nel);
+          a = a + drBadnell(b, te, elem, nel);
+        } else {
+          a = radRecFit(b, te, elem, elem - ion + 1);
+          real di = diRecOf(b, te, elem, ion);
+          if (di == (real)0. && ion < 7 && b.xref[8] > 0) di = diRecOf(b, te, 8, ion);
+          a = a + (di > (real)0. ? di : (real)0.);
+        }
+      } else {
+        a = radRecFit(b, te, elem, elem - ion + 1);
+        if (elem >= 3) {
+          real di = diRecOf(b, te, elem, ion);
+          if (di == (real)0. && ion < 7) di = diRecOf(b, te, 8, ion);
+          a = a + (di > (real)0. ? di : (real)0.);
+        }
+      }
+      b.alpha[pairOff(b, c, elem, ion)] = (double)a;
+    }
+  }
+}
+
+// chex(z, ion, 1) * 1e-9 without the temperature fit (ionBalance's heavy elements)
+__device__ __forceinline__ real chexRaw(const BalanceDev& b, int z, int ion) {
+  return (real)b.chex[z * 32 + ion].x * RF(1.e-9);
+}
+// chex(z, ion, 1) at Te (source/update_mod.f90:1711-1720, :3788-3797)
+__device__ real chexFit(const BalanceDev& b, int z, int ion, real te) {
+  const float4 x = b.chex[z * 32 + ion];
+  real a = (real)x.x * RF(1.e-9);
+  real t4 = te / (real)10000.;
+  real v = (te < (real)6000. || te > (real)5.e4) ? (real)0.
+                                                 : a * pow(t4, (real)x.y) * ((real)1. + (real)x.z * exp((real)x.w * t4));
+  return v < (real)0. ? (real)0. : v;
+}
+
+__device__ __forceinline__ const int32_t* outerOf(const BalanceDev& b, int z, int nElec) {
+  return b.outer + ((size_t)(z - 1) * kNE + (nElec - 1)) * 3;
+}
+
+// ------------------------------------------------------ J-only integrals
+
+// The parts of photoionisation / getPhotoRates / compton that depend on J
+// alone; one thread per cell.
+__global__ void __launch_bounds__(128) photoIntegralsKernel(BalanceDev b, const double* __restrict__ jste) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (cell > b.nCells) return;
+  const int C1 = b.nCells + 1;
+  const float* nu = b.nu;
+  const float* xs = b.xsec;
+  auto J = [&](int bin1) { return (real)jste[(size_t)(bin1 - 1) * C1 + cell]; };
+  bool hit = false;
+  for (int i = 1; i <= b.nbins; ++i)
+    if (jste[(size_t)(i - 1) * C1 + cell] > 0.) { hit = true; break; }
+  b.state[cell] = hit ? 0 : 2;
+  if (!hit) return;
+  const real hcRyd = kHcRyd();
+  for (int t = 0; t < b.nShellsTot; ++t) {
+    const PhotoShell sh = b.shells[t];
+    const size_t o = (size_t)t * C1 + cell;
+    if (sh.ipNuP < 1 || sh.ipNuP > b.nbins) {   // threshold outside the mesh
+      b.gam[o] = sh.heavy ? 0. : RD(1.e-20);
+      b.heatA[o] = 0.;
+      b.heatHi[o] = 0.;
+      continue;
+    }
+    if (!sh.heavy) {
+      real n1 = RF(1.e-20), h1 = 0;
+      const real nuIP = (real)nu[sh.ipNuP - 1];
+      for (int j = sh.ipNuP; j <= sh.highNuP; ++j) {
+        real ph = xs[j - sh.ipNuP + sh.xsecP - 1];
+        if (ph < RF(1.e-35)) ph = 0;
+        real jj = J(j);
+        if (jj > (real)0.) {
+          n1 = n1 + jj * ph / (hcRyd * (real)nu[j - 1]);
+          h1 = h1 + ph * jj * ((real)nu[j - 1] - nuIP) / (real)nu[j - 1];
+        }
+      }
+      b.gam[o] = n1;
+      b.heatA[o] = h1;
+      b.heatHi[o] = 0.;
+      continue;
+    }
+    const int nu1P = sh.ipNuP, IPnuP = sh.ipNuP;
+    const int iup = min(sh.highNuP, b.nbins);
+    const real augerE = hcRyd * (real)nu[nu1P - 1] * (real)sh.yield1;
+    real g = 0, h = 0;
+    const int top = min(iup, b.secIonP - 1);
+    for (int i = nu1P + 1; i <= top; ++i) {
+      real jj = J(i);
+      if (jj > (real)0.) {
+        real ph = xs[i + sh.xsecP - IPnuP - 1];
+        if (ph < RF(1.e-35)) ph = 0;
+        g = g + jj * ph / (hcRyd * (real)nu[i - 1]);
+        h = h + jj * ph;
+      }
+    }
+    h = h - g * augerE;
+    const real jIP = J(IPnuP);
+    const real ph0 = xs[sh.xsecP - 1];
+    g = g + jIP * ph0 / (hcRyd * (real)nu[IPnuP - 1]);
+    h = h + jIP * ph0 * (hcRyd * (real)nu[IPnuP - 1] - augerE) / (hcRyd * (real)nu[IPnuP - 1]);
+    real gh = 0, hh = 0;
+    const int ilow = max(IPnuP + 1, b.secIonP);
+    for (int i = ilow; i <= iup; ++i) {
+      real p = xs[i + sh.xsecP - IPnuP - 1];
+      gh = gh + jIP * p / (hcRyd * (real)nu[i - 1]);   // radField(IPnuP), as the reference
+      hh = hh + jIP * p;
+    }
+    g = g + gh;
+    hh = hh - gh * augerE;
+    b.gam[o] = g;
+    b.heatA[o] = h;
+    b.heatHi[o] = hh;
+  }
+  if (b.lgCompton) {
+    real s1 = 0, s2 = 0, rhH = 0, rhHe = 0;
+    for (int i = 1; i <= b.nbins; ++i) {
+      real rf = J(i);
+      s1 = s1 + rf;
+      s2 = s2 + rf / (real)nu[i - 1];
+      if (i > b.cRecoilHP) {
+        real energy = RF(2.66e-5) * (real)nu[i - 1] * (real)nu[i - 1] - (real)1.;
+        rhH = rhH + (real)b.xsecRecoil[i - 1] * rf * energy;
+      }
+      if (i > b.cRecoilHeP) {
+        real energy = RF(2.66e-5) * (real)nu[i - 1] * (real)nu[i - 1] - RF(1.8);
+        rhHe = rhHe + (real)b.xsecRecoil[i - 1] * rf * energy;
+      }
+    }
+    b.comp[0 * (size_t)C1 + cell] = s1 * kRyd2erg();
+    b.comp[1 * (size_t)C1 + cell] = s2;
+    b.comp[2 * (size_t)C1 + cell] = rhH;
+    b.comp[3 * (size_t)C1 + cell] = rhHe;
+  }
+}
+
+// Loads the grid state of the cells into the FP64 work arrays.
+__global__ void loadStateKernel(BalanceDev b, const float* __restrict__ te, const float* __restrict__ ne,
+                                const float* __restrict__ ionDen) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (cell > b.nCells) return;
+  const int C1 = b.nCells + 1;
+  b.te[cell] = te[cell];
+  b.ne[cell] = ne[cell];
+  const size_t nI = (size_t)b.nstages * b.nElemUsed;
+  for (size_t k = 0; k < nI; ++k) b.ion[k * C1 + cell] = ionDen[k * C1 + cell];
+  b.xOld[cell] = b.ion[(size_t)(b.xref[1] - 1) * C1 + cell];
+  b.tHigh[cell] = 0.; b.tLow[cell] = 0.; b.resHigh[cell] = 0.; b.resLow[cell] = 0.;
+  b.nIterT[cell] = 0;
+  b.ibConv[cell] = 1;
+}
+
+// -------------------------------------------------------------- one round
+
+// ionBalance (recursion as a loop); returns lgConv.  The ladder, its
+// normalisation and Ne are FP64 in both precisions.
+__device__ bool ionBalance(const BalanceDev& b, const CellIdx& c, double te, double& ne, double hden) {
+  const int ns = b.nstages;
+  const int zH = 1, zHe = 2;
+  const bool heOn = b.xref[zHe] > 0;
+  const int C1 = c.C1;
+  const real teR = (real)te;
+  for (int nIterateX = 1;; ++nIterateX) {
+    bool lgConv = true;
+    double ionRatio[3][3] = {{0., 0., 0.}, {0., 0., 0.}, {0., 0., 0.}};
+    double ionProd[3][3] = {{1., 1., 1.}, {1., 1., 1.}, {1., 1., 1.}};
+    double den[3] = {1., 1., 1.};
+    real expFact = RF(157893.94) / teR;
+    if (expFact > (real)75.) expFact = (real)75.;
+    real collIonH = RF(2.75E-16) * teR * sqrt(teR) * (RF(157893.94) / teR + (real)2.) * exp(-expFact);
+    const double HIOld = ionAt(b, c, zH, 1);
+    const double HeIOld = heOn ? ionAt(b, c, zHe, 1) : 0.;
+    const double HeIIOld = heOn ? ionAt(b, c, zHe, 2) : 0.;
+    for (int elem = 1; elem <= 2; ++elem) {
+      if (!b.xref[elem]) continue;
+      for (int ion = 1; ion <= min(elem, ns - 1); ++ion) {
+        double cx = chexFit(b, elem, ion, teR);
+        int outShell = outerOf(b, elem, elem - ion + 1)[0];
+        if (elem > 1 || ion > 1) collIonH = 0;
+        int p0 = b.pairShell0[(b.xref[elem] - 1) * 32 + (ion - 1)];
+        double pi = b.pi1[(size_t)(p0 + outShell - 1) * C1 + c.cell];
+        ionRatio[elem][ion] = (pi + (double)collIonH * ne + 0.) /
+                              (ne * b.alpha[pairOff(b, c, elem, ion)] + cx * hden * HIOld);
+      }
+    }
+    for (int elem = 1; elem <= 2; ++elem) {
+      if (!b.xref[elem]) continue;
+      for (int ion = 1; ion <= min(elem, ns - 1); ++ion)
+        for (int i = 1; i <= ion; ++i) ionProd[elem][ion] = ionProd[elem][ion] * ionRatio[elem][i];
+    }
+    for (int elem = 1; elem <= 2; ++elem) {
+      if (!b.xref[elem]) continue;
+      for (int ion = 1; ion <= min(elem, ns - 1); ++ion) den[elem] = den[elem] + ionProd[elem][ion];
+    }
+    for (int elem = 1; elem <= 2; ++elem) {
+      if (!b.xref[elem]) continue;
+      for (int ion = 1; ion <= min(elem + 1, ns); ++ion) {
+        double v = ion == 1 ? 1. / den[elem] : ionProd[elem][ion - 1] / den[elem];
+        if (v > kXMax()) v = kXMax();
+        if (v < RD(1.e-20)) v = RD(1.e-20);
+        ionAt(b, c, elem, ion) = v;
+      }
+    }
+    // X(H0) as just updated above (grid%ionDen in the reference)
+    const double xH0now = ionAt(b, c, zH, 1);
+    for (int e = 1; e <= b.nElemUsed; ++e) {
+      const int elem = b.zOf[e];
+      if (elem < 3) continue;
+      double out[33], inn[33], mat[33];
+      for (int k = 0; k < 33; ++k) { out[k] = 0.; inn[k] = 0.; }
+      const int topI = min(elem, ns - 1);
+      const int lim = min(ns - 1, elem);
+      for (int ion = 1; ion <= topI; ++ion) {
+        out[ion] = out[ion] + b.coll1[pairOff(b, c, elem, ion)] * ne;
+        const int p0 = b.pairShell0[(e - 1) * 32 + (ion - 1)];
+        const int nsh = b.pairNShell[(e - 1) * 32 + (ion - 1)];
+        for (int shell = 1; shell <= nsh; ++shell) {
+          const double pi = b.pi1[(size_t)(p0 + shell - 1) * C1 + c.cell];
+          out[ion] = out[ion] + pi;
+          const int nAug = b.nauger[((size_t)(elem - 1) * kNE + (ion - 1)) * 10 + (shell - 1)];
+          for (int nelec = 2; nelec <= nAug; ++nelec) {
+            int maxim = min(ion + nelec - 1, lim);
+            double xm = ionAt(b, c, elem, maxim);
+            double ratio = xm > 1e-30 ? ionAt(b, c, elem, ion) / xm : 1.;
+            out[maxim] = out[maxim] +
+                         pi * (double)b.auger[(((size_t)(elem - 1) * kNE + (ion - 1)) * 10 + (shell - 1)) * 10 + (nelec - 1)] * ratio;
+          }
+        }
+      }
+      for (int ion = 1; ion <= topI; ++ion)
+        inn[ion] = ne * b.alpha[pairOff(b, c, elem, ion)] + (double)chexRaw(b, elem, ion) * hden * xH0now;
+      mat[1] = 1.;
+      double sumMat = 1.;
+      const int top = min(ns, elem + 1);
+      for (int ion = 2; ion <= top; ++ion) {
+        mat[ion] = mat[ion - 1] * out[ion - 1] / inn[ion - 1];
+        sumMat = sumMat + mat[ion];
+      }
+      sumMat = 1. / sumMat;
+      ionAt(b, c, elem, top) = mat[top] * sumMat;
+      for (int ion = 1; ion <= topI; ++ion) {
+        double v;
+        if (nIterateX < 2 && mat[ion] * sumMat > 0.) {
+          double old = ionAt(b, c, elem, ion);
+          if (old <= 0.) old = RD(1.e-5);
+#if MCX_BAL_EXACT
+          v = pow(10., 0.5 * (log10(old) + log10(mat[ion] * sumMat)));
+#else
+          v = sqrt(old) * sqrt(mat[ion] * sumMat);   // the same geometric mean
+#endif
+        } else {
+          v = mat[ion] * sumMat;
+        }
+        if (v > kXMax()) v = kXMax();
+        if (v < RD(1.e-20)) v = RD(1.e-20);
+        ionAt(b, c, elem, ion) = v;
+      }
+    }
+    double nE = 0.;
+    for (int e = 1; e <= b.nElemUsed; ++e) {
+      const int elem = b.zOf[e];
+      for (int ion = 2; ion <= min(elem + 1, ns); ++ion) {
+        double x = ionAt(b, c, elem, ion);
+        if (x >= RD(1.e-10)) nE = nE + (double)(ion - 1) * (double)b.abun[elem] * x;
+      }
+    }
+    nE = nE * hden;
+    if (nE == 0.) nE = 1.;
+    ne = nE;
+    double dHI = (ionAt(b, c, zH, 1) - HIOld) / HIOld;
+    double dHeI = heOn ? (ionAt(b, c, zHe, 1) - HeIOld) / HeIOld : 0.;
+    double dHeII = heOn ? (ionAt(b, c, zHe, 2) - HeIIOld) / HeIIOld : 0.;
+    bool big = fabs(dHI) > RD(0.01) || fabs(dHeI) > RD(0.01) || fabs(dHeII) > RD(0.01);
+    if (big && nIterateX < 15) continue;
+    if (big && nIterateX == 15) lgConv = false;
+    return lgConv;
+  }
+}
+
+// calcAlpha, photoionisation, collisionalIonisation, compton, ionBalance and
+// the thermBalance terms without forLines; one thread per iterating cell.
+__global__ void __launch_bounds__(128) ratesKernel(BalanceDev b, const float* __restrict__ hdenG) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (cell > b.nCells || b.state[cell] != 0) return;
+  const CellIdx c{cell, b.nCells + 1};
+  const int C1 = c.C1, ns = b.nstages;
+  b.nIterT[cell] = b.nIterT[cell] + 1;
+  const double te = b.te[cell];
+  const real teR = (real)te;
+  double ne = b.ne[cell];
+  const double hden = hdenG[cell];
+  const real hdenR = (real)hden;
+  calcAlpha(b, c, teR);
+  // photoionisation
+  real xe = 0;
+  for (int e = 1; e <= b.nElemUsed; ++e) {
+    const int elem = b.zOf[e];
+    xe = xe + (real)ionAt(b, c, elem, 1) * (real)b.abun[elem] * hdenR;
+  }
+  xe = (real)ne / xe;
+  real heatef;
+  if (xe > RF(0.95)) heatef = 1;
+  else {
+    if (xe < RF(1.e-4)) xe = RF(1.e-4);
+    heatef = RF(0.9971) * ((real)1. - pow((real)1. - pow(xe, RF(0.2663)), RF(1.3163)));
+  }
+  for (int t = 0; t < b.nShellsTot; ++t) {
+    const size_t o = (size_t)t * C1 + cell;
+    b.pi1[o] = b.gam[o];
+    b.pi2[o] = b.shells[t].heavy ? (double)((real)b.heatA[o] + (real)b.heatHi[o] * heatef) : b.heatA[o];
+  }
+  // reverse charge exchange: deltaE_k > 1 only for N0 and O0
+  for (int k = 0; k < 2; ++k) {
+    const int elem = k == 0 ? 7 : 8;
+    const real dE = k == 0 ? RF(10863.) : RF(2205.);
+    if (!b.xref[elem] || ns - 1 < 1) continue;
+    const int32_t* o = outerOf(b, elem, elem);
+    const int nsh = b.pairNShell[(b.xref[elem] - 1) * 32];
+    if (o[0] > nsh) continue;
+    real cx = chexFit(b, elem, 1, teR);
+    real rev = cx * ((real)1. - (real)ionAt(b, c, 1, 1)) * hdenR * (real)2. * exp(-dE / teR) / ((real)o[1] / (real)o[2]);
+    const size_t off = (size_t)(b.pairShell0[(b.xref[elem] - 1) * 32] + o[0] - 1) * C1 + cell;
+    b.pi1[off] = b.pi1[off] + (double)rev;
+  }
+  // collisionalIonisation (returns at the first u > 80)
+  {
+    for (int e = 1; e <= b.nElemUsed; ++e)
+      for (int ion = 1; ion <= ns; ++ion) {
+        size_t o = ((size_t)(e - 1) * ns + (ion - 1)) * C1 + cell;
+        b.coll1[o] = 0.;
+        b.coll2[o] = 0.;
+      }
+    const real tev = teR * RF(8.617385e-05);
+    bool stop = false;
+    for (int e = 1; e <= b.nElemUsed && !stop; ++e) {
+      const int elem = b.zOf[e];
+      for (int ion = 1; ion <= min(ns - 1, elem - 1); ++ion) {
+        const int elec = elem - ion + 1;
+        const float* cf = b.CF + ((size_t)(elem - 1) * kNE + (elec - 1)) * 5;
+        real u = (real)cf[0] / tev;
+        if (u > (real)80.) { stop = true; break; }
+        real c1 = (real)cf[2] * ((real)1. + (real)cf[1] * sqrt(u)) / ((real)cf[3] + u) * pow(u, (real)cf[4]) * exp(-u);
+        b.coll1[pairOff(b, c, elem, ion)] = c1;
+        b.coll2[pairOff(b, c, elem, ion)] = (real)b.cionTherm[(elem - 1) * kNE + (ion - 1)] * c1 * kBoltz();
+      }
+    }
+  }
+  // compton, with the state before ionBalance
+  if (b.lgCompton) {
+    const real s1 = (real)b.comp[0 * (size_t)C1 + cell], s2 = (real)b.comp[1 * (size_t)C1 + cell];
+    const real rhH = (real)b.comp[2 * (size_t)C1 + cell], rhHe = (real)b.comp[3 * (size_t)C1 + cell];
+    real cool = (RF(6.65e-25) * RF(6.75e-10) * teR * s2) / hdenR;
+    real heat = (RF(6.65e-25) * s1 / RF(8.184e-7)) / hdenR;
+    real he = b.xref[2] ? rhHe * ((real)ionAt(b, c, 2, 1) * (real)b.abun[2]) * (real)2. : (real)0.;
+    real recoil = (rhH * (real)ionAt(b, c, 1, 1) * (real)b.abun[1] + he) * kRyd2erg();
+    b.compCool[cell] = cool;
+    b.compHeat[cell] = heat;
+    b.compRecoil[cell] = recoil;
+  }
+  bool conv = ionBalance(b, c, te, ne, hden);
+  b.ibConv[cell] = conv ? 1 : 0;
+  b.ne[cell] = ne;
+  // thermBalance without forLines
+  const real neR = (real)ne;
+  real coolFF = 0, coolRec = 0, L, Te4;
+  for (int e = 1; e <= b.nElemUsed; ++e) {
+    const int i = b.zOf[e];
+    if (!(ns > i)) continue;
+    L = log10(teR / (real)(i * i));
+    Te4 = teR / ((real)(i * i) * RF(1.e4));
+    real Np = (real)ionAt(b, c, i, i + 1) * (real)b.abun[i];
+    real betaFF = (real)i * (RF(1.0108464E-11) + RF(9.7930778E-13) * L - RF(6.6433144E-13) * L * L +
+                             RF(2.4793747E-13) * L * L * L - RF(2.3938215E-14) * L * L * L * L);
+    real t = Np * neR * betaFF * kBoltz() * teR / sqrt(teR);
+    if (!isnan(t)) coolFF = coolFF + t;
+    real betaRec = (real)i * (RF(9.4255985E-11) - RF(4.04794384E-12) * L - RF(1.0055237E-11) * L * L +
+                              RF(1.99266862E-12) * L * L * L - RF(1.06681387E-13) * L * L * L * L);
+    t = Np * neR * betaRec * kBoltz() * teR / sqrt(teR);
+    if (!isnan(t)) coolRec = coolRec + t;
+  }
+  Te4 = teR / RF(1.e4);
+  for (int e = 1; e <= b.nElemUsed; ++e) {
+    const int i = b.zOf[e];
+    if (i < 2 || !(ns > i)) continue;
+    L = log10((real)4. * teR / (real)(i * i));
+    Te4 = (real)4. * teR / ((real)(i * i) * RF(1.e4));
+    real Np = (real)ionAt(b, c, i, i) * (real)b.abun[i];
+    real betaFF = ((real)i / (real)2.) * (RF(1.070073e-11) - RF(2.5730207e-13) * L + RF(2.109134e-13) * L * L);
+    real t = Np * neR * betaFF * kBoltz() * teR / sqrt(teR);
+    if (!isnan(t)) coolFF = coolFF + t;
+    real betaRec = ((real)i / (real)2.) * (RF(1.06926e-10) - RF(2.41756e-11) * L + RF(1.14542e-12) * L * L -
+                                           RF(5.06535e-13) * L * L * L + RF(9.16745e-14) * L * L * L * L);
+    t = Np * neR * betaRec * kBoltz() * teR / sqrt(teR);
+    if (!isnan(t)) coolRec = coolRec + t;
+  }
+  real coolColl;
+  if (teR > (real)5000.)
+    coolColl = (RF(2.47e-8) * exp(-RF(118338.) / teR) * pow(Te4, RF(-0.228)) +
+                RF(1.32e-8) * exp(-RF(140252.) / teR) * pow(Te4, RF(-0.460))) * kHcRyd() * (real)ionAt(b, c, 1, 1) * neR;
+  else
+    coolColl = 0;
+  real coolCollH = 0;
+  for (int e = 1; e <= b.nElemUsed; ++e) {
+    const int elem = b.zOf[e];
+    for (int ion = 1; ion <= min(elem, ns - 1); ++ion)
+      coolCollH = coolCollH + (real)b.abun[elem] * (real)ionAt(b, c, elem, ion) * (real)b.coll2[pairOff(b, c, elem, ion)] * neR;
+  }
+  real heatSte = 0;
+  for (int e = 1; e <= b.nElemUsed; ++e) {
+    const int elem = b.zOf[e];
+    for (int ion = 1; ion <= min(elem, ns - 1); ++ion) {
+      const int p0 = b.pairShell0[(e - 1) * 32 + (ion - 1)];
+      const int nsh = b.pairNShell[(e - 1) * 32 + (ion - 1)];
+      for (int s = 0; s < nsh; ++s)
+        heatSte = heatSte + (real)b.pi2[(size_t)(p0 + s) * C1 + cell] * (real)ionAt(b, c, elem, ion) * (real)b.abun[elem];
+    }
+  }
+  b.coolA[cell] = coolFF + coolRec;
+  b.coolHex[cell] = coolColl;
+  b.coolCollH[cell] = coolCollH;
+  b.heat[cell] = heatSte;
+}
+
+// ------------------------------------------------------------- equilibrium
+
+#if MCX_BAL_EXACT
+__device__ __forceinline__ const real* atomTable(const BalanceDev& b) { return b.atomData; }
+#else
+__device__ __forceinline__ const real* atomTable(const BalanceDev& b) { return b.atomDataF; }
+#endif
+
+// splint with the interval search done once per atom: klo/khi and the
+// weights depend only on x and the temperature points
+struct SplineAt {
+  int klo, khi;    // 1-based, 0 = below the table, -1 = above
+  real a, bb, a3, b3, hh;
+};
+
+__device__ SplineAt splineAt(const real* xa, int n, real x) {
+  SplineAt s{};
+  if (x <= xa[0]) { s.klo = 0; return s; }
+  if (x >= xa[n - 1]) { s.klo = -1; return s; }
+  int klo = 1, khi = n;
+  for (int i = 0; i < 1000; ++i) {
+    if (khi - klo <= 1) break;
+    int k = (khi + klo) / 2;
+    if (xa[k - 1] > x) khi = k; else klo = k;
+  }
+  real h = xa[khi - 1] - xa[klo - 1];
+  s.klo = klo;
+  s.khi = khi;
+  s.a = (xa[khi - 1] - x) / h;
+  s.bb = (x - xa[klo - 1]) / h;
+  s.a3 = s.a * s.a * s.a - s.a;
+  s.b3 = s.bb * s.bb * s.bb - s.bb;
+  s.hh = h * h;
+  return s;
+}
+
+__device__ __forceinline__ real splineEval(const SplineAt& s, const real* ya, const real* y2a, int n) {
+  if (s.klo == 0) return ya[0];
+  if (s.klo < 0) return ya[n - 1];
+  return s.a * ya[s.klo - 1] + s.bb * ya[s.khi - 1] + (s.a3 * y2a[s.klo - 1] + s.b3 * y2a[s.khi - 1]) * s.hh / (real)6.;
+}
+
+// equilibrium of one atom: the sum over its lines of a(j,i)*E_ji*n_j*m1*m2*m3
+// that exceed 1e-35, lower level outer, upper level inner.  Collision rates
+// in the rate precision, the rate matrix and its LU solve in FP64.
+__device__ double equilibriumLines(const BalanceDev& b, int atom, double Te, double Ne, double ionDenUp, bool rec,
+                                   double m1, double m2, double m3) {
+  const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
+  const real* D = atomTable(b);
+  const double* DD = b.atomData;
+  const int nLev = h[kAtNLev], nT = h[kAtNTemp];
+  const real* logT = D + h[kAtOffLogT];
+  const real* qom = D + h[kAtOffQom];
+  const real* y2 = D + h[kAtOffY2];
+  const double* A = DD + h[kAtOffA];
+  const real* g = D + h[kAtOffG];
+  const real* e = D + h[kAtOffE];
+  const double* eD = DD + h[kAtOffE];
+  const double atp = DD[h[kAtOffAtp]];
+  const int iup2p = h[kAtIup2p];
+  const real TeR = (real)Te;
+  const real sqrTe = sqrt(TeR), log10Te = log10(TeR);
+  double alphaTotal[kMaxLevels + 1];
+  for (int i = 0; i <= nLev; ++i) alphaTotal[i] = 0.;
+  if (rec) {
+    const double* rr = DD + h[kAtOffRec];
+    const real one = (real)1.;
+    if (h[kAtRecType] == kRecPowerLaw) {
+      for (int r = 0; r < h[kAtNRec]; ++r) {
+        const double* v = rr + r * 11;
+        const int j = r + 2;
+        real br = (float)v[0], z = (float)v[1];
+        real ar0 = (float)v[2], ar1 = (float)v[3], ar2 = (float)v[4], ar3 = (float)v[5];
+        real ad0 = (float)v[6], ad1 = (float)v[7], ad2 = (float)v[8], ad3 = (float)v[9], ad4 = (float)v[10];
+        if (z > (real)0.) {
+          real tz = TeR * RF(1.e-4) / (z * z);
+          real t4 = TeR * RF(1.e-4);
+          alphaTotal[j] = RF(1.e-13) * br * z * ar0 * pow(tz, ar1) / (one + ar2 * pow(tz, ar3)) +
+                          RF(1.0e-12) * br * (ad0 / t4 + ad1 + ad2 * TeR * RF(1.e-4) + ad3 * (t4 * t4)) *
+                              pow(t4, (real)-1.5) * exp(-ad4 * RF(1.e4) / TeR);
+        }
+      }
+    } else if (h[kAtRecType] == kRecChianti) {
+      for (int r = 0; r < h[kAtNRec]; ++r) {
+        const double* v = rr + r * 5;
+        int jj = (int)v[0];
+        real a = (float)v[1], bb = (float)v[2], cc = (float)v[3], d = (float)v[4];
+        real L = log10(TeR);
+        alphaTotal[jj] = pow((real)10., a + bb * L + cc * (L * L) + d * (L * L * L));
+      }
+    }
+  }
+  real qeff[kMaxLevels + 1][kMaxLevels + 1];
+  double x[kMaxLevels + 1][kMaxLevels + 1], y[kMaxLevels + 1];
+  for (int i = 1; i <= nLev; ++i) {
+    y[i] = 0.;
+    for (int j = 1; j <= nLev; ++j) { qeff[i][j] = 0; x[i][j] = 0.; }
+  }
+  const SplineAt sp = nT > 2 ? splineAt(logT, nT, log10Te) : SplineAt{};
+  const real constant = (real)1.4388463, c863 = (real)8.63e-6;
+  int p = 0;
+  for (int i = 2; i <= nLev; ++i) {
+    for (int j = i; j <= nLev; ++j, ++p) {
+      const real* qq = qom + (size_t)p * nT;
+      real cs;
+      if (nT == 1) cs = qq[0];
+      else if (nT == 2) cs = qq[0] + (qq[1] - qq[0]) / (logT[1] - logT[0]) * (log10Te - logT[0]);
+      else cs = splineEval(sp, qq, y2 + (size_t)p * nT, nT);
+      if (eD[i - 2] <= eD[j - 1]) {
+        real expFac = exp((e[i - 2] - e[j - 1]) * constant / TeR);
+        qeff[i - 1][j] = c863 * cs * expFac / (g[i - 2] * sqrTe);
+        qeff[j][i - 1] = c863 * cs / (g[j - 1] * sqrTe);
+      } else {
+        real expFac = exp((e[j - 1] - e[i - 2]) * constant / TeR);
+        qeff[j][i - 1] = c863 * cs * expFac / (g[i - 2] * sqrTe);
+        qeff[i - 1][j] = c863 * cs / (g[j - 1] * sqrTe);
+      }
+    }
+  }
+  for (int j = 1; j <= nLev; ++j) x[1][j] = 1.;
+  y[1] = 1.;
+  for (int i = 2; i <= nLev; ++i) {
+    for (int j = 1; j <= nLev; ++j) {
+      if (j != i) {
+        x[i][j] = x[i][j] + Ne * (double)qeff[j][i];
+        x[i][i] = x[i][i] - Ne * (double)qeff[i][j];
+        if (j > i) x[i][j] = x[i][j] + A[(size_t)(j - 1) * nLev + (i - 1)];
+        else x[i][i] = x[i][i] - A[(size_t)(i - 1) * nLev + (j - 1)];
+      }
+    }
+    y[i] = -Ne * ionDenUp * alphaTotal[i];
+  }
+  const int n = nLev;
+#if MCX_BAL_EXACT
+  // lured + reslv as the reference writes them (no pivoting, multipliers recomputed)
+  if (n > 1) {
+    for (int i = 1; i <= n - 1; ++i)
+      for (int k = i + 1; k <= n; ++k) {
+        double factor = x[k][i] / x[i][i];
+        for (int j = i + 1; j <= n; ++j) x[k][j] = x[k][j] - x[i][j] * factor;
+      }
+    for (int i = 1; i <= n - 1; ++i)
+      for (int j = i + 1; j <= n; ++j) y[j] = y[j] - y[i] * x[j][i] / x[i][i];
+    y[n] = y[n] / x[n][n];
+    for (int i = 1; i <= n - 1; ++i) {
+      int k = n - i;
+      for (int j = k + 1; j <= n; ++j) y[k] = y[k] - y[j] * x[k][j];
+      y[k] = y[k] / x[k][k];
+    }
+  } else {
+    y[1] = y[1] / x[1][1];
+  }
+#else
+  // the same unpivoted elimination with one reciprocal per pivot and the
+  // multipliers kept for the forward substitution (FP64)
+  double rdiag[kMaxLevels + 1];
+  for (int i = 1; i <= n - 1; ++i) {
+    const double r = 1. / x[i][i];
+    rdiag[i] = r;
+    for (int k = i + 1; k <= n; ++k) {
+      const double factor = x[k][i] * r;
+      x[k][i] = factor;
+      for (int j = i + 1; j <= n; ++j) x[k][j] = x[k][j] - x[i][j] * factor;
+    }
+  }
+  rdiag[n] = 1. / x[n][n];
+  for (int i = 1; i <= n - 1; ++i)
+    for (int j = i + 1; j <= n; ++j) y[j] = y[j] - y[i] * x[j][i];
+  y[n] = y[n] * rdiag[n];
+  for (int k = n - 1; k >= 1; --k) {
+    double acc = y[k];
+    for (int j = k + 1; j <= n; ++j) acc = acc - y[j] * x[k][j];
+    y[k] = acc * rdiag[k];
+  }
+#endif
+  double sumN = 0.;
+  for (int i = 1; i <= nLev; ++i) sumN = sumN + y[i];
+  for (int i = 1; i <= nLev; ++i) y[i] = y[i] / sumN;
+  double total = 0.;
+  for (int i = 1; i <= nLev - 1; ++i)
+    for (int j = i + 1; j <= nLev; ++j) {
+      double aji = A[(size_t)(j - 1) * nLev + (i - 1)];
+      if (aji != 0.) {
+        double Eji = eD[j - 1] - eD[i - 1];
+        if (j == iup2p && i == 1 && atp > 0.) aji = aji - atp;
+        double f = aji * Eji * y[j] * m1 * m2 * m3;
+        if (f > RD(1.e-35)) total = total + f;
+      }
+    }
+  return total;
+}
+
+// forLines of update_mod: one thread per (cell, ion with data)
+__global__ void __launch_bounds__(128) atomsKernel(BalanceDev b) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int atom = blockIdx.y;
+  if (cell > b.nCells || b.state[cell] != 0) return;
+  const CellIdx c{cell, b.nCells + 1};
+  const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
+  const int elem = h[kAtElem], ion = h[kAtIon];
+  const int top = min(elem + 1, b.nstages);
+  const double x = ionAt(b, c, elem, ion);
+#if !MCX_BAL_EXACT
+  // an ion below 1e-16 per H contributes < 1e-9 of the cooling: no solve
+  if ((double)b.abun[elem] * x < kNegligibleIon) {
+    b.forSum[(size_t)atom * c.C1 + cell] = 0.;
+    return;
+  }
+#endif
+  double up = 0.;
+  if (ion < top && x > 0.) up = ionAt(b, c, elem, ion + 1) / x;
+  // forbiddenLines = fLineEm * elemAbun * ionDen * 1.9865e-16, summed where > 1e-35
+  b.forSum[(size_t)atom * c.C1 + cell] =
+      equilibriumLines(b, atom, b.te[cell], b.ne[cell], up, false, (double)b.abun[elem], x, RD(1.9865e-16));
+}
+
+// The emission phase's forLines (rec = .true., 1e-25 erg units): one thread
+// per (cell, ion with data), each ion's line total into forSum[atom][cell].
+__global__ void __launch_bounds__(128) forLinesAtomsKernel(BalanceDev b, const float* __restrict__ te,
+                                                           const float* __restrict__ ne,
+                                                           const float* __restrict__ ionDen,
+                                                           const uint8_t* __restrict__ compute) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+  const int atom = blockIdx.y;
+  const int C1 = b.nCells + 1;
+  if (cell >= C1 || !compute[cell]) return;
+  const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
+  const int elem = h[kAtElem], ion = h[kAtIon];
+  const int top = min(elem + 1, b.nstages);
+  const int e = b.xref[elem];
+  const double x = ionDen[((size_t)(ion - 1) * b.nElemUsed + (e - 1)) * C1 + cell];
+  double v = 0.;
+#if !MCX_BAL_EXACT
+  if ((double)b.abun[elem] * x >= kNegligibleIon)
+#endif
+  {
+    double up = 0.;
+    if (ion < top && x > 0.) up = (double)ionDen[((size_t)ion * b.nElemUsed + (e - 1)) * C1 + cell] / x;
+    v = equilibriumLines(b, atom, te[cell], ne[cell], up, true, (double)b.abun[elem], x, RD(1.9865e9));
+  }
+  b.forSum[(size_t)atom * C1 + cell] = v;
+}
+
+// normFor of emissionDriver: the ions' line totals summed in the reference's ion order
+__global__ void forLinesSumKernel(BalanceDev b, const uint8_t* __restrict__ compute, float* forLines) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+  const int C1 = b.nCells + 1;
+  if (cell >= C1 || !compute[cell]) return;
+  double normFor = 0.;
+  for (int atom = 0; atom < b.nAtoms; ++atom) normFor = normFor + b.forSum[(size_t)atom * C1 + cell];
+  forLines[cell] = (float)normFor;
+}
+
+// heating - cooling and the secant step of iterateT (FP64 in both precisions)
+__global__ void __launch_bounds__(128) secantKernel(BalanceDev b, int lastRound) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (cell > b.nCells || b.state[cell] != 0) return;
+  const int C1 = b.nCells + 1;
+  double coolColl = b.coolHex[cell];
+  for (int a = 0; a < b.nAtoms; ++a) coolColl = coolColl + b.forSum[(size_t)a * C1 + cell];
+  const double ne = b.ne[cell];
+  double heat = b.heat[cell];
+  double cool = b.coolA[cell] + coolColl + b.coolCollH[cell];
+  if (b.lgCompton) {
+    heat = heat + b.compHeat[cell] * ne + b.compRecoil[cell];
+    cool = cool + b.compCool[cell] * ne;
+  }
+  const int nIterateT = b.nIterT[cell];
+  const double res = heat - cool;
+  double te = b.te[cell];
+  double Thigh = b.tHigh[cell], Tlow = b.tLow[cell], resHigh = b.resHigh[cell], resLow = b.resLow[cell];
+  bool done = true;
+  if (fabs(res) >= RD(0.02) * (fabs(cool) + fabs(heat)) / 2.) {
+    if (nIterateT < 20) {
+      if (res < 0.) {
+        resLow = res;
+        Tlow = te;
+        if (Thigh != 0.) te = Tlow - (Thigh - Tlow) * resLow / (resHigh - resLow);
+        else te = te / RD(1.2);
+      } else {
+        resHigh = res;
+        Thigh = te;
+        if (Tlow != 0.) te = Tlow - (Thigh - Tlow) * resLow / (resHigh - resLow);
+        else te = te * RD(1.2);
+      }
+      if (nIterateT >= 6 && fabs(Thigh - Tlow) <= (RD(0.002) * (Thigh + Tlow))) {
+        if (res < 0.) { te = Thigh - 100.; Thigh = 0.; }
+        else { te = Tlow + 100.; Tlow = 0.; }
+      }
+      if (te <= 0.) te = 1.;
+      done = lastRound != 0;   // a caller-imposed round limit ends the cell here
+    } else {
+      if (Thigh == 0.) te = Tlow;
+      else if (Tlow == 0.) te = Thigh;
+      else te = (Thigh + Tlow) * 0.5;
+      atomicAdd(&b.counters->noTeBal, 1ull);
+    }
+  }
+  b.te[cell] = te;
+  b.tHigh[cell] = Thigh; b.tLow[cell] = Tlow; b.resHigh[cell] = resHigh; b.resLow[cell] = resLow;
+  if (done) {
+    b.state[cell] = 1;
+    if (!b.ibConv[cell]) atomicAdd(&b.counters->noIonBal, 1ull);
+  }
+}
+
+// Writes the results of the cells back to the grid (FP32) and the flags.
+__global__ void storeKernel(BalanceDev b, BalanceGrid g) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (cell > b.nCells) return;
+  const int C1 = b.nCells + 1;
+  const int8_t st = b.state[cell];
+  g.black[cell] = st == 2 ? 1 : 0;
+  g.nIterT[cell] = st == 2 ? 0 : b.nIterT[cell];
+  if (st == 2) {
+    g.converged[cell] = 0;
+    atomicAdd(&b.counters->noHit, 1ull);
+    return;
+  }
+  g.te[cell] = (float)b.te[cell];
+  g.ne[cell] = (float)b.ne[cell];
+  const size_t nI = (size_t)b.nstages * b.nElemUsed;
+  for (size_t k = 0; k < nI; ++k) g.ionDen[k * C1 + cell] = (float)b.ion[k * C1 + cell];
+  const double xH0 = b.ion[(size_t)(b.xref[1] - 1) * C1 + cell];
+  const double d = (xH0 - b.xOld[cell]) / b.xOld[cell];
+  const int conv = fabs(d) <= (double)b.xhiLimit ? 1 : 0;
+  g.converged[cell] = conv;
+  atomicAdd(&b.counters->updated, 1ull);
+  if (conv) atomicAdd(&b.counters->converged, 1ull);
+  atomicMax(&b.counters->maxIterT, (unsigned long long)b.nIterT[cell]);
+}
+
+#undef RF
+#undef RD
+
+cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStream_t s) {
+  BalanceDev& b = bd.dev;
+  const int C = b.nCells;
+  if (C <= 0) return cudaSuccess;
+  const int T = 128, nb = (C + T - 1) / T;
+  cudaError_t e = cudaMemsetAsync(b.counters, 0, sizeof(BalanceCounters), s);
+  if (e != cudaSuccess) return e;
+  photoIntegralsKernel<<<nb, T, 0, s>>>(b, g.jste);
+  loadStateKernel<<<nb, T, 0, s>>>(b, g.te, g.ne, g.ionDen);
+  const int rounds = std::min(std::max(maxRounds, 1), 20);
+  for (int r = 1; r <= rounds; ++r) {
+    ratesKernel<<<nb, T, 0, s>>>(b, g.hden);
+    if (b.nAtoms > 0) atomsKernel<<<dim3(nb, b.nAtoms), T, 0, s>>>(b);
+    secantKernel<<<nb, T, 0, s>>>(b, r == rounds && rounds < 20 ? 1 : 0);
+  }
+  storeKernel<<<nb, T, 0, s>>>(b, g);
+  return cudaGetLastError();
+}
+
+cudaError_t launchForLines(BalanceData& bd, const float* te, const float* ne, const float* ionDen,
+                           const uint8_t* compute, float* forLines, cudaStream_t s) {
+  BalanceDev& b = bd.dev;
+  const int C1 = b.nCells + 1, T = 128, nb = (C1 + T - 1) / T;
+  if (b.nAtoms <= 0) return cudaSuccess;
+  forLinesAtomsKernel<<<dim3(nb, b.nAtoms), T, 0, s>>>(b, te, ne, ionDen, compute);
+  forLinesSumKernel<<<nb, T, 0, s>>>(b, compute, forLines);
+  return cudaGetLastError();
+}
+
+}  // namespace MCX_BAL_NS
+}  // namespace mcx

@@ -350,6 +350,10 @@ struct mcx_ctx {
   std::unique_ptr<BalanceData> balance;
   DBuf<int32_t> lgConverged, lgBlack, nIterT;
   DBuf<float> forLines;
+  // mcx_state_save snapshot
+  DBuf<float> snapTe, snapNe, snapTeOld, snapNeOld, snapIonDen;
+  DBuf<int32_t> snapConverged;
+  bool haveSnapshot = false;
   bool haveOpacity = false, haveRecPDF = false, haveDustPDF = false;
 };
 
@@ -453,6 +457,38 @@ extern "C" int mcx_last_error(const mcx_ctx* c, char* buf, size_t len) {
   if (!buf || len == 0) return MCX_ERR_INPUT;
   const std::string& m = c ? c->err : g_setupError;
   std::snprintf(buf, len, "%s", m.c_str());
+  return MCX_OK;
+}
+
+extern "C" int mcx_state_save(mcx_ctx* c) {
+  if (!c) return MCX_ERR_INPUT;
+  if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_state_save: no model loaded");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  struct P { DBuf<float>* dst; DBuf<float>* src; } fp[] = {
+      {&c->snapTe, &c->te}, {&c->snapNe, &c->ne}, {&c->snapTeOld, &c->teOld}, {&c->snapNeOld, &c->neOld},
+      {&c->snapIonDen, &c->ionDen}};
+  for (auto& q : fp) {
+    if (q.dst->n != q.src->n) CK(q.dst->alloc(q.src->n), "alloc snapshot");
+    CK(cudaMemcpyAsync(q.dst->p, q.src->p, q.src->bytes(), cudaMemcpyDeviceToDevice, c->stream), "snapshot");
+  }
+  if (c->snapConverged.n != c->lgConverged.n) CK(c->snapConverged.alloc(c->lgConverged.n), "alloc snapshot");
+  CK(cudaMemcpyAsync(c->snapConverged.p, c->lgConverged.p, c->lgConverged.bytes(), cudaMemcpyDeviceToDevice,
+                     c->stream), "snapshot");
+  c->haveSnapshot = true;
+  return MCX_OK;
+}
+
+extern "C" int mcx_state_restore(mcx_ctx* c) {
+  if (!c) return MCX_ERR_INPUT;
+  if (!c->loaded || !c->haveSnapshot) return fail(c, MCX_ERR_STATE, "mcx_state_restore: no snapshot");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  struct P { DBuf<float>* dst; DBuf<float>* src; } fp[] = {
+      {&c->te, &c->snapTe}, {&c->ne, &c->snapNe}, {&c->teOld, &c->snapTeOld}, {&c->neOld, &c->snapNeOld},
+      {&c->ionDen, &c->snapIonDen}};
+  for (auto& q : fp)
+    CK(cudaMemcpyAsync(q.dst->p, q.src->p, q.src->bytes(), cudaMemcpyDeviceToDevice, c->stream), "restore");
+  CK(cudaMemcpyAsync(c->lgConverged.p, c->snapConverged.p, c->snapConverged.bytes(), cudaMemcpyDeviceToDevice,
+                     c->stream), "restore");
   return MCX_OK;
 }
 
@@ -625,6 +661,7 @@ extern "C" int mcx_load(mcx_ctx* c, const mcx_setup* m) {
   CK(cudaMemset(c->forLines.p, 0, c->forLines.bytes()), "memset");
   c->emission.reset();
   c->balance.reset();
+  c->haveSnapshot = false;
   if (c->lgGas) {
     std::string em = emissionDataCreate(s, c->emission);
     if (!em.empty()) return fail(c, MCX_ERR_INPUT, "mcx_load: " + em);
@@ -764,7 +801,9 @@ extern "C" int mcx_emission(mcx_ctx* c, const mcx_phase_opts* opts, mcx_phase_st
   CK(launchEmissionGaunt(c->emission->dev, c->gauntTeOld, c->stream), "emission gaunt");
   const float* forLines = nullptr;
   if (c->balance && c->balance->dev.nAtoms > 0) {
-    CK(launchForLinesEmission(*c->balance, c->te.p, c->ne.p, c->ionDen.p, c->computeMask.p, c->forLines.p, c->stream),
+    const int prec = (opts && opts->precision == MCX_PHASE_MIXED) ? kBalMixed : kBalFp64;
+    CK(launchForLinesEmission(*c->balance, c->te.p, c->ne.p, c->ionDen.p, c->computeMask.p, c->forLines.p, prec,
+                              c->stream),
        "emission forLines");
     forLines = c->forLines.p;
   }
@@ -936,7 +975,9 @@ extern "C" int mcx_balance(mcx_ctx* c, const mcx_balance_opts* opts, mcx_balance
   if (!c) return MCX_ERR_INPUT;
   if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_balance: no model loaded");
   if (!c->lgGas || !c->balance) return fail(c, MCX_ERR_STATE, "mcx_balance: the grid holds no gas");
-  if (opts && opts->precision != MCX_BAL_FP64) return fail(c, MCX_ERR_INPUT, "mcx_balance: unknown precision");
+  if (opts && opts->precision != MCX_BAL_FP64 && opts->precision != MCX_BAL_MIXED)
+    return fail(c, MCX_ERR_INPUT, "mcx_balance: unknown precision");
+  const int prec = (opts && opts->precision == MCX_BAL_MIXED) ? kBalMixed : kBalFp64;
   const int rounds = (opts && opts->max_rounds > 0) ? opts->max_rounds : 20;
   if (rounds > 20) return fail(c, MCX_ERR_INPUT, "mcx_balance: max_rounds above maxIterateT (20)");
   CK(cudaSetDevice(c->device), "cudaSetDevice");
@@ -946,7 +987,7 @@ extern "C" int mcx_balance(mcx_ctx* c, const mcx_balance_opts* opts, mcx_balance
   CK(cudaMemcpyAsync(c->teOld.p, c->te.p, C1 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream), "TeOld");
   CK(cudaMemcpyAsync(c->neOld.p, c->ne.p, C1 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream), "NeOld");
   BalanceGrid g{c->jste.p, c->hden.p, c->te.p, c->ne.p, c->ionDen.p, c->lgConverged.p, c->lgBlack.p, c->nIterT.p};
-  CK(launchBalance(*c->balance, g, rounds, c->stream), "balance kernels");
+  CK(launchBalance(*c->balance, g, rounds, prec, c->stream), "balance kernels");
   CK(cudaEventRecord(c->ev1, c->stream), "event");
   BalanceCounters h{};
   CK(cudaMemcpyAsync(&h, c->balance->dev.counters, sizeof(h), cudaMemcpyDeviceToHost, c->stream), "d2h counters");

@@ -131,9 +131,9 @@ class Context:
         self._check(lib().mcx_opacity(self._h, C.byref(o), C.byref(st)))
         return st
 
-    def emission(self, n_iterate_mc: int = 1) -> abi.PhaseStats:
+    def emission(self, n_iterate_mc: int = 1, precision: int = abi.PHASE_EXACT) -> abi.PhaseStats:
         st = abi.PhaseStats()
-        o = abi.PhaseOpts(n_iterate_mc=n_iterate_mc)
+        o = abi.PhaseOpts(n_iterate_mc=n_iterate_mc, precision=precision)
         self._check(lib().mcx_emission(self._h, C.byref(o), C.byref(st)))
         return st
 
@@ -152,6 +152,13 @@ class Context:
         st = abi.BalanceStats()
         self._check(lib().mcx_balance(self._h, C.byref(o), C.byref(st)))
         return st
+
+    def state_save(self) -> None:
+        """Device-side snapshot of Te, Ne, ionDen, TeOld, NeOld, lgConverged."""
+        self._check(lib().mcx_state_save(self._h))
+
+    def state_restore(self) -> None:
+        self._check(lib().mcx_state_restore(self._h))
 
     def normalize_j(self) -> None:
         self._check(lib().mcx_normalize_j(self._h))

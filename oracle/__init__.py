@@ -287,7 +287,9 @@ def _balance_lib():
         l.orc_equilibrium.argtypes = [C.POINTER(BalanceIn), C.c_int32, C.c_double, C.c_double, C.c_double, C.c_int32,
                                       _P, _P]
         l.orc_equilibrium.restype = C.c_int
-        l.orc_for_lines_emission.argtypes = [C.POINTER(BalanceIn), _P, _P, _P, _P]
+        l.orc_for_lines_emission.argtypes = [C.POINTER(BalanceIn), _P, _P, _P, _P, _P]
+        l.orc_balance_trace.argtypes = [C.POINTER(BalanceIn), C.POINTER(BalanceState), C.c_int32, _P]
+        l.orc_balance_trace.restype = C.c_int
         l.orc_for_lines_emission.restype = C.c_int
         l._balance_ready = True
     return l
@@ -361,12 +363,34 @@ def balance(tables: BalanceTables, jste, te, ne, ionden, nthreads: int = 1):
     return te, ne, ionden, conv, black, nit, stats
 
 
-def for_lines_emission(tables: BalanceTables, te, ne, ionden) -> np.ndarray:
-    """normFor of each cell: the emission phase's forbidden-line total [1e-25 erg/s per gas density]."""
+def for_lines_emission(tables: BalanceTables, te, ne, ionden, compute=None) -> np.ndarray:
+    """normFor of each cell (with compute[c] = 1): the emission phase's
+    forbidden-line total [1e-25 erg/s per gas density]."""
     C1 = tables.info.n_cells + 1
     te = np.ascontiguousarray(te, dtype=np.float32)
     ne = np.ascontiguousarray(ne, dtype=np.float32)
     ionden = np.ascontiguousarray(ionden, dtype=np.float32).reshape(-1)
+    comp = None if compute is None else np.ascontiguousarray(compute, dtype=np.uint8)
     out = np.zeros(C1, dtype=np.float64)
-    _balance_lib().orc_for_lines_emission(C.byref(tables.s), _p(te), _p(ne), _p(ionden), _p(out))
+    _balance_lib().orc_for_lines_emission(C.byref(tables.s), _p(te), _p(ne), _p(ionden), _p(comp), _p(out))
     return out
+
+
+def balance_trace(tables: BalanceTables, jste, te, ne, ionden, cell: int) -> np.ndarray:
+    """The T-iterations of one cell: rows of (Te, heating, cooling, Ne, X(H0))."""
+    i = tables.info
+    C1 = i.n_cells + 1
+    jste = np.ascontiguousarray(jste, dtype=np.float64)
+    te = np.array(te, dtype=np.float32, copy=True)
+    ne = np.array(ne, dtype=np.float32, copy=True)
+    ionden = np.array(ionden, dtype=np.float32, copy=True).reshape(-1)
+    conv = np.zeros(C1, dtype=np.int32)
+    black = np.zeros(C1, dtype=np.int32)
+    nit = np.zeros(C1, dtype=np.int32)
+    tables.s.jste = _p(jste)
+    st = BalanceState(te=_p(te), ne=_p(ne), ionden=_p(ionden), converged=_p(conv), black=_p(black),
+                      n_iter_t=_p(nit))
+    tr = np.zeros((20, 5), dtype=np.float64)
+    n = _balance_lib().orc_balance_trace(C.byref(tables.s), C.byref(st), cell, _p(tr))
+    tables.s.jste = None
+    return tr[:n]

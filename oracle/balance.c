@@ -769,8 +769,17 @@ static void therm_balance(const orc_balance_in* in, const cell_t* c, double* hea
 }
 
 /* updateCell + iterateT for one cell, source/update_mod.f90:15-482 */
+static void update_cell_tr(const orc_balance_in* in, orc_balance_state* st, int cell, cell_t* c, double* J,
+                           orc_balance_stats* s, double* trace);
+
 static void update_cell(const orc_balance_in* in, orc_balance_state* st, int cell, cell_t* c, double* J,
                         orc_balance_stats* s) {
+    update_cell_tr(in, st, cell, c, J, s, NULL);
+}
+
+/* the same with a record of each T-iteration: Te, heating, cooling, Ne, X(H0) */
+static void update_cell_tr(const orc_balance_in* in, orc_balance_state* st, int cell, cell_t* c, double* J,
+                           orc_balance_stats* s, double* trace) {
     const int C1 = in->n_cells + 1, nb = in->nbins, ns = in->nstages, E = in->n_elem_used;
     int hit = 0;
     for (int b = 0; b < nb; ++b) {
@@ -808,6 +817,10 @@ static void update_cell(const orc_balance_in* in, orc_balance_state* st, int cel
         lgIBConv = ion_balance(in, c);
         double heat, cool;
         therm_balance(in, c, &heat, &cool);
+        if (trace && nIterateT <= 20) {
+            double* t = trace + (nIterateT - 1) * 5;
+            t[0] = c->te; t[1] = heat; t[2] = cool; t[3] = c->ne; t[4] = c->ion[1][1];
+        }
         double res = heat - cool;
         if (fabs(res) >= thLimit * (fabs(cool) + fabs(heat)) / 2.) {
             if (nIterateT < 20) {
@@ -896,11 +909,12 @@ int orc_balance(const orc_balance_in* in, orc_balance_state* st, int32_t nthread
 /* forLines of emission_mod (rec = .true., scale 1.9865e9) and the normFor sum
  * of emissionDriver (source/emission_mod.f90:1481-1524, :1780-1795) */
 int orc_for_lines_emission(const orc_balance_in* in, const float* te, const float* ne, const float* ionden,
-                           double* for_lines) {
+                           const uint8_t* compute, double* for_lines) {
     const int C1 = in->n_cells + 1, ns = in->nstages, E = in->n_elem_used;
     double em[32 * 32];
     for (int cell = 0; cell < C1; ++cell) {
         double normFor = 0.;
+        if (compute && !compute[cell]) { for_lines[cell] = 0.; continue; }
         for (int elem = 3; elem <= NEL; ++elem) {
             if (!on(in, elem)) continue;
             const int top = elem + 1 < ns ? elem + 1 : ns;
@@ -922,4 +936,17 @@ int orc_for_lines_emission(const orc_balance_in* in, const float* te, const floa
         for_lines[cell] = normFor;
     }
     return 0;
+}
+
+/* updateCell of one cell with a record of its T-iterations (trace[20][5]:
+ * Te, heating, cooling, Ne, X(H0)); returns the number of T-iterations. */
+int orc_balance_trace(const orc_balance_in* in, orc_balance_state* st, int32_t cell, double* trace) {
+    cell_t* c = (cell_t*)malloc(sizeof(cell_t));
+    double* J = (double*)malloc(sizeof(double) * (size_t)in->nbins);
+    orc_balance_stats s;
+    memset(&s, 0, sizeof(s));
+    update_cell_tr(in, st, cell, c, J, &s, trace);
+    free(J);
+    free(c);
+    return st->n_iter_t[cell];
 }

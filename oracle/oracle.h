@@ -223,17 +223,22 @@ typedef struct orc_balance_stats {
  * Gas only (no grains).  Returns 0. */
 int orc_balance(const orc_balance_in* in, orc_balance_state* st, int32_t nthreads, orc_balance_stats* stats);
 
+/* updateCell of one cell recording each T-iteration in trace[20][5] (Te,
+ * heating, cooling, Ne, X(H0)); returns the number of T-iterations. */
+int orc_balance_trace(const orc_balance_in* in, orc_balance_state* st, int32_t cell, double* trace);
+
 /* equilibrium (source/emission_mod.f90:2505-3007) for atom slot `atom`:
  * level populations n[nLev] and line emissivities em[i][j] (lower i, upper j,
  * [nLev][nLev], zero where a(j,i) = 0).  rec selects the recombination term. */
 int orc_equilibrium(const orc_balance_in* in, int32_t atom, double te, double ne, double ion_den_up,
                     int32_t rec, double* n, double* em);
 
-/* The emission phase's forbidden-line total normFor of each cell
- * (forLines with rec = .true., source/emission_mod.f90:1481-1524 and
- * :1780-1795), in its units of 1e-25 erg/s per unit gas density. */
+/* The emission phase's forbidden-line total normFor of each cell with
+ * compute[c] = 1 (all cells if compute is NULL; forLines with rec = .true.,
+ * source/emission_mod.f90:1481-1524 and :1780-1795), in its units of 1e-25
+ * erg/s per unit gas density. */
 int orc_for_lines_emission(const orc_balance_in* in, const float* te, const float* ne, const float* ionden,
-                           double* for_lines);
+                           const uint8_t* compute, double* for_lines);
 
 #ifdef __cplusplus
 }

@@ -88,3 +88,60 @@ def test_emission_forbidden_lines(decks, data_dir, oracle_lib):
     assert np.all(fl_o[1:] > 0)
     np.testing.assert_allclose(fl[1:], fl_o[1:], rtol=2e-6)
     ctx.close()
+
+
+@pytest.mark.parametrize("name", ["lognormal_small", "xray_small"])
+def test_balance_mixed_precision(decks, data_dir, oracle_lib, name):
+    """The production balance (FP32 rates, collision strengths and
+    exponentials; FP64 level populations, ladder and bracketing; ions below
+    1e-16 per H skip the atom solve) against the FP64 oracle: Te and Ne to
+    1e-4, ionic fractions above 1e-6 to 1e-3, on the cells whose T-iteration
+    took the same path."""
+    s = Setup(decks[name], data_dir)
+    ctx = Context(0)
+    ctx.load(s)
+    te0, ne0, ion0 = s.get(abi.ARR_TE), s.get(abi.ARR_NE), s.get(abi.ARR_IONDEN)
+    j = _run_j(ctx, s, 30000, 11)
+    T = oracle_lib.BalanceTables(s)
+    te_o, ne_o, ion_o, conv_o, black_o, nit_o, st_o = oracle_lib.balance(T, j, te0, ne0, ion0, nthreads=8)
+    ctx.balance(precision=abi.BAL_MIXED)
+    te, ne = ctx.get(abi.ARR_TE), ctx.get(abi.ARR_NE)
+    ion = ctx.get(abi.ARR_IONDEN).reshape(-1)
+    nit = ctx.get(abi.ARR_N_ITER_T)
+    same = nit[1:] == nit_o[1:]
+    assert same.mean() >= 0.98
+    np.testing.assert_allclose(te[1:][same], te_o[1:][same], rtol=1e-4)
+    np.testing.assert_allclose(ne[1:][same], ne_o[1:][same], rtol=1e-4)
+    C1 = s.n_cells + 1
+    a = ion.reshape(-1, C1)[:, 1:][:, same]
+    b = ion_o.reshape(-1, C1)[:, 1:][:, same]
+    big = b > 1e-6
+    np.testing.assert_allclose(a[big], b[big], rtol=1e-3)
+    ctx.close()
+
+
+def test_emission_forbidden_lines_mixed(decks, data_dir, oracle_lib):
+    s = Setup(decks["xray_small"], data_dir)
+    ctx = Context(0)
+    ctx.load(s)
+    ctx.opacity(1)
+    ctx.emission(1, precision=abi.PHASE_MIXED)
+    fl = ctx.get(abi.ARR_FOR_LINES)
+    T = oracle_lib.BalanceTables(s)
+    fl_o = oracle_lib.for_lines_emission(T, s.get(abi.ARR_TE), s.get(abi.ARR_NE), s.get(abi.ARR_IONDEN))
+    np.testing.assert_allclose(fl[1:], fl_o[1:], rtol=1e-4)
+    ctx.close()
+
+
+def test_state_save_restore(decks, data_dir):
+    s = Setup(decks["h_small"], data_dir)
+    ctx = Context(0)
+    ctx.load(s)
+    ctx.state_save()
+    te0 = ctx.get(abi.ARR_TE)
+    _run_j(ctx, s, 5000, 3)
+    ctx.balance()
+    assert not np.array_equal(ctx.get(abi.ARR_TE), te0)
+    ctx.state_restore()
+    np.testing.assert_array_equal(ctx.get(abi.ARR_TE), te0)
+    ctx.close()
