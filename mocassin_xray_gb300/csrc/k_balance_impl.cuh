@@ -290,27 +290,38 @@ __device__ bool ionBalance(const BalanceDev& b, const CellIdx& c, double te, dou
   const bool heOn = b.xref[zHe] > 0;
   const int C1 = c.C1;
   const real teR = (real)te;
+  // the Te-only terms are the same on every X-iteration (the reference
+  // recomputes them on each recursive call)
+  real expFact = RF(157893.94) / teR;
+  if (expFact > (real)75.) expFact = (real)75.;
+  const real collIonH0 = RF(2.75E-16) * teR * sqrt(teR) * (RF(157893.94) / teR + (real)2.) * exp(-expFact);
+  double cxHHe[3][3] = {{0., 0., 0.}, {0., 0., 0.}, {0., 0., 0.}};
+  for (int elem = 1; elem <= 2; ++elem)
+    for (int ion = 1; ion <= min(elem, ns - 1); ++ion) cxHHe[elem][ion] = chexFit(b, elem, ion, teR);
   for (int nIterateX = 1;; ++nIterateX) {
     bool lgConv = true;
     double ionRatio[3][3] = {{0., 0., 0.}, {0., 0., 0.}, {0., 0., 0.}};
     double ionProd[3][3] = {{1., 1., 1.}, {1., 1., 1.}, {1., 1., 1.}};
     double den[3] = {1., 1., 1.};
-    real expFact = RF(157893.94) / teR;
-    if (expFact > (real)75.) expFact = (real)75.;
-    real collIonH = RF(2.75E-16) * teR * sqrt(teR) * (RF(157893.94) / teR + (real)2.) * exp(-expFact);
+    real collIonH = collIonH0;
     const double HIOld = ionAt(b, c, zH, 1);
     const double HeIOld = heOn ? ionAt(b, c, zHe, 1) : 0.;
     const double HeIIOld = heOn ? ionAt(b, c, zHe, 2) : 0.;
     for (int elem = 1; elem <= 2; ++elem) {
       if (!b.xref[elem]) continue;
       for (int ion = 1; ion <= min(elem, ns - 1); ++ion) {
-        double cx = chexFit(b, elem, ion, teR);
+        double cx = cxHHe[elem][ion];
         int outShell = outerOf(b, elem, elem - ion + 1)[0];
         if (elem > 1 || ion > 1) collIonH = 0;
         int p0 = b.pairShell0[(b.xref[elem] - 1) * 32 + (ion - 1)];
         double pi = b.pi1[(size_t)(p0 + outShell - 1) * C1 + c.cell];
-        ionRatio[elem][ion] = (pi + (double)collIonH * ne + 0.) /
-                              (ne * b.alpha[pairOff(b, c, elem, ion)] + cx * hden * HIOld);
+        const double num = pi + (double)collIonH * ne + 0.;
+        const double dnm = ne * b.alpha[pairOff(b, c, elem, ion)] + cx * hden * HIOld;
+#if MCX_BAL_EXACT
+        ionRatio[elem][ion] = num / dnm;
+#else
+        ionRatio[elem][ion] = (double)((float)num / (float)dnm);   // a rate ratio: FP32
+#endif
       }
     }
     for (int elem = 1; elem <= 2; ++elem) {
@@ -351,7 +362,11 @@ __device__ bool ionBalance(const BalanceDev& b, const CellIdx& c, double te, dou
           for (int nelec = 2; nelec <= nAug; ++nelec) {
             int maxim = min(ion + nelec - 1, lim);
             double xm = ionAt(b, c, elem, maxim);
+#if MCX_BAL_EXACT
             double ratio = xm > 1e-30 ? ionAt(b, c, elem, ion) / xm : 1.;
+#else
+            double ratio = xm > 1e-30 ? (double)((float)ionAt(b, c, elem, ion) / (float)xm) : 1.;
+#endif
             out[maxim] = out[maxim] +
                          pi * (double)b.auger[(((size_t)(elem - 1) * kNE + (ion - 1)) * 10 + (shell - 1)) * 10 + (nelec - 1)] * ratio;
           }
@@ -363,7 +378,12 @@ __device__ bool ionBalance(const BalanceDev& b, const CellIdx& c, double te, dou
       double sumMat = 1.;
       const int top = min(ns, elem + 1);
       for (int ion = 2; ion <= top; ++ion) {
+#if MCX_BAL_EXACT
         mat[ion] = mat[ion - 1] * out[ion - 1] / inn[ion - 1];
+#else
+        // the rate ratio in FP32, the ladder product and its normalisation in FP64
+        mat[ion] = mat[ion - 1] * (double)((float)out[ion - 1] / (float)inn[ion - 1]);
+#endif
         sumMat = sumMat + mat[ion];
       }
       sumMat = 1. / sumMat;
@@ -376,7 +396,7 @@ __device__ bool ionBalance(const BalanceDev& b, const CellIdx& c, double te, dou
 #if MCX_BAL_EXACT
           v = pow(10., 0.5 * (log10(old) + log10(mat[ion] * sumMat)));
 #else
-          v = sqrt(old) * sqrt(mat[ion] * sumMat);   // the same geometric mean
+          v = sqrt(old * (mat[ion] * sumMat));   // the same geometric mean
 #endif
         } else {
           v = mat[ion] * sumMat;
