@@ -338,6 +338,36 @@ int  mcx_transport(mcx_ctx* ctx, const mcx_transport_opts* opts, mcx_transport_s
  * escaped /8 in octant mode (source/iteration_mod.f90:1002-1031). */
 int  mcx_normalize_j(mcx_ctx* ctx);
 
+/* ------------------------------------------------------ one MC iteration */
+/* One pass of iterateMC's loop body (source/iteration_mod.f90:98-1260) for the
+ * stellar source: mcx_opacity, mcx_emission, mcx_transport (Jste cleared
+ * first), mcx_normalize_j and mcx_balance, in that order on the context's
+ * stream.  The balance's ~63 launches are captured as a CUDA graph on first
+ * use and replayed.  The convergence test of :1270-1480 is left to the caller
+ * (stats.balance.converged against nCells and minConvergence). */
+typedef struct mcx_iterate_opts {
+    int32_t n_iterate_mc;           /* nIterateMC (1-based): the skip rule applies when > 1 */
+    int32_t transport_precision;    /* MCX_PREC_*                                          */
+    int32_t balance_precision;      /* MCX_BAL_*                                           */
+    int32_t emission_precision;     /* MCX_PHASE_*                                         */
+    int64_t n_packets;              /* nPhotons(1)                                         */
+    uint64_t seed;                  /* Philox key                                          */
+    uint64_t counter_base;          /* global id of the iteration's first packet           */
+    int32_t reserved[8];
+} mcx_iterate_opts;
+
+typedef struct mcx_iterate_stats {
+    mcx_phase_stats opacity;
+    mcx_phase_stats emission;
+    mcx_transport_stats transport;
+    mcx_balance_stats balance;
+    float   total_ms;               /* CUDA-event time of the whole iteration              */
+    float   reserved_f[3];
+    int64_t reserved[4];
+} mcx_iterate_stats;
+
+int  mcx_iterate(mcx_ctx* ctx, const mcx_iterate_opts* opts, mcx_iterate_stats* stats);
+
 
 /* ------------------------------------------- transport without allocation */
 /* No counterpart in the reference.  Some callers cannot allocate device

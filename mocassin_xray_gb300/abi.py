@@ -68,6 +68,12 @@ class BalanceStats(C.Structure):
                 ("kernel_ms", C.c_float), ("reserved", C.c_int64 * 4)]
 
 
+class IterateOpts(C.Structure):
+    _fields_ = [("n_iterate_mc", C.c_int32), ("transport_precision", C.c_int32), ("balance_precision", C.c_int32),
+                ("emission_precision", C.c_int32), ("n_packets", C.c_int64), ("seed", C.c_uint64),
+                ("counter_base", C.c_uint64), ("reserved", C.c_int32 * 8)]
+
+
 class PhaseOpts(C.Structure):
     _fields_ = [("n_iterate_mc", C.c_int32), ("precision", C.c_int32), ("reserved", C.c_int32 * 6)]
 
@@ -112,6 +118,12 @@ NOALLOC_SCRATCH_BYTES = 64 * 1024 * 1024
 
 # exported symbols and their signatures: (name, restype, argtypes)
 _P = C.c_void_p
+class IterateStats(C.Structure):
+    _fields_ = [("opacity", PhaseStats), ("emission", PhaseStats), ("transport", TransportStats),
+                ("balance", BalanceStats), ("total_ms", C.c_float), ("reserved_f", C.c_float * 3),
+                ("reserved", C.c_int64 * 4)]
+
+
 SIGNATURES = [
     ("mcx_setup_from_input", C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(SetupOpts), C.POINTER(_P)]),
     ("mcx_setup_free", None, [_P]),
@@ -135,6 +147,7 @@ SIGNATURES = [
     ("mcx_transport", C.c_int, [_P, C.POINTER(TransportOpts), C.POINTER(TransportStats)]),
     ("mcx_normalize_j", C.c_int, [_P]),
     ("mcx_balance", C.c_int, [_P, C.POINTER(BalanceOpts), C.POINTER(BalanceStats)]),
+    ("mcx_iterate", C.c_int, [_P, C.POINTER(IterateOpts), C.POINTER(IterateStats)]),
     ("mcx_timer_start", C.c_int, [_P]),
     ("mcx_timer_stop", C.c_int, [_P, C.POINTER(C.c_float)]),
     ("mcx_version", C.c_char_p, []),

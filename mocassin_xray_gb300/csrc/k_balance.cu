@@ -70,6 +70,8 @@ T* carve(std::vector<void*>& blocks, size_t n, std::string& err) {
 }  // namespace
 
 BalanceData::~BalanceData() {
+  for (auto& g : graph)
+    if (g) cudaGraphExecDestroy(g);
   for (int i = 0; i < nBlocks; ++i)
     if (blocks[i]) cudaFree(blocks[i]);
 }
@@ -199,8 +201,45 @@ std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out)
   return "";
 }
 
+namespace {
+bool sameGrid(const BalanceGrid& a, const BalanceGrid& b) {
+  return a.jste == b.jste && a.hden == b.hden && a.te == b.te && a.ne == b.ne && a.ionDen == b.ionDen &&
+         a.converged == b.converged && a.black == b.black && a.nIterT == b.nIterT;
+}
+}  // namespace
+
 cudaError_t launchBalance(BalanceData& bd, const BalanceGrid& g, int maxRounds, int precision, cudaStream_t s) {
-  return precision == kBalMixed ? bal_mixed::launch(bd, g, maxRounds, s) : bal_f64::launch(bd, g, maxRounds, s);
+  auto direct = [&]() {
+    return precision == kBalMixed ? bal_mixed::launch(bd, g, maxRounds, s) : bal_f64::launch(bd, g, maxRounds, s);
+  };
+  if (maxRounds != 20) return direct();
+  const int k = precision == kBalMixed ? 1 : 0;
+  if (bd.graph[k] && !sameGrid(bd.graphGrid[k], g)) {
+    cudaGraphExecDestroy(bd.graph[k]);
+    bd.graph[k] = nullptr;
+  }
+  if (!bd.graph[k]) {
+    // capture the ~63 launches of one balance once; replays skip their launch overhead
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return direct();
+    cudaError_t le = direct();
+    e = cudaStreamEndCapture(s, &graph);
+    if (le != cudaSuccess || e != cudaSuccess || !graph) {
+      if (graph) cudaGraphDestroy(graph);
+      cudaGetLastError();
+      return direct();
+    }
+    e = cudaGraphInstantiate(&bd.graph[k], graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      bd.graph[k] = nullptr;
+      cudaGetLastError();
+      return direct();
+    }
+    bd.graphGrid[k] = g;
+  }
+  return cudaGraphLaunch(bd.graph[k], s);
 }
 
 cudaError_t launchForLinesEmission(BalanceData& bd, const float* te, const float* ne, const float* ionDen,

@@ -96,17 +96,6 @@ struct BalanceDev {
   BalanceCounters* counters;
 };
 
-class BalanceData {
- public:
-  ~BalanceData();
-  BalanceDev dev{};
-  void* blocks[64] = {};
-  int nBlocks = 0;
-};
-
-// Builds the device tables and the per-cell work arrays of a set-up.
-std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out);
-
 // Grid arrays the balance reads and writes (device memory).
 struct BalanceGrid {
   const double* jste;          // [nbins][C+1], normalised
@@ -114,6 +103,21 @@ struct BalanceGrid {
   float* te, *ne, *ionDen;     // [C+1], [C+1], [nstages][nElemUsed][C+1]
   int32_t* converged, *black, *nIterT;   // [C+1]
 };
+
+class BalanceData {
+ public:
+  ~BalanceData();
+  BalanceDev dev{};
+  void* blocks[64] = {};
+  int nBlocks = 0;
+  // the whole balance (counters reset, J pass, 20 rounds, store) captured as
+  // one CUDA graph per precision, replayed while the grid arrays stay put
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  BalanceGrid graphGrid[2] = {};
+};
+
+// Builds the device tables and the per-cell work arrays of a set-up.
+std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out);
 
 constexpr int kBalFp64 = 0;    // FP64 throughout (the plain path)
 constexpr int kBalMixed = 1;   // FP32 rates / splines / exponentials, FP64 solves and bracketing

@@ -1005,6 +1005,51 @@ extern "C" int mcx_balance(mcx_ctx* c, const mcx_balance_opts* opts, mcx_balance
   return MCX_OK;
 }
 
+extern "C" int mcx_iterate(mcx_ctx* c, const mcx_iterate_opts* o, mcx_iterate_stats* stats) {
+  if (!c || !o) return fail(c, MCX_ERR_INPUT, "mcx_iterate: null argument");
+  if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_iterate: no model loaded");
+  if (o->n_packets <= 0) return fail(c, MCX_ERR_INPUT, "mcx_iterate: n_packets must be positive");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  mcx_iterate_stats st{};
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  CK(cudaEventCreate(&t0), "event");
+  CK(cudaEventCreate(&t1), "event");
+  CK(cudaEventRecord(t0, c->stream), "event");
+  mcx_phase_opts po{};
+  po.n_iterate_mc = o->n_iterate_mc;
+  int rc = mcx_opacity(c, &po, &st.opacity);
+  if (rc == MCX_OK) {
+    po.precision = o->emission_precision;
+    rc = mcx_emission(c, &po, &st.emission);
+  }
+  if (rc == MCX_OK) {
+    mcx_transport_opts to{};
+    to.istar = 1;
+    to.precision = o->transport_precision;
+    to.n_packets = o->n_packets;
+    to.seed = o->seed;
+    to.counter_base = o->counter_base;
+    to.n_photons_norm = o->n_packets;
+    to.zero_estimators = 1;
+    rc = mcx_transport(c, &to, &st.transport);
+  }
+  if (rc == MCX_OK) rc = mcx_normalize_j(c);
+  if (rc == MCX_OK) {
+    mcx_balance_opts bo{};
+    bo.precision = o->balance_precision;
+    rc = mcx_balance(c, &bo, &st.balance);
+  }
+  if (rc == MCX_OK) {
+    cudaEventRecord(t1, c->stream);
+    cudaEventSynchronize(t1);
+    cudaEventElapsedTime(&st.total_ms, t0, t1);
+    if (stats) *stats = st;
+  }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  return rc;
+}
+
 extern "C" int mcx_timer_start(mcx_ctx* c) {
   if (!c) return MCX_ERR_INPUT;
   CK(cudaEventRecord(c->tev0, c->stream), "timer");

@@ -153,6 +153,17 @@ class Context:
         self._check(lib().mcx_balance(self._h, C.byref(o), C.byref(st)))
         return st
 
+    def iterate(self, n_packets: int, n_iterate_mc: int = 1, seed: int = 0, counter_base: int = 0,
+                transport_precision: int = abi.PREC_FP32_GEOM, balance_precision: int = abi.BAL_MIXED,
+                emission_precision: int = abi.PHASE_MIXED) -> abi.IterateStats:
+        """One MC iteration (opacity, emission, transport, normalisation, balance) in one ABI call."""
+        o = abi.IterateOpts(n_iterate_mc=n_iterate_mc, transport_precision=transport_precision,
+                            balance_precision=balance_precision, emission_precision=emission_precision,
+                            n_packets=n_packets, seed=seed, counter_base=counter_base)
+        st = abi.IterateStats()
+        self._check(lib().mcx_iterate(self._h, C.byref(o), C.byref(st)))
+        return st
+
     def state_save(self) -> None:
         """Device-side snapshot of Te, Ne, ionDen, TeOld, NeOld, lgConverged."""
         self._check(lib().mcx_state_save(self._h))

@@ -59,3 +59,33 @@ def test_iterate_mc_stops_at_min_convergence(decks, data_dir):
     s = Setup(decks["h_small"], data_dir)
     reps = iterate_mc(s, seed=2, n_photons=20000, max_iterations=5, min_convergence=0.0)
     assert len(reps) == 1
+
+
+def test_mcx_iterate_equals_phase_sequence(decks, data_dir):
+    """mcx_iterate (one ABI call, balance replayed from a CUDA graph) against
+    the five phase calls made one by one from the same state."""
+    s = Setup(decks["lognormal_small"], data_dir)
+    ctx = Context(0)
+    ctx.load(s)
+    ctx.state_save()
+    st = ctx.iterate(20000, seed=5, transport_precision=abi.PREC_FP64, balance_precision=abi.BAL_FP64,
+                     emission_precision=abi.PHASE_EXACT)
+    assert st.total_ms > 0 and st.balance.cells_updated > 0
+    te1, nit1 = ctx.get(abi.ARR_TE), ctx.get(abi.ARR_N_ITER_T)
+    ctx.state_restore()
+    ctx.opacity(1)
+    ctx.emission(1)
+    ctx.transport(20000, seed=5, precision=abi.PREC_FP64)
+    ctx.normalize_j()
+    ctx.balance(max_rounds=19)          # the direct launch path (no graph)
+    ctx.state_restore()
+    ctx.balance()                       # graph path, same J
+    te2, nit2 = ctx.get(abi.ARR_TE), ctx.get(abi.ARR_N_ITER_T)
+    same = nit1[1:] == nit2[1:]
+    assert same.mean() >= 0.99
+    np.testing.assert_allclose(te1[1:][same], te2[1:][same], rtol=1e-6)
+    # a graph replay from the same state and J is deterministic
+    ctx.state_restore()
+    ctx.balance()
+    np.testing.assert_array_equal(ctx.get(abi.ARR_TE), te2)
+    ctx.close()
