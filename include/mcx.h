@@ -79,6 +79,7 @@ enum mcx_array_id {
     MCX_ARR_LG_BLACK,        /* int32 [nCells+1] lgBlack: no photon hit in the last balance */
     MCX_ARR_N_ITER_T,        /* int32 [nCells+1] T-iterations of the last balance (0 = not updated) */
     MCX_ARR_FOR_LINES,       /* float [nCells+1] forbidden-line total of the last emission phase */
+    MCX_ARR_TDUST,           /* float [nSpecies+1][nSizes+1][nCells+1] Tdust(0:nSp,0:nSz,0:C) */
     MCX_ARR_COUNT_
 };
 
@@ -127,6 +128,16 @@ enum mcx_array_id {
 #define MCX_SARR_ATOM_HDR      1037  /* int32[nAtoms][16] packed atom headers (fields:
                                         elem, ion, nLev, nTemp, iup2p, recType, nRec, offLogT, offQom,
                                         offY2, offA, offG, offE, offRec, offAtp, 0)                     */
+#define MCX_SARR_DUST_DIMS     1039  /* int32[4] nSpecies, nSizes, nTemps, 0                           */
+#define MCX_SARR_DUST_CABS     1040  /* float[nSpecies][nSizes][nbins] pi a^2 Qabs [cm^2]               */
+#define MCX_SARR_DUST_CSCA     1041  /* float[nSpecies][nSizes][nbins] pi a^2 Qsca [cm^2]               */
+#define MCX_SARR_DUST_CTABS    1042  /* float[nbins] abundance- and size-weighted absorption             */
+#define MCX_SARR_DUST_CTSCA    1043  /* float[nbins] abundance- and size-weighted scattering             */
+#define MCX_SARR_DUST_ABUN     1044  /* float[nSpecies] grainAbun                                       */
+#define MCX_SARR_DUST_TSUB     1045  /* float[nSpecies] TdustSublime                                    */
+#define MCX_SARR_DUST_RADIUS   1046  /* float[nSizes] grainRadius [um]                                  */
+#define MCX_SARR_DUST_WEIGHT   1047  /* float[nSizes] normalised grainWeight                            */
+#define MCX_SARR_DUST_EMINT    1048  /* float[nSpecies][nSizes][nTemps] dustEmIntegral                  */
 #define MCX_SARR_ATOM_DATA     1038  /* double[n] packed atom data: log10 T[nTemp]; qom and its natural-
                                         spline second derivatives [pair (l<u) row-major][nTemp];
                                         a(j,i) at [j-1][i-1]; g; e [1/cm]; recombination fits; atp    */

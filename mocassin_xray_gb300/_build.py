@@ -45,6 +45,7 @@ def build_lib(verbose: bool = False) -> Path:
         ("setup.cpp", ["-x", "cu", *HOST_EXACT]),
         ("setup_emission.cpp", ["-x", "cu", *HOST_EXACT]),
         ("setup_balance.cpp", ["-x", "cu", *HOST_EXACT]),
+        ("setup_dust.cpp", ["-x", "cu", *HOST_EXACT]),
         ("k_emission.cu", []),
         ("mcx_api.cu", []),
         ("k_opacity.cu", []),
@@ -53,6 +54,7 @@ def build_lib(verbose: bool = False) -> Path:
         ("k_balance.cu", []),
         ("k_balance_f64.cu", ["--fmad=false"]),
         ("k_balance_mixed.cu", []),
+        ("k_dust.cu", ["--fmad=false"]),
         ("mcx_noalloc.cu", []),
     ]
     cmds = []

@@ -21,7 +21,7 @@ ERRORS = {1: "MCX_ERR_INPUT", 2: "MCX_ERR_IO", 3: "MCX_ERR_CUDA", 4: "MCX_ERR_NO
 (ARR_NU, ARR_WIDFLX, ARR_XSEC, ARR_SRC_CDF, ARR_KN_SIGMA_T, ARR_KN_CDF, ARR_PCOMP, ARR_XAXIS, ARR_YAXIS,
  ARR_ZAXIS, ARR_ACTIVE, ARR_HDEN, ARR_TE, ARR_NE, ARR_TEOLD, ARR_NEOLD, ARR_IONDEN, ARR_OPACITY, ARR_RECPDF,
  ARR_TOTAL_LINES, ARR_JSTE, ARR_ESCAPED, ARR_VOLUME, ARR_ELEM_ABUN, ARR_GAUNT_TE, ARR_SCAOPAC, ARR_DUSTPDF,
- ARR_NDUST, ARR_LG_CONVERGED, ARR_H_EST, ARR_LG_BLACK, ARR_N_ITER_T, ARR_FOR_LINES) = range(1, 34)
+ ARR_NDUST, ARR_LG_CONVERGED, ARR_H_EST, ARR_LG_BLACK, ARR_N_ITER_T, ARR_FOR_LINES, ARR_TDUST) = range(1, 35)
 SARR_POINTERS, SARR_ELEMENT_P, SARR_N_SHELLS, SARR_ELEM_XREF, SARR_ION_EDGE, SARR_COMXSEC_H, \
     SARR_COMXSEC_C, SARR_XSEC_RECOIL = range(1001, 1009)
 (SARR_EM_DIMS, SARR_EM_TK, SARR_EM_EDGE_P, SARR_EM_LOG_GAMMA, SARR_EM_FB_HEAVY, SARR_EM_HYDRO_MAP,
@@ -30,8 +30,11 @@ SARR_POINTERS, SARR_ELEMENT_P, SARR_N_SHELLS, SARR_ELEM_XREF, SARR_ION_EDGE, SAR
 (SARR_CION_CF, SARR_CION_THERM, SARR_NAUGER, SARR_AUGER, SARR_RR_BADNELL, SARR_DR_BADNELL_C,
  SARR_DR_BADNELL_E, SARR_RADREC_RREC, SARR_RADREC_RNEW, SARR_DIELEC, SARR_ALDRO, SARR_OUTER_SHELL,
  SARR_ATOM_INDEX, SARR_ATOM_HDR, SARR_ATOM_DATA) = range(1024, 1039)
+(SARR_DUST_DIMS, SARR_DUST_CABS, SARR_DUST_CSCA, SARR_DUST_CTABS, SARR_DUST_CTSCA, SARR_DUST_ABUN, SARR_DUST_TSUB,
+ SARR_DUST_RADIUS, SARR_DUST_WEIGHT, SARR_DUST_EMINT) = range(1039, 1049)
 INT_SARR = {SARR_POINTERS, SARR_ELEMENT_P, SARR_N_SHELLS, SARR_ELEM_XREF, SARR_EM_DIMS, SARR_EM_EDGE_P,
-            SARR_EM_FB_HEAVY, SARR_EM_HYDRO_MAP, SARR_NAUGER, SARR_OUTER_SHELL, SARR_ATOM_INDEX, SARR_ATOM_HDR}
+            SARR_EM_FB_HEAVY, SARR_EM_HYDRO_MAP, SARR_NAUGER, SARR_OUTER_SHELL, SARR_ATOM_INDEX, SARR_ATOM_HDR,
+            SARR_DUST_DIMS}
 F64_SARR = {SARR_ATOM_DATA}
 # packed atom header fields (MCX_SARR_ATOM_HDR)
 (AT_ELEM, AT_ION, AT_NLEV, AT_NTEMP, AT_IUP2P, AT_RECTYPE, AT_NREC, AT_OFF_LOGT, AT_OFF_QOM, AT_OFF_Y2,

@@ -15,6 +15,12 @@ path is measured on:
 * ``xray_gas``        41^3, n_H = 1e3, the same elements plus Mg, Si, Fe,
                       power law F_nu ~ nu^-1.5 over 1..740 Ryd with 2e49 s^-1
                       above 1 Ryd, 800 bins.
+* ``dust_shell``      dust-only shell on an 81^3 grid, R_in = 1e17, R_out =
+                      1e18 cm, grain density ~ r^-2 normalised to tau_V = 1
+                      (or 10), two grain species with seeded power-law
+                      Q_abs / Q_sca tables in the reference's 'Q' file format,
+                      10 log sizes 0.005..0.25 um with a^-3.5 weights, the
+                      reference's dust frequency mesh, 1e8 packets.
 
 ``scale`` shrinks grid edges and packet counts for parity tests.
 """
@@ -156,4 +162,99 @@ def xray_gas(root: str | Path, n: int = 41, packets: int = 10_000_000, iteration
         "TeStart 10000.",
         "nstages 27",
         "nebComposition 'input/abun_xray.in'",
+    ])
+
+
+# ------------------------------------------------------------------ dust
+DUST_SPECIES = (("Sil_syn", 1400.0, 3.3, 0.6), ("Gra_syn", 1700.0, 2.2, 0.4))   # label, Tsub, rho, abundance
+V_BAND_UM = 0.55
+
+
+def _q_efficiency(a_um: np.ndarray, lam_um: np.ndarray, p_abs: float, p_sca: float):
+    """Smooth absorption / scattering efficiencies: flat below 0.1 um, a power
+    law of index -p beyond 1 um, log-linear in between; larger grains are
+    more efficient."""
+    a = a_um[:, None]
+    lam = lam_um[None, :]
+    qa0 = a / (a + 0.02)
+    qs0 = 0.6 * a / (a + 0.05)
+
+    def shape(p):
+        f = np.ones_like(lam)
+        mid = (lam > 0.1) & (lam <= 1.0)
+        f = np.where(mid, (lam / 0.1) ** (-0.3), f)
+        far = lam > 1.0
+        return np.where(far, 10.0 ** (-0.3) * lam ** (-p), f)
+
+    return qa0 * shape(p_abs), qs0 * shape(p_sca)
+
+
+def _write_q_file(path: Path, label: str, tsub: float, rho: float, p_abs: float, p_sca: float) -> None:
+    radii = np.logspace(-3.0, 0.0, 16)                    # um
+    lam = np.logspace(3.0, -2.0, 150)                     # um, descending like the reference's files
+    qa, qs = _q_efficiency(radii, lam, p_abs, p_sca)
+    lines = ["Q", f"{label} {tsub:.1f} {rho:.2f} 0.588 20.077",
+             "synthetic efficiencies, seeded power laws", "for",
+             f" {radii.size} {radii[0]:.3E} {radii[-1]:.3E} = NRAD, a_1 (micron), a_NRAD (micron)",
+             f" {lam.size} {lam[0]:.3E} {lam[-1]:.3E} = NWAV, w_1 (micron), w_NWAV (micron)",
+             "    a(um)          lam(um)          Qabs            Qsca         g<cos>"]
+    for i, a in enumerate(radii):
+        for j, w in enumerate(lam):
+            lines.append(f"  {a:.7E}  {w:.7E}  {qa[i, j]:.7E}  {qs[i, j]:.7E}  0.0000000E+00")
+    path.write_text("\n".join(lines) + "\n")
+
+
+def _grain_sizes(n: int = 10, amin: float = 0.005, amax: float = 0.25):
+    a = np.logspace(math.log10(amin), math.log10(amax), n)
+    w = a ** (-3.5)
+    da = np.empty(n)
+    da[0] = a[1] - a[0]
+    da[1:-1] = (a[2:] - a[:-2]) / 2.0
+    da[-1] = a[-1] - a[-2]
+    return a, w, (w * da) / (w * da).sum()
+
+
+def dust_shell(root: str | Path, n: int = 81, tau_v: float = 1.0, packets: int = 100_000_000, iterations: int = 4,
+               r_in: float = 1.0e17, r_out: float = 1.0e18, seed: int = 0, nbins: int = 300) -> Path:
+    root = Path(root)
+    inp = root / "input"
+    inp.mkdir(parents=True, exist_ok=True)
+    rng = np.random.default_rng(seed)
+    sizes, w, weight = _grain_sizes()
+    (inp / "grainsizes.dat").write_text(f"{sizes.size} sizes\n" + "".join(
+        f"{k + 1} {a:.6e} {wk:.6e}\n" for k, (a, wk) in enumerate(zip(sizes, w))))
+    spec_lines = [f"{len(DUST_SPECIES)}"]
+    c_ext_v = 0.0
+    for label, tsub, rho, abun in DUST_SPECIES:
+        p_abs, p_sca = rng.uniform(1.5, 2.0, size=2)
+        _write_q_file(inp / f"{label}.Q", label, tsub, rho, p_abs, p_sca)
+        spec_lines.append(f"'input/{label}.Q' {abun}")
+        qa, qs = _q_efficiency(sizes, np.array([V_BAND_UM]), p_abs, p_sca)
+        c_ext_v += abun * float(np.sum(weight * math.pi * sizes ** 2 * 1e-8 * (qa[:, 0] + qs[:, 0])))
+    (inp / "grainspecies.dat").write_text("\n".join(spec_lines) + "\n")
+    # grain number density n0 (r_in / r)^2 between r_in and r_out with tau_V along a radius
+    n0 = tau_v / (c_ext_v * r_in * (1.0 - r_in / r_out))
+    ax = np.linspace(-r_out, r_out, n)
+    rows = []
+    for x in ax:
+        for y in ax:
+            for z in ax:
+                r = math.sqrt(x * x + y * y + z * z)
+                nd = n0 * (r_in / r) ** 2 if r_in <= r <= r_out else 0.0
+                rows.append(f"{x:.7e} {y:.7e} {z:.7e} {nd:.7e}\n")
+    (inp / "ndust.dat").write_text("".join(rows))
+    return _deck(root, [
+        "nebComposition noGas",
+        "contShape blackbody",
+        "TStellar 10000.",
+        "LStar 38.26",
+        f"nPhotons {packets}",
+        f"nx {n}", f"ny {n}", f"nz {n}",
+        f"nbins {nbins}",
+        f"Rin {r_in:.4e}",
+        f"Rout {r_out:.4e}",
+        "Ndust file 'input/ndust.dat'",
+        "dustFile 'input/grainspecies.dat' 'input/grainsizes.dat'",
+        f"maxIterateMC {iterations} 95.",
+        "convLimit 0.05",
     ])

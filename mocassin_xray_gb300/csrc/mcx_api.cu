@@ -4,6 +4,7 @@
 #include "../../include/mcx.h"
 #include "k_emission.cuh"
 #include "k_balance.cuh"
+#include "k_dust.cuh"
 #include "k_opacity.cuh"
 #include "k_transport_launch.h"
 #include "mcx_device.cuh"
@@ -216,6 +217,17 @@ extern "C" int mcx_setup_get(const mcx_setup* m, int32_t id, void* dst, size_t n
     case MCX_SARR_ATOM_INDEX: return copyRaw(&s.bal.atomIndex[0][0], sizeof(s.bal.atomIndex), dst, nbytes);
     case MCX_SARR_ATOM_HDR: return copyOut(s.bal.atomHdr, dst, nbytes);
     case MCX_SARR_ATOM_DATA: return copyOut(s.bal.atomData, dst, nbytes);
+    case MCX_SARR_DUST_DIMS: return copyOut(std::vector<int32_t>{s.dust.nSpecies, s.dust.nSizes, kNTemps, 0}, dst, nbytes);
+    case MCX_SARR_DUST_CABS: return copyOut(s.dust.Cabs, dst, nbytes);
+    case MCX_SARR_DUST_CSCA: return copyOut(s.dust.Csca, dst, nbytes);
+    case MCX_SARR_DUST_CTABS: return copyOut(s.dust.CTabs, dst, nbytes);
+    case MCX_SARR_DUST_CTSCA: return copyOut(s.dust.CTsca, dst, nbytes);
+    case MCX_SARR_DUST_ABUN: return copyOut(s.dust.grainAbun, dst, nbytes);
+    case MCX_SARR_DUST_TSUB: return copyOut(s.dust.TdustSublime, dst, nbytes);
+    case MCX_SARR_DUST_RADIUS: return copyOut(s.dust.grainRadius, dst, nbytes);
+    case MCX_SARR_DUST_WEIGHT: return copyOut(s.dust.grainWeight, dst, nbytes);
+    case MCX_SARR_DUST_EMINT: return copyOut(s.dust.emIntegral, dst, nbytes);
+    case MCX_ARR_TDUST: return copyOut(s.Tdust, dst, nbytes);
     default: g_setupError = "mcx_setup_get: unknown array id " + std::to_string(id); return MCX_ERR_INPUT;
   }
 }
@@ -270,6 +282,13 @@ extern "C" int mcx_setup_len(const mcx_setup* m, int32_t id, int64_t* count) {
     case MCX_SARR_ATOM_INDEX: *count = 30 * 31; break;
     case MCX_SARR_ATOM_HDR: *count = (int64_t)s.bal.atomHdr.size(); break;
     case MCX_SARR_ATOM_DATA: *count = (int64_t)s.bal.atomData.size(); break;
+    case MCX_SARR_DUST_DIMS: *count = 4; break;
+    case MCX_SARR_DUST_CABS: case MCX_SARR_DUST_CSCA: *count = (int64_t)s.dust.Cabs.size(); break;
+    case MCX_SARR_DUST_CTABS: case MCX_SARR_DUST_CTSCA: *count = (int64_t)s.dust.CTabs.size(); break;
+    case MCX_SARR_DUST_ABUN: case MCX_SARR_DUST_TSUB: *count = s.dust.nSpecies; break;
+    case MCX_SARR_DUST_RADIUS: case MCX_SARR_DUST_WEIGHT: *count = s.dust.nSizes; break;
+    case MCX_SARR_DUST_EMINT: *count = (int64_t)s.dust.emIntegral.size(); break;
+    case MCX_ARR_TDUST: *count = (int64_t)s.Tdust.size(); break;
 
     default: g_setupError = "mcx_setup_len: unknown array id " + std::to_string(id); return MCX_ERR_INPUT;
   }
@@ -348,6 +367,8 @@ struct mcx_ctx {
   DBuf<DevTransportCounters> counters;
   std::unique_ptr<EmissionData> emission;
   std::unique_ptr<BalanceData> balance;
+  std::unique_ptr<DustData> dust;
+  DBuf<float> tdust;                 // [nSpecies+1][nSizes+1][nCells+1]
   DBuf<int32_t> lgConverged, lgBlack, nIterT;
   DBuf<float> forLines;
   // mcx_state_save snapshot
@@ -661,7 +682,13 @@ extern "C" int mcx_load(mcx_ctx* c, const mcx_setup* m) {
   CK(cudaMemset(c->forLines.p, 0, c->forLines.bytes()), "memset");
   c->emission.reset();
   c->balance.reset();
+  c->dust.reset();
   c->haveSnapshot = false;
+  if (c->lgDust) {
+    std::string dm = dustDataCreate(s, c->dust);
+    if (!dm.empty()) return fail(c, MCX_ERR_INPUT, "mcx_load: " + dm);
+    CK(upload(c->tdust, s.Tdust), "upload Tdust");
+  }
   if (c->lgGas) {
     std::string em = emissionDataCreate(s, c->emission);
     if (!em.empty()) return fail(c, MCX_ERR_INPUT, "mcx_load: " + em);
@@ -712,6 +739,7 @@ ArrView viewOf(mcx_ctx* c, int id) {
     case MCX_ARR_LG_BLACK: return {c->lgBlack.p, c->lgBlack.bytes()};
     case MCX_ARR_N_ITER_T: return {c->nIterT.p, c->nIterT.bytes()};
     case MCX_ARR_FOR_LINES: return {c->forLines.p, c->forLines.bytes()};
+    case MCX_ARR_TDUST: return {c->tdust.p, c->tdust.bytes()};
     default: return {nullptr, 0};
   }
 }
@@ -786,6 +814,23 @@ static int skipMask(mcx_ctx* c, int it, std::vector<float>& te, std::vector<uint
 extern "C" int mcx_emission(mcx_ctx* c, const mcx_phase_opts* opts, mcx_phase_stats* stats) {
   if (!c) return MCX_ERR_INPUT;
   if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_emission: no model loaded");
+  if (!c->lgGas && c->dust) {
+    // dust-only grid: setDustPDF for every cell (source/emission_mod.f90:1921-1986)
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    const int C1d = c->nCells + 1;
+    CK(cudaEventRecord(c->ev0, c->stream), "event");
+    CK(launchDustPDF(c->dust->dev, c->tdust.p, c->dustPDF.p, c->stream), "dust emission");
+    CK(transpose(c->dustPDF.p, c->dustCDFT.p, c->nbins, C1d, c->stream), "transpose dustPDF");
+    CK(cudaEventRecord(c->ev1, c->stream), "event");
+    CK(cudaStreamSynchronize(c->stream), "mcx_emission");
+    if (stats) {
+      std::memset(stats, 0, sizeof(*stats));
+      stats->cells_computed = c->nCells;
+      cudaEventElapsedTime(&stats->kernel_ms, c->ev0, c->ev1);
+    }
+    c->haveDustPDF = true;
+    return MCX_OK;
+  }
   if (!c->lgGas || !c->emission) return fail(c, MCX_ERR_STATE, "mcx_emission: the grid holds no gas");
   if (c->gauntTeOld <= 0.f) return fail(c, MCX_ERR_STATE, "mcx_emission: run mcx_opacity first (its Gaunt factors are reused)");
   CK(cudaSetDevice(c->device), "cudaSetDevice");
@@ -825,8 +870,23 @@ extern "C" int mcx_emission(mcx_ctx* c, const mcx_phase_opts* opts, mcx_phase_st
 extern "C" int mcx_opacity(mcx_ctx* c, const mcx_phase_opts* opts, mcx_phase_stats* stats) {
   if (!c) return MCX_ERR_INPUT;
   if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_opacity: no model loaded");
-  if (!c->lgGas) return fail(c, MCX_ERR_STATE, "mcx_opacity: the grid holds no gas");
   CK(cudaSetDevice(c->device), "cudaSetDevice");
+  if (!c->lgGas) {
+    // dust-only grid: the grain contribution of every cell is added to the
+    // opacity, which the reference never resets on such a grid
+    // (source/iteration_mod.f90:194-246)
+    CK(cudaEventRecord(c->ev0, c->stream), "event");
+    CK(launchDustOpacity(c->dust->dev, c->ndust.p, c->tdust.p, c->opacity.p, c->scaOpac.p, c->stream), "dust opacity");
+    CK(cudaEventRecord(c->ev1, c->stream), "event");
+    CK(cudaStreamSynchronize(c->stream), "mcx_opacity");
+    if (stats) {
+      std::memset(stats, 0, sizeof(*stats));
+      stats->cells_computed = c->nCells;
+      cudaEventElapsedTime(&stats->kernel_ms, c->ev0, c->ev1);
+    }
+    c->haveOpacity = true;
+    return MCX_OK;
+  }
   const int it = opts ? opts->n_iterate_mc : 1;
   const size_t C1 = (size_t)c->nCells + 1;
   // the skip rule and the Gaunt cache are sequential host logic over four
@@ -974,6 +1034,24 @@ extern "C" int mcx_normalize_j(mcx_ctx* c) {
 extern "C" int mcx_balance(mcx_ctx* c, const mcx_balance_opts* opts, mcx_balance_stats* stats) {
   if (!c) return MCX_ERR_INPUT;
   if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_balance: no model loaded");
+  if (!c->lgGas && c->dust) {
+    // dust-only grid: getDustT for every cell hit by a photon (source/update_mod.f90:234-265, :3346-3453)
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    CK(cudaEventRecord(c->ev0, c->stream), "event");
+    CK(launchDustT(c->dust->dev, c->jste.p, c->tdust.p, c->lgConverged.p, c->lgBlack.p, c->stream), "grain balance");
+    CK(cudaEventRecord(c->ev1, c->stream), "event");
+    DustCounters h{};
+    CK(cudaMemcpyAsync(&h, c->dust->dev.counters, sizeof(h), cudaMemcpyDeviceToHost, c->stream), "d2h counters");
+    CK(cudaStreamSynchronize(c->stream), "mcx_balance");
+    if (stats) {
+      std::memset(stats, 0, sizeof(*stats));
+      stats->cells_updated = (int64_t)h.updated;
+      stats->no_hit = (int64_t)h.noHit;
+      stats->converged = (int64_t)h.converged;
+      cudaEventElapsedTime(&stats->kernel_ms, c->ev0, c->ev1);
+    }
+    return MCX_OK;
+  }
   if (!c->lgGas || !c->balance) return fail(c, MCX_ERR_STATE, "mcx_balance: the grid holds no gas");
   if (opts && opts->precision != MCX_BAL_FP64 && opts->precision != MCX_BAL_MIXED)
     return fail(c, MCX_ERR_INPUT, "mcx_balance: unknown precision");

@@ -926,7 +926,13 @@ void buildSetup(Setup& s, const std::string& inputFile, const std::string& dataD
   if (s.p.lgGas) computeIonEdges(s);
   buildMesh(s);
   if (s.p.lgGas) initXSecArray(s);
-  else fail("initXSecArray: dust x sections are outside this library's scope");
+  if (s.p.lgGas && s.p.lgDust) fail("makeDustXsec: gas and dust in one grid are outside this library's scope");
+  if (s.p.lgDust) buildDustTables(s);
+  if (!s.p.lgGas) {   // no Compton tables without gas (setCompton is part of initXSecArray)
+    s.KNsigmaT.assign(s.nbins, 0.f);
+    s.KNcdf.assign((size_t)kNAngles * s.nbins, 0.f);
+    s.Pcomp.assign((size_t)kNAngles * s.nbins, 0.f);
+  }
   if (s.p.lgGas) {
     buildEmissionTables(s);
     buildBalanceTables(s);
@@ -934,6 +940,10 @@ void buildSetup(Setup& s, const std::string& inputFile, const std::string& dataD
   setContinuum(s);
   fillGrid(s);
   setStarPosition(s);
+  if (s.p.lgDust) {   // dustDriver's initial grain temperatures (source/dust_mod.f90:66-73)
+    const size_t planes = (size_t)(s.dust.nSpecies + 1) * (s.dust.nSizes + 1);
+    s.Tdust.assign(planes * ((size_t)s.nCells + 1), 50.f);
+  }
 }
 
 }  // namespace mcx

@@ -109,10 +109,25 @@ struct BalanceTables {
   int maxLev = 0;
 };
 
+// Grain species and sizes (makeDustXsec, source/ph_mod.f90:938-1720, the 'Q'
+// file type) and the emission integrals of dustEmissionInt
+// (source/dust_mod.f90:141-184).
+constexpr int kNTemps = 3000;     // nTemps (source/constants_mod.f90:69)
+struct DustTables {
+  int nSpecies = 0, nSizes = 0;
+  std::vector<std::string> grainLabel;
+  std::vector<float> grainAbun, TdustSublime;        // [nSpecies]
+  std::vector<float> grainRadius, grainWeight, da;   // [nSizes]
+  std::vector<float> Cabs, Csca, gCos;               // [nSpecies][nSizes][nbins] cm^2
+  std::vector<float> CTabs, CTsca;                   // [nbins] abundance- and size-weighted
+  std::vector<float> emIntegral;                     // [nSpecies][nSizes][nTemps]
+};
+
 struct Setup {
   Params p;
   EmissionTables em;
   BalanceTables bal;
+  DustTables dust;
   std::string dataDir;
   int meshMode = 0;
 
@@ -163,6 +178,7 @@ struct Setup {
   std::vector<float> ionDen;                         // [nstages][nElemUsed][nCells+1]
   std::vector<float> volume;                         // [nCells+1]
   std::vector<float> Ndust;                          // [nCells+1]
+  std::vector<float> Tdust;                          // [nSpecies+1][nSizes+1][nCells+1]
   int starIdx[3] = {-1, -1, -1};
   float starPos[3] = {0.f, 0.f, 0.f};
 
@@ -179,6 +195,12 @@ void buildEmissionTables(Setup& s);
 
 // Reads the rate tables and the multi-level atoms of the balance phase.
 void buildBalanceTables(Setup& s);
+
+// Reads the grain species and sizes and tabulates their emission integrals.
+void buildDustTables(Setup& s);
+
+// getFlux of source/continuum_mod.f90:358-405 for a blackbody (FP32).
+float blackbodyFlux(float energy, float temperature);
 
 // Builds a Setup from an input deck; throws std::runtime_error with a message.
 void buildSetup(Setup& s, const std::string& inputFile, const std::string& dataDir, int meshMode);

@@ -111,8 +111,15 @@ class Context:
             abi.ARR_NDUST: ((C1,), f32), abi.ARR_LG_CONVERGED: ((C1,), np.int32),
             abi.ARR_LG_BLACK: ((C1,), np.int32), abi.ARR_N_ITER_T: ((C1,), np.int32), abi.ARR_FOR_LINES: ((C1,), f32),
             abi.ARR_IONDEN: ((s.nstages, max(s.n_elem_used, 1), C1), f32),
+            abi.ARR_TDUST: ((self._dust_planes(), C1), f32),
         }
         return shapes[arr_id]
+
+    def _dust_planes(self) -> int:
+        if not self.setup.info.lg_dust:
+            return 0
+        d = self.setup.get(abi.SARR_DUST_DIMS)
+        return int((d[0] + 1) * (d[1] + 1))
 
     def get(self, arr_id: int) -> np.ndarray:
         shape, dt = self._shape(arr_id)

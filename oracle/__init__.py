@@ -394,3 +394,74 @@ def balance_trace(tables: BalanceTables, jste, te, ne, ionden, cell: int) -> np.
     n = _balance_lib().orc_balance_trace(C.byref(tables.s), C.byref(st), cell, _p(tr))
     tables.s.jste = None
     return tr[:n]
+
+
+class DustIn(C.Structure):
+    _fields_ = [("n_cells", C.c_int32), ("nbins", C.c_int32), ("n_species", C.c_int32), ("n_sizes", C.c_int32),
+                ("xhi_limit", C.c_float), ("nu", _P), ("widflx", _P), ("cabs", _P), ("csca", _P), ("abun", _P),
+                ("tsub", _P), ("weight", _P), ("em_int", _P)]
+
+
+class DustStats(C.Structure):
+    _fields_ = [("no_hit", C.c_int64), ("updated", C.c_int64), ("converged", C.c_int64)]
+
+
+class DustTables:
+    """The grain tables of a dust-only Setup, for the dust oracle."""
+
+    def __init__(self, setup):
+        from mocassin_xray_gb300 import abi
+        g = setup.get
+        d = g(abi.SARR_DUST_DIMS)
+        self.n_species, self.n_sizes = int(d[0]), int(d[1])
+        self.k = dict(nu=g(abi.ARR_NU), wid=g(abi.ARR_WIDFLX), cabs=g(abi.SARR_DUST_CABS),
+                      csca=g(abi.SARR_DUST_CSCA), abun=g(abi.SARR_DUST_ABUN), tsub=g(abi.SARR_DUST_TSUB),
+                      weight=g(abi.SARR_DUST_WEIGHT), em=g(abi.SARR_DUST_EMINT))
+        k = self.k
+        i = setup.info
+        self.info = i
+        self.s = DustIn(n_cells=i.n_cells, nbins=i.nbins, n_species=self.n_species, n_sizes=self.n_sizes,
+                        xhi_limit=i.xhi_limit, nu=_p(k["nu"]), widflx=_p(k["wid"]), cabs=_p(k["cabs"]),
+                        csca=_p(k["csca"]), abun=_p(k["abun"]), tsub=_p(k["tsub"]), weight=_p(k["weight"]),
+                        em_int=_p(k["em"]))
+
+
+def _dust_lib():
+    l = lib()
+    if not getattr(l, "_dust_ready", False):
+        l.orc_dust_opacity.argtypes = [C.POINTER(DustIn), _P, _P, _P, _P]
+        l.orc_dust_pdf.argtypes = [C.POINTER(DustIn), _P, _P]
+        l.orc_dust_t.argtypes = [C.POINTER(DustIn), _P, _P, _P, _P, C.POINTER(DustStats)]
+        l._dust_ready = True
+    return l
+
+
+def dust_opacity(t: DustTables, ndust, tdust, opacity=None):
+    C1 = t.info.n_cells + 1
+    nb = t.info.nbins
+    op = np.zeros((nb, C1), np.float32) if opacity is None else np.array(opacity, dtype=np.float32, copy=True)
+    sca = np.zeros((nb, C1), np.float32)
+    nd = np.ascontiguousarray(ndust, dtype=np.float32)
+    td = np.ascontiguousarray(tdust, dtype=np.float32)
+    _dust_lib().orc_dust_opacity(C.byref(t.s), _p(nd), _p(td), _p(op), _p(sca))
+    return op, sca
+
+
+def dust_pdf(t: DustTables, tdust):
+    C1 = t.info.n_cells + 1
+    pdf = np.zeros((t.info.nbins, C1), np.float32)
+    td = np.ascontiguousarray(tdust, dtype=np.float32)
+    _dust_lib().orc_dust_pdf(C.byref(t.s), _p(td), _p(pdf))
+    return pdf
+
+
+def dust_t(t: DustTables, jste, tdust):
+    """getDustT: returns (tdust, converged, black, stats)."""
+    C1 = t.info.n_cells + 1
+    j = np.ascontiguousarray(jste, dtype=np.float64)
+    td = np.array(tdust, dtype=np.float32, copy=True)
+    conv = np.zeros(C1, np.int32)
+    black = np.zeros(C1, np.int32)
+    st = DustStats()
+    _dust_lib().orc_dust_t(C.byref(t.s), _p(j), _p(td.reshape(-1)), _p(conv), _p(black), C.byref(st))
+    return td, conv, black, st

@@ -240,6 +240,33 @@ int orc_equilibrium(const orc_balance_in* in, int32_t atom, double te, double ne
 int orc_for_lines_emission(const orc_balance_in* in, const float* te, const float* ne, const float* ionden,
                            const uint8_t* compute, double* for_lines);
 
+/* ----------------------------------------------------------------- dust */
+typedef struct orc_dust_in {
+    int32_t n_cells, nbins, n_species, n_sizes;
+    float xhi_limit;
+    const float* nu;            /* [nbins] */
+    const float* widflx;        /* [nbins] */
+    const float* cabs;          /* [nSpecies][nSizes][nbins] cm^2 */
+    const float* csca;
+    const float* abun;          /* [nSpecies] grainAbun */
+    const float* tsub;          /* [nSpecies] TdustSublime */
+    const float* weight;        /* [nSizes] grainWeight */
+    const float* em_int;        /* [nSpecies][nSizes][3000] dustEmIntegral */
+} orc_dust_in;
+
+typedef struct orc_dust_stats {
+    int64_t no_hit, updated, converged;
+} orc_dust_stats;
+
+/* Tdust is [nSpecies+1][nSizes+1][C+1].  Grain scattering and absorption of
+ * every cell below sublimation; opacity += their sum. */
+int orc_dust_opacity(const orc_dust_in* in, const float* ndust, const float* tdust, float* opacity, float* sca_opac);
+/* setDustPDF for every cell: pdf[nu][c] */
+int orc_dust_pdf(const orc_dust_in* in, const float* tdust, float* pdf);
+/* getDustT for every cell hit by a photon, with lgBlack and lgConverged */
+int orc_dust_t(const orc_dust_in* in, const double* jste, float* tdust, int32_t* converged, int32_t* black,
+               orc_dust_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -60,6 +60,11 @@ def main(src: str) -> None:
     for f in FILES + listed_hydro_files(src_dir) + listed_ion_files(src_dir):
         shutil.copyfile(src_dir / f, dst / f)
         print("copied", f)
+    # the dust-only frequency mesh, read from <data>/../dustData (source/grid_mod.f90:216-259)
+    dust_dst = dst.parent / "dustData"
+    dust_dst.mkdir(exist_ok=True)
+    shutil.copyfile(src_dir.parent / "dustData" / "nuDustRyd.dat", dust_dst / "nuDustRyd.dat")
+    print("copied dustData/nuDustRyd.dat")
 
 if __name__ == "__main__":
     main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/data")
