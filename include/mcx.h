@@ -379,6 +379,45 @@ typedef struct mcx_iterate_stats {
 
 int  mcx_iterate(mcx_ctx* ctx, const mcx_iterate_opts* opts, mcx_iterate_stats* stats);
 
+/* ---------------------------------------------- analytical line luminosities */
+/* The analytical part of outputGas (source/output_mod.f90:13-805) from the
+ * current grid state: over the active cells with lgBlack < 1, the volume
+ * emissivities sum(eps * Hden * dV) of Hbeta, of the hydrogenic recombination
+ * lines of every element on with nstages > Z, of the 34 HeI recombination
+ * lines and of every forbidden line of the ions with multi-level data
+ * (equilibrium with the recombination term, 1e-25 erg/s units), and the
+ * Ne * Hden * dV weighted ionic temperatures TeVol and fractions ionDenVol
+ * (Harrington et al. 1982).  When HbetaVol > 0 the line sums are divided by
+ * it ("relative" = 1); then HbetaVol is scaled to 1e36 erg/s (x 1e-16) and by
+ * 8 in symmetricXYZ mode.  All sums are FP64 and reduced in a fixed order, so
+ * repeated calls give the same bits.  Gas grids only.
+ *
+ * Output arrays are caller-owned, may be NULL, and use the reference's
+ * column-major layouts of the iAb = 0 (total) slice:
+ *   hydro_vol  double[8][14][30]        hydroVol(iz,iup,ilow)   at (iz-1) + 30*(iup-2) + 420*(ilow-1)
+ *   hei_vol    double[34]               HeIVol(l)
+ *   forb_vol   double[30][30][S][30]    forbVol(elem,ion,i,j)   at (elem-1) + 30*(ion-1) + 30*S*(i-1) + 900*S*(j-1)
+ *              (S = nstages; i the lower and j the upper level, as fLineEm(i,j) of equilibrium)
+ *   wav        double, forb_vol layout  wavelength 1e8/(E_j - E_i) [A] of each line with a(j,i) /= 0
+ *   te_vol     double[S][30]            TeVol(elem,ion)         at (elem-1) + 30*(ion-1)
+ *   ion_vol    double[S][30]            ionDenVol(elem,ion) */
+typedef struct mcx_lines {
+    double  hbeta_vol;          /* out: HbetaVol [1e36 erg/s]                              */
+    int32_t relative;           /* out: 1 when the line sums were divided by HbetaVol      */
+    int32_t n_cells;            /* out: cells summed (active, lgBlack < 1)                 */
+    double* hydro_vol;
+    double* hei_vol;
+    double* forb_vol;
+    double* wav;
+    double* te_vol;
+    double* ion_vol;
+    float   kernel_ms;          /* out: CUDA-event time of the sums                        */
+    float   reserved_f[3];
+    int64_t reserved[4];
+} mcx_lines;
+
+int  mcx_line_luminosities(mcx_ctx* ctx, mcx_lines* out);
+
 
 /* ------------------------------------------- transport without allocation */
 /* No counterpart in the reference.  Some callers cannot allocate device

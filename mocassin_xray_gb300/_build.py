@@ -55,6 +55,7 @@ def build_lib(verbose: bool = False) -> Path:
         ("k_balance_f64.cu", ["--fmad=false"]),
         ("k_balance_mixed.cu", []),
         ("k_dust.cu", ["--fmad=false"]),
+        ("k_lines.cu", ["--fmad=false"]),
         ("mcx_noalloc.cu", []),
     ]
     cmds = []

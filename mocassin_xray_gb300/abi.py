@@ -127,6 +127,13 @@ class IterateStats(C.Structure):
                 ("reserved", C.c_int64 * 4)]
 
 
+class Lines(C.Structure):
+    _fields_ = [("hbeta_vol", C.c_double), ("relative", C.c_int32), ("n_cells", C.c_int32),
+                ("hydro_vol", _P), ("hei_vol", _P), ("forb_vol", _P), ("wav", _P), ("te_vol", _P),
+                ("ion_vol", _P), ("kernel_ms", C.c_float), ("reserved_f", C.c_float * 3),
+                ("reserved", C.c_int64 * 4)]
+
+
 SIGNATURES = [
     ("mcx_setup_from_input", C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(SetupOpts), C.POINTER(_P)]),
     ("mcx_setup_free", None, [_P]),
@@ -151,6 +158,7 @@ SIGNATURES = [
     ("mcx_normalize_j", C.c_int, [_P]),
     ("mcx_balance", C.c_int, [_P, C.POINTER(BalanceOpts), C.POINTER(BalanceStats)]),
     ("mcx_iterate", C.c_int, [_P, C.POINTER(IterateOpts), C.POINTER(IterateStats)]),
+    ("mcx_line_luminosities", C.c_int, [_P, C.POINTER(Lines)]),
     ("mcx_timer_start", C.c_int, [_P]),
     ("mcx_timer_stop", C.c_int, [_P, C.POINTER(C.c_float)]),
     ("mcx_version", C.c_char_p, []),

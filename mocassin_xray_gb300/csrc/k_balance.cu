@@ -15,6 +15,7 @@ namespace bal_f64 {
 cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStream_t s);
 cudaError_t launchForLines(BalanceData& bd, const float* te, const float* ne, const float* ionDen,
                            const uint8_t* compute, float* forLines, cudaStream_t s);
+cudaError_t launchForbSums(BalanceData& bd, const LineSumArgs& a, cudaStream_t s);
 }  // namespace bal_f64
 namespace bal_mixed {
 cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStream_t s);
@@ -246,6 +247,10 @@ cudaError_t launchForLinesEmission(BalanceData& bd, const float* te, const float
                                    const uint8_t* compute, float* forLines, int precision, cudaStream_t s) {
   return precision == kBalMixed ? bal_mixed::launchForLines(bd, te, ne, ionDen, compute, forLines, s)
                                 : bal_f64::launchForLines(bd, te, ne, ionDen, compute, forLines, s);
+}
+
+cudaError_t launchForbLevelSums(BalanceData& bd, const LineSumArgs& a, cudaStream_t s) {
+  return bal_f64::launchForbSums(bd, a, s);
 }
 
 }  // namespace mcx

@@ -26,6 +26,7 @@
 namespace mcx {
 
 struct Setup;
+struct LineSumArgs;
 
 // One photoionised shell (elem, ion, shell) of an element that is on.
 struct PhotoShell {
@@ -132,5 +133,9 @@ cudaError_t launchBalance(BalanceData& b, const BalanceGrid& g, int maxRounds, i
 // the grid state.
 cudaError_t launchForLinesEmission(BalanceData& b, const float* te, const float* ne, const float* ionDen,
                                    const uint8_t* compute, float* forLines, int precision, cudaStream_t s);
+
+// outputGas forbidden-line level sums of every multi-level atom into the
+// partial rows of `a` (FP64; the layout is described in k_lines.cuh).
+cudaError_t launchForbLevelSums(BalanceData& b, const LineSumArgs& a, cudaStream_t s);
 
 }  // namespace mcx

@@ -15,6 +15,7 @@
 // (:887-1215), forLines (:1221-1262), equilibrium / luSlv
 // (source/emission_mod.f90:2505-3106), splint (source/interpolation_mod.f90:286-335).
 #include "k_balance.cuh"
+#include "k_lines.cuh"
 #include "setup_internal.h"
 
 #include <algorithm>
@@ -613,11 +614,11 @@ __device__ __forceinline__ real splineEval(const SplineAt& s, const real* ya, co
   return s.a * ya[s.klo - 1] + s.bb * ya[s.khi - 1] + (s.a3 * y2a[s.klo - 1] + s.b3 * y2a[s.khi - 1]) * s.hh / (real)6.;
 }
 
-// equilibrium of one atom: the sum over its lines of a(j,i)*E_ji*n_j*m1*m2*m3
-// that exceed 1e-35, lower level outer, upper level inner.  Collision rates
-// in the rate precision, the rate matrix and its LU solve in FP64.
-__device__ double equilibriumLines(const BalanceDev& b, int atom, double Te, double Ne, double ionDenUp, bool rec,
-                                   double m1, double m2, double m3) {
+// equilibrium of one atom: the normalised level populations y[1..nLev]
+// (source/emission_mod.f90:2884-2984).  Collision rates in the rate
+// precision, the rate matrix and its LU solve in FP64.
+__device__ __forceinline__ void equilibriumPops(const BalanceDev& b, int atom, double Te, double Ne, double ionDenUp,
+                                                bool rec, double* y) {
   const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
   const real* D = atomTable(b);
   const double* DD = b.atomData;
@@ -629,8 +630,6 @@ __device__ double equilibriumLines(const BalanceDev& b, int atom, double Te, dou
   const real* g = D + h[kAtOffG];
   const real* e = D + h[kAtOffE];
   const double* eD = DD + h[kAtOffE];
-  const double atp = DD[h[kAtOffAtp]];
-  const int iup2p = h[kAtIup2p];
   const real TeR = (real)Te;
   const real sqrTe = sqrt(TeR), log10Te = log10(TeR);
   double alphaTotal[kMaxLevels + 1];
@@ -664,7 +663,7 @@ __device__ double equilibriumLines(const BalanceDev& b, int atom, double Te, dou
     }
   }
   real qeff[kMaxLevels + 1][kMaxLevels + 1];
-  double x[kMaxLevels + 1][kMaxLevels + 1], y[kMaxLevels + 1];
+  double x[kMaxLevels + 1][kMaxLevels + 1];
   for (int i = 1; i <= nLev; ++i) {
     y[i] = 0.;
     for (int j = 1; j <= nLev; ++j) { qeff[i][j] = 0; x[i][j] = 0.; }
@@ -749,6 +748,21 @@ __device__ double equilibriumLines(const BalanceDev& b, int atom, double Te, dou
   double sumN = 0.;
   for (int i = 1; i <= nLev; ++i) sumN = sumN + y[i];
   for (int i = 1; i <= nLev; ++i) y[i] = y[i] / sumN;
+}
+
+// equilibrium of one atom: the sum over its lines of a(j,i)*E_ji*n_j*m1*m2*m3
+// that exceed 1e-35, lower level outer, upper level inner.
+__device__ double equilibriumLines(const BalanceDev& b, int atom, double Te, double Ne, double ionDenUp, bool rec,
+                                   double m1, double m2, double m3) {
+  double y[kMaxLevels + 1];
+  equilibriumPops(b, atom, Te, Ne, ionDenUp, rec, y);
+  const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
+  const double* DD = b.atomData;
+  const int nLev = h[kAtNLev];
+  const double* A = DD + h[kAtOffA];
+  const double* eD = DD + h[kAtOffE];
+  const double atp = DD[h[kAtOffAtp]];
+  const int iup2p = h[kAtIup2p];
   double total = 0.;
   for (int i = 1; i <= nLev - 1; ++i)
     for (int j = i + 1; j <= nLev; ++j) {
@@ -823,6 +837,52 @@ __global__ void forLinesSumKernel(BalanceDev b, const uint8_t* __restrict__ comp
   for (int atom = 0; atom < b.nAtoms; ++atom) normFor = normFor + b.forSum[(size_t)atom * C1 + cell];
   forLines[cell] = (float)normFor;
 }
+
+#if MCX_BAL_EXACT
+// outputGas forbidden-line volume sums (source/output_mod.f90:410-432 with
+// forLines at :1943-1984): per (cell, ion with data) the level populations of
+// equilibrium(rec = .true.), weighted by elemAbun * ionDen * 1.9865e9 * Hden
+// * dV over the cells with lgBlack < 1.  Each warp (32 consecutive cells)
+// reduces level j into partial[group][forbBase[atom] + j - 1]; the line
+// factors a(j,i) E_ji multiply the sums afterwards.
+__global__ void __launch_bounds__(128) forbLevelSumsKernel(BalanceDev b, LineSumArgs a) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int group = t >> 5;
+  if (group >= a.nGroups) return;   // whole warps only
+  const int cell = t + 1;
+  const int atom = blockIdx.y;
+  const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
+  const int elem = h[kAtElem], ion = h[kAtIon], nLev = h[kAtNLev];
+  const int top = min(elem + 1, b.nstages);
+  const size_t C1 = (size_t)b.nCells + 1;
+  const int e = b.xref[elem];
+  const bool valid = cell <= b.nCells && a.black[cell] < 1;
+  double y[kMaxLevels + 1];
+  double w = 0.;
+  if (valid) {
+    const double x = a.ionDen[((size_t)(ion - 1) * b.nElemUsed + (e - 1)) * C1 + cell];
+    double up = 0.;
+    if (ion < top && x > 0.) up = (double)a.ionDen[((size_t)ion * b.nElemUsed + (e - 1)) * C1 + cell] / x;
+    equilibriumPops(b, atom, a.te[cell], a.ne[cell], up, true, y);
+    w = (double)b.abun[elem] * x * RD(1.9865e9) * (double)a.hden[cell] * a.vol[cell];
+  } else {
+    for (int j = 1; j <= nLev; ++j) y[j] = 0.;
+  }
+  double* row = a.partial + (size_t)group * a.nEntries + a.forbBase[atom];
+  for (int j = 1; j <= nLev; ++j) {
+    const double v = warpSumD(valid ? y[j] * w : 0.);
+    if ((threadIdx.x & 31) == 0) row[j - 1] = v;
+  }
+}
+
+cudaError_t launchForbSums(BalanceData& bd, const LineSumArgs& a, cudaStream_t s) {
+  BalanceDev& b = bd.dev;
+  if (b.nAtoms <= 0 || a.nGroups <= 0) return cudaSuccess;
+  const int T = 128, nb = (a.nGroups * 32 + T - 1) / T;
+  forbLevelSumsKernel<<<dim3(nb, b.nAtoms), T, 0, s>>>(b, a);
+  return cudaGetLastError();
+}
+#endif
 
 // heating - cooling and the secant step of iterateT (FP64 in both precisions)
 __global__ void __launch_bounds__(128) secantKernel(BalanceDev b, int lastRound) {

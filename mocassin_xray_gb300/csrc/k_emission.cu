@@ -349,7 +349,8 @@ emissionKernel(EmissionDev e, const float* __restrict__ te, const float* __restr
         } else {
           const float* e3 = e.r2aEdge + 2 * 18;
           yy1 = e3[idenp - 1] + ((idenp < 13) ? (e3[idenp - 1] - e3[idenp]) * wN : 0.f);
-          yy2 = e3[8 + idenp] + ((idenp < 13) ? (e3[8 + idenp] - e3[9 + idenp]) * wN : 0.f);
+          // r2aEdge(3, 9+idenp+1) lies past the table for idenp = 9: read as r2aEdge(3,18)
+          yy2 = e3[8 + idenp] + ((idenp < 13) ? (e3[8 + idenp] - e3[9 + idenp < 18 ? 9 + idenp : 17]) * wN : 0.f);
           x1 = e.r2aEdge[0]; x2 = e.r2aEdge[9];
         }
         const float xx = log10f(T4 * 1.e4f);

@@ -1,0 +1,60 @@
+// k_lines.cuh - analytical line luminosities and ionic volume averages of
+// outputGas (source/output_mod.f90:13-820) as per-warp partial sums.
+//
+// Every quantity outputGas integrates is a sum over the active cells with
+// lgBlack < 1 of a per-cell value times Hden * dV.  Each warp takes 32
+// consecutive cells (group g = cells 32g+1 .. 32g+32), reduces every entry
+// over its lanes with a fixed shuffle tree and writes one row of
+// partial[group][entry]; a second kernel adds the rows in group order.  The
+// sums are therefore the same from run to run.
+//
+// Entry layout (LineSumArgs):
+//   0                              Hbeta: hydroLines(1,4,2)*Hden*dV where > 1e-35
+//   hydroBase + 84 k + l           hydroVol of the k-th hydrogenic element, line l
+//                                  (iup = 2..15, ilow = 1..min(8, iup-1), iup outer)
+//   heiBase + l                    HeIVol, 34 lines (absent when He is off)
+//   ionBase + 2 p, + 2 p + 1       TeVol numerator / denominator of the p-th
+//                                  (element on, ion <= min(elem+1, nstages)) pair
+//   forbBase[atom] + j - 1         sum of n_j * elemAbun * ionDen * 1.9865e9 * Hden * dV
+//                                  for level j of the multi-level atom (the line
+//                                  a(j,i) E_ji factors are applied on the host)
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mcx {
+
+struct EmissionDev;
+
+constexpr int kHydroLinesPerElem = 84;
+
+struct LineSumArgs {
+  const float* te;          // [C+1]
+  const float* ne;          // [C+1]
+  const float* ionDen;      // [nstages][nElemUsed][C+1]
+  const float* hden;        // [C+1]
+  const double* vol;        // [C+1] getVolume in FP64
+  const int32_t* black;     // [C+1] lgBlack
+  double* partial;          // [nGroups][nEntries]
+  const int32_t* forbBase;  // [nAtoms] device
+  int32_t nCells, nGroups, nEntries;
+  int32_t nHydro, hydroBase, heiBase, ionBase, nIonElem;
+  int32_t hydroIz[30];      // elements with hydrogenic lines, ascending
+  int32_t ionElem[30];      // elements on, ascending
+};
+
+// Shuffle-tree sum over the 32 lanes; lane 0 holds the result.
+__device__ __forceinline__ double warpSumD(double v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  return v;
+}
+
+// Hbeta, hydrogenic and HeI recombination lines and the ionic Te/ionDen
+// sums into partial rows (FP64).
+cudaError_t launchGasLineSums(const EmissionDev& e, const LineSumArgs& a, cudaStream_t s);
+
+// out[entry] = sum over groups of partial[group][entry], in group order.
+cudaError_t launchLineSumReduce(const double* partial, int nGroups, int nEntries, double* out, cudaStream_t s);
+
+}  // namespace mcx

@@ -4,6 +4,7 @@
 #include "../../include/mcx.h"
 #include "k_emission.cuh"
 #include "k_balance.cuh"
+#include "k_lines.cuh"
 #include "k_dust.cuh"
 #include "k_opacity.cuh"
 #include "k_transport_launch.h"
@@ -371,6 +372,16 @@ struct mcx_ctx {
   DBuf<float> tdust;                 // [nSpecies+1][nSizes+1][nCells+1]
   DBuf<int32_t> lgConverged, lgBlack, nIterT;
   DBuf<float> forLines;
+  // outputGas: per multi-level atom the line factors a(j,i) E_ji (two-photon
+  // part removed) and wavelengths at [i-1][j-1], i lower, j upper level
+  struct LineAtom {
+    int elem = 0, ion = 0, nLev = 0;
+    std::vector<double> fac, wav;
+  };
+  std::vector<LineAtom> lineAtoms;
+  int xrefAll[30] = {};
+  DBuf<double> linePartial, lineSums;
+  DBuf<int32_t> lineForbBase;
   // mcx_state_save snapshot
   DBuf<float> snapTe, snapNe, snapTeOld, snapNeOld, snapIonDen;
   DBuf<int32_t> snapConverged;
@@ -694,6 +705,31 @@ extern "C" int mcx_load(mcx_ctx* c, const mcx_setup* m) {
     if (!em.empty()) return fail(c, MCX_ERR_INPUT, "mcx_load: " + em);
     std::string bl = balanceDataCreate(s, c->balance);
     if (!bl.empty()) return fail(c, MCX_ERR_INPUT, "mcx_load: " + bl);
+    // the line factors of equilibrium (source/emission_mod.f90:2987-3004)
+    c->lineAtoms.clear();
+    for (int a = 0; a < s.bal.nAtoms; ++a) {
+      const int32_t* h = s.bal.atomHdr.data() + (size_t)a * kAtHdrSize;
+      const double* D = s.bal.atomData.data();
+      mcx_ctx::LineAtom la;
+      la.elem = h[kAtElem]; la.ion = h[kAtIon]; la.nLev = h[kAtNLev];
+      const int n = la.nLev;
+      la.fac.assign((size_t)n * n, 0.);
+      la.wav.assign((size_t)n * n, 0.);
+      const double* A = D + h[kAtOffA];
+      const double* E = D + h[kAtOffE];
+      const double atp = D[h[kAtOffAtp]];
+      for (int i = 1; i <= n - 1; ++i)
+        for (int j = i + 1; j <= n; ++j) {
+          double aji = A[(size_t)(j - 1) * n + (i - 1)];
+          if (aji == 0.) continue;
+          const double Eji = E[j - 1] - E[i - 1];
+          if (j == h[kAtIup2p] && i == 1 && atp > 0.) aji = aji - atp;
+          la.fac[(size_t)(i - 1) * n + (j - 1)] = aji * Eji;
+          la.wav[(size_t)(i - 1) * n + (j - 1)] = Eji > 0. ? 1.e8 / Eji : 0.;
+        }
+      c->lineAtoms.push_back(std::move(la));
+    }
+    for (int z = 0; z < 30; ++z) c->xrefAll[z] = s.elemXref[z];
   }
   CK(cudaDeviceSynchronize(), "mcx_load");
   c->haveOpacity = c->haveRecPDF = c->haveDustPDF = false;
@@ -1126,6 +1162,114 @@ extern "C" int mcx_iterate(mcx_ctx* c, const mcx_iterate_opts* o, mcx_iterate_st
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
   return rc;
+}
+
+extern "C" int mcx_line_luminosities(mcx_ctx* c, mcx_lines* out) {
+  if (!c || !out) return fail(c, MCX_ERR_INPUT, "mcx_line_luminosities: null argument");
+  if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_line_luminosities: no model loaded");
+  if (!c->lgGas || !c->emission || !c->balance)
+    return fail(c, MCX_ERR_STATE, "mcx_line_luminosities: the grid holds no gas");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  const int S = c->nstages, C = c->nCells;
+  // entry layout of the partial sums (k_lines.cuh)
+  LineSumArgs a{};
+  a.te = c->te.p; a.ne = c->ne.p; a.ionDen = c->ionDen.p; a.hden = c->hden.p;
+  a.vol = c->volD.p; a.black = c->lgBlack.p;
+  a.nCells = C;
+  a.nGroups = (C + 31) / 32;
+  int n = 1;
+  a.hydroBase = n;
+  for (int iz = 1; iz <= 30; ++iz)
+    if (c->xrefAll[iz - 1] > 0 && S > iz) a.hydroIz[a.nHydro++] = iz;
+  n += kHydroLinesPerElem * a.nHydro;
+  a.heiBase = -1;
+  if (c->xrefAll[1] > 0) { a.heiBase = n; n += 34; }
+  a.ionBase = n;
+  for (int z = 1; z <= 30; ++z)
+    if (c->xrefAll[z - 1] > 0) {
+      a.ionElem[a.nIonElem++] = z;
+      n += 2 * std::min(z + 1, S);
+    }
+  std::vector<int32_t> forbBase(c->lineAtoms.size());
+  for (size_t k = 0; k < c->lineAtoms.size(); ++k) { forbBase[k] = n; n += c->lineAtoms[k].nLev; }
+  a.nEntries = n;
+  const size_t partialCount = (size_t)a.nGroups * (size_t)n;
+  if (c->linePartial.n < partialCount) CK(c->linePartial.alloc(partialCount), "alloc line sums");
+  if (c->lineSums.n < (size_t)n) CK(c->lineSums.alloc(n), "alloc line sums");
+  if (!forbBase.empty()) CK(upload(c->lineForbBase, forbBase), "upload line layout");
+  a.partial = c->linePartial.p;
+  a.forbBase = c->lineForbBase.p;
+
+  CK(cudaEventRecord(c->ev0, c->stream), "event");
+  CK(launchGasLineSums(c->emission->dev, a, c->stream), "line sums");
+  if (!forbBase.empty()) CK(launchForbLevelSums(*c->balance, a, c->stream), "forbidden-line sums");
+  CK(launchLineSumReduce(a.partial, a.nGroups, n, c->lineSums.p, c->stream), "line sum reduce");
+  CK(cudaEventRecord(c->ev1, c->stream), "event");
+  std::vector<double> sum(n);
+  std::vector<int32_t> black((size_t)C + 1);
+  CK(cudaMemcpyAsync(sum.data(), c->lineSums.p, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "d2h sums");
+  CK(cudaMemcpyAsync(black.data(), c->lgBlack.p, black.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream),
+     "d2h lgBlack");
+  CK(cudaStreamSynchronize(c->stream), "mcx_line_luminosities");
+  cudaEventElapsedTime(&out->kernel_ms, c->ev0, c->ev1);
+
+  // normalisation and units (source/output_mod.f90:684-805)
+  int nUsed = 0;
+  for (int cell = 1; cell <= C; ++cell) nUsed += black[cell] < 1 ? 1 : 0;
+  out->n_cells = nUsed;
+  double hb = sum[0];
+  const bool rel = hb > 0.;
+  out->relative = rel ? 1 : 0;
+  const double div = rel ? hb : 1.;
+  if (out->hydro_vol) {
+    std::fill(out->hydro_vol, out->hydro_vol + 30 * 14 * 8, 0.);
+    for (int k = 0; k < a.nHydro; ++k) {
+      const int iz = a.hydroIz[k];
+      int l = 0;
+      for (int iup = 2; iup <= 15; ++iup)
+        for (int ilow = 1; ilow <= std::min(8, iup - 1); ++ilow, ++l)
+          out->hydro_vol[(iz - 1) + 30 * (iup - 2) + 420 * (ilow - 1)] =
+              sum[a.hydroBase + kHydroLinesPerElem * k + l] / div;
+    }
+  }
+  if (out->hei_vol)
+    for (int l = 0; l < 34; ++l) out->hei_vol[l] = a.heiBase >= 0 ? sum[a.heiBase + l] / div : 0.;
+  const size_t forbN = (size_t)30 * S * 30 * 30;
+  if (out->forb_vol) std::fill(out->forb_vol, out->forb_vol + forbN, 0.);
+  if (out->wav) std::fill(out->wav, out->wav + forbN, 0.);
+  for (size_t k = 0; k < c->lineAtoms.size(); ++k) {
+    const auto& la = c->lineAtoms[k];
+    if (la.ion > S) continue;
+    const int nl = la.nLev;
+    for (int i = 1; i <= nl; ++i)
+      for (int j = 1; j <= nl; ++j) {
+        const size_t at = (size_t)(la.elem - 1) + 30 * (size_t)(la.ion - 1) + (size_t)30 * S * (i - 1) +
+                          (size_t)900 * S * (j - 1);
+        const double f = la.fac[(size_t)(i - 1) * nl + (j - 1)];
+        if (out->forb_vol && f != 0.) out->forb_vol[at] = f * sum[forbBase[k] + j - 1] / div;
+        if (out->wav) out->wav[at] = la.wav[(size_t)(i - 1) * nl + (j - 1)];
+      }
+  }
+  if (out->te_vol || out->ion_vol) {
+    if (out->te_vol) std::fill(out->te_vol, out->te_vol + (size_t)30 * S, 0.);
+    if (out->ion_vol) std::fill(out->ion_vol, out->ion_vol + (size_t)30 * S, 0.);
+    int p = 0;
+    for (int q = 0; q < a.nIonElem; ++q) {
+      const int elem = a.ionElem[q], top = std::min(elem + 1, S);
+      double denIon = 0.;
+      for (int ion = 1; ion <= top; ++ion) denIon = denIon + sum[a.ionBase + 2 * (p + ion - 1) + 1];
+      for (int ion = 1; ion <= top; ++ion, ++p) {
+        const double num = sum[a.ionBase + 2 * p], den = sum[a.ionBase + 2 * p + 1];
+        const size_t at = (size_t)(elem - 1) + 30 * (size_t)(ion - 1);
+        if (out->te_vol) out->te_vol[at] = den <= 0. ? 0. : num / den;
+        if (out->ion_vol) out->ion_vol[at] = denIon <= 0. ? 0. : den / denIon;
+      }
+    }
+  }
+  hb = hb * (double)1.e-16f;
+  if (c->symmetric) hb = 8. * hb;
+  out->hbeta_vol = hb;
+  return MCX_OK;
 }
 
 extern "C" int mcx_timer_start(mcx_ctx* c) {

@@ -171,6 +171,32 @@ class Context:
         self._check(lib().mcx_iterate(self._h, C.byref(o), C.byref(st)))
         return st
 
+    def line_luminosities(self) -> dict:
+        """outputGas's analytical line luminosities and ionic volume averages from the current state
+        (source/output_mod.f90:13-805).
+
+        Returns hbeta_vol [1e36 erg/s] (x8 in symmetricXYZ mode), relative (line sums divided by
+        HbetaVol), n_cells, kernel_ms, hydro[30,14,8] at [iz-1, iup-2, ilow-1], hei[34],
+        forb and wav [30, nstages, 30, 30] at [elem-1, ion-1, i-1, j-1] (i lower, j upper level),
+        te_vol and ion_vol [30, nstages] at [elem-1, ion-1]."""
+        S = self.setup.info.nstages
+        hydro = np.zeros(30 * 14 * 8)
+        hei = np.zeros(34)
+        forb = np.zeros(30 * S * 30 * 30)
+        wav = np.zeros(30 * S * 30 * 30)
+        te_vol = np.zeros(30 * S)
+        ion_vol = np.zeros(30 * S)
+        o = abi.Lines(hydro_vol=hydro.ctypes.data, hei_vol=hei.ctypes.data, forb_vol=forb.ctypes.data,
+                      wav=wav.ctypes.data, te_vol=te_vol.ctypes.data, ion_vol=ion_vol.ctypes.data)
+        self._check(lib().mcx_line_luminosities(self._h, C.byref(o)))
+        # the ABI arrays are column-major (the reference's layouts): reverse the axes
+        return dict(hbeta_vol=o.hbeta_vol, relative=bool(o.relative), n_cells=int(o.n_cells),
+                    kernel_ms=float(o.kernel_ms),
+                    hydro=hydro.reshape(8, 14, 30).transpose(2, 1, 0).copy(),
+                    hei=hei, forb=forb.reshape(30, 30, S, 30).transpose(3, 2, 1, 0).copy(),
+                    wav=wav.reshape(30, 30, S, 30).transpose(3, 2, 1, 0).copy(),
+                    te_vol=te_vol.reshape(S, 30).T.copy(), ion_vol=ion_vol.reshape(S, 30).T.copy())
+
     def state_save(self) -> None:
         """Device-side snapshot of Te, Ne, ionDen, TeOld, NeOld, lgConverged."""
         self._check(lib().mcx_state_save(self._h))

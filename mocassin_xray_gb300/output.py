@@ -1,0 +1,109 @@
+"""Writers of outputGas's analytical result files (source/output_mod.f90:812-1160)
+from Context.line_luminosities():
+
+* ``lineFlux.out``    - Hbeta [1e36 erg/s] and every line relative to it: the
+  hydrogenic recombination lines, the 34 HeI recombination lines and the
+  forbidden lines of the ions with multi-level data;
+* ``temperature.out`` - the mean ionic temperatures Te(elem, ion);
+* ``ionratio.out``    - the mean ionic fractions <ion> (Harrington et al. 1982).
+
+Column order and line numbering (iLine) follow the reference's writers; the
+number formatting is plain whitespace-separated text rather than Fortran's
+list-directed layout, so readers that split on whitespace see the same
+columns.
+"""
+from __future__ import annotations
+
+from pathlib import Path
+
+import numpy as np
+
+from . import abi
+from .model import Context, Setup
+
+
+def _elements_on(setup: Setup) -> np.ndarray:
+    return setup.get(abi.SARR_ELEM_XREF)[:30] > 0
+
+
+def write_line_flux(path: str | Path, lines: dict, setup: Setup) -> None:
+    """lineFlux.out (source/output_mod.f90:812-1025, the iAb = 0 block without the
+    lgDebug Monte Carlo columns)."""
+    on = _elements_on(setup)
+    S = setup.info.nstages
+    hei_wav = setup.get(abi.SARR_EM_HEI_REC).reshape(34, 3, 4)[:, 0, 3]
+    out = [" Totals integrated over all nebular components: ", "", "",
+           " Line Ratios (Hbeta=1.) :               Analytical",
+           f" Hbeta [E36 erg/s]:     {lines['hbeta_vol']:.9g}", "",
+           " Hydrogenic recombination lines:", ""]
+    iline = 1
+    for iz in range(1, 31):
+        if not on[iz - 1]:
+            continue
+        for iup in range(2, 16):
+            for ilow in range(1, min(8, iup - 1) + 1):
+                wave = np.float32(iz * iz) * np.float32(109677.576) * (np.float32(1.0 / (ilow * ilow)) -
+                                                                       np.float32(1.0 / (iup * iup)))
+                wave = np.float32(1.e8) / wave
+                out.append(f" {iz:11d} {iup:11d} {ilow:11d} {float(wave):14.7g} "
+                           f"{lines['hydro'][iz - 1, iup - 2, ilow - 1]:16.8g} {iline:11d}")
+                iline += 1
+    out += ["", " HeI", "  lambda [A]   I/I(Hbeta)  "]
+    for l in range(34):
+        out.append(f" {float(hei_wav[l]):14.7g} {lines['hei'][l]:16.8g} {iline:11d}")
+        iline += 1
+    out += ["", " Heavy ions forbidden lines", "",
+            "  Z    Ion    lowlev  highlev   lambda[A] I/I(Hbeta)  index"]
+    forb = lines["forb"]
+    wav = lines.get("wav", np.zeros_like(forb))
+    atom_index = setup.get(abi.SARR_ATOM_INDEX).reshape(30, 31)
+    for elem in range(3, 31):
+        if not on[elem - 1]:
+            continue
+        for ion in range(1, min(elem + 1, S) + 1):
+            if atom_index[elem - 1, ion - 1] < 0:
+                continue    # no multi-level data for this ion (lgDataAvailable)
+            block = forb[elem - 1, ion - 1]
+            for i in range(1, 31):
+                for j in range(1, 31):
+                    if block[i - 1, j - 1] > 0.0:
+                        out.append(f"{elem:5d}  {ion:5d}  {i:5d}  {j:5d}  {wav[elem - 1, ion - 1, i - 1, j - 1]:12.2f}"
+                                   f"  {block[i - 1, j - 1]:12.2g}  {iline:5d}")
+                    iline += 1
+    Path(path).write_text("\n".join(out) + "\n")
+
+
+def write_temperature(path: str | Path, lines: dict, setup: Setup) -> None:
+    """temperature.out (source/output_mod.f90:1079-1118)."""
+    S = setup.info.nstages
+    out = ["", " Mean ionic temperatures Te(ion)", "", " Total, integrated over all nebular components",
+           " Element      Ion        Te(Element,ion)", ""]
+    for elem in range(1, 31):
+        for ion in range(1, S + 1):
+            out.append(f" {elem:11d} {ion:11d} {lines['te_vol'][elem - 1, ion - 1]:16.8g}")
+    Path(path).write_text("\n".join(out) + "\n")
+
+
+def write_ionratio(path: str | Path, lines: dict, setup: Setup) -> None:
+    """ionratio.out (source/output_mod.f90:1084-1128)."""
+    S = setup.info.nstages
+    out = ["", " Mean ionic ratio <ion>/<H+>", "", " Total, integrated over all nebular components", "",
+           " Element      Ion        <ion>/<H+>I     <ion>/<H+>II", ""]
+    for elem in range(1, 31):
+        for ion in range(1, S + 1):
+            out.append(f" {elem:11d} {ion:11d} {lines['ion_vol'][elem - 1, ion - 1]:16.8g}")
+    Path(path).write_text("\n".join(out) + "\n")
+
+
+def output_gas(ctx: Context, out_dir: str | Path) -> dict:
+    """outputGas for the context's current grid state: computes the line luminosities on the device
+    and writes lineFlux.out, temperature.out and ionratio.out into out_dir.  Returns the sums."""
+    if ctx.setup is None:
+        raise RuntimeError("output_gas: no model loaded")
+    d = Path(out_dir)
+    d.mkdir(parents=True, exist_ok=True)
+    lines = ctx.line_luminosities()
+    write_line_flux(d / "lineFlux.out", lines, ctx.setup)
+    write_temperature(d / "temperature.out", lines, ctx.setup)
+    write_ionratio(d / "ionratio.out", lines, ctx.setup)
+    return lines

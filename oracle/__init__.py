@@ -206,13 +206,10 @@ def transport(setup, opacity_arr, rec_pdf, total_lines, ne=None, n: int = 1000, 
     return j, e, st
 
 
-def emission(setup, gaunt_te: float, te=None, ne=None, ionden=None, compute=None, for_lines=None,
-             rec_pdf=None, total_lines=None):
-    """Oracle emission phase for a mocassin_xray_gb300.Setup: returns (recPDF [nbins][C+1], totalLines [C+1]).
-    `gaunt_te` is the temperature of the last Gaunt tabulation of the opacity phase."""
+def _emission_struct(setup, te=None, ne=None, ionden=None):
+    """EmissionIn for a Setup and a grid state, with the arrays it points at (keep them alive)."""
     from mocassin_xray_gb300 import abi
     i = setup.info
-    C1, nb = i.n_cells + 1, i.nbins
     dims = setup.get(abi.SARR_EM_DIMS)
     k = dict(
         nu=setup.get(abi.ARR_NU), wid=setup.get(abi.ARR_WIDFLX), xsec=setup.get(abi.ARR_XSEC),
@@ -228,9 +225,32 @@ def emission(setup, gaunt_te: float, te=None, ne=None, ionden=None, compute=None
         ne=np.ascontiguousarray(ne if ne is not None else setup.get(abi.ARR_NE), dtype=np.float32),
         ion=np.ascontiguousarray(ionden if ionden is not None else setup.get(abi.ARR_IONDEN), dtype=np.float32),
     )
+    s = EmissionIn(n_cells=i.n_cells, nbins=i.nbins, nstages=i.nstages, n_elem_used=max(i.n_elem_used, 1),
+                   n_xsec=k["xsec"].size, n_fb_heavy=int(dims[4]), n_tk=int(dims[0]), j2ts_p=int(dims[6]))
+    s.nlim[:] = [int(x) for x in dims[1:4]]
+    s.heii_lyman_p[:] = [int(x) for x in dims[7:11]]
+    for f, key in (("nu", "nu"), ("widflx", "wid"), ("xsec", "xsec"), ("ptr", "ptr"), ("elem_abun", "abun"),
+                   ("elem_xref", "xref"), ("tk", "tk"), ("gamma_edge_p", "edge"), ("log_gamma", "lg"),
+                   ("fb_heavy", "fb"), ("hei2phot", "h2"),
+                   ("heii_lyman", "ly"), ("hydro_file_map", "hmap"), ("hydro_dens", "hdens"),
+                   ("hydro_lines", "hlines"), ("hydro_temps", "htemps"), ("hb_coeff", "hb"), ("rb_edge", "rb"),
+                   ("r2a_edge", "r2a"), ("hei_rec", "heirec"), ("te", "te"), ("ne", "ne"), ("ionden", "ion")):
+        setattr(s, f, _p(k[key]))
+    return s, k
+
+
+def emission(setup, gaunt_te: float, te=None, ne=None, ionden=None, compute=None, for_lines=None,
+             rec_pdf=None, total_lines=None):
+    """Oracle emission phase for a mocassin_xray_gb300.Setup: returns (recPDF [nbins][C+1], totalLines [C+1]).
+    `gaunt_te` is the temperature of the last Gaunt tabulation of the opacity phase."""
+    i = setup.info
+    C1, nb = i.n_cells + 1, i.nbins
+    s, k = _emission_struct(setup, te, ne, ionden)
     nu = k["nu"]
     k["g1"] = gaunt_ff(0.0, math.log10(gaunt_te), nu).astype(np.float32)
     k["g2"] = gaunt_ff(0.30103, math.log10(gaunt_te), nu).astype(np.float32)
+    s.gaunt_ff = _p(k["g1"])
+    s.gaunt_ff_heii = _p(k["g2"])
     fl = None if for_lines is None else np.ascontiguousarray(for_lines, dtype=np.float32)
     if compute is None:
         compute = np.ones(C1, dtype=np.uint8)
@@ -240,17 +260,6 @@ def emission(setup, gaunt_te: float, te=None, ne=None, ionden=None, compute=None
         rec_pdf = np.zeros((nb, C1), dtype=np.float32)
     if total_lines is None:
         total_lines = np.zeros(C1, dtype=np.float32)
-    s = EmissionIn(n_cells=i.n_cells, nbins=nb, nstages=i.nstages, n_elem_used=max(i.n_elem_used, 1),
-                   n_xsec=k["xsec"].size, n_fb_heavy=int(dims[4]), n_tk=int(dims[0]), j2ts_p=int(dims[6]))
-    s.nlim[:] = [int(x) for x in dims[1:4]]
-    s.heii_lyman_p[:] = [int(x) for x in dims[7:11]]
-    for f, key in (("nu", "nu"), ("widflx", "wid"), ("xsec", "xsec"), ("ptr", "ptr"), ("elem_abun", "abun"),
-                   ("elem_xref", "xref"), ("tk", "tk"), ("gamma_edge_p", "edge"), ("log_gamma", "lg"),
-                   ("fb_heavy", "fb"), ("gaunt_ff", "g1"), ("gaunt_ff_heii", "g2"), ("hei2phot", "h2"),
-                   ("heii_lyman", "ly"), ("hydro_file_map", "hmap"), ("hydro_dens", "hdens"),
-                   ("hydro_lines", "hlines"), ("hydro_temps", "htemps"), ("hb_coeff", "hb"), ("rb_edge", "rb"),
-                   ("r2a_edge", "r2a"), ("hei_rec", "heirec"), ("te", "te"), ("ne", "ne"), ("ionden", "ion")):
-        setattr(s, f, _p(k[key]))
     s.for_lines = _p(fl)
     s.compute = _p(compute)
     rc = lib().orc_emission(C.byref(s), _p(rec_pdf), _p(total_lines))
@@ -465,3 +474,72 @@ def dust_t(t: DustTables, jste, tdust):
     st = DustStats()
     _dust_lib().orc_dust_t(C.byref(t.s), _p(j), _p(td.reshape(-1)), _p(conv), _p(black), C.byref(st))
     return td, conv, black, st
+
+
+def cell_volumes(setup) -> np.ndarray:
+    """getVolume (source/grid_mod.f90:2887-2986) of every active cell in FP64 [e45 cm^3], [C+1]."""
+    from mocassin_xray_gb300 import abi
+    i = setup.info
+    keep = dict(x=setup.get(abi.ARR_XAXIS), y=setup.get(abi.ARR_YAXIS), z=setup.get(abi.ARR_ZAXIS))
+    s = TransportIn(nx=i.nx, ny=i.ny, nz=i.nz, n_cells=i.n_cells, symmetric_xyz=i.symmetric_xyz,
+                    x_axis=_p(keep["x"]), y_axis=_p(keep["y"]), z_axis=_p(keep["z"]))
+    l = lib()
+    l.orc_cell_volume.argtypes = [C.POINTER(TransportIn), C.c_int32, C.c_int32, C.c_int32]
+    l.orc_cell_volume.restype = C.c_double
+    act = setup.get(abi.ARR_ACTIVE).reshape(i.nz, i.ny, i.nx)
+    vol = np.zeros(i.n_cells + 1, dtype=np.float64)
+    for kk, jj, ii in zip(*np.nonzero(act > 0)):
+        vol[act[kk, jj, ii]] = l.orc_cell_volume(C.byref(s), int(ii) + 1, int(jj) + 1, int(kk) + 1)
+    return vol
+
+
+class LinesOut(C.Structure):
+    _fields_ = [("hbeta", C.c_double), ("hydro", _P), ("hei", _P), ("forb", _P), ("ion_num", _P),
+                ("ion_den", _P), ("n_cells", C.c_int64)]
+
+
+def line_luminosities(setup, tables: BalanceTables, te, ne, ionden, black, vol=None) -> dict:
+    """outputGas's analytical line luminosities from a grid state (source/output_mod.f90:280-805).
+
+    Returns hbeta_vol [1e36 erg/s] (x8 in symmetricXYZ mode), relative (lines divided by HbetaVol),
+    n_cells, hydro[30,14,8] at [iz-1, iup-2, ilow-1], hei[34], forb[30, nstages, 30, 30] at
+    [elem-1, ion-1, i-1, j-1] (i lower, j upper level), te_vol and ion_vol [30, nstages]."""
+    i = setup.info
+    S = i.nstages
+    em, keep = _emission_struct(setup, te, ne, ionden)
+    if vol is None:
+        vol = cell_volumes(setup)
+    vol = np.ascontiguousarray(vol, dtype=np.float64)
+    bl = np.ascontiguousarray(black, dtype=np.int32)
+    n_atoms = tables.s.n_atoms
+    hydro = np.zeros((30, 14, 8))
+    hei = np.zeros(34)
+    forb = np.zeros((max(n_atoms, 1), 30, 30))
+    num = np.zeros((30, S))
+    den = np.zeros((30, S))
+    out = LinesOut(hydro=_p(hydro), hei=_p(hei), forb=_p(forb), ion_num=_p(num), ion_den=_p(den))
+    l = lib()
+    l.orc_line_sums.argtypes = [C.POINTER(EmissionIn), C.POINTER(BalanceIn), _P, _P, C.POINTER(LinesOut)]
+    l.orc_line_sums.restype = C.c_int
+    rc = l.orc_line_sums(C.byref(em), C.byref(tables.s), _p(vol), _p(bl), C.byref(out))
+    if rc != 0:
+        raise RuntimeError(f"orc_line_sums failed: {rc}")
+    # normalisation (source/output_mod.f90:684-805)
+    hb = out.hbeta
+    rel = hb > 0.0
+    d = hb if rel else 1.0
+    forb_full = np.zeros((30, S, 30, 30))
+    aidx = tables.k["aidx"].reshape(30, 31)
+    for elem in range(1, 31):
+        for ion in range(1, S + 1):
+            a = int(aidx[elem - 1, ion - 1]) if ion <= 31 else -1
+            if a >= 0:
+                forb_full[elem - 1, ion - 1] = forb[a] / d
+    te_vol = np.where(den > 0.0, num / np.where(den > 0.0, den, 1.0), 0.0)
+    tot = den.sum(axis=1, keepdims=True)
+    ion_vol = np.where(tot > 0.0, den / np.where(tot > 0.0, tot, 1.0), 0.0)
+    hbv = hb * float(np.float32(1.e-16))
+    if i.symmetric_xyz:
+        hbv = 8.0 * hbv
+    return dict(hbeta_vol=hbv, relative=bool(rel), n_cells=int(out.n_cells), hydro=hydro / d, hei=hei / d,
+                forb=forb_full, te_vol=te_vol, ion_vol=ion_vol)

@@ -274,7 +274,8 @@ int orc_emission(const orc_emission_in* in, float* rec_pdf, float* total_lines) 
                         if (idenp < 13) {
                             double w = (Ne - (double)dens[idenp - 1]) / ((double)dens[idenp] - (double)dens[idenp - 1]);
                             yy1 = e3[idenp - 1] + ((double)e3[idenp - 1] - e3[idenp]) * w;
-                            yy2 = e3[9 + idenp - 1] + ((double)e3[9 + idenp - 1] - e3[9 + idenp]) * w;
+                            /* r2aEdge(3, 9+idenp+1) lies past the table for idenp = 9: read as r2aEdge(3,18) */
+                            yy2 = e3[9 + idenp - 1] + ((double)e3[9 + idenp - 1] - e3[9 + idenp < 18 ? 9 + idenp : 17]) * w;
                         } else { yy1 = e3[idenp - 1]; yy2 = e3[9 + idenp - 1]; }
                         x1 = e1[0]; x2 = e1[9];
                     }

@@ -240,6 +240,24 @@ int orc_equilibrium(const orc_balance_in* in, int32_t atom, double te, double ne
 int orc_for_lines_emission(const orc_balance_in* in, const float* te, const float* ne, const float* ionden,
                            const uint8_t* compute, double* for_lines);
 
+/* ---------------------------------------------------------------- lines */
+typedef struct orc_lines_out {
+    double hbeta;               /* sum of hydroLines(1,4,2)*Hden*dV over the terms > 1e-35 */
+    double* hydro;              /* [30][14][8] hydroVol at [iz-1][iup-2][ilow-1]            */
+    double* hei;                /* [34] HeIVol                                              */
+    double* forb;               /* [n_atoms][30][30] forbVol of atom slot at [i-1][j-1],
+                                   i the lower and j the upper level                        */
+    double* ion_num;            /* [30][nstages] sum ionDen*Te*Ne*Hden*dV                   */
+    double* ion_den;            /* [30][nstages] sum ionDen*Ne*Hden*dV                      */
+    int64_t n_cells;            /* cells summed                                             */
+} orc_lines_out;
+
+/* outputGas's volume sums (source/output_mod.f90:280-680) over the cells with
+ * black[c] < 1, from the grid state em->te, em->ne, em->ionden and bal->hden,
+ * with the FP64 cell volumes vol[C+1].  Raw sums, not yet divided by Hbeta. */
+int orc_line_sums(const orc_emission_in* em, const orc_balance_in* bal, const double* vol, const int32_t* black,
+                  orc_lines_out* out);
+
 /* ----------------------------------------------------------------- dust */
 typedef struct orc_dust_in {
     int32_t n_cells, nbins, n_species, n_sizes;
