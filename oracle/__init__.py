@@ -543,3 +543,46 @@ def line_luminosities(setup, tables: BalanceTables, te, ne, ionden, black, vol=N
         hbv = 8.0 * hbv
     return dict(hbeta_vol=hbv, relative=bool(rel), n_cells=int(out.n_cells), hydro=hydro / d, hei=hei / d,
                 forb=forb_full, te_vol=te_vol, ion_vol=ion_vol)
+
+
+def iterate_chain(setup, n_photons: int, iterations: int, seed: int, nthreads: int = 8, tables=None):
+    """The loop body of iterateMC (source/iteration_mod.f90:98-1260) repeated `iterations` times from the
+    set-up's initial state, all in the oracle: the skip rule of the opacity and emission loops
+    (:131-149, :340-356), opacity with the Gaunt cache, emission with its forbidden lines, transport of
+    the packets [(it-1)*2^40, (it-1)*2^40 + n_photons) of Philox key `seed`, J x 1e-9 (and / 8 in
+    symmetricXYZ mode), then updateCell for every cell.  Returns (te, ne, ionden, black)."""
+    from mocassin_xray_gb300 import abi
+    i = setup.info
+    C1, nb = i.n_cells + 1, i.nbins
+    T = tables if tables is not None else BalanceTables(setup)
+    te = setup.get(abi.ARR_TE).astype(np.float32)
+    ne = setup.get(abi.ARR_NE).astype(np.float32)
+    ion = setup.get(abi.ARR_IONDEN).astype(np.float32)
+    te_old, ne_old = setup.get(abi.ARR_TEOLD).astype(np.float32), setup.get(abi.ARR_NEOLD).astype(np.float32)
+    active = setup.get(abi.ARR_ACTIVE)
+    op = np.zeros((nb, C1), np.float32)
+    rec = np.zeros((nb, C1), np.float32)
+    tl = np.zeros(C1, np.float32)
+    gaunt_last = -1.0
+    black = np.zeros(C1, np.int32)
+    for it in range(1, iterations + 1):
+        comp = np.ones(C1, np.uint8)
+        if it > 1:
+            with np.errstate(divide="ignore", invalid="ignore"):
+                skip = (np.abs(te - te_old) / te_old < np.float32(0.005)) & \
+                       (np.abs(ne - ne_old) / ne_old < np.float32(0.005))
+            comp[skip] = 0
+        comp[0] = 0
+        gte, gaunt_last = gaunt_cache(i.nx, i.ny, i.nz, active, te, comp, gaunt_last)
+        op = opacity(setup, te, ne, ion, gaunt_te=gte, compute=comp, out=op)
+        fl = for_lines_emission(T, te, ne, ion, comp)
+        rec, tl = emission(setup, gaunt_last, te, ne, ion, compute=comp, for_lines=fl, rec_pdf=rec, total_lines=tl)
+        j, _, _ = transport(setup, op, rec, tl, ne=ne, n=n_photons, seed=seed, counter_base=(it - 1) << 40,
+                            nthreads=nthreads)
+        j = j * 1e-9
+        if i.symmetric_xyz:
+            j = j / 8.0
+        te_old, ne_old = te.copy(), ne.copy()
+        te, ne, ion, _, black, _, _ = balance(T, j, te, ne, ion, nthreads=nthreads)
+        te, ne, ion = te.astype(np.float32), ne.astype(np.float32), ion.astype(np.float32)
+    return te, ne, ion, black
