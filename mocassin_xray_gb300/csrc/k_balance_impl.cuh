@@ -614,22 +614,117 @@ __device__ __forceinline__ real splineEval(const SplineAt& s, const real* ya, co
   return s.a * ya[s.klo - 1] + s.bb * ya[s.khi - 1] + (s.a3 * y2a[s.klo - 1] + s.b3 * y2a[s.khi - 1]) * s.hh / (real)6.;
 }
 
-// equilibrium of one atom: the normalised level populations y[1..nLev]
-// (source/emission_mod.f90:2884-2984).  Collision rates in the rate
-// precision, the rate matrix and its LU solve in FP64.
-__device__ __forceinline__ void equilibriumPops(const BalanceDev& b, int atom, double Te, double Ne, double ionDenUp,
-                                                bool rec, double* y) {
-  const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
+// The collision rate coefficients qeff of every level pair (source/emission_mod.f90:2884-2936):
+// f(lo, up, qeff(lo,up), qeff(up,lo)) for lo < up, in the rate precision.
+template <typename F>
+__device__ __forceinline__ void collisionPairs(const BalanceDev& b, const int32_t* h, real TeR, real sqrTe,
+                                               real log10Te, F f) {
   const real* D = atomTable(b);
-  const double* DD = b.atomData;
+  const double* eD = b.atomData + h[kAtOffE];
   const int nLev = h[kAtNLev], nT = h[kAtNTemp];
   const real* logT = D + h[kAtOffLogT];
   const real* qom = D + h[kAtOffQom];
   const real* y2 = D + h[kAtOffY2];
-  const double* A = DD + h[kAtOffA];
   const real* g = D + h[kAtOffG];
   const real* e = D + h[kAtOffE];
-  const double* eD = DD + h[kAtOffE];
+  const SplineAt sp = nT > 2 ? splineAt(logT, nT, log10Te) : SplineAt{};
+  const real constant = (real)1.4388463, c863 = (real)8.63e-6;
+  int p = 0;
+  for (int i = 2; i <= nLev; ++i) {
+    for (int j = i; j <= nLev; ++j, ++p) {
+      const real* qq = qom + (size_t)p * nT;
+      real cs;
+      if (nT == 1) cs = qq[0];
+      else if (nT == 2) cs = qq[0] + (qq[1] - qq[0]) / (logT[1] - logT[0]) * (log10Te - logT[0]);
+      else cs = splineEval(sp, qq, y2 + (size_t)p * nT, nT);
+      if (eD[i - 2] <= eD[j - 1]) {
+        real expFac = exp((e[i - 2] - e[j - 1]) * constant / TeR);
+        f(i - 1, j, c863 * cs * expFac / (g[i - 2] * sqrTe), c863 * cs / (g[j - 1] * sqrTe));
+      } else {
+        real expFac = exp((e[j - 1] - e[i - 2]) * constant / TeR);
+        f(i - 1, j, c863 * cs / (g[j - 1] * sqrTe), c863 * cs * expFac / (g[i - 2] * sqrTe));
+      }
+    }
+  }
+}
+
+#if !MCX_BAL_EXACT
+// The same populations by state reduction in FP32 (Grassmann, Taksar & Heyman,
+// Oper. Res. 33 (1985) 1107).  Rows 2..n of equilibrium's matrix are the
+// balance of level i between the rates r(j->i) = Ne qeff(j,i) + a(j,i) into it,
+// the rates out of it and, with rec, a recombination source
+// s_i = Ne ionDenUp alpha_i; row 1 is the normalisation.  Eliminating levels
+// n..2 redirects the flows through each removed level k in proportion to its
+// exits r(k->j) / D_k, D_k = sum_{j<k} r(k->j), and back-substitution gives
+// n_k = n_1 u_k + v_k with u_k the share fed from level 1 and v_k the share
+// fed by the sources; the normalisation fixes n_1.  Every step adds or
+// multiplies non-negative numbers, so each population keeps a relative error
+// of a few FP32 ulps whatever the spread of the rates; the unpivoted LU of the
+// reference cancels and needs FP64.  Returns false (the caller falls back to
+// the FP64 LU) when a level has no exit to the levels below it.
+__device__ __forceinline__ bool gthPops(const BalanceDev& b, const int32_t* h, double Ne, double ionDenUp, bool rec,
+                                        const double* alphaTotal, real TeR, real sqrTe, real log10Te, double* y) {
+  const int n = h[kAtNLev];
+  const double* A = b.atomData + h[kAtOffA];
+  const float NeF = (float)Ne;
+  float R[kMaxLevels + 1][kMaxLevels + 1];   // R[a][c]: rate from level a to level c
+  for (int i = 1; i <= n; ++i)
+    for (int j = 1; j <= n; ++j) R[i][j] = 0.f;
+  collisionPairs(b, h, TeR, sqrTe, log10Te, [&](int lo, int up, real qLoUp, real qUpLo) {
+    R[lo][up] = NeF * qLoUp;
+    R[up][lo] = NeF * qUpLo + (float)A[(size_t)(up - 1) * n + (lo - 1)];
+  });
+  float src[kMaxLevels + 1], Dk[kMaxLevels + 1];
+  for (int i = 1; i <= n; ++i) src[i] = (rec && i >= 2) ? (float)(Ne * ionDenUp * alphaTotal[i]) : 0.f;
+  for (int k = n; k >= 2; --k) {
+    float d = 0.f;
+    for (int j = 1; j < k; ++j) d += R[k][j];
+    if (!(d > 0.f) || !(d < 3.0e38f)) return false;
+    Dk[k] = d;
+    const float rd = 1.f / d;
+    for (int i = 1; i < k; ++i) {
+      const float fi = R[i][k] * rd;
+      if (fi != 0.f)
+        for (int j = 1; j < k; ++j) R[i][j] += fi * R[k][j];   // R[i][i] collects unused self-loops
+    }
+    if (rec) {
+      const float fs = src[k] * rd;
+      if (fs != 0.f)
+        for (int j = 2; j < k; ++j) src[j] += fs * R[k][j];
+    }
+  }
+  float u[kMaxLevels + 1], v[kMaxLevels + 1];
+  u[1] = 1.f;
+  v[1] = 0.f;
+  float su = 0.f, sv = 0.f;
+  for (int k = 2; k <= n; ++k) {
+    float a = 0.f, c = rec ? src[k] : 0.f;
+    for (int i = 1; i < k; ++i) {
+      a += u[i] * R[i][k];
+      if (rec) c += v[i] * R[i][k];
+    }
+    u[k] = a / Dk[k];
+    v[k] = c / Dk[k];
+    su += u[k];
+    sv += v[k];
+  }
+  const float n1 = (1.f - sv) / (1.f + su);
+  y[1] = n1;
+  for (int k = 2; k <= n; ++k) y[k] = (double)(n1 * u[k] + v[k]);
+  return true;
+}
+#endif
+
+// equilibrium of one atom: the normalised level populations y[1..nLev]
+// (source/emission_mod.f90:2884-2984).  Collision rates in the rate
+// precision; the FP64 path solves the rate matrix by the reference's
+// unpivoted LU, the mixed path by FP32 state reduction (gthPops).
+__device__ __forceinline__ void equilibriumPops(const BalanceDev& b, int atom, double Te, double Ne, double ionDenUp,
+                                                bool rec, double* y) {
+  const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
+  const double* DD = b.atomData;
+  const int nLev = h[kAtNLev];
+  const double* A = DD + h[kAtOffA];
   const real TeR = (real)Te;
   const real sqrTe = sqrt(TeR), log10Te = log10(TeR);
   double alphaTotal[kMaxLevels + 1];
@@ -662,33 +757,19 @@ __device__ __forceinline__ void equilibriumPops(const BalanceDev& b, int atom, d
       }
     }
   }
+#if !MCX_BAL_EXACT
+  if (gthPops(b, h, Ne, ionDenUp, rec, alphaTotal, TeR, sqrTe, log10Te, y)) return;
+#endif
   real qeff[kMaxLevels + 1][kMaxLevels + 1];
   double x[kMaxLevels + 1][kMaxLevels + 1];
   for (int i = 1; i <= nLev; ++i) {
     y[i] = 0.;
     for (int j = 1; j <= nLev; ++j) { qeff[i][j] = 0; x[i][j] = 0.; }
   }
-  const SplineAt sp = nT > 2 ? splineAt(logT, nT, log10Te) : SplineAt{};
-  const real constant = (real)1.4388463, c863 = (real)8.63e-6;
-  int p = 0;
-  for (int i = 2; i <= nLev; ++i) {
-    for (int j = i; j <= nLev; ++j, ++p) {
-      const real* qq = qom + (size_t)p * nT;
-      real cs;
-      if (nT == 1) cs = qq[0];
-      else if (nT == 2) cs = qq[0] + (qq[1] - qq[0]) / (logT[1] - logT[0]) * (log10Te - logT[0]);
-      else cs = splineEval(sp, qq, y2 + (size_t)p * nT, nT);
-      if (eD[i - 2] <= eD[j - 1]) {
-        real expFac = exp((e[i - 2] - e[j - 1]) * constant / TeR);
-        qeff[i - 1][j] = c863 * cs * expFac / (g[i - 2] * sqrTe);
-        qeff[j][i - 1] = c863 * cs / (g[j - 1] * sqrTe);
-      } else {
-        real expFac = exp((e[j - 1] - e[i - 2]) * constant / TeR);
-        qeff[j][i - 1] = c863 * cs * expFac / (g[i - 2] * sqrTe);
-        qeff[i - 1][j] = c863 * cs / (g[j - 1] * sqrTe);
-      }
-    }
-  }
+  collisionPairs(b, h, TeR, sqrTe, log10Te, [&](int lo, int up, real qLoUp, real qUpLo) {
+    qeff[lo][up] = qLoUp;
+    qeff[up][lo] = qUpLo;
+  });
   for (int j = 1; j <= nLev; ++j) x[1][j] = 1.;
   y[1] = 1.;
   for (int i = 2; i <= nLev; ++i) {

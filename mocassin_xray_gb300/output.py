@@ -107,3 +107,53 @@ def output_gas(ctx: Context, out_dir: str | Path) -> dict:
     write_temperature(d / "temperature.out", lines, ctx.setup)
     write_ionratio(d / "ionratio.out", lines, ctx.setup)
     return lines
+
+
+_C_LIGHT = 2.9979250e10        # c [cm/s] (source/constants_mod.f90:12)
+_FR1RYD = 3.28984e15           # frequency of 1 Ryd [Hz] (source/constants_mod.f90:13)
+_RADIO_4P9GHZ = 1.489434e-6    # 4.9 GHz in Ryd (source/constants_mod.f90:19)
+
+
+def _radio_pointer(nu: np.ndarray) -> int:
+    """radio4p9GHzP of the frequency mesh (source/grid_mod.f90:383-389): set only for the
+    nuMax <= 25 mesh that starts at or below 4.9 GHz, else left 0."""
+    if nu[-1] > 25.0 or nu[0] > _RADIO_4P9GHZ:
+        return 0
+    p = int(np.searchsorted(nu, np.float32(_RADIO_4P9GHZ), side="right"))   # locate: last nu <= x
+    if p < nu.size and _RADIO_4P9GHZ > (float(nu[p - 1]) + float(nu[p])) / 2.0:
+        p += 1
+    return p
+
+
+def sed(setup: Setup, escaped: np.ndarray) -> tuple[np.ndarray, float]:
+    """SED(freq) of writeSED (source/output_mod.f90:2984-3015): escapedPackets summed over the cells,
+    times 8 in symmetricXYZ mode; returns (SED [nbins] in e36 erg/s per bin, total energy)."""
+    nb = setup.info.nbins
+    esc = np.asarray(escaped, dtype=np.float64).reshape(nb + 1, -1)
+    s = esc[1:, :].sum(axis=1)
+    if setup.info.symmetric_xyz:
+        s = s * 8.0
+    return s, float(s.sum())
+
+
+def write_sed(path: str | Path, setup: Setup, escaped: np.ndarray) -> float:
+    """SED.out (source/output_mod.f90:2947-3064) for the integrated direction (no viewing angles):
+    nu [Ryd], lambda [um] and nu*F(nu) per row, the total energy and, where the mesh reaches
+    4.9 GHz, the radio flux.  Returns the total energy radiated [e36 erg/s]."""
+    nu = setup.get(abi.ARR_NU).astype(np.float64)
+    wid = setup.get(abi.ARR_WIDFLX).astype(np.float64)
+    s, total = sed(setup, escaped)
+    out = [" Spectral energy distribution at the surface of the nebula: ", "   viewPoints = ",
+           "    nu [Ryd]        lambda [um]        nu*F(nu)            ",
+           " to obtain [E36 erg/sec/cm^2/str] divide column 3 by 4*Pi*D^2 or column 4 and higher by the "
+           "emitting surface"]
+    for f in range(nu.size):
+        lam = _C_LIGHT / (nu[f] * _FR1RYD) * 1.e4
+        out.append(f" {nu[f]:16.8g} {lam:16.8g} {s[f] * nu[f] / wid[f]:16.8g}")
+    out += [" ", f" Total energy radiated out of the nebula [e36 erg/s]: {total:16.8g}", " "]
+    p = _radio_pointer(setup.get(abi.ARR_NU))
+    if p > 0:
+        flux = s[p - 1] * 3.141592654 * 1.e23 / (nu[p - 1] * _FR1RYD)
+        out.append(f" Flux at 4.9GHz (must multiply by 1./(4 Pi D[cm]^2 to obtain units of [Jy]) : {flux:16.8g}")
+    Path(path).write_text("\n".join(out) + "\n")
+    return total
