@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=0, help="packets of the CPU sample (0 = auto)")
     ap.add_argument("--cpu-cells", type=int, default=0, help="cells of the CPU emission/balance sample (0 = auto)")
     ap.add_argument("--plain-steps", type=int, default=2, help="steps of the plain FP64 path timed beside")
+    ap.add_argument("--workload", default="lognormal41", choices=["lognormal41", "batch256"],
+                    help="lognormal41: one 41^3 nebula (the headline); batch256: 256 small H+He nebulae "
+                         "in one batched context")
+    ap.add_argument("--nebulae", type=int, default=256, help="nebulae of the batch256 workload")
     return ap.parse_args()
 
 
@@ -412,11 +416,128 @@ def run_gpu(args, dist, ws, rank, local):
     ctx.close()
 
 
+def run_batch(args, dist, ws, rank, local):
+    """256 H + He nebulae (edges 9..33 cells, n_H 10..1e4, 30-60 kK, 1e5..1e7 packets each) as one
+    batched context: a step is one MC iteration of every nebula (mcx_iterate_batched).  Reported:
+    aggregate packets/s, p50 / p99 of the step time, and the same nebulae run one context after
+    another (the single-nebula path) for comparison."""
+    import torch
+    from mocassin_xray_gb300 import Context, Setup, abi, configs
+    torch.cuda.set_device(local)
+    root = Path(tempfile.mkdtemp(prefix="mcx_batch_"))
+    decks = configs.nebula_batch(root, n=args.nebulae, seed=rank)
+    setups = [Setup(d, DATA_DIR, mesh_mode=abi.MESH_LOG_EDGES) for d, _ in decks]
+    packets = np.array([pk for _, pk in decks], dtype=np.int64)
+    seeds = np.arange(len(decks), dtype=np.uint64) + np.uint64(1000 * (rank + 1))
+    ctx = Context(local)
+    ctx.load_batched(setups)
+    ctx.state_save()
+    nb = setups[0].nbins
+    cells = int(ctx.cell_offsets[-1])
+
+    def step(i: int):
+        ctx.state_restore()
+        return ctx.iterate_batched(packets, seeds + np.uint64(i), 0, n_iterate_mc=1)
+
+    for i in range(args.warmup):
+        step(i)
+    ctx.sync()
+    barrier(dist)
+    clocks = ClockSampler(local)
+    clocks.start()
+    stats = []
+    ctx.timer_start()
+    for i in range(args.steps):
+        stats.append(step(args.warmup + i))
+    ms = ctx.timer_stop()
+    ctx.sync()
+    barrier(dist)
+    clk = clocks.stop()
+    ms_step = max_over_ranks(dist, ms / args.steps)
+    total_packets = int(packets.sum())
+    value = ws * total_packets / (ms_step / 1e3)
+    per_step = np.array([st.total_ms for st in stats])
+    tst = [st.transport for st in stats]
+    upd = np.mean([t.crossings + t.interactions for t in tst])
+    emis = np.mean([t.emissions for t in tst])
+    kms = np.mean([t.kernel_ms for t in tst])
+    alg_bytes = upd * 20.0 + emis * math.ceil(math.log2(nb)) * 4.0
+    achieved = alg_bytes / (kms / 1e3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+    tr = profiled_traffic()
+
+    # e2e: the batched step with the state of every nebula uploaded from pinned host memory and read back
+    te = torch.from_numpy(ctx.get(abi.ARR_TE)).pin_memory()
+    ne = torch.from_numpy(ctx.get(abi.ARR_NE)).pin_memory()
+    ion = torch.from_numpy(ctx.get(abi.ARR_IONDEN).reshape(-1)).pin_memory()
+    outs = [torch.empty_like(x).pin_memory() for x in (te, ne, ion)]
+    import ctypes
+    lib = abi.lib()
+
+    def xfer(fn, arr_id, t):
+        ctx._check(fn(ctx._h, arr_id, ctypes.c_void_p(t.data_ptr()), t.numel() * t.element_size()))
+
+    ids = (abi.ARR_TE, abi.ARR_NE, abi.ARR_IONDEN)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        for a, t in zip(ids, (te, ne, ion)):
+            xfer(lib.mcx_put, a, t)
+        ctx.iterate_batched(packets, seeds + np.uint64(5000 + i), 0, n_iterate_mc=1)
+        for a, t in zip(ids, outs):
+            xfer(lib.mcx_get, a, t)
+    ms_e2e_step = max_over_ranks(dist, (time.perf_counter() - t0) * 1e3 / args.steps)
+    h2d = sum(x.numel() * x.element_size() for x in (te, ne, ion))
+
+    # the same nebulae one context after another (the single-nebula path)
+    seq_ms = None
+    if args.plain_steps > 0:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for b, s in enumerate(setups):
+            with Context(local) as c1:
+                c1.load(s)
+                c1.iterate(int(packets[b]), seed=int(seeds[b]))
+        seq_ms = (time.perf_counter() - t0) * 1e3
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": f"{len(setups)} H+He nebulae in one batched context (edges 9..33 cells, n_H 10..1e4, "
+                               "30-60 kK, 1e5..1e7 packets each), 600-bin mesh",
+                   "n_nebulae": len(setups), "n_cells": cells, "packets_per_step": total_packets, "nbins": nb,
+                   "step": "one MC iteration of every nebula from its initial state (mcx_iterate_batched)",
+                   "precision": "fp32 geometry, fp64 estimators, mixed balance",
+                   "l2": "inputs larger than L2 (Jste fp64 of the batch)", "parallelism": "single GPU"},
+        "iteration_ms": {"p50": float(np.percentile(per_step, 50)), "p99": float(np.percentile(per_step, 99))},
+        "e2e": {"value": ws * total_packets / (ms_e2e_step / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": h2d},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None if not tr else tr["dram_bytes_per_update"] * upd,
+                     "kernel": "transportKernelBatched<float>", "peak_kind": peak_kind,
+                     "alg_bytes_per_launch": alg_bytes, "kernel_ms": kms},
+        "gpu_launches": (KERNELS_PER_STEP + len(setups)) * args.steps,
+        "phase_ms": {"opacity": float(np.mean([st.opacity.kernel_ms for st in stats])),
+                     "emission": float(np.mean([st.emission.kernel_ms for st in stats])),
+                     "transport": float(kms),
+                     "balance": float(np.mean([st.balance.kernel_ms for st in stats]))},
+        "single_nebula_contexts": None if seq_ms is None else {
+            "ms_all_nebulae": seq_ms, "value": total_packets / (seq_ms / 1e3),
+            "speedup_of_batch": seq_ms / ms_step},
+    }
+    if clk:
+        line["clocks"] = clk
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+
+
 def main():
     args = parse()
     dist, ws, rank, local = dist_init()
     if args.impl == "reference":
         run_reference(args, dist, ws, rank)
+    elif args.workload == "batch256":
+        run_batch(args, dist, ws, rank, local)
     else:
         run_gpu(args, dist, ws, rank, local)
     if dist is not None:

@@ -379,6 +379,43 @@ typedef struct mcx_iterate_stats {
 
 int  mcx_iterate(mcx_ctx* ctx, const mcx_iterate_opts* opts, mcx_iterate_stats* stats);
 
+/* ------------------------------------------------------- batches of nebulae */
+/* No counterpart in the reference, which runs one nebula per job.  A batch
+ * holds n nebulae (gas only) that share the frequency mesh, the elements and
+ * abundances, nstages and the data tables (set-ups read from one data
+ * directory); each keeps its own grid, density, source and octant flag.  Their
+ * cells are numbered batch-wide: nebula b owns cells cell_offset[b]+1 ..
+ * cell_offset[b+1], and every per-cell array of the context (MCX_ARR_TE,
+ * MCX_ARR_OPACITY, MCX_ARR_JSTE, ...) is the concatenation of the nebulae's
+ * behind one dump cell 0.  mcx_opacity, mcx_emission, mcx_normalize_j,
+ * mcx_balance, mcx_state_save / restore and mcx_get / put act on every nebula
+ * at once, each nebula with its own Gaunt cache and octant factor; the
+ * transport runs all nebulae's packets in one launch (mcx_transport_batched),
+ * packet k of nebula b drawing from Philox stream (seed[b], counter_base[b] +
+ * k) with deltaE = L*(b) / nPhotons(b), so that each nebula's histories are
+ * those of a run of that nebula alone. */
+int  mcx_load_batched(mcx_ctx* ctx, const mcx_setup* const* setups, int32_t n_nebulae);
+
+/* Number of nebulae (0 for a context loaded by mcx_load) and, if cell_offset
+ * is not NULL, the n+1 cell offsets. */
+int  mcx_batch_info(mcx_ctx* ctx, int32_t* n_nebulae, int32_t* cell_offset);
+
+typedef struct mcx_batch_packets {
+    const int64_t*  n_packets;      /* [n] packets of each nebula (0 leaves it dark)            */
+    const uint64_t* seed;           /* [n] Philox key of each nebula                            */
+    const uint64_t* counter_base;   /* [n] global id of each nebula's first packet              */
+    const int64_t*  n_photons_norm; /* [n] nPhotons of deltaE = Lstar / nPhotons, or NULL (n_packets) */
+} mcx_batch_packets;
+
+/* mcx_transport for every nebula of a batch; of opts only precision,
+ * zero_estimators, block_size and grid_mult are read (istar must be 1). */
+int  mcx_transport_batched(mcx_ctx* ctx, const mcx_transport_opts* opts, const mcx_batch_packets* packets,
+                           mcx_transport_stats* stats);
+
+/* mcx_iterate for a batch (opts.n_packets, seed and counter_base unused). */
+int  mcx_iterate_batched(mcx_ctx* ctx, const mcx_iterate_opts* opts, const mcx_batch_packets* packets,
+                         mcx_iterate_stats* stats);
+
 /* ---------------------------------------------- analytical line luminosities */
 /* The analytical part of outputGas (source/output_mod.f90:13-805) from the
  * current grid state: over the active cells with lgBlack < 1, the volume

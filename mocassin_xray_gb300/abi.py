@@ -127,6 +127,10 @@ class IterateStats(C.Structure):
                 ("reserved", C.c_int64 * 4)]
 
 
+class BatchPackets(C.Structure):
+    _fields_ = [("n_packets", _P), ("seed", _P), ("counter_base", _P), ("n_photons_norm", _P)]
+
+
 class Lines(C.Structure):
     _fields_ = [("hbeta_vol", C.c_double), ("relative", C.c_int32), ("n_cells", C.c_int32),
                 ("hydro_vol", _P), ("hei_vol", _P), ("forb_vol", _P), ("wav", _P), ("te_vol", _P),
@@ -159,6 +163,12 @@ SIGNATURES = [
     ("mcx_balance", C.c_int, [_P, C.POINTER(BalanceOpts), C.POINTER(BalanceStats)]),
     ("mcx_iterate", C.c_int, [_P, C.POINTER(IterateOpts), C.POINTER(IterateStats)]),
     ("mcx_line_luminosities", C.c_int, [_P, C.POINTER(Lines)]),
+    ("mcx_load_batched", C.c_int, [_P, _P, C.c_int32]),
+    ("mcx_batch_info", C.c_int, [_P, C.POINTER(C.c_int32), _P]),
+    ("mcx_transport_batched", C.c_int, [_P, C.POINTER(TransportOpts), C.POINTER(BatchPackets),
+                                        C.POINTER(TransportStats)]),
+    ("mcx_iterate_batched", C.c_int, [_P, C.POINTER(IterateOpts), C.POINTER(BatchPackets),
+                                      C.POINTER(IterateStats)]),
     ("mcx_timer_start", C.c_int, [_P]),
     ("mcx_timer_stop", C.c_int, [_P, C.POINTER(C.c_float)]),
     ("mcx_version", C.c_char_p, []),

@@ -15,6 +15,9 @@ path is measured on:
 * ``xray_gas``        41^3, n_H = 1e3, the same elements plus Mg, Si, Fe,
                       power law F_nu ~ nu^-1.5 over 1..740 Ryd with 2e49 s^-1
                       above 1 Ryd, 800 bins.
+* ``nebula_batch``    256 small H + He nebulae for the batched path: edges
+                      of 9..33 cells, n_H log-uniform in [10, 1e4], 30-60 kK
+                      blackbodies, 1e5..1e7 packets each.
 * ``dust_shell``      dust-only shell on an 81^3 grid, R_in = 1e17, R_out =
                       1e18 cm, grain density ~ r^-2 normalised to tau_V = 1
                       (or 10), two grain species with seeded power-law
@@ -258,3 +261,50 @@ def dust_shell(root: str | Path, n: int = 81, tau_v: float = 1.0, packets: int =
         f"maxIterateMC {iterations} 95.",
         "convLimit 0.05",
     ])
+
+
+def nebula_batch(root: str | Path, n: int = 256, seed: int = 0, nbins: int = 600,
+                 packets_range: tuple[float, float] = (1e5, 1e7), octant_every: int = 0,
+                 max_edge: int = 33) -> list[tuple[Path, int]]:
+    """A batch of `n` seeded H + He nebulae (He/H = 0.1), each a uniform sphere on a full grid whose
+    edge is drawn from {9, 11, ..., 33} cells, n_H log-uniform in [10, 1e4] cm^-3, a blackbody of
+    T* uniform in [30, 60] kK with Q(H) log-uniform in [1e48, 1e49] s^-1, the grid's half-width
+    1.5 times the Stromgren radius (alpha_B = 2.6e-13), 600 bins to 500 Ryd.  Returns
+    (input.in path, packets per iteration) per nebula, the packets log-uniform in packets_range.
+    With octant_every = k > 0 every k-th nebula is an octant (symmetricXYZ) grid; max_edge caps the
+    edge for small test batches."""
+    root = Path(root)
+    rng = np.random.default_rng(seed)
+    out = []
+    for b in range(n):
+        edge = min(int(rng.integers(0, 13)) * 2 + 9, max_edge)
+        nh = 10.0 ** rng.uniform(1.0, 4.0)
+        tstar = rng.uniform(30000.0, 60000.0)
+        q = 10.0 ** rng.uniform(48.0, 49.0)
+        rs = (3.0 * q / (4.0 * math.pi * nh * nh * 2.6e-13)) ** (1.0 / 3.0)
+        half = 1.5 * rs
+        pk = int(round(10.0 ** rng.uniform(math.log10(packets_range[0]), math.log10(packets_range[1]))))
+        d = root / f"neb{b:03d}"
+        (d / "input").mkdir(parents=True, exist_ok=True)
+        _write_abundances(d / "input" / "abun_hhe.in", {"H": 1.0, "He": 0.1})
+        octant = octant_every > 0 and b % octant_every == 0
+        deck = _deck(d, (["symmetricXYZ"] if octant else []) + [
+            f"nx {edge}", f"ny {edge}", f"nz {edge}",
+            f"Hdensity {nh:.6e}",
+            f"edges {half:.6e} {half:.6e} {half:.6e}",
+            "Rin 0.",
+            f"Rout {half:.6e}",
+            "contShape blackbody",
+            f"TStellar {tstar:.1f}",
+            f"LPhot {q / 1e36:.6e}",
+            f"nbins {nbins}",
+            "nuMin 1.e-4",
+            "nuMax 500.",
+            f"nPhotons {pk}",
+            "maxIterateMC 12 95.",
+            "TeStart 10000.",
+            "nstages 3",
+            "nebComposition 'input/abun_hhe.in'",
+        ])
+        out.append((deck, pk))
+    return out

@@ -172,6 +172,26 @@ std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out)
   d.atomData = (const double*)up(t.atomData.data(), t.atomData.size() * sizeof(double));
   std::vector<float> atomF(t.atomData.begin(), t.atomData.end());
   d.atomDataF = (const float*)up(atomF.data(), atomF.size() * sizeof(float));
+  // per upper level j the summed line factors sum_i a(j,i) E_ji of its lines
+  // that carry positive power (the mixed path's cooling; equilibrium's loop
+  // drops the others)
+  std::vector<double> pow_((size_t)std::max(t.nAtoms, 1) * (kMaxLevels + 1), 0.);
+  for (int a = 0; a < t.nAtoms; ++a) {
+    const int32_t* h = t.atomHdr.data() + (size_t)a * kAtHdrSize;
+    const int n = h[kAtNLev];
+    const double* A = t.atomData.data() + h[kAtOffA];
+    const double* Ev = t.atomData.data() + h[kAtOffE];
+    const double atp = t.atomData[h[kAtOffAtp]];
+    for (int i = 1; i <= n - 1; ++i)
+      for (int j = i + 1; j <= n; ++j) {
+        double aji = A[(size_t)(j - 1) * n + (i - 1)];
+        if (aji == 0.) continue;
+        if (j == h[kAtIup2p] && i == 1 && atp > 0.) aji = aji - atp;
+        const double f = aji * (Ev[j - 1] - Ev[i - 1]);
+        if (f > 0.) pow_[(size_t)a * (kMaxLevels + 1) + j] += f;
+      }
+  }
+  d.linePow = (const double*)up(pow_.data(), pow_.size() * sizeof(double));
   const size_t nPair = (size_t)E * ns;
   d.ion = carve<double>(blocks, nPair * C1, err);
   d.alpha = carve<double>(blocks, nPair * C1, err);

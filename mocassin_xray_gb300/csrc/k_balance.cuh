@@ -72,6 +72,7 @@ struct BalanceDev {
   const int32_t* atomHdr;      // [nAtoms][16]
   const double* atomData;
   const float* atomDataF;      // the same values in FP32 (mixed precision)
+  const double* linePow;       // [nAtoms][kMaxLevels+1] sum over lines from level j of a(j,i) E_ji > 0
   // per-cell work, [k][C+1] (cell fastest)
   double* ion;                 // [nstages][nElemUsed]
   double* alpha;               // [nElemUsed][nstages]

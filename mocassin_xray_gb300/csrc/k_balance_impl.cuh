@@ -665,14 +665,14 @@ __device__ __forceinline__ void collisionPairs(const BalanceDev& b, const int32_
 __device__ __forceinline__ bool gthPops(const BalanceDev& b, const int32_t* h, double Ne, double ionDenUp, bool rec,
                                         const double* alphaTotal, real TeR, real sqrTe, real log10Te, double* y) {
   const int n = h[kAtNLev];
-  const double* A = b.atomData + h[kAtOffA];
+  const float* A = b.atomDataF + h[kAtOffA];
   const float NeF = (float)Ne;
   float R[kMaxLevels + 1][kMaxLevels + 1];   // R[a][c]: rate from level a to level c
   for (int i = 1; i <= n; ++i)
     for (int j = 1; j <= n; ++j) R[i][j] = 0.f;
   collisionPairs(b, h, TeR, sqrTe, log10Te, [&](int lo, int up, real qLoUp, real qUpLo) {
     R[lo][up] = NeF * qLoUp;
-    R[up][lo] = NeF * qUpLo + (float)A[(size_t)(up - 1) * n + (lo - 1)];
+    R[up][lo] = NeF * qUpLo + A[(size_t)(up - 1) * n + (lo - 1)];
   });
   float src[kMaxLevels + 1], Dk[kMaxLevels + 1];
   for (int i = 1; i <= n; ++i) src[i] = (rec && i >= 2) ? (float)(Ne * ionDenUp * alphaTotal[i]) : 0.f;
@@ -838,6 +838,18 @@ __device__ double equilibriumLines(const BalanceDev& b, int atom, double Te, dou
   double y[kMaxLevels + 1];
   equilibriumPops(b, atom, Te, Ne, ionDenUp, rec, y);
   const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
+#if !MCX_BAL_EXACT
+  // sum_j n_j sum_i a(j,i) E_ji with the line factors summed at set-up: the
+  // per-line 1e-35 cut of the reference drops terms that are below 1e-12 of
+  // any cooling rate the balance resolves
+  {
+    const double* P = b.linePow + (size_t)atom * (kMaxLevels + 1);
+    const int n = h[kAtNLev];
+    double acc = 0.;
+    for (int j = 2; j <= n; ++j) acc = acc + y[j] * P[j];
+    return acc * m1 * m2 * m3;
+  }
+#endif
   const double* DD = b.atomData;
   const int nLev = h[kAtNLev];
   const double* A = DD + h[kAtOffA];
@@ -875,11 +887,11 @@ __global__ void __launch_bounds__(128) atomsKernel(BalanceDev b) {
     return;
   }
 #endif
-  double up = 0.;
-  if (ion < top && x > 0.) up = ionAt(b, c, elem, ion + 1) / x;
-  // forbiddenLines = fLineEm * elemAbun * ionDen * 1.9865e-16, summed where > 1e-35
+  // forbiddenLines = fLineEm * elemAbun * ionDen * 1.9865e-16, summed where > 1e-35;
+  // without the recombination term the ratio ionDen(ion+1)/ionDen(ion) is not used
+  (void)top;
   b.forSum[(size_t)atom * c.C1 + cell] =
-      equilibriumLines(b, atom, b.te[cell], b.ne[cell], up, false, (double)b.abun[elem], x, RD(1.9865e-16));
+      equilibriumLines(b, atom, b.te[cell], b.ne[cell], 0., false, (double)b.abun[elem], x, RD(1.9865e-16));
 }
 
 // The emission phase's forLines (rec = .true., 1e-25 erg units): one thread

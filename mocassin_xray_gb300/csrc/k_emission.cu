@@ -173,6 +173,27 @@ cudaError_t launchEmissionGaunt(const EmissionDev& e, float gauntTe, cudaStream_
   return cudaGetLastError();
 }
 
+// one table per nebula of a batch: table b (blockIdx.y) at temperature temps[b]
+__global__ void emissionGauntBatchKernel(EmissionDev e, const float* __restrict__ temps) {
+  const int b = blockIdx.y;
+  float c0[9], con0, g20, c1[9], con1, g21;
+  gauntCoeffs(0.f, log10f(temps[b]), c0, con0, g20);
+  gauntCoeffs(0.30103f, log10f(temps[b]), c1, con1, g21);
+  const float k = 4.f * 3.141592654f * 54.43f;
+  float* ffK = e.ffK + (size_t)b * 2 * e.nbins;
+  for (int i = threadIdx.x + blockIdx.x * blockDim.x; i < e.nbins; i += blockDim.x * gridDim.x) {
+    float l = log10f(e.nu[i]);
+    ffK[i] = k * 1.f * gauntAt(c0, con0, g20, l);
+    ffK[e.nbins + i] = k * 4.f * gauntAt(c1, con1, g21, l);
+  }
+}
+
+cudaError_t launchEmissionGauntBatched(const EmissionDev& e, const float* temps, int nTables, cudaStream_t s) {
+  if (nTables <= 0) return cudaSuccess;
+  emissionGauntBatchKernel<<<dim3((e.nbins + 255) / 256, nTables), 256, 0, s>>>(e, temps);
+  return cudaGetLastError();
+}
+
 namespace {
 
 __device__ __forceinline__ float ionFrac(const float* ionDen, size_t C1, size_t cell, int xref, int E, int stage,
@@ -205,6 +226,7 @@ emissionKernel(EmissionDev e, const float* __restrict__ te, const float* __restr
   if (cell > e.nCells || !compute[cell]) return;
   const size_t C1 = (size_t)e.nCells + 1;
   const int nb = e.nbins, E = e.nElemUsed, S = e.nstages;
+  const float* ffK = e.ffK + (e.ffIdx ? (size_t)e.ffIdx[cell] * 2 * (size_t)nb : (size_t)0);
   const float Te = te[cell], NeCell = ne[cell];
   float Ne = NeCell;
   const float sqrTe = sqrtf(Te), log10Te = log10f(Te), log10Ne = log10f(Ne);
@@ -269,10 +291,10 @@ emissionKernel(EmissionDev e, const float* __restrict__ te, const float* __restr
     gHI = g[0]; gHeI = g[1]; gHeII = g[2];
     const float exff = expf(-v * hk) / sqrTe;
     if (i >= e.HIPnuP) {
-      gHI = e.milne[i - 1] * invTe15 * expf((e.nuHIP - v) * hk) + e.ffK[i - 1] * exff;
+      gHI = e.milne[i - 1] * invTe15 * expf((e.nuHIP - v) * hk) + ffK[i - 1] * exff;
       if (i >= e.HeIlast) {
-        gHeI = e.milne[nb + i - 1] * invTe15 * expf((e.nuHeIP - v) * hk) + e.ffK[i - 1] * exff;
-        if (i >= e.HeIIlast) gHeII = e.milne[2 * nb + i - 1] * invTe15 * expf((e.nuHeIIP - v) * hk) + e.ffK[nb + i - 1] * exff;
+        gHeI = e.milne[nb + i - 1] * invTe15 * expf((e.nuHeIP - v) * hk) + ffK[i - 1] * exff;
+        if (i >= e.HeIIlast) gHeII = e.milne[2 * nb + i - 1] * invTe15 * expf((e.nuHeIIP - v) * hk) + ffK[nb + i - 1] * exff;
       }
     }
     float hv = 0.f;

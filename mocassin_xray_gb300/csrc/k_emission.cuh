@@ -32,7 +32,8 @@ struct EmissionDev {
   const float* tk;            // [nTk]
   const float* logGamma;      // [3][nTk][32]
   const float* milne;         // [3][nbins] 4 pi xs statW hcRyd const nu^3 1e40 (0 where unused)
-  float* ffK;                 // [2][nbins] 4 pi 54.43 Z^2 gauntFF(Z) (per phase)
+  float* ffK;                 // [2][nbins] 4 pi 54.43 Z^2 gauntFF(Z) (per phase); [nTables][2][nbins] in a batch
+  const int16_t* ffIdx;       // [C+1] the Gaunt table of each cell in a batch (its nebula's), or null
   const int32_t* fbStart;     // [nbins+1]
   const FbTerm* fbTerm;
   const float* fbK;           // [nbins] 4 pi const hcRyd nu^3 1e40
@@ -66,6 +67,9 @@ std::string emissionDataCreate(const Setup& s, std::unique_ptr<EmissionData>& ou
 
 // Tabulates 4 pi 54.43 Z^2 gauntFF(Z) at the Gaunt cache temperature (free_free).
 cudaError_t launchEmissionGaunt(const EmissionDev& e, float gauntTe, cudaStream_t s);
+
+// The same for the nebulae of a batch: table b of e.ffK at temps[b] (device array).
+cudaError_t launchEmissionGauntBatched(const EmissionDev& e, const float* temps, int nTables, cudaStream_t s);
 
 // emissionDriver for every cell with compute[c] = 1: writes recPDF[nu][c] and totalLines[c].
 cudaError_t launchEmission(const EmissionDev& e, const float* te, const float* ne, const float* ionDen,

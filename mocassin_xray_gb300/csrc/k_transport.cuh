@@ -67,12 +67,57 @@ struct LocalCounters {
 
 template <typename R>
 struct TransportShared {
-  const float* X; const float* Y; const float* Z;
-  const float* nu; const float* cdf;
+  const float* nu;           // frequency mesh (shared memory)
 };
 
-__device__ __forceinline__ int activeAt(const DevGrid& g, int i, int j, int k) {
-  return __ldg(g.active + (size_t)(i - 1) + (size_t)g.nx * ((size_t)(j - 1) + (size_t)g.ny * (size_t)(k - 1)));
+// The grid a packet travels in, read through accessors so that one emit /
+// step code serves both kernels: OneGrid reads the context's single grid from
+// the kernel parameters (axes and source CDF staged in shared memory);
+// NebulaGeo holds, in registers, the nebula of a batch that the packet belongs
+// to (axes, active map and CDF slices of the concatenated batch arrays; the
+// active map holds batch-wide cell ids).
+struct OneGrid {
+  const DevGrid& g;
+  const float* sX; const float* sY; const float* sZ; const float* sCdf;
+  __device__ __forceinline__ int nx() const { return g.nx; }
+  __device__ __forceinline__ int ny() const { return g.ny; }
+  __device__ __forceinline__ int nz() const { return g.nz; }
+  __device__ __forceinline__ int symmetric() const { return g.symmetric; }
+  __device__ __forceinline__ float rOut() const { return g.rOut; }
+  __device__ __forceinline__ const float* X() const { return sX; }
+  __device__ __forceinline__ const float* Y() const { return sY; }
+  __device__ __forceinline__ const float* Z() const { return sZ; }
+  __device__ __forceinline__ const int32_t* active() const { return g.active; }
+  __device__ __forceinline__ const float* cdf() const { return sCdf; }
+  __device__ __forceinline__ int starIdx(int d) const { return g.starIdx[d]; }
+  __device__ __forceinline__ float starPos(int d) const { return g.starPos[d]; }
+};
+
+struct NebulaGeo {
+  int nx_, ny_, nz_, symmetric_;
+  float rOut_;
+  const float* X_; const float* Y_; const float* Z_;
+  const int32_t* active_;
+  const float* cdf_;
+  int starIdx_[3];
+  float starPos_[3];
+  __device__ __forceinline__ int nx() const { return nx_; }
+  __device__ __forceinline__ int ny() const { return ny_; }
+  __device__ __forceinline__ int nz() const { return nz_; }
+  __device__ __forceinline__ int symmetric() const { return symmetric_; }
+  __device__ __forceinline__ float rOut() const { return rOut_; }
+  __device__ __forceinline__ const float* X() const { return X_; }
+  __device__ __forceinline__ const float* Y() const { return Y_; }
+  __device__ __forceinline__ const float* Z() const { return Z_; }
+  __device__ __forceinline__ const int32_t* active() const { return active_; }
+  __device__ __forceinline__ const float* cdf() const { return cdf_; }
+  __device__ __forceinline__ int starIdx(int d) const { return starIdx_[d]; }
+  __device__ __forceinline__ float starPos(int d) const { return starPos_[d]; }
+};
+
+template <typename Geo>
+__device__ __forceinline__ int activeAt(const Geo& q, int i, int j, int k) {
+  return __ldg(q.active() + (size_t)(i - 1) + (size_t)q.nx() * ((size_t)(j - 1) + (size_t)q.ny() * (size_t)(k - 1)));
 }
 
 // getNu2 on a monotone CDF: the reference's linear scan "last i with u >= cdf(i)"
@@ -95,8 +140,8 @@ __device__ __forceinline__ R draw(Packet<R>& p) { return uniformFrom<R>(p.rng.ne
 // initPhotonPacket (source/photon_mod.f90:744-896): position, frequency, an
 // isotropic direction (re-drawn while a component is exactly zero) and the
 // octant fold for stellar packets.
-template <typename R>
-__device__ __forceinline__ void initPacket(const DevGrid& g, const TransportShared<R>& sh, Packet<R>& p, int nuP,
+template <typename R, typename Geo>
+__device__ __forceinline__ void initPacket(const Geo& q, const TransportShared<R>& sh, Packet<R>& p, int nuP,
                                            bool line, bool stellar, int xP, int yP, int zP) {
   using M = RMath<R>;
   p.nuP = nuP;
@@ -112,12 +157,12 @@ __device__ __forceinline__ void initPacket(const DevGrid& g, const TransportShar
     p.vx = t * M::cos_(ang); p.vy = t * M::sin_(ang); p.vz = w;
     if (p.vx != R(0) && p.vy != R(0) && p.vz != R(0)) break;
   }
-  if (g.symmetric && stellar) {
+  if (q.symmetric() && stellar) {
     if (p.vx < R(0)) p.vx = -p.vx;
     if (p.vy < R(0)) p.vy = -p.vy;
     if (p.vz < R(0)) p.vz = -p.vz;
   }
-  p.origin = (xP > 0 && yP > 0 && zP > 0) ? activeAt(g, xP, yP, zP) : 0;
+  p.origin = (xP > 0 && yP > 0 && zP > 0) ? activeAt(q, xP, yP, zP) : 0;
 }
 
 template <typename R>
@@ -180,37 +225,37 @@ template <> __device__ __forceinline__ double cellVolume<double>(const DevGrid& 
 
 // energyPacketRun + newPhotonPacket: create the packet of history step p.type
 // at (p.x,p.y,p.z; p.xP,p.yP,p.zP).  Returns the next state.
-template <typename R>
-__device__ int emitPacket(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,
+template <typename R, typename Geo>
+__device__ int emitPacket(const DevGrid& g, const Geo& q, const DevTransportIn& in, const DevTransportOut& out,
                           const TransportShared<R>& sh, Packet<R>& p, double deltaE, LocalCounters& lc) {
   using M = RMath<R>;
   if (p.nEmit >= kRecursionLimit) { ++lc.trapped; return ST_IDLE; }
   ++p.nEmit;
   bool line = false;
   if (p.type == PT_STELLAR) {
-    int nuP = sampleCDF<R>(sh.cdf, g.nbins, g.nbins, draw(p));
+    int nuP = sampleCDF<R>(q.cdf(), g.nbins, g.nbins, draw(p));
     ++lc.emissions;
-    p.x = (R)g.starPos[0]; p.y = (R)g.starPos[1]; p.z = (R)g.starPos[2];
-    initPacket<R>(g, sh, p, nuP, false, true, g.starIdx[0], g.starIdx[1], g.starIdx[2]);
+    p.x = (R)q.starPos(0); p.y = (R)q.starPos(1); p.z = (R)q.starPos(2);
+    initPacket<R>(q, sh, p, nuP, false, true, q.starIdx(0), q.starIdx(1), q.starIdx(2));
     if (p.nu >= R(1)) lc.qPhot += deltaE / (2.1799153e-11 * (double)p.nu);
   } else {
-    if (p.xP < 1 || p.xP > g.nx || p.yP < 1 || p.yP > g.ny || p.zP < 1 || p.zP > g.nz) { ++lc.errors; return ST_IDLE; }
-    int cell = activeAt(g, p.xP, p.yP, p.zP);
+    if (p.xP < 1 || p.xP > q.nx() || p.yP < 1 || p.yP > q.ny() || p.zP < 1 || p.zP > q.nz()) { ++lc.errors; return ST_IDLE; }
+    int cell = activeAt(q, p.xP, p.yP, p.zP);
     if (cell <= 0) { ++lc.errors; return ST_IDLE; }
     if (p.type == PT_DIFFUSE) {
       R rnd = R(1) - draw(p);
       if (rnd <= (R)__ldg(in.totalLines + cell)) {
-        initPacket<R>(g, sh, p, 0, true, false, p.xP, p.yP, p.zP);
+        initPacket<R>(q, sh, p, 0, true, false, p.xP, p.yP, p.zP);
         line = true;
       } else {
         int nuP = sampleCDF<R>(in.recCDFT + (size_t)cell * g.nbins, g.nbins, g.nbins, draw(p));
         ++lc.emissions;
-        initPacket<R>(g, sh, p, nuP, false, false, p.xP, p.yP, p.zP);
+        initPacket<R>(q, sh, p, nuP, false, false, p.xP, p.yP, p.zP);
       }
     } else {
       int nuP = sampleCDF<R>(in.dustCDFT + (size_t)cell * g.nbins, g.nbins, g.nbins, draw(p));
       ++lc.emissions;
-      initPacket<R>(g, sh, p, nuP, false, false, p.xP, p.yP, p.zP);
+      initPacket<R>(q, sh, p, nuP, false, false, p.xP, p.yP, p.zP);
     }
   }
   if (line) {
@@ -224,7 +269,7 @@ __device__ int emitPacket(const DevGrid& g, const DevTransportIn& in, const DevT
     return ST_IDLE;
   }
   // pathSegment entry (source/photon_mod.f90:1813-1878)
-  if (p.xP <= 0 || p.xP > g.nx || p.yP <= 0 || p.yP > g.ny || p.zP <= 0 || p.zP > g.nz) { ++lc.errors; return ST_IDLE; }
+  if (p.xP <= 0 || p.xP > q.nx() || p.yP <= 0 || p.yP > q.ny() || p.zP <= 0 || p.zP > q.nz()) { ++lc.errors; return ST_IDLE; }
   p.absTau = R(0);
   p.passProb = -M::log_(R(1) - draw(p));
   p.nStep = 0;
@@ -232,12 +277,12 @@ __device__ int emitPacket(const DevGrid& g, const DevTransportIn& in, const DevT
 }
 
 // One iteration of pathSegment's main loop (source/photon_mod.f90:1880-4036).
-template <typename R>
-__device__ int stepPacket(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,
+template <typename R, typename Geo>
+__device__ int stepPacket(const DevGrid& g, const Geo& q, const DevTransportIn& in, const DevTransportOut& out,
                           const TransportShared<R>& sh, Packet<R>& p, R deltaER, double deltaE, LocalCounters& lc) {
   using M = RMath<R>;
-  const int nx = g.nx, ny = g.ny, nz = g.nz;
-  const float* X = sh.X; const float* Y = sh.Y; const float* Z = sh.Z;
+  const int nx = q.nx(), ny = q.ny(), nz = q.nz();
+  const float* X = q.X(); const float* Y = q.Y(); const float* Z = q.Z();
 #define AXR(A, i) ((R)(A)[(i) - 1])
   if (++p.nStep > kSafeLimit) { ++lc.trapped; if (p.nEmit >= kRecursionLimit) ++lc.trapped; return ST_IDLE; }
   int xP = p.xP, yP = p.yP, zP = p.zP;
@@ -254,7 +299,7 @@ __device__ int stepPacket(const DevGrid& g, const DevTransportIn& in, const DevT
 
   // distances from the walls (source/photon_mod.f90:1933-2084); with one
   // mother grid the reference's inner loop runs exactly once
-  if (g.symmetric) {
+  if (q.symmetric()) {
     if (rx <= AXR(X, 1)) { if (vx < R(0)) vx = -vx; rx = AXR(X, 1); }
     if (ry <= AXR(Y, 1)) { if (vy < R(0)) vy = -vy; ry = AXR(Y, 1); }
     if (rz <= AXR(Z, 1)) { if (vz < R(0)) vz = -vz; rz = AXR(Z, 1); }
@@ -305,7 +350,7 @@ __device__ int stepPacket(const DevGrid& g, const DevTransportIn& in, const DevT
   else { dS = M::min_(dSx, dSy); dS = M::min_(dS, dSz); }
   if (!(dS > R(0))) { ++lc.errors; return ST_IDLE; }
 
-  const int cell = activeAt(g, xP, yP, zP);
+  const int cell = activeAt(q, xP, yP, zP);
   const size_t C1 = (size_t)g.nCells + 1;
   const R kap = (R)__ldg(in.opacity + (size_t)cell + C1 * (size_t)(p.nuP - 1));
   const R tauCell = dS * kap;
@@ -322,7 +367,7 @@ __device__ int stepPacket(const DevGrid& g, const DevTransportIn& in, const DevT
     // interaction within the cell (source/photon_mod.f90:2244-2700)
     R dlLoc = (p.passProb - p.absTau) / kap;
     rx = rx + dlLoc * vx; ry = ry + dlLoc * vy; rz = rz + dlLoc * vz;
-    if (g.symmetric) {
+    if (q.symmetric()) {
       if (rx <= AXR(X, 1)) { if (vx < R(0)) vx = -vx; rx = AXR(X, 1); }
       if (ry <= AXR(Y, 1)) { if (vy < R(0)) vy = -vy; ry = AXR(Y, 1); }
       if (rz <= AXR(Z, 1)) { if (vz < R(0)) vz = -vz; rz = AXR(Z, 1); }
@@ -331,7 +376,7 @@ __device__ int stepPacket(const DevGrid& g, const DevTransportIn& in, const DevT
     ++lc.interactions;
     R rad = M::sqrt_((rx / R(1.e10)) * (rx / R(1.e10)) + (ry / R(1.e10)) * (ry / R(1.e10)) +
                      (rz / R(1.e10)) * (rz / R(1.e10))) * R(1.e10);
-    if (rad >= (R)g.rOut && g.rOut > 0.f) {
+    if (rad >= (R)q.rOut() && q.rOut() > 0.f) {
       escapeTally<R>(g, out, p, deltaE, lc);
       if (p.nEmit >= kRecursionLimit) ++lc.trapped;
       return ST_IDLE;
@@ -345,7 +390,7 @@ __device__ int stepPacket(const DevGrid& g, const DevTransportIn& in, const DevT
         next = ST_EMIT;
       } else {
         ++lc.scatterings;
-        initPacket<R>(g, sh, p, p.nuP, false, false, xP, yP, zP);
+        initPacket<R>(q, sh, p, p.nuP, false, false, xP, yP, zP);
         vx = p.vx; vy = p.vy; vz = p.vz;
         p.absTau = R(0);
         p.passProb = -M::log_(R(1) - draw(p));
@@ -379,7 +424,7 @@ __device__ int stepPacket(const DevGrid& g, const DevTransportIn& in, const DevT
     else if (dS == dSz && vz > R(0)) zP = zP + 1;
     else if (dS == dSz && vz < R(0)) zP = zP - 1;
     bool esc = false;
-    if (!g.symmetric) {
+    if (!q.symmetric()) {
       // full-grid escape (source/photon_mod.f90:2884-3244)
       if (ry < AXR(Y, 1) || yP < 1) esc = true;
       if (ry > AXR(Y, ny) || yP > ny) esc = true;
@@ -389,7 +434,7 @@ __device__ int stepPacket(const DevGrid& g, const DevTransportIn& in, const DevT
       if (rz >= AXR(Z, nz) || zP > nz) esc = true;
     }
     // grid boundary and mirror planes (source/photon_mod.f90:3607-3890)
-    if (!esc && ((!g.symmetric && (rx <= AXR(X, 1) || ry <= AXR(Y, 1) || rz <= AXR(Z, 1))) ||
+    if (!esc && ((!q.symmetric() && (rx <= AXR(X, 1) || ry <= AXR(Y, 1) || rz <= AXR(Z, 1))) ||
                  rx >= AXR(X, nx) || ry >= AXR(Y, ny) || rz >= AXR(Z, nz) || xP > nx || yP > ny || zP > nz))
       esc = true;
     if (esc) {
@@ -397,7 +442,7 @@ __device__ int stepPacket(const DevGrid& g, const DevTransportIn& in, const DevT
       if (p.nEmit >= kRecursionLimit) ++lc.trapped;
       return ST_IDLE;
     }
-    if (g.symmetric) {
+    if (q.symmetric()) {
       if (rx <= AXR(X, 1) || xP < 1) { if (vx < R(0)) vx = -vx; xP = 1; rx = AXR(X, 1); }
       if (ry <= AXR(Y, 1) || yP < 1) { if (vy < R(0)) vy = -vy; yP = 1; ry = AXR(Y, 1); }
       if (rz <= AXR(Z, 1) || zP < 1) { if (vz < R(0)) vz = -vz; zP = 1; rz = AXR(Z, 1); }
@@ -415,6 +460,41 @@ __device__ int stepPacket(const DevGrid& g, const DevTransportIn& in, const DevT
 #undef AXR
 }
 
+// one atomic per counter per warp
+__device__ __forceinline__ void flushCounters(const LocalCounters& lc, DevTransportCounters* cnt) {
+  const unsigned FULL = 0xffffffffu;
+  const unsigned lane = threadIdx.x & 31u;
+  auto wsum = [&](unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+    return v;
+  };
+  unsigned long long v;
+  v = wsum(lc.crossings);    if (lane == 0 && v) atomicAdd(&cnt->crossings, v);
+  v = wsum(lc.interactions); if (lane == 0 && v) atomicAdd(&cnt->interactions, v);
+  v = wsum(lc.absorptions);  if (lane == 0 && v) atomicAdd(&cnt->absorptions, v);
+  v = wsum(lc.scatterings);  if (lane == 0 && v) atomicAdd(&cnt->scatterings, v);
+  v = wsum(lc.escaped);      if (lane == 0 && v) atomicAdd(&cnt->escaped, v);
+  v = wsum(lc.lineEscapes);  if (lane == 0 && v) atomicAdd(&cnt->lineEscapes, v);
+  v = wsum(lc.trapped);      if (lane == 0 && v) atomicAdd(&cnt->trapped, v);
+  v = wsum(lc.emissions);    if (lane == 0 && v) atomicAdd(&cnt->emissions, v);
+  v = wsum(lc.errors);       if (lane == 0 && v) atomicAdd(&cnt->errors, v);
+  double qp = lc.qPhot;
+  for (int o = 16; o > 0; o >>= 1) qp += __shfl_down_sync(FULL, qp, o);
+  if (lane == 0 && qp != 0.) atomicAdd(&cnt->qPhot, qp);
+}
+
+// Idle lanes of the warp take the next packet ids from the work queue with one
+// atomic; returns this lane's id (meaningful when the lane was idle).
+__device__ __forceinline__ unsigned long long refill(unsigned need, DevTransportCounters* cnt) {
+  const unsigned FULL = 0xffffffffu;
+  const unsigned lane = threadIdx.x & 31u;
+  const int leader = __ffs(need) - 1;
+  unsigned long long first = 0;
+  if ((int)lane == leader) first = atomicAdd(&cnt->queue, (unsigned long long)__popc(need));
+  first = __shfl_sync(FULL, first, leader);
+  return first + (unsigned long long)__popc(need & ((1u << lane) - 1u));
+}
+
 template <typename R>
 __global__ void __launch_bounds__(256)
 transportKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportCounters* cnt,
@@ -430,10 +510,10 @@ transportKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportC
   for (int i = threadIdx.x; i < g.nz; i += blockDim.x) sZ[i] = g.zAxis[i];
   for (int i = threadIdx.x; i < g.nbins; i += blockDim.x) { sNu[i] = g.nu[i]; sCdf[i] = g.srcCDF[i]; }
   __syncthreads();
-  TransportShared<R> sh{sX, sY, sZ, sNu, sCdf};
+  TransportShared<R> sh{sNu};
+  const OneGrid q{g, sX, sY, sZ, sCdf};
 
   const unsigned FULL = 0xffffffffu;
-  const unsigned lane = threadIdx.x & 31u;
   const R deltaER = (R)deltaE;
   LocalCounters lc;
   Packet<R> p;
@@ -443,12 +523,8 @@ transportKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportC
   for (;;) {
     const unsigned need = __ballot_sync(FULL, state == ST_IDLE);
     if (need) {
-      const int leader = __ffs(need) - 1;
-      unsigned long long first = 0;
-      if ((int)lane == leader) first = atomicAdd(&cnt->queue, (unsigned long long)__popc(need));
-      first = __shfl_sync(FULL, first, leader);
+      const unsigned long long id = refill(need, cnt);
       if (state == ST_IDLE) {
-        const unsigned long long id = first + (unsigned long long)__popc(need & ((1u << lane) - 1u));
         if (id < n) {
           p.rng.init(seed, base + id);
           p.type = PT_STELLAR;
@@ -460,28 +536,75 @@ transportKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportC
       }
     }
     if (__ballot_sync(FULL, state != ST_DONE) == 0u) break;
-    if (state == ST_EMIT) state = emitPacket<R>(g, in, out, sh, p, deltaE, lc);
-    else if (state == ST_STEP) state = stepPacket<R>(g, in, out, sh, p, deltaER, deltaE, lc);
+    if (state == ST_EMIT) state = emitPacket<R>(g, q, in, out, sh, p, deltaE, lc);
+    else if (state == ST_STEP) state = stepPacket<R>(g, q, in, out, sh, p, deltaER, deltaE, lc);
   }
+  flushCounters(lc, cnt);
+}
 
-  // one atomic per counter per warp
-  auto wsum = [&](unsigned long long v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
-    return v;
-  };
-  unsigned long long v;
-  v = wsum(lc.crossings);    if (lane == 0 && v) atomicAdd(&cnt->crossings, v);
-  v = wsum(lc.interactions); if (lane == 0 && v) atomicAdd(&cnt->interactions, v);
-  v = wsum(lc.absorptions);  if (lane == 0 && v) atomicAdd(&cnt->absorptions, v);
-  v = wsum(lc.scatterings);  if (lane == 0 && v) atomicAdd(&cnt->scatterings, v);
-  v = wsum(lc.escaped);      if (lane == 0 && v) atomicAdd(&cnt->escaped, v);
-  v = wsum(lc.lineEscapes);  if (lane == 0 && v) atomicAdd(&cnt->lineEscapes, v);
-  v = wsum(lc.trapped);      if (lane == 0 && v) atomicAdd(&cnt->trapped, v);
-  v = wsum(lc.emissions);    if (lane == 0 && v) atomicAdd(&cnt->emissions, v);
-  v = wsum(lc.errors);       if (lane == 0 && v) atomicAdd(&cnt->errors, v);
-  double q = lc.qPhot;
-  for (int o = 16; o > 0; o >>= 1) q += __shfl_down_sync(FULL, q, o);
-  if (lane == 0 && q != 0.) atomicAdd(&cnt->qPhot, q);
+// A batch of nebulae sharing one frequency mesh and chemistry: their cells are
+// numbered batch-wide (the per-cell arrays are the concatenation of the
+// nebulae's), and packet ids are handed out batch-wide, nebula b owning
+// [pktBegin[b], pktBegin[b+1]).  A lane that takes a packet looks up its
+// nebula (bisection over the batch), then runs the same emit / step code in
+// that nebula's geometry with its own deltaE = L*/nPhotons and its own Philox
+// key and counter base, so every nebula's histories are those of a run of the
+// nebula alone.
+template <typename R>
+__global__ void __launch_bounds__(256)
+transportKernelBatched(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportCounters* cnt,
+                       const NebulaDesc* __restrict__ neb, const unsigned long long* __restrict__ pktBegin, int nNeb,
+                       const float* __restrict__ axes, const int32_t* __restrict__ active,
+                       const float* __restrict__ cdfs) {
+  extern __shared__ float smem[];
+  float* sNu = smem;
+  for (int i = threadIdx.x; i < g.nbins; i += blockDim.x) sNu[i] = g.nu[i];
+  __syncthreads();
+  TransportShared<R> sh{sNu};
+  const unsigned long long n = pktBegin[nNeb];
+
+  const unsigned FULL = 0xffffffffu;
+  LocalCounters lc;
+  Packet<R> p;
+  p.nEmit = 0; p.nStep = 0;
+  NebulaGeo q{};
+  double deltaE = 0.;
+  R deltaER = R(0);
+  int state = ST_IDLE;
+
+  for (;;) {
+    const unsigned need = __ballot_sync(FULL, state == ST_IDLE);
+    if (need) {
+      const unsigned long long id = refill(need, cnt);
+      if (state == ST_IDLE) {
+        if (id < n) {
+          int lo = 0, hi = nNeb - 1;      // last b with pktBegin[b] <= id
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(pktBegin + mid) <= id) lo = mid; else hi = mid - 1;
+          }
+          const NebulaDesc& d = neb[lo];
+          q.nx_ = d.nx; q.ny_ = d.ny; q.nz_ = d.nz; q.symmetric_ = d.symmetric; q.rOut_ = d.rOut;
+          q.X_ = axes + d.axOff; q.Y_ = q.X_ + d.nx; q.Z_ = q.Y_ + d.ny;
+          q.active_ = active + d.actOff;
+          q.cdf_ = cdfs + d.cdfOff;
+          for (int k = 0; k < 3; ++k) { q.starIdx_[k] = d.starIdx[k]; q.starPos_[k] = d.starPos[k]; }
+          deltaE = d.deltaE;
+          deltaER = (R)deltaE;
+          p.rng.init(d.seed, d.counterBase + (id - __ldg(pktBegin + lo)));
+          p.type = PT_STELLAR;
+          p.nEmit = 0;
+          state = ST_EMIT;
+        } else {
+          state = ST_DONE;
+        }
+      }
+    }
+    if (__ballot_sync(FULL, state != ST_DONE) == 0u) break;
+    if (state == ST_EMIT) state = emitPacket<R>(g, q, in, out, sh, p, deltaE, lc);
+    else if (state == ST_STEP) state = stepPacket<R>(g, q, in, out, sh, p, deltaER, deltaE, lc);
+  }
+  flushCounters(lc, cnt);
 }
 
 }  // namespace mcx

@@ -11,6 +11,20 @@ cudaError_t launchTransportF32(const DevGrid& g, const DevTransportIn& in, const
   return cudaGetLastError();
 }
 
+cudaError_t launchTransportBatchedF32(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,
+                                      DevTransportCounters* cnt, const NebulaDesc* neb,
+                                      const unsigned long long* pktBegin, int nNeb, const float* axes,
+                                      const int32_t* active, const float* cdfs, const TransportLaunch& L,
+                                      cudaStream_t s) {
+  transportKernelBatched<float><<<L.blocks, L.threads, L.smem, s>>>(g, in, out, cnt, neb, pktBegin, nNeb, axes, active,
+                                                                  cdfs);
+  return cudaGetLastError();
+}
+
+cudaError_t transportOccupancyBatchedF32(int threads, size_t smem, int* blocksPerSM) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, transportKernelBatched<float>, threads, smem);
+}
+
 cudaError_t transportOccupancyF32(int threads, size_t smem, int* blocksPerSM) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, transportKernel<float>, threads, smem);
 }

@@ -11,6 +11,20 @@ cudaError_t launchTransportF64(const DevGrid& g, const DevTransportIn& in, const
   return cudaGetLastError();
 }
 
+cudaError_t launchTransportBatchedF64(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,
+                                      DevTransportCounters* cnt, const NebulaDesc* neb,
+                                      const unsigned long long* pktBegin, int nNeb, const float* axes,
+                                      const int32_t* active, const float* cdfs, const TransportLaunch& L,
+                                      cudaStream_t s) {
+  transportKernelBatched<double><<<L.blocks, L.threads, L.smem, s>>>(g, in, out, cnt, neb, pktBegin, nNeb, axes, active,
+                                                                  cdfs);
+  return cudaGetLastError();
+}
+
+cudaError_t transportOccupancyBatchedF64(int threads, size_t smem, int* blocksPerSM) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, transportKernelBatched<double>, threads, smem);
+}
+
 cudaError_t transportOccupancyF64(int threads, size_t smem, int* blocksPerSM) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, transportKernel<double>, threads, smem);
 }

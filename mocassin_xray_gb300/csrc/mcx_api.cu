@@ -382,6 +382,21 @@ struct mcx_ctx {
   int xrefAll[30] = {};
   DBuf<double> linePartial, lineSums;
   DBuf<int32_t> lineForbBase;
+  // batch of nebulae (mcx_load_batched); nNeb = 0 for a single grid
+  int nNeb = 0;
+  std::vector<int32_t> nebCellOff;                 // [nNeb+1]
+  std::vector<NebulaDesc> nebDesc;                 // geometry; packet constants set per transport
+  std::vector<float> nebLStar;
+  std::vector<int32_t> nebSym, nebNx, nebNy, nebNz;
+  std::vector<std::vector<int32_t>> nebActive;     // [nz][ny][nx] per nebula, batch-wide ids
+  std::vector<float> nebGauntTeOld;                // each nebula's Gaunt cache temperature
+  std::vector<float> nebGauntTemps;                // host staging of the Gaunt temperatures for the upload
+  DBuf<float> nebGauntTeDev;
+  DBuf<NebulaDesc> nebDescDev;
+  DBuf<unsigned long long> nebPktBegin;
+  DBuf<float> nebAxes, nebCdf, nebFfK, jDiv;
+  DBuf<int32_t> nebActiveDev;
+  DBuf<int16_t> nebFfIdx;
   // mcx_state_save snapshot
   DBuf<float> snapTe, snapNe, snapTeOld, snapNeOld, snapIonDen;
   DBuf<int32_t> snapConverged;
@@ -428,6 +443,18 @@ cudaError_t transpose(const float* in, float* out, int rows, int cols, cudaStrea
 }
 
 // j = (j * mul) / div, two roundings as in source/iteration_mod.f90:1002-1031
+// the same with the divisor of each cell's nebula (a batch mixing octant and full grids)
+__global__ void scaleJCellKernel(double* j, size_t n, size_t C1, double mul, const float* __restrict__ div) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (; i < n; i += stride) {
+    double v = j[i] * mul;
+    const double d = (double)div[i % C1];
+    if (d != 1.) v = v / d;
+    j[i] = v;
+  }
+}
+
 __global__ void scaleJKernel(double* j, size_t n, double mul, double div) {
   size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   size_t stride = (size_t)gridDim.x * blockDim.x;
@@ -590,9 +617,16 @@ static void buildOpacityTables(const Setup& s, std::vector<int32_t>& csrStart, s
   csrStart[nb] = (int32_t)csrTerm.size();
 }
 
+static int loadSetup(mcx_ctx* c, const Setup& s);
+
 extern "C" int mcx_load(mcx_ctx* c, const mcx_setup* m) {
   if (!c || !m) return fail(c, MCX_ERR_INPUT, "mcx_load: null argument");
-  const Setup& s = m->s;
+  c->nNeb = 0;
+  c->nebCellOff.clear();
+  return loadSetup(c, m->s);
+}
+
+static int loadSetup(mcx_ctx* c, const Setup& s) {
   CK(cudaSetDevice(c->device), "cudaSetDevice");
   c->loaded = false;
   c->nx = s.nx; c->ny = s.ny; c->nz = s.nz; c->nCells = s.nCells; c->nbins = s.nbins;
@@ -734,6 +768,138 @@ extern "C" int mcx_load(mcx_ctx* c, const mcx_setup* m) {
   CK(cudaDeviceSynchronize(), "mcx_load");
   c->haveOpacity = c->haveRecPDF = c->haveDustPDF = false;
   c->loaded = true;
+  return MCX_OK;
+}
+
+// -------------------------------------------------------------- batches
+extern "C" int mcx_load_batched(mcx_ctx* c, const mcx_setup* const* setups, int32_t n) {
+  if (!c || !setups || n < 1) return fail(c, MCX_ERR_INPUT, "mcx_load_batched: null argument or empty batch");
+  if (n > 32767) return fail(c, MCX_ERR_INPUT, "mcx_load_batched: at most 32767 nebulae");
+  for (int b = 0; b < n; ++b)
+    if (!setups[b]) return fail(c, MCX_ERR_INPUT, "mcx_load_batched: null set-up");
+  const Setup& s0 = setups[0]->s;
+  auto bad = [&](int b, const char* what) {
+    return fail(c, MCX_ERR_INPUT, "mcx_load_batched: nebula " + std::to_string(b) + " differs from nebula 0 in " + what);
+  };
+  int64_t total = 0;
+  for (int b = 0; b < n; ++b) {
+    const Setup& s = setups[b]->s;
+    if (!s.p.lgGas || s.p.lgDust) return fail(c, MCX_ERR_INPUT, "mcx_load_batched: a batch holds gas-only nebulae");
+    if (s.p.lgRadPress) return fail(c, MCX_ERR_INPUT, "mcx_load_batched: radiation pressure is not supported in a batch");
+    if (s.nbins != s0.nbins || s.nu != s0.nu || s.widFlx != s0.widFlx) return bad(b, "the frequency mesh");
+    if (s.p.nstages != s0.p.nstages || s.nElemUsed != s0.nElemUsed) return bad(b, "nstages or the elements");
+    for (int z = 0; z < kNElements; ++z)
+      if (s.elemXref[z] != s0.elemXref[z] || s.elemAbun[z] != s0.elemAbun[z]) return bad(b, "the abundances");
+    if (s.p.lgCompton != s0.p.lgCompton) return bad(b, "the Compton switch");
+    if (s.xSec != s0.xSec || s.ionEdge != s0.ionEdge) return bad(b, "the cross-section tables");
+    for (int32_t a : s.active)
+      if (a < 0 || a > s.nCells) return fail(c, MCX_ERR_INPUT, "mcx_load_batched: sub-grids are not supported");
+    if (s.starIdx[0] < 1 || s.starIdx[0] > s.nx || s.starIdx[1] < 1 || s.starIdx[1] > s.ny || s.starIdx[2] < 1 ||
+        s.starIdx[2] > s.nz)
+      return fail(c, MCX_ERR_INPUT, "mcx_load_batched: a source lies outside its grid");
+    total += s.nCells;
+  }
+  if (total > (int64_t)INT32_MAX - 1) return fail(c, MCX_ERR_INPUT, "mcx_load_batched: too many cells");
+  // the concatenated per-cell state: nebula b owns cells off[b]+1 .. off[b+1]
+  std::vector<int32_t> off(n + 1, 0);
+  for (int b = 0; b < n; ++b) off[b + 1] = off[b] + setups[b]->s.nCells;
+  const size_t C1 = (size_t)total + 1;
+  const int S = s0.p.nstages, E = std::max(s0.nElemUsed, 1);
+  Setup comb = s0;
+  comb.nCells = (int)total;
+  auto concat = [&](std::vector<float> Setup::*f, float fill0) {
+    std::vector<float> v(C1, fill0);
+    for (int b = 0; b < n; ++b) {
+      const std::vector<float>& src = setups[b]->s.*f;
+      for (int k = 1; k <= setups[b]->s.nCells; ++k) v[off[b] + k] = src[k];
+    }
+    comb.*f = std::move(v);
+  };
+  concat(&Setup::Hden, s0.Hden[0]);
+  concat(&Setup::Te, s0.Te[0]);
+  concat(&Setup::Ne, s0.Ne[0]);
+  concat(&Setup::TeOld, s0.TeOld[0]);
+  concat(&Setup::NeOld, s0.NeOld[0]);
+  concat(&Setup::volume, 1.f);
+  comb.Ndust.assign(C1, 0.f);
+  comb.ionDen.assign((size_t)S * E * C1, 0.f);
+  for (int b = 0; b < n; ++b) {
+    const Setup& s = setups[b]->s;
+    const size_t Cb1 = (size_t)s.nCells + 1;
+    for (size_t plane = 0; plane < (size_t)S * E; ++plane) {
+      comb.ionDen[plane * C1] = s0.ionDen[plane * ((size_t)s0.nCells + 1)];
+      for (int k = 1; k <= s.nCells; ++k) comb.ionDen[plane * C1 + off[b] + k] = s.ionDen[plane * Cb1 + k];
+    }
+  }
+  int rc = loadSetup(c, comb);
+  if (rc != MCX_OK) return rc;
+  c->loaded = false;
+  // batch geometry
+  std::vector<double> vd(C1, 1.0);
+  std::vector<float> vf(C1, 1.f), axes, cdfs, jdiv(C1, 1.f);
+  std::vector<int32_t> act;
+  std::vector<int16_t> ffIdx(C1, 0);
+  c->nebDesc.assign(n, NebulaDesc{});
+  c->nebLStar.assign(n, 0.f);
+  c->nebSym.assign(n, 0);
+  c->nebNx.assign(n, 0); c->nebNy.assign(n, 0); c->nebNz.assign(n, 0);
+  c->nebActive.assign(n, {});
+  for (int b = 0; b < n; ++b) {
+    const Setup& s = setups[b]->s;
+    NebulaDesc& d = c->nebDesc[b];
+    d.nx = s.nx; d.ny = s.ny; d.nz = s.nz; d.symmetric = s.p.lgSymmetricXYZ ? 1 : 0;
+    d.axOff = (int32_t)axes.size();
+    axes.insert(axes.end(), s.xAxis.begin(), s.xAxis.end());
+    axes.insert(axes.end(), s.yAxis.begin(), s.yAxis.end());
+    axes.insert(axes.end(), s.zAxis.begin(), s.zAxis.end());
+    d.actOff = (int32_t)act.size();
+    std::vector<int32_t> ab(s.active.size());
+    for (size_t v = 0; v < s.active.size(); ++v) ab[v] = s.active[v] > 0 ? s.active[v] + off[b] : 0;
+    act.insert(act.end(), ab.begin(), ab.end());
+    c->nebActive[b] = std::move(ab);
+    d.cdfOff = (int32_t)cdfs.size();
+    cdfs.insert(cdfs.end(), s.srcCDF.begin(), s.srcCDF.end());
+    for (int k = 0; k < 3; ++k) { d.starIdx[k] = s.starIdx[k]; d.starPos[k] = s.starPos[k]; }
+    d.rOut = s.p.R_out;
+    c->nebLStar[b] = s.LStar;
+    c->nebSym[b] = d.symmetric;
+    c->nebNx[b] = s.nx; c->nebNy[b] = s.ny; c->nebNz[b] = s.nz;
+    for (int i = 1; i <= s.nx; ++i)
+      for (int j = 1; j <= s.ny; ++j)
+        for (int k = 1; k <= s.nz; ++k) {
+          const int cell = s.activeAt(i, j, k);
+          if (cell > 0) { vd[off[b] + cell] = volumeD(s, i, j, k); vf[off[b] + cell] = s.volume[cell]; }
+        }
+    for (int k = 1; k <= s.nCells; ++k) {
+      ffIdx[off[b] + k] = (int16_t)b;
+      jdiv[off[b] + k] = d.symmetric ? 8.f : 1.f;
+    }
+  }
+  CK(upload(c->volD, vd), "upload volume");
+  CK(upload(c->volF, vf), "upload volume");
+  CK(upload(c->nebAxes, axes), "upload batch axes");
+  CK(upload(c->nebActiveDev, act), "upload batch active");
+  CK(upload(c->nebCdf, cdfs), "upload batch source CDFs");
+  CK(upload(c->nebFfIdx, ffIdx), "upload batch Gaunt index");
+  CK(upload(c->jDiv, jdiv), "upload batch octant factors");
+  CK(c->nebFfK.alloc((size_t)n * 2 * c->nbins), "alloc batch Gaunt tables");
+  CK(c->nebGauntTeDev.alloc(n), "alloc batch Gaunt temperatures");
+  CK(c->nebDescDev.alloc(n), "alloc batch descriptors");
+  CK(c->nebPktBegin.alloc((size_t)n + 1), "alloc batch packet offsets");
+  CK(cudaDeviceSynchronize(), "mcx_load_batched");
+  c->nebGauntTeOld.assign(n, -1.f);
+  c->nebCellOff = off;
+  c->nNeb = n;
+  c->loaded = true;
+  return MCX_OK;
+}
+
+extern "C" int mcx_batch_info(mcx_ctx* c, int32_t* n_nebulae, int32_t* cell_offset) {
+  if (!c || !n_nebulae) return fail(c, MCX_ERR_INPUT, "mcx_batch_info: null argument");
+  if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_batch_info: no model loaded");
+  *n_nebulae = c->nNeb;
+  if (cell_offset)
+    for (int b = 0; b <= c->nNeb; ++b) cell_offset[b] = c->nebCellOff[b];
   return MCX_OK;
 }
 
@@ -879,7 +1045,20 @@ extern "C" int mcx_emission(mcx_ctx* c, const mcx_phase_opts* opts, mcx_phase_st
   const size_t C1 = (size_t)c->nCells + 1;
   CK(cudaMemcpyAsync(c->computeMask.p, mask.data(), C1, cudaMemcpyHostToDevice, c->stream), "h2d mask");
   CK(cudaEventRecord(c->ev0, c->stream), "event");
-  CK(launchEmissionGaunt(c->emission->dev, c->gauntTeOld, c->stream), "emission gaunt");
+  EmissionDev ed = c->emission->dev;
+  if (c->nNeb > 0) {
+    // one Gaunt table per nebula, each at its own cache temperature
+    c->nebGauntTemps.resize(c->nNeb);
+    for (int b = 0; b < c->nNeb; ++b)
+      c->nebGauntTemps[b] = c->nebGauntTeOld[b] > 0.f ? c->nebGauntTeOld[b] : c->gauntTeOld;
+    CK(cudaMemcpyAsync(c->nebGauntTeDev.p, c->nebGauntTemps.data(), sizeof(float) * c->nNeb, cudaMemcpyHostToDevice,
+                       c->stream), "h2d Gaunt temperatures");
+    ed.ffK = c->nebFfK.p;
+    CK(launchEmissionGauntBatched(ed, c->nebGauntTeDev.p, c->nNeb, c->stream), "emission gaunt");
+    ed.ffIdx = c->nebFfIdx.p;
+  } else {
+    CK(launchEmissionGaunt(ed, c->gauntTeOld, c->stream), "emission gaunt");
+  }
   const float* forLines = nullptr;
   if (c->balance && c->balance->dev.nAtoms > 0) {
     const int prec = (opts && opts->precision == MCX_PHASE_MIXED) ? kBalMixed : kBalFp64;
@@ -888,8 +1067,8 @@ extern "C" int mcx_emission(mcx_ctx* c, const mcx_phase_opts* opts, mcx_phase_st
        "emission forLines");
     forLines = c->forLines.p;
   }
-  CK(launchEmission(c->emission->dev, c->te.p, c->ne.p, c->ionDen.p, c->computeMask.p, forLines, c->recPDF.p,
-                    c->totalLines.p, c->stream), "emission kernel");
+  CK(launchEmission(ed, c->te.p, c->ne.p, c->ionDen.p, c->computeMask.p, forLines, c->recPDF.p, c->totalLines.p,
+                    c->stream), "emission kernel");
   CK(transpose(c->recPDF.p, c->recCDFT.p, c->nbins, (int)C1, c->stream), "transpose recPDF");
   CK(cudaEventRecord(c->ev1, c->stream), "event");
   CK(cudaStreamSynchronize(c->stream), "mcx_emission");
@@ -935,19 +1114,29 @@ extern "C" int mcx_opacity(mcx_ctx* c, const mcx_phase_opts* opts, mcx_phase_sta
   CK(cudaMemcpyAsync(neOld.data(), c->neOld.p, C1 * 4, cudaMemcpyDeviceToHost, c->stream), "d2h NeOld");
   CK(cudaStreamSynchronize(c->stream), "mcx_opacity");
   int64_t computed = 0, skipped = 0;
-  for (int i = 1; i <= c->nx; ++i)
-    for (int j = 1; j <= c->ny; ++j)
-      for (int k = 1; k <= c->nz; ++k) {
-        int cell = c->activeHost[(size_t)(i - 1) + (size_t)c->nx * ((size_t)(j - 1) + (size_t)c->ny * (size_t)(k - 1))];
-        if (cell <= 0) continue;
-        bool skip = it > 1 && (std::fabs(te[cell] - teOld[cell]) / teOld[cell]) < 0.005f &&
-                    (std::fabs(ne[cell] - neOld[cell]) / neOld[cell]) < 0.005f;
-        if (skip) { ++skipped; continue; }
-        mask[cell] = 1;
-        ++computed;
-        if (std::fabs(1.f - c->gauntTeOld / te[cell]) > 0.10f) c->gauntTeOld = te[cell];
-        gte[cell] = c->gauntTeOld;
-      }
+  // each grid in its processing order (i, j, k nested, k fastest) with its own Gaunt cache
+  auto replay = [&](int nx, int ny, int nz, const int32_t* act, float& gauntTeOld) {
+    for (int i = 1; i <= nx; ++i)
+      for (int j = 1; j <= ny; ++j)
+        for (int k = 1; k <= nz; ++k) {
+          int cell = act[(size_t)(i - 1) + (size_t)nx * ((size_t)(j - 1) + (size_t)ny * (size_t)(k - 1))];
+          if (cell <= 0) continue;
+          bool skip = it > 1 && (std::fabs(te[cell] - teOld[cell]) / teOld[cell]) < 0.005f &&
+                      (std::fabs(ne[cell] - neOld[cell]) / neOld[cell]) < 0.005f;
+          if (skip) { ++skipped; continue; }
+          mask[cell] = 1;
+          ++computed;
+          if (std::fabs(1.f - gauntTeOld / te[cell]) > 0.10f) gauntTeOld = te[cell];
+          gte[cell] = gauntTeOld;
+        }
+  };
+  if (c->nNeb > 0) {
+    for (int b = 0; b < c->nNeb; ++b)
+      replay(c->nebNx[b], c->nebNy[b], c->nebNz[b], c->nebActive[b].data(), c->nebGauntTeOld[b]);
+    c->gauntTeOld = c->nebGauntTeOld[0];
+  } else {
+    replay(c->nx, c->ny, c->nz, c->activeHost.data(), c->gauntTeOld);
+  }
   CK(cudaMemcpyAsync(c->computeMask.p, mask.data(), C1, cudaMemcpyHostToDevice, c->stream), "h2d mask");
   CK(cudaMemcpyAsync(c->gauntTe.p, gte.data(), C1 * 4, cudaMemcpyHostToDevice, c->stream), "h2d gauntTe");
   OpacityDev t{};
@@ -972,6 +1161,30 @@ extern "C" int mcx_opacity(mcx_ctx* c, const mcx_phase_opts* opts, mcx_phase_sta
 }
 
 // ---------------------------------------------------------- transport phase
+// counters of the launch just queued (events ev0/ev1 around it) into stats
+static int transportFinish(mcx_ctx* c, mcx_transport_stats* stats, const char* who) {
+  DevTransportCounters h{};
+  CK(cudaMemcpyAsync(&h, c->counters.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream), "d2h counters");
+  CK(cudaStreamSynchronize(c->stream), who);
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->crossings = (int64_t)h.crossings;
+    stats->interactions = (int64_t)h.interactions;
+    stats->absorptions = (int64_t)h.absorptions;
+    stats->scatterings = (int64_t)h.scatterings;
+    stats->escaped = (int64_t)h.escaped;
+    stats->line_escapes = (int64_t)h.lineEscapes;
+    stats->trapped = (int64_t)h.trapped;
+    stats->emissions = (int64_t)h.emissions;
+    stats->q_phot = h.qPhot;
+    cudaEventElapsedTime(&stats->kernel_ms, c->ev0, c->ev1);
+  }
+  if (h.errors)
+    return fail(c, MCX_ERR_INTERNAL,
+                std::string(who) + ": " + std::to_string(h.errors) + " packet(s) reached a state where the reference stops");
+  return MCX_OK;
+}
+
 extern "C" int mcx_transport(mcx_ctx* c, const mcx_transport_opts* o, mcx_transport_stats* stats) {
   if (!c || !o) return fail(c, MCX_ERR_INPUT, "mcx_transport: null argument");
   if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_transport: no model loaded");
@@ -982,6 +1195,7 @@ extern "C" int mcx_transport(mcx_ctx* c, const mcx_transport_opts* o, mcx_transp
   if (c->lgDust && !c->lgGas && !c->haveDustPDF) return fail(c, MCX_ERR_STATE, "mcx_transport: no dust emission CDF");
   if (o->precision != MCX_PREC_FP32_GEOM && o->precision != MCX_PREC_FP64)
     return fail(c, MCX_ERR_INPUT, "mcx_transport: unknown precision");
+  if (c->nNeb > 0) return fail(c, MCX_ERR_STATE, "mcx_transport: the context holds a batch (use mcx_transport_batched)");
   CK(cudaSetDevice(c->device), "cudaSetDevice");
   const int64_t norm = o->n_photons_norm > 0 ? o->n_photons_norm : o->n_packets;
   const double deltaE = norm > 0 ? (double)c->lStar / (double)norm : 0.;
@@ -1029,34 +1243,95 @@ extern "C" int mcx_transport(mcx_ctx* c, const mcx_transport_opts* o, mcx_transp
     if (e != cudaSuccess) return cudaFail(c, e, "transport kernel");
   }
   CK(cudaEventRecord(c->ev1, c->stream), "event");
-  DevTransportCounters h{};
-  CK(cudaMemcpyAsync(&h, c->counters.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream), "d2h counters");
-  CK(cudaStreamSynchronize(c->stream), "mcx_transport");
-  if (stats) {
-    std::memset(stats, 0, sizeof(*stats));
-    stats->crossings = (int64_t)h.crossings;
-    stats->interactions = (int64_t)h.interactions;
-    stats->absorptions = (int64_t)h.absorptions;
-    stats->scatterings = (int64_t)h.scatterings;
-    stats->escaped = (int64_t)h.escaped;
-    stats->line_escapes = (int64_t)h.lineEscapes;
-    stats->trapped = (int64_t)h.trapped;
-    stats->emissions = (int64_t)h.emissions;
-    stats->q_phot = h.qPhot;
-    cudaEventElapsedTime(&stats->kernel_ms, c->ev0, c->ev1);
+  return transportFinish(c, stats, "mcx_transport");
+}
+
+// transport of every nebula of a batch in one launch
+extern "C" int mcx_transport_batched(mcx_ctx* c, const mcx_transport_opts* o, const mcx_batch_packets* pk,
+                                     mcx_transport_stats* stats) {
+  if (!c || !o || !pk || !pk->n_packets || !pk->seed || !pk->counter_base)
+    return fail(c, MCX_ERR_INPUT, "mcx_transport_batched: null argument");
+  if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_transport_batched: no model loaded");
+  if (c->nNeb <= 0) return fail(c, MCX_ERR_STATE, "mcx_transport_batched: the context holds no batch (mcx_load_batched)");
+  if (o->istar != 1) return fail(c, MCX_ERR_INPUT, "mcx_transport_batched: only source 1 is supported");
+  if (!c->haveOpacity || !c->haveRecPDF)
+    return fail(c, MCX_ERR_STATE, "mcx_transport_batched: run mcx_opacity and mcx_emission first");
+  if (o->precision != MCX_PREC_FP32_GEOM && o->precision != MCX_PREC_FP64)
+    return fail(c, MCX_ERR_INPUT, "mcx_transport_batched: unknown precision");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  const int n = c->nNeb;
+  std::vector<unsigned long long> begin(n + 1, 0);
+  std::vector<NebulaDesc> desc = c->nebDesc;
+  for (int b = 0; b < n; ++b) {
+    if (pk->n_packets[b] < 0) return fail(c, MCX_ERR_INPUT, "mcx_transport_batched: negative packet count");
+    const int64_t norm = (pk->n_photons_norm && pk->n_photons_norm[b] > 0) ? pk->n_photons_norm[b] : pk->n_packets[b];
+    desc[b].deltaE = norm > 0 ? (double)c->nebLStar[b] / (double)norm : 0.;
+    desc[b].seed = pk->seed[b];
+    desc[b].counterBase = pk->counter_base[b];
+    begin[b + 1] = begin[b] + (unsigned long long)pk->n_packets[b];
   }
-  if (h.errors)
-    return fail(c, MCX_ERR_INTERNAL,
-                "mcx_transport: " + std::to_string(h.errors) + " packet(s) reached a state where the reference stops");
-  return MCX_OK;
+  if (o->zero_estimators) {
+    CK(cudaMemsetAsync(c->jste.p, 0, c->jste.bytes(), c->stream), "memset Jste");
+    CK(cudaMemsetAsync(c->escaped.p, 0, c->escaped.bytes(), c->stream), "memset escaped");
+  }
+  CK(cudaMemsetAsync(c->counters.p, 0, sizeof(DevTransportCounters), c->stream), "memset counters");
+  CK(cudaMemcpyAsync(c->nebDescDev.p, desc.data(), sizeof(NebulaDesc) * n, cudaMemcpyHostToDevice, c->stream),
+     "h2d batch descriptors");
+  CK(cudaMemcpyAsync(c->nebPktBegin.p, begin.data(), sizeof(unsigned long long) * (n + 1), cudaMemcpyHostToDevice,
+                     c->stream), "h2d batch packet offsets");
+  DevGrid g{};
+  g.nCells = c->nCells; g.nbins = c->nbins;
+  g.lgDust = 0; g.lgGas = 1; g.lgCompton = c->lgCompton; g.radPress = 0;
+  g.ionEdge1 = c->ionEdge1;
+  g.nu = c->nu.p; g.KNsigmaT = c->KNsigmaT.p; g.KNcdfT = c->KNcdfT.p; g.PcompT = c->PcompT.p;
+  g.volD = c->volD.p; g.volF = c->volF.p;
+  DevTransportIn in{};
+  in.opacity = c->opacity.p; in.recCDFT = c->recCDFT.p; in.totalLines = c->totalLines.p; in.ne = c->ne.p;
+  DevTransportOut out{};
+  out.jste = c->jste.p; out.escaped = c->escaped.p;
+  TransportLaunch L{};
+  L.threads = o->block_size > 0 ? o->block_size : 256;
+  if (L.threads % 32 != 0 || L.threads > 256)
+    return fail(c, MCX_ERR_INPUT, "mcx_transport_batched: block_size must be a multiple of 32 up to 256");
+  L.smem = (size_t)c->nbins * sizeof(float);
+  const bool fp64 = o->precision == MCX_PREC_FP64;
+  int perSM = 0;
+  CK(fp64 ? transportOccupancyBatchedF64(L.threads, L.smem, &perSM) : transportOccupancyBatchedF32(L.threads, L.smem, &perSM),
+     "occupancy");
+  if (perSM < 1) perSM = 1;
+  L.blocks = c->numSMs * (o->grid_mult > 0 ? std::min(o->grid_mult, perSM) : perSM);
+  const unsigned long long total = begin[n];
+  if (total > 0) {
+    const unsigned long long maxBlocks = (total + L.threads - 1) / L.threads;
+    if ((unsigned long long)L.blocks > maxBlocks) L.blocks = (int)maxBlocks;
+  }
+  CK(cudaEventRecord(c->ev0, c->stream), "event");
+  if (total > 0) {
+    cudaError_t e = fp64 ? launchTransportBatchedF64(g, in, out, c->counters.p, c->nebDescDev.p, c->nebPktBegin.p, n,
+                                                     c->nebAxes.p, c->nebActiveDev.p, c->nebCdf.p, L, c->stream)
+                         : launchTransportBatchedF32(g, in, out, c->counters.p, c->nebDescDev.p, c->nebPktBegin.p, n,
+                                                     c->nebAxes.p, c->nebActiveDev.p, c->nebCdf.p, L, c->stream);
+    if (e != cudaSuccess) return cudaFail(c, e, "batched transport kernel");
+  }
+  CK(cudaEventRecord(c->ev1, c->stream), "event");
+  return transportFinish(c, stats, "mcx_transport_batched");
 }
 
 extern "C" int mcx_normalize_j(mcx_ctx* c) {
   if (!c) return MCX_ERR_INPUT;
   if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_normalize_j: no model loaded");
   CK(cudaSetDevice(c->device), "cudaSetDevice");
-  const double div = c->symmetric ? 8. : 1.;
   int blocks = c->numSMs * 4;
+  if (c->nNeb > 0) {
+    const size_t C1 = (size_t)c->nCells + 1;
+    scaleJCellKernel<<<blocks, 256, 0, c->stream>>>(c->jste.p, c->jste.n, C1, 1.e-9, c->jDiv.p);
+    CK(cudaGetLastError(), "scale J");
+    scaleJCellKernel<<<blocks, 256, 0, c->stream>>>(c->escaped.p, c->escaped.n, C1, 1., c->jDiv.p);
+    CK(cudaGetLastError(), "scale escaped");
+    CK(cudaStreamSynchronize(c->stream), "mcx_normalize_j");
+    return MCX_OK;
+  }
+  const double div = c->symmetric ? 8. : 1.;
   scaleJKernel<<<blocks, 256, 0, c->stream>>>(c->jste.p, c->jste.n, 1.e-9, div);
   CK(cudaGetLastError(), "scale J");
   if (div != 1.) {
@@ -1119,10 +1394,25 @@ extern "C" int mcx_balance(mcx_ctx* c, const mcx_balance_opts* opts, mcx_balance
   return MCX_OK;
 }
 
+static int iterateImpl(mcx_ctx* c, const mcx_iterate_opts* o, const mcx_batch_packets* pk, mcx_iterate_stats* stats);
+
 extern "C" int mcx_iterate(mcx_ctx* c, const mcx_iterate_opts* o, mcx_iterate_stats* stats) {
   if (!c || !o) return fail(c, MCX_ERR_INPUT, "mcx_iterate: null argument");
   if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_iterate: no model loaded");
   if (o->n_packets <= 0) return fail(c, MCX_ERR_INPUT, "mcx_iterate: n_packets must be positive");
+  if (c->nNeb > 0) return fail(c, MCX_ERR_STATE, "mcx_iterate: the context holds a batch (use mcx_iterate_batched)");
+  return iterateImpl(c, o, nullptr, stats);
+}
+
+extern "C" int mcx_iterate_batched(mcx_ctx* c, const mcx_iterate_opts* o, const mcx_batch_packets* pk,
+                                   mcx_iterate_stats* stats) {
+  if (!c || !o || !pk) return fail(c, MCX_ERR_INPUT, "mcx_iterate_batched: null argument");
+  if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_iterate_batched: no model loaded");
+  if (c->nNeb <= 0) return fail(c, MCX_ERR_STATE, "mcx_iterate_batched: the context holds no batch");
+  return iterateImpl(c, o, pk, stats);
+}
+
+static int iterateImpl(mcx_ctx* c, const mcx_iterate_opts* o, const mcx_batch_packets* pk, mcx_iterate_stats* stats) {
   CK(cudaSetDevice(c->device), "cudaSetDevice");
   mcx_iterate_stats st{};
   cudaEvent_t t0 = nullptr, t1 = nullptr;
@@ -1145,7 +1435,7 @@ extern "C" int mcx_iterate(mcx_ctx* c, const mcx_iterate_opts* o, mcx_iterate_st
     to.counter_base = o->counter_base;
     to.n_photons_norm = o->n_packets;
     to.zero_estimators = 1;
-    rc = mcx_transport(c, &to, &st.transport);
+    rc = pk ? mcx_transport_batched(c, &to, pk, &st.transport) : mcx_transport(c, &to, &st.transport);
   }
   if (rc == MCX_OK) rc = mcx_normalize_j(c);
   if (rc == MCX_OK) {

@@ -42,6 +42,19 @@ struct DevTransportOut {
   double* hEst;              // [nbins][C+1] or null
 };
 
+// One nebula of a batch (mcx_load_batched): its geometry as slices of the
+// batch's concatenated axes / active map / source CDFs, and the constants of
+// its packets.
+struct NebulaDesc {
+  int32_t nx, ny, nz, symmetric;
+  int32_t axOff, actOff, cdfOff, pad0;  // offsets into the batch's axes / active / source-CDF arrays
+  int32_t starIdx[3];
+  float starPos[3];
+  float rOut, pad1;
+  double deltaE;                        // L* / nPhotons of this nebula
+  uint64_t seed, counterBase;           // Philox key and the global id of its first packet
+};
+
 // Counters accumulated by the transport kernel (device scratch).
 struct DevTransportCounters {
   unsigned long long crossings, interactions, absorptions, scatterings;

@@ -76,6 +76,9 @@ class Context:
             raise abi.McxError(rc, lib().mcx_setup_last_error().decode())
         self._h = h
         self.setup: Setup | None = None
+        self.batch: list[Setup] | None = None
+        self.cell_offsets: np.ndarray | None = None
+        self._cells = 0
 
     def close(self) -> None:
         if self._h:
@@ -97,10 +100,65 @@ class Context:
     def load(self, setup: Setup) -> None:
         self._check(lib().mcx_load(self._h, setup.handle))
         self.setup = setup
+        self.batch = None
+        self.cell_offsets = None
+        self._cells = setup.info.n_cells
+
+    def load_batched(self, setups: list[Setup]) -> None:
+        """A batch of nebulae in one context (mcx_load_batched): per-cell arrays are the concatenation
+        of the nebulae's behind one dump cell; `cell_offsets[b]` is nebula b's offset."""
+        arr = (C.c_void_p * len(setups))(*[x.handle.value for x in setups])
+        self._check(lib().mcx_load_batched(self._h, arr, len(setups)))
+        n = C.c_int32()
+        offs = (C.c_int32 * (len(setups) + 1))()
+        self._check(lib().mcx_batch_info(self._h, C.byref(n), offs))
+        self.setup = setups[0]
+        self.batch = list(setups)
+        self.cell_offsets = np.array(offs[:], dtype=np.int64)
+        self._cells = int(self.cell_offsets[-1])
+
+    def nebula_cells(self, a: np.ndarray, b: int) -> np.ndarray:
+        """The cells 1..nCells of nebula b from a batch-wide per-cell array (cells on the last axis)."""
+        return a[..., self.cell_offsets[b] + 1:self.cell_offsets[b + 1] + 1]
+
+    def _batch_packets(self, n_packets, seeds, counter_bases, n_photons_norm):
+        nb = len(self.batch)
+        keep = dict(n=np.ascontiguousarray(np.broadcast_to(np.asarray(n_packets, dtype=np.int64), (nb,))),
+                    s=np.ascontiguousarray(np.broadcast_to(np.asarray(seeds, dtype=np.uint64), (nb,))),
+                    c=np.ascontiguousarray(np.broadcast_to(np.asarray(0 if counter_bases is None else counter_bases,
+                                                                      dtype=np.uint64), (nb,))))
+        if n_photons_norm is not None:
+            keep["p"] = np.ascontiguousarray(np.broadcast_to(np.asarray(n_photons_norm, dtype=np.int64), (nb,)))
+        pk = abi.BatchPackets(n_packets=keep["n"].ctypes.data, seed=keep["s"].ctypes.data,
+                              counter_base=keep["c"].ctypes.data,
+                              n_photons_norm=keep["p"].ctypes.data if "p" in keep else None)
+        return pk, keep
+
+    def transport_batched(self, n_packets, seeds, counter_bases=None, precision: int = abi.PREC_FP32_GEOM,
+                          zero: bool = True, n_photons_norm=None, block_size: int = 0,
+                          grid_mult: int = 0) -> abi.TransportStats:
+        """Every nebula's packets in one launch: n_packets, seeds, counter_bases per nebula (scalars broadcast)."""
+        pk, keep = self._batch_packets(n_packets, seeds, counter_bases, n_photons_norm)
+        o = abi.TransportOpts(istar=1, precision=precision, zero_estimators=1 if zero else 0, block_size=block_size,
+                              grid_mult=grid_mult)
+        st = abi.TransportStats()
+        self._check(lib().mcx_transport_batched(self._h, C.byref(o), C.byref(pk), C.byref(st)))
+        return st
+
+    def iterate_batched(self, n_packets, seeds, counter_bases=None, n_iterate_mc: int = 1,
+                        transport_precision: int = abi.PREC_FP32_GEOM, balance_precision: int = abi.BAL_MIXED,
+                        emission_precision: int = abi.PHASE_MIXED) -> abi.IterateStats:
+        """One MC iteration of every nebula of the batch in one ABI call."""
+        pk, keep = self._batch_packets(n_packets, seeds, counter_bases, None)
+        o = abi.IterateOpts(n_iterate_mc=n_iterate_mc, transport_precision=transport_precision,
+                            balance_precision=balance_precision, emission_precision=emission_precision)
+        st = abi.IterateStats()
+        self._check(lib().mcx_iterate_batched(self._h, C.byref(o), C.byref(pk), C.byref(st)))
+        return st
 
     def _shape(self, arr_id: int) -> tuple[tuple, type]:
         s = self.setup.info
-        C1, nb = s.n_cells + 1, s.nbins
+        C1, nb = self._cells + 1, s.nbins
         f32, f64 = np.float32, np.float64
         shapes = {
             abi.ARR_OPACITY: ((nb, C1), f32), abi.ARR_RECPDF: ((nb, C1), f32), abi.ARR_SCAOPAC: ((nb, C1), f32),
