@@ -41,8 +41,9 @@ METRIC = "MC packets/s"
 UNIT = "packets/s"
 # kernels of one step: opacity 1; emission 5 (Gaunt table, forbidden lines per
 # ion and their sum, emissivity, CDF transpose); transport 1; J normalisation
-# 1; balance 63 (J integrals, state load, 20 rounds x (rates, atoms, secant), store)
-KERNELS_PER_STEP = 1 + 5 + 1 + 1 + 63
+# 1; balance 64 (hit test + Compton sums, shell integrals, state load, 20 rounds
+# x (rates, atoms, secant), store)
+KERNELS_PER_STEP = 1 + 5 + 1 + 1 + 64
 
 
 def parse():
@@ -488,16 +489,26 @@ def run_batch(args, dist, ws, rank, local):
     ms_e2e_step = max_over_ranks(dist, (time.perf_counter() - t0) * 1e3 / args.steps)
     h2d = sum(x.numel() * x.element_size() for x in (te, ne, ion))
 
-    # the same nebulae one context after another (the single-nebula path)
+    # the same nebulae, each in its own context (loaded beforehand), iterated one after another:
+    # the single-nebula path
     seq_ms = None
     if args.plain_steps > 0:
+        singles = []
+        for s in setups:
+            c1 = Context(local)
+            c1.load(s)
+            c1.state_save()
+            singles.append(c1)
+        for b, c1 in enumerate(singles):            # warm-up (graph capture of each balance)
+            c1.iterate(int(packets[b]), seed=int(seeds[b]))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for b, s in enumerate(setups):
-            with Context(local) as c1:
-                c1.load(s)
-                c1.iterate(int(packets[b]), seed=int(seeds[b]))
+        for b, c1 in enumerate(singles):
+            c1.state_restore()
+            c1.iterate(int(packets[b]), seed=int(seeds[b]) + 1)
         seq_ms = (time.perf_counter() - t0) * 1e3
+        for c1 in singles:
+            c1.close()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

@@ -325,7 +325,9 @@ typedef struct mcx_transport_opts {
     int32_t block_size;         /* 0 = library default                                 */
     int32_t grid_mult;          /* persistent blocks per SM; 0 = library default        */
     int32_t chunk;              /* packets handed out per queue grab; 0 = default       */
-    int32_t reserved[4];
+    int32_t emit_batch;         /* lanes of a warp that wait for an emission before the
+                                   warp runs the emission code; 0 = library default (12) */
+    int32_t reserved[3];
 } mcx_transport_opts;
 
 typedef struct mcx_transport_stats {
@@ -353,7 +355,7 @@ int  mcx_normalize_j(mcx_ctx* ctx);
 /* One pass of iterateMC's loop body (source/iteration_mod.f90:98-1260) for the
  * stellar source: mcx_opacity, mcx_emission, mcx_transport (Jste cleared
  * first), mcx_normalize_j and mcx_balance, in that order on the context's
- * stream.  The balance's ~63 launches are captured as a CUDA graph on first
+ * stream.  The balance's ~64 launches are captured as a CUDA graph on first
  * use and replayed.  The convergence test of :1270-1480 is left to the caller
  * (stats.balance.converged against nCells and minConvergence). */
 typedef struct mcx_iterate_opts {

@@ -90,7 +90,7 @@ class TransportOpts(C.Structure):
     _fields_ = [("istar", C.c_int32), ("precision", C.c_int32), ("n_packets", C.c_int64), ("seed", C.c_uint64),
                 ("counter_base", C.c_uint64), ("n_photons_norm", C.c_int64), ("zero_estimators", C.c_int32),
                 ("block_size", C.c_int32), ("grid_mult", C.c_int32), ("chunk", C.c_int32),
-                ("reserved", C.c_int32 * 4)]
+                ("emit_batch", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class TransportStats(C.Structure):

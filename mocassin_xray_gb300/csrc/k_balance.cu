@@ -16,8 +16,10 @@ cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStr
 cudaError_t launchForLines(BalanceData& bd, const float* te, const float* ne, const float* ionDen,
                            const uint8_t* compute, float* forLines, cudaStream_t s);
 cudaError_t launchForbSums(BalanceData& bd, const LineSumArgs& a, cudaStream_t s);
+cudaError_t prepare(const BalanceData& bd);
 }  // namespace bal_f64
 namespace bal_mixed {
+cudaError_t prepare(const BalanceData& bd);
 cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStream_t s);
 cudaError_t launchForLines(BalanceData& bd, const float* te, const float* ne, const float* ionDen,
                            const uint8_t* compute, float* forLines, cudaStream_t s);
@@ -164,6 +166,26 @@ std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out)
   d.diel = (const float*)up(t.diel.data(), t.diel.size() * sizeof(float));
   d.aldro = (const float*)up(t.aldro.data(), t.aldro.size() * sizeof(float));
   d.outer = (const int32_t*)up(t.outer, sizeof(t.outer));
+  {
+    // the rows diRec would end on (dielectronic, source/update_mod.f90:3204-3305)
+    std::vector<int16_t> rows((size_t)31 * 32 * 3, -1);
+    const int nd = (int)t.diel.size() / 8, na = (int)t.aldro.size() / 6;
+    for (int r = 0; r < nd; ++r) {
+      const float* q = t.diel.data() + (size_t)r * 8;
+      const int elem = (int)q[0], ion = (int)q[0] + 1 - (int)q[1], g = (int)q[7];
+      if (elem < 1 || elem > 30 || ion < 1 || ion > 31) continue;
+      int16_t* x = rows.data() + ((size_t)elem * 32 + ion) * 3;
+      if (g == 0 || g == 1) x[0] = (int16_t)r;
+      if (g == 0 || g == 2) x[1] = (int16_t)r;
+    }
+    for (int r = 0; r < na; ++r) {
+      const float* q = t.aldro.data() + (size_t)r * 6;
+      const int elem = (int)q[0], ion = (int)q[0] - (int)q[1] + 1;
+      if (elem < 1 || elem > 30 || ion < 1 || ion > 31) continue;
+      rows[((size_t)elem * 32 + ion) * 3 + 2] = (int16_t)r;
+    }
+    d.dielRow = (const int16_t*)up(rows.data(), rows.size() * sizeof(int16_t));
+  }
   std::vector<float4> chex(31 * 32, make_float4(0.f, 0.f, 0.f, 0.f));
   for (const auto& r : kChexRows)   // in order: later rows overwrite earlier ones
     chex[(int)r[0] * 32 + (int)r[1]] = make_float4(r[2], r[3], r[4], r[5]);
@@ -194,15 +216,10 @@ std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out)
   d.linePow = (const double*)up(pow_.data(), pow_.size() * sizeof(double));
   const size_t nPair = (size_t)E * ns;
   d.ion = carve<double>(blocks, nPair * C1, err);
-  d.alpha = carve<double>(blocks, nPair * C1, err);
-  d.coll1 = carve<double>(blocks, nPair * C1, err);
-  d.coll2 = carve<double>(blocks, nPair * C1, err);
   const size_t nSh = std::max<size_t>(sh.size(), 1);
   d.gam = carve<double>(blocks, nSh * C1, err);
   d.heatA = carve<double>(blocks, nSh * C1, err);
   d.heatHi = carve<double>(blocks, nSh * C1, err);
-  d.pi1 = carve<double>(blocks, nSh * C1, err);
-  d.pi2 = carve<double>(blocks, nSh * C1, err);
   d.comp = carve<double>(blocks, 4 * (size_t)C1, err);
   double** scal[] = {&d.te, &d.ne, &d.xOld, &d.tHigh, &d.tLow, &d.resHigh, &d.resLow, &d.heat, &d.coolA,
                      &d.coolHex, &d.coolCollH, &d.compHeat, &d.compRecoil, &d.compCool};
@@ -218,6 +235,21 @@ std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out)
   if (!err.empty()) return err;
   // no photon hit until the J pass says otherwise
   cudaMemset(d.state, 2, C1);
+  // the rates kernel's shared memory per cell: ionDen, alphaTot, coll1 per
+  // (element, stage), the shell rates, an ordered-sum scratch and the ladders
+  {
+    const int NP = d.nElemUsed * ns, nSh = d.nShellsTot;
+    int nHeavy = 0;
+    for (int e = 1; e <= d.nElemUsed; ++e) nHeavy += d.zOf[e] >= 3 ? 1 : 0;
+    d.warpDoubles = 3 * NP + nSh + std::max(NP, nSh) + std::max(nHeavy * 3 * (ns + 3), 4 * d.nElemUsed);
+    // zOf, xref, abun (3 x 32 words) and the (element, ion) shell offsets and counts (2 x E x 32 int16)
+    d.metaDoubles = (3 * 32 * 4 + 2 * d.nElemUsed * 32 * 2 + 7) / 8;
+    if (((size_t)d.metaDoubles + 4 * (size_t)d.warpDoubles) * sizeof(double) > 200 * 1024)
+      return "balance: too many ions for the rates kernel";
+    if (nHeavy > 32) return "balance: more than 32 heavy elements";
+    cudaError_t e1 = bal_f64::prepare(*bd), e2 = bal_mixed::prepare(*bd);
+    if (e1 != cudaSuccess || e2 != cudaSuccess) return "balance: cannot reserve the rates kernel's shared memory";
+  }
   out = std::move(bd);
   return "";
 }

@@ -45,6 +45,8 @@ struct BalanceCounters {
 struct BalanceDev {
   int32_t nbins, nCells, nstages, nElemUsed, nShellsTot, nAtoms, nDiel, nAldro;
   int32_t lgBadnell, lgCompton;
+  int32_t warpDoubles;         // shared memory of one cell of the rates kernel, in doubles
+  int32_t metaDoubles;         // its per-block element tables, in doubles
   int32_t secIonP, cRecoilHP, cRecoilHeP;
   float xhiLimit;
   int32_t xref[31];            // elementXref by Z (index 1..30), 0 = off
@@ -67,6 +69,7 @@ struct BalanceDev {
   const float* rnew;           // [30][30][4]
   const float* diel;           // [nDiel][8]
   const float* aldro;          // [nAldro][6]
+  const int16_t* dielRow;      // [31][32][3] by (Z, ion): last dielectronic row with flag 0|1, with 0|2; aldrovandi row
   const int32_t* outer;        // [30][30][3]
   const float4* chex;          // [31][32] charge-exchange a, b, c, d of (Z, ion), 0 where none
   const int32_t* atomHdr;      // [nAtoms][16]
@@ -75,14 +78,9 @@ struct BalanceDev {
   const double* linePow;       // [nAtoms][kMaxLevels+1] sum over lines from level j of a(j,i) E_ji > 0
   // per-cell work, [k][C+1] (cell fastest)
   double* ion;                 // [nstages][nElemUsed]
-  double* alpha;               // [nElemUsed][nstages]
-  double* coll1;               // [nElemUsed][nstages]
-  double* coll2;
-  double* gam;                 // [nShellsTot] photoionisation rate (J integral, + charge exchange)
+  double* gam;                 // [nShellsTot] photoionisation rate (J integral; the rates kernel adds the reverse charge exchange to its copy)
   double* heatA;               // [nShellsTot] heating without the secondary-ionisation tail
   double* heatHi;              // [nShellsTot] tail heating, times heatef
-  double* pi1;                 // [nShellsTot] photoIon(1, ...)
-  double* pi2;                 // [nShellsTot] photoIon(2, ...)
   double* comp;                // [4] s1, s2, recoil H, recoil He
   double* te, *ne, *xOld;
   double* tHigh, *tLow, *resHigh, *resLow;

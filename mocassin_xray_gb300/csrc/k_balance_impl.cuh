@@ -46,9 +46,6 @@ struct CellIdx {
 __device__ __forceinline__ double& ionAt(const BalanceDev& b, const CellIdx& c, int z, int st) {
   return b.ion[((size_t)(st - 1) * b.nElemUsed + (b.xref[z] - 1)) * c.C1 + c.cell];
 }
-__device__ __forceinline__ size_t pairOff(const BalanceDev& b, const CellIdx& c, int z, int ion) {
-  return ((size_t)(b.xref[z] - 1) * b.nstages + (ion - 1)) * c.C1 + c.cell;
-}
 
 // ------------------------------------------------------------- rate functions
 
@@ -91,63 +88,51 @@ __device__ real radRecFit(const BalanceDev& b, real te, int z, int n) {
 
 // diRec(elem, ion) of dielectronic: the last row of dielectronic.dat for
 // (elem, ion) whose temperature flag applies, or above 6e4 K the last row of
-// aldrovandi.dat (the whole diRec array is replaced there).
+// aldrovandi.dat (the whole diRec array is replaced there).  The row indices
+// are found at set-up (dielRow: last row with flag 0 or 1, with flag 0 or 2,
+// and the aldrovandi row; -1 none).
 __device__ real diRecOf(const BalanceDev& b, real te, int elem, int ion) {
-  if (ion > b.nstages) return 0;
+  if (ion > b.nstages || elem < 1 || elem > 30 || ion < 1 || ion > 31) return 0;
   const real one = (real)1.;
+  const int16_t* idx = b.dielRow + ((size_t)elem * 32 + ion) * 3;
   if (te > (real)60000.) {
-    real v = 0;
-    for (int r = 0; r < b.nAldro; ++r) {
-      const float* d = b.aldro + (size_t)r * 6;
-      if ((int)d[0] != elem || (int)d[0] - (int)d[1] + 1 != ion) continue;
-      real a = d[2], bb = d[3], t0 = d[4], t1 = d[5];
-      v = a * pow(te, (real)-1.5) * exp(-t0 / te) * (one + bb * exp(-t1 / te));
-    }
-    return v;
+    const int r = idx[2];
+    if (r < 0) return 0;
+    const float* d = b.aldro + (size_t)r * 6;
+    real a = d[2], bb = d[3], t0 = d[4], t1 = d[5];
+    return a * pow(te, (real)-1.5) * exp(-t0 / te) * (one + bb * exp(-t1 / te));
   }
   real t = te > (real)1000. ? te / (real)10000. : RF(0.1);
-  real v = 0;
-  for (int r = 0; r < b.nDiel; ++r) {
-    const float* d = b.diel + (size_t)r * 8;
-    if ((int)d[0] != elem || (int)d[0] + 1 - (int)d[1] != ion) continue;
-    int g = (int)d[7];
-    bool use = g == 0 || (g == 1 && te < (real)20000.) || (g == 2 && te >= (real)20000.);
-    if (!use) continue;
-    real a = d[2], bb = d[3], cc = d[4], dd = d[5], f = d[6];
-    v = RF(1e-12) * (a / t + bb + cc * t + dd * (t * t)) * pow(t, (real)-1.5) * exp(-f / t);
-  }
-  return v;
+  const int r = te < (real)20000. ? idx[0] : idx[1];
+  if (r < 0) return 0;
+  const float* d = b.diel + (size_t)r * 8;
+  real a = d[2], bb = d[3], cc = d[4], dd = d[5], f = d[6];
+  return RF(1e-12) * (a / t + bb + cc * t + dd * (t * t)) * pow(t, (real)-1.5) * exp(-f / t);
 }
 
-__device__ void calcAlpha(const BalanceDev& b, const CellIdx& c, real te) {
-  const int ns = b.nstages;
-  for (int e = 1; e <= b.nElemUsed; ++e) {
-    const int elem = b.zOf[e];
-    const int top = min(ns - 1, elem);
-    for (int ion = 1; ion <= top; ++ion) {
-      real a;
-      if (b.lgBadnell) {
-        int nel = elem - ion;
-        if (nel <= 11) {
-          a = rrBadnell(b, te, elem, nel);
-          a = a + drBadnell(b, te, elem, nel);
-        } else {
-          a = radRecFit(b, te, elem, elem - ion + 1);
-          real di = diRecOf(b, te, elem, ion);
-          if (di == (real)0. && ion < 7 && b.xref[8] > 0) di = diRecOf(b, te, 8, ion);
-          a = a + (di > (real)0. ? di : (real)0.);
-        }
-      } else {
-        a = radRecFit(b, te, elem, elem - ion + 1);
-        if (elem >= 3) {
-          real di = diRecOf(b, te, elem, ion);
-          if (di == (real)0. && ion < 7) di = diRecOf(b, te, 8, ion);
-          a = a + (di > (real)0. ? di : (real)0.);
-        }
-      }
-      b.alpha[pairOff(b, c, elem, ion)] = (double)a;
+// calcAlpha of one (element, ion) pair (source/update_mod.f90:2298-2413)
+__device__ real alphaOf(const BalanceDev& b, real te, int elem, int ion) {
+  real a;
+  if (b.lgBadnell) {
+    int nel = elem - ion;
+    if (nel <= 11) {
+      a = rrBadnell(b, te, elem, nel);
+      a = a + drBadnell(b, te, elem, nel);
+    } else {
+      a = radRecFit(b, te, elem, elem - ion + 1);
+      real di = diRecOf(b, te, elem, ion);
+      if (di == (real)0. && ion < 7 && b.xref[8] > 0) di = diRecOf(b, te, 8, ion);
+      a = a + (di > (real)0. ? di : (real)0.);
+    }
+  } else {
+    a = radRecFit(b, te, elem, elem - ion + 1);
+    if (elem >= 3) {
+      real di = diRecOf(b, te, elem, ion);
+      if (di == (real)0. && ion < 7) di = diRecOf(b, te, 8, ion);
+      a = a + (di > (real)0. ? di : (real)0.);
     }
   }
+  return a;
 }
 
 // chex(z, ion, 1) * 1e-9 without the temperature fit (ionBalance's heavy elements)
@@ -171,78 +156,22 @@ __device__ __forceinline__ const int32_t* outerOf(const BalanceDev& b, int z, in
 // ------------------------------------------------------ J-only integrals
 
 // The parts of photoionisation / getPhotoRates / compton that depend on J
-// alone; one thread per cell.
-__global__ void __launch_bounds__(128) photoIntegralsKernel(BalanceDev b, const double* __restrict__ jste) {
+// alone.  hitComptonKernel (one thread per cell) marks the cells no packet
+// reached and forms the Compton sums; shellIntegralsKernel (one thread per
+// (cell, photoionised shell), the shell on the grid's y axis) integrates J
+// over each shell's cross section, so that a warp streams one shell's bins of
+// 32 neighbouring cells' J rows.
+__global__ void __launch_bounds__(128) hitComptonKernel(BalanceDev b, const double* __restrict__ jste) {
   const int cell = blockIdx.x * blockDim.x + threadIdx.x + 1;
   if (cell > b.nCells) return;
   const int C1 = b.nCells + 1;
   const float* nu = b.nu;
-  const float* xs = b.xsec;
   auto J = [&](int bin1) { return (real)jste[(size_t)(bin1 - 1) * C1 + cell]; };
   bool hit = false;
   for (int i = 1; i <= b.nbins; ++i)
     if (jste[(size_t)(i - 1) * C1 + cell] > 0.) { hit = true; break; }
   b.state[cell] = hit ? 0 : 2;
   if (!hit) return;
-  const real hcRyd = kHcRyd();
-  for (int t = 0; t < b.nShellsTot; ++t) {
-    const PhotoShell sh = b.shells[t];
-    const size_t o = (size_t)t * C1 + cell;
-    if (sh.ipNuP < 1 || sh.ipNuP > b.nbins) {   // threshold outside the mesh
-      b.gam[o] = sh.heavy ? 0. : RD(1.e-20);
-      b.heatA[o] = 0.;
-      b.heatHi[o] = 0.;
-      continue;
-    }
-    if (!sh.heavy) {
-      real n1 = RF(1.e-20), h1 = 0;
-      const real nuIP = (real)nu[sh.ipNuP - 1];
-      for (int j = sh.ipNuP; j <= sh.highNuP; ++j) {
-        real ph = xs[j - sh.ipNuP + sh.xsecP - 1];
-        if (ph < RF(1.e-35)) ph = 0;
-        real jj = J(j);
-        if (jj > (real)0.) {
-          n1 = n1 + jj * ph / (hcRyd * (real)nu[j - 1]);
-          h1 = h1 + ph * jj * ((real)nu[j - 1] - nuIP) / (real)nu[j - 1];
-        }
-      }
-      b.gam[o] = n1;
-      b.heatA[o] = h1;
-      b.heatHi[o] = 0.;
-      continue;
-    }
-    const int nu1P = sh.ipNuP, IPnuP = sh.ipNuP;
-    const int iup = min(sh.highNuP, b.nbins);
-    const real augerE = hcRyd * (real)nu[nu1P - 1] * (real)sh.yield1;
-    real g = 0, h = 0;
-    const int top = min(iup, b.secIonP - 1);
-    for (int i = nu1P + 1; i <= top; ++i) {
-      real jj = J(i);
-      if (jj > (real)0.) {
-        real ph = xs[i + sh.xsecP - IPnuP - 1];
-        if (ph < RF(1.e-35)) ph = 0;
-        g = g + jj * ph / (hcRyd * (real)nu[i - 1]);
-        h = h + jj * ph;
-      }
-    }
-    h = h - g * augerE;
-    const real jIP = J(IPnuP);
-    const real ph0 = xs[sh.xsecP - 1];
-    g = g + jIP * ph0 / (hcRyd * (real)nu[IPnuP - 1]);
-    h = h + jIP * ph0 * (hcRyd * (real)nu[IPnuP - 1] - augerE) / (hcRyd * (real)nu[IPnuP - 1]);
-    real gh = 0, hh = 0;
-    const int ilow = max(IPnuP + 1, b.secIonP);
-    for (int i = ilow; i <= iup; ++i) {
-      real p = xs[i + sh.xsecP - IPnuP - 1];
-      gh = gh + jIP * p / (hcRyd * (real)nu[i - 1]);   // radField(IPnuP), as the reference
-      hh = hh + jIP * p;
-    }
-    g = g + gh;
-    hh = hh - gh * augerE;
-    b.gam[o] = g;
-    b.heatA[o] = h;
-    b.heatHi[o] = hh;
-  }
   if (b.lgCompton) {
     real s1 = 0, s2 = 0, rhH = 0, rhHe = 0;
     for (int i = 1; i <= b.nbins; ++i) {
@@ -265,6 +194,73 @@ __global__ void __launch_bounds__(128) photoIntegralsKernel(BalanceDev b, const 
   }
 }
 
+__global__ void __launch_bounds__(128) shellIntegralsKernel(BalanceDev b, const double* __restrict__ jste) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int t = blockIdx.y;
+  if (cell > b.nCells || b.state[cell] == 2) return;
+  const int C1 = b.nCells + 1;
+  const float* nu = b.nu;
+  const float* xs = b.xsec;
+  auto J = [&](int bin1) { return (real)jste[(size_t)(bin1 - 1) * C1 + cell]; };
+  const real hcRyd = kHcRyd();
+  const PhotoShell sh = b.shells[t];
+  const size_t o = (size_t)t * C1 + cell;
+  if (sh.ipNuP < 1 || sh.ipNuP > b.nbins) {   // threshold outside the mesh
+    b.gam[o] = sh.heavy ? 0. : RD(1.e-20);
+    b.heatA[o] = 0.;
+    b.heatHi[o] = 0.;
+    return;
+  }
+  if (!sh.heavy) {
+    real n1 = RF(1.e-20), h1 = 0;
+    const real nuIP = (real)nu[sh.ipNuP - 1];
+    for (int j = sh.ipNuP; j <= sh.highNuP; ++j) {
+      real ph = xs[j - sh.ipNuP + sh.xsecP - 1];
+      if (ph < RF(1.e-35)) ph = 0;
+      real jj = J(j);
+      if (jj > (real)0.) {
+        n1 = n1 + jj * ph / (hcRyd * (real)nu[j - 1]);
+        h1 = h1 + ph * jj * ((real)nu[j - 1] - nuIP) / (real)nu[j - 1];
+      }
+    }
+    b.gam[o] = n1;
+    b.heatA[o] = h1;
+    b.heatHi[o] = 0.;
+    return;
+  }
+  const int nu1P = sh.ipNuP, IPnuP = sh.ipNuP;
+  const int iup = min(sh.highNuP, b.nbins);
+  const real augerE = hcRyd * (real)nu[nu1P - 1] * (real)sh.yield1;
+  real g = 0, h = 0;
+  const int top = min(iup, b.secIonP - 1);
+  for (int i = nu1P + 1; i <= top; ++i) {
+    real jj = J(i);
+    if (jj > (real)0.) {
+      real ph = xs[i + sh.xsecP - IPnuP - 1];
+      if (ph < RF(1.e-35)) ph = 0;
+      g = g + jj * ph / (hcRyd * (real)nu[i - 1]);
+      h = h + jj * ph;
+    }
+  }
+  h = h - g * augerE;
+  const real jIP = J(IPnuP);
+  const real ph0 = xs[sh.xsecP - 1];
+  g = g + jIP * ph0 / (hcRyd * (real)nu[IPnuP - 1]);
+  h = h + jIP * ph0 * (hcRyd * (real)nu[IPnuP - 1] - augerE) / (hcRyd * (real)nu[IPnuP - 1]);
+  real gh = 0, hh = 0;
+  const int ilow = max(IPnuP + 1, b.secIonP);
+  for (int i = ilow; i <= iup; ++i) {
+    real p = xs[i + sh.xsecP - IPnuP - 1];
+    gh = gh + jIP * p / (hcRyd * (real)nu[i - 1]);   // radField(IPnuP), as the reference
+    hh = hh + jIP * p;
+  }
+  g = g + gh;
+  hh = hh - gh * augerE;
+  b.gam[o] = g;
+  b.heatA[o] = h;
+  b.heatHi[o] = hh;
+}
+
 // Loads the grid state of the cells into the FP64 work arrays.
 __global__ void loadStateKernel(BalanceDev b, const float* __restrict__ te, const float* __restrict__ ne,
                                 const float* __restrict__ ionDen) {
@@ -283,145 +279,222 @@ __global__ void loadStateKernel(BalanceDev b, const float* __restrict__ te, cons
 
 // -------------------------------------------------------------- one round
 
-// ionBalance (recursion as a loop); returns lgConv.  The ladder, its
-// normalisation and Ne are FP64 in both precisions.
-__device__ bool ionBalance(const BalanceDev& b, const CellIdx& c, double te, double& ne, double hden) {
-  const int ns = b.nstages;
+// One cell per warp.  The cell's ionic fractions, recombination and
+// collisional rates and photoionisation rates sit in the warp's slice of
+// shared memory for the whole T-iteration, so the ionisation-balance
+// X-iterations read nothing from global memory; the lanes share the per-ion
+// and per-shell work (calcAlpha, collisionalIonisation, the photoionisation
+// rates) and, inside each X-iteration, lane h runs the ionisation ladder of
+// the h-th heavy element.  Every sum keeps the reference's order (one lane
+// adds the terms in sequence), so the FP64 build matches the sequential code
+// operation for operation.
+// Per-element tables of the used elements, copied to shared memory once per
+// block: the lanes of a warp index them by different elements at once, which
+// the kernel-parameter (constant) bank would serialise.
+struct ElemMeta {
+  const int32_t* zOf;     // [32] Z of used element e
+  const int32_t* xref;    // [32] e of Z (0 = off)
+  const float* abun;      // [32] elemAbun by Z
+  const int16_t* p0;      // [E][32] first photoionised shell of (e, ion)
+  const int16_t* nsh;     // [E][32] its number of shells
+};
+
+// In the rate precision: FP64 in the plain build; FP32 in the mixed build,
+// whose X-iterations then run without an FP64 instruction (GB300 issues FP64
+// at 1/64 of the FP32 rate, and the loop is a long dependent chain).
+struct WarpCell {
+  real* X;       // [S][E] ionic fractions at (st-1)*E + (e-1), the global ionDen order
+  real* AL;      // [E][S] alphaTotal at (e-1)*S + (ion-1)
+  real* CC;      // [E][S] collisional ionisation rate coefficient (coll1)
+  real* PI;      // [nShellsTot] photoIon(1): rate per shell, with the reverse charge exchange
+  real* T;       // scratch for ordered sums
+  real* LAD;     // [nHeavy][3][S+3] out, inn, mat of the ladders; later the thermBalance terms [4][E]
+};
+
+__device__ __forceinline__ real& xAt(const BalanceDev& b, const ElemMeta& m, const WarpCell& w, int z, int st) {
+  return w.X[(st - 1) * b.nElemUsed + (m.xref[z] - 1)];
+}
+
+// ionBalance (source/update_mod.f90:1575-1992; the recursion as a loop) for
+// the warp's cell; returns lgConv (uniform across the warp).  In the mixed
+// build the ladder runs on the logarithms of its products (FP32 cannot hold
+// the products themselves).
+__device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const WarpCell& w, int lane, double te, double& ne, double hden) {
+  const int ns = b.nstages, E = b.nElemUsed;
   const int zH = 1, zHe = 2;
-  const bool heOn = b.xref[zHe] > 0;
-  const int C1 = c.C1;
+  const bool heOn = m.xref[zHe] > 0;
   const real teR = (real)te;
   // the Te-only terms are the same on every X-iteration (the reference
   // recomputes them on each recursive call)
   real expFact = RF(157893.94) / teR;
   if (expFact > (real)75.) expFact = (real)75.;
   const real collIonH0 = RF(2.75E-16) * teR * sqrt(teR) * (RF(157893.94) / teR + (real)2.) * exp(-expFact);
-  double cxHHe[3][3] = {{0., 0., 0.}, {0., 0., 0.}, {0., 0., 0.}};
-  for (int elem = 1; elem <= 2; ++elem)
-    for (int ion = 1; ion <= min(elem, ns - 1); ++ion) cxHHe[elem][ion] = chexFit(b, elem, ion, teR);
+  const real hdenR = (real)hden;
+  real neR = (real)ne;
+  real cxHHe[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  if (lane == 0)
+    for (int elem = 1; elem <= 2; ++elem)
+      for (int ion = 1; ion <= min(elem, ns - 1); ++ion) cxHHe[elem][ion] = chexFit(b, elem, ion, teR);
+  // this lane's heavy element (the lane-th element with Z >= 3, in element order)
+  int myE = 0;
+  for (int e = 1, h = 0; e <= E; ++e)
+    if (m.zOf[e] >= 3) {
+      if (h == lane) myE = e;
+      ++h;
+    }
   for (int nIterateX = 1;; ++nIterateX) {
     bool lgConv = true;
-    double ionRatio[3][3] = {{0., 0., 0.}, {0., 0., 0.}, {0., 0., 0.}};
-    double ionProd[3][3] = {{1., 1., 1.}, {1., 1., 1.}, {1., 1., 1.}};
-    double den[3] = {1., 1., 1.};
-    real collIonH = collIonH0;
-    const double HIOld = ionAt(b, c, zH, 1);
-    const double HeIOld = heOn ? ionAt(b, c, zHe, 1) : 0.;
-    const double HeIIOld = heOn ? ionAt(b, c, zHe, 2) : 0.;
-    for (int elem = 1; elem <= 2; ++elem) {
-      if (!b.xref[elem]) continue;
-      for (int ion = 1; ion <= min(elem, ns - 1); ++ion) {
-        double cx = cxHHe[elem][ion];
-        int outShell = outerOf(b, elem, elem - ion + 1)[0];
-        if (elem > 1 || ion > 1) collIonH = 0;
-        int p0 = b.pairShell0[(b.xref[elem] - 1) * 32 + (ion - 1)];
-        double pi = b.pi1[(size_t)(p0 + outShell - 1) * C1 + c.cell];
-        const double num = pi + (double)collIonH * ne + 0.;
-        const double dnm = ne * b.alpha[pairOff(b, c, elem, ion)] + cx * hden * HIOld;
-#if MCX_BAL_EXACT
-        ionRatio[elem][ion] = num / dnm;
-#else
-        ionRatio[elem][ion] = (double)((float)num / (float)dnm);   // a rate ratio: FP32
-#endif
+    const real HIOld = xAt(b, m, w, zH, 1);
+    const real HeIOld = heOn ? xAt(b, m, w, zHe, 1) : (real)0.;
+    const real HeIIOld = heOn ? xAt(b, m, w, zHe, 2) : (real)0.;
+    __syncwarp();
+    if (lane == 0) {
+      real ionRatio[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+      real ionProd[3][3] = {{1, 1, 1}, {1, 1, 1}, {1, 1, 1}};
+      real den[3] = {1, 1, 1};
+      real collIonH = collIonH0;
+      for (int elem = 1; elem <= 2; ++elem) {
+        if (!m.xref[elem]) continue;
+        for (int ion = 1; ion <= min(elem, ns - 1); ++ion) {
+          real cx = cxHHe[elem][ion];
+          int outShell = outerOf(b, elem, elem - ion + 1)[0];
+          if (elem > 1 || ion > 1) collIonH = 0;
+          int p0 = m.p0[(m.xref[elem] - 1) * 32 + (ion - 1)];
+          real pi = w.PI[p0 + outShell - 1];
+          const real num = pi + collIonH * neR + (real)0.;
+          const real dnm = neR * w.AL[(m.xref[elem] - 1) * ns + (ion - 1)] + cx * hdenR * HIOld;
+          ionRatio[elem][ion] = num / dnm;
+        }
+      }
+      for (int elem = 1; elem <= 2; ++elem) {
+        if (!m.xref[elem]) continue;
+        for (int ion = 1; ion <= min(elem, ns - 1); ++ion)
+          for (int i = 1; i <= ion; ++i) ionProd[elem][ion] = ionProd[elem][ion] * ionRatio[elem][i];
+      }
+      for (int elem = 1; elem <= 2; ++elem) {
+        if (!m.xref[elem]) continue;
+        for (int ion = 1; ion <= min(elem, ns - 1); ++ion) den[elem] = den[elem] + ionProd[elem][ion];
+      }
+      for (int elem = 1; elem <= 2; ++elem) {
+        if (!m.xref[elem]) continue;
+        for (int ion = 1; ion <= min(elem + 1, ns); ++ion) {
+          real v = ion == 1 ? (real)1. / den[elem] : ionProd[elem][ion - 1] / den[elem];
+          if (v > (real)kXMax()) v = (real)kXMax();
+          if (v < (real)RD(1.e-20)) v = (real)RD(1.e-20);
+          xAt(b, m, w, elem, ion) = v;
+        }
       }
     }
-    for (int elem = 1; elem <= 2; ++elem) {
-      if (!b.xref[elem]) continue;
-      for (int ion = 1; ion <= min(elem, ns - 1); ++ion)
-        for (int i = 1; i <= ion; ++i) ionProd[elem][ion] = ionProd[elem][ion] * ionRatio[elem][i];
-    }
-    for (int elem = 1; elem <= 2; ++elem) {
-      if (!b.xref[elem]) continue;
-      for (int ion = 1; ion <= min(elem, ns - 1); ++ion) den[elem] = den[elem] + ionProd[elem][ion];
-    }
-    for (int elem = 1; elem <= 2; ++elem) {
-      if (!b.xref[elem]) continue;
-      for (int ion = 1; ion <= min(elem + 1, ns); ++ion) {
-        double v = ion == 1 ? 1. / den[elem] : ionProd[elem][ion - 1] / den[elem];
-        if (v > kXMax()) v = kXMax();
-        if (v < RD(1.e-20)) v = RD(1.e-20);
-        ionAt(b, c, elem, ion) = v;
-      }
-    }
+    __syncwarp();
     // X(H0) as just updated above (grid%ionDen in the reference)
-    const double xH0now = ionAt(b, c, zH, 1);
-    for (int e = 1; e <= b.nElemUsed; ++e) {
-      const int elem = b.zOf[e];
-      if (elem < 3) continue;
-      double out[33], inn[33], mat[33];
-      for (int k = 0; k < 33; ++k) { out[k] = 0.; inn[k] = 0.; }
+    const real xH0now = xAt(b, m, w, zH, 1);
+    if (myE > 0) {
+      const int e = myE;
+      const int elem = m.zOf[e];
+      int h = 0;
+      for (int f = 1; f < e; ++f) h += m.zOf[f] >= 3 ? 1 : 0;
+      typedef real lad;
+      lad* out = w.LAD + (size_t)h * 3 * (ns + 3);
+      lad* inn = out + (ns + 3);
+      real* mat = inn + (ns + 3);
+      for (int k = 0; k < ns + 3; ++k) { out[k] = 0; inn[k] = 0; }
       const int topI = min(elem, ns - 1);
       const int lim = min(ns - 1, elem);
       for (int ion = 1; ion <= topI; ++ion) {
-        out[ion] = out[ion] + b.coll1[pairOff(b, c, elem, ion)] * ne;
-        const int p0 = b.pairShell0[(e - 1) * 32 + (ion - 1)];
-        const int nsh = b.pairNShell[(e - 1) * 32 + (ion - 1)];
+        out[ion] = out[ion] + w.CC[(e - 1) * ns + (ion - 1)] * neR;
+        const int p0 = m.p0[(e - 1) * 32 + (ion - 1)];
+        const int nsh = m.nsh[(e - 1) * 32 + (ion - 1)];
         for (int shell = 1; shell <= nsh; ++shell) {
-          const double pi = b.pi1[(size_t)(p0 + shell - 1) * C1 + c.cell];
+          const lad pi = w.PI[p0 + shell - 1];
           out[ion] = out[ion] + pi;
           const int nAug = b.nauger[((size_t)(elem - 1) * kNE + (ion - 1)) * 10 + (shell - 1)];
           for (int nelec = 2; nelec <= nAug; ++nelec) {
             int maxim = min(ion + nelec - 1, lim);
-            double xm = ionAt(b, c, elem, maxim);
-#if MCX_BAL_EXACT
-            double ratio = xm > 1e-30 ? ionAt(b, c, elem, ion) / xm : 1.;
-#else
-            double ratio = xm > 1e-30 ? (double)((float)ionAt(b, c, elem, ion) / (float)xm) : 1.;
-#endif
+            real xm = xAt(b, m, w, elem, maxim);
+            real ratio = xm > (real)1e-30 ? xAt(b, m, w, elem, ion) / xm : (real)1.;
             out[maxim] = out[maxim] +
-                         pi * (double)b.auger[(((size_t)(elem - 1) * kNE + (ion - 1)) * 10 + (shell - 1)) * 10 + (nelec - 1)] * ratio;
+                         pi * (lad)b.auger[(((size_t)(elem - 1) * kNE + (ion - 1)) * 10 + (shell - 1)) * 10 + (nelec - 1)] * ratio;
           }
         }
       }
       for (int ion = 1; ion <= topI; ++ion)
-        inn[ion] = ne * b.alpha[pairOff(b, c, elem, ion)] + (double)chexRaw(b, elem, ion) * hden * xH0now;
+        inn[ion] = neR * w.AL[(e - 1) * ns + (ion - 1)] + chexRaw(b, elem, ion) * hdenR * xH0now;
+      const int top = min(ns, elem + 1);
+#if MCX_BAL_EXACT
       mat[1] = 1.;
       double sumMat = 1.;
-      const int top = min(ns, elem + 1);
       for (int ion = 2; ion <= top; ++ion) {
-#if MCX_BAL_EXACT
         mat[ion] = mat[ion - 1] * out[ion - 1] / inn[ion - 1];
-#else
-        // the rate ratio in FP32, the ladder product and its normalisation in FP64
-        mat[ion] = mat[ion - 1] * (double)((float)out[ion - 1] / (float)inn[ion - 1]);
-#endif
         sumMat = sumMat + mat[ion];
       }
       sumMat = 1. / sumMat;
-      ionAt(b, c, elem, top) = mat[top] * sumMat;
+      xAt(b, m, w, elem, top) = mat[top] * sumMat;
       for (int ion = 1; ion <= topI; ++ion) {
         double v;
         if (nIterateX < 2 && mat[ion] * sumMat > 0.) {
-          double old = ionAt(b, c, elem, ion);
+          double old = xAt(b, m, w, elem, ion);
           if (old <= 0.) old = RD(1.e-5);
-#if MCX_BAL_EXACT
           v = pow(10., 0.5 * (log10(old) + log10(mat[ion] * sumMat)));
-#else
-          v = sqrt(old * (mat[ion] * sumMat));   // the same geometric mean
-#endif
         } else {
           v = mat[ion] * sumMat;
         }
         if (v > kXMax()) v = kXMax();
         if (v < RD(1.e-20)) v = RD(1.e-20);
-        ionAt(b, c, elem, ion) = v;
+        xAt(b, m, w, elem, ion) = v;
       }
-    }
-    double nE = 0.;
-    for (int e = 1; e <= b.nElemUsed; ++e) {
-      const int elem = b.zOf[e];
-      for (int ion = 2; ion <= min(elem + 1, ns); ++ion) {
-        double x = ionAt(b, c, elem, ion);
-        if (x >= RD(1.e-10)) nE = nE + (double)(ion - 1) * (double)b.abun[elem] * x;
+#else
+      // the same ladder in FP32 on log2 of the products (the products span far
+      // more than FP32's range; their logarithms do not), normalised against
+      // the largest term; the first X-iteration's geometric mean is the mean
+      // of the logarithms
+      float* lm = mat;
+      lm[1] = 0.f;
+      float lmax = 0.f;
+      for (int ion = 2; ion <= top; ++ion) {
+        lm[ion] = lm[ion - 1] + log2f((float)out[ion - 1] / (float)inn[ion - 1]);
+        lmax = fmaxf(lmax, lm[ion]);
       }
+      float sum = 0.f;
+      for (int ion = 1; ion <= top; ++ion) sum += exp2f(lm[ion] - lmax);
+      const float lsum = lmax + log2f(sum);
+      xAt(b, m, w, elem, top) = exp2f(lm[top] - lsum);
+      for (int ion = 1; ion <= topI; ++ion) {
+        const float lx = lm[ion] - lsum;
+        float v;
+        if (nIterateX < 2 && lx > -1.e30f) {
+          float old = xAt(b, m, w, elem, ion);
+          if (old <= 0.f) old = 1.e-5f;
+          v = exp2f(0.5f * (log2f(old) + lx));
+        } else {
+          v = exp2f(lx);
+        }
+        if (v > 0.99999f) v = 0.99999f;
+        if (v < 1.e-20f) v = 1.e-20f;
+        xAt(b, m, w, elem, ion) = v;
+      }
+#endif
     }
-    nE = nE * hden;
-    if (nE == 0.) nE = 1.;
-    ne = nE;
-    double dHI = (ionAt(b, c, zH, 1) - HIOld) / HIOld;
-    double dHeI = heOn ? (ionAt(b, c, zHe, 1) - HeIOld) / HeIOld : 0.;
-    double dHeII = heOn ? (ionAt(b, c, zHe, 2) - HeIIOld) / HeIIOld : 0.;
-    bool big = fabs(dHI) > RD(0.01) || fabs(dHeI) > RD(0.01) || fabs(dHeII) > RD(0.01);
+    __syncwarp();
+    // Ne in the reference's order, by lane 0
+    real nE = 0;
+    if (lane == 0) {
+      for (int e = 1; e <= E; ++e) {
+        const int elem = m.zOf[e];
+        for (int ion = 2; ion <= min(elem + 1, ns); ++ion) {
+          real x = xAt(b, m, w, elem, ion);
+          if (x >= (real)RD(1.e-10)) nE = nE + (real)(ion - 1) * (real)m.abun[elem] * x;
+        }
+      }
+      nE = nE * hdenR;
+      if (nE == (real)0.) nE = 1;
+    }
+    neR = __shfl_sync(0xffffffffu, nE, 0);
+    ne = (double)neR;
+    real dHI = (xAt(b, m, w, zH, 1) - HIOld) / HIOld;
+    real dHeI = heOn ? (xAt(b, m, w, zHe, 1) - HeIOld) / HeIOld : (real)0.;
+    real dHeII = heOn ? (xAt(b, m, w, zHe, 2) - HeIIOld) / HeIIOld : (real)0.;
+    const real lim = (real)RD(0.01);
+    bool big = fabs(dHI) > lim || fabs(dHeI) > lim || fabs(dHeII) > lim;
     if (big && nIterateX < 15) continue;
     if (big && nIterateX == 15) lgConv = false;
     return lgConv;
@@ -429,24 +502,58 @@ __device__ bool ionBalance(const BalanceDev& b, const CellIdx& c, double te, dou
 }
 
 // calcAlpha, photoionisation, collisionalIonisation, compton, ionBalance and
-// the thermBalance terms without forLines; one thread per iterating cell.
+// the thermBalance terms without forLines, one warp per iterating cell
+// (b.warpDoubles doubles of shared memory per warp).
 __global__ void __launch_bounds__(128) ratesKernel(BalanceDev b, const float* __restrict__ hdenG) {
-  const int cell = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  if (cell > b.nCells || b.state[cell] != 0) return;
-  const CellIdx c{cell, b.nCells + 1};
-  const int C1 = c.C1, ns = b.nstages;
-  b.nIterT[cell] = b.nIterT[cell] + 1;
+  extern __shared__ double wsm[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int cell = blockIdx.x * (blockDim.x >> 5) + wib + 1;
+  const int C1 = b.nCells + 1, ns = b.nstages, E = b.nElemUsed, NP = E * ns, nSh = b.nShellsTot;
+  // the element tables, then one slice per warp
+  int32_t* sZ = reinterpret_cast<int32_t*>(wsm);
+  int32_t* sX = sZ + 32;
+  float* sA = reinterpret_cast<float*>(sX + 32);
+  int16_t* sP0 = reinterpret_cast<int16_t*>(sA + 32);
+  int16_t* sNs = sP0 + E * 32;
+  for (int i = threadIdx.x; i < 32; i += blockDim.x) {
+    sZ[i] = i <= 30 ? b.zOf[i] : 0;
+    sX[i] = i <= 30 ? b.xref[i] : 0;
+    sA[i] = i <= 30 ? b.abun[i] : 0.f;
+  }
+  for (int i = threadIdx.x; i < E * 32; i += blockDim.x) {
+    sP0[i] = (int16_t)b.pairShell0[i];
+    sNs[i] = (int16_t)b.pairNShell[i];
+  }
+  __syncthreads();
+  if (cell > b.nCells || b.state[cell] != 0) return;   // the whole warp
+  const ElemMeta m{sZ, sX, sA, sP0, sNs};
+  WarpCell w;
+  w.X = reinterpret_cast<real*>(wsm + b.metaDoubles + (size_t)wib * b.warpDoubles);
+  w.AL = w.X + NP;
+  w.CC = w.AL + NP;
+  w.PI = w.CC + NP;
+  w.T = w.PI + nSh;
+  w.LAD = w.T + max(NP, nSh);
+  for (int k = lane; k < NP; k += 32) w.X[k] = (real)b.ion[(size_t)k * C1 + cell];
+  if (lane == 0) b.nIterT[cell] = b.nIterT[cell] + 1;
   const double te = b.te[cell];
   const real teR = (real)te;
   double ne = b.ne[cell];
   const double hden = hdenG[cell];
   const real hdenR = (real)hden;
-  calcAlpha(b, c, teR);
-  // photoionisation
+  // calcAlpha, one pair per lane
+  for (int k = lane; k < NP; k += 32) {
+    const int e = k / ns + 1, ion = k % ns + 1;
+    const int elem = m.zOf[e];
+    w.AL[k] = ion <= min(ns - 1, elem) ? alphaOf(b, teR, elem, ion) : (real)0.;
+  }
+  // photoionisation rates per shell
+  for (int t = lane; t < nSh; t += 32) w.PI[t] = (real)b.gam[(size_t)t * C1 + cell];
+  __syncwarp();
   real xe = 0;
-  for (int e = 1; e <= b.nElemUsed; ++e) {
-    const int elem = b.zOf[e];
-    xe = xe + (real)ionAt(b, c, elem, 1) * (real)b.abun[elem] * hdenR;
+  for (int e = 1; e <= E; ++e) {
+    const int elem = m.zOf[e];
+    xe = xe + (real)xAt(b, m, w, elem, 1) * (real)m.abun[elem] * hdenR;
   }
   xe = (real)ne / xe;
   real heatef;
@@ -455,115 +562,155 @@ __global__ void __launch_bounds__(128) ratesKernel(BalanceDev b, const float* __
     if (xe < RF(1.e-4)) xe = RF(1.e-4);
     heatef = RF(0.9971) * ((real)1. - pow((real)1. - pow(xe, RF(0.2663)), RF(1.3163)));
   }
-  for (int t = 0; t < b.nShellsTot; ++t) {
-    const size_t o = (size_t)t * C1 + cell;
-    b.pi1[o] = b.gam[o];
-    b.pi2[o] = b.shells[t].heavy ? (double)((real)b.heatA[o] + (real)b.heatHi[o] * heatef) : b.heatA[o];
-  }
   // reverse charge exchange: deltaE_k > 1 only for N0 and O0
-  for (int k = 0; k < 2; ++k) {
-    const int elem = k == 0 ? 7 : 8;
-    const real dE = k == 0 ? RF(10863.) : RF(2205.);
-    if (!b.xref[elem] || ns - 1 < 1) continue;
-    const int32_t* o = outerOf(b, elem, elem);
-    const int nsh = b.pairNShell[(b.xref[elem] - 1) * 32];
-    if (o[0] > nsh) continue;
-    real cx = chexFit(b, elem, 1, teR);
-    real rev = cx * ((real)1. - (real)ionAt(b, c, 1, 1)) * hdenR * (real)2. * exp(-dE / teR) / ((real)o[1] / (real)o[2]);
-    const size_t off = (size_t)(b.pairShell0[(b.xref[elem] - 1) * 32] + o[0] - 1) * C1 + cell;
-    b.pi1[off] = b.pi1[off] + (double)rev;
-  }
-  // collisionalIonisation (returns at the first u > 80)
-  {
-    for (int e = 1; e <= b.nElemUsed; ++e)
-      for (int ion = 1; ion <= ns; ++ion) {
-        size_t o = ((size_t)(e - 1) * ns + (ion - 1)) * C1 + cell;
-        b.coll1[o] = 0.;
-        b.coll2[o] = 0.;
-      }
-    const real tev = teR * RF(8.617385e-05);
-    bool stop = false;
-    for (int e = 1; e <= b.nElemUsed && !stop; ++e) {
-      const int elem = b.zOf[e];
-      for (int ion = 1; ion <= min(ns - 1, elem - 1); ++ion) {
-        const int elec = elem - ion + 1;
-        const float* cf = b.CF + ((size_t)(elem - 1) * kNE + (elec - 1)) * 5;
-        real u = (real)cf[0] / tev;
-        if (u > (real)80.) { stop = true; break; }
-        real c1 = (real)cf[2] * ((real)1. + (real)cf[1] * sqrt(u)) / ((real)cf[3] + u) * pow(u, (real)cf[4]) * exp(-u);
-        b.coll1[pairOff(b, c, elem, ion)] = c1;
-        b.coll2[pairOff(b, c, elem, ion)] = (real)b.cionTherm[(elem - 1) * kNE + (ion - 1)] * c1 * kBoltz();
-      }
+  if (lane == 0)
+    for (int k = 0; k < 2; ++k) {
+      const int elem = k == 0 ? 7 : 8;
+      const real dE = k == 0 ? RF(10863.) : RF(2205.);
+      if (!m.xref[elem] || ns - 1 < 1) continue;
+      const int32_t* o = outerOf(b, elem, elem);
+      const int nsh = m.nsh[(m.xref[elem] - 1) * 32];
+      if (o[0] > nsh) continue;
+      real cx = chexFit(b, elem, 1, teR);
+      real rev = cx * ((real)1. - (real)xAt(b, m, w, 1, 1)) * hdenR * (real)2. * exp(-dE / teR) / ((real)o[1] / (real)o[2]);
+      const int off = m.p0[(m.xref[elem] - 1) * 32] + o[0] - 1;
+      w.PI[off] = w.PI[off] + rev;
     }
+  // collisionalIonisation: the reference returns from the whole routine at the
+  // first pair (element outer, ion inner) with u > 80, so that pair and every
+  // later one keep 0
+  {
+    const real tev = teR * RF(8.617385e-05);
+    int firstStop = NP;
+    for (int k = lane; k < NP; k += 32) {
+      const int e = k / ns + 1, ion = k % ns + 1;
+      const int elem = m.zOf[e];
+      w.CC[k] = 0;
+      if (ion > min(ns - 1, elem - 1)) continue;
+      const int elec = elem - ion + 1;
+      const float* cf = b.CF + ((size_t)(elem - 1) * kNE + (elec - 1)) * 5;
+      real u = (real)cf[0] / tev;
+      if (u > (real)80.) { firstStop = min(firstStop, k); continue; }
+      w.CC[k] = (real)cf[2] * ((real)1. + (real)cf[1] * sqrt(u)) / ((real)cf[3] + u) * pow(u, (real)cf[4]) * exp(-u);
+    }
+    for (int o = 16; o > 0; o >>= 1) firstStop = min(firstStop, __shfl_xor_sync(0xffffffffu, firstStop, o));
+    for (int k = lane; k < NP; k += 32)
+      if (k >= firstStop) w.CC[k] = 0;
   }
+  __syncwarp();
   // compton, with the state before ionBalance
-  if (b.lgCompton) {
+  if (b.lgCompton && lane == 0) {
     const real s1 = (real)b.comp[0 * (size_t)C1 + cell], s2 = (real)b.comp[1 * (size_t)C1 + cell];
     const real rhH = (real)b.comp[2 * (size_t)C1 + cell], rhHe = (real)b.comp[3 * (size_t)C1 + cell];
     real cool = (RF(6.65e-25) * RF(6.75e-10) * teR * s2) / hdenR;
     real heat = (RF(6.65e-25) * s1 / RF(8.184e-7)) / hdenR;
-    real he = b.xref[2] ? rhHe * ((real)ionAt(b, c, 2, 1) * (real)b.abun[2]) * (real)2. : (real)0.;
-    real recoil = (rhH * (real)ionAt(b, c, 1, 1) * (real)b.abun[1] + he) * kRyd2erg();
+    real he = m.xref[2] ? rhHe * ((real)xAt(b, m, w, 2, 1) * (real)m.abun[2]) * (real)2. : (real)0.;
+    real recoil = (rhH * (real)xAt(b, m, w, 1, 1) * (real)m.abun[1] + he) * kRyd2erg();
     b.compCool[cell] = cool;
     b.compHeat[cell] = heat;
     b.compRecoil[cell] = recoil;
   }
-  bool conv = ionBalance(b, c, te, ne, hden);
+  const bool conv = ionBalanceWarp(b, m, w, lane, te, ne, hden);
+  __syncwarp();
+  for (int k = lane; k < NP; k += 32) b.ion[(size_t)k * C1 + cell] = (double)w.X[k];
+  // photoIon(2) of every shell for the heating sum (secondary-ionisation tail times heatef)
+  for (int t = lane; t < nSh; t += 32) {
+    const size_t o = (size_t)t * C1 + cell;
+    w.T[t] = b.shells[t].heavy ? (real)b.heatA[o] + (real)b.heatHi[o] * heatef : (real)b.heatA[o];
+  }
+  __syncwarp();
+  // thermBalance without forLines: the terms by lane, their sums in the
+  // reference's order by lane 0
+  const real neR = (real)ne;
+  real* termFF = w.LAD;              // [E] free-free, then recombination, of H-like ions
+  real* termRec = w.LAD + E;
+  real* termFF2 = w.LAD + 2 * E;     // the same of He-like ions
+  real* termRec2 = w.LAD + 3 * E;
+  if (lane < E) {
+    const int e = lane + 1;
+    const int i = m.zOf[e];
+    termFF[lane] = termRec[lane] = termFF2[lane] = termRec2[lane] = 0;
+    if (ns > i) {
+      real L = log10(teR / (real)(i * i));
+      real Np = (real)xAt(b, m, w, i, i + 1) * (real)m.abun[i];
+      real betaFF = (real)i * (RF(1.0108464E-11) + RF(9.7930778E-13) * L - RF(6.6433144E-13) * L * L +
+                               RF(2.4793747E-13) * L * L * L - RF(2.3938215E-14) * L * L * L * L);
+      termFF[lane] = Np * neR * betaFF * kBoltz() * teR / sqrt(teR);
+      real betaRec = (real)i * (RF(9.4255985E-11) - RF(4.04794384E-12) * L - RF(1.0055237E-11) * L * L +
+                                RF(1.99266862E-12) * L * L * L - RF(1.06681387E-13) * L * L * L * L);
+      termRec[lane] = Np * neR * betaRec * kBoltz() * teR / sqrt(teR);
+      if (i >= 2) {
+        L = log10((real)4. * teR / (real)(i * i));
+        Np = (real)xAt(b, m, w, i, i) * (real)m.abun[i];
+        betaFF = ((real)i / (real)2.) * (RF(1.070073e-11) - RF(2.5730207e-13) * L + RF(2.109134e-13) * L * L);
+        termFF2[lane] = Np * neR * betaFF * kBoltz() * teR / sqrt(teR);
+        betaRec = ((real)i / (real)2.) * (RF(1.06926e-10) - RF(2.41756e-11) * L + RF(1.14542e-12) * L * L -
+                                          RF(5.06535e-13) * L * L * L + RF(9.16745e-14) * L * L * L * L);
+        termRec2[lane] = Np * neR * betaRec * kBoltz() * teR / sqrt(teR);
+      }
+    }
+  }
+  // collisional ionisation cooling per pair into w.AL (alpha is not needed any more)
+  for (int k = lane; k < NP; k += 32) {
+    const int e = k / ns + 1, ion = k % ns + 1;
+    const int elem = m.zOf[e];
+    real v = 0;
+    if (ion <= min(elem, ns - 1)) {
+      const real c2 = (real)b.cionTherm[(elem - 1) * kNE + (ion - 1)] * w.CC[k] * kBoltz();
+      v = (real)m.abun[elem] * xAt(b, m, w, elem, ion) * c2 * neR;
+    }
+    w.AL[k] = v;
+  }
+  // photoheating per shell into w.T (the photoIon(2) values staged above)
+  for (int t = lane; t < nSh; t += 32) {
+    const PhotoShell sh = b.shells[t];
+    w.T[t] = w.T[t] * xAt(b, m, w, sh.elem, sh.ion) * (real)m.abun[sh.elem];
+  }
+  __syncwarp();
+  if (lane != 0) return;
   b.ibConv[cell] = conv ? 1 : 0;
   b.ne[cell] = ne;
-  // thermBalance without forLines
-  const real neR = (real)ne;
-  real coolFF = 0, coolRec = 0, L, Te4;
-  for (int e = 1; e <= b.nElemUsed; ++e) {
-    const int i = b.zOf[e];
-    if (!(ns > i)) continue;
-    L = log10(teR / (real)(i * i));
-    Te4 = teR / ((real)(i * i) * RF(1.e4));
-    real Np = (real)ionAt(b, c, i, i + 1) * (real)b.abun[i];
-    real betaFF = (real)i * (RF(1.0108464E-11) + RF(9.7930778E-13) * L - RF(6.6433144E-13) * L * L +
-                             RF(2.4793747E-13) * L * L * L - RF(2.3938215E-14) * L * L * L * L);
-    real t = Np * neR * betaFF * kBoltz() * teR / sqrt(teR);
+  real coolFF = 0, coolRec = 0;
+  for (int e = 1; e <= E; ++e) {
+    if (!(ns > m.zOf[e])) continue;
+    real t = (real)termFF[e - 1];
     if (!isnan(t)) coolFF = coolFF + t;
-    real betaRec = (real)i * (RF(9.4255985E-11) - RF(4.04794384E-12) * L - RF(1.0055237E-11) * L * L +
-                              RF(1.99266862E-12) * L * L * L - RF(1.06681387E-13) * L * L * L * L);
-    t = Np * neR * betaRec * kBoltz() * teR / sqrt(teR);
+    t = (real)termRec[e - 1];
     if (!isnan(t)) coolRec = coolRec + t;
   }
-  Te4 = teR / RF(1.e4);
-  for (int e = 1; e <= b.nElemUsed; ++e) {
-    const int i = b.zOf[e];
+  for (int e = 1; e <= E; ++e) {
+    const int i = m.zOf[e];
     if (i < 2 || !(ns > i)) continue;
-    L = log10((real)4. * teR / (real)(i * i));
-    Te4 = (real)4. * teR / ((real)(i * i) * RF(1.e4));
-    real Np = (real)ionAt(b, c, i, i) * (real)b.abun[i];
-    real betaFF = ((real)i / (real)2.) * (RF(1.070073e-11) - RF(2.5730207e-13) * L + RF(2.109134e-13) * L * L);
-    real t = Np * neR * betaFF * kBoltz() * teR / sqrt(teR);
+    real t = (real)termFF2[e - 1];
     if (!isnan(t)) coolFF = coolFF + t;
-    real betaRec = ((real)i / (real)2.) * (RF(1.06926e-10) - RF(2.41756e-11) * L + RF(1.14542e-12) * L * L -
-                                           RF(5.06535e-13) * L * L * L + RF(9.16745e-14) * L * L * L * L);
-    t = Np * neR * betaRec * kBoltz() * teR / sqrt(teR);
+    t = (real)termRec2[e - 1];
     if (!isnan(t)) coolRec = coolRec + t;
+  }
+  // Te4 as the He-like loop leaves it: 4 Te / (i^2 1e4) of the last element with nstages > i
+  real Te4 = teR / RF(1.e4);
+  for (int e = 1; e <= E; ++e) {
+    const int i = m.zOf[e];
+    if (i < 2 || !(ns > i)) continue;
+    Te4 = (real)4. * teR / ((real)(i * i) * RF(1.e4));
   }
   real coolColl;
   if (teR > (real)5000.)
     coolColl = (RF(2.47e-8) * exp(-RF(118338.) / teR) * pow(Te4, RF(-0.228)) +
-                RF(1.32e-8) * exp(-RF(140252.) / teR) * pow(Te4, RF(-0.460))) * kHcRyd() * (real)ionAt(b, c, 1, 1) * neR;
+                RF(1.32e-8) * exp(-RF(140252.) / teR) * pow(Te4, RF(-0.460))) * kHcRyd() * (real)xAt(b, m, w, 1, 1) * neR;
   else
     coolColl = 0;
   real coolCollH = 0;
-  for (int e = 1; e <= b.nElemUsed; ++e) {
-    const int elem = b.zOf[e];
-    for (int ion = 1; ion <= min(elem, ns - 1); ++ion)
-      coolCollH = coolCollH + (real)b.abun[elem] * (real)ionAt(b, c, elem, ion) * (real)b.coll2[pairOff(b, c, elem, ion)] * neR;
+  for (int e = 1; e <= E; ++e) {
+    const int elem = m.zOf[e];
+    for (int ion = 1; ion <= min(elem, ns - 1); ++ion) coolCollH = coolCollH + (real)w.AL[(e - 1) * ns + (ion - 1)];
   }
   real heatSte = 0;
-  for (int e = 1; e <= b.nElemUsed; ++e) {
-    const int elem = b.zOf[e];
+  for (int e = 1; e <= E; ++e) {
+    const int elem = m.zOf[e];
     for (int ion = 1; ion <= min(elem, ns - 1); ++ion) {
-      const int p0 = b.pairShell0[(e - 1) * 32 + (ion - 1)];
-      const int nsh = b.pairNShell[(e - 1) * 32 + (ion - 1)];
-      for (int s = 0; s < nsh; ++s)
-        heatSte = heatSte + (real)b.pi2[(size_t)(p0 + s) * C1 + cell] * (real)ionAt(b, c, elem, ion) * (real)b.abun[elem];
+      const int p0 = m.p0[(e - 1) * 32 + (ion - 1)];
+      const int nsh = m.nsh[(e - 1) * 32 + (ion - 1)];
+      for (int q = 0; q < nsh; ++q) heatSte = heatSte + (real)w.T[p0 + q];
     }
   }
   b.coolA[cell] = coolFF + coolRec;
@@ -1066,16 +1213,23 @@ cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStr
   const int T = 128, nb = (C + T - 1) / T;
   cudaError_t e = cudaMemsetAsync(b.counters, 0, sizeof(BalanceCounters), s);
   if (e != cudaSuccess) return e;
-  photoIntegralsKernel<<<nb, T, 0, s>>>(b, g.jste);
+  hitComptonKernel<<<nb, T, 0, s>>>(b, g.jste);
+  if (b.nShellsTot > 0) shellIntegralsKernel<<<dim3(nb, b.nShellsTot), T, 0, s>>>(b, g.jste);
   loadStateKernel<<<nb, T, 0, s>>>(b, g.te, g.ne, g.ionDen);
   const int rounds = std::min(std::max(maxRounds, 1), 20);
   for (int r = 1; r <= rounds; ++r) {
-    ratesKernel<<<nb, T, 0, s>>>(b, g.hden);
+    ratesKernel<<<(C + 3) / 4, 128, ((size_t)b.metaDoubles + 4 * (size_t)b.warpDoubles) * sizeof(double), s>>>(b, g.hden);
     if (b.nAtoms > 0) atomsKernel<<<dim3(nb, b.nAtoms), T, 0, s>>>(b);
     secantKernel<<<nb, T, 0, s>>>(b, r == rounds && rounds < 20 ? 1 : 0);
   }
   storeKernel<<<nb, T, 0, s>>>(b, g);
   return cudaGetLastError();
+}
+
+// the rates kernel's dynamic shared memory (four warps of b.warpDoubles doubles)
+cudaError_t prepare(const BalanceData& bd) {
+  const size_t bytes = ((size_t)bd.dev.metaDoubles + 4 * (size_t)bd.dev.warpDoubles) * sizeof(double);
+  return cudaFuncSetAttribute(ratesKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
 cudaError_t launchForLines(BalanceData& bd, const float* te, const float* ne, const float* ionDen,

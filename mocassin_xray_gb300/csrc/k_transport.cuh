@@ -483,6 +483,22 @@ __device__ __forceinline__ void flushCounters(const LocalCounters& lc, DevTransp
   if (lane == 0 && qp != 0.) atomicAdd(&cnt->qPhot, qp);
 }
 
+// Emission and cell steps take turns by warp: an iteration runs the emission
+// code only once kEmitBatch lanes wait for it (or no lane is stepping), else
+// it runs one cell step of every stepping lane.  Emissions are about one event
+// in ten but long (a CDF bisection through global memory, the direction
+// draw); run one lane at a time they would stall the other 31 lanes on almost
+// every iteration.  Only the order of events across lanes changes, not any
+// packet's history.
+constexpr int kEmitBatch = 12;   // default; the launch may choose another
+
+__device__ __forceinline__ bool emitTurn(int state, int emitBatch) {
+  const unsigned FULL = 0xffffffffu;
+  const unsigned emit = __ballot_sync(FULL, state == ST_EMIT);
+  const unsigned step = __ballot_sync(FULL, state == ST_STEP);
+  return emit != 0u && (__popc(emit) >= emitBatch || step == 0u);
+}
+
 // Idle lanes of the warp take the next packet ids from the work queue with one
 // atomic; returns this lane's id (meaningful when the lane was idle).
 __device__ __forceinline__ unsigned long long refill(unsigned need, DevTransportCounters* cnt) {
@@ -498,7 +514,7 @@ __device__ __forceinline__ unsigned long long refill(unsigned need, DevTransport
 template <typename R>
 __global__ void __launch_bounds__(256)
 transportKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportCounters* cnt,
-                uint64_t seed, uint64_t base, unsigned long long n, double deltaE) {
+                uint64_t seed, uint64_t base, unsigned long long n, double deltaE, int emitBatch) {
   extern __shared__ float smem[];
   float* sX = smem;
   float* sY = sX + g.nx;
@@ -536,8 +552,11 @@ transportKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportC
       }
     }
     if (__ballot_sync(FULL, state != ST_DONE) == 0u) break;
-    if (state == ST_EMIT) state = emitPacket<R>(g, q, in, out, sh, p, deltaE, lc);
-    else if (state == ST_STEP) state = stepPacket<R>(g, q, in, out, sh, p, deltaER, deltaE, lc);
+    if (emitTurn(state, emitBatch)) {
+      if (state == ST_EMIT) state = emitPacket<R>(g, q, in, out, sh, p, deltaE, lc);
+    } else if (state == ST_STEP) {
+      state = stepPacket<R>(g, q, in, out, sh, p, deltaER, deltaE, lc);
+    }
   }
   flushCounters(lc, cnt);
 }
@@ -555,7 +574,7 @@ __global__ void __launch_bounds__(256)
 transportKernelBatched(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportCounters* cnt,
                        const NebulaDesc* __restrict__ neb, const unsigned long long* __restrict__ pktBegin, int nNeb,
                        const float* __restrict__ axes, const int32_t* __restrict__ active,
-                       const float* __restrict__ cdfs) {
+                       const float* __restrict__ cdfs, int emitBatch) {
   extern __shared__ float smem[];
   float* sNu = smem;
   for (int i = threadIdx.x; i < g.nbins; i += blockDim.x) sNu[i] = g.nu[i];
@@ -601,8 +620,11 @@ transportKernelBatched(DevGrid g, DevTransportIn in, DevTransportOut out, DevTra
       }
     }
     if (__ballot_sync(FULL, state != ST_DONE) == 0u) break;
-    if (state == ST_EMIT) state = emitPacket<R>(g, q, in, out, sh, p, deltaE, lc);
-    else if (state == ST_STEP) state = stepPacket<R>(g, q, in, out, sh, p, deltaER, deltaE, lc);
+    if (emitTurn(state, emitBatch)) {
+      if (state == ST_EMIT) state = emitPacket<R>(g, q, in, out, sh, p, deltaE, lc);
+    } else if (state == ST_STEP) {
+      state = stepPacket<R>(g, q, in, out, sh, p, deltaER, deltaE, lc);
+    }
   }
   flushCounters(lc, cnt);
 }

@@ -7,7 +7,8 @@ namespace mcx {
 cudaError_t launchTransportF64(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,
                                DevTransportCounters* cnt, uint64_t seed, uint64_t base, unsigned long long n,
                                double deltaE, const TransportLaunch& L, cudaStream_t s) {
-  transportKernel<double><<<L.blocks, L.threads, L.smem, s>>>(g, in, out, cnt, seed, base, n, deltaE);
+  transportKernel<double><<<L.blocks, L.threads, L.smem, s>>>(g, in, out, cnt, seed, base, n, deltaE,
+                                                         L.emitBatch > 0 ? L.emitBatch : kEmitBatch);
   return cudaGetLastError();
 }
 
@@ -17,7 +18,7 @@ cudaError_t launchTransportBatchedF64(const DevGrid& g, const DevTransportIn& in
                                       const int32_t* active, const float* cdfs, const TransportLaunch& L,
                                       cudaStream_t s) {
   transportKernelBatched<double><<<L.blocks, L.threads, L.smem, s>>>(g, in, out, cnt, neb, pktBegin, nNeb, axes, active,
-                                                                  cdfs);
+                                                                  cdfs, L.emitBatch > 0 ? L.emitBatch : kEmitBatch);
   return cudaGetLastError();
 }
 

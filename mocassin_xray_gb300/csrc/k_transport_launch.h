@@ -9,6 +9,7 @@ struct TransportLaunch {
   int blocks;
   int threads;
   size_t smem;
+  int emitBatch;   // 0 = the kernel's default
 };
 
 cudaError_t launchTransportF32(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,

@@ -1222,6 +1222,7 @@ extern "C" int mcx_transport(mcx_ctx* c, const mcx_transport_opts* o, mcx_transp
   out.jste = c->jste.p; out.escaped = c->escaped.p; out.hEst = c->hEst.p;
 
   TransportLaunch L{};
+  L.emitBatch = o->emit_batch > 32 ? 32 : o->emit_batch;
   L.threads = o->block_size > 0 ? o->block_size : 256;
   if (L.threads % 32 != 0 || L.threads > 256) return fail(c, MCX_ERR_INPUT, "mcx_transport: block_size must be a multiple of 32 up to 256");
   L.smem = (size_t)(c->nx + c->ny + c->nz + 2 * c->nbins) * sizeof(float);
@@ -1290,6 +1291,7 @@ extern "C" int mcx_transport_batched(mcx_ctx* c, const mcx_transport_opts* o, co
   DevTransportOut out{};
   out.jste = c->jste.p; out.escaped = c->escaped.p;
   TransportLaunch L{};
+  L.emitBatch = o->emit_batch > 32 ? 32 : o->emit_batch;
   L.threads = o->block_size > 0 ? o->block_size : 256;
   if (L.threads % 32 != 0 || L.threads > 256)
     return fail(c, MCX_ERR_INPUT, "mcx_transport_batched: block_size must be a multiple of 32 up to 256");
