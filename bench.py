@@ -272,7 +272,7 @@ def config_dict(args, setup) -> dict:
             "grid": f"{args.grid}^3", "n_cells": setup.n_cells, "nbins": setup.nbins,
             "packets_per_step": args.packets, "elements": "H,He,C,N,O,Ne,S",
             "geometry_precision": "fp32", "estimator_precision": "fp64",
-            "balance_precision": "fp32 rates, fp64 level populations / ladder / bracketing",
+            "balance_precision": "fp32 rates, ionisation ladder (log space) and level populations (state reduction); fp64 Te bracketing",
             "l2": "inputs larger than L2 (Jste fp64 331 MB, opacity 165 MB)",
             "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU"}
 

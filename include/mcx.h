@@ -276,9 +276,10 @@ int  mcx_emission(mcx_ctx* ctx, const mcx_phase_opts* opts, mcx_phase_stats* sta
  * TeOld/NeOld take Te/Ne first, then Te, Ne, ionDen, lgConverged and lgBlack
  * are updated on the device.  Gas only; grains are outside this phase. */
 #define MCX_BAL_FP64  0         /* FP64 throughout (the plain path)                    */
-#define MCX_BAL_MIXED 1         /* FP32 rates, collision strengths and exponentials;
-                                   FP64 level-population LU, ionisation ladder and
-                                   normalisation, electron density, Te bracketing      */
+#define MCX_BAL_MIXED 1         /* FP32 rates, collision strengths, exponentials,
+                                   ionisation ladder (on the logarithms of its
+                                   products) and level populations (state
+                                   reduction); FP64 Te bracketing                     */
 
 typedef struct mcx_balance_opts {
     int32_t precision;          /* MCX_BAL_*                                            */

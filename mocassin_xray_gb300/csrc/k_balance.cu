@@ -229,6 +229,8 @@ std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out)
   d.state = carve<int8_t>(blocks, C1, err);
   d.ibConv = carve<int8_t>(blocks, C1, err);
   d.counters = carve<BalanceCounters>(blocks, 1, err);
+  d.list = carve<int32_t>(blocks, 2 * C1, err);
+  d.listCount = carve<unsigned int>(blocks, kMaxRounds + 1, err);
   if ((int)blocks.size() > (int)(sizeof(bd->blocks) / sizeof(bd->blocks[0]))) err = "balance: too many device blocks";
   for (size_t i = 0; i < blocks.size() && i < sizeof(bd->blocks) / sizeof(bd->blocks[0]); ++i) bd->blocks[i] = blocks[i];
   bd->nBlocks = (int)std::min(blocks.size(), sizeof(bd->blocks) / sizeof(bd->blocks[0]));

@@ -28,6 +28,8 @@ namespace mcx {
 struct Setup;
 struct LineSumArgs;
 
+constexpr int kMaxRounds = 20;   // maxIterateT (source/update_mod.f90:106-107)
+
 // One photoionised shell (elem, ion, shell) of an element that is on.
 struct PhotoShell {
   int32_t elem, ion, shell;   // Z, stage, shell (1-based)
@@ -45,6 +47,8 @@ struct BalanceCounters {
 struct BalanceDev {
   int32_t nbins, nCells, nstages, nElemUsed, nShellsTot, nAtoms, nDiel, nAldro;
   int32_t lgBadnell, lgCompton;
+  int32_t* list;               // [2][C+1] the cells of the current and the next T-iteration round
+  unsigned int* listCount;     // [kMaxRounds+1] cells listed for each round
   int32_t warpDoubles;         // shared memory of one cell of the rates kernel, in doubles
   int32_t metaDoubles;         // its per-block element tables, in doubles
   int32_t secIonP, cRecoilHP, cRecoilHeP;

@@ -172,6 +172,7 @@ __global__ void __launch_bounds__(128) hitComptonKernel(BalanceDev b, const doub
     if (jste[(size_t)(i - 1) * C1 + cell] > 0.) { hit = true; break; }
   b.state[cell] = hit ? 0 : 2;
   if (!hit) return;
+  b.list[atomicAdd(&b.listCount[0], 1u)] = cell;   // the cells of the first T-iteration
   if (b.lgCompton) {
     real s1 = 0, s2 = 0, rhH = 0, rhHe = 0;
     for (int i = 1; i <= b.nbins; ++i) {
@@ -504,10 +505,12 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
 // calcAlpha, photoionisation, collisionalIonisation, compton, ionBalance and
 // the thermBalance terms without forLines, one warp per iterating cell
 // (b.warpDoubles doubles of shared memory per warp).
-__global__ void __launch_bounds__(128) ratesKernel(BalanceDev b, const float* __restrict__ hdenG) {
+__global__ void __launch_bounds__(128) ratesKernel(BalanceDev b, const float* __restrict__ hdenG, int round) {
   extern __shared__ double wsm[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int cell = blockIdx.x * (blockDim.x >> 5) + wib + 1;
+  const int li = blockIdx.x * (blockDim.x >> 5) + wib;   // index into this round's cell list
+  const unsigned cnt = b.listCount[round];
+  if ((unsigned)(blockIdx.x * (blockDim.x >> 5)) >= cnt) return;   // the whole block
   const int C1 = b.nCells + 1, ns = b.nstages, E = b.nElemUsed, NP = E * ns, nSh = b.nShellsTot;
   // the element tables, then one slice per warp
   int32_t* sZ = reinterpret_cast<int32_t*>(wsm);
@@ -525,7 +528,8 @@ __global__ void __launch_bounds__(128) ratesKernel(BalanceDev b, const float* __
     sNs[i] = (int16_t)b.pairNShell[i];
   }
   __syncthreads();
-  if (cell > b.nCells || b.state[cell] != 0) return;   // the whole warp
+  if ((unsigned)li >= cnt) return;   // the whole warp
+  const int cell = b.list[(size_t)(round & 1) * C1 + li];
   const ElemMeta m{sZ, sX, sA, sP0, sNs};
   WarpCell w;
   w.X = reinterpret_cast<real*>(wsm + b.metaDoubles + (size_t)wib * b.warpDoubles);
@@ -1018,10 +1022,11 @@ __device__ double equilibriumLines(const BalanceDev& b, int atom, double Te, dou
 }
 
 // forLines of update_mod: one thread per (cell, ion with data)
-__global__ void __launch_bounds__(128) atomsKernel(BalanceDev b) {
-  const int cell = blockIdx.x * blockDim.x + threadIdx.x + 1;
+__global__ void __launch_bounds__(128) atomsKernel(BalanceDev b, int round) {
+  const int li = blockIdx.x * blockDim.x + threadIdx.x;
   const int atom = blockIdx.y;
-  if (cell > b.nCells || b.state[cell] != 0) return;
+  if ((unsigned)li >= b.listCount[round]) return;
+  const int cell = b.list[(size_t)(round & 1) * (b.nCells + 1) + li];
   const CellIdx c{cell, b.nCells + 1};
   const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
   const int elem = h[kAtElem], ion = h[kAtIon];
@@ -1125,10 +1130,11 @@ cudaError_t launchForbSums(BalanceData& bd, const LineSumArgs& a, cudaStream_t s
 #endif
 
 // heating - cooling and the secant step of iterateT (FP64 in both precisions)
-__global__ void __launch_bounds__(128) secantKernel(BalanceDev b, int lastRound) {
-  const int cell = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  if (cell > b.nCells || b.state[cell] != 0) return;
+__global__ void __launch_bounds__(128) secantKernel(BalanceDev b, int round, int lastRound) {
+  const int li = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((unsigned)li >= b.listCount[round]) return;
   const int C1 = b.nCells + 1;
+  const int cell = b.list[(size_t)(round & 1) * C1 + li];
   double coolColl = b.coolHex[cell];
   for (int a = 0; a < b.nAtoms; ++a) coolColl = coolColl + b.forSum[(size_t)a * C1 + cell];
   const double ne = b.ne[cell];
@@ -1174,6 +1180,8 @@ __global__ void __launch_bounds__(128) secantKernel(BalanceDev b, int lastRound)
   if (done) {
     b.state[cell] = 1;
     if (!b.ibConv[cell]) atomicAdd(&b.counters->noIonBal, 1ull);
+  } else if (round + 1 < kMaxRounds) {
+    b.list[(size_t)((round + 1) & 1) * C1 + atomicAdd(&b.listCount[round + 1], 1u)] = cell;
   }
 }
 
@@ -1213,14 +1221,19 @@ cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStr
   const int T = 128, nb = (C + T - 1) / T;
   cudaError_t e = cudaMemsetAsync(b.counters, 0, sizeof(BalanceCounters), s);
   if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(b.listCount, 0, sizeof(unsigned) * (kMaxRounds + 1), s);
+  if (e != cudaSuccess) return e;
   hitComptonKernel<<<nb, T, 0, s>>>(b, g.jste);
   if (b.nShellsTot > 0) shellIntegralsKernel<<<dim3(nb, b.nShellsTot), T, 0, s>>>(b, g.jste);
   loadStateKernel<<<nb, T, 0, s>>>(b, g.te, g.ne, g.ionDen);
   const int rounds = std::min(std::max(maxRounds, 1), 20);
+  // round r works on the cells listed for it (the first list holds every cell
+  // a packet reached; each secant step lists the cells that go on)
   for (int r = 1; r <= rounds; ++r) {
-    ratesKernel<<<(C + 3) / 4, 128, ((size_t)b.metaDoubles + 4 * (size_t)b.warpDoubles) * sizeof(double), s>>>(b, g.hden);
-    if (b.nAtoms > 0) atomsKernel<<<dim3(nb, b.nAtoms), T, 0, s>>>(b);
-    secantKernel<<<nb, T, 0, s>>>(b, r == rounds && rounds < 20 ? 1 : 0);
+    ratesKernel<<<(C + 3) / 4, 128, ((size_t)b.metaDoubles + 4 * (size_t)b.warpDoubles) * sizeof(double), s>>>(
+        b, g.hden, r - 1);
+    if (b.nAtoms > 0) atomsKernel<<<dim3(nb, b.nAtoms), T, 0, s>>>(b, r - 1);
+    secantKernel<<<nb, T, 0, s>>>(b, r - 1, r == rounds && rounds < 20 ? 1 : 0);
   }
   storeKernel<<<nb, T, 0, s>>>(b, g);
   return cudaGetLastError();
