@@ -445,24 +445,30 @@ cudaError_t transpose(const float* in, float* out, int rows, int cols, cudaStrea
 // j = (j * mul) / div, two roundings as in source/iteration_mod.f90:1002-1031
 // the same with the divisor of each cell's nebula (a batch mixing octant and full grids)
 __global__ void scaleJCellKernel(double* j, size_t n, size_t C1, double mul, const float* __restrict__ div) {
-  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (; i < n; i += stride) {
-    double v = j[i] * mul;
-    const double d = (double)div[i % C1];
-    if (d != 1.) v = v / d;
-    j[i] = v;
-  }
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double v = j[i] * mul;
+  const double d = (double)div[i % C1];
+  if (d != 1.) v = v / d;
+  j[i] = v;
 }
 
+// four entries per thread, one thread per four (a memory-bound pass over 331 MB
+// wants every load in flight at once rather than a grid-stride loop)
 __global__ void scaleJKernel(double* j, size_t n, double mul, double div) {
-  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (; i < n; i += stride) {
-    double v = j[i] * mul;
-    if (div != 1.) v = v / div;
-    j[i] = v;
+  const size_t i0 = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) * 4;
+  if (i0 >= n) return;
+  double v[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) v[q] = i0 + q < n ? j[i0 + q] : 0.;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    v[q] = v[q] * mul;
+    if (div != 1.) v[q] = v[q] / div;
   }
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    if (i0 + q < n) j[i0 + q] = v[q];
 }
 
 template <typename T>
@@ -1323,21 +1329,22 @@ extern "C" int mcx_normalize_j(mcx_ctx* c) {
   if (!c) return MCX_ERR_INPUT;
   if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_normalize_j: no model loaded");
   CK(cudaSetDevice(c->device), "cudaSetDevice");
-  int blocks = c->numSMs * 4;
   if (c->nNeb > 0) {
     const size_t C1 = (size_t)c->nCells + 1;
-    scaleJCellKernel<<<blocks, 256, 0, c->stream>>>(c->jste.p, c->jste.n, C1, 1.e-9, c->jDiv.p);
+    scaleJCellKernel<<<(unsigned)((c->jste.n + 255) / 256), 256, 0, c->stream>>>(c->jste.p, c->jste.n, C1, 1.e-9,
+                                                                               c->jDiv.p);
     CK(cudaGetLastError(), "scale J");
-    scaleJCellKernel<<<blocks, 256, 0, c->stream>>>(c->escaped.p, c->escaped.n, C1, 1., c->jDiv.p);
+    scaleJCellKernel<<<(unsigned)((c->escaped.n + 255) / 256), 256, 0, c->stream>>>(c->escaped.p, c->escaped.n, C1, 1.,
+                                                                                  c->jDiv.p);
     CK(cudaGetLastError(), "scale escaped");
     CK(cudaStreamSynchronize(c->stream), "mcx_normalize_j");
     return MCX_OK;
   }
   const double div = c->symmetric ? 8. : 1.;
-  scaleJKernel<<<blocks, 256, 0, c->stream>>>(c->jste.p, c->jste.n, 1.e-9, div);
+  scaleJKernel<<<(unsigned)((c->jste.n + 1023) / 1024), 256, 0, c->stream>>>(c->jste.p, c->jste.n, 1.e-9, div);
   CK(cudaGetLastError(), "scale J");
   if (div != 1.) {
-    scaleJKernel<<<blocks, 256, 0, c->stream>>>(c->escaped.p, c->escaped.n, 1., div);
+    scaleJKernel<<<(unsigned)((c->escaped.n + 1023) / 1024), 256, 0, c->stream>>>(c->escaped.p, c->escaped.n, 1., div);
     CK(cudaGetLastError(), "scale escaped");
   }
   CK(cudaStreamSynchronize(c->stream), "mcx_normalize_j");
