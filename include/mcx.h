@@ -458,6 +458,10 @@ typedef struct mcx_lines {
 
 int  mcx_line_luminosities(mcx_ctx* ctx, mcx_lines* out);
 
+/* The same for nebula b of a batch (mcx_load_batched): its cells only, its
+ * octant factor. */
+int  mcx_line_luminosities_nebula(mcx_ctx* ctx, int32_t nebula, mcx_lines* out);
+
 
 /* ------------------------------------------- transport without allocation */
 /* No counterpart in the reference.  Some callers cannot allocate device

@@ -163,6 +163,7 @@ SIGNATURES = [
     ("mcx_balance", C.c_int, [_P, C.POINTER(BalanceOpts), C.POINTER(BalanceStats)]),
     ("mcx_iterate", C.c_int, [_P, C.POINTER(IterateOpts), C.POINTER(IterateStats)]),
     ("mcx_line_luminosities", C.c_int, [_P, C.POINTER(Lines)]),
+    ("mcx_line_luminosities_nebula", C.c_int, [_P, C.c_int32, C.POINTER(Lines)]),
     ("mcx_load_batched", C.c_int, [_P, _P, C.c_int32]),
     ("mcx_batch_info", C.c_int, [_P, C.POINTER(C.c_int32), _P]),
     ("mcx_transport_batched", C.c_int, [_P, C.POINTER(TransportOpts), C.POINTER(BatchPackets),

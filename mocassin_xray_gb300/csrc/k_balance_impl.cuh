@@ -37,7 +37,8 @@ __device__ __forceinline__ double kXMax() { return RD(0.99999); }       // const
 
 constexpr int kNE = 30;
 // mixed precision: ions with elemAbun * ionDen below this skip the atom solve
-constexpr double kNegligibleIon = 1e-16;
+// (their forbidden lines carry below 1e-7 of any cell's cooling)
+constexpr double kNegligibleIon = 1e-12;
 
 struct CellIdx {
   int cell, C1;
@@ -1094,14 +1095,14 @@ __global__ void __launch_bounds__(128) forbLevelSumsKernel(BalanceDev b, LineSum
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int group = t >> 5;
   if (group >= a.nGroups) return;   // whole warps only
-  const int cell = t + 1;
+  const int cell = a.cellBase + t + 1;
   const int atom = blockIdx.y;
   const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
   const int elem = h[kAtElem], ion = h[kAtIon], nLev = h[kAtNLev];
   const int top = min(elem + 1, b.nstages);
   const size_t C1 = (size_t)b.nCells + 1;
   const int e = b.xref[elem];
-  const bool valid = cell <= b.nCells && a.black[cell] < 1;
+  const bool valid = t + 1 <= a.nRange && a.black[cell] < 1;
   double y[kMaxLevels + 1];
   double w = 0.;
   if (valid) {

@@ -41,8 +41,8 @@ __global__ void __launch_bounds__(128) gasLineSumsKernel(EmissionDev e, LineSumA
   const int group = t >> 5;
   if (group >= a.nGroups) return;   // whole warps only
   const int lane = threadIdx.x & 31;
-  const int cell = t + 1;
-  const bool valid = cell <= a.nCells && a.black[cell] < 1;
+  const int cell = a.cellBase + t + 1;
+  const bool valid = t + 1 <= a.nRange && a.black[cell] < 1;
   double* row = a.partial + (size_t)group * a.nEntries;
   // lanes without a cell evaluate a benign state and contribute 0
   double Te = 1.e4, Ne = 100., Hden = 0., dV = 0.;

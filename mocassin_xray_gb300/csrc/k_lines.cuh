@@ -3,7 +3,8 @@
 //
 // Every quantity outputGas integrates is a sum over the active cells with
 // lgBlack < 1 of a per-cell value times Hden * dV.  Each warp takes 32
-// consecutive cells (group g = cells 32g+1 .. 32g+32), reduces every entry
+// consecutive cells of the range summed (group g = cells cellBase+32g+1 ..
+// cellBase+32g+32: all cells, or one nebula of a batch), reduces every entry
 // over its lanes with a fixed shuffle tree and writes one row of
 // partial[group][entry]; a second kernel adds the rows in group order.  The
 // sums are therefore the same from run to run.
@@ -37,7 +38,8 @@ struct LineSumArgs {
   const int32_t* black;     // [C+1] lgBlack
   double* partial;          // [nGroups][nEntries]
   const int32_t* forbBase;  // [nAtoms] device
-  int32_t nCells, nGroups, nEntries;
+  int32_t nCells, nGroups, nEntries;   // nCells: of the whole context (the arrays' C+1)
+  int32_t cellBase, nRange;            // the cells summed: cellBase+1 .. cellBase+nRange
   int32_t nHydro, hydroBase, heiBase, ionBase, nIonElem;
   int32_t hydroIz[30];      // elements with hydrogenic lines, ascending
   int32_t ionElem[30];      // elements on, ascending

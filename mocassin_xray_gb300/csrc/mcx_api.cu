@@ -1463,9 +1463,26 @@ static int iterateImpl(mcx_ctx* c, const mcx_iterate_opts* o, const mcx_batch_pa
   return rc;
 }
 
+static int lineLuminosities(mcx_ctx* c, int cellBase, int nRange, bool symmetric, mcx_lines* out);
+
 extern "C" int mcx_line_luminosities(mcx_ctx* c, mcx_lines* out) {
   if (!c || !out) return fail(c, MCX_ERR_INPUT, "mcx_line_luminosities: null argument");
   if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_line_luminosities: no model loaded");
+  if (c->nNeb > 0)
+    return fail(c, MCX_ERR_STATE, "mcx_line_luminosities: the context holds a batch (use mcx_line_luminosities_nebula)");
+  return lineLuminosities(c, 0, c->nCells, c->symmetric, out);
+}
+
+extern "C" int mcx_line_luminosities_nebula(mcx_ctx* c, int32_t nebula, mcx_lines* out) {
+  if (!c || !out) return fail(c, MCX_ERR_INPUT, "mcx_line_luminosities_nebula: null argument");
+  if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_line_luminosities_nebula: no model loaded");
+  if (c->nNeb <= 0) return fail(c, MCX_ERR_STATE, "mcx_line_luminosities_nebula: the context holds no batch");
+  if (nebula < 0 || nebula >= c->nNeb) return fail(c, MCX_ERR_INPUT, "mcx_line_luminosities_nebula: no such nebula");
+  return lineLuminosities(c, c->nebCellOff[nebula], c->nebCellOff[nebula + 1] - c->nebCellOff[nebula],
+                          c->nebSym[nebula] != 0, out);
+}
+
+static int lineLuminosities(mcx_ctx* c, int cellBase, int nRange, bool symmetric, mcx_lines* out) {
   if (!c->lgGas || !c->emission || !c->balance)
     return fail(c, MCX_ERR_STATE, "mcx_line_luminosities: the grid holds no gas");
   CK(cudaSetDevice(c->device), "cudaSetDevice");
@@ -1475,7 +1492,9 @@ extern "C" int mcx_line_luminosities(mcx_ctx* c, mcx_lines* out) {
   a.te = c->te.p; a.ne = c->ne.p; a.ionDen = c->ionDen.p; a.hden = c->hden.p;
   a.vol = c->volD.p; a.black = c->lgBlack.p;
   a.nCells = C;
-  a.nGroups = (C + 31) / 32;
+  a.cellBase = cellBase;
+  a.nRange = nRange;
+  a.nGroups = (nRange + 31) / 32;
   int n = 1;
   a.hydroBase = n;
   for (int iz = 1; iz <= 30; ++iz)
@@ -1514,7 +1533,7 @@ extern "C" int mcx_line_luminosities(mcx_ctx* c, mcx_lines* out) {
 
   // normalisation and units (source/output_mod.f90:684-805)
   int nUsed = 0;
-  for (int cell = 1; cell <= C; ++cell) nUsed += black[cell] < 1 ? 1 : 0;
+  for (int cell = cellBase + 1; cell <= cellBase + nRange; ++cell) nUsed += black[cell] < 1 ? 1 : 0;
   out->n_cells = nUsed;
   double hb = sum[0];
   const bool rel = hb > 0.;
@@ -1566,7 +1585,7 @@ extern "C" int mcx_line_luminosities(mcx_ctx* c, mcx_lines* out) {
     }
   }
   hb = hb * (double)1.e-16f;
-  if (c->symmetric) hb = 8. * hb;
+  if (symmetric) hb = 8. * hb;
   out->hbeta_vol = hb;
   return MCX_OK;
 }

@@ -230,9 +230,9 @@ class Context:
         self._check(lib().mcx_iterate(self._h, C.byref(o), C.byref(st)))
         return st
 
-    def line_luminosities(self) -> dict:
+    def line_luminosities(self, nebula: int | None = None) -> dict:
         """outputGas's analytical line luminosities and ionic volume averages from the current state
-        (source/output_mod.f90:13-805).
+        (source/output_mod.f90:13-805); of nebula `nebula` for a batch.
 
         Returns hbeta_vol [1e36 erg/s] (x8 in symmetricXYZ mode), relative (line sums divided by
         HbetaVol), n_cells, kernel_ms, hydro[30,14,8] at [iz-1, iup-2, ilow-1], hei[34],
@@ -247,7 +247,10 @@ class Context:
         ion_vol = np.zeros(30 * S)
         o = abi.Lines(hydro_vol=hydro.ctypes.data, hei_vol=hei.ctypes.data, forb_vol=forb.ctypes.data,
                       wav=wav.ctypes.data, te_vol=te_vol.ctypes.data, ion_vol=ion_vol.ctypes.data)
-        self._check(lib().mcx_line_luminosities(self._h, C.byref(o)))
+        if nebula is None:
+            self._check(lib().mcx_line_luminosities(self._h, C.byref(o)))
+        else:
+            self._check(lib().mcx_line_luminosities_nebula(self._h, nebula, C.byref(o)))
         # the ABI arrays are column-major (the reference's layouts): reverse the axes
         return dict(hbeta_vol=o.hbeta_vol, relative=bool(o.relative), n_cells=int(o.n_cells),
                     kernel_ms=float(o.kernel_ms),

@@ -74,3 +74,24 @@ def test_incompatible_nebulae_are_rejected(batch_setups, decks, data_dir):
     with pytest.raises(RuntimeError, match="frequency mesh"):
         bc.load_batched([setups[0], other])
     bc.close()
+
+
+def test_line_luminosities_per_nebula(batch_setups):
+    """mcx_line_luminosities_nebula sums one nebula's cells in the same groups as a context holding that
+    nebula alone: the same bits."""
+    setups, _ = batch_setups
+    bc = Context(0)
+    bc.load_batched(setups)
+    for b, s in enumerate(setups):
+        sc = Context(0)
+        sc.load(s)
+        g1 = bc.line_luminosities(nebula=b)
+        g2 = sc.line_luminosities()
+        assert g1["n_cells"] == g2["n_cells"] == s.info.n_cells
+        assert g1["hbeta_vol"] == g2["hbeta_vol"]
+        for key in ("hydro", "hei", "te_vol", "ion_vol"):
+            np.testing.assert_array_equal(g1[key], g2[key])
+        sc.close()
+    with pytest.raises(RuntimeError, match="batch"):
+        bc.line_luminosities()
+    bc.close()
