@@ -382,6 +382,44 @@ typedef struct mcx_iterate_stats {
 
 int  mcx_iterate(mcx_ctx* ctx, const mcx_iterate_opts* opts, mcx_iterate_stats* stats);
 
+/* ------------------------------------------- frozen-field line sensitivities */
+/* No counterpart in the reference.  With the radiation field of the context
+ * (the normalised Jste of the last transport) held fixed, the balance of a
+ * cell depends on that cell's density and on the abundances alone.  So one
+ * balance with every Hden scaled by (1 + h) gives each cell's response to its
+ * own density, and one balance per listed element its response to that
+ * element's abundance.  For each requested forbidden line (element, ion and
+ * the lower and upper level of fLineEm(i,j) in equilibrium) the call returns
+ * its outputGas volume sum L (1e-25 erg/s x 1e45 cm^3, before the division by
+ * Hbeta), dL/dHden of every cell and dL/d(elemAbun) of every listed element,
+ * as forward differences from the unperturbed balance of the current state.
+ * The balance's response to J (the transport) is outside these derivatives.
+ * The context is left as after the unperturbed balance.  Gas, one nebula. */
+typedef struct mcx_line_ref {
+    int32_t elem, ion, lower, upper;
+} mcx_line_ref;
+
+typedef struct mcx_sens_opts {
+    int32_t n_lines;
+    int32_t n_abun;
+    const mcx_line_ref* lines;  /* [n_lines]                                           */
+    const int32_t* abun_z;      /* [n_abun] atomic numbers whose abundance is varied    */
+    double h;                   /* relative step (may be negative); 0 = 1e-3            */
+    int32_t precision;          /* MCX_BAL_* of the balances                            */
+    int32_t reserved[5];
+} mcx_sens_opts;
+
+typedef struct mcx_sens_out {
+    double* L;                  /* [n_lines]                                            */
+    double* dL_dhden;           /* [n_lines][nCells+1] or NULL                          */
+    double* dL_dabun;           /* [n_lines][n_abun] or NULL                            */
+    float   kernel_ms;          /* out: CUDA-event time of the balances and line sums   */
+    float   reserved_f[3];
+    int64_t reserved[4];
+} mcx_sens_out;
+
+int  mcx_line_sensitivities(mcx_ctx* ctx, const mcx_sens_opts* opts, mcx_sens_out* out);
+
 /* ------------------------------------------------------- batches of nebulae */
 /* No counterpart in the reference, which runs one nebula per job.  A batch
  * holds n nebulae (gas only) that share the frequency mesh, the elements and

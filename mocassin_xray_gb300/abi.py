@@ -131,6 +131,20 @@ class BatchPackets(C.Structure):
     _fields_ = [("n_packets", _P), ("seed", _P), ("counter_base", _P), ("n_photons_norm", _P)]
 
 
+class LineRef(C.Structure):
+    _fields_ = [("elem", C.c_int32), ("ion", C.c_int32), ("lower", C.c_int32), ("upper", C.c_int32)]
+
+
+class SensOpts(C.Structure):
+    _fields_ = [("n_lines", C.c_int32), ("n_abun", C.c_int32), ("lines", _P), ("abun_z", _P), ("h", C.c_double),
+                ("precision", C.c_int32), ("reserved", C.c_int32 * 5)]
+
+
+class SensOut(C.Structure):
+    _fields_ = [("L", _P), ("dL_dhden", _P), ("dL_dabun", _P), ("kernel_ms", C.c_float),
+                ("reserved_f", C.c_float * 3), ("reserved", C.c_int64 * 4)]
+
+
 class Lines(C.Structure):
     _fields_ = [("hbeta_vol", C.c_double), ("relative", C.c_int32), ("n_cells", C.c_int32),
                 ("hydro_vol", _P), ("hei_vol", _P), ("forb_vol", _P), ("wav", _P), ("te_vol", _P),
@@ -164,6 +178,7 @@ SIGNATURES = [
     ("mcx_iterate", C.c_int, [_P, C.POINTER(IterateOpts), C.POINTER(IterateStats)]),
     ("mcx_line_luminosities", C.c_int, [_P, C.POINTER(Lines)]),
     ("mcx_line_luminosities_nebula", C.c_int, [_P, C.c_int32, C.POINTER(Lines)]),
+    ("mcx_line_sensitivities", C.c_int, [_P, C.POINTER(SensOpts), C.POINTER(SensOut)]),
     ("mcx_load_batched", C.c_int, [_P, _P, C.c_int32]),
     ("mcx_batch_info", C.c_int, [_P, C.POINTER(C.c_int32), _P]),
     ("mcx_transport_batched", C.c_int, [_P, C.POINTER(TransportOpts), C.POINTER(BatchPackets),

@@ -16,6 +16,7 @@ cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStr
 cudaError_t launchForLines(BalanceData& bd, const float* te, const float* ne, const float* ionDen,
                            const uint8_t* compute, float* forLines, cudaStream_t s);
 cudaError_t launchForbSums(BalanceData& bd, const LineSumArgs& a, cudaStream_t s);
+cudaError_t launchLineCells(BalanceData& bd, const LineCellArgs& a, cudaStream_t s);
 cudaError_t prepare(const BalanceData& bd);
 }  // namespace bal_f64
 namespace bal_mixed {
@@ -305,6 +306,18 @@ cudaError_t launchForLinesEmission(BalanceData& bd, const float* te, const float
 
 cudaError_t launchForbLevelSums(BalanceData& bd, const LineSumArgs& a, cudaStream_t s) {
   return bal_f64::launchForbSums(bd, a, s);
+}
+
+cudaError_t launchLineCellLuminosities(BalanceData& bd, const LineCellArgs& a, cudaStream_t s) {
+  return bal_f64::launchLineCells(bd, a, s);
+}
+
+void invalidateBalanceGraphs(BalanceData& bd) {
+  for (auto& g : bd.graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
 }
 
 }  // namespace mcx

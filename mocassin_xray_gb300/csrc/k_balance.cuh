@@ -141,4 +141,11 @@ cudaError_t launchForLinesEmission(BalanceData& b, const float* te, const float*
 // partial rows of `a` (FP64; the layout is described in k_lines.cuh).
 cudaError_t launchForbLevelSums(BalanceData& b, const LineSumArgs& a, cudaStream_t s);
 
+// Per-cell luminosities of requested forbidden lines (FP64, k_lines.cuh).
+struct LineCellArgs;
+cudaError_t launchLineCellLuminosities(BalanceData& b, const LineCellArgs& a, cudaStream_t s);
+
+// Drops the captured balance graphs (after a change of the tables they bake in).
+void invalidateBalanceGraphs(BalanceData& b);
+
 }  // namespace mcx

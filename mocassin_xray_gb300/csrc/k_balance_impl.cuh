@@ -1121,6 +1121,44 @@ __global__ void __launch_bounds__(128) forbLevelSumsKernel(BalanceDev b, LineSum
   }
 }
 
+// one thread per (cell, requested line): equilibrium with the recombination
+// term, then the line's share (source/output_mod.f90:1943-1984, :410-432)
+__global__ void __launch_bounds__(128) lineCellKernel(BalanceDev b, LineCellArgs a) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int k = blockIdx.y;
+  if (cell > b.nCells) return;
+  const size_t C1 = (size_t)b.nCells + 1;
+  double v = 0.;
+  if (a.black[cell] < 1) {
+    const int atom = a.req[3 * k], lo = a.req[3 * k + 1], hi = a.req[3 * k + 2];
+    const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
+    const int elem = h[kAtElem], ion = h[kAtIon], nLev = h[kAtNLev];
+    const int top = min(elem + 1, b.nstages);
+    const int e = b.xref[elem];
+    const double x = a.ionDen[((size_t)(ion - 1) * b.nElemUsed + (e - 1)) * C1 + cell];
+    double up = 0.;
+    if (ion < top && x > 0.) up = (double)a.ionDen[((size_t)ion * b.nElemUsed + (e - 1)) * C1 + cell] / x;
+    double y[kMaxLevels + 1];
+    equilibriumPops(b, atom, a.te[cell], a.ne[cell], up, true, y);
+    const double* A = b.atomData + h[kAtOffA];
+    const double* E = b.atomData + h[kAtOffE];
+    const double atp = b.atomData[h[kAtOffAtp]];
+    double aji = A[(size_t)(hi - 1) * nLev + (lo - 1)];
+    if (aji != 0.) {
+      const double Eji = E[hi - 1] - E[lo - 1];
+      if (hi == h[kAtIup2p] && lo == 1 && atp > 0.) aji = aji - atp;
+      v = aji * Eji * y[hi] * (double)b.abun[elem] * x * RD(1.9865e9) * (double)a.hden[cell] * a.vol[cell];
+    }
+  }
+  a.out[(size_t)k * C1 + cell] = v;
+}
+
+cudaError_t launchLineCells(BalanceData& bd, const LineCellArgs& a, cudaStream_t s) {
+  if (a.nReq <= 0 || bd.dev.nCells <= 0) return cudaSuccess;
+  lineCellKernel<<<dim3((bd.dev.nCells + 127) / 128, a.nReq), 128, 0, s>>>(bd.dev, a);
+  return cudaGetLastError();
+}
+
 cudaError_t launchForbSums(BalanceData& bd, const LineSumArgs& a, cudaStream_t s) {
   BalanceDev& b = bd.dev;
   if (b.nAtoms <= 0 || a.nGroups <= 0) return cudaSuccess;

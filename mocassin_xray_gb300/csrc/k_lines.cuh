@@ -45,6 +45,21 @@ struct LineSumArgs {
   int32_t ionElem[30];      // elements on, ascending
 };
 
+// Per-cell luminosity of requested forbidden lines (outputGas's forbVol terms
+// before the sum over cells): out[k][cell] = fLineEm(lower, upper) * elemAbun
+// * ionDen * 1.9865e9 * Hden * dV of line k, 0 where lgBlack >= 1.
+struct LineCellArgs {
+  const float* te;          // [C+1]
+  const float* ne;          // [C+1]
+  const float* ionDen;      // [nstages][nElemUsed][C+1]
+  const float* hden;        // [C+1]
+  const double* vol;        // [C+1]
+  const int32_t* black;     // [C+1]
+  const int32_t* req;       // [nReq][3] atom slot, lower level, upper level
+  double* out;              // [nReq][C+1]
+  int32_t nReq;
+};
+
 // Shuffle-tree sum over the 32 lanes; lane 0 holds the result.
 __device__ __forceinline__ double warpSumD(double v) {
 #pragma unroll

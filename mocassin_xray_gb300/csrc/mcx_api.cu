@@ -1590,6 +1590,138 @@ static int lineLuminosities(mcx_ctx* c, int cellBase, int nRange, bool symmetric
   return MCX_OK;
 }
 
+// ------------------------------------------------ frozen-field sensitivities
+namespace {
+
+// the grid state a balance reads and writes
+struct StateCopy {
+  DBuf<float> te, ne, teOld, neOld, ionDen;
+  DBuf<int32_t> conv, black, nIterT;
+};
+
+int copyState(mcx_ctx* c, StateCopy& d, bool save) {
+  struct F { DBuf<float>* snap; DBuf<float>* live; } fs[] = {
+      {&d.te, &c->te}, {&d.ne, &c->ne}, {&d.teOld, &c->teOld}, {&d.neOld, &c->neOld}, {&d.ionDen, &c->ionDen}};
+  struct I { DBuf<int32_t>* snap; DBuf<int32_t>* live; } is[] = {
+      {&d.conv, &c->lgConverged}, {&d.black, &c->lgBlack}, {&d.nIterT, &c->nIterT}};
+  for (auto& f : fs) {
+    if (save && f.snap->n != f.live->n) CK(f.snap->alloc(f.live->n), "alloc state copy");
+    CK(cudaMemcpyAsync(save ? f.snap->p : f.live->p, save ? f.live->p : f.snap->p, f.live->bytes(),
+                       cudaMemcpyDeviceToDevice, c->stream), "state copy");
+  }
+  for (auto& f : is) {
+    if (save && f.snap->n != f.live->n) CK(f.snap->alloc(f.live->n), "alloc state copy");
+    CK(cudaMemcpyAsync(save ? f.snap->p : f.live->p, save ? f.live->p : f.snap->p, f.live->bytes(),
+                       cudaMemcpyDeviceToDevice, c->stream), "state copy");
+  }
+  return MCX_OK;
+}
+
+}  // namespace
+
+extern "C" int mcx_line_sensitivities(mcx_ctx* c, const mcx_sens_opts* o, mcx_sens_out* out) {
+  if (!c || !o || !out || !out->L || (o->n_lines > 0 && !o->lines) || (o->n_abun > 0 && !o->abun_z))
+    return fail(c, MCX_ERR_INPUT, "mcx_line_sensitivities: null argument");
+  if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_line_sensitivities: no model loaded");
+  if (!c->lgGas || !c->balance) return fail(c, MCX_ERR_STATE, "mcx_line_sensitivities: the grid holds no gas");
+  if (c->nNeb > 0) return fail(c, MCX_ERR_STATE, "mcx_line_sensitivities: not for a batch");
+  if (o->n_lines < 1 || o->n_abun < 0) return fail(c, MCX_ERR_INPUT, "mcx_line_sensitivities: no lines");
+  const double h = o->h != 0. ? o->h : 1.e-3;
+  const int nL = o->n_lines, C = c->nCells;
+  const size_t C1 = (size_t)C + 1;
+  // the requested lines as (atom slot, lower, upper)
+  std::vector<int32_t> req(3 * (size_t)nL);
+  for (int k = 0; k < nL; ++k) {
+    const mcx_line_ref& l = o->lines[k];
+    int slot = -1;
+    for (size_t a = 0; a < c->lineAtoms.size(); ++a)
+      if (c->lineAtoms[a].elem == l.elem && c->lineAtoms[a].ion == l.ion) slot = (int)a;
+    if (slot < 0) return fail(c, MCX_ERR_INPUT, "mcx_line_sensitivities: no multi-level data for line " + std::to_string(k));
+    const int n = c->lineAtoms[slot].nLev;
+    if (l.lower < 1 || l.upper <= l.lower || l.upper > n ||
+        c->lineAtoms[slot].fac[(size_t)(l.lower - 1) * n + (l.upper - 1)] == 0.)
+      return fail(c, MCX_ERR_INPUT, "mcx_line_sensitivities: line " + std::to_string(k) + " has no transition");
+    req[3 * k] = slot; req[3 * k + 1] = l.lower; req[3 * k + 2] = l.upper;
+  }
+  for (int q = 0; q < o->n_abun; ++q)
+    if (o->abun_z[q] < 1 || o->abun_z[q] > 30 || c->xrefAll[o->abun_z[q] - 1] <= 0)
+      return fail(c, MCX_ERR_INPUT, "mcx_line_sensitivities: element " + std::to_string(o->abun_z[q]) + " is not on");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  DBuf<int32_t> dReq;
+  DBuf<double> cellL;
+  CK(upload(dReq, req), "upload line requests");
+  CK(cellL.alloc((size_t)nL * C1), "alloc line cells");
+  LineCellArgs la{};
+  la.te = c->te.p; la.ne = c->ne.p; la.ionDen = c->ionDen.p; la.hden = c->hden.p; la.vol = c->volD.p;
+  la.black = c->lgBlack.p; la.req = dReq.p; la.out = cellL.p; la.nReq = nL;
+  mcx_balance_opts bo{};
+  bo.precision = o->precision;
+  std::vector<double> base((size_t)nL * C1), pert((size_t)nL * C1);
+  auto balanceAndLines = [&](std::vector<double>& dst) -> int {
+    int rc = mcx_balance(c, &bo, nullptr);
+    if (rc != MCX_OK) return rc;
+    CK(launchLineCellLuminosities(*c->balance, la, c->stream), "line cells");
+    CK(cudaMemcpyAsync(dst.data(), cellL.p, dst.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "d2h");
+    CK(cudaStreamSynchronize(c->stream), "mcx_line_sensitivities");
+    return MCX_OK;
+  };
+  auto total = [&](const std::vector<double>& v, int k) {
+    double t = 0.;
+    for (size_t cell = 1; cell < C1; ++cell) t += v[(size_t)k * C1 + cell];
+    return t;
+  };
+  StateCopy s0, s1;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  CK(cudaEventCreate(&t0), "event");
+  CK(cudaEventCreate(&t1), "event");
+  CK(cudaEventRecord(t0, c->stream), "event");
+  int rc = copyState(c, s0, true);
+  if (rc == MCX_OK) rc = balanceAndLines(base);
+  if (rc == MCX_OK) rc = copyState(c, s1, true);
+  if (rc == MCX_OK)
+    for (int k = 0; k < nL; ++k) out->L[k] = total(base, k);
+  // every density at once: each cell answers for itself under the fixed J
+  if (rc == MCX_OK && out->dL_dhden) {
+    std::vector<float> hd(C1), hdp(C1);
+    CK(cudaMemcpy(hd.data(), c->hden.p, C1 * sizeof(float), cudaMemcpyDeviceToHost), "d2h Hden");
+    for (size_t cell = 0; cell < C1; ++cell) hdp[cell] = (float)((double)hd[cell] * (1. + h));
+    CK(cudaMemcpy(c->hden.p, hdp.data(), C1 * sizeof(float), cudaMemcpyHostToDevice), "h2d Hden");
+    rc = copyState(c, s0, false);
+    if (rc == MCX_OK) rc = balanceAndLines(pert);
+    CK(cudaMemcpy(c->hden.p, hd.data(), C1 * sizeof(float), cudaMemcpyHostToDevice), "h2d Hden");
+    if (rc == MCX_OK)
+      for (int k = 0; k < nL; ++k)
+        for (size_t cell = 0; cell < C1; ++cell) {
+          const double dh = (double)hdp[cell] - (double)hd[cell];
+          out->dL_dhden[(size_t)k * C1 + cell] =
+              (cell > 0 && dh != 0.) ? (pert[(size_t)k * C1 + cell] - base[(size_t)k * C1 + cell]) / dh : 0.;
+        }
+  }
+  // one balance per abundance
+  for (int q = 0; rc == MCX_OK && out->dL_dabun && q < o->n_abun; ++q) {
+    const int z = o->abun_z[q];
+    float& ab = c->balance->dev.abun[z];
+    const float a0 = ab;
+    ab = (float)((double)a0 * (1. + h));
+    const double da = (double)ab - (double)a0;
+    invalidateBalanceGraphs(*c->balance);
+    rc = copyState(c, s0, false);
+    if (rc == MCX_OK) rc = balanceAndLines(pert);
+    ab = a0;
+    invalidateBalanceGraphs(*c->balance);
+    if (rc == MCX_OK)
+      for (int k = 0; k < nL; ++k) out->dL_dabun[(size_t)k * o->n_abun + q] = (total(pert, k) - out->L[k]) / da;
+  }
+  if (rc == MCX_OK) rc = copyState(c, s1, false);
+  cudaEventRecord(t1, c->stream);
+  cudaEventSynchronize(t1);
+  cudaEventElapsedTime(&out->kernel_ms, t0, t1);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  if (rc == MCX_OK) CK(cudaStreamSynchronize(c->stream), "mcx_line_sensitivities");
+  return rc;
+}
+
 extern "C" int mcx_timer_start(mcx_ctx* c) {
   if (!c) return MCX_ERR_INPUT;
   CK(cudaEventRecord(c->tev0, c->stream), "timer");

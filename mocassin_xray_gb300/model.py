@@ -259,6 +259,25 @@ class Context:
                     wav=wav.reshape(30, 30, S, 30).transpose(3, 2, 1, 0).copy(),
                     te_vol=te_vol.reshape(S, 30).T.copy(), ion_vol=ion_vol.reshape(S, 30).T.copy())
 
+    def line_sensitivities(self, lines, abun_z=(), h: float = 1e-3, precision: int = abi.BAL_MIXED,
+                           per_cell: bool = True) -> dict:
+        """Frozen-field sensitivities (mcx_line_sensitivities): with the context's J fixed, the outputGas
+        volume sums L of the forbidden lines `lines` [(elem, ion, lower, upper), ...], dL/dHden per cell
+        ([n_lines, nCells+1]) and dL/d(elemAbun) of the elements `abun_z` ([n_lines, len(abun_z)]),
+        by forward differences of relative step h."""
+        n = len(lines)
+        refs = (abi.LineRef * n)(*[abi.LineRef(*map(int, l)) for l in lines])
+        z = np.ascontiguousarray(np.asarray(abun_z, dtype=np.int32))
+        L = np.zeros(n)
+        dh = np.zeros((n, self._cells + 1)) if per_cell else None
+        da = np.zeros((n, max(len(z), 1)))
+        o = abi.SensOpts(n_lines=n, n_abun=len(z), lines=C.cast(refs, C.c_void_p),
+                         abun_z=z.ctypes.data if len(z) else None, h=h, precision=precision)
+        out = abi.SensOut(L=L.ctypes.data, dL_dhden=dh.ctypes.data if per_cell else None,
+                          dL_dabun=da.ctypes.data if len(z) else None)
+        self._check(lib().mcx_line_sensitivities(self._h, C.byref(o), C.byref(out)))
+        return dict(L=L, dL_dhden=dh, dL_dabun=da[:, :len(z)], kernel_ms=float(out.kernel_ms))
+
     def state_save(self) -> None:
         """Device-side snapshot of Te, Ne, ionDen, TeOld, NeOld, lgConverged."""
         self._check(lib().mcx_state_save(self._h))
