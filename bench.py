@@ -62,6 +62,8 @@ def parse():
                     help="lognormal41: one 41^3 nebula (the headline); batch256: 256 small H+He nebulae "
                          "in one batched context")
     ap.add_argument("--nebulae", type=int, default=256, help="nebulae of the batch256 workload")
+    ap.add_argument("--converge-iterations", type=int, default=12,
+                    help="iteration limit of the time-to-converged-grid runs (0 = skip them)")
     return ap.parse_args()
 
 
@@ -278,6 +280,72 @@ def config_dict(args, setup) -> dict:
 
 
 # ------------------------------------------------------------------ GPU arm
+CONVERGED_TE_CHANGE = 0.01      # converged: the H+-weighted mean Te changes by less than 1 % between iterations
+
+
+def ionised_mean_te(ctx, setup, vol) -> float:
+    """T(H+) of outputGas's temperature.out: Te weighted by n(H+) Hden dV over the cells with lgBlack < 1."""
+    from mocassin_xray_gb300 import abi
+    i = setup.info
+    C1 = i.n_cells + 1
+    xh = int(setup.get(abi.SARR_ELEM_XREF)[0]) - 1
+    te = ctx.get(abi.ARR_TE).astype(np.float64)
+    black = ctx.get(abi.ARR_LG_BLACK)
+    ion = ctx.get(abi.ARR_IONDEN).reshape(i.nstages, max(i.n_elem_used, 1), C1)
+    w = ion[1, xh].astype(np.float64) * setup.get(abi.ARR_HDEN) * vol
+    w[0] = 0.0
+    w[black > 0] = 0.0
+    return float((te * w).sum() / w.sum())
+
+
+def to_converged_grid(ctx, setup, n: int, counter0: int, plain: bool, max_it: int) -> dict:
+    """Iterations from the deck's initial state until T(H+), the ionised gas's mean temperature, changes by
+    less than CONVERGED_TE_CHANGE between two iterations (or max_it): wall time including the per-iteration
+    test, the T(H+) history, iterateMC's own converged-cell percentage and the final outputGas lines.
+    Per-cell Te changes are no criterion here: Monte Carlo noise keeps them near 2 % at 1e7 packets, and
+    the neutral gas beyond the ionisation front, heated by almost nothing, walks iterateT's x1.2 steps
+    towards a few K without converging."""
+    from mocassin_xray_gb300 import abi
+    vol = ctx.get(abi.ARR_VOLUME).astype(np.float64)
+    ctx.state_restore()
+    ctx.sync()
+    t0 = time.perf_counter()
+    hist, conv_pct, conv = [], [], False
+    for it in range(1, max_it + 1):
+        ctx.opacity(it)
+        ctx.emission(it, precision=abi.PHASE_EXACT if plain else abi.PHASE_MIXED)
+        ctx.transport(n, seed=4242, counter_base=counter0 + (it - 1) * (1 << 40),
+                      precision=abi.PREC_FP64 if plain else abi.PREC_FP32_GEOM, zero=True, n_photons_norm=n)
+        ctx.normalize_j()
+        bs = ctx.balance(precision=abi.BAL_FP64 if plain else abi.BAL_MIXED)
+        hist.append(ionised_mean_te(ctx, setup, vol))
+        conv_pct.append(100.0 * bs.converged / setup.n_cells)
+        if it >= 2 and abs(hist[-1] / hist[-2] - 1.0) < CONVERGED_TE_CHANGE:
+            conv = True
+            break
+    ctx.sync()
+    wall = time.perf_counter() - t0
+    return {"s": wall, "iterations": len(hist), "converged": conv, "t_h_plus": hist,
+            "iteratemc_converged_pct": conv_pct, "lines": ctx.line_luminosities()}
+
+
+def line_agreement(a: dict, b: dict, floor: float = 0.01) -> dict:
+    """Relative differences of a's outputGas lines against b's: Hbeta, T(H+) and T(O++), and every
+    forbidden, hydrogenic and HeI line brighter than `floor` x Hbeta in b (the line arrays are relative
+    to Hbeta)."""
+    out = {"hbeta": abs(a["hbeta_vol"] / b["hbeta_vol"] - 1.0),
+           "t_h_plus": abs(a["te_vol"][0, 1] / b["te_vol"][0, 1] - 1.0),
+           "t_o_plus2": abs(a["te_vol"][7, 2] / b["te_vol"][7, 2] - 1.0)}
+    diffs = []
+    for key in ("forb", "hydro", "hei"):
+        ref, val = np.asarray(b[key]), np.asarray(a[key])
+        m = np.isfinite(ref) & np.isfinite(val) & (ref > floor)
+        diffs.extend(np.abs(val[m] / ref[m] - 1.0).tolist())
+    out.update(lines=len(diffs), max_rel=float(max(diffs)) if diffs else None,
+               mean_rel=float(np.mean(diffs)) if diffs else None)
+    return out
+
+
 def run_gpu(args, dist, ws, rank, local):
     import torch
     from mocassin_xray_gb300 import Context, Setup, abi
@@ -341,6 +409,19 @@ def run_gpu(args, dist, ws, rank, local):
     plain = [step(10_000 + i, plain=True) for i in range(args.plain_steps)] if args.plain_steps > 0 else []
     plain_ms = float(np.mean([sum(p.values()) for _, _, p in plain])) if plain else None
 
+    # time to a converged grid, production against the plain FP64 path, with the line fluxes compared
+    conv = None
+    if args.converge_iterations > 0:
+        prod = to_converged_grid(ctx, setup, n, base, plain=False, max_it=args.converge_iterations)
+        ref64 = to_converged_grid(ctx, setup, n, base, plain=True, max_it=args.converge_iterations)
+        keys = ("s", "iterations", "converged", "t_h_plus", "iteratemc_converged_pct")
+        conv = {"criterion": f"|T(H+) change| < {CONVERGED_TE_CHANGE:g} between iterations (T(H+): Te weighted "
+                             "by n(H+) Hden dV, temperature.out)",
+                "production": {k: prod[k] for k in keys},
+                "plain_fp64_gpu": {k: ref64[k] for k in keys},
+                "speedup": ref64["s"] / prod["s"],
+                "lines_vs_plain_fp64": line_agreement(prod["lines"], ref64["lines"])}
+
     # e2e: the same step through the C ABI from pinned host memory, the updated state read back
     te = torch.from_numpy(setup.get(abi.ARR_TE)).pin_memory()
     ne = torch.from_numpy(setup.get(abi.ARR_NE)).pin_memory()
@@ -399,6 +480,7 @@ def run_gpu(args, dist, ws, rank, local):
             "ms_per_step": plain_ms, "value": ws * n / (plain_ms / 1e3),
             "phase_ms": {k: float(np.mean([p[k] for _, _, p in plain])) for k in plain[0][2]},
             "speedup_of_production": plain_ms / ms_step},
+        "time_to_converged_grid": conv,
         "transport": {k: float(np.mean([getattr(s, k) for s in tst])) for k in
                       ("crossings", "interactions", "absorptions", "scatterings", "escaped", "line_escapes",
                        "emissions", "trapped", "kernel_ms")},

@@ -284,7 +284,21 @@ int  mcx_emission(mcx_ctx* ctx, const mcx_phase_opts* opts, mcx_phase_stats* sta
 typedef struct mcx_balance_opts {
     int32_t precision;          /* MCX_BAL_*                                            */
     int32_t max_rounds;         /* T-iteration cap; 0 = 20 (maxIterateT)                */
-    int32_t reserved[6];
+    int32_t atom_solves;        /* MCX_BAL_MIXED: 1 = solve every ion's levels in every cell and
+                                   T-iteration instead of reading the cooling surfaces (ln of each
+                                   ion's line cooling per ion tabulated over ln Te, ln Ne once per
+                                   context, 4-point Lagrange in both; ~1e-6 relative)     */
+    int32_t converge;           /* 1 = converge every cell tightly instead of iterateT's stopping
+                                   rules: heating - cooling to 1e-9 of their mean and ionBalance's
+                                   X(H0), X(He0), X(He+) changes to 1e-9 (MCX_BAL_MIXED: 1e-6 and
+                                   1e-5), a residual with the ladder not yet converged evaluated
+                                   again at the same Te, Illinois-weighted regula
+                                   falsi without the 100 K step, unbracketed steps x(1 + 1e-4 2^n)
+                                   (at most x1.2) at T-iteration n, up to 64 T-iterations
+                                   (max_rounds up to 64).  The solution is then a smooth function
+                                   of the inputs away from the balance's discontinuities (used for
+                                   derivatives)                                           */
+    int32_t reserved[4];
 } mcx_balance_opts;
 
 typedef struct mcx_balance_stats {
@@ -392,7 +406,19 @@ int  mcx_iterate(mcx_ctx* ctx, const mcx_iterate_opts* opts, mcx_iterate_stats* 
  * the lower and upper level of fLineEm(i,j) in equilibrium) the call returns
  * its outputGas volume sum L (1e-25 erg/s x 1e45 cm^3, before the division by
  * Hbeta), dL/dHden of every cell and dL/d(elemAbun) of every listed element,
- * as forward differences from the unperturbed balance of the current state.
+ * as forward differences from the unperturbed balance of the current state
+ * (central differences: call twice with h and -h).  The balances are converged
+ * tightly unless reference_stopping is set, so the differences approximate
+ * the derivatives of the converged per-cell balance (the implicit-function
+ * derivative of heating = cooling and the ionisation ladder at fixed J).
+ * In that mode a perturbed balance continues from the converged unperturbed
+ * one (whose first steps are small), so that it follows the same branch of
+ * heating = cooling; a cell whose Te still moves by more than max(5|h|, 1e-4) has
+ * crossed a discontinuity of the balance (the reference's charge-exchange fits
+ * switch off below 6000 K and above 5e4 K) and has no derivative there; so has
+ * a cell whose bracket closed on such a jump instead of a root, and a cell
+ * that did not converge in 64 T-iterations has none either: they are left out
+ * of the differences and counted in branch_cells_*.
  * The balance's response to J (the transport) is outside these derivatives.
  * The context is left as after the unperturbed balance.  Gas, one nebula. */
 typedef struct mcx_line_ref {
@@ -406,7 +432,12 @@ typedef struct mcx_sens_opts {
     const int32_t* abun_z;      /* [n_abun] atomic numbers whose abundance is varied    */
     double h;                   /* relative step (may be negative); 0 = 1e-3            */
     int32_t precision;          /* MCX_BAL_* of the balances                            */
-    int32_t reserved[5];
+    int32_t reference_stopping; /* 0: every balance converged tightly (mcx_balance_opts.converge),
+                                   so that L is a smooth function of Hden and the abundances and
+                                   the differences are derivatives of the converged balance;
+                                   1: iterateT's own stopping rules (2 % residual), whose
+                                   discrete stops make the differences noisy            */
+    int32_t reserved[4];
 } mcx_sens_opts;
 
 typedef struct mcx_sens_out {
@@ -415,7 +446,9 @@ typedef struct mcx_sens_out {
     double* dL_dabun;           /* [n_lines][n_abun] or NULL                            */
     float   kernel_ms;          /* out: CUDA-event time of the balances and line sums   */
     float   reserved_f[3];
-    int64_t reserved[4];
+    int64_t branch_cells_hden;  /* out: cells left out of dL_dhden (tight mode)         */
+    int64_t branch_cells_abun;  /* out: cell-balances left out of dL_dabun, summed over the elements */
+    int64_t reserved[2];
 } mcx_sens_out;
 
 int  mcx_line_sensitivities(mcx_ctx* ctx, const mcx_sens_opts* opts, mcx_sens_out* out);

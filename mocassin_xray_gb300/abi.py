@@ -62,7 +62,8 @@ class SetupInfo(C.Structure):
 
 
 class BalanceOpts(C.Structure):
-    _fields_ = [("precision", C.c_int32), ("max_rounds", C.c_int32), ("reserved", C.c_int32 * 6)]
+    _fields_ = [("precision", C.c_int32), ("max_rounds", C.c_int32), ("atom_solves", C.c_int32),
+                ("converge", C.c_int32), ("reserved", C.c_int32 * 4)]
 
 
 class BalanceStats(C.Structure):
@@ -137,12 +138,13 @@ class LineRef(C.Structure):
 
 class SensOpts(C.Structure):
     _fields_ = [("n_lines", C.c_int32), ("n_abun", C.c_int32), ("lines", _P), ("abun_z", _P), ("h", C.c_double),
-                ("precision", C.c_int32), ("reserved", C.c_int32 * 5)]
+                ("precision", C.c_int32), ("reference_stopping", C.c_int32), ("reserved", C.c_int32 * 4)]
 
 
 class SensOut(C.Structure):
     _fields_ = [("L", _P), ("dL_dhden", _P), ("dL_dabun", _P), ("kernel_ms", C.c_float),
-                ("reserved_f", C.c_float * 3), ("reserved", C.c_int64 * 4)]
+                ("reserved_f", C.c_float * 3), ("branch_cells_hden", C.c_int64), ("branch_cells_abun", C.c_int64),
+                ("reserved", C.c_int64 * 2)]
 
 
 class Lines(C.Structure):

@@ -12,7 +12,7 @@
 namespace mcx {
 
 namespace bal_f64 {
-cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStream_t s);
+cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStream_t s, int atomSolves);
 cudaError_t launchForLines(BalanceData& bd, const float* te, const float* ne, const float* ionDen,
                            const uint8_t* compute, float* forLines, cudaStream_t s);
 cudaError_t launchForbSums(BalanceData& bd, const LineSumArgs& a, cudaStream_t s);
@@ -21,7 +21,8 @@ cudaError_t prepare(const BalanceData& bd);
 }  // namespace bal_f64
 namespace bal_mixed {
 cudaError_t prepare(const BalanceData& bd);
-cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStream_t s);
+cudaError_t buildCoolTable(const BalanceData& bd, float* tab, cudaStream_t s);
+cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStream_t s, int atomSolves);
 cudaError_t launchForLines(BalanceData& bd, const float* te, const float* ne, const float* ionDen,
                            const uint8_t* compute, float* forLines, cudaStream_t s);
 }  // namespace bal_mixed
@@ -89,6 +90,11 @@ std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out)
   d.lgBadnell = s.p.lgBadnell; d.lgCompton = s.p.lgCompton;
   d.secIonP = s.secIonP; d.cRecoilHP = s.cRecoilHP; d.cRecoilHeP = s.cRecoilHeP;
   d.xhiLimit = s.p.XHILimit;
+  d.converge = 0;
+  d.maxIterT = kRefRounds;
+  d.resTol = (double)0.02f;
+  d.stepMin = 0.2;
+  d.xTol = 0.01f;
   d.nAtoms = t.nAtoms;
   d.nDiel = (int)(t.diel.size() / 8);
   d.nAldro = (int)(t.aldro.size() / 6);
@@ -229,6 +235,7 @@ std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out)
   d.nIterT = carve<int32_t>(blocks, C1, err);
   d.state = carve<int8_t>(blocks, C1, err);
   d.ibConv = carve<int8_t>(blocks, C1, err);
+  d.side = carve<int8_t>(blocks, C1, err);
   d.counters = carve<BalanceCounters>(blocks, 1, err);
   d.list = carve<int32_t>(blocks, 2 * C1, err);
   d.listCount = carve<unsigned int>(blocks, kMaxRounds + 1, err);
@@ -257,6 +264,8 @@ std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out)
   return "";
 }
 
+void invalidateBalanceGraphs(BalanceData& bd);
+
 namespace {
 bool sameGrid(const BalanceGrid& a, const BalanceGrid& b) {
   return a.jste == b.jste && a.hden == b.hden && a.te == b.te && a.ne == b.ne && a.ionDen == b.ionDen &&
@@ -264,18 +273,48 @@ bool sameGrid(const BalanceGrid& a, const BalanceGrid& b) {
 }
 }  // namespace
 
-cudaError_t launchBalance(BalanceData& bd, const BalanceGrid& g, int maxRounds, int precision, cudaStream_t s) {
+cudaError_t launchBalance(BalanceData& bd, const BalanceGrid& g, int maxRounds, int precision, cudaStream_t s,
+                          int atomSolves, int converge) {
+  {
+    // the stopping rules: the reference's, or tight ones at the level the precision resolves
+    BalanceDev& d = bd.dev;
+    const int want = converge ? 1 : 0;
+    const bool mixed = precision == kBalMixed;
+    const double resTol = want ? (mixed ? 1e-6 : 1e-9) : (double)0.02f;
+    const float xTol = want ? (mixed ? 1e-5f : 1e-9f) : 0.01f;
+    if (d.converge != want || d.resTol != resTol || d.xTol != xTol) {
+      d.converge = want;
+      d.maxIterT = want ? kMaxRounds : kRefRounds;
+      d.resTol = resTol;
+      d.xTol = xTol;
+      d.stepMin = want ? 1e-4 : 0.2;
+      invalidateBalanceGraphs(bd);
+    }
+  }
+  if (precision == kBalMixed && !atomSolves && bd.dev.nAtoms > 0 && !bd.dev.coolTab) {
+    // the cooling surfaces, once per context, before the first graph capture
+    const int slots = (int)(sizeof(bd.blocks) / sizeof(bd.blocks[0]));
+    if (bd.nBlocks >= slots) return cudaErrorMemoryAllocation;
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, (size_t)bd.dev.nAtoms * kCoolNNe * kCoolNTe * sizeof(float));
+    if (e != cudaSuccess) return e;
+    bd.blocks[bd.nBlocks++] = p;
+    e = bal_mixed::buildCoolTable(bd, (float*)p, s);
+    if (e != cudaSuccess) return e;
+    bd.dev.coolTab = (const float*)p;
+  }
   auto direct = [&]() {
-    return precision == kBalMixed ? bal_mixed::launch(bd, g, maxRounds, s) : bal_f64::launch(bd, g, maxRounds, s);
+    return precision == kBalMixed ? bal_mixed::launch(bd, g, maxRounds, s, atomSolves)
+                                  : bal_f64::launch(bd, g, maxRounds, s, 1);
   };
-  if (maxRounds != 20) return direct();
+  if (maxRounds != kRefRounds || atomSolves || converge) return direct();
   const int k = precision == kBalMixed ? 1 : 0;
   if (bd.graph[k] && !sameGrid(bd.graphGrid[k], g)) {
     cudaGraphExecDestroy(bd.graph[k]);
     bd.graph[k] = nullptr;
   }
   if (!bd.graph[k]) {
-    // capture the ~63 launches of one balance once; replays skip their launch overhead
+    // capture the launches of one balance once; replays skip their launch overhead
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return direct();

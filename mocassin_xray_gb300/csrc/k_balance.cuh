@@ -3,19 +3,31 @@
 //
 // The reference recurses per cell (iterateT calls itself up to maxIterateT =
 // 20 times, ionBalance up to 15 times).  Here every cell advances one
-// T-iteration per round, and a round is three launches over the cells still
+// T-iteration per round, and a round is launches over the cells still
 // iterating:
-//   rates   (thread per cell)         calcAlpha, photoionisation, collisional
+//   rates   (warp per cell)           calcAlpha, photoionisation, collisional
 //                                     ionisation, compton, ionBalance, and the
 //                                     thermBalance terms that need no atom solve
 //   atoms   (thread per cell and ion) forLines: equilibrium of every ion with
 //                                     data, summed to that ion's line cooling
+//                                     (FP64 balance, or on request)
 //   secant  (thread per cell)         heating - cooling, the bracketing secant
-//                                     step, convergence and the cell's results
+//                                     step, convergence and the cell's results;
+//                                     in the mixed balance it reads each ion's
+//                                     line cooling from its cooling surface
 // A J-only pass before the first round integrates the photoionisation rates
 // and Compton sums, which the reference recomputes on every T-iteration from
-// the same J.  Two precisions: FP64 throughout, or FP32 rates with FP64 level
-// populations, ionisation ladder and Te bracketing (k_balance_impl.cuh).
+// the same J.  Two precisions: FP64 throughout, or FP32 rates, ladder and
+// level populations with FP64 Te bracketing (k_balance_impl.cuh).
+//
+// Cooling surfaces (mixed balance).  Without the recombination term an ion's
+// level populations, and so the sum G(Te, Ne) = sum_j n_j sum_i a(j,i) E_ji of
+// its forLines cooling per ion, depend on Te and Ne alone (not on the cell).
+// ln G of every atom is tabulated once per context on a grid uniform in ln Te
+// (1e2..1e6 K, 1024 nodes) and ln Ne (1e-2..1e9 cm^-3, 512 nodes) from the same
+// FP32 state-reduction solve, and read back by 4-point Lagrange interpolation
+// in both directions (relative error of G ~1e-6, the size of the solve's own
+// FP32 error); cells outside the grid solve their atoms directly.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -28,7 +40,14 @@ namespace mcx {
 struct Setup;
 struct LineSumArgs;
 
-constexpr int kMaxRounds = 20;   // maxIterateT (source/update_mod.f90:106-107)
+constexpr int kRefRounds = 20;   // maxIterateT (source/update_mod.f90:106-107)
+constexpr int kMaxRounds = 64;   // T-iterations of the tightly converged balance
+
+constexpr int kCoolNTe = 1024, kCoolNNe = 512;
+constexpr double kCoolLnTe0 = 4.6051701859880914;    // ln 1e2
+constexpr double kCoolLnTe1 = 13.815510557964274;    // ln 1e6
+constexpr double kCoolLnNe0 = -4.6051701859880914;   // ln 1e-2
+constexpr double kCoolLnNe1 = 20.723265836946411;    // ln 1e9
 
 // One photoionised shell (elem, ion, shell) of an element that is on.
 struct PhotoShell {
@@ -53,6 +72,17 @@ struct BalanceDev {
   int32_t metaDoubles;         // its per-block element tables, in doubles
   int32_t secIonP, cRecoilHP, cRecoilHeP;
   float xhiLimit;
+  // T-iteration controls: the reference's (2 % residual, 1 % X(H0), X(He0),
+  // X(He+) changes, 20 T-iterations, the 100 K step of a collapsed bracket),
+  // or tight (converge = 1): residual 1e-9, X changes 1e-9 (mixed: 1e-6, 1e-5),
+  // up to kMaxRounds T-iterations, a residual whose ladder has not converged
+  // evaluated again at the same Te, Illinois-weighted regula falsi until the
+  // bracket is 1e-12 wide, and unbracketed steps that start small (a converged
+  // state stays on its branch of heating = cooling) and double up to x1.2
+  int32_t converge, maxIterT;
+  double resTol;
+  double stepMin;              // tight mode: unbracketed steps 1 + stepMin 2^n at T-iteration n, at most 1.2
+  float xTol;
   int32_t xref[31];            // elementXref by Z (index 1..30), 0 = off
   int32_t zOf[31];             // Z of used element e (1-based)
   float abun[31];              // elemAbun by Z
@@ -80,6 +110,7 @@ struct BalanceDev {
   const double* atomData;
   const float* atomDataF;      // the same values in FP32 (mixed precision)
   const double* linePow;       // [nAtoms][kMaxLevels+1] sum over lines from level j of a(j,i) E_ji > 0
+  const float* coolTab;        // [nAtoms][kCoolNNe][kCoolNTe] ln G, built before the first mixed balance
   // per-cell work, [k][C+1] (cell fastest)
   double* ion;                 // [nstages][nElemUsed]
   double* gam;                 // [nShellsTot] photoionisation rate (J integral; the rates kernel adds the reverse charge exchange to its copy)
@@ -97,6 +128,8 @@ struct BalanceDev {
   int32_t* nIterT;
   int8_t* state;               // 0 iterating, 1 done, 2 no photon hit
   int8_t* ibConv;
+  int8_t* side;                // tight mode: bracket end replaced last (1 low, 2 high); 3 = the
+                               // bracket closed on a discontinuity of heating - cooling
   BalanceCounters* counters;
 };
 
@@ -129,7 +162,10 @@ constexpr int kBalMixed = 1;   // FP32 rates / splines / exponentials, FP64 solv
 // updateCell for every cell: up to maxRounds T-iterations (the reference's
 // maxIterateT = 20).  Asynchronous on the stream; counters are left in
 // BalanceDev::counters.
-cudaError_t launchBalance(BalanceData& b, const BalanceGrid& g, int maxRounds, int precision, cudaStream_t s);
+// atomSolves = 1: the mixed balance solves every ion's levels per cell and
+// T-iteration instead of reading the cooling surfaces.
+cudaError_t launchBalance(BalanceData& b, const BalanceGrid& g, int maxRounds, int precision, cudaStream_t s,
+                          int atomSolves = 0, int converge = 0);
 
 // The forLines line total of every cell with compute[c] = 1 (the emission
 // phase's normFor, rec = .true., units of 1e-25 erg/s per gas density) from

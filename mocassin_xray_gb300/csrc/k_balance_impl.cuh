@@ -277,6 +277,7 @@ __global__ void loadStateKernel(BalanceDev b, const float* __restrict__ te, cons
   b.tHigh[cell] = 0.; b.tLow[cell] = 0.; b.resHigh[cell] = 0.; b.resLow[cell] = 0.;
   b.nIterT[cell] = 0;
   b.ibConv[cell] = 1;
+  b.side[cell] = 0;
 }
 
 // -------------------------------------------------------------- one round
@@ -495,7 +496,7 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
     real dHI = (xAt(b, m, w, zH, 1) - HIOld) / HIOld;
     real dHeI = heOn ? (xAt(b, m, w, zHe, 1) - HeIOld) / HeIOld : (real)0.;
     real dHeII = heOn ? (xAt(b, m, w, zHe, 2) - HeIIOld) / HeIIOld : (real)0.;
-    const real lim = (real)RD(0.01);
+    const real lim = (real)b.xTol;
     bool big = fabs(dHI) > lim || fabs(dHeI) > lim || fabs(dHeII) > lim;
     if (big && nIterateX < 15) continue;
     if (big && nIterateX == 15) lgConv = false;
@@ -1168,14 +1169,96 @@ cudaError_t launchForbSums(BalanceData& bd, const LineSumArgs& a, cudaStream_t s
 }
 #endif
 
-// heating - cooling and the secant step of iterateT (FP64 in both precisions)
-__global__ void __launch_bounds__(128) secantKernel(BalanceDev b, int round, int lastRound) {
+#if !MCX_BAL_EXACT
+// ------------------------------------------------------------- cooling surfaces
+
+// ln G(Te, Ne) of every atom at the grid nodes (see k_balance.cuh), one thread
+// per node; G below 1e-37 is stored as 1e-37 (an ion that cools by less is
+// below any cooling rate the balance resolves).
+__global__ void __launch_bounds__(128) coolTableKernel(BalanceDev b, float* tab) {
+  const size_t n = (size_t)b.nAtoms * kCoolNNe * kCoolNTe;
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  const int iT = (int)(idx % kCoolNTe);
+  const int iN = (int)((idx / kCoolNTe) % kCoolNNe);
+  const int atom = (int)(idx / ((size_t)kCoolNTe * kCoolNNe));
+  const double te = exp(kCoolLnTe0 + iT * ((kCoolLnTe1 - kCoolLnTe0) / (kCoolNTe - 1)));
+  const double ne = exp(kCoolLnNe0 + iN * ((kCoolLnNe1 - kCoolLnNe0) / (kCoolNNe - 1)));
+  const double g = equilibriumLines(b, atom, te, ne, 0., false, 1., 1., 1.);
+  tab[idx] = (float)log(fmax(g, 1e-37));
+}
+
+// weights of the 4-point Lagrange interpolant at nodes -1, 0, 1, 2 for t in [0, 1)
+__device__ __forceinline__ void lagrange4(float t, float* w) {
+  const float tm1 = t - 1.f, tm2 = t - 2.f, tp1 = t + 1.f;
+  w[0] = -t * tm1 * tm2 * (1.f / 6.f);
+  w[1] = tp1 * tm1 * tm2 * 0.5f;
+  w[2] = -tp1 * t * tm2 * 0.5f;
+  w[3] = tp1 * t * tm1 * (1.f / 6.f);
+}
+
+// The forLines cooling of a cell summed over its ions (the secant's forSum
+// total), each ion's G read from its cooling surface.  The stencil is
+// interpolated as differences from its (iN, iT) node so that the FP32 sums
+// keep the precision of the stored values.
+__device__ double surfaceCooling(const BalanceDev& b, const CellIdx& c, double te, double ne) {
+  const double sT = (log(te) - kCoolLnTe0) * ((kCoolNTe - 1) / (kCoolLnTe1 - kCoolLnTe0));
+  const double sN = (log(ne) - kCoolLnNe0) * ((kCoolNNe - 1) / (kCoolLnNe1 - kCoolLnNe0));
+  const bool inside = sT >= 1. && sT < kCoolNTe - 2 && sN >= 1. && sN < kCoolNNe - 2;
+  int iT = 1, iN = 1;
+  float wT[4], wN[4];
+  if (inside) {
+    iT = (int)sT;
+    iN = (int)sN;
+    lagrange4((float)(sT - iT), wT);
+    lagrange4((float)(sN - iN), wN);
+  }
+  double total = 0.;
+  for (int atom = 0; atom < b.nAtoms; ++atom) {
+    const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
+    const int elem = h[kAtElem], ion = h[kAtIon];
+    const double w = (double)b.abun[elem] * ionAt(b, c, elem, ion);
+    if (w < kNegligibleIon) continue;
+    double g;
+    if (inside) {
+      const float* t = b.coolTab + ((size_t)atom * kCoolNNe + (iN - 1)) * kCoolNTe + (iT - 1);
+      const float ref = __ldg(t + kCoolNTe + 1);
+      float acc = 0.f;
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        const float* row = t + (size_t)a * kCoolNTe;
+        const float r = wT[0] * (__ldg(row) - ref) + wT[1] * (__ldg(row + 1) - ref) + wT[2] * (__ldg(row + 2) - ref) +
+                        wT[3] * (__ldg(row + 3) - ref);
+        acc += wN[a] * r;
+      }
+      g = (double)expf(ref) * (double)expf(acc);
+    } else {
+      g = equilibriumLines(b, atom, te, ne, 0., false, 1., 1., 1.);
+    }
+    total = total + w * RD(1.9865e-16) * g;
+  }
+  return total;
+}
+#endif
+
+// heating - cooling and the secant step of iterateT (FP64 in both precisions);
+// useSurfaces (mixed balance): the ions' line cooling from the cooling
+// surfaces instead of the atoms kernel's forSum
+__global__ void __launch_bounds__(128) secantKernel(BalanceDev b, int round, int lastRound, int useSurfaces) {
   const int li = blockIdx.x * blockDim.x + threadIdx.x;
   if ((unsigned)li >= b.listCount[round]) return;
   const int C1 = b.nCells + 1;
   const int cell = b.list[(size_t)(round & 1) * C1 + li];
   double coolColl = b.coolHex[cell];
-  for (int a = 0; a < b.nAtoms; ++a) coolColl = coolColl + b.forSum[(size_t)a * C1 + cell];
+#if !MCX_BAL_EXACT
+  if (useSurfaces) {
+    if (b.nAtoms > 0) coolColl = coolColl + surfaceCooling(b, CellIdx{cell, C1}, b.te[cell], b.ne[cell]);
+  } else
+#endif
+  {
+    (void)useSurfaces;
+    for (int a = 0; a < b.nAtoms; ++a) coolColl = coolColl + b.forSum[(size_t)a * C1 + cell];
+  }
   const double ne = b.ne[cell];
   double heat = b.heat[cell];
   double cool = b.coolA[cell] + coolColl + b.coolCollH[cell];
@@ -1188,22 +1271,55 @@ __global__ void __launch_bounds__(128) secantKernel(BalanceDev b, int round, int
   double te = b.te[cell];
   double Thigh = b.tHigh[cell], Tlow = b.tLow[cell], resHigh = b.resHigh[cell], resLow = b.resLow[cell];
   bool done = true;
-  if (fabs(res) >= RD(0.02) * (fabs(cool) + fabs(heat)) / 2.) {
-    if (nIterateT < 20) {
-      if (res < 0.) {
-        resLow = res;
-        Tlow = te;
-        if (Thigh != 0.) te = Tlow - (Thigh - Tlow) * resLow / (resHigh - resLow);
-        else te = te / RD(1.2);
+  const bool tight = b.converge != 0;
+  // tight mode: a residual whose ionisation ladder has not converged is evaluated again at the same Te
+  // (the X-iterations go on from where they stopped) rather than taken as a bracket end
+  const bool xPending = tight && !b.ibConv[cell];
+  bool open = xPending || fabs(res) >= b.resTol * (fabs(cool) + fabs(heat)) / 2.;
+  if (open && !xPending && tight && Thigh != 0. && Tlow != 0. && fabs(Thigh - Tlow) <= 1e-12 * (Thigh + Tlow)) {
+    open = false;
+    // closed on the rounding noise of the residual, or on a jump of heating - cooling (not a root)
+    if (fabs(res) > 1e3 * b.resTol * (fabs(cool) + fabs(heat)) / 2.) b.side[cell] = 3;
+  }
+  if (open) {
+    if (nIterateT < b.maxIterT) {
+      if (xPending) {
+      } else if (tight) {
+        // Illinois: an end kept twice in a row has its residual halved
+        const int8_t last = b.side[cell];
+        if (res < 0.) {
+          if (last == 1 && Thigh != 0.) resHigh = resHigh * 0.5;
+          resLow = res;
+          Tlow = te;
+          b.side[cell] = 1;
+        } else {
+          if (last == 2 && Tlow != 0.) resLow = resLow * 0.5;
+          resHigh = res;
+          Thigh = te;
+          b.side[cell] = 2;
+        }
+        if (Thigh != 0. && Tlow != 0.) {
+          te = Tlow - (Thigh - Tlow) * resLow / (resHigh - resLow);
+        } else {
+          const double f = 1. + fmin(0.2, b.stepMin * ldexp(1., min(nIterateT, 60)));
+          te = res < 0. ? te / f : te * f;
+        }
       } else {
-        resHigh = res;
-        Thigh = te;
-        if (Tlow != 0.) te = Tlow - (Thigh - Tlow) * resLow / (resHigh - resLow);
-        else te = te * RD(1.2);
-      }
-      if (nIterateT >= 6 && fabs(Thigh - Tlow) <= (RD(0.002) * (Thigh + Tlow))) {
-        if (res < 0.) { te = Thigh - 100.; Thigh = 0.; }
-        else { te = Tlow + 100.; Tlow = 0.; }
+        if (res < 0.) {
+          resLow = res;
+          Tlow = te;
+          if (Thigh != 0.) te = Tlow - (Thigh - Tlow) * resLow / (resHigh - resLow);
+          else te = te / RD(1.2);
+        } else {
+          resHigh = res;
+          Thigh = te;
+          if (Tlow != 0.) te = Tlow - (Thigh - Tlow) * resLow / (resHigh - resLow);
+          else te = te * RD(1.2);
+        }
+        if (nIterateT >= 6 && fabs(Thigh - Tlow) <= (RD(0.002) * (Thigh + Tlow))) {
+          if (res < 0.) { te = Thigh - 100.; Thigh = 0.; }
+          else { te = Tlow + 100.; Tlow = 0.; }
+        }
       }
       if (te <= 0.) te = 1.;
       done = lastRound != 0;   // a caller-imposed round limit ends the cell here
@@ -1253,8 +1369,14 @@ __global__ void storeKernel(BalanceDev b, BalanceGrid g) {
 #undef RF
 #undef RD
 
-cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStream_t s) {
+cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStream_t s, int atomSolves) {
   BalanceDev& b = bd.dev;
+#if MCX_BAL_EXACT
+  const int useSurfaces = 0;
+  (void)atomSolves;
+#else
+  const int useSurfaces = atomSolves || b.coolTab == nullptr ? 0 : 1;
+#endif
   const int C = b.nCells;
   if (C <= 0) return cudaSuccess;
   const int T = 128, nb = (C + T - 1) / T;
@@ -1265,18 +1387,28 @@ cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStr
   hitComptonKernel<<<nb, T, 0, s>>>(b, g.jste);
   if (b.nShellsTot > 0) shellIntegralsKernel<<<dim3(nb, b.nShellsTot), T, 0, s>>>(b, g.jste);
   loadStateKernel<<<nb, T, 0, s>>>(b, g.te, g.ne, g.ionDen);
-  const int rounds = std::min(std::max(maxRounds, 1), 20);
+  const int rounds = std::min(std::max(maxRounds, 1), (int)b.maxIterT);
   // round r works on the cells listed for it (the first list holds every cell
   // a packet reached; each secant step lists the cells that go on)
   for (int r = 1; r <= rounds; ++r) {
     ratesKernel<<<(C + 3) / 4, 128, ((size_t)b.metaDoubles + 4 * (size_t)b.warpDoubles) * sizeof(double), s>>>(
         b, g.hden, r - 1);
-    if (b.nAtoms > 0) atomsKernel<<<dim3(nb, b.nAtoms), T, 0, s>>>(b, r - 1);
-    secantKernel<<<nb, T, 0, s>>>(b, r - 1, r == rounds && rounds < 20 ? 1 : 0);
+    if (b.nAtoms > 0 && !useSurfaces) atomsKernel<<<dim3(nb, b.nAtoms), T, 0, s>>>(b, r - 1);
+    secantKernel<<<nb, T, 0, s>>>(b, r - 1, r == rounds && rounds < b.maxIterT ? 1 : 0, useSurfaces);
   }
   storeKernel<<<nb, T, 0, s>>>(b, g);
   return cudaGetLastError();
 }
+
+#if !MCX_BAL_EXACT
+// the cooling surfaces of every atom into tab ([nAtoms][kCoolNNe][kCoolNTe] floats)
+cudaError_t buildCoolTable(const BalanceData& bd, float* tab, cudaStream_t s) {
+  const size_t n = (size_t)bd.dev.nAtoms * kCoolNNe * kCoolNTe;
+  if (n == 0) return cudaSuccess;
+  coolTableKernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(bd.dev, tab);
+  return cudaGetLastError();
+}
+#endif
 
 // the rates kernel's dynamic shared memory (four warps of b.warpDoubles doubles)
 cudaError_t prepare(const BalanceData& bd) {

@@ -1376,8 +1376,12 @@ extern "C" int mcx_balance(mcx_ctx* c, const mcx_balance_opts* opts, mcx_balance
   if (opts && opts->precision != MCX_BAL_FP64 && opts->precision != MCX_BAL_MIXED)
     return fail(c, MCX_ERR_INPUT, "mcx_balance: unknown precision");
   const int prec = (opts && opts->precision == MCX_BAL_MIXED) ? kBalMixed : kBalFp64;
-  const int rounds = (opts && opts->max_rounds > 0) ? opts->max_rounds : 20;
-  if (rounds > 20) return fail(c, MCX_ERR_INPUT, "mcx_balance: max_rounds above maxIterateT (20)");
+  const int converge = opts && opts->converge ? 1 : 0;
+  const int roundCap = converge ? kMaxRounds : kRefRounds;
+  const int rounds = (opts && opts->max_rounds > 0) ? opts->max_rounds : roundCap;
+  if (rounds > roundCap)
+    return fail(c, MCX_ERR_INPUT, "mcx_balance: max_rounds above " + std::to_string(roundCap) +
+                                      (converge ? " (tight convergence)" : " (maxIterateT)"));
   CK(cudaSetDevice(c->device), "cudaSetDevice");
   const size_t C1 = (size_t)c->nCells + 1;
   CK(cudaEventRecord(c->ev0, c->stream), "event");
@@ -1385,7 +1389,8 @@ extern "C" int mcx_balance(mcx_ctx* c, const mcx_balance_opts* opts, mcx_balance
   CK(cudaMemcpyAsync(c->teOld.p, c->te.p, C1 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream), "TeOld");
   CK(cudaMemcpyAsync(c->neOld.p, c->ne.p, C1 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream), "NeOld");
   BalanceGrid g{c->jste.p, c->hden.p, c->te.p, c->ne.p, c->ionDen.p, c->lgConverged.p, c->lgBlack.p, c->nIterT.p};
-  CK(launchBalance(*c->balance, g, rounds, prec, c->stream), "balance kernels");
+  CK(launchBalance(*c->balance, g, rounds, prec, c->stream, opts && opts->atom_solves ? 1 : 0, converge),
+     "balance kernels");
   CK(cudaEventRecord(c->ev1, c->stream), "event");
   BalanceCounters h{};
   CK(cudaMemcpyAsync(&h, c->balance->dev.counters, sizeof(h), cudaMemcpyDeviceToHost, c->stream), "d2h counters");
@@ -1656,46 +1661,70 @@ extern "C" int mcx_line_sensitivities(mcx_ctx* c, const mcx_sens_opts* o, mcx_se
   la.black = c->lgBlack.p; la.req = dReq.p; la.out = cellL.p; la.nReq = nL;
   mcx_balance_opts bo{};
   bo.precision = o->precision;
+  const bool tight = !o->reference_stopping;
+  bo.converge = tight ? 1 : 0;
   std::vector<double> base((size_t)nL * C1), pert((size_t)nL * C1);
-  auto balanceAndLines = [&](std::vector<double>& dst) -> int {
+  std::vector<float> teBase(C1), tePert(C1);
+  std::vector<int32_t> nitBase(C1), nitPert(C1);
+  std::vector<int8_t> sideBase(C1), sidePert(C1);
+  auto balanceAndLines = [&](std::vector<double>& dst, std::vector<float>& te, std::vector<int32_t>& nit,
+                             std::vector<int8_t>& side) -> int {
     int rc = mcx_balance(c, &bo, nullptr);
     if (rc != MCX_OK) return rc;
     CK(launchLineCellLuminosities(*c->balance, la, c->stream), "line cells");
     CK(cudaMemcpyAsync(dst.data(), cellL.p, dst.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "d2h");
+    CK(cudaMemcpyAsync(te.data(), c->te.p, C1 * sizeof(float), cudaMemcpyDeviceToHost, c->stream), "d2h Te");
+    CK(cudaMemcpyAsync(nit.data(), c->nIterT.p, C1 * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream), "d2h");
+    CK(cudaMemcpyAsync(side.data(), c->balance->dev.side, C1, cudaMemcpyDeviceToHost, c->stream), "d2h");
     CK(cudaStreamSynchronize(c->stream), "mcx_line_sensitivities");
     return MCX_OK;
   };
-  auto total = [&](const std::vector<double>& v, int k) {
-    double t = 0.;
-    for (size_t cell = 1; cell < C1; ++cell) t += v[(size_t)k * C1 + cell];
-    return t;
+  // tight mode: a cell left out of the differences did not converge in one of the two balances,
+  // or ended one of them on a discontinuity of heating - cooling (its bracket closed on a jump),
+  // or moved its Te by more than a smooth response to a step h can (it crossed a discontinuity)
+  const double jump = std::max(5. * std::fabs(h), 1e-4);
+  auto branched = [&](size_t cell) {
+    return tight && (nitBase[cell] >= kMaxRounds || nitPert[cell] >= kMaxRounds || sideBase[cell] == 3 ||
+                     sidePert[cell] == 3 ||
+                     std::fabs((double)tePert[cell] - (double)teBase[cell]) > jump * (double)teBase[cell]);
   };
+  // perturbed balances: continued from the converged unperturbed state (tight mode, whose first
+  // steps are small), or from the state before the call (iterateT's own stopping rules)
+  auto startPerturbed = [&](StateCopy& s0, StateCopy& s1) { return copyState(c, tight ? s1 : s0, false); };
   StateCopy s0, s1;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   CK(cudaEventCreate(&t0), "event");
   CK(cudaEventCreate(&t1), "event");
   CK(cudaEventRecord(t0, c->stream), "event");
+  out->branch_cells_hden = 0;
+  out->branch_cells_abun = 0;
   int rc = copyState(c, s0, true);
-  if (rc == MCX_OK) rc = balanceAndLines(base);
+  if (rc == MCX_OK) rc = balanceAndLines(base, teBase, nitBase, sideBase);
   if (rc == MCX_OK) rc = copyState(c, s1, true);
   if (rc == MCX_OK)
-    for (int k = 0; k < nL; ++k) out->L[k] = total(base, k);
+    for (int k = 0; k < nL; ++k) {
+      double t = 0.;
+      for (size_t cell = 1; cell < C1; ++cell) t += base[(size_t)k * C1 + cell];
+      out->L[k] = t;
+    }
   // every density at once: each cell answers for itself under the fixed J
   if (rc == MCX_OK && out->dL_dhden) {
     std::vector<float> hd(C1), hdp(C1);
     CK(cudaMemcpy(hd.data(), c->hden.p, C1 * sizeof(float), cudaMemcpyDeviceToHost), "d2h Hden");
     for (size_t cell = 0; cell < C1; ++cell) hdp[cell] = (float)((double)hd[cell] * (1. + h));
     CK(cudaMemcpy(c->hden.p, hdp.data(), C1 * sizeof(float), cudaMemcpyHostToDevice), "h2d Hden");
-    rc = copyState(c, s0, false);
-    if (rc == MCX_OK) rc = balanceAndLines(pert);
+    rc = startPerturbed(s0, s1);
+    if (rc == MCX_OK) rc = balanceAndLines(pert, tePert, nitPert, sidePert);
     CK(cudaMemcpy(c->hden.p, hd.data(), C1 * sizeof(float), cudaMemcpyHostToDevice), "h2d Hden");
     if (rc == MCX_OK)
-      for (int k = 0; k < nL; ++k)
-        for (size_t cell = 0; cell < C1; ++cell) {
-          const double dh = (double)hdp[cell] - (double)hd[cell];
+      for (size_t cell = 0; cell < C1; ++cell) {
+        const double dh = (double)hdp[cell] - (double)hd[cell];
+        const bool skip = cell == 0 || dh == 0. || branched(cell);
+        if (cell > 0 && branched(cell)) ++out->branch_cells_hden;
+        for (int k = 0; k < nL; ++k)
           out->dL_dhden[(size_t)k * C1 + cell] =
-              (cell > 0 && dh != 0.) ? (pert[(size_t)k * C1 + cell] - base[(size_t)k * C1 + cell]) / dh : 0.;
-        }
+              skip ? 0. : (pert[(size_t)k * C1 + cell] - base[(size_t)k * C1 + cell]) / dh;
+      }
   }
   // one balance per abundance
   for (int q = 0; rc == MCX_OK && out->dL_dabun && q < o->n_abun; ++q) {
@@ -1705,12 +1734,21 @@ extern "C" int mcx_line_sensitivities(mcx_ctx* c, const mcx_sens_opts* o, mcx_se
     ab = (float)((double)a0 * (1. + h));
     const double da = (double)ab - (double)a0;
     invalidateBalanceGraphs(*c->balance);
-    rc = copyState(c, s0, false);
-    if (rc == MCX_OK) rc = balanceAndLines(pert);
+    rc = startPerturbed(s0, s1);
+    if (rc == MCX_OK) rc = balanceAndLines(pert, tePert, nitPert, sidePert);
     ab = a0;
     invalidateBalanceGraphs(*c->balance);
-    if (rc == MCX_OK)
-      for (int k = 0; k < nL; ++k) out->dL_dabun[(size_t)k * o->n_abun + q] = (total(pert, k) - out->L[k]) / da;
+    if (rc == MCX_OK) {
+      std::vector<double> dsum(nL, 0.);
+      for (size_t cell = 1; cell < C1; ++cell) {
+        if (branched(cell)) {
+          ++out->branch_cells_abun;
+          continue;
+        }
+        for (int k = 0; k < nL; ++k) dsum[k] += pert[(size_t)k * C1 + cell] - base[(size_t)k * C1 + cell];
+      }
+      for (int k = 0; k < nL; ++k) out->dL_dabun[(size_t)k * o->n_abun + q] = dsum[k] / da;
+    }
   }
   if (rc == MCX_OK) rc = copyState(c, s1, false);
   cudaEventRecord(t1, c->stream);

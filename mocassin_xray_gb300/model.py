@@ -212,9 +212,13 @@ class Context:
         self._check(lib().mcx_transport(self._h, C.byref(o), C.byref(st)))
         return st
 
-    def balance(self, max_rounds: int = 0, precision: int = abi.BAL_FP64) -> abi.BalanceStats:
-        """updateCell for every cell (Te, Ne, ionDen, lgConverged) from the normalised J."""
-        o = abi.BalanceOpts(precision=precision, max_rounds=max_rounds)
+    def balance(self, max_rounds: int = 0, precision: int = abi.BAL_FP64,
+                atom_solves: bool = False, converge: bool = False) -> abi.BalanceStats:
+        """updateCell for every cell (Te, Ne, ionDen, lgConverged) from the normalised J.  atom_solves
+        (mixed precision): solve every ion's levels per cell instead of reading the cooling surfaces;
+        converge: converge every cell tightly instead of iterateT's stopping rules."""
+        o = abi.BalanceOpts(precision=precision, max_rounds=max_rounds, atom_solves=int(atom_solves),
+                            converge=int(converge))
         st = abi.BalanceStats()
         self._check(lib().mcx_balance(self._h, C.byref(o), C.byref(st)))
         return st
@@ -260,11 +264,12 @@ class Context:
                     te_vol=te_vol.reshape(S, 30).T.copy(), ion_vol=ion_vol.reshape(S, 30).T.copy())
 
     def line_sensitivities(self, lines, abun_z=(), h: float = 1e-3, precision: int = abi.BAL_MIXED,
-                           per_cell: bool = True) -> dict:
+                           per_cell: bool = True, reference_stopping: bool = False) -> dict:
         """Frozen-field sensitivities (mcx_line_sensitivities): with the context's J fixed, the outputGas
         volume sums L of the forbidden lines `lines` [(elem, ion, lower, upper), ...], dL/dHden per cell
         ([n_lines, nCells+1]) and dL/d(elemAbun) of the elements `abun_z` ([n_lines, len(abun_z)]),
-        by forward differences of relative step h."""
+        by forward differences of relative step h of tightly converged balances (of balances stopped
+        by iterateT's own rules with reference_stopping)."""
         n = len(lines)
         refs = (abi.LineRef * n)(*[abi.LineRef(*map(int, l)) for l in lines])
         z = np.ascontiguousarray(np.asarray(abun_z, dtype=np.int32))
@@ -272,11 +277,13 @@ class Context:
         dh = np.zeros((n, self._cells + 1)) if per_cell else None
         da = np.zeros((n, max(len(z), 1)))
         o = abi.SensOpts(n_lines=n, n_abun=len(z), lines=C.cast(refs, C.c_void_p),
-                         abun_z=z.ctypes.data if len(z) else None, h=h, precision=precision)
+                         abun_z=z.ctypes.data if len(z) else None, h=h, precision=precision,
+                         reference_stopping=int(reference_stopping))
         out = abi.SensOut(L=L.ctypes.data, dL_dhden=dh.ctypes.data if per_cell else None,
                           dL_dabun=da.ctypes.data if len(z) else None)
         self._check(lib().mcx_line_sensitivities(self._h, C.byref(o), C.byref(out)))
-        return dict(L=L, dL_dhden=dh, dL_dabun=da[:, :len(z)], kernel_ms=float(out.kernel_ms))
+        return dict(L=L, dL_dhden=dh, dL_dabun=da[:, :len(z)], kernel_ms=float(out.kernel_ms),
+                    branch_cells_hden=int(out.branch_cells_hden), branch_cells_abun=int(out.branch_cells_abun))
 
     def state_save(self) -> None:
         """Device-side snapshot of Te, Ne, ionDen, TeOld, NeOld, lgConverged."""

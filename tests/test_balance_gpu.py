@@ -120,6 +120,35 @@ def test_balance_mixed_precision(decks, data_dir, oracle_lib, name):
     ctx.close()
 
 
+@pytest.mark.parametrize("name", ["lognormal_small", "xray_small"])
+def test_cooling_surfaces_match_atom_solves(decks, data_dir, name):
+    """The mixed balance reading each ion's line cooling from its cooling surface (ln G over ln Te, ln Ne,
+    4-point Lagrange) against the same balance solving every ion's levels per cell and T-iteration: Te and
+    Ne to 2e-5, ionic fractions above 1e-6 to 2e-4, on the cells whose T-iteration took the same path."""
+    s = Setup(decks[name], data_dir)
+    ctx = Context(0)
+    ctx.load(s)
+    _run_j(ctx, s, 30000, 11)
+    ctx.state_save()
+    ctx.balance(precision=abi.BAL_MIXED, atom_solves=True)
+    te_a, ne_a = ctx.get(abi.ARR_TE), ctx.get(abi.ARR_NE)
+    ion_a, nit_a = ctx.get(abi.ARR_IONDEN), ctx.get(abi.ARR_N_ITER_T)
+    ctx.state_restore()
+    ctx.balance(precision=abi.BAL_MIXED)
+    te, ne = ctx.get(abi.ARR_TE), ctx.get(abi.ARR_NE)
+    ion, nit = ctx.get(abi.ARR_IONDEN), ctx.get(abi.ARR_N_ITER_T)
+    same = nit[1:] == nit_a[1:]
+    assert same.mean() >= 0.98
+    np.testing.assert_allclose(te[1:][same], te_a[1:][same], rtol=2e-5)
+    np.testing.assert_allclose(ne[1:][same], ne_a[1:][same], rtol=2e-5)
+    C1 = s.n_cells + 1
+    a = ion.reshape(-1, C1)[:, 1:][:, same]
+    b = ion_a.reshape(-1, C1)[:, 1:][:, same]
+    big = b > 1e-6
+    np.testing.assert_allclose(a[big], b[big], rtol=2e-4)
+    ctx.close()
+
+
 def test_emission_forbidden_lines_mixed(decks, data_dir, oracle_lib):
     s = Setup(decks["xray_small"], data_dir)
     ctx = Context(0)

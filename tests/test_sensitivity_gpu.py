@@ -42,37 +42,93 @@ def test_line_sums_match_line_luminosities_and_oracle(iterated, oracle_lib):
         assert r["L"][k] == pytest.approx(o["forb"][z - 1, ion - 1, lo - 1, up - 1] * ohb, rel=1e-9)
 
 
+def _state(ctx):
+    return [(a, ctx.get(a)) for a in (abi.ARR_TE, abi.ARR_NE, abi.ARR_IONDEN)]
+
+
+def _put_state(ctx, st):
+    for a, v in st:
+        ctx.put(a, v)
+
+
 def test_density_derivative_is_local(iterated):
+    """All densities perturbed at once give each cell's own derivative: the central differences of 64
+    random cells, each perturbed alone by +-h under the same J and continued from the same converged
+    state, equal the all-at-once ones; forward and backward differences agree."""
     s, ctx = iterated
+    h = 1e-3
     ctx.state_restore()
-    r = ctx.line_sensitivities(LINES[:2], precision=abi.BAL_MIXED)
+    fwd = ctx.line_sensitivities(LINES[:2], precision=abi.BAL_FP64, h=h)
+    s1 = _state(ctx)                      # the converged unperturbed balance
+    ctx.state_restore()
+    bwd = ctx.line_sensitivities(LINES[:2], precision=abi.BAL_FP64, h=-h)
+    assert fwd["branch_cells_hden"] < 0.03 * s.n_cells and bwd["branch_cells_hden"] < 0.03 * s.n_cells
     hden0 = ctx.get(abi.ARR_HDEN)
-    ctx.state_restore()
-    base = ctx.line_sensitivities(LINES[:2], per_cell=False, precision=abi.BAL_MIXED)["L"]
     black = ctx.get(abi.ARR_LG_BLACK)
-    cells = [c for c in np.linspace(1, s.info.n_cells, 40).astype(int) if black[c] < 1][:16]
+    rng = np.random.default_rng(64)
+    cand = np.nonzero(black[1:] < 1)[0] + 1
+    cells = rng.choice(cand, size=min(64, cand.size), replace=False)
+    _put_state(ctx, s1)
+    base = ctx.line_sensitivities(LINES[:2], per_cell=False, precision=abi.BAL_FP64)["L"]
+    # cells left out of the differences (no convergence, or a discontinuity crossed) carry 0
+    cells = [c for c in cells if fwd["dL_dhden"][0, c] != 0 and bwd["dL_dhden"][0, c] != 0]
+    assert len(cells) >= 60
+    agree = 0
     for c in cells:
-        ctx.state_restore()
-        hd = hden0.copy()
-        hd[c] = np.float32(float(hd[c]) * (1.0 + 1e-3))
-        ctx.put(abi.ARR_HDEN, hd)
-        one = ctx.line_sensitivities(LINES[:2], per_cell=False, precision=abi.BAL_MIXED)["L"]
-        ctx.put(abi.ARR_HDEN, hden0)
-        dh = float(hd[c]) - float(hden0[c])
+        one = {}
+        for sign in (1.0, -1.0):
+            _put_state(ctx, s1)
+            hd = hden0.copy()
+            hd[c] = np.float32(float(hd[c]) * (1.0 + sign * h))
+            ctx.put(abi.ARR_HDEN, hd)
+            one[sign] = (ctx.line_sensitivities(LINES[:2], per_cell=False, precision=abi.BAL_FP64)["L"],
+                         float(hd[c]) - float(hden0[c]))
+            ctx.put(abi.ARR_HDEN, hden0)
+        ok = True
         for k in range(2):
-            fd = (one[k] - base[k]) / dh
-            assert fd == pytest.approx(r["dL_dhden"][k, c], rel=1e-6, abs=1e-9 * abs(base[k]) / dh)
+            (lp, dp), (lm, dm) = one[1.0], one[-1.0]
+            central = 0.5 * ((lp[k] - base[k]) / dp + (lm[k] - base[k]) / dm)
+            ref = 0.5 * (fwd["dL_dhden"][k, c] + bwd["dL_dhden"][k, c])
+            scale = 1e-6 * abs(base[k]) / abs(dp)
+            ok &= abs(central - ref) <= 1e-3 * abs(ref) + scale
+            ok &= abs(fwd["dL_dhden"][k, c] - bwd["dL_dhden"][k, c]) <= 0.02 * abs(ref) + scale
+        agree += ok
+    assert agree >= len(cells) - 1
 
 
-def test_abundance_derivative(iterated):
+@pytest.mark.parametrize("precision", [abi.BAL_FP64, abi.BAL_MIXED])
+def test_abundance_derivative(iterated, precision):
+    """Differences of the tightly converged balance: the forward and backward differences of every
+    line's abundance derivative agree (the reference's 2 % stopping rule makes them disagree)."""
     s, ctx = iterated
     ctx.state_restore()
-    fwd = ctx.line_sensitivities(LINES, abun_z=[8, 7, 10], per_cell=False, h=1e-3)
+    fwd = ctx.line_sensitivities(LINES, abun_z=[8, 7, 10], per_cell=False, h=1e-3, precision=precision)
     ctx.state_restore()
-    bwd = ctx.line_sensitivities(LINES, abun_z=[8, 7, 10], per_cell=False, h=-1e-3)
+    bwd = ctx.line_sensitivities(LINES, abun_z=[8, 7, 10], per_cell=False, h=-1e-3, precision=precision)
     d = fwd["dL_dabun"]
     # every line answers to its own element's abundance.  The sign is not fixed: at O/H = 5e-4 more
-    # oxygen cools the gas enough that [OIII] 5007 falls, the metallicity turnover of the line
+    # oxygen cools the gas enough that [OIII] 5007 can fall, the metallicity turnover of the line
     assert np.all(np.isfinite(d))
     assert d[0, 0] != 0 and d[1, 0] != 0 and d[2, 1] != 0 and d[3, 2] != 0
-    np.testing.assert_allclose(d, bwd["dL_dabun"], rtol=0.05, atol=1e-6 * np.abs(d).max())
+    assert fwd["branch_cells_abun"] < 0.03 * 3 * s.n_cells
+    np.testing.assert_allclose(d, bwd["dL_dabun"], rtol=0.03, atol=1e-3 * np.abs(d).max())
+
+
+def test_tight_balance_is_a_fixed_point(iterated):
+    """The tightly converged balance started again from its own result stays put (Te to 1e-6), and it
+    lies within the reference's 2 % residual stop of the reference-stopped balance."""
+    s, ctx = iterated
+    ctx.state_restore()
+    ctx.balance(precision=abi.BAL_FP64)
+    te_ref = ctx.get(abi.ARR_TE)
+    ctx.state_restore()
+    ctx.balance(precision=abi.BAL_FP64, converge=True)
+    te1, nit1 = ctx.get(abi.ARR_TE), ctx.get(abi.ARR_N_ITER_T)
+    lit = ctx.get(abi.ARR_LG_BLACK)[1:] < 1
+    ctx.balance(precision=abi.BAL_FP64, converge=True)
+    te2 = ctx.get(abi.ARR_TE)
+    ok = lit & (nit1[1:] < 64)
+    assert ok.sum() >= 0.98 * lit.sum()
+    stay = np.abs(te2[1:][ok] / te1[1:][ok] - 1) <= 1e-6
+    assert stay.mean() >= 0.995
+    assert np.median(np.abs(te1[1:][ok] / te_ref[1:][ok] - 1)) < 0.02
