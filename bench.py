@@ -41,9 +41,9 @@ METRIC = "MC packets/s"
 UNIT = "packets/s"
 # kernels of one step: opacity 1; emission 5 (Gaunt table, forbidden lines per
 # ion and their sum, emissivity, CDF transpose); transport 1; J normalisation
-# 1; balance 64 (hit test + Compton sums, shell integrals, state load, 20 rounds
-# x (rates, atoms, secant), store)
-KERNELS_PER_STEP = 1 + 5 + 1 + 1 + 64
+# 1; balance 44 (hit test + Compton sums, shell integrals, state load, 20 rounds
+# x (rates, secant with the cooling surfaces), store)
+KERNELS_PER_STEP = 1 + 5 + 1 + 1 + 44
 
 
 def parse():
