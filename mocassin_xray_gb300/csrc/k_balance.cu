@@ -251,11 +251,16 @@ std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out)
     const int NP = d.nElemUsed * ns, nSh = d.nShellsTot;
     int nHeavy = 0;
     for (int e = 1; e <= d.nElemUsed; ++e) nHeavy += d.zOf[e] >= 3 ? 1 : 0;
-    d.warpDoubles = 3 * NP + nSh + std::max(NP, nSh) + std::max(nHeavy * 3 * (ns + 3), 4 * d.nElemUsed);
+    d.cellReals = 3 * NP + nSh + std::max(NP, nSh) + std::max(nHeavy * 3 * (ns + 3), 4 * d.nElemUsed);
     // zOf, xref, abun (3 x 32 words) and the (element, ion) shell offsets and counts (2 x E x 32 int16)
     d.metaDoubles = (3 * 32 * 4 + 2 * d.nElemUsed * 32 * 2 + 7) / 8;
-    if (((size_t)d.metaDoubles + 4 * (size_t)d.warpDoubles) * sizeof(double) > 200 * 1024)
-      return "balance: too many ions for the rates kernel";
+    // as many warps (4 cells each) per block as fit 200 KB in FP64
+    d.ratesWarps = 0;
+    for (int wps : {4, 2, 1})
+      if (!d.ratesWarps &&
+          ((size_t)d.metaDoubles + (size_t)wps * 4 * (size_t)d.cellReals) * sizeof(double) <= 200 * 1024)
+        d.ratesWarps = wps;
+    if (!d.ratesWarps) return "balance: too many ions for the rates kernel";
     if (nHeavy > 32) return "balance: more than 32 heavy elements";
     cudaError_t e1 = bal_f64::prepare(*bd), e2 = bal_mixed::prepare(*bd);
     if (e1 != cudaSuccess || e2 != cudaSuccess) return "balance: cannot reserve the rates kernel's shared memory";

@@ -5,7 +5,7 @@
 // 20 times, ionBalance up to 15 times).  Here every cell advances one
 // T-iteration per round, and a round is launches over the cells still
 // iterating:
-//   rates   (warp per cell)           calcAlpha, photoionisation, collisional
+//   rates   (8 lanes per cell)        calcAlpha, photoionisation, collisional
 //                                     ionisation, compton, ionBalance, and the
 //                                     thermBalance terms that need no atom solve
 //   atoms   (thread per cell and ion) forLines: equilibrium of every ion with
@@ -68,8 +68,9 @@ struct BalanceDev {
   int32_t lgBadnell, lgCompton;
   int32_t* list;               // [2][C+1] the cells of the current and the next T-iteration round
   unsigned int* listCount;     // [kMaxRounds+1] cells listed for each round
-  int32_t warpDoubles;         // shared memory of one cell of the rates kernel, in doubles
+  int32_t cellReals;           // shared memory of one cell of the rates kernel, in values of the rate precision
   int32_t metaDoubles;         // its per-block element tables, in doubles
+  int32_t ratesWarps;          // warps per block of the rates kernel (4 cells per warp)
   int32_t secIonP, cRecoilHP, cRecoilHeP;
   float xhiLimit;
   // T-iteration controls: the reference's (2 % residual, 1 % X(H0), X(He0),

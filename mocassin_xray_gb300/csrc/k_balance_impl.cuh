@@ -44,6 +44,16 @@ struct CellIdx {
   int cell, C1;
 };
 
+// The rates kernel gives each cell a group of kGroup lanes (kCellsPerWarp
+// cells per warp): the per-ion and per-shell loops stride over the group, the
+// ladders of the heavy elements run one per lane, and the sums in the
+// reference's order run on the group's first lane, four cells at a time.
+constexpr int kGroup = 8, kCellsPerWarp = 32 / kGroup;
+struct Lanes {
+  int gl;           // lane within the cell's group
+  unsigned mask;    // the group's lanes in the warp
+};
+
 __device__ __forceinline__ double& ionAt(const BalanceDev& b, const CellIdx& c, int z, int st) {
   return b.ion[((size_t)(st - 1) * b.nElemUsed + (b.xref[z] - 1)) * c.C1 + c.cell];
 }
@@ -322,7 +332,8 @@ __device__ __forceinline__ real& xAt(const BalanceDev& b, const ElemMeta& m, con
 // the warp's cell; returns lgConv (uniform across the warp).  In the mixed
 // build the ladder runs on the logarithms of its products (FP32 cannot hold
 // the products themselves).
-__device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const WarpCell& w, int lane, double te, double& ne, double hden) {
+__device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const WarpCell& w, const Lanes& L, double te,
+                               double& ne, double hden) {
   const int ns = b.nstages, E = b.nElemUsed;
   const int zH = 1, zHe = 2;
   const bool heOn = m.xref[zHe] > 0;
@@ -335,14 +346,16 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
   const real hdenR = (real)hden;
   real neR = (real)ne;
   real cxHHe[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-  if (lane == 0)
+  if (L.gl == 0)
     for (int elem = 1; elem <= 2; ++elem)
       for (int ion = 1; ion <= min(elem, ns - 1); ++ion) cxHHe[elem][ion] = chexFit(b, elem, ion, teR);
-  // this lane's heavy element (the lane-th element with Z >= 3, in element order)
-  int myE = 0;
+  // this lane's heavy elements (the h-th element with Z >= 3, in element order,
+  // for h = gl, gl + kGroup, ...; at most 32 heavy elements)
+  int myE[32 / kGroup] = {};
+  int nMine = 0;
   for (int e = 1, h = 0; e <= E; ++e)
     if (m.zOf[e] >= 3) {
-      if (h == lane) myE = e;
+      if (h % kGroup == L.gl && nMine < 32 / kGroup) myE[nMine++] = e;
       ++h;
     }
   for (int nIterateX = 1;; ++nIterateX) {
@@ -350,8 +363,8 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
     const real HIOld = xAt(b, m, w, zH, 1);
     const real HeIOld = heOn ? xAt(b, m, w, zHe, 1) : (real)0.;
     const real HeIIOld = heOn ? xAt(b, m, w, zHe, 2) : (real)0.;
-    __syncwarp();
-    if (lane == 0) {
+    __syncwarp(L.mask);
+    if (L.gl == 0) {
       real ionRatio[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
       real ionProd[3][3] = {{1, 1, 1}, {1, 1, 1}, {1, 1, 1}};
       real den[3] = {1, 1, 1};
@@ -388,11 +401,11 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
         }
       }
     }
-    __syncwarp();
+    __syncwarp(L.mask);
     // X(H0) as just updated above (grid%ionDen in the reference)
     const real xH0now = xAt(b, m, w, zH, 1);
-    if (myE > 0) {
-      const int e = myE;
+    for (int q = 0; q < nMine; ++q) {
+      const int e = myE[q];
       const int elem = m.zOf[e];
       int h = 0;
       for (int f = 1; f < e; ++f) h += m.zOf[f] >= 3 ? 1 : 0;
@@ -477,10 +490,10 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
       }
 #endif
     }
-    __syncwarp();
-    // Ne in the reference's order, by lane 0
+    __syncwarp(L.mask);
+    // Ne in the reference's order, by the group's first lane
     real nE = 0;
-    if (lane == 0) {
+    if (L.gl == 0) {
       for (int e = 1; e <= E; ++e) {
         const int elem = m.zOf[e];
         for (int ion = 2; ion <= min(elem + 1, ns); ++ion) {
@@ -491,7 +504,7 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
       nE = nE * hdenR;
       if (nE == (real)0.) nE = 1;
     }
-    neR = __shfl_sync(0xffffffffu, nE, 0);
+    neR = __shfl_sync(L.mask, nE, 0, kGroup);
     ne = (double)neR;
     real dHI = (xAt(b, m, w, zH, 1) - HIOld) / HIOld;
     real dHeI = heOn ? (xAt(b, m, w, zHe, 1) - HeIOld) / HeIOld : (real)0.;
@@ -505,14 +518,17 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
 }
 
 // calcAlpha, photoionisation, collisionalIonisation, compton, ionBalance and
-// the thermBalance terms without forLines, one warp per iterating cell
-// (b.warpDoubles doubles of shared memory per warp).
+// the thermBalance terms without forLines, kGroup lanes per iterating cell
+// (b.cellReals values of the rate precision in shared memory per cell).
 __global__ void __launch_bounds__(128) ratesKernel(BalanceDev b, const float* __restrict__ hdenG, int round) {
   extern __shared__ double wsm[];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int li = blockIdx.x * (blockDim.x >> 5) + wib;   // index into this round's cell list
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, grp = lane / kGroup;
+  const Lanes L{lane % kGroup, ((1u << kGroup) - 1u) << (grp * kGroup)};
+  const int cellsPerBlock = (blockDim.x >> 5) * kCellsPerWarp;
+  const int slot = wib * kCellsPerWarp + grp;
+  const int li = blockIdx.x * cellsPerBlock + slot;   // index into this round's cell list
   const unsigned cnt = b.listCount[round];
-  if ((unsigned)(blockIdx.x * (blockDim.x >> 5)) >= cnt) return;   // the whole block
+  if ((unsigned)(blockIdx.x * cellsPerBlock) >= cnt) return;   // the whole block
   const int C1 = b.nCells + 1, ns = b.nstages, E = b.nElemUsed, NP = E * ns, nSh = b.nShellsTot;
   // the element tables, then one slice per warp
   int32_t* sZ = reinterpret_cast<int32_t*>(wsm);
@@ -530,32 +546,32 @@ __global__ void __launch_bounds__(128) ratesKernel(BalanceDev b, const float* __
     sNs[i] = (int16_t)b.pairNShell[i];
   }
   __syncthreads();
-  if ((unsigned)li >= cnt) return;   // the whole warp
+  if ((unsigned)li >= cnt) return;   // the whole group
   const int cell = b.list[(size_t)(round & 1) * C1 + li];
   const ElemMeta m{sZ, sX, sA, sP0, sNs};
   WarpCell w;
-  w.X = reinterpret_cast<real*>(wsm + b.metaDoubles + (size_t)wib * b.warpDoubles);
+  w.X = reinterpret_cast<real*>(wsm + b.metaDoubles) + (size_t)slot * b.cellReals;
   w.AL = w.X + NP;
   w.CC = w.AL + NP;
   w.PI = w.CC + NP;
   w.T = w.PI + nSh;
   w.LAD = w.T + max(NP, nSh);
-  for (int k = lane; k < NP; k += 32) w.X[k] = (real)b.ion[(size_t)k * C1 + cell];
-  if (lane == 0) b.nIterT[cell] = b.nIterT[cell] + 1;
+  for (int k = L.gl; k < NP; k += kGroup) w.X[k] = (real)b.ion[(size_t)k * C1 + cell];
+  if (L.gl == 0) b.nIterT[cell] = b.nIterT[cell] + 1;
   const double te = b.te[cell];
   const real teR = (real)te;
   double ne = b.ne[cell];
   const double hden = hdenG[cell];
   const real hdenR = (real)hden;
   // calcAlpha, one pair per lane
-  for (int k = lane; k < NP; k += 32) {
+  for (int k = L.gl; k < NP; k += kGroup) {
     const int e = k / ns + 1, ion = k % ns + 1;
     const int elem = m.zOf[e];
     w.AL[k] = ion <= min(ns - 1, elem) ? alphaOf(b, teR, elem, ion) : (real)0.;
   }
   // photoionisation rates per shell
-  for (int t = lane; t < nSh; t += 32) w.PI[t] = (real)b.gam[(size_t)t * C1 + cell];
-  __syncwarp();
+  for (int t = L.gl; t < nSh; t += kGroup) w.PI[t] = (real)b.gam[(size_t)t * C1 + cell];
+  __syncwarp(L.mask);
   real xe = 0;
   for (int e = 1; e <= E; ++e) {
     const int elem = m.zOf[e];
@@ -569,7 +585,7 @@ __global__ void __launch_bounds__(128) ratesKernel(BalanceDev b, const float* __
     heatef = RF(0.9971) * ((real)1. - pow((real)1. - pow(xe, RF(0.2663)), RF(1.3163)));
   }
   // reverse charge exchange: deltaE_k > 1 only for N0 and O0
-  if (lane == 0)
+  if (L.gl == 0)
     for (int k = 0; k < 2; ++k) {
       const int elem = k == 0 ? 7 : 8;
       const real dE = k == 0 ? RF(10863.) : RF(2205.);
@@ -588,7 +604,7 @@ __global__ void __launch_bounds__(128) ratesKernel(BalanceDev b, const float* __
   {
     const real tev = teR * RF(8.617385e-05);
     int firstStop = NP;
-    for (int k = lane; k < NP; k += 32) {
+    for (int k = L.gl; k < NP; k += kGroup) {
       const int e = k / ns + 1, ion = k % ns + 1;
       const int elem = m.zOf[e];
       w.CC[k] = 0;
@@ -599,13 +615,13 @@ __global__ void __launch_bounds__(128) ratesKernel(BalanceDev b, const float* __
       if (u > (real)80.) { firstStop = min(firstStop, k); continue; }
       w.CC[k] = (real)cf[2] * ((real)1. + (real)cf[1] * sqrt(u)) / ((real)cf[3] + u) * pow(u, (real)cf[4]) * exp(-u);
     }
-    for (int o = 16; o > 0; o >>= 1) firstStop = min(firstStop, __shfl_xor_sync(0xffffffffu, firstStop, o));
-    for (int k = lane; k < NP; k += 32)
+    for (int o = kGroup / 2; o > 0; o >>= 1) firstStop = min(firstStop, __shfl_xor_sync(L.mask, firstStop, o, kGroup));
+    for (int k = L.gl; k < NP; k += kGroup)
       if (k >= firstStop) w.CC[k] = 0;
   }
-  __syncwarp();
+  __syncwarp(L.mask);
   // compton, with the state before ionBalance
-  if (b.lgCompton && lane == 0) {
+  if (b.lgCompton && L.gl == 0) {
     const real s1 = (real)b.comp[0 * (size_t)C1 + cell], s2 = (real)b.comp[1 * (size_t)C1 + cell];
     const real rhH = (real)b.comp[2 * (size_t)C1 + cell], rhHe = (real)b.comp[3 * (size_t)C1 + cell];
     real cool = (RF(6.65e-25) * RF(6.75e-10) * teR * s2) / hdenR;
@@ -616,48 +632,48 @@ __global__ void __launch_bounds__(128) ratesKernel(BalanceDev b, const float* __
     b.compHeat[cell] = heat;
     b.compRecoil[cell] = recoil;
   }
-  const bool conv = ionBalanceWarp(b, m, w, lane, te, ne, hden);
-  __syncwarp();
-  for (int k = lane; k < NP; k += 32) b.ion[(size_t)k * C1 + cell] = (double)w.X[k];
+  const bool conv = ionBalanceWarp(b, m, w, L, te, ne, hden);
+  __syncwarp(L.mask);
+  for (int k = L.gl; k < NP; k += kGroup) b.ion[(size_t)k * C1 + cell] = (double)w.X[k];
   // photoIon(2) of every shell for the heating sum (secondary-ionisation tail times heatef)
-  for (int t = lane; t < nSh; t += 32) {
+  for (int t = L.gl; t < nSh; t += kGroup) {
     const size_t o = (size_t)t * C1 + cell;
     w.T[t] = b.shells[t].heavy ? (real)b.heatA[o] + (real)b.heatHi[o] * heatef : (real)b.heatA[o];
   }
-  __syncwarp();
+  __syncwarp(L.mask);
   // thermBalance without forLines: the terms by lane, their sums in the
-  // reference's order by lane 0
+  // reference's order by the group's first lane
   const real neR = (real)ne;
   real* termFF = w.LAD;              // [E] free-free, then recombination, of H-like ions
   real* termRec = w.LAD + E;
   real* termFF2 = w.LAD + 2 * E;     // the same of He-like ions
   real* termRec2 = w.LAD + 3 * E;
-  if (lane < E) {
-    const int e = lane + 1;
+  for (int l = L.gl; l < E; l += kGroup) {
+    const int e = l + 1;
     const int i = m.zOf[e];
-    termFF[lane] = termRec[lane] = termFF2[lane] = termRec2[lane] = 0;
+    termFF[l] = termRec[l] = termFF2[l] = termRec2[l] = 0;
     if (ns > i) {
       real L = log10(teR / (real)(i * i));
       real Np = (real)xAt(b, m, w, i, i + 1) * (real)m.abun[i];
       real betaFF = (real)i * (RF(1.0108464E-11) + RF(9.7930778E-13) * L - RF(6.6433144E-13) * L * L +
                                RF(2.4793747E-13) * L * L * L - RF(2.3938215E-14) * L * L * L * L);
-      termFF[lane] = Np * neR * betaFF * kBoltz() * teR / sqrt(teR);
+      termFF[l] = Np * neR * betaFF * kBoltz() * teR / sqrt(teR);
       real betaRec = (real)i * (RF(9.4255985E-11) - RF(4.04794384E-12) * L - RF(1.0055237E-11) * L * L +
                                 RF(1.99266862E-12) * L * L * L - RF(1.06681387E-13) * L * L * L * L);
-      termRec[lane] = Np * neR * betaRec * kBoltz() * teR / sqrt(teR);
+      termRec[l] = Np * neR * betaRec * kBoltz() * teR / sqrt(teR);
       if (i >= 2) {
         L = log10((real)4. * teR / (real)(i * i));
         Np = (real)xAt(b, m, w, i, i) * (real)m.abun[i];
         betaFF = ((real)i / (real)2.) * (RF(1.070073e-11) - RF(2.5730207e-13) * L + RF(2.109134e-13) * L * L);
-        termFF2[lane] = Np * neR * betaFF * kBoltz() * teR / sqrt(teR);
+        termFF2[l] = Np * neR * betaFF * kBoltz() * teR / sqrt(teR);
         betaRec = ((real)i / (real)2.) * (RF(1.06926e-10) - RF(2.41756e-11) * L + RF(1.14542e-12) * L * L -
                                           RF(5.06535e-13) * L * L * L + RF(9.16745e-14) * L * L * L * L);
-        termRec2[lane] = Np * neR * betaRec * kBoltz() * teR / sqrt(teR);
+        termRec2[l] = Np * neR * betaRec * kBoltz() * teR / sqrt(teR);
       }
     }
   }
   // collisional ionisation cooling per pair into w.AL (alpha is not needed any more)
-  for (int k = lane; k < NP; k += 32) {
+  for (int k = L.gl; k < NP; k += kGroup) {
     const int e = k / ns + 1, ion = k % ns + 1;
     const int elem = m.zOf[e];
     real v = 0;
@@ -668,12 +684,12 @@ __global__ void __launch_bounds__(128) ratesKernel(BalanceDev b, const float* __
     w.AL[k] = v;
   }
   // photoheating per shell into w.T (the photoIon(2) values staged above)
-  for (int t = lane; t < nSh; t += 32) {
+  for (int t = L.gl; t < nSh; t += kGroup) {
     const PhotoShell sh = b.shells[t];
     w.T[t] = w.T[t] * xAt(b, m, w, sh.elem, sh.ion) * (real)m.abun[sh.elem];
   }
-  __syncwarp();
-  if (lane != 0) return;
+  __syncwarp(L.mask);
+  if (L.gl != 0) return;
   b.ibConv[cell] = conv ? 1 : 0;
   b.ne[cell] = ne;
   real coolFF = 0, coolRec = 0;
@@ -1369,6 +1385,8 @@ __global__ void storeKernel(BalanceDev b, BalanceGrid g) {
 #undef RF
 #undef RD
 
+size_t ratesSmem(const BalanceDev& b);
+
 cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStream_t s, int atomSolves) {
   BalanceDev& b = bd.dev;
 #if MCX_BAL_EXACT
@@ -1388,11 +1406,11 @@ cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStr
   if (b.nShellsTot > 0) shellIntegralsKernel<<<dim3(nb, b.nShellsTot), T, 0, s>>>(b, g.jste);
   loadStateKernel<<<nb, T, 0, s>>>(b, g.te, g.ne, g.ionDen);
   const int rounds = std::min(std::max(maxRounds, 1), (int)b.maxIterT);
+  const int cellsPerBlock = b.ratesWarps * kCellsPerWarp;
   // round r works on the cells listed for it (the first list holds every cell
   // a packet reached; each secant step lists the cells that go on)
   for (int r = 1; r <= rounds; ++r) {
-    ratesKernel<<<(C + 3) / 4, 128, ((size_t)b.metaDoubles + 4 * (size_t)b.warpDoubles) * sizeof(double), s>>>(
-        b, g.hden, r - 1);
+    ratesKernel<<<(C + cellsPerBlock - 1) / cellsPerBlock, 32 * b.ratesWarps, ratesSmem(b), s>>>(b, g.hden, r - 1);
     if (b.nAtoms > 0 && !useSurfaces) atomsKernel<<<dim3(nb, b.nAtoms), T, 0, s>>>(b, r - 1);
     secantKernel<<<nb, T, 0, s>>>(b, r - 1, r == rounds && rounds < b.maxIterT ? 1 : 0, useSurfaces);
   }
@@ -1410,10 +1428,13 @@ cudaError_t buildCoolTable(const BalanceData& bd, float* tab, cudaStream_t s) {
 }
 #endif
 
-// the rates kernel's dynamic shared memory (four warps of b.warpDoubles doubles)
+// the rates kernel's dynamic shared memory: the element tables and one slice per cell of the block
+size_t ratesSmem(const BalanceDev& b) {
+  return (size_t)b.metaDoubles * sizeof(double) + (size_t)b.ratesWarps * kCellsPerWarp * b.cellReals * sizeof(real);
+}
+
 cudaError_t prepare(const BalanceData& bd) {
-  const size_t bytes = ((size_t)bd.dev.metaDoubles + 4 * (size_t)bd.dev.warpDoubles) * sizeof(double);
-  return cudaFuncSetAttribute(ratesKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  return cudaFuncSetAttribute(ratesKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ratesSmem(bd.dev));
 }
 
 cudaError_t launchForLines(BalanceData& bd, const float* te, const float* ne, const float* ionDen,
