@@ -41,9 +41,9 @@ METRIC = "MC packets/s"
 UNIT = "packets/s"
 # kernels of one step: opacity 1; emission 5 (Gaunt table, forbidden lines per
 # ion and their sum, emissivity, CDF transpose); transport 1; J normalisation
-# 1; balance 44 (hit test + Compton sums, shell integrals, state load, 20 rounds
-# x (rates, secant with the cooling surfaces), store)
-KERNELS_PER_STEP = 1 + 5 + 1 + 1 + 44
+# 1; balance 64 (hit test + Compton sums, shell integrals, state load, 20 rounds
+# x (rates, line cooling from the cooling surfaces, secant), store)
+KERNELS_PER_STEP = 1 + 5 + 1 + 1 + 64
 
 
 def parse():
@@ -58,9 +58,10 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=0, help="packets of the CPU sample (0 = auto)")
     ap.add_argument("--cpu-cells", type=int, default=0, help="cells of the CPU emission/balance sample (0 = auto)")
     ap.add_argument("--plain-steps", type=int, default=2, help="steps of the plain FP64 path timed beside")
-    ap.add_argument("--workload", default="lognormal41", choices=["lognormal41", "batch256"],
+    ap.add_argument("--workload", default="lognormal41", choices=["lognormal41", "batch256", "dust81"],
                     help="lognormal41: one 41^3 nebula (the headline); batch256: 256 small H+He nebulae "
-                         "in one batched context")
+                         "in one batched context; dust81: the 81^3 dust-only shell (1e8 packets)")
+    ap.add_argument("--tau", type=float, default=1.0, help="tau_V of the dust81 shell")
     ap.add_argument("--nebulae", type=int, default=256, help="nebulae of the batch256 workload")
     ap.add_argument("--converge-iterations", type=int, default=12,
                     help="iteration limit of the time-to-converged-grid runs (0 = skip them)")
@@ -624,6 +625,86 @@ def run_batch(args, dist, ws, rank, local):
     ctx.close()
 
 
+def run_dust(args, dist, ws, rank, local):
+    """The 81^3 dust-only shell (two grain species, 10 sizes, r^-2 between 1e17 and 1e18 cm, tau_V = args.tau;
+    1e8 packets): a step is one MC iteration from the grain state after loading (grain opacity, the grain
+    emission CDF, the transport with scattering, J normalisation and the grain temperatures of every
+    species and size).  The reference adds the grain opacity to the previous iteration's on a dust-only
+    grid, so each step starts from a freshly loaded opacity; the steps are timed one by one with CUDA
+    events on the context's stream and the reloads stay outside the timed intervals."""
+    import torch
+    from mocassin_xray_gb300 import Context, Setup, abi, configs
+    torch.cuda.set_device(local)
+    n = args.packets if args.packets != 10_000_000 else 100_000_000
+    d = Path(tempfile.gettempdir()) / f"mcx_bench_dust81_tau{args.tau:g}"
+    deck = d / "input" / "input.in"
+    if not deck.exists():
+        configs.dust_shell(d, n=81, tau_v=args.tau, packets=n)
+    setup = Setup(deck, DATA_DIR)
+    ctx = Context(local)
+    ctx.load(setup)
+    op0 = ctx.get(abi.ARR_OPACITY)
+    td0 = ctx.get(abi.ARR_TDUST)
+
+    def step(i: int, plain: bool = False):
+        ctx.put(abi.ARR_OPACITY, op0)
+        ctx.put(abi.ARR_TDUST, td0)
+        ctx.sync()
+        ctx.timer_start()
+        ph = {"opacity": ctx.opacity(1).kernel_ms, "emission": ctx.emission(1).kernel_ms}
+        st = ctx.transport(n, seed=100 + i, counter_base=rank * n,
+                           precision=abi.PREC_FP64 if plain else abi.PREC_FP32_GEOM, zero=True, n_photons_norm=n)
+        ph["transport"] = st.kernel_ms
+        ctx.normalize_j()
+        ph["grain_t"] = ctx.balance().kernel_ms
+        return ctx.timer_stop(), st, ph
+
+    for i in range(args.warmup):
+        step(i)
+    barrier(dist)
+    clocks = ClockSampler(local)
+    clocks.start()
+    runs = [step(args.warmup + i) for i in range(args.steps)]
+    clk = clocks.stop()
+    barrier(dist)
+    ms_step = max_over_ranks(dist, float(np.mean([r[0] for r in runs])))
+    plain = [step(10_000 + i, plain=True) for i in range(args.plain_steps)] if args.plain_steps > 0 else []
+    tst = [r[1] for r in runs]
+    upd = np.mean([t.crossings + t.interactions for t in tst])
+    kms = np.mean([t.kernel_ms for t in tst])
+    alg_bytes = upd * 20.0 + np.mean([t.emissions for t in tst]) * math.ceil(math.log2(setup.nbins)) * 4.0
+    achieved = alg_bytes / (kms / 1e3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+    line = {
+        "metric": METRIC, "value": ws * n / (ms_step / 1e3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": f"dust-only shell, 81^3, tau_V = {args.tau:g}, 2 species x 10 sizes, "
+                               f"{setup.nbins}-bin mesh, {n:.0e} packets/iteration",
+                   "n_cells": setup.n_cells, "packets_per_step": n,
+                   "step": "one MC iteration from the loaded grain state: grain opacity, grain emission CDF, "
+                           "transport, J normalisation, grain temperatures",
+                   "timing": "each step timed alone (CUDA events); the opacity and Tdust reloads between steps "
+                             "are outside", "parallelism": "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": "transportKernel<float>", "peak_kind": peak_kind,
+                     "alg_bytes_per_launch": alg_bytes, "kernel_ms": kms},
+        "phase_ms": {k: float(np.mean([r[2][k] for r in runs])) for k in runs[0][2]},
+        "plain_fp64_gpu": None if not plain else {
+            "ms_per_step": float(np.mean([r[0] for r in plain])),
+            "transport_ms": float(np.mean([r[2]["transport"] for r in plain])),
+            "speedup_of_production": float(np.mean([r[0] for r in plain])) / ms_step},
+        "transport": {k: float(np.mean([getattr(t, k) for t in tst])) for k in
+                      ("crossings", "interactions", "absorptions", "scatterings", "escaped", "emissions",
+                       "trapped", "kernel_ms")},
+    }
+    if clk:
+        line["clocks"] = clk
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+
+
 def main():
     args = parse()
     dist, ws, rank, local = dist_init()
@@ -631,6 +712,8 @@ def main():
         run_reference(args, dist, ws, rank)
     elif args.workload == "batch256":
         run_batch(args, dist, ws, rank, local)
+    elif args.workload == "dust81":
+        run_dust(args, dist, ws, rank, local)
     else:
         run_gpu(args, dist, ws, rank, local)
     if dist is not None:

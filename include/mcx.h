@@ -372,8 +372,8 @@ int  mcx_normalize_j(mcx_ctx* ctx);
 /* One pass of iterateMC's loop body (source/iteration_mod.f90:98-1260) for the
  * stellar source: mcx_opacity, mcx_emission, mcx_transport (Jste cleared
  * first), mcx_normalize_j and mcx_balance, in that order on the context's
- * stream.  The balance's launches (44 in MCX_BAL_MIXED, 64 in MCX_BAL_FP64)
- * are captured as a CUDA graph on first use and replayed.  The convergence test of :1270-1480 is left to the caller
+ * stream.  The balance's 64 launches are captured as a CUDA graph on first
+ * use and replayed.  The convergence test of :1270-1480 is left to the caller
  * (stats.balance.converged against nCells and minConvergence). */
 typedef struct mcx_iterate_opts {
     int32_t n_iterate_mc;           /* nIterateMC (1-based): the skip rule applies when > 1 */

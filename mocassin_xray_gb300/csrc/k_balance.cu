@@ -232,6 +232,7 @@ std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out)
                      &d.coolHex, &d.coolCollH, &d.compHeat, &d.compRecoil, &d.compCool};
   for (double** p : scal) *p = carve<double>(blocks, C1, err);
   d.forSum = carve<double>(blocks, (size_t)std::max(t.nAtoms, 1) * C1, err);
+  d.coolAt = carve<CoolAt>(blocks, C1, err);
   d.nIterT = carve<int32_t>(blocks, C1, err);
   d.state = carve<int8_t>(blocks, C1, err);
   d.ibConv = carve<int8_t>(blocks, C1, err);

@@ -8,13 +8,11 @@
 //   rates   (8 lanes per cell)        calcAlpha, photoionisation, collisional
 //                                     ionisation, compton, ionBalance, and the
 //                                     thermBalance terms that need no atom solve
-//   atoms   (thread per cell and ion) forLines: equilibrium of every ion with
-//                                     data, summed to that ion's line cooling
-//                                     (FP64 balance, or on request)
+//   atoms   (thread per cell and ion) forLines: every ion's line cooling, by
+//                                     its equilibrium (FP64 balance, or on
+//                                     request) or read from its cooling surface
 //   secant  (thread per cell)         heating - cooling, the bracketing secant
-//                                     step, convergence and the cell's results;
-//                                     in the mixed balance it reads each ion's
-//                                     line cooling from its cooling surface
+//                                     step, convergence and the cell's results
 // A J-only pass before the first round integrates the photoionisation rates
 // and Compton sums, which the reference recomputes on every T-iteration from
 // the same J.  Two precisions: FP64 throughout, or FP32 rates, ladder and
@@ -24,7 +22,7 @@
 // level populations, and so the sum G(Te, Ne) = sum_j n_j sum_i a(j,i) E_ji of
 // its forLines cooling per ion, depend on Te and Ne alone (not on the cell).
 // ln G of every atom is tabulated once per context on a grid uniform in ln Te
-// (1e2..1e6 K, 1024 nodes) and ln Ne (1e-2..1e9 cm^-3, 512 nodes) from the same
+// (1..1e6 K, 1280 nodes) and ln Ne (1e-6..1e9 cm^-3, 640 nodes) from the same
 // FP32 state-reduction solve, and read back by 4-point Lagrange interpolation
 // in both directions (relative error of G ~1e-6, the size of the solve's own
 // FP32 error); cells outside the grid solve their atoms directly.
@@ -43,10 +41,10 @@ struct LineSumArgs;
 constexpr int kRefRounds = 20;   // maxIterateT (source/update_mod.f90:106-107)
 constexpr int kMaxRounds = 64;   // T-iterations of the tightly converged balance
 
-constexpr int kCoolNTe = 1024, kCoolNNe = 512;
-constexpr double kCoolLnTe0 = 4.6051701859880914;    // ln 1e2
+constexpr int kCoolNTe = 1280, kCoolNNe = 640;
+constexpr double kCoolLnTe0 = 0.;                    // ln 1
 constexpr double kCoolLnTe1 = 13.815510557964274;    // ln 1e6
-constexpr double kCoolLnNe0 = -4.6051701859880914;   // ln 1e-2
+constexpr double kCoolLnNe0 = -13.815510557964274;   // ln 1e-6
 constexpr double kCoolLnNe1 = 20.723265836946411;    // ln 1e9
 
 // One photoionised shell (elem, ion, shell) of an element that is on.
@@ -60,6 +58,12 @@ struct PhotoShell {
 
 struct BalanceCounters {
   unsigned long long noHit, noIonBal, noTeBal, converged, updated, maxIterT;
+};
+
+// A cell's place on the cooling surfaces (iT = -1: outside the grid).
+struct CoolAt {
+  int32_t iT, iN;
+  float tT, tN;
 };
 
 // Device view (by value as a kernel parameter; pointers are device memory).
@@ -112,6 +116,7 @@ struct BalanceDev {
   const float* atomDataF;      // the same values in FP32 (mixed precision)
   const double* linePow;       // [nAtoms][kMaxLevels+1] sum over lines from level j of a(j,i) E_ji > 0
   const float* coolTab;        // [nAtoms][kCoolNNe][kCoolNTe] ln G, built before the first mixed balance
+  CoolAt* coolAt;              // [C+1] the cell's stencil on the surfaces, set by the rates kernel
   // per-cell work, [k][C+1] (cell fastest)
   double* ion;                 // [nstages][nElemUsed]
   double* gam;                 // [nShellsTot] photoionisation rate (J integral; the rates kernel adds the reverse charge exchange to its copy)

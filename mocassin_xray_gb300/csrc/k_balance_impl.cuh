@@ -49,6 +49,10 @@ struct CellIdx {
 // ladders of the heavy elements run one per lane, and the sums in the
 // reference's order run on the group's first lane, four cells at a time.
 constexpr int kGroup = 8, kCellsPerWarp = 32 / kGroup;
+
+#if !MCX_BAL_EXACT
+__device__ CoolAt coolStencil(double te, double ne);
+#endif
 struct Lanes {
   int gl;           // lane within the cell's group
   unsigned mask;    // the group's lanes in the warp
@@ -692,6 +696,9 @@ __global__ void __launch_bounds__(128) ratesKernel(BalanceDev b, const float* __
   if (L.gl != 0) return;
   b.ibConv[cell] = conv ? 1 : 0;
   b.ne[cell] = ne;
+#if !MCX_BAL_EXACT
+  if (b.coolTab) b.coolAt[cell] = coolStencil(te, ne);
+#endif
   real coolFF = 0, coolRec = 0;
   for (int e = 1; e <= E; ++e) {
     if (!(ns > m.zOf[e])) continue;
@@ -1213,68 +1220,73 @@ __device__ __forceinline__ void lagrange4(float t, float* w) {
   w[3] = tp1 * t * tm1 * (1.f / 6.f);
 }
 
-// The forLines cooling of a cell summed over its ions (the secant's forSum
-// total), each ion's G read from its cooling surface.  The stencil is
-// interpolated as differences from its (iN, iT) node so that the FP32 sums
-// keep the precision of the stored values.
-__device__ double surfaceCooling(const BalanceDev& b, const CellIdx& c, double te, double ne) {
+// Where a cell's (Te, Ne) sits on the cooling surfaces: the nodes iT, iN of
+// the 4 x 4 stencil's second row and column and the fractions within the
+// cell of the grid (iT = -1 outside it).
+__device__ CoolAt coolStencil(double te, double ne) {
   const double sT = (log(te) - kCoolLnTe0) * ((kCoolNTe - 1) / (kCoolLnTe1 - kCoolLnTe0));
   const double sN = (log(ne) - kCoolLnNe0) * ((kCoolNNe - 1) / (kCoolLnNe1 - kCoolLnNe0));
-  const bool inside = sT >= 1. && sT < kCoolNTe - 2 && sN >= 1. && sN < kCoolNNe - 2;
-  int iT = 1, iN = 1;
-  float wT[4], wN[4];
-  if (inside) {
-    iT = (int)sT;
-    iN = (int)sN;
-    lagrange4((float)(sT - iT), wT);
-    lagrange4((float)(sN - iN), wN);
+  CoolAt a{-1, -1, 0.f, 0.f};
+  if (sT >= 1. && sT < kCoolNTe - 2 && sN >= 1. && sN < kCoolNNe - 2) {
+    a.iT = (int)sT;
+    a.iN = (int)sN;
+    a.tT = (float)(sT - a.iT);
+    a.tN = (float)(sN - a.iN);
   }
-  double total = 0.;
-  for (int atom = 0; atom < b.nAtoms; ++atom) {
-    const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
-    const int elem = h[kAtElem], ion = h[kAtIon];
-    const double w = (double)b.abun[elem] * ionAt(b, c, elem, ion);
-    if (w < kNegligibleIon) continue;
-    double g;
-    if (inside) {
-      const float* t = b.coolTab + ((size_t)atom * kCoolNNe + (iN - 1)) * kCoolNTe + (iT - 1);
-      const float ref = __ldg(t + kCoolNTe + 1);
-      float acc = 0.f;
+  return a;
+}
+
+// forLines of update_mod with the cooling surfaces: one thread per (listed
+// cell, ion with data), that ion's line cooling into forSum[atom][cell].  The
+// stencil is interpolated as differences from its (iN, iT) node so that the
+// FP32 sums keep the precision of the stored values; cells outside the grid
+// solve the ion directly.
+__global__ void __launch_bounds__(128) surfaceAtomsKernel(BalanceDev b, int round) {
+  const int li = blockIdx.x * blockDim.x + threadIdx.x;
+  const int atom = blockIdx.y;
+  if ((unsigned)li >= b.listCount[round]) return;
+  const int cell = b.list[(size_t)(round & 1) * (b.nCells + 1) + li];
+  const CellIdx c{cell, b.nCells + 1};
+  const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
+  const int elem = h[kAtElem], ion = h[kAtIon];
+  const double w = (double)b.abun[elem] * ionAt(b, c, elem, ion);
+  double* out = b.forSum + (size_t)atom * c.C1 + cell;
+  if (w < kNegligibleIon) {
+    *out = 0.;
+    return;
+  }
+  const CoolAt a = b.coolAt[cell];
+  double g;
+  if (a.iT >= 0) {
+    float wT[4], wN[4];
+    lagrange4(a.tT, wT);
+    lagrange4(a.tN, wN);
+    const float* t = b.coolTab + ((size_t)atom * kCoolNNe + (a.iN - 1)) * kCoolNTe + (a.iT - 1);
+    const float ref = __ldg(t + kCoolNTe + 1);
+    float acc = 0.f;
 #pragma unroll
-      for (int a = 0; a < 4; ++a) {
-        const float* row = t + (size_t)a * kCoolNTe;
-        const float r = wT[0] * (__ldg(row) - ref) + wT[1] * (__ldg(row + 1) - ref) + wT[2] * (__ldg(row + 2) - ref) +
-                        wT[3] * (__ldg(row + 3) - ref);
-        acc += wN[a] * r;
-      }
-      g = (double)expf(ref) * (double)expf(acc);
-    } else {
-      g = equilibriumLines(b, atom, te, ne, 0., false, 1., 1., 1.);
+    for (int r = 0; r < 4; ++r) {
+      const float* row = t + (size_t)r * kCoolNTe;
+      const float v = wT[0] * (__ldg(row) - ref) + wT[1] * (__ldg(row + 1) - ref) + wT[2] * (__ldg(row + 2) - ref) +
+                      wT[3] * (__ldg(row + 3) - ref);
+      acc += wN[r] * v;
     }
-    total = total + w * RD(1.9865e-16) * g;
+    g = (double)expf(ref) * (double)expf(acc);
+  } else {
+    g = equilibriumLines(b, atom, b.te[cell], b.ne[cell], 0., false, 1., 1., 1.);
   }
-  return total;
+  *out = w * RD(1.9865e-16) * g;
 }
 #endif
 
-// heating - cooling and the secant step of iterateT (FP64 in both precisions);
-// useSurfaces (mixed balance): the ions' line cooling from the cooling
-// surfaces instead of the atoms kernel's forSum
-__global__ void __launch_bounds__(128) secantKernel(BalanceDev b, int round, int lastRound, int useSurfaces) {
+// heating - cooling and the secant step of iterateT (FP64 in both precisions)
+__global__ void __launch_bounds__(128) secantKernel(BalanceDev b, int round, int lastRound) {
   const int li = blockIdx.x * blockDim.x + threadIdx.x;
   if ((unsigned)li >= b.listCount[round]) return;
   const int C1 = b.nCells + 1;
   const int cell = b.list[(size_t)(round & 1) * C1 + li];
   double coolColl = b.coolHex[cell];
-#if !MCX_BAL_EXACT
-  if (useSurfaces) {
-    if (b.nAtoms > 0) coolColl = coolColl + surfaceCooling(b, CellIdx{cell, C1}, b.te[cell], b.ne[cell]);
-  } else
-#endif
-  {
-    (void)useSurfaces;
-    for (int a = 0; a < b.nAtoms; ++a) coolColl = coolColl + b.forSum[(size_t)a * C1 + cell];
-  }
+  for (int a = 0; a < b.nAtoms; ++a) coolColl = coolColl + b.forSum[(size_t)a * C1 + cell];
   const double ne = b.ne[cell];
   double heat = b.heat[cell];
   double cool = b.coolA[cell] + coolColl + b.coolCollH[cell];
@@ -1411,8 +1423,12 @@ cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStr
   // a packet reached; each secant step lists the cells that go on)
   for (int r = 1; r <= rounds; ++r) {
     ratesKernel<<<(C + cellsPerBlock - 1) / cellsPerBlock, 32 * b.ratesWarps, ratesSmem(b), s>>>(b, g.hden, r - 1);
-    if (b.nAtoms > 0 && !useSurfaces) atomsKernel<<<dim3(nb, b.nAtoms), T, 0, s>>>(b, r - 1);
-    secantKernel<<<nb, T, 0, s>>>(b, r - 1, r == rounds && rounds < b.maxIterT ? 1 : 0, useSurfaces);
+#if !MCX_BAL_EXACT
+    if (b.nAtoms > 0 && useSurfaces) surfaceAtomsKernel<<<dim3(nb, b.nAtoms), T, 0, s>>>(b, r - 1);
+    else
+#endif
+    if (b.nAtoms > 0) atomsKernel<<<dim3(nb, b.nAtoms), T, 0, s>>>(b, r - 1);
+    secantKernel<<<nb, T, 0, s>>>(b, r - 1, r == rounds && rounds < b.maxIterT ? 1 : 0);
   }
   storeKernel<<<nb, T, 0, s>>>(b, g);
   return cudaGetLastError();
