@@ -161,6 +161,26 @@ std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out)
   rec.resize(s.nbins, 0.f);
   d.xsecRecoil = (const float*)up(rec.data(), rec.size() * sizeof(float));
   d.shells = (const PhotoShell*)up(sh.data(), sh.size() * sizeof(PhotoShell));
+  // the J-free tail of getPhotoRates (radField(IPnuP) times the cross-section sums above the
+  // secondary-ionisation threshold), summed once for the mixed balance
+  {
+    std::vector<float> tail(2 * std::max<size_t>(sh.size(), 1), 0.f);
+    const double hcRyd = (double)2.1799153e-11f;
+    for (size_t k = 0; k < sh.size(); ++k) {
+      const PhotoShell& p = sh[k];
+      if (!p.heavy || p.ipNuP < 1 || p.ipNuP > s.nbins) continue;
+      const int iup = std::min(p.highNuP, s.nbins), ilow = std::max(p.ipNuP + 1, s.secIonP);
+      double g = 0., h = 0.;
+      for (int i = ilow; i <= iup; ++i) {
+        const double ph = s.xSec[(size_t)(i + p.xsecP - p.ipNuP - 1)];
+        g += ph / (hcRyd * (double)s.nu[(size_t)(i - 1)]);
+        h += ph;
+      }
+      tail[2 * k] = (float)g;
+      tail[2 * k + 1] = (float)h;
+    }
+    d.shellTail = (const float*)up(tail.data(), tail.size() * sizeof(float));
+  }
   d.CF = (const float*)up(t.CF, sizeof(t.CF));
   d.cionTherm = (const float*)up(t.cionTherm, sizeof(t.cionTherm));
   d.nauger = (const int32_t*)up(t.nauger, sizeof(t.nauger));

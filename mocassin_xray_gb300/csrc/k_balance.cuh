@@ -97,6 +97,7 @@ struct BalanceDev {
   const float* xsec;
   const float* xsecRecoil;     // [nbins]
   const PhotoShell* shells;    // [nShellsTot]
+  const float* shellTail;      // [nShellsTot][2] sum of xs/(hc nu) and of xs above the secondary-ionisation threshold
   const float* CF;             // [30][30][5]
   const float* cionTherm;      // [30][30]
   const int32_t* nauger;       // [30][30][10]

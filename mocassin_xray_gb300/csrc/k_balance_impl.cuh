@@ -173,7 +173,7 @@ __device__ __forceinline__ const int32_t* outerOf(const BalanceDev& b, int z, in
 // The parts of photoionisation / getPhotoRates / compton that depend on J
 // alone.  hitComptonKernel (one thread per cell) marks the cells no packet
 // reached and forms the Compton sums; shellIntegralsKernel (one thread per
-// (cell, photoionised shell), the shell on the grid's y axis) integrates J
+// (cell, photoionised shell), the shell fastest in the block index) integrates J
 // over each shell's cross section, so that a warp streams one shell's bins of
 // 32 neighbouring cells' J rows.
 __global__ void __launch_bounds__(128) hitComptonKernel(BalanceDev b, const double* __restrict__ jste) {
@@ -182,9 +182,15 @@ __global__ void __launch_bounds__(128) hitComptonKernel(BalanceDev b, const doub
   const int C1 = b.nCells + 1;
   const float* nu = b.nu;
   auto J = [&](int bin1) { return (real)jste[(size_t)(bin1 - 1) * C1 + cell]; };
+  // any J > 0, eight bins in flight at a time
   bool hit = false;
-  for (int i = 1; i <= b.nbins; ++i)
-    if (jste[(size_t)(i - 1) * C1 + cell] > 0.) { hit = true; break; }
+  for (int i0 = 1; i0 <= b.nbins && !hit; i0 += 8) {
+    double v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = i0 + k <= b.nbins ? __ldg(jste + (size_t)(i0 + k - 1) * C1 + cell) : 0.;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) hit = hit || v[k] > 0.;
+  }
   b.state[cell] = hit ? 0 : 2;
   if (!hit) return;
   b.list[atomicAdd(&b.listCount[0], 1u)] = cell;   // the cells of the first T-iteration
@@ -211,8 +217,9 @@ __global__ void __launch_bounds__(128) hitComptonKernel(BalanceDev b, const doub
 }
 
 __global__ void __launch_bounds__(128) shellIntegralsKernel(BalanceDev b, const double* __restrict__ jste) {
-  const int cell = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int t = blockIdx.y;
+  // the shells of one block of cells launch next to each other, so their J rows are read from L2
+  const int t = (int)(blockIdx.x % (unsigned)b.nShellsTot);
+  const int cell = (int)(blockIdx.x / (unsigned)b.nShellsTot) * blockDim.x + threadIdx.x + 1;
   if (cell > b.nCells || b.state[cell] == 2) return;
   const int C1 = b.nCells + 1;
   const float* nu = b.nu;
@@ -264,12 +271,18 @@ __global__ void __launch_bounds__(128) shellIntegralsKernel(BalanceDev b, const 
   g = g + jIP * ph0 / (hcRyd * (real)nu[IPnuP - 1]);
   h = h + jIP * ph0 * (hcRyd * (real)nu[IPnuP - 1] - augerE) / (hcRyd * (real)nu[IPnuP - 1]);
   real gh = 0, hh = 0;
+#if MCX_BAL_EXACT
   const int ilow = max(IPnuP + 1, b.secIonP);
   for (int i = ilow; i <= iup; ++i) {
     real p = xs[i + sh.xsecP - IPnuP - 1];
     gh = gh + jIP * p / (hcRyd * (real)nu[i - 1]);   // radField(IPnuP), as the reference
     hh = hh + jIP * p;
   }
+#else
+  // the same sums with radField(IPnuP) taken out of them (summed once at set-up)
+  gh = jIP * (real)b.shellTail[2 * t];
+  hh = jIP * (real)b.shellTail[2 * t + 1];
+#endif
   g = g + gh;
   hh = hh - gh * augerE;
   b.gam[o] = g;
@@ -1415,7 +1428,7 @@ cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStr
   e = cudaMemsetAsync(b.listCount, 0, sizeof(unsigned) * (kMaxRounds + 1), s);
   if (e != cudaSuccess) return e;
   hitComptonKernel<<<nb, T, 0, s>>>(b, g.jste);
-  if (b.nShellsTot > 0) shellIntegralsKernel<<<dim3(nb, b.nShellsTot), T, 0, s>>>(b, g.jste);
+  if (b.nShellsTot > 0) shellIntegralsKernel<<<(unsigned)b.nShellsTot * (unsigned)nb, T, 0, s>>>(b, g.jste);
   loadStateKernel<<<nb, T, 0, s>>>(b, g.te, g.ne, g.ionDen);
   const int rounds = std::min(std::max(maxRounds, 1), (int)b.maxIterT);
   const int cellsPerBlock = b.ratesWarps * kCellsPerWarp;

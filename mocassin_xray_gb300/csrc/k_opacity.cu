@@ -2,16 +2,19 @@
 //
 // Restates ionizationDriver / BoltGaunt / getGauntFF / eDenSum / addOpacity
 // (source/ionization_mod.f90:26-477) as one kernel: a thread owns one cell
-// and walks the frequency mesh, so that the store kappa[nu][cell] of a warp is
-// one coalesced 128-byte row segment.  The bound-free terms are grouped per
-// frequency bin in a CSR list (built once on the host in the reference's
-// summation order: H, HeI, HeII, then element / ion / shell), every lane of a
-// warp reads the same cross section (a broadcast) and its own ion density
-// from shared memory.  Arithmetic is FP32 as in the reference.
+// and walks one chunk of the frequency mesh (blockIdx.y), so that the store
+// kappa[nu][cell] of a warp is one coalesced 128-byte row segment and the
+// chunks give the SMs enough warps to hide the table reads.  The bound-free
+// terms are grouped per frequency bin in a CSR list (built once on the host
+// in the reference's summation order: H, HeI, HeII, then element / ion /
+// shell), every lane of a warp reads the same cross section (a broadcast) and
+// its own ion density from shared memory.  Arithmetic is FP32 as in the reference.
 // Behaviours of the reference kept here: the free-free prefactor has no H+ or
 // He++ term (density(1,2) and density(2,3) are never filled,
 // source/ionization_mod.f90:71-84), and an empty shell adds one term at bin 2
 // (inOpacity's loop bound, source/ionization_mod.f90:451-476).
+#include <algorithm>
+
 #include "k_opacity.cuh"
 #include "k_gaunt.cuh"
 
@@ -44,7 +47,9 @@ opacityKernel(OpacityDev t, const float* __restrict__ hden, const float* __restr
   const float fac2 = fac1 * Te1Ryd / Te;
   const float* den = sDen + threadIdx.x;
   const int stride = blockDim.x;
-  for (int i = 1; i <= t.nbins; ++i) {
+  const int chunk = (t.nbins + gridDim.y - 1) / gridDim.y;
+  const int i0 = 1 + blockIdx.y * chunk, i1 = min(t.nbins, i0 + chunk - 1);
+  for (int i = i0; i <= i1; ++i) {
     const float nui = t.nu[i - 1];
     const float ex = Te1Ryd / Te + nui;
     const float boltz = ex > 84.f ? 0.f : expf(-ex);
@@ -70,12 +75,14 @@ cudaError_t launchOpacity(const OpacityDev& t, const float* hden, const float* t
   while (threads > 32 && (size_t)t.nSlots * threads * sizeof(float) > 200 * 1024) threads >>= 1;
   if ((size_t)t.nSlots * threads * sizeof(float) > 200 * 1024) return cudaErrorInvalidValue;
   const int blocks = (t.nCells + threads - 1) / threads;
+  // enough blocks for ~8 per SM of the 152, in mesh chunks of at least 32 bins
+  const int chunks = std::max(1, std::min((8 * 152 + blocks - 1) / blocks, t.nbins / 32));
   const size_t smem = (size_t)t.nSlots * threads * sizeof(float);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(opacityKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  opacityKernel<<<blocks, threads, smem, stream>>>(t, hden, te, ne, ionDen, gauntTe, compute, opacity);
+  opacityKernel<<<dim3(blocks, chunks), threads, smem, stream>>>(t, hden, te, ne, ionDen, gauntTe, compute, opacity);
   return cudaGetLastError();
 }
 
