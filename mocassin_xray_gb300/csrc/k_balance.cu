@@ -21,7 +21,7 @@ cudaError_t prepare(const BalanceData& bd);
 }  // namespace bal_f64
 namespace bal_mixed {
 cudaError_t prepare(const BalanceData& bd);
-cudaError_t buildCoolTable(const BalanceData& bd, float* tab, cudaStream_t s);
+cudaError_t buildCoolTable(const BalanceData& bd, float* tab, float* rtab, cudaStream_t s);
 cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStream_t s, int atomSolves);
 cudaError_t launchForLines(BalanceData& bd, const float* te, const float* ne, const float* ionDen,
                            const uint8_t* compute, float* forLines, cudaStream_t s);
@@ -292,6 +292,29 @@ std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out)
 
 void invalidateBalanceGraphs(BalanceData& bd);
 
+// the cooling surfaces (ln G and B of every atom), once per context and before
+// any graph capture that bakes their pointers in
+cudaError_t ensureSurfaces(BalanceData& bd, cudaStream_t s) {
+  if (bd.dev.nAtoms <= 0 || bd.dev.coolTab) return cudaSuccess;
+  const int slots = (int)(sizeof(bd.blocks) / sizeof(bd.blocks[0]));
+  if (bd.nBlocks + 2 > slots) return cudaErrorMemoryAllocation;
+  const size_t bytes = (size_t)bd.dev.nAtoms * kCoolNNe * kCoolNTe * sizeof(float);
+  void* p = nullptr;
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) return e;
+  bd.blocks[bd.nBlocks++] = p;
+  e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess) return e;
+  bd.blocks[bd.nBlocks++] = q;
+  e = bal_mixed::buildCoolTable(bd, (float*)p, (float*)q, s);
+  if (e != cudaSuccess) return e;
+  invalidateBalanceGraphs(bd);
+  bd.dev.coolTab = (const float*)p;
+  bd.dev.recTab = (const float*)q;
+  return cudaSuccess;
+}
+
 namespace {
 bool sameGrid(const BalanceGrid& a, const BalanceGrid& b) {
   return a.jste == b.jste && a.hden == b.hden && a.te == b.te && a.ne == b.ne && a.ionDen == b.ionDen &&
@@ -317,17 +340,9 @@ cudaError_t launchBalance(BalanceData& bd, const BalanceGrid& g, int maxRounds, 
       invalidateBalanceGraphs(bd);
     }
   }
-  if (precision == kBalMixed && !atomSolves && bd.dev.nAtoms > 0 && !bd.dev.coolTab) {
-    // the cooling surfaces, once per context, before the first graph capture
-    const int slots = (int)(sizeof(bd.blocks) / sizeof(bd.blocks[0]));
-    if (bd.nBlocks >= slots) return cudaErrorMemoryAllocation;
-    void* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, (size_t)bd.dev.nAtoms * kCoolNNe * kCoolNTe * sizeof(float));
+  if (precision == kBalMixed && !atomSolves) {
+    cudaError_t e = ensureSurfaces(bd, s);
     if (e != cudaSuccess) return e;
-    bd.blocks[bd.nBlocks++] = p;
-    e = bal_mixed::buildCoolTable(bd, (float*)p, s);
-    if (e != cudaSuccess) return e;
-    bd.dev.coolTab = (const float*)p;
   }
   auto direct = [&]() {
     return precision == kBalMixed ? bal_mixed::launch(bd, g, maxRounds, s, atomSolves)
@@ -365,6 +380,10 @@ cudaError_t launchBalance(BalanceData& bd, const BalanceGrid& g, int maxRounds, 
 
 cudaError_t launchForLinesEmission(BalanceData& bd, const float* te, const float* ne, const float* ionDen,
                                    const uint8_t* compute, float* forLines, int precision, cudaStream_t s) {
+  if (precision == kBalMixed) {
+    cudaError_t e = ensureSurfaces(bd, s);
+    if (e != cudaSuccess) return e;
+  }
   return precision == kBalMixed ? bal_mixed::launchForLines(bd, te, ne, ionDen, compute, forLines, s)
                                 : bal_f64::launchForLines(bd, te, ne, ionDen, compute, forLines, s);
 }

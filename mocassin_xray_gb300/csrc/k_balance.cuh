@@ -117,6 +117,8 @@ struct BalanceDev {
   const float* atomDataF;      // the same values in FP32 (mixed precision)
   const double* linePow;       // [nAtoms][kMaxLevels+1] sum over lines from level j of a(j,i) E_ji > 0
   const float* coolTab;        // [nAtoms][kCoolNNe][kCoolNTe] ln G, built before the first mixed balance
+  const float* recTab;         // [nAtoms][kCoolNNe][kCoolNTe] B: the slope of forLines in ionDenUp with the
+                               // recombination term (emission phase), built with coolTab
   CoolAt* coolAt;              // [C+1] the cell's stencil on the surfaces, set by the rates kernel
   // per-cell work, [k][C+1] (cell fastest)
   double* ion;                 // [nstages][nElemUsed]

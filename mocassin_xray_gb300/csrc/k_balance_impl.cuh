@@ -52,6 +52,7 @@ constexpr int kGroup = 8, kCellsPerWarp = 32 / kGroup;
 
 #if !MCX_BAL_EXACT
 __device__ CoolAt coolStencil(double te, double ne);
+__device__ __forceinline__ float2 surfaceAt(const float* tab, int atom, const CoolAt& a);
 #endif
 struct Lanes {
   int gl;           // lane within the cell's group
@@ -851,8 +852,9 @@ __device__ __forceinline__ void collisionPairs(const BalanceDev& b, const int32_
 // of a few FP32 ulps whatever the spread of the rates; the unpivoted LU of the
 // reference cancels and needs FP64.  Returns false (the caller falls back to
 // the FP64 LU) when a level has no exit to the levels below it.
-__device__ __forceinline__ bool gthPops(const BalanceDev& b, const int32_t* h, double Ne, double ionDenUp, bool rec,
-                                        const double* alphaTotal, real TeR, real sqrTe, real log10Te, double* y) {
+__device__ __forceinline__ bool gthParts(const BalanceDev& b, const int32_t* h, double Ne, double srcMul, bool rec,
+                                         const double* alphaTotal, real TeR, real sqrTe, real log10Te, float* u,
+                                         float* v) {
   const int n = h[kAtNLev];
   const float* A = b.atomDataF + h[kAtOffA];
   const float NeF = (float)Ne;
@@ -864,7 +866,7 @@ __device__ __forceinline__ bool gthPops(const BalanceDev& b, const int32_t* h, d
     R[up][lo] = NeF * qUpLo + A[(size_t)(up - 1) * n + (lo - 1)];
   });
   float src[kMaxLevels + 1], Dk[kMaxLevels + 1];
-  for (int i = 1; i <= n; ++i) src[i] = (rec && i >= 2) ? (float)(Ne * ionDenUp * alphaTotal[i]) : 0.f;
+  for (int i = 1; i <= n; ++i) src[i] = (rec && i >= 2) ? (float)(srcMul * alphaTotal[i]) : 0.f;
   for (int k = n; k >= 2; --k) {
     float d = 0.f;
     for (int j = 1; j < k; ++j) d += R[k][j];
@@ -882,10 +884,8 @@ __device__ __forceinline__ bool gthPops(const BalanceDev& b, const int32_t* h, d
         for (int j = 2; j < k; ++j) src[j] += fs * R[k][j];
     }
   }
-  float u[kMaxLevels + 1], v[kMaxLevels + 1];
   u[1] = 1.f;
   v[1] = 0.f;
-  float su = 0.f, sv = 0.f;
   for (int k = 2; k <= n; ++k) {
     float a = 0.f, c = rec ? src[k] : 0.f;
     for (int i = 1; i < k; ++i) {
@@ -894,6 +894,17 @@ __device__ __forceinline__ bool gthPops(const BalanceDev& b, const int32_t* h, d
     }
     u[k] = a / Dk[k];
     v[k] = c / Dk[k];
+  }
+  return true;
+}
+
+__device__ __forceinline__ bool gthPops(const BalanceDev& b, const int32_t* h, double Ne, double ionDenUp, bool rec,
+                                        const double* alphaTotal, real TeR, real sqrTe, real log10Te, double* y) {
+  float u[kMaxLevels + 1], v[kMaxLevels + 1];
+  if (!gthParts(b, h, Ne, Ne * ionDenUp, rec, alphaTotal, TeR, sqrTe, log10Te, u, v)) return false;
+  const int n = h[kAtNLev];
+  float su = 0.f, sv = 0.f;
+  for (int k = 2; k <= n; ++k) {
     su += u[k];
     sv += v[k];
   }
@@ -908,17 +919,13 @@ __device__ __forceinline__ bool gthPops(const BalanceDev& b, const int32_t* h, d
 // (source/emission_mod.f90:2884-2984).  Collision rates in the rate
 // precision; the FP64 path solves the rate matrix by the reference's
 // unpivoted LU, the mixed path by FP32 state reduction (gthPops).
-__device__ __forceinline__ void equilibriumPops(const BalanceDev& b, int atom, double Te, double Ne, double ionDenUp,
-                                                bool rec, double* y) {
-  const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
+// the recombination coefficients of equilibrium's source term, alphaTotal[1..nLev]
+// (source/emission_mod.f90:2836-2880)
+__device__ __forceinline__ void recAlphas(const BalanceDev& b, const int32_t* h, real TeR, double* alphaTotal) {
   const double* DD = b.atomData;
   const int nLev = h[kAtNLev];
-  const double* A = DD + h[kAtOffA];
-  const real TeR = (real)Te;
-  const real sqrTe = sqrt(TeR), log10Te = log10(TeR);
-  double alphaTotal[kMaxLevels + 1];
   for (int i = 0; i <= nLev; ++i) alphaTotal[i] = 0.;
-  if (rec) {
+  {
     const double* rr = DD + h[kAtOffRec];
     const real one = (real)1.;
     if (h[kAtRecType] == kRecPowerLaw) {
@@ -946,6 +953,20 @@ __device__ __forceinline__ void equilibriumPops(const BalanceDev& b, int atom, d
       }
     }
   }
+}
+
+__device__ __forceinline__ void equilibriumPops(const BalanceDev& b, int atom, double Te, double Ne, double ionDenUp,
+                                                bool rec, double* y) {
+  const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
+  const double* DD = b.atomData;
+  const int nLev = h[kAtNLev];
+  const double* A = DD + h[kAtOffA];
+  const real TeR = (real)Te;
+  const real sqrTe = sqrt(TeR), log10Te = log10(TeR);
+  double alphaTotal[kMaxLevels + 1];
+  if (rec) recAlphas(b, h, TeR, alphaTotal);
+  else
+    for (int i = 0; i <= nLev; ++i) alphaTotal[i] = 0.;
 #if !MCX_BAL_EXACT
   if (gthPops(b, h, Ne, ionDenUp, rec, alphaTotal, TeR, sqrTe, log10Te, y)) return;
 #endif
@@ -1111,6 +1132,51 @@ __global__ void __launch_bounds__(128) forLinesAtomsKernel(BalanceDev b, const f
   b.forSum[(size_t)atom * C1 + cell] = v;
 }
 
+#if !MCX_BAL_EXACT
+// The emission phase's forLines from the surfaces: each cell placed on the
+// grid once, then one thread per (cell, ion with data) forms
+// (G + ionDenUp B) elemAbun ionDen 1.9865e9; cells outside the grid solve
+// the ion directly.
+__global__ void __launch_bounds__(128) surfaceStencilKernel(BalanceDev b, const float* __restrict__ te,
+                                                            const float* __restrict__ ne,
+                                                            const uint8_t* __restrict__ compute) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell > b.nCells || !compute[cell]) return;
+  b.coolAt[cell] = coolStencil((double)te[cell], (double)ne[cell]);
+}
+
+__global__ void __launch_bounds__(128) forLinesSurfaceKernel(BalanceDev b, const float* __restrict__ te,
+                                                             const float* __restrict__ ne,
+                                                             const float* __restrict__ ionDen,
+                                                             const uint8_t* __restrict__ compute) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+  const int atom = blockIdx.y;
+  const int C1 = b.nCells + 1;
+  if (cell >= C1 || !compute[cell]) return;
+  const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
+  const int elem = h[kAtElem], ion = h[kAtIon];
+  const int top = min(elem + 1, b.nstages);
+  const int e = b.xref[elem];
+  const double x = ionDen[((size_t)(ion - 1) * b.nElemUsed + (e - 1)) * C1 + cell];
+  double v = 0.;
+  if ((double)b.abun[elem] * x >= kNegligibleIon) {
+    double up = 0.;
+    if (ion < top && x > 0.) up = (double)ionDen[((size_t)ion * b.nElemUsed + (e - 1)) * C1 + cell] / x;
+    const CoolAt a = b.coolAt[cell];
+    double L;
+    if (a.iT >= 0) {
+      const float2 g = surfaceAt(b.coolTab, atom, a);
+      const float2 r = surfaceAt(b.recTab, atom, a);
+      L = (double)expf(g.x) * (double)expf(g.y) + up * (double)(r.x + r.y);
+    } else {
+      L = equilibriumLines(b, atom, te[cell], ne[cell], up, true, 1., 1., 1.);
+    }
+    v = L * (double)b.abun[elem] * x * RD(1.9865e9);
+  }
+  b.forSum[(size_t)atom * C1 + cell] = v;
+}
+#endif
+
 // normFor of emissionDriver: the ions' line totals summed in the reference's ion order
 __global__ void forLinesSumKernel(BalanceDev b, const uint8_t* __restrict__ compute, float* forLines) {
   const int cell = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1208,10 +1274,41 @@ cudaError_t launchForbSums(BalanceData& bd, const LineSumArgs& a, cudaStream_t s
 #if !MCX_BAL_EXACT
 // ------------------------------------------------------------- cooling surfaces
 
-// ln G(Te, Ne) of every atom at the grid nodes (see k_balance.cuh), one thread
+// G and B of one atom at (Te, Ne): forLines' line sum per ion without the
+// recombination term (G) and its slope in ionDenUp with it (B), so that the
+// sum with the term is G + ionDenUp B.  The state reduction gives both from
+// one solve: with sources Ne alpha_i, n_k = n_1 u_k + ionDenUp w_k and
+// n_1 = (1 - ionDenUp W) / (1 + U), U = sum u_k, W = sum w_k; a level without
+// an exit below it falls back to two LU solves.
+__device__ void surfaceValues(const BalanceDev& b, int atom, double Te, double Ne, double& G, double& B) {
+  const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
+  const int n = h[kAtNLev];
+  const real TeR = (real)Te;
+  const real sqrTe = sqrt(TeR), log10Te = log10(TeR);
+  double alphaTotal[kMaxLevels + 1];
+  recAlphas(b, h, TeR, alphaTotal);
+  float u[kMaxLevels + 1], v[kMaxLevels + 1];
+  if (gthParts(b, h, Ne, Ne, true, alphaTotal, TeR, sqrTe, log10Te, u, v)) {
+    const double* P = b.linePow + (size_t)atom * (kMaxLevels + 1);
+    double U = 0., UP = 0., W = 0., WP = 0.;
+    for (int k = 2; k <= n; ++k) {
+      U += u[k];
+      UP += (double)u[k] * P[k];
+      W += v[k];
+      WP += (double)v[k] * P[k];
+    }
+    G = UP / (1. + U);
+    B = WP - W * G;
+  } else {
+    G = equilibriumLines(b, atom, Te, Ne, 0., false, 1., 1., 1.);
+    B = equilibriumLines(b, atom, Te, Ne, 1., true, 1., 1., 1.) - G;
+  }
+}
+
+// ln G and B of every atom at the grid nodes (see k_balance.cuh), one thread
 // per node; G below 1e-37 is stored as 1e-37 (an ion that cools by less is
 // below any cooling rate the balance resolves).
-__global__ void __launch_bounds__(128) coolTableKernel(BalanceDev b, float* tab) {
+__global__ void __launch_bounds__(128) coolTableKernel(BalanceDev b, float* tab, float* rtab) {
   const size_t n = (size_t)b.nAtoms * kCoolNNe * kCoolNTe;
   const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= n) return;
@@ -1220,8 +1317,10 @@ __global__ void __launch_bounds__(128) coolTableKernel(BalanceDev b, float* tab)
   const int atom = (int)(idx / ((size_t)kCoolNTe * kCoolNNe));
   const double te = exp(kCoolLnTe0 + iT * ((kCoolLnTe1 - kCoolLnTe0) / (kCoolNTe - 1)));
   const double ne = exp(kCoolLnNe0 + iN * ((kCoolLnNe1 - kCoolLnNe0) / (kCoolNNe - 1)));
-  const double g = equilibriumLines(b, atom, te, ne, 0., false, 1., 1., 1.);
+  double g, bb;
+  surfaceValues(b, atom, te, ne, g, bb);
   tab[idx] = (float)log(fmax(g, 1e-37));
+  rtab[idx] = (float)bb;
 }
 
 // weights of the 4-point Lagrange interpolant at nodes -1, 0, 1, 2 for t in [0, 1)
@@ -1249,6 +1348,27 @@ __device__ CoolAt coolStencil(double te, double ne) {
   return a;
 }
 
+// A surface of atom `atom` ([nAtoms][kCoolNNe][kCoolNTe]) at the stencil a:
+// 4-point Lagrange in both directions, summed as differences from the
+// stencil's (iN, iT) node so that the FP32 sums keep the stored precision;
+// returns the node value and the interpolated difference.
+__device__ __forceinline__ float2 surfaceAt(const float* tab, int atom, const CoolAt& a) {
+  float wT[4], wN[4];
+  lagrange4(a.tT, wT);
+  lagrange4(a.tN, wN);
+  const float* t = tab + ((size_t)atom * kCoolNNe + (a.iN - 1)) * kCoolNTe + (a.iT - 1);
+  const float ref = __ldg(t + kCoolNTe + 1);
+  float acc = 0.f;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const float* row = t + (size_t)r * kCoolNTe;
+    const float v = wT[0] * (__ldg(row) - ref) + wT[1] * (__ldg(row + 1) - ref) + wT[2] * (__ldg(row + 2) - ref) +
+                    wT[3] * (__ldg(row + 3) - ref);
+    acc += wN[r] * v;
+  }
+  return make_float2(ref, acc);
+}
+
 // forLines of update_mod with the cooling surfaces: one thread per (listed
 // cell, ion with data), that ion's line cooling into forSum[atom][cell].  The
 // stencil is interpolated as differences from its (iN, iT) node so that the
@@ -1271,20 +1391,9 @@ __global__ void __launch_bounds__(128) surfaceAtomsKernel(BalanceDev b, int roun
   const CoolAt a = b.coolAt[cell];
   double g;
   if (a.iT >= 0) {
-    float wT[4], wN[4];
-    lagrange4(a.tT, wT);
-    lagrange4(a.tN, wN);
-    const float* t = b.coolTab + ((size_t)atom * kCoolNNe + (a.iN - 1)) * kCoolNTe + (a.iT - 1);
-    const float ref = __ldg(t + kCoolNTe + 1);
-    float acc = 0.f;
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const float* row = t + (size_t)r * kCoolNTe;
-      const float v = wT[0] * (__ldg(row) - ref) + wT[1] * (__ldg(row + 1) - ref) + wT[2] * (__ldg(row + 2) - ref) +
-                      wT[3] * (__ldg(row + 3) - ref);
-      acc += wN[r] * v;
-    }
-    g = (double)expf(ref) * (double)expf(acc);
+    // exp of the node value and of the interpolated difference apart: each is exact to an FP32 ulp
+    const float2 r = surfaceAt(b.coolTab, atom, a);
+    g = (double)expf(r.x) * (double)expf(r.y);
   } else {
     g = equilibriumLines(b, atom, b.te[cell], b.ne[cell], 0., false, 1., 1., 1.);
   }
@@ -1448,11 +1557,11 @@ cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStr
 }
 
 #if !MCX_BAL_EXACT
-// the cooling surfaces of every atom into tab ([nAtoms][kCoolNNe][kCoolNTe] floats)
-cudaError_t buildCoolTable(const BalanceData& bd, float* tab, cudaStream_t s) {
+// the surfaces of every atom into tab (ln G) and rtab (B), [nAtoms][kCoolNNe][kCoolNTe] floats each
+cudaError_t buildCoolTable(const BalanceData& bd, float* tab, float* rtab, cudaStream_t s) {
   const size_t n = (size_t)bd.dev.nAtoms * kCoolNNe * kCoolNTe;
   if (n == 0) return cudaSuccess;
-  coolTableKernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(bd.dev, tab);
+  coolTableKernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(bd.dev, tab, rtab);
   return cudaGetLastError();
 }
 #endif
@@ -1471,7 +1580,13 @@ cudaError_t launchForLines(BalanceData& bd, const float* te, const float* ne, co
   BalanceDev& b = bd.dev;
   const int C1 = b.nCells + 1, T = 128, nb = (C1 + T - 1) / T;
   if (b.nAtoms <= 0) return cudaSuccess;
-  forLinesAtomsKernel<<<dim3(nb, b.nAtoms), T, 0, s>>>(b, te, ne, ionDen, compute);
+#if !MCX_BAL_EXACT
+  if (b.coolTab && b.recTab) {
+    surfaceStencilKernel<<<nb, T, 0, s>>>(b, te, ne, compute);
+    forLinesSurfaceKernel<<<dim3(nb, b.nAtoms), T, 0, s>>>(b, te, ne, ionDen, compute);
+  } else
+#endif
+    forLinesAtomsKernel<<<dim3(nb, b.nAtoms), T, 0, s>>>(b, te, ne, ionDen, compute);
   forLinesSumKernel<<<nb, T, 0, s>>>(b, compute, forLines);
   return cudaGetLastError();
 }

@@ -58,10 +58,8 @@ opacityKernel(OpacityDev t, const float* __restrict__ hden, const float* __restr
     float op = boltz < 0.995f ? xb * (1.f - boltz) * g * fac1 : xb * nui * g * fac2;
     const int e0 = t.csrStart[i - 1], e1 = t.csrStart[i];
     for (int e = e0; e < e1; ++e) {
-      const int2 term = t.csrTerm[e];
-      const int xi = i + term.x;   // 1-based index into xSecArray
-      const float xs = (xi >= 1 && xi <= t.nXsec) ? t.xsec[xi - 1] : 0.f;
-      op += xs * den[term.y * stride];
+      const int2 term = __ldg(t.csrTerm + e);
+      op += __int_as_float(term.x) * den[term.y * stride];
     }
     if (t.lgCompton) op += t.KNsigmaT[i - 1] * Ne;
     opacity[(size_t)cell + C1 * (size_t)(i - 1)] = op;

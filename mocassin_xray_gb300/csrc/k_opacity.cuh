@@ -12,7 +12,7 @@ struct OpacityDev {
   const float* xsec;          // [nXsec]
   const float* KNsigmaT;      // [nbins]
   const int32_t* csrStart;    // [nbins+1] bound-free terms of bin i in [csrStart[i-1], csrStart[i])
-  const int2* csrTerm;        // {xSecArray index minus bin index, ion slot}
+  const int2* csrTerm;        // {float bits of the cross section at the bin, ion slot}
   const int32_t* slotPlane;   // [nSlots] ionDen plane (xref-1) + nElemUsed*(ion-1)
   const float* slotAbun;      // [nSlots] elemAbun of the slot's element
   const float* slotFFWeight;  // [nSlots] weight of the slot in the free-free electron sum

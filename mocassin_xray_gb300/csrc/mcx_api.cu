@@ -614,11 +614,19 @@ static void buildOpacityTables(const Setup& s, std::vector<int32_t>& csrStart, s
   std::vector<std::vector<int2>> per(nb + 1);
   for (const auto& r : ranges)
     for (int i = std::max(r.lo, 1); i <= std::min(r.hi, nb); ++i) per[i].push_back(make_int2(r.k, r.slot));
+  // each term carries its cross section at the bin (xSecArray(i + k), 0 outside the table) as float bits
   csrStart.assign(nb + 1, 0);
   csrTerm.clear();
+  const int nX = (int)s.xSec.size();
   for (int i = 1; i <= nb; ++i) {
     csrStart[i - 1] = (int32_t)csrTerm.size();
-    csrTerm.insert(csrTerm.end(), per[i].begin(), per[i].end());
+    for (const int2& t : per[i]) {
+      const int xi = i + t.x;
+      const float xs = (xi >= 1 && xi <= nX) ? s.xSec[(size_t)(xi - 1)] : 0.f;
+      int32_t bits;
+      std::memcpy(&bits, &xs, sizeof bits);
+      csrTerm.push_back(make_int2(bits, t.y));
+    }
   }
   csrStart[nb] = (int32_t)csrTerm.size();
 }
