@@ -40,6 +40,8 @@ template <> struct RMath<float> {
   static __device__ __forceinline__ float sin_(float x) { return sinf(x); }
   static __device__ __forceinline__ float abs_(float x) { return fabsf(x); }
   static __device__ __forceinline__ float min_(float a, float b) { return fminf(a, b); }
+  // the step's quotients: reciprocal-approximation division (2 ulp; operands far below 2^126)
+  static __device__ __forceinline__ float div_(float a, float b) { return __fdividef(a, b); }
 };
 template <> struct RMath<double> {
   static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
@@ -48,6 +50,7 @@ template <> struct RMath<double> {
   static __device__ __forceinline__ double sin_(double x) { return sin(x); }
   static __device__ __forceinline__ double abs_(double x) { return fabs(x); }
   static __device__ __forceinline__ double min_(double a, double b) { return fmin(a, b); }
+  static __device__ __forceinline__ double div_(double a, double b) { return a / b; }
 };
 
 template <typename R>
@@ -177,7 +180,7 @@ __device__ __forceinline__ void deposit(const DevGrid& g, const DevTransportOut&
                                         R dV, R deltaE, R costheta) {
   if (cell <= 0) return;
   size_t idx = (size_t)cell + ((size_t)g.nCells + 1) * (size_t)(nuP - 1);
-  atomicAdd(out.jste + idx, (double)(dl * deltaE / dV));
+  atomicAdd(out.jste + idx, (double)RMath<R>::div_(dl * deltaE, dV));
   if (out.hEst) atomicAdd(out.hEst + idx, (double)((dl * deltaE) * costheta / dV));
 }
 
@@ -292,12 +295,12 @@ __device__ int stepPacket(const DevGrid& g, const Geo& q, const DevTransportIn& 
   R rx = p.x, ry = p.y, rz = p.z, vx = p.vx, vy = p.vy, vz = p.vz;
 
   // wall-snap heuristics (source/photon_mod.f90:1882-1919), signed divisor as in the reference
-  if (xP < nx) { R m = (AXR(X, xP) + AXR(X, xP + 1)) / R(2); if (vx > R(0) && M::abs_(rx - m) / m < R(2.e-2)) xP = xP + 1; }
-  if (xP > 1)  { R m = (AXR(X, xP) + AXR(X, xP - 1)) / R(2); if (vx < R(0) && M::abs_(rx - m) / m < R(2.e-2)) xP = xP - 1; }
-  if (yP < ny) { R m = (AXR(Y, yP) + AXR(Y, yP + 1)) / R(2); if (vy > R(0) && M::abs_(ry - m) / m < R(2.e-2)) yP = yP + 1; }
-  if (yP > 1)  { R m = (AXR(Y, yP) + AXR(Y, yP - 1)) / R(2); if (vy < R(0) && M::abs_(ry - m) / m < R(2.e-2)) yP = yP - 1; }
-  if (zP < nz) { R m = (AXR(Z, zP) + AXR(Z, zP + 1)) / R(2); if (vz > R(0) && M::abs_(rz - m) / m < R(2.e-2)) zP = zP + 1; }
-  if (zP > 1)  { R m = (AXR(Z, zP) + AXR(Z, zP - 1)) / R(2); if (vz < R(0) && M::abs_(rz - m) / m < R(2.e-2)) zP = zP - 1; }
+  if (xP < nx) { R m = (AXR(X, xP) + AXR(X, xP + 1)) / R(2); if (vx > R(0) && M::div_(M::abs_(rx - m), m) < R(2.e-2)) xP = xP + 1; }
+  if (xP > 1)  { R m = (AXR(X, xP) + AXR(X, xP - 1)) / R(2); if (vx < R(0) && M::div_(M::abs_(rx - m), m) < R(2.e-2)) xP = xP - 1; }
+  if (yP < ny) { R m = (AXR(Y, yP) + AXR(Y, yP + 1)) / R(2); if (vy > R(0) && M::div_(M::abs_(ry - m), m) < R(2.e-2)) yP = yP + 1; }
+  if (yP > 1)  { R m = (AXR(Y, yP) + AXR(Y, yP - 1)) / R(2); if (vy < R(0) && M::div_(M::abs_(ry - m), m) < R(2.e-2)) yP = yP - 1; }
+  if (zP < nz) { R m = (AXR(Z, zP) + AXR(Z, zP + 1)) / R(2); if (vz > R(0) && M::div_(M::abs_(rz - m), m) < R(2.e-2)) zP = zP + 1; }
+  if (zP > 1)  { R m = (AXR(Z, zP) + AXR(Z, zP - 1)) / R(2); if (vz < R(0) && M::div_(M::abs_(rz - m), m) < R(2.e-2)) zP = zP - 1; }
 
   // distances from the walls (source/photon_mod.f90:1933-2084); with one
   // mother grid the reference's inner loop runs exactly once
@@ -309,33 +312,33 @@ __device__ int stepPacket(const DevGrid& g, const Geo& q, const DevTransportIn& 
   R dSx, dSy, dSz;
   bool lost = false;
   if (vx > R(0)) {
-    if (xP < nx) { dSx = ((AXR(X, xP + 1) + AXR(X, xP)) / R(2) - rx) / vx;
+    if (xP < nx) { dSx = M::div_((AXR(X, xP + 1) + AXR(X, xP)) / R(2) - rx, vx);
                    if (M::abs_(dSx) < R(1.e-5)) { rx = (AXR(X, xP + 1) + AXR(X, xP)) / R(2); xP = xP + 1; } }
-    else { dSx = (AXR(X, nx) - rx) / vx; if (M::abs_(dSx) < R(1.e-5)) { rx = AXR(X, nx); lost = true; } }
+    else { dSx = M::div_(AXR(X, nx) - rx, vx); if (M::abs_(dSx) < R(1.e-5)) { rx = AXR(X, nx); lost = true; } }
   } else if (vx < R(0)) {
-    if (xP > 1) { dSx = ((AXR(X, xP) + AXR(X, xP - 1)) / R(2) - rx) / vx;
+    if (xP > 1) { dSx = M::div_((AXR(X, xP) + AXR(X, xP - 1)) / R(2) - rx, vx);
                   if (M::abs_(dSx) < R(1.e-5)) { rx = (AXR(X, xP) + AXR(X, xP - 1)) / R(2); xP = xP - 1; } }
-    else { dSx = (AXR(X, 1) - rx) / vx; if (M::abs_(dSx) < R(1.e-5)) rx = AXR(X, 1); }
+    else { dSx = M::div_(AXR(X, 1) - rx, vx); if (M::abs_(dSx) < R(1.e-5)) rx = AXR(X, 1); }
   } else dSx = AXR(X, nx);
   if (lost) { if (p.nEmit >= kRecursionLimit) ++lc.trapped; return ST_IDLE; }
   if (vy > R(0)) {
-    if (yP < ny) { dSy = ((AXR(Y, yP + 1) + AXR(Y, yP)) / R(2) - ry) / vy;
+    if (yP < ny) { dSy = M::div_((AXR(Y, yP + 1) + AXR(Y, yP)) / R(2) - ry, vy);
                    if (M::abs_(dSy) < R(1.e-5)) { ry = (AXR(Y, yP + 1) + AXR(Y, yP)) / R(2); yP = yP + 1; } }
-    else { dSy = (AXR(Y, ny) - ry) / vy; if (M::abs_(dSy) < R(1.e-5)) { ry = AXR(Y, ny); lost = true; } }
+    else { dSy = M::div_(AXR(Y, ny) - ry, vy); if (M::abs_(dSy) < R(1.e-5)) { ry = AXR(Y, ny); lost = true; } }
   } else if (vy < R(0)) {
-    if (yP > 1) { dSy = ((AXR(Y, yP) + AXR(Y, yP - 1)) / R(2) - ry) / vy;
+    if (yP > 1) { dSy = M::div_((AXR(Y, yP) + AXR(Y, yP - 1)) / R(2) - ry, vy);
                   if (M::abs_(dSy) < R(1.e-5)) { ry = (AXR(Y, yP) + AXR(Y, yP - 1)) / R(2); yP = yP - 1; } }
-    else { dSy = (AXR(Y, 1) - ry) / vy; if (M::abs_(dSy) < R(1.e-5)) ry = AXR(Y, 1); }
+    else { dSy = M::div_(AXR(Y, 1) - ry, vy); if (M::abs_(dSy) < R(1.e-5)) ry = AXR(Y, 1); }
   } else dSy = AXR(Y, ny);
   if (lost) { if (p.nEmit >= kRecursionLimit) ++lc.trapped; return ST_IDLE; }
   if (vz > R(0)) {
-    if (zP < nz) { dSz = ((AXR(Z, zP + 1) + AXR(Z, zP)) / R(2) - rz) / vz;
+    if (zP < nz) { dSz = M::div_((AXR(Z, zP + 1) + AXR(Z, zP)) / R(2) - rz, vz);
                    if (M::abs_(dSz) < R(1.e-5)) { rz = (AXR(Z, zP + 1) + AXR(Z, zP)) / R(2); zP = zP + 1; } }
-    else { dSz = (AXR(Z, nz) - rz) / vz; if (M::abs_(dSz) < R(1.e-5)) { rz = AXR(Z, nz); lost = true; } }
+    else { dSz = M::div_(AXR(Z, nz) - rz, vz); if (M::abs_(dSz) < R(1.e-5)) { rz = AXR(Z, nz); lost = true; } }
   } else if (vz < R(0)) {
-    if (zP > 1) { dSz = ((AXR(Z, zP) + AXR(Z, zP - 1)) / R(2) - rz) / vz;
+    if (zP > 1) { dSz = M::div_((AXR(Z, zP) + AXR(Z, zP - 1)) / R(2) - rz, vz);
                   if (M::abs_(dSz) < R(1.e-5)) { rz = (AXR(Z, zP) + AXR(Z, zP - 1)) / R(2); zP = zP - 1; } }
-    else { dSz = (AXR(Z, 1) - rz) / vz; if (M::abs_(dSz) < R(1.e-5)) rz = AXR(Z, 1); }
+    else { dSz = M::div_(AXR(Z, 1) - rz, vz); if (M::abs_(dSz) < R(1.e-5)) rz = AXR(Z, 1); }
   } else dSz = AXR(Z, nz);
   if (lost) { if (p.nEmit >= kRecursionLimit) ++lc.trapped; return ST_IDLE; }
   if (xP > nx || xP < 1 || yP > ny || yP < 1 || zP > nz || zP < 1) { ++lc.errors; return ST_IDLE; }
@@ -367,7 +370,7 @@ __device__ int stepPacket(const DevGrid& g, const Geo& q, const DevTransportIn& 
   int next = ST_STEP;
   if ((p.absTau + tauCell > p.passProb) && cell > 0) {
     // interaction within the cell (source/photon_mod.f90:2244-2700)
-    R dlLoc = (p.passProb - p.absTau) / kap;
+    R dlLoc = M::div_(p.passProb - p.absTau, kap);
     rx = rx + dlLoc * vx; ry = ry + dlLoc * vy; rz = rz + dlLoc * vz;
     if (q.symmetric()) {
       if (rx <= AXR(X, 1)) { if (vx < R(0)) vx = -vx; rx = AXR(X, 1); }
