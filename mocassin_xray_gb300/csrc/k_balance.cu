@@ -22,6 +22,7 @@ cudaError_t prepare(const BalanceData& bd);
 namespace bal_mixed {
 cudaError_t prepare(const BalanceData& bd);
 cudaError_t buildCoolTable(const BalanceData& bd, float* tab, float* rtab, cudaStream_t s);
+cudaError_t buildAlphaTable(const BalanceData& bd, float* tab, uint8_t* jump, cudaStream_t s);
 cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStream_t s, int atomSolves);
 cudaError_t launchForLines(BalanceData& bd, const float* te, const float* ne, const float* ionDen,
                            const uint8_t* compute, float* forLines, cudaStream_t s);
@@ -295,8 +296,26 @@ void invalidateBalanceGraphs(BalanceData& bd);
 // the cooling surfaces (ln G and B of every atom), once per context and before
 // any graph capture that bakes their pointers in
 cudaError_t ensureSurfaces(BalanceData& bd, cudaStream_t s) {
-  if (bd.dev.nAtoms <= 0 || bd.dev.coolTab) return cudaSuccess;
   const int slots = (int)(sizeof(bd.blocks) / sizeof(bd.blocks[0]));
+  if (!bd.dev.alphaTab && bd.dev.nElemUsed > 0) {
+    // the recombination coefficients of the mixed rates kernel
+    if (bd.nBlocks + 2 > slots) return cudaErrorMemoryAllocation;
+    const size_t n = (size_t)bd.dev.nElemUsed * bd.dev.nstages * kAlphaN;
+    void* p = nullptr;
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&p, n * sizeof(float));
+    if (e != cudaSuccess) return e;
+    bd.blocks[bd.nBlocks++] = p;
+    e = cudaMalloc(&q, n);
+    if (e != cudaSuccess) return e;
+    bd.blocks[bd.nBlocks++] = q;
+    e = bal_mixed::buildAlphaTable(bd, (float*)p, (uint8_t*)q, s);
+    if (e != cudaSuccess) return e;
+    invalidateBalanceGraphs(bd);
+    bd.dev.alphaTab = (const float*)p;
+    bd.dev.alphaJump = (const uint8_t*)q;
+  }
+  if (bd.dev.nAtoms <= 0 || bd.dev.coolTab) return cudaSuccess;
   if (bd.nBlocks + 2 > slots) return cudaErrorMemoryAllocation;
   const size_t bytes = (size_t)bd.dev.nAtoms * kCoolNNe * kCoolNTe * sizeof(float);
   void* p = nullptr;

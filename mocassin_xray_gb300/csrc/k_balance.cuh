@@ -41,6 +41,13 @@ struct LineSumArgs;
 constexpr int kRefRounds = 20;   // maxIterateT (source/update_mod.f90:106-107)
 constexpr int kMaxRounds = 64;   // T-iterations of the tightly converged balance
 
+// alphaTotal of every (element, ion) pair of the mixed balance, tabulated in
+// ln Te (1..1e7 K, kAlphaN nodes) and read by 4-point Lagrange; an interval
+// where the reference's fits switch (a jump the interpolant cannot follow) is
+// flagged at build time and evaluated directly
+constexpr int kAlphaN = 4097;
+constexpr double kAlphaLnT0 = 0., kAlphaLnT1 = 16.11809565095832;   // ln 1, ln 1e7
+
 constexpr int kCoolNTe = 1280, kCoolNNe = 640;
 constexpr double kCoolLnTe0 = 0.;                    // ln 1
 constexpr double kCoolLnTe1 = 13.815510557964274;    // ln 1e6
@@ -120,6 +127,8 @@ struct BalanceDev {
   const float* recTab;         // [nAtoms][kCoolNNe][kCoolNTe] B: the slope of forLines in ionDenUp with the
                                // recombination term (emission phase), built with coolTab
   CoolAt* coolAt;              // [C+1] the cell's stencil on the surfaces, set by the rates kernel
+  const float* alphaTab;       // [nElemUsed * nstages][kAlphaN] ln alphaTotal (mixed balance), with coolTab
+  const uint8_t* alphaJump;    // [nElemUsed * nstages][kAlphaN] 1: interval [i, i+1] evaluated directly
   // per-cell work, [k][C+1] (cell fastest)
   double* ion;                 // [nstages][nElemUsed]
   double* gam;                 // [nShellsTot] photoionisation rate (J integral; the rates kernel adds the reverse charge exchange to its copy)

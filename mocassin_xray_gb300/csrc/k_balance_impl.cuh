@@ -151,6 +151,59 @@ __device__ real alphaOf(const BalanceDev& b, real te, int elem, int ion) {
   return a;
 }
 
+#if !MCX_BAL_EXACT
+__device__ __forceinline__ void lagrange4(float t, float* w);
+
+// ln alphaTotal of pair k = (e - 1) * nstages + (ion - 1) at the nodes of its
+// table, and the jump flags: an interval whose midpoint and quarter points the
+// interpolant misses by more than 1e-5 holds a switch of the fits
+__global__ void __launch_bounds__(128) alphaTableKernel(BalanceDev b, float* tab) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
+  if (i >= kAlphaN) return;
+  const int e = k / b.nstages + 1, ion = k % b.nstages + 1;
+  const int elem = b.zOf[e];
+  const double h = (kAlphaLnT1 - kAlphaLnT0) / (kAlphaN - 1);
+  const real a = ion <= min(b.nstages - 1, elem) ? alphaOf(b, (real)exp(kAlphaLnT0 + i * h), elem, ion) : (real)0.;
+  tab[(size_t)k * kAlphaN + i] = a > 0.f ? logf(a) : -1.e30f;
+}
+__global__ void __launch_bounds__(128) alphaJumpKernel(BalanceDev b, const float* tab, uint8_t* jump) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
+  if (i >= kAlphaN) return;
+  const int e = k / b.nstages + 1, ion = k % b.nstages + 1;
+  const int elem = b.zOf[e];
+  uint8_t bad = 1;
+  if (i >= 1 && i + 2 < kAlphaN && ion <= min(b.nstages - 1, elem)) {
+    const float* t = tab + (size_t)k * kAlphaN + (i - 1);
+    bad = 0;
+    if (t[0] < -1.e29f || t[1] < -1.e29f || t[2] < -1.e29f || t[3] < -1.e29f) bad = 1;
+    const double h = (kAlphaLnT1 - kAlphaLnT0) / (kAlphaN - 1);
+    for (int q = 1; q <= 3 && !bad; ++q) {
+      const float f = 0.25f * q;
+      float w[4];
+      lagrange4(f, w);
+      const float lnA = w[0] * t[0] + w[1] * t[1] + w[2] * t[2] + w[3] * t[3];
+      const real ex = alphaOf(b, (real)exp(kAlphaLnT0 + (i + f) * h), elem, ion);
+      if (!(ex > 0.f) || fabsf(expf(lnA - logf(ex)) - 1.f) > 1.e-5f) bad = 1;
+    }
+  }
+  jump[(size_t)k * kAlphaN + i] = bad;
+}
+
+// alphaTotal of pair k at Te from the table (direct where the table cannot serve)
+__device__ __forceinline__ real alphaLookup(const BalanceDev& b, int k, real teR, int elem, int ion) {
+  const float s = (logf(teR) - (float)kAlphaLnT0) * (float)((kAlphaN - 1) / (kAlphaLnT1 - kAlphaLnT0));
+  const int i = (int)s;
+  if (s >= 1.f && i + 2 < kAlphaN && !b.alphaJump[(size_t)k * kAlphaN + i]) {
+    const float* t = b.alphaTab + (size_t)k * kAlphaN + (i - 1);
+    float w[4];
+    lagrange4(s - (float)i, w);
+    const float ref = __ldg(t + 1);
+    return expf(ref) * expf(w[0] * (__ldg(t) - ref) + w[2] * (__ldg(t + 2) - ref) + w[3] * (__ldg(t + 3) - ref));
+  }
+  return alphaOf(b, teR, elem, ion);
+}
+#endif
+
 // chex(z, ion, 1) * 1e-9 without the temperature fit (ionBalance's heavy elements)
 __device__ __forceinline__ real chexRaw(const BalanceDev& b, int z, int ion) {
   return (real)b.chex[z * 32 + ion].x * RF(1.e-9);
@@ -585,7 +638,12 @@ __global__ void __launch_bounds__(128) ratesKernel(BalanceDev b, const float* __
   for (int k = L.gl; k < NP; k += kGroup) {
     const int e = k / ns + 1, ion = k % ns + 1;
     const int elem = m.zOf[e];
+#if MCX_BAL_EXACT
     w.AL[k] = ion <= min(ns - 1, elem) ? alphaOf(b, teR, elem, ion) : (real)0.;
+#else
+    w.AL[k] = ion <= min(ns - 1, elem) ? (b.alphaTab ? alphaLookup(b, k, teR, elem, ion) : alphaOf(b, teR, elem, ion))
+                                       : (real)0.;
+#endif
   }
   // photoionisation rates per shell
   for (int t = L.gl; t < nSh; t += kGroup) w.PI[t] = (real)b.gam[(size_t)t * C1 + cell];
@@ -1557,6 +1615,16 @@ cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStr
 }
 
 #if !MCX_BAL_EXACT
+// the alphaTotal tables of every (element, ion) pair and their jump flags
+cudaError_t buildAlphaTable(const BalanceData& bd, float* tab, uint8_t* jump, cudaStream_t s) {
+  const int pairs = bd.dev.nElemUsed * bd.dev.nstages;
+  if (pairs <= 0) return cudaSuccess;
+  const dim3 grid((kAlphaN + 127) / 128, pairs);
+  alphaTableKernel<<<grid, 128, 0, s>>>(bd.dev, tab);
+  alphaJumpKernel<<<grid, 128, 0, s>>>(bd.dev, tab, jump);
+  return cudaGetLastError();
+}
+
 // the surfaces of every atom into tab (ln G) and rtab (B), [nAtoms][kCoolNNe][kCoolNTe] floats each
 cudaError_t buildCoolTable(const BalanceData& bd, float* tab, float* rtab, cudaStream_t s) {
   const size_t n = (size_t)bd.dev.nAtoms * kCoolNNe * kCoolNTe;
