@@ -274,13 +274,16 @@ std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out)
     int nHeavy = 0;
     for (int e = 1; e <= d.nElemUsed; ++e) nHeavy += d.zOf[e] >= 3 ? 1 : 0;
     d.cellReals = 3 * NP + nSh + std::max(NP, nSh) + std::max(nHeavy * 3 * (ns + 3), 4 * d.nElemUsed);
+    // the mixed build's per-heavy-element sums of the photoionisation rates, Auger band and charge exchange
+    d.augReals = nHeavy * 12 * (ns + 1);
     // zOf, xref, abun (3 x 32 words) and the (element, ion) shell offsets and counts (2 x E x 32 int16)
     d.metaDoubles = (3 * 32 * 4 + 2 * d.nElemUsed * 32 * 2 + 7) / 8;
-    // as many warps (4 cells each) per block as fit 200 KB in FP64
+    // as many warps (4 cells each) per block as fit 200 KB in both builds
+    const size_t cellBytes = std::max((size_t)d.cellReals * sizeof(double),
+                                      ((size_t)d.cellReals + (size_t)d.augReals) * sizeof(float));
     d.ratesWarps = 0;
     for (int wps : {4, 2, 1})
-      if (!d.ratesWarps &&
-          ((size_t)d.metaDoubles + (size_t)wps * 4 * (size_t)d.cellReals) * sizeof(double) <= 200 * 1024)
+      if (!d.ratesWarps && (size_t)d.metaDoubles * sizeof(double) + (size_t)wps * 4 * cellBytes <= 200 * 1024)
         d.ratesWarps = wps;
     if (!d.ratesWarps) return "balance: too many ions for the rates kernel";
     if (nHeavy > 32) return "balance: more than 32 heavy elements";

@@ -82,6 +82,7 @@ struct BalanceDev {
   int32_t cellReals;           // shared memory of one cell of the rates kernel, in values of the rate precision
   int32_t metaDoubles;         // its per-block element tables, in doubles
   int32_t ratesWarps;          // warps per block of the rates kernel (4 cells per warp)
+  int32_t augReals;            // mixed build: further shared memory per cell, in floats
   int32_t secIonP, cRecoilHP, cRecoilHeP;
   float xhiLimit;
   // T-iteration controls: the reference's (2 % residual, 1 % X(H0), X(He0),

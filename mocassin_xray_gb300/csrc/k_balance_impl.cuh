@@ -393,6 +393,9 @@ struct WarpCell {
   real* PI;      // [nShellsTot] photoIon(1): rate per shell, with the reverse charge exchange
   real* T;       // scratch for ordered sums
   real* LAD;     // [nHeavy][3][S+3] out, inn, mat of the ladders; later the thermBalance terms [4][E]
+  real* AUG;     // mixed build: [nHeavy][12 (S+1)] per heavy element the sums over shells of the
+                 // photoionisation rate per ion, charge exchange per ion, and the Auger band
+                 // A[ion][d] = sum of photoIon * auger feeding ion + d
 };
 
 __device__ __forceinline__ real& xAt(const BalanceDev& b, const ElemMeta& m, const WarpCell& w, int z, int st) {
@@ -429,6 +432,37 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
       if (h % kGroup == L.gl && nMine < 32 / kGroup) myE[nMine++] = e;
       ++h;
     }
+#if !MCX_BAL_EXACT
+  // the parts of the ladders' out and inn terms that stay put over the X-iterations: the
+  // photoionisation rates summed per ion, the Auger terms summed per (ion, ion + d) (each is
+  // multiplied by X(ion) / X(ion + d) in the X-iteration), the charge-exchange coefficients
+  for (int q = 0; q < nMine; ++q) {
+    const int e = myE[q];
+    const int elem = m.zOf[e];
+    int h = 0;
+    for (int f = 1; f < e; ++f) h += m.zOf[f] >= 3 ? 1 : 0;
+    real* S = w.AUG + (size_t)h * 12 * (ns + 1);
+    real* CH = S + (ns + 1);
+    real* A = CH + (ns + 1);
+    const int topI = min(elem, ns - 1), lim = min(ns - 1, elem);
+    for (int k = 0; k < 12 * (ns + 1); ++k) S[k] = 0;
+    for (int ion = 1; ion <= topI; ++ion) {
+      CH[ion] = chexRaw(b, elem, ion);
+      const int p0 = m.p0[(e - 1) * 32 + (ion - 1)];
+      const int nsh = m.nsh[(e - 1) * 32 + (ion - 1)];
+      for (int shell = 1; shell <= nsh; ++shell) {
+        const real pi = w.PI[p0 + shell - 1];
+        S[ion] = S[ion] + pi;
+        const int nAug = b.nauger[((size_t)(elem - 1) * kNE + (ion - 1)) * 10 + (shell - 1)];
+        for (int nelec = 2; nelec <= nAug; ++nelec) {
+          const int maxim = min(ion + nelec - 1, lim);
+          A[ion * 10 + (maxim - ion)] +=
+              pi * (real)b.auger[(((size_t)(elem - 1) * kNE + (ion - 1)) * 10 + (shell - 1)) * 10 + (nelec - 1)];
+        }
+      }
+    }
+  }
+#endif
   for (int nIterateX = 1;; ++nIterateX) {
     bool lgConv = true;
     const real HIOld = xAt(b, m, w, zH, 1);
@@ -486,6 +520,7 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
       real* mat = inn + (ns + 3);
       for (int k = 0; k < ns + 3; ++k) { out[k] = 0; inn[k] = 0; }
       const int topI = min(elem, ns - 1);
+#if MCX_BAL_EXACT
       const int lim = min(ns - 1, elem);
       for (int ion = 1; ion <= topI; ++ion) {
         out[ion] = out[ion] + w.CC[(e - 1) * ns + (ion - 1)] * neR;
@@ -506,6 +541,25 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
       }
       for (int ion = 1; ion <= topI; ++ion)
         inn[ion] = neR * w.AL[(e - 1) * ns + (ion - 1)] + chexRaw(b, elem, ion) * hdenR * xH0now;
+#else
+      {
+        const real* S = w.AUG + (size_t)h * 12 * (ns + 1);
+        const real* CH = S + (ns + 1);
+        const real* A = CH + (ns + 1);
+        for (int ion = 1; ion <= topI; ++ion) out[ion] = out[ion] + (w.CC[(e - 1) * ns + (ion - 1)] * neR + S[ion]);
+        for (int ion = 1; ion <= topI; ++ion) {
+          const real xi = xAt(b, m, w, elem, ion);
+          for (int d = 0; d <= 9 && ion + d <= topI; ++d) {   // d = 0: Auger electrons clamped at lim
+            const real a = A[ion * 10 + d];
+            if (a == (real)0.) continue;
+            const real xm = xAt(b, m, w, elem, ion + d);
+            out[ion + d] = out[ion + d] + a * (xm > (real)1e-30 ? xi / xm : (real)1.);
+          }
+        }
+        for (int ion = 1; ion <= topI; ++ion)
+          inn[ion] = neR * w.AL[(e - 1) * ns + (ion - 1)] + CH[ion] * hdenR * xH0now;
+      }
+#endif
       const int top = min(ns, elem + 1);
 #if MCX_BAL_EXACT
       mat[1] = 1.;
@@ -621,12 +675,17 @@ __global__ void __launch_bounds__(128) ratesKernel(BalanceDev b, const float* __
   const int cell = b.list[(size_t)(round & 1) * C1 + li];
   const ElemMeta m{sZ, sX, sA, sP0, sNs};
   WarpCell w;
+#if MCX_BAL_EXACT
   w.X = reinterpret_cast<real*>(wsm + b.metaDoubles) + (size_t)slot * b.cellReals;
+#else
+  w.X = reinterpret_cast<real*>(wsm + b.metaDoubles) + (size_t)slot * (b.cellReals + b.augReals);
+#endif
   w.AL = w.X + NP;
   w.CC = w.AL + NP;
   w.PI = w.CC + NP;
   w.T = w.PI + nSh;
   w.LAD = w.T + max(NP, nSh);
+  w.AUG = w.X + b.cellReals;
   for (int k = L.gl; k < NP; k += kGroup) w.X[k] = (real)b.ion[(size_t)k * C1 + cell];
   if (L.gl == 0) b.nIterT[cell] = b.nIterT[cell] + 1;
   const double te = b.te[cell];
@@ -1636,7 +1695,12 @@ cudaError_t buildCoolTable(const BalanceData& bd, float* tab, float* rtab, cudaS
 
 // the rates kernel's dynamic shared memory: the element tables and one slice per cell of the block
 size_t ratesSmem(const BalanceDev& b) {
-  return (size_t)b.metaDoubles * sizeof(double) + (size_t)b.ratesWarps * kCellsPerWarp * b.cellReals * sizeof(real);
+#if MCX_BAL_EXACT
+  const size_t cell = (size_t)b.cellReals;
+#else
+  const size_t cell = (size_t)b.cellReals + (size_t)b.augReals;
+#endif
+  return (size_t)b.metaDoubles * sizeof(double) + (size_t)b.ratesWarps * kCellsPerWarp * cell * sizeof(real);
 }
 
 cudaError_t prepare(const BalanceData& bd) {
