@@ -420,9 +420,16 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
   const real hdenR = (real)hden;
   real neR = (real)ne;
   real cxHHe[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  real piHHe[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};   // the outer shell's photoionisation rate
   if (L.gl == 0)
     for (int elem = 1; elem <= 2; ++elem)
-      for (int ion = 1; ion <= min(elem, ns - 1); ++ion) cxHHe[elem][ion] = chexFit(b, elem, ion, teR);
+      for (int ion = 1; ion <= min(elem, ns - 1); ++ion) {
+        cxHHe[elem][ion] = chexFit(b, elem, ion, teR);
+        if (m.xref[elem]) {
+          const int outShell = outerOf(b, elem, elem - ion + 1)[0];
+          piHHe[elem][ion] = w.PI[m.p0[(m.xref[elem] - 1) * 32 + (ion - 1)] + outShell - 1];
+        }
+      }
   // this lane's heavy elements (the h-th element with Z >= 3, in element order,
   // for h = gl, gl + kGroup, ...; at most 32 heavy elements)
   int myE[32 / kGroup] = {};
@@ -478,10 +485,8 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
         if (!m.xref[elem]) continue;
         for (int ion = 1; ion <= min(elem, ns - 1); ++ion) {
           real cx = cxHHe[elem][ion];
-          int outShell = outerOf(b, elem, elem - ion + 1)[0];
           if (elem > 1 || ion > 1) collIonH = 0;
-          int p0 = m.p0[(m.xref[elem] - 1) * 32 + (ion - 1)];
-          real pi = w.PI[p0 + outShell - 1];
+          real pi = piHHe[elem][ion];
           const real num = pi + collIonH * neR + (real)0.;
           const real dnm = neR * w.AL[(m.xref[elem] - 1) * ns + (ion - 1)] + cx * hdenR * HIOld;
           ionRatio[elem][ion] = num / dnm;
@@ -616,6 +621,7 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
 #endif
     }
     __syncwarp(L.mask);
+#if MCX_BAL_EXACT
     // Ne in the reference's order, by the group's first lane
     real nE = 0;
     if (L.gl == 0) {
@@ -630,6 +636,22 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
       if (nE == (real)0.) nE = 1;
     }
     neR = __shfl_sync(L.mask, nE, 0, kGroup);
+#else
+    // Ne: the (element, stage) terms strided over the group's lanes, then a butterfly sum
+    real nE = 0;
+    for (int k = L.gl; k < E * ns; k += kGroup) {
+      const int e = k / ns + 1, ion = k % ns + 1;
+      const int elem = m.zOf[e];
+      if (ion < 2 || ion > min(elem + 1, ns)) continue;
+      const real x = w.X[(ion - 1) * E + (e - 1)];
+      if (x >= (real)RD(1.e-10)) nE = nE + (real)(ion - 1) * (real)m.abun[elem] * x;
+    }
+#pragma unroll
+    for (int o = kGroup / 2; o > 0; o >>= 1) nE += __shfl_xor_sync(L.mask, nE, o, kGroup);
+    nE = nE * hdenR;
+    if (nE == (real)0.) nE = 1;
+    neR = nE;
+#endif
     ne = (double)neR;
     real dHI = (xAt(b, m, w, zH, 1) - HIOld) / HIOld;
     real dHeI = heOn ? (xAt(b, m, w, zHe, 1) - HeIOld) / HeIOld : (real)0.;
