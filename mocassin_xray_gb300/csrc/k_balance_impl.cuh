@@ -432,11 +432,14 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
       }
   // this lane's heavy elements (the h-th element with Z >= 3, in element order,
   // for h = gl, gl + kGroup, ...; at most 32 heavy elements)
-  int myE[32 / kGroup] = {};
+  int myE[32 / kGroup] = {}, myH[32 / kGroup] = {};
   int nMine = 0;
   for (int e = 1, h = 0; e <= E; ++e)
     if (m.zOf[e] >= 3) {
-      if (h % kGroup == L.gl && nMine < 32 / kGroup) myE[nMine++] = e;
+      if (h % kGroup == L.gl && nMine < 32 / kGroup) {
+        myE[nMine] = e;
+        myH[nMine++] = h;
+      }
       ++h;
     }
 #if !MCX_BAL_EXACT
@@ -444,10 +447,8 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
   // photoionisation rates summed per ion, the Auger terms summed per (ion, ion + d) (each is
   // multiplied by X(ion) / X(ion + d) in the X-iteration), the charge-exchange coefficients
   for (int q = 0; q < nMine; ++q) {
-    const int e = myE[q];
+    const int e = myE[q], h = myH[q];
     const int elem = m.zOf[e];
-    int h = 0;
-    for (int f = 1; f < e; ++f) h += m.zOf[f] >= 3 ? 1 : 0;
     real* S = w.AUG + (size_t)h * 12 * (ns + 1);
     real* CH = S + (ns + 1);
     real* A = CH + (ns + 1);
@@ -515,17 +516,15 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
     // X(H0) as just updated above (grid%ionDen in the reference)
     const real xH0now = xAt(b, m, w, zH, 1);
     for (int q = 0; q < nMine; ++q) {
-      const int e = myE[q];
+      const int e = myE[q], h = myH[q];
       const int elem = m.zOf[e];
-      int h = 0;
-      for (int f = 1; f < e; ++f) h += m.zOf[f] >= 3 ? 1 : 0;
       typedef real lad;
       lad* out = w.LAD + (size_t)h * 3 * (ns + 3);
       lad* inn = out + (ns + 3);
       real* mat = inn + (ns + 3);
-      for (int k = 0; k < ns + 3; ++k) { out[k] = 0; inn[k] = 0; }
       const int topI = min(elem, ns - 1);
 #if MCX_BAL_EXACT
+      for (int k = 0; k < ns + 3; ++k) { out[k] = 0; inn[k] = 0; }
       const int lim = min(ns - 1, elem);
       for (int ion = 1; ion <= topI; ++ion) {
         out[ion] = out[ion] + w.CC[(e - 1) * ns + (ion - 1)] * neR;
@@ -546,24 +545,6 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
       }
       for (int ion = 1; ion <= topI; ++ion)
         inn[ion] = neR * w.AL[(e - 1) * ns + (ion - 1)] + chexRaw(b, elem, ion) * hdenR * xH0now;
-#else
-      {
-        const real* S = w.AUG + (size_t)h * 12 * (ns + 1);
-        const real* CH = S + (ns + 1);
-        const real* A = CH + (ns + 1);
-        for (int ion = 1; ion <= topI; ++ion) out[ion] = out[ion] + (w.CC[(e - 1) * ns + (ion - 1)] * neR + S[ion]);
-        for (int ion = 1; ion <= topI; ++ion) {
-          const real xi = xAt(b, m, w, elem, ion);
-          for (int d = 0; d <= 9 && ion + d <= topI; ++d) {   // d = 0: Auger electrons clamped at lim
-            const real a = A[ion * 10 + d];
-            if (a == (real)0.) continue;
-            const real xm = xAt(b, m, w, elem, ion + d);
-            out[ion + d] = out[ion + d] + a * (xm > (real)1e-30 ? xi / xm : (real)1.);
-          }
-        }
-        for (int ion = 1; ion <= topI; ++ion)
-          inn[ion] = neR * w.AL[(e - 1) * ns + (ion - 1)] + CH[ion] * hdenR * xH0now;
-      }
 #endif
       const int top = min(ns, elem + 1);
 #if MCX_BAL_EXACT
@@ -593,12 +574,27 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
       // more than FP32's range; their logarithms do not), normalised against
       // the largest term; the first X-iteration's geometric mean is the mean
       // of the logarithms
+      // one pass over the stages: out (collisional and photoionisation, the Auger electrons of
+      // the lower stages ion - d into ion, times X(ion - d) / X(ion)) and inn of each stage, and
+      // the running log of the ladder's product
+      const real* S = w.AUG + (size_t)h * 12 * (ns + 1);
+      const real* CH = S + (ns + 1);
+      const real* A = CH + (ns + 1);
+      const real* XE = w.X + (e - 1);   // X of this element's stage ion at XE[(ion - 1) * E]
       float* lm = mat;
       lm[1] = 0.f;
-      float lmax = 0.f;
-      for (int ion = 2; ion <= top; ++ion) {
-        lm[ion] = lm[ion - 1] + log2f((float)out[ion - 1] / (float)inn[ion - 1]);
-        lmax = fmaxf(lmax, lm[ion]);
+      float lmax = 0.f, lcur = 0.f;
+      for (int ion = 1; ion <= topI; ++ion) {
+        const real xi = XE[(ion - 1) * E];
+        real o = w.CC[(e - 1) * ns + (ion - 1)] * neR + S[ion];
+        for (int d = 0; d <= 9 && d < ion; ++d) {   // d = 0: Auger electrons clamped at lim
+          const real a = A[(ion - d) * 10 + d];
+          if (a != (real)0.) o = o + a * (xi > (real)1e-30 ? __fdividef(XE[(ion - d - 1) * E], xi) : (real)1.);
+        }
+        const real in_ = neR * w.AL[(e - 1) * ns + (ion - 1)] + CH[ion] * hdenR * xH0now;
+        lcur = lcur + log2f(__fdividef(o, in_));
+        lm[ion + 1] = lcur;
+        lmax = fmaxf(lmax, lcur);
       }
       float sum = 0.f;
       for (int ion = 1; ion <= top; ++ion) sum += exp2f(lm[ion] - lmax);
