@@ -233,7 +233,10 @@ int  mcx_state_restore(mcx_ctx* ctx);
  * (source/ionization_mod.f90:26-477), including the skip rule for cells whose
  * Te and Ne changed by less than 0.5 % (source/iteration_mod.f90:131-149). */
 #define MCX_PHASE_EXACT  0     /* the reference's arithmetic (FP64 multi-level atoms)      */
-#define MCX_PHASE_MIXED  1     /* emission: forbidden lines from the mixed-precision solver */
+#define MCX_PHASE_MIXED  1     /* emission: forbidden lines from the cooling surfaces (or the
+                                  mixed-precision solver), and the cumulative distribution summed
+                                  over frequency chunks with offsets (differs from the sequential
+                                  FP32 sum by rounding) */
 
 typedef struct mcx_phase_opts {
     int32_t n_iterate_mc;       /* nIterateMC (1-based); the skip rule applies when > 1 */

@@ -10,6 +10,8 @@
 // the gamma-edge pair covering each bin) is tabulated once on the host in FP64
 // and stored in FP32, so the per-cell work is FP32 exponentials and FMAs.
 #include "k_emission.cuh"
+
+#include <algorithm>
 #include "k_gaunt.cuh"
 #include "setup_internal.h"
 
@@ -151,6 +153,11 @@ std::string emissionDataCreate(const Setup& s, std::unique_ptr<EmissionData>& ou
     err = up(*d, ffK, &fk);
     e.ffK = const_cast<float*>(fk);
   }
+  if (err == cudaSuccess) {
+    const float* pp = nullptr;
+    err = up(*d, std::vector<float>((size_t)4 * kEmChunksMax * ((size_t)s.nCells + 1), 0.f), &pp);
+    e.part = const_cast<float*>(pp);
+  }
   if (err != cudaSuccess) return std::string("emission tables: ") + cudaGetErrorString(err);
   out = std::move(d);
   return "";
@@ -218,10 +225,17 @@ __device__ __forceinline__ int locateF(const float* xa, int n, float x) {
 
 }  // namespace
 
+// Two passes.  mode 1, grid (cells, chunks): the frequency mesh in nChunks
+// contiguous chunks, each chunk's cumulative sums from 0 into recPDF and its
+// totals (the chunk's sum and its HI, HeI, HeII parts) into part[4][nChunks][C+1];
+// enough independent chunks per cell keep the SMs busy.  mode 2, one thread per
+// cell: the chunk offsets added and the distribution normalised, then the
+// recombination lines and totalLines.
 __global__ void __launch_bounds__(128)
 emissionKernel(EmissionDev e, const float* __restrict__ te, const float* __restrict__ ne,
                const float* __restrict__ ionDen, const uint8_t* __restrict__ compute,
-               const float* __restrict__ forLines, float* __restrict__ recPDF, float* __restrict__ totalLines) {
+               const float* __restrict__ forLines, float* __restrict__ recPDF, float* __restrict__ totalLines,
+               float* __restrict__ part, int nChunks, int mode) {
   const int cell = blockIdx.x * blockDim.x + threadIdx.x + 1;
   if (cell > e.nCells || !compute[cell]) return;
   const size_t C1 = (size_t)e.nCells + 1;
@@ -274,7 +288,11 @@ emissionKernel(EmissionDev e, const float* __restrict__ te, const float* __restr
   const float lyA = exp10f(-0.792f * log10Te + 6.01f) * Ne * xHe3 * e.abunHe;
 
   float normHI = 0.f, normHeI = 0.f, normHeII = 0.f, cum = 0.f;
-  for (int i = 1; i <= nb; ++i) {
+  const int chunkLen = (nb + nChunks - 1) / nChunks;
+  if (mode == 1) {
+  const int q = blockIdx.y;
+  const int i0 = 1 + q * chunkLen, i1 = min(nb, (q + 1) * chunkLen);
+  for (int i = i0; i <= i1; ++i) {
     const float v = e.nu[i - 1];
     float gHI = 0.f, gHeI = 0.f, gHeII = 0.f;
     float g[3] = {0.f, 0.f, 0.f};
@@ -318,6 +336,21 @@ emissionKernel(EmissionDev e, const float* __restrict__ te, const float* __restr
       if (i == e.HeIILymanP[k]) sHeII += (k == 3) ? lyA : e.heiiLyman[k] * lyA;
     cum = cum + (sHI + sHeI + sHeII);
     recPDF[(size_t)cell + C1 * (size_t)(i - 1)] = cum;
+  }
+  part[((size_t)0 * nChunks + q) * C1 + cell] = cum;
+  part[((size_t)1 * nChunks + q) * C1 + cell] = normHI;
+  part[((size_t)2 * nChunks + q) * C1 + cell] = normHeI;
+  part[((size_t)3 * nChunks + q) * C1 + cell] = normHeII;
+  return;
+  }
+  // mode 2: the chunks' offsets and the norms in chunk order
+  float off[kEmChunksMax];
+  for (int q = 0; q < nChunks; ++q) {
+    off[q] = cum;
+    cum = cum + part[((size_t)0 * nChunks + q) * C1 + cell];
+    normHI += part[((size_t)1 * nChunks + q) * C1 + cell];
+    normHeI += part[((size_t)2 * nChunks + q) * C1 + cell];
+    normHeII += part[((size_t)3 * nChunks + q) * C1 + cell];
   }
   normHeI += corrHeI;
   normHeII += lyA * (1.f + e.heiiLyman[0] + e.heiiLyman[1] + e.heiiLyman[2]);
@@ -420,11 +453,12 @@ emissionKernel(EmissionDev e, const float* __restrict__ te, const float* __restr
   }
   const float tl = normRec + (forLines ? forLines[cell] : 0.f);
 
-  // normalise the cumulative distribution (source/emission_mod.f90:1880-1884)
-  const float last = recPDF[(size_t)cell + C1 * (size_t)(nb - 1)];
+  // normalise the cumulative distribution (source/emission_mod.f90:1880-1884),
+  // each chunk's entries shifted by the chunk's offset first
+  const float last = off[(nb - 1) / chunkLen] + recPDF[(size_t)cell + C1 * (size_t)(nb - 1)];
   for (int i = 1; i < nb; ++i) {
     size_t idx = (size_t)cell + C1 * (size_t)(i - 1);
-    recPDF[idx] = recPDF[idx] / last;
+    recPDF[idx] = (off[(i - 1) / chunkLen] + recPDF[idx]) / last;
   }
   recPDF[(size_t)cell + C1 * (size_t)(nb - 1)] = 1.f;
   totalLines[cell] = tl / (normHI + normHeI + normHeII + tl);
@@ -432,10 +466,15 @@ emissionKernel(EmissionDev e, const float* __restrict__ te, const float* __restr
 
 cudaError_t launchEmission(const EmissionDev& e, const float* te, const float* ne, const float* ionDen,
                            const uint8_t* compute, const float* forLines, float* recPDF, float* totalLines,
-                           cudaStream_t s) {
-  const int threads = 128;
-  emissionKernel<<<(e.nCells + threads - 1) / threads, threads, 0, s>>>(e, te, ne, ionDen, compute, forLines, recPDF,
-                                                                       totalLines);
+                           bool chunked, cudaStream_t s) {
+  const int threads = 128, blocks = (e.nCells + threads - 1) / threads;
+  // enough chunks for ~8 blocks per SM of the 152, each at least 32 bins long
+  const int nChunks =
+      chunked ? std::max(1, std::min({kEmChunksMax, (8 * 152 + blocks - 1) / blocks, e.nbins / 32})) : 1;
+  emissionKernel<<<dim3(blocks, nChunks), threads, 0, s>>>(e, te, ne, ionDen, compute, forLines, recPDF, totalLines,
+                                                           e.part, nChunks, 1);
+  emissionKernel<<<blocks, threads, 0, s>>>(e, te, ne, ionDen, compute, forLines, recPDF, totalLines, e.part, nChunks,
+                                            2);
   return cudaGetLastError();
 }
 

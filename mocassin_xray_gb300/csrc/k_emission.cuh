@@ -19,6 +19,8 @@ struct FbTerm {
 };
 
 // Device view of the emission tables (all pointers device memory).
+constexpr int kEmChunksMax = 8;   // frequency chunks of the emission kernel
+
 struct EmissionDev {
   int32_t nbins, nCells, nstages, nElemUsed, nTk, nlim[3], nHydroFiles;
   int32_t HIPnuP, HeIPnuP, HeIIPnuP, HeIlast, HeIIlast, j2TsP, HeIILymanP[4];
@@ -52,6 +54,7 @@ struct EmissionDev {
   const int8_t* hydroOn;      // [31] izp computed (element on and nstages > izp)
   const int32_t* xrefAll;     // [30] elementXref
   const float* abunAll;       // [30] elemAbun
+  float* part;                // [4][kEmChunksMax][C+1] per-chunk sums of the emission kernel's first pass
 };
 
 class EmissionData {
@@ -72,8 +75,11 @@ cudaError_t launchEmissionGaunt(const EmissionDev& e, float gauntTe, cudaStream_
 cudaError_t launchEmissionGauntBatched(const EmissionDev& e, const float* temps, int nTables, cudaStream_t s);
 
 // emissionDriver for every cell with compute[c] = 1: writes recPDF[nu][c] and totalLines[c].
+// chunked: the cumulative sums over frequency chunks with offsets (the mixed
+// phase; the CDF then differs from the sequential FP32 sum by rounding); else
+// one sequential sum per cell, operation for operation the reference's.
 cudaError_t launchEmission(const EmissionDev& e, const float* te, const float* ne, const float* ionDen,
                            const uint8_t* compute, const float* forLines, float* recPDF, float* totalLines,
-                           cudaStream_t s);
+                           bool chunked, cudaStream_t s);
 
 }  // namespace mcx

@@ -1082,7 +1082,7 @@ extern "C" int mcx_emission(mcx_ctx* c, const mcx_phase_opts* opts, mcx_phase_st
     forLines = c->forLines.p;
   }
   CK(launchEmission(ed, c->te.p, c->ne.p, c->ionDen.p, c->computeMask.p, forLines, c->recPDF.p, c->totalLines.p,
-                    c->stream), "emission kernel");
+                    opts && opts->precision == MCX_PHASE_MIXED, c->stream), "emission kernel");
   CK(transpose(c->recPDF.p, c->recCDFT.p, c->nbins, (int)C1, c->stream), "transpose recPDF");
   CK(cudaEventRecord(c->ev1, c->stream), "event");
   CK(cudaStreamSynchronize(c->stream), "mcx_emission");
