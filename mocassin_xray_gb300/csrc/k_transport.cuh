@@ -62,6 +62,13 @@ struct Packet {
   PacketRng rng;
 };
 
+// Shared memory of a transport block after its tables: each thread's packet
+// state (one Packet per thread; its address goes to the out-of-line emission
+// code, so it cannot live in registers, and shared memory keeps it on chip).
+__host__ __device__ constexpr size_t packetStateOffset(size_t tableBytes) { return (tableBytes + 15) / 16 * 16; }
+template <typename R>
+__host__ __device__ constexpr size_t packetStateBytes(int threads) { return (size_t)threads * sizeof(Packet<R>); }
+
 struct LocalCounters {
   unsigned long long crossings = 0, interactions = 0, absorptions = 0, scatterings = 0;
   unsigned long long escaped = 0, lineEscapes = 0, trapped = 0, emissions = 0, errors = 0;
@@ -537,7 +544,9 @@ transportKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportC
   const unsigned FULL = 0xffffffffu;
   const R deltaER = (R)deltaE;
   LocalCounters lc;
-  Packet<R> p;
+  Packet<R>& p = reinterpret_cast<Packet<R>*>(
+      reinterpret_cast<char*>(smem) +
+      packetStateOffset((size_t)(g.nx + g.ny + g.nz + 2 * g.nbins) * sizeof(float)))[threadIdx.x];
   p.nEmit = 0; p.nStep = 0;
   int state = ST_IDLE;
 
@@ -589,7 +598,8 @@ transportKernelBatched(DevGrid g, DevTransportIn in, DevTransportOut out, DevTra
 
   const unsigned FULL = 0xffffffffu;
   LocalCounters lc;
-  Packet<R> p;
+  Packet<R>& p = reinterpret_cast<Packet<R>*>(reinterpret_cast<char*>(smem) +
+                                              packetStateOffset((size_t)g.nbins * sizeof(float)))[threadIdx.x];
   p.nEmit = 0; p.nStep = 0;
   NebulaGeo q{};
   double deltaE = 0.;

@@ -7,7 +7,10 @@ namespace mcx {
 cudaError_t launchTransportF32(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,
                                DevTransportCounters* cnt, uint64_t seed, uint64_t base, unsigned long long n,
                                double deltaE, const TransportLaunch& L, cudaStream_t s) {
-  transportKernel<float><<<L.blocks, L.threads, L.smem, s>>>(g, in, out, cnt, seed, base, n, deltaE,
+  const size_t smem = packetStateOffset(L.smem) + packetStateBytes<float>(L.threads);
+  cudaError_t e = cudaFuncSetAttribute(transportKernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  transportKernel<float><<<L.blocks, L.threads, smem, s>>>(g, in, out, cnt, seed, base, n, deltaE,
                                                          L.emitBatch > 0 ? L.emitBatch : kEmitBatch);
   return cudaGetLastError();
 }
@@ -17,17 +20,28 @@ cudaError_t launchTransportBatchedF32(const DevGrid& g, const DevTransportIn& in
                                       const unsigned long long* pktBegin, int nNeb, const float* axes,
                                       const int32_t* active, const float* cdfs, const TransportLaunch& L,
                                       cudaStream_t s) {
-  transportKernelBatched<float><<<L.blocks, L.threads, L.smem, s>>>(g, in, out, cnt, neb, pktBegin, nNeb, axes, active,
+  const size_t smem = packetStateOffset(L.smem) + packetStateBytes<float>(L.threads);
+  cudaError_t e =
+      cudaFuncSetAttribute(transportKernelBatched<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  transportKernelBatched<float><<<L.blocks, L.threads, smem, s>>>(g, in, out, cnt, neb, pktBegin, nNeb, axes, active,
                                                                   cdfs, L.emitBatch > 0 ? L.emitBatch : kEmitBatch);
   return cudaGetLastError();
 }
 
 cudaError_t transportOccupancyBatchedF32(int threads, size_t smem, int* blocksPerSM) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, transportKernelBatched<float>, threads, smem);
+  const size_t all = packetStateOffset(smem) + packetStateBytes<float>(threads);
+  cudaError_t e =
+      cudaFuncSetAttribute(transportKernelBatched<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)all);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, transportKernelBatched<float>, threads, all);
 }
 
 cudaError_t transportOccupancyF32(int threads, size_t smem, int* blocksPerSM) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, transportKernel<float>, threads, smem);
+  const size_t all = packetStateOffset(smem) + packetStateBytes<float>(threads);
+  cudaError_t e = cudaFuncSetAttribute(transportKernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)all);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, transportKernel<float>, threads, all);
 }
 
 }  // namespace mcx

@@ -7,7 +7,10 @@ namespace mcx {
 cudaError_t launchTransportF64(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,
                                DevTransportCounters* cnt, uint64_t seed, uint64_t base, unsigned long long n,
                                double deltaE, const TransportLaunch& L, cudaStream_t s) {
-  transportKernel<double><<<L.blocks, L.threads, L.smem, s>>>(g, in, out, cnt, seed, base, n, deltaE,
+  const size_t smem = packetStateOffset(L.smem) + packetStateBytes<double>(L.threads);
+  cudaError_t e = cudaFuncSetAttribute(transportKernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  transportKernel<double><<<L.blocks, L.threads, smem, s>>>(g, in, out, cnt, seed, base, n, deltaE,
                                                          L.emitBatch > 0 ? L.emitBatch : kEmitBatch);
   return cudaGetLastError();
 }
@@ -17,17 +20,28 @@ cudaError_t launchTransportBatchedF64(const DevGrid& g, const DevTransportIn& in
                                       const unsigned long long* pktBegin, int nNeb, const float* axes,
                                       const int32_t* active, const float* cdfs, const TransportLaunch& L,
                                       cudaStream_t s) {
-  transportKernelBatched<double><<<L.blocks, L.threads, L.smem, s>>>(g, in, out, cnt, neb, pktBegin, nNeb, axes, active,
+  const size_t smem = packetStateOffset(L.smem) + packetStateBytes<double>(L.threads);
+  cudaError_t e =
+      cudaFuncSetAttribute(transportKernelBatched<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  transportKernelBatched<double><<<L.blocks, L.threads, smem, s>>>(g, in, out, cnt, neb, pktBegin, nNeb, axes, active,
                                                                   cdfs, L.emitBatch > 0 ? L.emitBatch : kEmitBatch);
   return cudaGetLastError();
 }
 
 cudaError_t transportOccupancyBatchedF64(int threads, size_t smem, int* blocksPerSM) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, transportKernelBatched<double>, threads, smem);
+  const size_t all = packetStateOffset(smem) + packetStateBytes<double>(threads);
+  cudaError_t e =
+      cudaFuncSetAttribute(transportKernelBatched<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)all);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, transportKernelBatched<double>, threads, all);
 }
 
 cudaError_t transportOccupancyF64(int threads, size_t smem, int* blocksPerSM) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, transportKernel<double>, threads, smem);
+  const size_t all = packetStateOffset(smem) + packetStateBytes<double>(threads);
+  cudaError_t e = cudaFuncSetAttribute(transportKernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)all);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, transportKernel<double>, threads, all);
 }
 
 }  // namespace mcx
