@@ -17,10 +17,10 @@ cudaError_t launchForLines(BalanceData& bd, const float* te, const float* ne, co
                            const uint8_t* compute, float* forLines, cudaStream_t s);
 cudaError_t launchForbSums(BalanceData& bd, const LineSumArgs& a, cudaStream_t s);
 cudaError_t launchLineCells(BalanceData& bd, const LineCellArgs& a, cudaStream_t s);
-cudaError_t prepare(const BalanceData& bd);
+cudaError_t prepare(BalanceData& bd);
 }  // namespace bal_f64
 namespace bal_mixed {
-cudaError_t prepare(const BalanceData& bd);
+cudaError_t prepare(BalanceData& bd);
 cudaError_t buildCoolTable(const BalanceData& bd, float* tab, float* rtab, cudaStream_t s);
 cudaError_t buildAlphaTable(const BalanceData& bd, float* tab, uint8_t* jump, cudaStream_t s);
 cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStream_t s, int atomSolves);
@@ -278,14 +278,11 @@ std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out)
     d.augReals = nHeavy * 12 * (ns + 1);
     // zOf, xref, abun (3 x 32 words) and the (element, ion) shell offsets and counts (2 x E x 32 int16)
     d.metaDoubles = (3 * 32 * 4 + 2 * d.nElemUsed * 32 * 2 + 7) / 8;
-    // as many warps (4 cells each) per block as fit 200 KB in both builds
+    // one warp (4 cells) per block must fit 200 KB in both builds; prepare() picks the block size
     const size_t cellBytes = std::max((size_t)d.cellReals * sizeof(double),
                                       ((size_t)d.cellReals + (size_t)d.augReals) * sizeof(float));
-    d.ratesWarps = 0;
-    for (int wps : {4, 2, 1})
-      if (!d.ratesWarps && (size_t)d.metaDoubles * sizeof(double) + (size_t)wps * 4 * cellBytes <= 200 * 1024)
-        d.ratesWarps = wps;
-    if (!d.ratesWarps) return "balance: too many ions for the rates kernel";
+    if ((size_t)d.metaDoubles * sizeof(double) + 4 * cellBytes > 200 * 1024)
+      return "balance: too many ions for the rates kernel";
     if (nHeavy > 32) return "balance: more than 32 heavy elements";
     cudaError_t e1 = bal_f64::prepare(*bd), e2 = bal_mixed::prepare(*bd);
     if (e1 != cudaSuccess || e2 != cudaSuccess) return "balance: cannot reserve the rates kernel's shared memory";

@@ -81,7 +81,7 @@ struct BalanceDev {
   unsigned int* listCount;     // [kMaxRounds+1] cells listed for each round
   int32_t cellReals;           // shared memory of one cell of the rates kernel, in values of the rate precision
   int32_t metaDoubles;         // its per-block element tables, in doubles
-  int32_t ratesWarps;          // warps per block of the rates kernel (4 cells per warp)
+  int32_t ratesWarps[2];       // warps per block of the rates kernel (4 cells per warp), FP64 and mixed builds
   int32_t augReals;            // mixed build: further shared memory per cell, in floats
   int32_t secIonP, cRecoilHP, cRecoilHeP;
   float xhiLimit;

@@ -1655,6 +1655,7 @@ __global__ void storeKernel(BalanceDev b, BalanceGrid g) {
 #undef RD
 
 size_t ratesSmem(const BalanceDev& b);
+constexpr int kBuildL = MCX_BAL_EXACT ? 0 : 1;
 
 cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStream_t s, int atomSolves) {
   BalanceDev& b = bd.dev;
@@ -1675,11 +1676,12 @@ cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStr
   if (b.nShellsTot > 0) shellIntegralsKernel<<<(unsigned)b.nShellsTot * (unsigned)nb, T, 0, s>>>(b, g.jste);
   loadStateKernel<<<nb, T, 0, s>>>(b, g.te, g.ne, g.ionDen);
   const int rounds = std::min(std::max(maxRounds, 1), (int)b.maxIterT);
-  const int cellsPerBlock = b.ratesWarps * kCellsPerWarp;
+  const int cellsPerBlock = b.ratesWarps[kBuildL] * kCellsPerWarp;
   // round r works on the cells listed for it (the first list holds every cell
   // a packet reached; each secant step lists the cells that go on)
   for (int r = 1; r <= rounds; ++r) {
-    ratesKernel<<<(C + cellsPerBlock - 1) / cellsPerBlock, 32 * b.ratesWarps, ratesSmem(b), s>>>(b, g.hden, r - 1);
+    ratesKernel<<<(C + cellsPerBlock - 1) / cellsPerBlock, 32 * b.ratesWarps[kBuildL], ratesSmem(b), s>>>(b, g.hden,
+                                                                                                        r - 1);
 #if !MCX_BAL_EXACT
     if (b.nAtoms > 0 && useSurfaces) surfaceAtomsKernel<<<dim3(nb, b.nAtoms), T, 0, s>>>(b, r - 1);
     else
@@ -1711,17 +1713,39 @@ cudaError_t buildCoolTable(const BalanceData& bd, float* tab, float* rtab, cudaS
 }
 #endif
 
-// the rates kernel's dynamic shared memory: the element tables and one slice per cell of the block
-size_t ratesSmem(const BalanceDev& b) {
+constexpr int kBuild = MCX_BAL_EXACT ? 0 : 1;
+
+// the rates kernel's dynamic shared memory for wps warps per block: the element
+// tables and one slice per cell of the block
+size_t ratesSmemFor(const BalanceDev& b, int wps) {
 #if MCX_BAL_EXACT
   const size_t cell = (size_t)b.cellReals;
 #else
   const size_t cell = (size_t)b.cellReals + (size_t)b.augReals;
 #endif
-  return (size_t)b.metaDoubles * sizeof(double) + (size_t)b.ratesWarps * kCellsPerWarp * cell * sizeof(real);
+  return (size_t)b.metaDoubles * sizeof(double) + (size_t)wps * kCellsPerWarp * cell * sizeof(real);
 }
+size_t ratesSmem(const BalanceDev& b) { return ratesSmemFor(b, b.ratesWarps[kBuild]); }
 
-cudaError_t prepare(const BalanceData& bd) {
+// the block size (4, 2 or 1 warps) that keeps the most warps resident with
+// this build's shared memory per cell and registers
+cudaError_t prepare(BalanceData& bd) {
+  int best = 0, bestWarps = 0;
+  for (int wps : {4, 2, 1}) {
+    const size_t smem = ratesSmemFor(bd.dev, wps);
+    if (smem > 200 * 1024) continue;
+    cudaError_t e = cudaFuncSetAttribute(ratesKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int blocks = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, ratesKernel, 32 * wps, smem);
+    if (e != cudaSuccess) return e;
+    if (blocks * wps > bestWarps) {
+      bestWarps = blocks * wps;
+      best = wps;
+    }
+  }
+  if (!best) return cudaErrorInvalidValue;
+  bd.dev.ratesWarps[kBuild] = best;
   return cudaFuncSetAttribute(ratesKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ratesSmem(bd.dev));
 }
 
