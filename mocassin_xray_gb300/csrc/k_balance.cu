@@ -275,7 +275,7 @@ std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out)
     for (int e = 1; e <= d.nElemUsed; ++e) nHeavy += d.zOf[e] >= 3 ? 1 : 0;
     d.cellReals = 3 * NP + nSh + std::max(NP, nSh) + std::max(nHeavy * 3 * (ns + 3), 4 * d.nElemUsed);
     // the mixed build's per-heavy-element sums of the photoionisation rates, Auger band and charge exchange
-    d.augReals = nHeavy * 12 * (ns + 1);
+    d.augReals = nHeavy * 13 * (ns + 1);
     // zOf, xref, abun (3 x 32 words) and the (element, ion) shell offsets and counts (2 x E x 32 int16)
     d.metaDoubles = (3 * 32 * 4 + 2 * d.nElemUsed * 32 * 2 + 7) / 8;
     // one warp (4 cells) per block must fit 200 KB in both builds; prepare() picks the block size

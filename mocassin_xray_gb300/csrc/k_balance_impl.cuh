@@ -393,9 +393,10 @@ struct WarpCell {
   real* PI;      // [nShellsTot] photoIon(1): rate per shell, with the reverse charge exchange
   real* T;       // scratch for ordered sums
   real* LAD;     // [nHeavy][3][S+3] out, inn, mat of the ladders; later the thermBalance terms [4][E]
-  real* AUG;     // mixed build: [nHeavy][12 (S+1)] per heavy element the sums over shells of the
-                 // photoionisation rate per ion, charge exchange per ion, and the Auger band
-                 // A[ion][d] = sum of photoIon * auger feeding ion + d
+  real* AUG;     // mixed build: [nHeavy][13 (S+1)] per heavy element the sums over shells of the
+                 // photoionisation rate per ion, charge exchange per ion, the Auger band
+                 // A[ion][d] = sum of photoIon * auger feeding ion + d, and per ion the mask of
+                 // the d with A[ion - d][d] != 0
 };
 
 __device__ __forceinline__ real& xAt(const BalanceDev& b, const ElemMeta& m, const WarpCell& w, int z, int st) {
@@ -421,7 +422,7 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
   real neR = (real)ne;
   real cxHHe[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
   real piHHe[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};   // the outer shell's photoionisation rate
-  if (L.gl == 0)
+  if (L.gl < 2)
     for (int elem = 1; elem <= 2; ++elem)
       for (int ion = 1; ion <= min(elem, ns - 1); ++ion) {
         cxHHe[elem][ion] = chexFit(b, elem, ion, teR);
@@ -449,11 +450,12 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
   for (int q = 0; q < nMine; ++q) {
     const int e = myE[q], h = myH[q];
     const int elem = m.zOf[e];
-    real* S = w.AUG + (size_t)h * 12 * (ns + 1);
+    real* S = w.AUG + (size_t)h * 13 * (ns + 1);
     real* CH = S + (ns + 1);
     real* A = CH + (ns + 1);
+    unsigned* feed = reinterpret_cast<unsigned*>(A + 10 * (ns + 1));   // [ion]: bit d set if A[ion - d][d] != 0
     const int topI = min(elem, ns - 1), lim = min(ns - 1, elem);
-    for (int k = 0; k < 12 * (ns + 1); ++k) S[k] = 0;
+    for (int k = 0; k < 13 * (ns + 1); ++k) S[k] = 0;
     for (int ion = 1; ion <= topI; ++ion) {
       CH[ion] = chexRaw(b, elem, ion);
       const int p0 = m.p0[(e - 1) * 32 + (ion - 1)];
@@ -469,6 +471,12 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
         }
       }
     }
+    for (int t = 1; t <= topI; ++t) {
+      unsigned mask = 0u;
+      for (int d = 0; d <= 9 && d < t; ++d)
+        if (A[(t - d) * 10 + d] != (real)0.) mask |= 1u << d;
+      feed[t] = mask;
+    }
   }
 #endif
   for (int nIterateX = 1;; ++nIterateX) {
@@ -477,39 +485,29 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
     const real HeIOld = heOn ? xAt(b, m, w, zHe, 1) : (real)0.;
     const real HeIIOld = heOn ? xAt(b, m, w, zHe, 2) : (real)0.;
     __syncwarp(L.mask);
-    if (L.gl == 0) {
-      real ionRatio[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-      real ionProd[3][3] = {{1, 1, 1}, {1, 1, 1}, {1, 1, 1}};
-      real den[3] = {1, 1, 1};
+    // H on the group's first lane, He on its second (independent of each other within an X-iteration)
+    if (L.gl < 2 && m.xref[L.gl + 1]) {
+      const int elem = L.gl + 1;
+      real ionRatio[3] = {0, 0, 0};
+      real ionProd[3] = {1, 1, 1};
+      real den = 1;
       real collIonH = collIonH0;
-      for (int elem = 1; elem <= 2; ++elem) {
-        if (!m.xref[elem]) continue;
-        for (int ion = 1; ion <= min(elem, ns - 1); ++ion) {
-          real cx = cxHHe[elem][ion];
-          if (elem > 1 || ion > 1) collIonH = 0;
-          real pi = piHHe[elem][ion];
-          const real num = pi + collIonH * neR + (real)0.;
-          const real dnm = neR * w.AL[(m.xref[elem] - 1) * ns + (ion - 1)] + cx * hdenR * HIOld;
-          ionRatio[elem][ion] = num / dnm;
-        }
+      for (int ion = 1; ion <= min(elem, ns - 1); ++ion) {
+        real cx = cxHHe[elem][ion];
+        if (elem > 1 || ion > 1) collIonH = 0;
+        real pi = piHHe[elem][ion];
+        const real num = pi + collIonH * neR + (real)0.;
+        const real dnm = neR * w.AL[(m.xref[elem] - 1) * ns + (ion - 1)] + cx * hdenR * HIOld;
+        ionRatio[ion] = num / dnm;
       }
-      for (int elem = 1; elem <= 2; ++elem) {
-        if (!m.xref[elem]) continue;
-        for (int ion = 1; ion <= min(elem, ns - 1); ++ion)
-          for (int i = 1; i <= ion; ++i) ionProd[elem][ion] = ionProd[elem][ion] * ionRatio[elem][i];
-      }
-      for (int elem = 1; elem <= 2; ++elem) {
-        if (!m.xref[elem]) continue;
-        for (int ion = 1; ion <= min(elem, ns - 1); ++ion) den[elem] = den[elem] + ionProd[elem][ion];
-      }
-      for (int elem = 1; elem <= 2; ++elem) {
-        if (!m.xref[elem]) continue;
-        for (int ion = 1; ion <= min(elem + 1, ns); ++ion) {
-          real v = ion == 1 ? (real)1. / den[elem] : ionProd[elem][ion - 1] / den[elem];
-          if (v > (real)kXMax()) v = (real)kXMax();
-          if (v < (real)RD(1.e-20)) v = (real)RD(1.e-20);
-          xAt(b, m, w, elem, ion) = v;
-        }
+      for (int ion = 1; ion <= min(elem, ns - 1); ++ion)
+        for (int i = 1; i <= ion; ++i) ionProd[ion] = ionProd[ion] * ionRatio[i];
+      for (int ion = 1; ion <= min(elem, ns - 1); ++ion) den = den + ionProd[ion];
+      for (int ion = 1; ion <= min(elem + 1, ns); ++ion) {
+        real v = ion == 1 ? (real)1. / den : ionProd[ion - 1] / den;
+        if (v > (real)kXMax()) v = (real)kXMax();
+        if (v < (real)RD(1.e-20)) v = (real)RD(1.e-20);
+        xAt(b, m, w, elem, ion) = v;
       }
     }
     __syncwarp(L.mask);
@@ -577,9 +575,10 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
       // one pass over the stages: out (collisional and photoionisation, the Auger electrons of
       // the lower stages ion - d into ion, times X(ion - d) / X(ion)) and inn of each stage, and
       // the running log of the ladder's product
-      const real* S = w.AUG + (size_t)h * 12 * (ns + 1);
+      const real* S = w.AUG + (size_t)h * 13 * (ns + 1);
       const real* CH = S + (ns + 1);
       const real* A = CH + (ns + 1);
+      const unsigned* feed = reinterpret_cast<const unsigned*>(A + 10 * (ns + 1));
       const real* XE = w.X + (e - 1);   // X of this element's stage ion at XE[(ion - 1) * E]
       float* lm = mat;
       lm[1] = 0.f;
@@ -587,9 +586,9 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
       for (int ion = 1; ion <= topI; ++ion) {
         const real xi = XE[(ion - 1) * E];
         real o = w.CC[(e - 1) * ns + (ion - 1)] * neR + S[ion];
-        for (int d = 0; d <= 9 && d < ion; ++d) {   // d = 0: Auger electrons clamped at lim
-          const real a = A[(ion - d) * 10 + d];
-          if (a != (real)0.) o = o + a * (xi > (real)1e-30 ? __fdividef(XE[(ion - d - 1) * E], xi) : (real)1.);
+        for (unsigned mk = feed[ion]; mk; mk &= mk - 1u) {   // the stages ion - d feeding ion (d = 0: clamped at lim)
+          const int d = __ffs(mk) - 1;
+          o = o + A[(ion - d) * 10 + d] * (xi > (real)1e-30 ? __fdividef(XE[(ion - d - 1) * E], xi) : (real)1.);
         }
         const real in_ = neR * w.AL[(e - 1) * ns + (ion - 1)] + CH[ion] * hdenR * xH0now;
         lcur = lcur + log2f(__fdividef(o, in_));
