@@ -276,11 +276,12 @@ std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out)
     d.cellReals = 3 * NP + nSh + std::max(NP, nSh) + std::max(nHeavy * 3 * (ns + 3), 4 * d.nElemUsed);
     // the mixed build's per-heavy-element sums of the photoionisation rates, Auger band and charge exchange
     d.augReals = nHeavy * 13 * (ns + 1);
+    d.cellRealsMixed = 3 * NP + nSh + std::max(NP, nSh) + std::max(nHeavy * (ns + 3), 4 * d.nElemUsed);
     // zOf, xref, abun (3 x 32 words) and the (element, ion) shell offsets and counts (2 x E x 32 int16)
     d.metaDoubles = (3 * 32 * 4 + 2 * d.nElemUsed * 32 * 2 + 7) / 8;
     // one warp (4 cells) per block must fit 200 KB in both builds; prepare() picks the block size
     const size_t cellBytes = std::max((size_t)d.cellReals * sizeof(double),
-                                      ((size_t)d.cellReals + (size_t)d.augReals) * sizeof(float));
+                                      ((size_t)d.cellRealsMixed + (size_t)d.augReals) * sizeof(float));
     if ((size_t)d.metaDoubles * sizeof(double) + 4 * cellBytes > 200 * 1024)
       return "balance: too many ions for the rates kernel";
     if (nHeavy > 32) return "balance: more than 32 heavy elements";

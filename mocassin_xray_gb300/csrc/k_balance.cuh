@@ -83,6 +83,7 @@ struct BalanceDev {
   int32_t metaDoubles;         // its per-block element tables, in doubles
   int32_t ratesWarps[2];       // warps per block of the rates kernel (4 cells per warp), FP64 and mixed builds
   int32_t augReals;            // mixed build: further shared memory per cell, in floats
+  int32_t cellRealsMixed;      // mixed build: cellReals with one scratch row per ladder instead of three
   int32_t secIonP, cRecoilHP, cRecoilHeP;
   float xhiLimit;
   // T-iteration controls: the reference's (2 % residual, 1 % X(H0), X(He0),

@@ -517,9 +517,13 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
       const int e = myE[q], h = myH[q];
       const int elem = m.zOf[e];
       typedef real lad;
+#if MCX_BAL_EXACT
       lad* out = w.LAD + (size_t)h * 3 * (ns + 3);
       lad* inn = out + (ns + 3);
       real* mat = inn + (ns + 3);
+#else
+      real* mat = w.LAD + (size_t)h * (ns + 3);   // the running logs only
+#endif
       const int topI = min(elem, ns - 1);
 #if MCX_BAL_EXACT
       for (int k = 0; k < ns + 3; ++k) { out[k] = 0; inn[k] = 0; }
@@ -695,14 +699,14 @@ __global__ void __launch_bounds__(128) ratesKernel(BalanceDev b, const float* __
 #if MCX_BAL_EXACT
   w.X = reinterpret_cast<real*>(wsm + b.metaDoubles) + (size_t)slot * b.cellReals;
 #else
-  w.X = reinterpret_cast<real*>(wsm + b.metaDoubles) + (size_t)slot * (b.cellReals + b.augReals);
+  w.X = reinterpret_cast<real*>(wsm + b.metaDoubles) + (size_t)slot * (b.cellRealsMixed + b.augReals);
 #endif
   w.AL = w.X + NP;
   w.CC = w.AL + NP;
   w.PI = w.CC + NP;
   w.T = w.PI + nSh;
   w.LAD = w.T + max(NP, nSh);
-  w.AUG = w.X + b.cellReals;
+  w.AUG = w.X + b.cellRealsMixed;
   for (int k = L.gl; k < NP; k += kGroup) w.X[k] = (real)b.ion[(size_t)k * C1 + cell];
   if (L.gl == 0) b.nIterT[cell] = b.nIterT[cell] + 1;
   const double te = b.te[cell];
@@ -1720,7 +1724,7 @@ size_t ratesSmemFor(const BalanceDev& b, int wps) {
 #if MCX_BAL_EXACT
   const size_t cell = (size_t)b.cellReals;
 #else
-  const size_t cell = (size_t)b.cellReals + (size_t)b.augReals;
+  const size_t cell = (size_t)b.cellRealsMixed + (size_t)b.augReals;
 #endif
   return (size_t)b.metaDoubles * sizeof(double) + (size_t)wps * kCellsPerWarp * cell * sizeof(real);
 }
