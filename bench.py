@@ -39,11 +39,12 @@ sys.path.insert(0, str(ROOT))
 DATA_DIR = ROOT / "tests" / "golden" / "atomic_data"
 METRIC = "MC packets/s"
 UNIT = "packets/s"
-# kernels of one step: opacity 1; emission 5 (Gaunt table, forbidden lines per
-# ion and their sum, emissivity, CDF transpose); transport 1; J normalisation
-# 1; balance 64 (hit test + Compton sums, shell integrals, state load, 20 rounds
-# x (rates, line cooling from the cooling surfaces, secant), store)
-KERNELS_PER_STEP = 1 + 5 + 1 + 1 + 64
+# kernels of one step: opacity 1; emission 7 (Gaunt table, the cells' places on
+# the surfaces, forbidden lines per ion and their sum, the two passes of the
+# emissivity, CDF transpose); transport 1; J normalisation 1; balance 64 (hit
+# test + Compton sums, shell integrals, state load, 20 rounds x (rates, line
+# cooling from the cooling surfaces, secant), store)
+KERNELS_PER_STEP = 1 + 7 + 1 + 1 + 64
 
 
 def parse():
