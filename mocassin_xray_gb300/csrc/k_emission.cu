@@ -292,6 +292,8 @@ emissionKernel(EmissionDev e, const float* __restrict__ te, const float* __restr
   if (mode == 1) {
   const int q = blockIdx.y;
   const int i0 = 1 + q * chunkLen, i1 = min(nb, (q + 1) * chunkLen);
+  int gP[3] = {0, 0, 0};
+  float gL2[3] = {0.f, 0.f, 0.f}, gA[3] = {0.f, 0.f, 0.f}, gNu[3] = {0.f, 0.f, 0.f};
   for (int i = i0; i <= i1; ++i) {
     const float v = e.nu[i - 1];
     float gHI = 0.f, gHeI = 0.f, gHeII = 0.f;
@@ -300,10 +302,15 @@ emissionKernel(EmissionDev e, const float* __restrict__ te, const float* __restr
     for (int k = 0; k < 3; ++k) {
       int p = e.pairIdx[(size_t)k * nb + (i - 1)];
       if (p > 0) {
-        int iup = e.edgeP[k * 32 + 2 * p - 1], ilow = e.edgeP[k * 32 + 2 * p - 2];
-        float l2 = logG(k, 2 * p), l1 = logG(k, 2 * p - 1);
-        float aFit = (l2 - l1) / (e.nu[iup - 1] - e.nu[ilow - 1]);
-        g[k] = exp10f(l2 + aFit * (v - e.nu[iup - 1]));
+        if (p != gP[k]) {   // a new edge pair: its fit, kept for the following bins of the pair
+          int iup = e.edgeP[k * 32 + 2 * p - 1], ilow = e.edgeP[k * 32 + 2 * p - 2];
+          float l2 = logG(k, 2 * p), l1 = logG(k, 2 * p - 1);
+          gP[k] = p;
+          gL2[k] = l2;
+          gA[k] = (l2 - l1) / (e.nu[iup - 1] - e.nu[ilow - 1]);
+          gNu[k] = e.nu[iup - 1];
+        }
+        g[k] = exp10f(gL2[k] + gA[k] * (v - gNu[k]));
       }
     }
     gHI = g[0]; gHeI = g[1]; gHeII = g[2];
