@@ -250,6 +250,7 @@ __global__ void __launch_bounds__(128) hitComptonKernel(BalanceDev b, const doub
   b.list[atomicAdd(&b.listCount[0], 1u)] = cell;   // the cells of the first T-iteration
   if (b.lgCompton) {
     real s1 = 0, s2 = 0, rhH = 0, rhHe = 0;
+#pragma unroll 4
     for (int i = 1; i <= b.nbins; ++i) {
       real rf = J(i);
       s1 = s1 + rf;
