@@ -82,6 +82,8 @@ struct BalanceDev {
   int32_t cellReals;           // shared memory of one cell of the rates kernel, in values of the rate precision
   int32_t metaDoubles;         // its per-block element tables, in doubles
   int32_t ratesWarps[2];       // warps per block of the rates kernel (4 cells per warp), FP64 and mixed builds
+  int32_t ratesGrid[2];        // its resident blocks on the GPU, the grid of the per-round launches
+  int32_t smCount;
   int32_t augReals;            // mixed build: further shared memory per cell, in floats
   int32_t cellRealsMixed;      // mixed build: cellReals with one scratch row per ladder instead of three
   int32_t secIonP, cRecoilHP, cRecoilHeP;

@@ -667,35 +667,11 @@ __device__ bool ionBalanceWarp(const BalanceDev& b, const ElemMeta& m, const War
 // calcAlpha, photoionisation, collisionalIonisation, compton, ionBalance and
 // the thermBalance terms without forLines, kGroup lanes per iterating cell
 // (b.cellReals values of the rate precision in shared memory per cell).
-__global__ void __launch_bounds__(128) ratesKernel(BalanceDev b, const float* __restrict__ hdenG, int round) {
-  extern __shared__ double wsm[];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, grp = lane / kGroup;
-  const Lanes L{lane % kGroup, ((1u << kGroup) - 1u) << (grp * kGroup)};
-  const int cellsPerBlock = (blockDim.x >> 5) * kCellsPerWarp;
-  const int slot = wib * kCellsPerWarp + grp;
-  const int li = blockIdx.x * cellsPerBlock + slot;   // index into this round's cell list
-  const unsigned cnt = b.listCount[round];
-  if ((unsigned)(blockIdx.x * cellsPerBlock) >= cnt) return;   // the whole block
+// One listed cell of the rates kernel on its group of lanes.
+__device__ __forceinline__ void ratesCell(const BalanceDev& b, const float* __restrict__ hdenG, int round, int li,
+                                          const ElemMeta& m, const Lanes& L, double* wsm, int slot) {
   const int C1 = b.nCells + 1, ns = b.nstages, E = b.nElemUsed, NP = E * ns, nSh = b.nShellsTot;
-  // the element tables, then one slice per warp
-  int32_t* sZ = reinterpret_cast<int32_t*>(wsm);
-  int32_t* sX = sZ + 32;
-  float* sA = reinterpret_cast<float*>(sX + 32);
-  int16_t* sP0 = reinterpret_cast<int16_t*>(sA + 32);
-  int16_t* sNs = sP0 + E * 32;
-  for (int i = threadIdx.x; i < 32; i += blockDim.x) {
-    sZ[i] = i <= 30 ? b.zOf[i] : 0;
-    sX[i] = i <= 30 ? b.xref[i] : 0;
-    sA[i] = i <= 30 ? b.abun[i] : 0.f;
-  }
-  for (int i = threadIdx.x; i < E * 32; i += blockDim.x) {
-    sP0[i] = (int16_t)b.pairShell0[i];
-    sNs[i] = (int16_t)b.pairNShell[i];
-  }
-  __syncthreads();
-  if ((unsigned)li >= cnt) return;   // the whole group
   const int cell = b.list[(size_t)(round & 1) * C1 + li];
-  const ElemMeta m{sZ, sX, sA, sP0, sNs};
   WarpCell w;
 #if MCX_BAL_EXACT
   w.X = reinterpret_cast<real*>(wsm + b.metaDoubles) + (size_t)slot * b.cellReals;
@@ -899,6 +875,39 @@ __global__ void __launch_bounds__(128) ratesKernel(BalanceDev b, const float* __
   b.coolHex[cell] = coolColl;
   b.coolCollH[cell] = coolCollH;
   b.heat[cell] = heatSte;
+}
+
+__global__ void __launch_bounds__(128) ratesKernel(BalanceDev b, const float* __restrict__ hdenG, int round) {
+  extern __shared__ double wsm[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, grp = lane / kGroup;
+  const Lanes L{lane % kGroup, ((1u << kGroup) - 1u) << (grp * kGroup)};
+  const int cellsPerBlock = (blockDim.x >> 5) * kCellsPerWarp;
+  const int slot = wib * kCellsPerWarp + grp;
+  const unsigned cnt = b.listCount[round];
+  if ((unsigned)(blockIdx.x * cellsPerBlock) >= cnt) return;   // the whole block
+  const int E = b.nElemUsed;
+  // the element tables, then one slice per warp
+  int32_t* sZ = reinterpret_cast<int32_t*>(wsm);
+  int32_t* sX = sZ + 32;
+  float* sA = reinterpret_cast<float*>(sX + 32);
+  int16_t* sP0 = reinterpret_cast<int16_t*>(sA + 32);
+  int16_t* sNs = sP0 + E * 32;
+  for (int i = threadIdx.x; i < 32; i += blockDim.x) {
+    sZ[i] = i <= 30 ? b.zOf[i] : 0;
+    sX[i] = i <= 30 ? b.xref[i] : 0;
+    sA[i] = i <= 30 ? b.abun[i] : 0.f;
+  }
+  for (int i = threadIdx.x; i < E * 32; i += blockDim.x) {
+    sP0[i] = (int16_t)b.pairShell0[i];
+    sNs[i] = (int16_t)b.pairNShell[i];
+  }
+  __syncthreads();
+  const ElemMeta m{sZ, sX, sA, sP0, sNs};
+  // the listed cells in strides of the grid (the grid is sized for the resident blocks)
+  for (unsigned base = blockIdx.x * cellsPerBlock; base < cnt; base += gridDim.x * cellsPerBlock) {
+    const unsigned li = base + slot;
+    if (li < cnt) ratesCell(b, hdenG, round, (int)li, m, L, wsm, slot);
+  }
 }
 
 // ------------------------------------------------------------- equilibrium
@@ -1513,10 +1522,8 @@ __device__ __forceinline__ float2 surfaceAt(const float* tab, int atom, const Co
 // stencil is interpolated as differences from its (iN, iT) node so that the
 // FP32 sums keep the precision of the stored values; cells outside the grid
 // solve the ion directly.
-__global__ void __launch_bounds__(128) surfaceAtomsKernel(BalanceDev b, int round) {
-  const int li = blockIdx.x * blockDim.x + threadIdx.x;
-  const int atom = blockIdx.y;
-  if ((unsigned)li >= b.listCount[round]) return;
+// one (listed cell, ion) of surfaceAtomsKernel
+__device__ __forceinline__ void surfaceAtom(const BalanceDev& b, int round, int li, int atom) {
   const int cell = b.list[(size_t)(round & 1) * (b.nCells + 1) + li];
   const CellIdx c{cell, b.nCells + 1};
   const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
@@ -1538,12 +1545,17 @@ __global__ void __launch_bounds__(128) surfaceAtomsKernel(BalanceDev b, int roun
   }
   *out = w * RD(1.9865e-16) * g;
 }
+
+__global__ void __launch_bounds__(128) surfaceAtomsKernel(BalanceDev b, int round) {
+  const int atom = blockIdx.y;
+  const unsigned cnt = b.listCount[round];
+  for (unsigned li = blockIdx.x * blockDim.x + threadIdx.x; li < cnt; li += gridDim.x * blockDim.x)
+    surfaceAtom(b, round, (int)li, atom);
+}
 #endif
 
 // heating - cooling and the secant step of iterateT (FP64 in both precisions)
-__global__ void __launch_bounds__(128) secantKernel(BalanceDev b, int round, int lastRound) {
-  const int li = blockIdx.x * blockDim.x + threadIdx.x;
-  if ((unsigned)li >= b.listCount[round]) return;
+__device__ __forceinline__ void secantCell(const BalanceDev& b, int round, int lastRound, int li) {
   const int C1 = b.nCells + 1;
   const int cell = b.list[(size_t)(round & 1) * C1 + li];
   double coolColl = b.coolHex[cell];
@@ -1629,6 +1641,12 @@ __global__ void __launch_bounds__(128) secantKernel(BalanceDev b, int round, int
   }
 }
 
+__global__ void __launch_bounds__(128) secantKernel(BalanceDev b, int round, int lastRound) {
+  const unsigned cnt = b.listCount[round];
+  for (unsigned li = blockIdx.x * blockDim.x + threadIdx.x; li < cnt; li += gridDim.x * blockDim.x)
+    secantCell(b, round, lastRound, (int)li);
+}
+
 // Writes the results of the cells back to the grid (FP32) and the flags.
 __global__ void storeKernel(BalanceDev b, BalanceGrid g) {
   const int cell = blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -1681,17 +1699,21 @@ cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStr
   loadStateKernel<<<nb, T, 0, s>>>(b, g.te, g.ne, g.ionDen);
   const int rounds = std::min(std::max(maxRounds, 1), (int)b.maxIterT);
   const int cellsPerBlock = b.ratesWarps[kBuildL] * kCellsPerWarp;
+  // the per-round kernels stride over their lists with grids of resident size, so
+  // the late rounds (few listed cells) do not launch a block per cell of the grid
+  const int rGrid = std::max(1, std::min((C + cellsPerBlock - 1) / cellsPerBlock, b.ratesGrid[kBuildL]));
+  const int aGrid = std::max(1, std::min(nb, 8 * b.smCount / std::max(1, b.nAtoms) + 1));
+  const int sGrid = std::max(1, std::min(nb, 8 * b.smCount));
   // round r works on the cells listed for it (the first list holds every cell
   // a packet reached; each secant step lists the cells that go on)
   for (int r = 1; r <= rounds; ++r) {
-    ratesKernel<<<(C + cellsPerBlock - 1) / cellsPerBlock, 32 * b.ratesWarps[kBuildL], ratesSmem(b), s>>>(b, g.hden,
-                                                                                                        r - 1);
+    ratesKernel<<<rGrid, 32 * b.ratesWarps[kBuildL], ratesSmem(b), s>>>(b, g.hden, r - 1);
 #if !MCX_BAL_EXACT
-    if (b.nAtoms > 0 && useSurfaces) surfaceAtomsKernel<<<dim3(nb, b.nAtoms), T, 0, s>>>(b, r - 1);
+    if (b.nAtoms > 0 && useSurfaces) surfaceAtomsKernel<<<dim3(aGrid, b.nAtoms), T, 0, s>>>(b, r - 1);
     else
 #endif
     if (b.nAtoms > 0) atomsKernel<<<dim3(nb, b.nAtoms), T, 0, s>>>(b, r - 1);
-    secantKernel<<<nb, T, 0, s>>>(b, r - 1, r == rounds && rounds < b.maxIterT ? 1 : 0);
+    secantKernel<<<sGrid, T, 0, s>>>(b, r - 1, r == rounds && rounds < b.maxIterT ? 1 : 0);
   }
   storeKernel<<<nb, T, 0, s>>>(b, g);
   return cudaGetLastError();
@@ -1734,7 +1756,7 @@ size_t ratesSmem(const BalanceDev& b) { return ratesSmemFor(b, b.ratesWarps[kBui
 // the block size (4, 2 or 1 warps) that keeps the most warps resident with
 // this build's shared memory per cell and registers
 cudaError_t prepare(BalanceData& bd) {
-  int best = 0, bestWarps = 0;
+  int best = 0, bestWarps = 0, bestBlocks = 0;
   for (int wps : {4, 2, 1}) {
     const size_t smem = ratesSmemFor(bd.dev, wps);
     if (smem > 200 * 1024) continue;
@@ -1746,10 +1768,17 @@ cudaError_t prepare(BalanceData& bd) {
     if (blocks * wps > bestWarps) {
       bestWarps = blocks * wps;
       best = wps;
+      bestBlocks = blocks;
     }
   }
   if (!best) return cudaErrorInvalidValue;
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  bd.dev.smCount = sms;
   bd.dev.ratesWarps[kBuild] = best;
+  bd.dev.ratesGrid[kBuild] = bestBlocks * sms;
   return cudaFuncSetAttribute(ratesKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ratesSmem(bd.dev));
 }
 
