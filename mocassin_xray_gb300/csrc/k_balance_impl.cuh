@@ -1,10 +1,17 @@
 // k_balance_impl.cuh - device code of the balance phase, compiled twice:
 //   k_balance_f64.cu    real = double, --fmad=false: the plain FP64 path that is
-//                       checked against the oracle operation by operation
+//                       checked against the oracle operation by operation; its
+//                       exp, log, log10 and pow are the portable routines of
+//                       mcx_fmath.h, which the oracle uses too
 //   k_balance_mixed.cu  real = float: rates, splines and exponentials in FP32
-//                       (the reference's own REAL), while the level-population
-//                       LU solve, the ionisation ladder and its normalisation,
-//                       the electron density and the Te bracketing stay FP64
+//                       (the reference's own REAL); the X-iteration loop in
+//                       FP32 too (the ionisation ladder on the base-2
+//                       logarithms of its products, its normalisation, H/He
+//                       ratios and Ne); level populations by FP32 state
+//                       reduction (the FP64 LU only for a level without an
+//                       exit below it); line cooling read from per-ion cooling
+//                       surfaces; only the Te bracketing of the secant step
+//                       stays FP64
 // The including file defines MCX_BAL_REAL, MCX_BAL_NS and MCX_BAL_EXACT.
 //
 // Reference routines: updateCell / iterateT (source/update_mod.f90:15-482),
@@ -17,6 +24,7 @@
 #include "k_balance.cuh"
 #include "k_lines.cuh"
 #include "setup_internal.h"
+#include "mcx_fmath.h"
 
 #include <algorithm>
 
@@ -24,6 +32,16 @@ namespace mcx {
 namespace MCX_BAL_NS {
 
 typedef MCX_BAL_REAL real;
+
+#if MCX_BAL_EXACT
+// Unqualified exp / log / log10 / pow calls of this namespace resolve here
+// (before the global CUDA overloads): the portable routines shared with the
+// oracle, so that both round alike and take the same branches.
+__host__ __device__ __forceinline__ double exp(double x) { return mcx_fm_exp(x); }
+__host__ __device__ __forceinline__ double log(double x) { return mcx_fm_log(x); }
+__host__ __device__ __forceinline__ double log10(double x) { return mcx_fm_log10(x); }
+__host__ __device__ __forceinline__ double pow(double x, double y) { return mcx_fm_pow(x, y); }
+#endif
 
 // a default-REAL constant of the reference, at its single-precision value, in
 // the rate precision (RF) or in FP64 (RD)

@@ -582,9 +582,17 @@ void setCompton(Setup& s) {
     s.comXSecC[i - 1] = alpha * beta * v * 3.858e-25f;
     if (i <= s.xrayP) s.xSecRecoil[i - 1] = thom;
     else {
-      float dx = v / 3.7573e4f;
-      s.xSecRecoil[i - 1] = thom * 3.f / 4.f * ((1.f + dx) / (dx * dx * dx) * (2.f * dx * (1.f + dx) / (1.f + 2.f * dx) - logf(1.f + 2.f * dx)) +
-                                               1.f / 2.f / dx * logf(1.f + 2.f * dx) - (1.f + 3.f * dx) / powf(1.f + 2.f * dx, 3.f));
+      // The reference evaluates this in single precision, where the first
+      // bracket (of order dx^3 against terms of order dx) cancels
+      // catastrophically below dx ~ 0.05 (about 2000 Ryd): its values there
+      // depend on the compiler's logf, swing up to 150 sigma_T and turn
+      // negative.  The same formula (with the reference's (1+2dx)^3 in the
+      // last term) is evaluated here in FP64 and stored in single precision.
+      const double dx = (double)v / 3.7573e4;
+      const double l = std::log(1. + 2. * dx);
+      s.xSecRecoil[i - 1] = (float)((double)thom * 3. / 4. *
+                                    ((1. + dx) / (dx * dx * dx) * (2. * dx * (1. + dx) / (1. + 2. * dx) - l) +
+                                     1. / 2. / dx * l - (1. + 3. * dx) / ((1. + 2. * dx) * (1. + 2. * dx) * (1. + 2. * dx))));
     }
   }
 }

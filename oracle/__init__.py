@@ -88,6 +88,8 @@ def lib() -> C.CDLL:
         l = C.CDLL(str(LIB_PATH))
         l.orc_philox4x32_10.argtypes = [_P, _P, _P]
         l.orc_philox4x32_10.restype = None
+        l.orc_fm_eval.argtypes = [C.c_int32, _P, _P, C.c_int64, _P]
+        l.orc_fm_eval.restype = None
         l.orc_transport.argtypes = [C.POINTER(TransportIn), C.c_uint64, C.c_uint64, C.c_int64, C.c_int32,
                                     C.POINTER(TransportOut), C.POINTER(TransportStats)]
         l.orc_transport.restype = C.c_int
@@ -112,6 +114,19 @@ def philox(ctr, key) -> np.ndarray:
     k = np.ascontiguousarray(key, dtype=np.uint32)
     out = np.zeros(4, dtype=np.uint32)
     lib().orc_philox4x32_10(_p(c), _p(k), _p(out))
+    return out
+
+
+FM_EXP, FM_LOG, FM_LOG10, FM_POW = 0, 1, 2, 3
+
+
+def fm_eval(fn: int, x, y=None) -> np.ndarray:
+    """The portable FP64 exp / log / log10 / pow that the oracle's balance and
+    the device's FP64 balance share, evaluated on the host."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(np.zeros_like(x) if y is None else y, dtype=np.float64)
+    out = np.empty_like(x)
+    lib().orc_fm_eval(fn, _p(x), _p(y), x.size, _p(out))
     return out
 
 

@@ -21,6 +21,15 @@
 #include <stdlib.h>
 #include <string.h>
 
+/* exp, log, log10 and pow from the portable FP64 routines that the device's
+ * FP64 balance uses too: both sides then round every step alike and every
+ * cell takes the same iterateT / ionBalance branches */
+#include "mcx_fmath.h"
+#define exp(x) mcx_fm_exp(x)
+#define log(x) mcx_fm_log(x)
+#define log10(x) mcx_fm_log10(x)
+#define pow(x, y) mcx_fm_pow((x), (y))
+
 #define R(x) ((double)(x##f))     /* a default-REAL constant of the reference */
 #define NEL 30
 #define MAXST 32

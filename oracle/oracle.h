@@ -31,6 +31,10 @@ extern "C" {
  * ctr=(p_lo, p_hi, k/4, 0)). */
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 
+/* The portable FP64 routines of mcx_fmath.h over arrays: fn 0 exp(x), 1 log(x),
+ * 2 log10(x), 3 pow(x, y). */
+void orc_fm_eval(int32_t fn, const double* x, const double* y, int64_t n, double* out);
+
 /* ------------------------------------------------------------ transport */
 typedef struct orc_transport_in {
     int32_t nx, ny, nz, n_cells, nbins;

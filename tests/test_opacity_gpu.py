@@ -78,19 +78,29 @@ def test_opacity_skip_rule(decks, data_dir, oracle_lib):
 
 
 def test_hydrogen_threshold_opacity(decks, data_dir):
-    """Analytic check: at the Lyman edge the H-only opacity is
-    sigma_H(1 Ryd) * n(H0) + sigma_KN * Ne (no H+ free-free term in the reference)."""
+    """Analytic check, independent of the set-up's tables: at the Lyman edge the
+    H-only opacity is sigma_H(1 Ryd) n(H0) + sigma_KN Ne (no H+ free-free term in
+    the reference), with sigma_H from the Verner fit of data/ph1.dat
+    (6.30e-18 cm^2, oracle/setup_tables.py) and the Klein-Nishina total from
+    its angular integral, both built without libmcx."""
+    from oracle import setup_tables as ST
     s = Setup(decks["h_small"], data_dir)
     ctx = Context(0)
     ctx.load(s)
     ctx.opacity(1)
     op = ctx.get(abi.ARR_OPACITY)
-    ptr = s.get(abi.SARR_POINTERS)
-    hxs, hnu = ptr[0], ptr[1]
-    xs = s.get(abi.ARR_XSEC)
-    kn = s.get(abi.ARR_KN_SIGMA_T)
+    d = ST.read_deck(decks["h_small"])
+    ver = ST.Verner(data_dir)
+    nu, _ = ST.mesh(d, ver, abi.MESH_REFERENCE, data_dir)
+    hnu = ST.pointers(nu)["HlevNuP1"]
+    sigma_h = ver.xsec_mb(1, 1, 1, max(float(nu[hnu - 1]) * ST.RYD_TO_EV, ver.ph1[1, 1, 1, 1])) * 1e-18
+    assert sigma_h == pytest.approx(6.30e-18, rel=0.01)
+    kn = ST.compton(nu, ST.pointers(nu)["xrayP"])["kn_sigma_t"]
+    g = ST.grid(d)
     c = 1
-    n_h0 = 1e-5 * s.get(abi.ARR_HDEN)[c]
-    expect = xs[hxs - 1] * n_h0 + kn[hnu - 1] * s.get(abi.ARR_NE)[c]
+    n_h0 = 1e-5 * float(g["hden"][c])
+    ne = float(s.get(abi.ARR_NE)[c])
+    assert ne == pytest.approx(float(g["hden"][c]), rel=1e-6)     # Ne = Hden at start (grid_mod.f90:1627)
+    expect = sigma_h * n_h0 + kn[hnu - 1] * ne
     assert op[hnu - 1, c] == pytest.approx(expect, rel=1e-5)
     ctx.close()
