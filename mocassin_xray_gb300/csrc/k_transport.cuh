@@ -7,7 +7,10 @@
 // a warp stay on the same code path.  Packet geometry and optical depth run in
 // the template precision R (float: the production path; double: the plain
 // FP64 path); the mean-intensity estimator J_nu is accumulated with FP64
-// atomics into the Fortran-layout array Jste[nu][cell].  The source spectrum
+// atomics into the Fortran-layout array Jste[nu][cell], compensated: each
+// atomic's exact rounding error (TwoSum of the value it returned and the
+// deposit) goes to a second array Jlo, folded in after the launch, so the
+// result is the correctly rounded sum of the deposits whatever their order.  The source spectrum
 // CDF, the frequency mesh and the axes are staged in shared memory.
 //
 // Physics follows the reference routine by routine (single mother grid, no
@@ -23,6 +26,7 @@
 // reads, is not accumulated.
 #pragma once
 #include "mcx_device.cuh"
+#include "mcx_fmath.h"
 
 namespace mcx {
 
@@ -43,11 +47,13 @@ template <> struct RMath<float> {
   // the step's quotients: reciprocal-approximation division (2 ulp; operands far below 2^126)
   static __device__ __forceinline__ float div_(float a, float b) { return __fdividef(a, b); }
 };
+// the plain FP64 path: log, cos and sin from the portable routines the oracle
+// uses too (mcx_fmath.h), so that both draw the same packet histories
 template <> struct RMath<double> {
   static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
-  static __device__ __forceinline__ double log_(double x) { return log(x); }
-  static __device__ __forceinline__ double cos_(double x) { return cos(x); }
-  static __device__ __forceinline__ double sin_(double x) { return sin(x); }
+  static __device__ __forceinline__ double log_(double x) { return mcx_fm_log(x); }
+  static __device__ __forceinline__ double cos_(double x) { return mcx_fm_cos(x); }
+  static __device__ __forceinline__ double sin_(double x) { return mcx_fm_sin(x); }
   static __device__ __forceinline__ double abs_(double x) { return fabs(x); }
   static __device__ __forceinline__ double min_(double a, double b) { return fmin(a, b); }
   static __device__ __forceinline__ double div_(double a, double b) { return a / b; }
@@ -182,12 +188,39 @@ __device__ __forceinline__ void escapeTally(const DevGrid& g, const DevTransport
   ++lc.escaped;
 }
 
+// A J deposit whose rounding error is still to be added to Jlo.  The FP64
+// atomic returns the value it added to; that return is consumed one deposit
+// later (or when the lane goes idle), so the wait for it hides behind the
+// packet's next step instead of stalling this one.
+struct PendingJ {
+  double old, v;
+  size_t idx;
+  bool on;
+};
+
+__device__ __forceinline__ void flushJ(const DevTransportOut& out, PendingJ& pj) {
+  if (pj.on) {
+    const double err = mcx_fm_two_sum_err(pj.old, pj.v, pj.old + pj.v);
+    if (err != 0.) atomicAdd(out.jlo + pj.idx, err);
+    pj.on = false;
+  }
+}
+
 template <typename R>
 __device__ __forceinline__ void deposit(const DevGrid& g, const DevTransportOut& out, int cell, int nuP, R dl,
-                                        R dV, R deltaE, R costheta) {
+                                        R dV, R deltaE, R costheta, PendingJ& pj) {
   if (cell <= 0) return;
   size_t idx = (size_t)cell + ((size_t)g.nCells + 1) * (size_t)(nuP - 1);
-  atomicAdd(out.jste + idx, (double)RMath<R>::div_(dl * deltaE, dV));
+  const double v = (double)RMath<R>::div_(dl * deltaE, dV);
+  if (out.jlo) {
+    flushJ(out, pj);
+    pj.old = atomicAdd(out.jste + idx, v);
+    pj.v = v;
+    pj.idx = idx;
+    pj.on = true;
+  } else {
+    atomicAdd(out.jste + idx, v);
+  }
   if (out.hEst) atomicAdd(out.hEst + idx, (double)((dl * deltaE) * costheta / dV));
 }
 
@@ -290,8 +323,9 @@ __device__ __noinline__ int emitPacket(const DevGrid& g, const Geo& q, const Dev
 
 // One iteration of pathSegment's main loop (source/photon_mod.f90:1880-4036).
 template <typename R, typename Geo>
-__device__ int stepPacket(const DevGrid& g, const Geo& q, const DevTransportIn& in, const DevTransportOut& out,
-                          const TransportShared<R>& sh, Packet<R>& p, R deltaER, double deltaE, LocalCounters& lc) {
+__device__ __forceinline__ int stepPacket(const DevGrid& g, const Geo& q, const DevTransportIn& in,
+                                          const DevTransportOut& out, const TransportShared<R>& sh, Packet<R>& p,
+                                          R deltaER, double deltaE, LocalCounters& lc, PendingJ& pj) {
   using M = RMath<R>;
   const int nx = q.nx(), ny = q.ny(), nz = q.nz();
   const float* X = q.X(); const float* Y = q.Y(); const float* Z = q.Z();
@@ -384,7 +418,7 @@ __device__ int stepPacket(const DevGrid& g, const Geo& q, const DevTransportIn& 
       if (ry <= AXR(Y, 1)) { if (vy < R(0)) vy = -vy; ry = AXR(Y, 1); }
       if (rz <= AXR(Z, 1)) { if (vz < R(0)) vz = -vz; rz = AXR(Z, 1); }
     }
-    deposit<R>(g, out, cell, p.nuP, dlLoc, dV, deltaER, costheta);
+    deposit<R>(g, out, cell, p.nuP, dlLoc, dV, deltaER, costheta, pj);
     ++lc.interactions;
     R rad = M::sqrt_((rx / R(1.e10)) * (rx / R(1.e10)) + (ry / R(1.e10)) * (ry / R(1.e10)) +
                      (rz / R(1.e10)) * (rz / R(1.e10))) * R(1.e10);
@@ -425,7 +459,7 @@ __device__ int stepPacket(const DevGrid& g, const Geo& q, const DevTransportIn& 
     }
   } else {
     // the packet crosses the cell (source/photon_mod.f90:2703-2881)
-    deposit<R>(g, out, cell, p.nuP, dS, dV, deltaER, costheta);
+    deposit<R>(g, out, cell, p.nuP, dS, dV, deltaER, costheta, pj);
     ++lc.crossings;
     p.absTau = p.absTau + tauCell;
     rx = rx + dS * vx; ry = ry + dS * vy; rz = rz + dS * vz;
@@ -548,6 +582,7 @@ transportKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportC
       reinterpret_cast<char*>(smem) +
       packetStateOffset((size_t)(g.nx + g.ny + g.nz + 2 * g.nbins) * sizeof(float)))[threadIdx.x];
   p.nEmit = 0; p.nStep = 0;
+  PendingJ pj{0., 0., 0, false};
   int state = ST_IDLE;
 
   for (;;) {
@@ -569,9 +604,10 @@ transportKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportC
     if (emitTurn(state, emitBatch)) {
       if (state == ST_EMIT) state = emitPacket<R>(g, q, in, out, sh, p, deltaE, lc);
     } else if (state == ST_STEP) {
-      state = stepPacket<R>(g, q, in, out, sh, p, deltaER, deltaE, lc);
+      state = stepPacket<R>(g, q, in, out, sh, p, deltaER, deltaE, lc, pj);
     }
   }
+  flushJ(out, pj);
   flushCounters(lc, cnt);
 }
 
@@ -602,6 +638,7 @@ transportKernelBatched(DevGrid g, DevTransportIn in, DevTransportOut out, DevTra
                                               packetStateOffset((size_t)g.nbins * sizeof(float)))[threadIdx.x];
   p.nEmit = 0; p.nStep = 0;
   NebulaGeo q{};
+  PendingJ pj{0., 0., 0, false};
   double deltaE = 0.;
   R deltaER = R(0);
   int state = ST_IDLE;
@@ -638,9 +675,10 @@ transportKernelBatched(DevGrid g, DevTransportIn in, DevTransportOut out, DevTra
     if (emitTurn(state, emitBatch)) {
       if (state == ST_EMIT) state = emitPacket<R>(g, q, in, out, sh, p, deltaE, lc);
     } else if (state == ST_STEP) {
-      state = stepPacket<R>(g, q, in, out, sh, p, deltaER, deltaE, lc);
+      state = stepPacket<R>(g, q, in, out, sh, p, deltaER, deltaE, lc, pj);
     }
   }
+  flushJ(out, pj);
   flushCounters(lc, cnt);
 }
 

@@ -361,7 +361,7 @@ struct mcx_ctx {
   DBuf<float> hden, te, ne, teOld, neOld, ionDen, ndust;
   // phase arrays
   DBuf<float> opacity, recPDF, recCDFT, totalLines, scaOpac, dustPDF, dustCDFT;
-  DBuf<double> jste, escaped, hEst;
+  DBuf<double> jste, jlo, escaped, hEst;   // jlo: the compensation of jste during a transport call
   // scratch
   DBuf<float> gauntTe;
   DBuf<uint8_t> computeMask;
@@ -451,6 +451,23 @@ __global__ void scaleJCellKernel(double* j, size_t n, size_t C1, double mul, con
   const double d = (double)div[i % C1];
   if (d != 1.) v = v / d;
   j[i] = v;
+}
+
+// After a transport launch: J += Jlo (the exact rounding errors of its FP64
+// atomics) and Jlo = 0, so J is the correctly rounded sum of the deposits.
+__global__ void foldJKernel(double* __restrict__ j, double* __restrict__ lo, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double e = lo[i];
+    if (e != 0.) {
+      j[i] += e;
+      lo[i] = 0.;
+    }
+  }
+}
+
+static cudaError_t foldJ(mcx_ctx* c) {
+  foldJKernel<<<(unsigned)c->numSMs * 8, 256, 0, c->stream>>>(c->jste.p, c->jlo.p, c->jste.n);
+  return cudaGetLastError();
 }
 
 // four entries per thread, one thread per four (a memory-bound pass over 331 MB
@@ -713,6 +730,7 @@ static int loadSetup(mcx_ctx* c, const Setup& s) {
   CK(c->recCDFT.alloc(C1 * nb), "alloc recCDF");
   CK(c->totalLines.alloc(C1), "alloc totalLines");
   CK(c->jste.alloc(C1 * nb), "alloc Jste");
+  CK(c->jlo.alloc(C1 * nb), "alloc Jste compensation");
   CK(c->escaped.alloc(C1 * (nb + 1)), "alloc escaped");
   if (c->radPress) CK(c->hEst.alloc(C1 * nb), "alloc H");
   if (c->lgDust) {
@@ -728,6 +746,7 @@ static int loadSetup(mcx_ctx* c, const Setup& s) {
   CK(cudaMemset(c->recCDFT.p, 0, c->recCDFT.bytes()), "memset");
   CK(cudaMemset(c->totalLines.p, 0, c->totalLines.bytes()), "memset");
   CK(cudaMemset(c->jste.p, 0, c->jste.bytes()), "memset");
+  CK(cudaMemset(c->jlo.p, 0, c->jlo.bytes()), "memset");
   CK(cudaMemset(c->escaped.p, 0, c->escaped.bytes()), "memset");
   if (c->hEst.p) CK(cudaMemset(c->hEst.p, 0, c->hEst.bytes()), "memset");
   if (c->scaOpac.p) CK(cudaMemset(c->scaOpac.p, 0, c->scaOpac.bytes()), "memset");
@@ -1215,6 +1234,7 @@ extern "C" int mcx_transport(mcx_ctx* c, const mcx_transport_opts* o, mcx_transp
   const double deltaE = norm > 0 ? (double)c->lStar / (double)norm : 0.;
   if (o->zero_estimators) {
     CK(cudaMemsetAsync(c->jste.p, 0, c->jste.bytes(), c->stream), "memset Jste");
+    CK(cudaMemsetAsync(c->jlo.p, 0, c->jlo.bytes(), c->stream), "memset Jste compensation");
     CK(cudaMemsetAsync(c->escaped.p, 0, c->escaped.bytes(), c->stream), "memset escaped");
     if (c->hEst.p) CK(cudaMemsetAsync(c->hEst.p, 0, c->hEst.bytes(), c->stream), "memset H");
   }
@@ -1233,7 +1253,7 @@ extern "C" int mcx_transport(mcx_ctx* c, const mcx_transport_opts* o, mcx_transp
   in.opacity = c->opacity.p; in.scaOpac = c->scaOpac.p; in.recCDFT = c->recCDFT.p; in.dustCDFT = c->dustCDFT.p;
   in.totalLines = c->totalLines.p; in.ne = c->ne.p;
   DevTransportOut out{};
-  out.jste = c->jste.p; out.escaped = c->escaped.p; out.hEst = c->hEst.p;
+  out.jste = c->jste.p; out.jlo = c->jlo.p; out.escaped = c->escaped.p; out.hEst = c->hEst.p;
 
   TransportLaunch L{};
   L.emitBatch = o->emit_batch > 32 ? 32 : o->emit_batch;
@@ -1258,6 +1278,7 @@ extern "C" int mcx_transport(mcx_ctx* c, const mcx_transport_opts* o, mcx_transp
     if (e != cudaSuccess) return cudaFail(c, e, "transport kernel");
   }
   CK(cudaEventRecord(c->ev1, c->stream), "event");
+  if (n > 0) CK(foldJ(c), "fold J compensation");
   return transportFinish(c, stats, "mcx_transport");
 }
 
@@ -1287,6 +1308,7 @@ extern "C" int mcx_transport_batched(mcx_ctx* c, const mcx_transport_opts* o, co
   }
   if (o->zero_estimators) {
     CK(cudaMemsetAsync(c->jste.p, 0, c->jste.bytes(), c->stream), "memset Jste");
+    CK(cudaMemsetAsync(c->jlo.p, 0, c->jlo.bytes(), c->stream), "memset Jste compensation");
     CK(cudaMemsetAsync(c->escaped.p, 0, c->escaped.bytes(), c->stream), "memset escaped");
   }
   CK(cudaMemsetAsync(c->counters.p, 0, sizeof(DevTransportCounters), c->stream), "memset counters");
@@ -1303,7 +1325,7 @@ extern "C" int mcx_transport_batched(mcx_ctx* c, const mcx_transport_opts* o, co
   DevTransportIn in{};
   in.opacity = c->opacity.p; in.recCDFT = c->recCDFT.p; in.totalLines = c->totalLines.p; in.ne = c->ne.p;
   DevTransportOut out{};
-  out.jste = c->jste.p; out.escaped = c->escaped.p;
+  out.jste = c->jste.p; out.jlo = c->jlo.p; out.escaped = c->escaped.p;
   TransportLaunch L{};
   L.emitBatch = o->emit_batch > 32 ? 32 : o->emit_batch;
   L.threads = o->block_size > 0 ? o->block_size : 256;
@@ -1330,6 +1352,7 @@ extern "C" int mcx_transport_batched(mcx_ctx* c, const mcx_transport_opts* o, co
     if (e != cudaSuccess) return cudaFail(c, e, "batched transport kernel");
   }
   CK(cudaEventRecord(c->ev1, c->stream), "event");
+  if (total > 0) CK(foldJ(c), "fold J compensation");
   return transportFinish(c, stats, "mcx_transport_batched");
 }
 

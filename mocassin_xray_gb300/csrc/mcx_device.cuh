@@ -38,6 +38,7 @@ struct DevTransportIn {
 
 struct DevTransportOut {
   double* jste;              // [nbins][C+1]
+  double* jlo;               // [nbins][C+1] rounding errors of the jste additions, or null (uncompensated)
   double* escaped;           // [nbins+1][C+1]
   double* hEst;              // [nbins][C+1] or null
 };

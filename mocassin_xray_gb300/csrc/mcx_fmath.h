@@ -21,8 +21,14 @@
  *   log10 = log / ln 10;  pow(x, y) = exp(y log x) for x > 0, with the
  *         C99 special cases for zero, negative bases with integral y,
  *         infinities and NaN.
+ *   sin, cos: x = k pi/2 + r with pi/2 split into a 33-bit head and a tail,
+ *         |r| <= pi/4, sin r and cos r by their Taylor series to r^19 and
+ *         r^20, the quadrant k mod 4 choosing the sign and the function;
+ *         meant for |x| < 1e6 (the transport's angles lie in [-pi, pi]).
  * Accuracy (tests/test_fmath_cpu.py, against the host's libm): exp and log
- * within 2 ulp, log10 within 3 ulp, pow within (2 |y ln x| + 4) ulp.
+ * within 2 ulp, log10 within 3 ulp, pow within (2 |y ln x| + 4) ulp, sin
+ * and cos within 2 ulp plus an absolute 1e-22 (the pi/2 reduction's error
+ * near a zero of the function).
  */
 #ifndef MCX_FMATH_H
 #define MCX_FMATH_H
@@ -167,6 +173,79 @@ MCX_FM_FN double mcx_fm_pow(double x, double y) {
   if (x == 0.0) return sign * (y > 0.0 ? 0.0 : inf);
   if (x == inf) return sign * (y > 0.0 ? inf : 0.0);
   return sign * mcx_fm_exp(y * mcx_fm_log(x));
+}
+
+#define MCX_FM_PIO2_HI 1.5707963267341256     /* pi/2 with its low 20 mantissa bits cleared */
+#define MCX_FM_PIO2_LO 6.077100506506192e-11   /* pi/2 - MCX_FM_PIO2_HI */
+#define MCX_FM_TWO_OVER_PI 0.6366197723675814
+
+/* sin r and cos r for |r| <= pi/4 */
+MCX_FM_FN double mcx_fm_sin_kernel(double r) {
+  const double z = r * r;
+  double p = -8.22063524662433e-18;            /* -1/19! */
+  p = 2.8114572543455206e-15 + z * p;          /*  1/17! */
+  p = -7.647163731819816e-13 + z * p;          /* -1/15! */
+  p = 1.6059043836821613e-10 + z * p;          /*  1/13! */
+  p = -2.505210838544172e-08 + z * p;          /* -1/11! */
+  p = 2.7557319223985893e-06 + z * p;          /*  1/9!  */
+  p = -1.984126984126984e-04 + z * p;          /* -1/7!  */
+  p = 8.333333333333333e-03 + z * p;           /*  1/5!  */
+  p = -1.6666666666666666e-01 + z * p;         /* -1/3!  */
+  return r + (r * z) * p;
+}
+
+MCX_FM_FN double mcx_fm_cos_kernel(double r) {
+  const double z = r * r;
+  double p = 4.110317623312165e-19;            /*  1/20! */
+  p = -1.5619206968586225e-16 + z * p;         /* -1/18! */
+  p = 4.779477332387385e-14 + z * p;           /*  1/16! */
+  p = -1.1470745597729725e-11 + z * p;         /* -1/14! */
+  p = 2.08767569878681e-09 + z * p;            /*  1/12! */
+  p = -2.755731922398589e-07 + z * p;          /* -1/10! */
+  p = 2.48015873015873e-05 + z * p;            /*  1/8!  */
+  p = -1.388888888888889e-03 + z * p;          /* -1/6!  */
+  p = 4.1666666666666664e-02 + z * p;          /*  1/4!  */
+  p = -0.5 + z * p;                            /* -1/2!  */
+  return 1.0 + z * p;
+}
+
+/* x = k pi/2 + r; returns r and the quadrant k mod 4 */
+MCX_FM_FN double mcx_fm_reduce_pio2(double x, int* quadrant) {
+  const double kd = mcx_fm_floor(x * MCX_FM_TWO_OVER_PI + 0.5);
+  const double r = (x - kd * MCX_FM_PIO2_HI) - kd * MCX_FM_PIO2_LO;
+  const long long k = (long long)kd;
+  *quadrant = (int)(((k % 4) + 4) % 4);
+  return r;
+}
+
+MCX_FM_FN double mcx_fm_sin(double x) {
+  if (!(x == x) || x == mcx_fm_inf() || x == -mcx_fm_inf()) return mcx_fm_nan();
+  int q;
+  const double r = mcx_fm_reduce_pio2(x, &q);
+  switch (q) {
+    case 0: return mcx_fm_sin_kernel(r);
+    case 1: return mcx_fm_cos_kernel(r);
+    case 2: return -mcx_fm_sin_kernel(r);
+    default: return -mcx_fm_cos_kernel(r);
+  }
+}
+
+MCX_FM_FN double mcx_fm_cos(double x) {
+  if (!(x == x) || x == mcx_fm_inf() || x == -mcx_fm_inf()) return mcx_fm_nan();
+  int q;
+  const double r = mcx_fm_reduce_pio2(x, &q);
+  switch (q) {
+    case 0: return mcx_fm_cos_kernel(r);
+    case 1: return -mcx_fm_sin_kernel(r);
+    case 2: return -mcx_fm_cos_kernel(r);
+    default: return mcx_fm_sin_kernel(r);
+  }
+}
+
+/* TwoSum (Knuth): the rounding error of s = RN(a + b), exactly: a + b = s + err */
+MCX_FM_FN double mcx_fm_two_sum_err(double a, double b, double s) {
+  const double bb = s - a;
+  return (a - (s - bb)) + (b - bb);
 }
 
 #endif /* MCX_FMATH_H */

@@ -117,12 +117,12 @@ def philox(ctr, key) -> np.ndarray:
     return out
 
 
-FM_EXP, FM_LOG, FM_LOG10, FM_POW = 0, 1, 2, 3
+FM_EXP, FM_LOG, FM_LOG10, FM_POW, FM_SIN, FM_COS = 0, 1, 2, 3, 4, 5
 
 
 def fm_eval(fn: int, x, y=None) -> np.ndarray:
-    """The portable FP64 exp / log / log10 / pow that the oracle's balance and
-    the device's FP64 balance share, evaluated on the host."""
+    """The portable FP64 exp / log / log10 / pow / sin / cos that the oracle
+    and the device's FP64 balance and transport share, evaluated on the host."""
     x = np.ascontiguousarray(x, dtype=np.float64)
     y = np.ascontiguousarray(np.zeros_like(x) if y is None else y, dtype=np.float64)
     out = np.empty_like(x)

@@ -13,6 +13,8 @@ void orc_fm_eval(int32_t fn, const double* x, const double* y, int64_t n, double
         case 0: out[i] = mcx_fm_exp(x[i]); break;
         case 1: out[i] = mcx_fm_log(x[i]); break;
         case 2: out[i] = mcx_fm_log10(x[i]); break;
+        case 4: out[i] = mcx_fm_sin(x[i]); break;
+        case 5: out[i] = mcx_fm_cos(x[i]); break;
         default: out[i] = mcx_fm_pow(x[i], y[i]); break;
         }
     }

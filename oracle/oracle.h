@@ -32,7 +32,7 @@ extern "C" {
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 
 /* The portable FP64 routines of mcx_fmath.h over arrays: fn 0 exp(x), 1 log(x),
- * 2 log10(x), 3 pow(x, y). */
+ * 2 log10(x), 3 pow(x, y), 4 sin(x), 5 cos(x). */
 void orc_fm_eval(int32_t fn, const double* x, const double* y, int64_t n, double* out);
 
 /* ------------------------------------------------------------ transport */

@@ -28,6 +28,13 @@
 #include <stdlib.h>
 #include <string.h>
 
+/* log, sin and cos from the portable FP64 routines that the device's FP64
+ * transport uses too, so that every packet history is the same on both sides */
+#include "mcx_fmath.h"
+#define log(x) mcx_fm_log(x)
+#define sin(x) mcx_fm_sin(x)
+#define cos(x) mcx_fm_cos(x)
+
 /* ------------------------------------------------------------ Philox */
 static inline void mulhilo32(uint32_t a, uint32_t b, uint32_t* hi, uint32_t* lo) {
     uint64_t p = (uint64_t)a * (uint64_t)b;
@@ -89,6 +96,7 @@ typedef struct {
 typedef struct {
     const orc_transport_in* in;
     double* jste;
+    double* jlo;        /* the exact rounding errors of the jste additions (TwoSum) */
     double* escaped;
     double* h_est;
     orc_transport_stats st;
@@ -178,7 +186,12 @@ static void escape_tally(tctx_t* c, const packet_t* p) {
 static inline void deposit(tctx_t* c, int cell, int nuP, double dl, double dV, double costheta) {
     if (cell <= 0) return;
     size_t idx = (size_t)cell + c->C1 * (size_t)(nuP - 1);
-    c->jste[idx] += dl * c->in->delta_e / dV;
+    /* compensated accumulation: jste + jlo holds the sum of the deposits to
+     * within the rounding of jlo, so the final jste + jlo is the correctly
+     * rounded sum whatever the order of the deposits */
+    const double v = dl * c->in->delta_e / dV, old = c->jste[idx], sum = old + v;
+    c->jlo[idx] += mcx_fm_two_sum_err(old, v, sum);
+    c->jste[idx] = sum;
     if (c->h_est) c->h_est[idx] += (dl * c->in->delta_e) * costheta / dV;
 }
 
@@ -530,6 +543,8 @@ int orc_transport(const orc_transport_in* in, uint64_t seed, uint64_t counter_ba
         jb->first = first;
         jb->count = per + ((uint64_t)t < rest ? 1 : 0);
         first += jb->count;
+        jb->c.jlo = (double*)calloc(nj, sizeof(double));
+        if (!jb->c.jlo) rc = 3;
         if (t == 0) {
             jb->c.jste = out->jste; jb->c.escaped = out->escaped;
             jb->c.h_est = (in->rad_press && out->h_est) ? out->h_est : NULL;
@@ -546,13 +561,25 @@ int orc_transport(const orc_transport_in* in, uint64_t seed, uint64_t counter_ba
         for (int t = 1; t < nthreads; ++t) pthread_join(th[t], NULL);
     }
     memset(stats, 0, sizeof(*stats));
+    /* J: the compensated sum of every thread's (jste, jlo) pair, rounded once */
+    if (rc == 0) {
+        for (size_t k = 0; k < nj; ++k) {
+            double s = out->jste[k], e = jobs[0].c.jlo[k];
+            for (int t = 1; t < nthreads; ++t) {
+                const double h = jobs[t].c.jste[k], s2 = s + h;
+                e += mcx_fm_two_sum_err(s, h, s2) + jobs[t].c.jlo[k];
+                s = s2;
+            }
+            out->jste[k] = s + e;
+        }
+    }
     for (int t = 0; t < nthreads; ++t) {
         job_t* jb = &jobs[t];
         if (t > 0 && rc == 0) {
-            for (size_t k = 0; k < nj; ++k) out->jste[k] += jb->c.jste[k];
             for (size_t k = 0; k < ne; ++k) out->escaped[k] += jb->c.escaped[k];
             if (jb->c.h_est) for (size_t k = 0; k < nj; ++k) out->h_est[k] += jb->c.h_est[k];
         }
+        free(jb->c.jlo);
         if (t > 0) { free(jb->c.jste); free(jb->c.escaped); free(jb->c.h_est); }
         stats->crossings += jb->c.st.crossings;
         stats->interactions += jb->c.st.interactions;

@@ -1,5 +1,6 @@
-"""Accuracy of the portable FP64 exp / log / log10 / pow (mcx_fmath.h) that the
-device's FP64 balance and the oracle's balance share: within a few ulp of the
+"""Accuracy of the portable FP64 exp / log / log10 / pow / sin / cos
+(mcx_fmath.h) that the device's FP64 balance and transport and the oracle's
+share: within a few ulp of the
 host's libm (numpy) over the ranges the balance evaluates, plus the C99
 special cases.  pow = exp(y ln x) carries the relative error of y ln x into
 its result, about 2 |y ln x| ulp (1e-14 for Te^-1.5 at 1e4 K)."""
@@ -73,3 +74,15 @@ def test_pow(rng):
     for k in (2.0, 3.0, -1.0, 0.5):
         assert np.all(_ulps(oracle.fm_eval(oracle.FM_POW, xi, np.full_like(xi, k)), xi ** k)
                       <= 2.0 * np.abs(k * np.log(xi)) + 4.0)
+
+
+def test_sin_cos(rng):
+    x = np.concatenate([rng.uniform(-np.pi, np.pi, 200000), rng.uniform(-1e3, 1e3, 50000),
+                        rng.uniform(-1e-3, 1e-3, 10000), [0.0, np.pi / 2, -np.pi, np.pi, 3.141592654]])
+    for fn, ref in ((oracle.FM_SIN, np.sin), (oracle.FM_COS, np.cos)):
+        got = oracle.fm_eval(fn, x)
+        want = ref(x)
+        # near a zero of the function the absolute error of the pi/2 reduction
+        # (about k 1e-26) sets the bound
+        assert np.all(np.abs(got - want) <= 2.0 * np.spacing(np.abs(want)) + 1e-22), fn
+    assert np.isnan(oracle.fm_eval(oracle.FM_SIN, np.array([np.inf]))[0])
