@@ -218,12 +218,20 @@ int  mcx_put(mcx_ctx* ctx, int32_t array_id, const void* host, size_t nbytes);
 /* Raw device pointer of a context array (for zero-copy callers). */
 int  mcx_device_ptr(mcx_ctx* ctx, int32_t array_id, void** dptr);
 
-/* Device-side snapshot of the per-cell gas state (Te, Ne, ionDen, TeOld,
- * NeOld, lgConverged) and its restoration, stream-ordered with the phases.
- * No counterpart in the reference, which keeps one grid state; used to rerun
- * an iteration from the same state (timing, tests, restarts in memory). */
+/* Device-side snapshots of everything an iteration hands to the next: the
+ * gas state (Te, Ne, ionDen, TeOld, NeOld, lgConverged), the phase outputs
+ * the skip rule keeps for unchanged cells (opacity, recPDF, totalLines,
+ * forLines and the Gaunt-cache temperatures; the grain arrays of a dust
+ * grid), in numbered slots held in device memory, stream-ordered with the
+ * phases.  mcx_state_save / mcx_state_restore use slot 0.  No counterpart in
+ * the reference, which keeps one grid state; used to rerun an iteration from
+ * the state it started from (timing, tests, restarts in memory).  Each slot
+ * holds about 3 nbins x (nCells+1) x 4 bytes. */
+#define MCX_STATE_SLOTS 64
 int  mcx_state_save(mcx_ctx* ctx);
 int  mcx_state_restore(mcx_ctx* ctx);
+int  mcx_state_save_slot(mcx_ctx* ctx, int32_t slot);
+int  mcx_state_restore_slot(mcx_ctx* ctx, int32_t slot);
 
 /* ------------------------------------------------------- phase: opacity */
 /* Per-cell opacity kappa(nu): free-free + sum of bound-free x-sections times

@@ -172,6 +172,8 @@ SIGNATURES = [
     ("mcx_device_ptr", C.c_int, [_P, C.c_int32, C.POINTER(_P)]),
     ("mcx_state_save", C.c_int, [_P]),
     ("mcx_state_restore", C.c_int, [_P]),
+    ("mcx_state_save_slot", C.c_int, [_P, C.c_int32]),
+    ("mcx_state_restore_slot", C.c_int, [_P, C.c_int32]),
     ("mcx_opacity", C.c_int, [_P, C.POINTER(PhaseOpts), C.POINTER(PhaseStats)]),
     ("mcx_emission", C.c_int, [_P, C.POINTER(PhaseOpts), C.POINTER(PhaseStats)]),
     ("mcx_transport", C.c_int, [_P, C.POINTER(TransportOpts), C.POINTER(TransportStats)]),

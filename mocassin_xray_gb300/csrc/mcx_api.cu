@@ -318,6 +318,19 @@ template <typename T>
 struct DBuf {
   T* p = nullptr;
   size_t n = 0;
+  DBuf() = default;
+  // owns its allocation: moved, never copied (a copy would free it twice)
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) {
+      if (p) cudaFree(p);
+      p = o.p; n = o.n;
+      o.p = nullptr; o.n = 0;
+    }
+    return *this;
+  }
   ~DBuf() { if (p) cudaFree(p); }
   cudaError_t alloc(size_t count) {
     if (p) { cudaFree(p); p = nullptr; n = 0; }
@@ -397,10 +410,16 @@ struct mcx_ctx {
   DBuf<float> nebAxes, nebCdf, nebFfK, jDiv;
   DBuf<int32_t> nebActiveDev;
   DBuf<int16_t> nebFfIdx;
-  // mcx_state_save snapshot
-  DBuf<float> snapTe, snapNe, snapTeOld, snapNeOld, snapIonDen;
-  DBuf<int32_t> snapConverged;
-  bool haveSnapshot = false;
+  // mcx_state_save snapshots: everything an iteration carries into the next
+  struct Snapshot {
+    std::vector<DBuf<float>> f;       // the float arrays of snapshotArrays(), in order
+    DBuf<int32_t> converged;
+    float gauntTeOld = -1.f;
+    std::vector<float> nebGauntTeOld;
+    bool haveOpacity = false, haveRecPDF = false, haveDustPDF = false;
+    bool valid = false;
+  };
+  std::vector<Snapshot> snaps;        // slot k at snaps[k]
   bool haveOpacity = false, haveRecPDF = false, haveDustPDF = false;
 };
 
@@ -542,37 +561,65 @@ extern "C" int mcx_last_error(const mcx_ctx* c, char* buf, size_t len) {
   return MCX_OK;
 }
 
-extern "C" int mcx_state_save(mcx_ctx* c) {
+// The float arrays of an iteration-boundary snapshot: the gas state and the
+// phase outputs that the skip rule (source/iteration_mod.f90:131-149,
+// :340-356) carries from one iteration into the next.
+static std::vector<DBuf<float>*> snapshotArrays(mcx_ctx* c) {
+  std::vector<DBuf<float>*> v = {&c->te, &c->ne, &c->teOld, &c->neOld, &c->ionDen, &c->opacity, &c->recPDF,
+                                 &c->recCDFT, &c->totalLines, &c->forLines, &c->gauntTe};
+  for (DBuf<float>* d : {&c->scaOpac, &c->dustPDF, &c->dustCDFT, &c->tdust})
+    if (d->p) v.push_back(d);
+  return v;
+}
+
+extern "C" int mcx_state_save_slot(mcx_ctx* c, int32_t slot) {
   if (!c) return MCX_ERR_INPUT;
   if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_state_save: no model loaded");
+  if (slot < 0 || slot >= MCX_STATE_SLOTS)
+    return fail(c, MCX_ERR_INPUT, "mcx_state_save: slot out of range [0, MCX_STATE_SLOTS)");
   CK(cudaSetDevice(c->device), "cudaSetDevice");
-  struct P { DBuf<float>* dst; DBuf<float>* src; } fp[] = {
-      {&c->snapTe, &c->te}, {&c->snapNe, &c->ne}, {&c->snapTeOld, &c->teOld}, {&c->snapNeOld, &c->neOld},
-      {&c->snapIonDen, &c->ionDen}};
-  for (auto& q : fp) {
-    if (q.dst->n != q.src->n) CK(q.dst->alloc(q.src->n), "alloc snapshot");
-    CK(cudaMemcpyAsync(q.dst->p, q.src->p, q.src->bytes(), cudaMemcpyDeviceToDevice, c->stream), "snapshot");
+  if ((int)c->snaps.size() <= slot) c->snaps.resize(slot + 1);
+  mcx_ctx::Snapshot& sn = c->snaps[slot];
+  std::vector<DBuf<float>*> src = snapshotArrays(c);
+  if (sn.f.size() != src.size()) sn.f = std::vector<DBuf<float>>(src.size());
+  for (size_t k = 0; k < src.size(); ++k) {
+    if (sn.f[k].n != src[k]->n) CK(sn.f[k].alloc(src[k]->n), "alloc snapshot");
+    if (src[k]->n)
+      CK(cudaMemcpyAsync(sn.f[k].p, src[k]->p, src[k]->bytes(), cudaMemcpyDeviceToDevice, c->stream), "snapshot");
   }
-  if (c->snapConverged.n != c->lgConverged.n) CK(c->snapConverged.alloc(c->lgConverged.n), "alloc snapshot");
-  CK(cudaMemcpyAsync(c->snapConverged.p, c->lgConverged.p, c->lgConverged.bytes(), cudaMemcpyDeviceToDevice,
-                     c->stream), "snapshot");
-  c->haveSnapshot = true;
+  if (sn.converged.n != c->lgConverged.n) CK(sn.converged.alloc(c->lgConverged.n), "alloc snapshot");
+  CK(cudaMemcpyAsync(sn.converged.p, c->lgConverged.p, c->lgConverged.bytes(), cudaMemcpyDeviceToDevice, c->stream),
+     "snapshot");
+  sn.gauntTeOld = c->gauntTeOld;
+  sn.nebGauntTeOld = c->nebGauntTeOld;
+  sn.haveOpacity = c->haveOpacity; sn.haveRecPDF = c->haveRecPDF; sn.haveDustPDF = c->haveDustPDF;
+  sn.valid = true;
   return MCX_OK;
 }
 
-extern "C" int mcx_state_restore(mcx_ctx* c) {
+extern "C" int mcx_state_restore_slot(mcx_ctx* c, int32_t slot) {
   if (!c) return MCX_ERR_INPUT;
-  if (!c->loaded || !c->haveSnapshot) return fail(c, MCX_ERR_STATE, "mcx_state_restore: no snapshot");
+  if (!c->loaded || slot < 0 || slot >= (int)c->snaps.size() || !c->snaps[slot].valid)
+    return fail(c, MCX_ERR_STATE, "mcx_state_restore: no snapshot in this slot");
   CK(cudaSetDevice(c->device), "cudaSetDevice");
-  struct P { DBuf<float>* dst; DBuf<float>* src; } fp[] = {
-      {&c->te, &c->snapTe}, {&c->ne, &c->snapNe}, {&c->teOld, &c->snapTeOld}, {&c->neOld, &c->snapNeOld},
-      {&c->ionDen, &c->snapIonDen}};
-  for (auto& q : fp)
-    CK(cudaMemcpyAsync(q.dst->p, q.src->p, q.src->bytes(), cudaMemcpyDeviceToDevice, c->stream), "restore");
-  CK(cudaMemcpyAsync(c->lgConverged.p, c->snapConverged.p, c->snapConverged.bytes(), cudaMemcpyDeviceToDevice,
-                     c->stream), "restore");
+  mcx_ctx::Snapshot& sn = c->snaps[slot];
+  std::vector<DBuf<float>*> dst = snapshotArrays(c);
+  if (dst.size() != sn.f.size()) return fail(c, MCX_ERR_STATE, "mcx_state_restore: snapshot of another model");
+  for (size_t k = 0; k < dst.size(); ++k) {
+    if (dst[k]->n != sn.f[k].n) return fail(c, MCX_ERR_STATE, "mcx_state_restore: snapshot of another model");
+    if (dst[k]->n)
+      CK(cudaMemcpyAsync(dst[k]->p, sn.f[k].p, sn.f[k].bytes(), cudaMemcpyDeviceToDevice, c->stream), "restore");
+  }
+  CK(cudaMemcpyAsync(c->lgConverged.p, sn.converged.p, sn.converged.bytes(), cudaMemcpyDeviceToDevice, c->stream),
+     "restore");
+  c->gauntTeOld = sn.gauntTeOld;
+  c->nebGauntTeOld = sn.nebGauntTeOld;
+  c->haveOpacity = sn.haveOpacity; c->haveRecPDF = sn.haveRecPDF; c->haveDustPDF = sn.haveDustPDF;
   return MCX_OK;
 }
+
+extern "C" int mcx_state_save(mcx_ctx* c) { return mcx_state_save_slot(c, 0); }
+extern "C" int mcx_state_restore(mcx_ctx* c) { return mcx_state_restore_slot(c, 0); }
 
 extern "C" int mcx_sync(mcx_ctx* c) {
   if (!c) return MCX_ERR_INPUT;
@@ -761,7 +808,7 @@ static int loadSetup(mcx_ctx* c, const Setup& s) {
   c->emission.reset();
   c->balance.reset();
   c->dust.reset();
-  c->haveSnapshot = false;
+  c->snaps.clear();
   if (c->lgDust) {
     std::string dm = dustDataCreate(s, c->dust);
     if (!dm.empty()) return fail(c, MCX_ERR_INPUT, "mcx_load: " + dm);

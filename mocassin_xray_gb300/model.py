@@ -285,12 +285,14 @@ class Context:
         return dict(L=L, dL_dhden=dh, dL_dabun=da[:, :len(z)], kernel_ms=float(out.kernel_ms),
                     branch_cells_hden=int(out.branch_cells_hden), branch_cells_abun=int(out.branch_cells_abun))
 
-    def state_save(self) -> None:
-        """Device-side snapshot of Te, Ne, ionDen, TeOld, NeOld, lgConverged."""
-        self._check(lib().mcx_state_save(self._h))
+    def state_save(self, slot: int = 0) -> None:
+        """Device-side snapshot, in slot `slot`, of everything an iteration
+        hands to the next (gas state, the skip rule's kept opacity and
+        emission CDF, Gaunt-cache temperatures, grain arrays)."""
+        self._check(lib().mcx_state_save_slot(self._h, slot))
 
-    def state_restore(self) -> None:
-        self._check(lib().mcx_state_restore(self._h))
+    def state_restore(self, slot: int = 0) -> None:
+        self._check(lib().mcx_state_restore_slot(self._h, slot))
 
     def normalize_j(self) -> None:
         self._check(lib().mcx_normalize_j(self._h))

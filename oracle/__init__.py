@@ -109,6 +109,27 @@ def _p(a):
     return None if a is None else C.c_void_p(a.ctypes.data)
 
 
+def _split_mask(compute: np.ndarray, nthreads: int) -> list[np.ndarray]:
+    """The cells of a compute mask cut into nthreads contiguous runs of about
+    equal count (the oracle's per-cell phases then run one run per thread:
+    ctypes releases the GIL for the foreign call)."""
+    idx = np.nonzero(compute)[0]
+    out = []
+    for part in np.array_split(idx, max(1, min(nthreads, idx.size))):
+        m = np.zeros_like(compute)
+        m[part] = 1
+        out.append(m)
+    return out
+
+
+def _threads(fn, masks):
+    if len(masks) == 1:
+        return [fn(masks[0])]
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=len(masks)) as ex:
+        return list(ex.map(fn, masks))
+
+
 def philox(ctr, key) -> np.ndarray:
     c = np.ascontiguousarray(ctr, dtype=np.uint32)
     k = np.ascontiguousarray(key, dtype=np.uint32)
@@ -147,8 +168,10 @@ def gaunt_cache(nx, ny, nz, active, te, compute, te_old: float) -> tuple[np.ndar
     return out, t.value
 
 
-def opacity(setup, te=None, ne=None, ionden=None, hden=None, gaunt_te=None, compute=None, out=None) -> np.ndarray:
-    """Oracle opacity for a mocassin_xray_gb300.Setup (arrays default to the set-up's state)."""
+def opacity(setup, te=None, ne=None, ionden=None, hden=None, gaunt_te=None, compute=None, out=None,
+            nthreads: int = 1) -> np.ndarray:
+    """Oracle opacity for a mocassin_xray_gb300.Setup (arrays default to the set-up's state); the
+    cells are shared among `nthreads` threads (each writes only its own cells)."""
     from mocassin_xray_gb300 import abi
     i = setup.info
     C1, nb = i.n_cells + 1, i.nbins
@@ -170,15 +193,18 @@ def opacity(setup, te=None, ne=None, ionden=None, hden=None, gaunt_te=None, comp
     gaunt_te = np.ascontiguousarray(gaunt_te, dtype=np.float32)
     if out is None:
         out = np.zeros((nb, C1), dtype=np.float32)
-    s = OpacityIn(n_cells=i.n_cells, nbins=nb, nstages=i.nstages, n_elem_used=max(i.n_elem_used, 1),
-                  lg_compton=i.lg_compton, n_xsec=arrs["xsec"].size, nu=_p(arrs["nu"]), xsec=_p(arrs["xsec"]),
-                  kn_sigma_t=_p(arrs["kn"]), ptr=_p(arrs["ptr"]), elem_abun=_p(arrs["abun"]),
-                  elem_xref=_p(arrs["xref"]), n_shells=_p(arrs["nsh"]), element_p=_p(arrs["ep"]),
-                  hden=_p(arrs["hden"]), te=_p(arrs["te"]), ne=_p(arrs["ne"]), ionden=_p(arrs["ion"]),
-                  gaunt_te=_p(gaunt_te), compute=_p(compute))
-    rc = lib().orc_opacity(C.byref(s), _p(out))
-    if rc != 0:
-        raise RuntimeError(f"orc_opacity failed: {rc}")
+    def run(mask):
+        s = OpacityIn(n_cells=i.n_cells, nbins=nb, nstages=i.nstages, n_elem_used=max(i.n_elem_used, 1),
+                      lg_compton=i.lg_compton, n_xsec=arrs["xsec"].size, nu=_p(arrs["nu"]), xsec=_p(arrs["xsec"]),
+                      kn_sigma_t=_p(arrs["kn"]), ptr=_p(arrs["ptr"]), elem_abun=_p(arrs["abun"]),
+                      elem_xref=_p(arrs["xref"]), n_shells=_p(arrs["nsh"]), element_p=_p(arrs["ep"]),
+                      hden=_p(arrs["hden"]), te=_p(arrs["te"]), ne=_p(arrs["ne"]), ionden=_p(arrs["ion"]),
+                      gaunt_te=_p(gaunt_te), compute=_p(mask))
+        return lib().orc_opacity(C.byref(s), _p(out))
+
+    for rc in _threads(run, _split_mask(compute, nthreads)):
+        if rc != 0:
+            raise RuntimeError(f"orc_opacity failed: {rc}")
     return out
 
 
@@ -255,9 +281,10 @@ def _emission_struct(setup, te=None, ne=None, ionden=None):
 
 
 def emission(setup, gaunt_te: float, te=None, ne=None, ionden=None, compute=None, for_lines=None,
-             rec_pdf=None, total_lines=None):
+             rec_pdf=None, total_lines=None, nthreads: int = 1):
     """Oracle emission phase for a mocassin_xray_gb300.Setup: returns (recPDF [nbins][C+1], totalLines [C+1]).
-    `gaunt_te` is the temperature of the last Gaunt tabulation of the opacity phase."""
+    `gaunt_te` is the temperature of the last Gaunt tabulation of the opacity phase; the cells are
+    shared among `nthreads` threads (each writes only its own cells)."""
     i = setup.info
     C1, nb = i.n_cells + 1, i.nbins
     s, k = _emission_struct(setup, te, ne, ionden)
@@ -276,10 +303,15 @@ def emission(setup, gaunt_te: float, te=None, ne=None, ionden=None, compute=None
     if total_lines is None:
         total_lines = np.zeros(C1, dtype=np.float32)
     s.for_lines = _p(fl)
-    s.compute = _p(compute)
-    rc = lib().orc_emission(C.byref(s), _p(rec_pdf), _p(total_lines))
-    if rc != 0:
-        raise RuntimeError(f"orc_emission failed: {rc}")
+
+    def run(mask):
+        si = EmissionIn.from_buffer_copy(s)
+        si.compute = _p(mask)
+        return lib().orc_emission(C.byref(si), _p(rec_pdf), _p(total_lines))
+
+    for rc in _threads(run, _split_mask(compute, nthreads)):
+        if rc != 0:
+            raise RuntimeError(f"orc_emission failed: {rc}")
     return rec_pdf, total_lines
 
 
@@ -387,16 +419,25 @@ def balance(tables: BalanceTables, jste, te, ne, ionden, nthreads: int = 1):
     return te, ne, ionden, conv, black, nit, stats
 
 
-def for_lines_emission(tables: BalanceTables, te, ne, ionden, compute=None) -> np.ndarray:
+def for_lines_emission(tables: BalanceTables, te, ne, ionden, compute=None, nthreads: int = 1) -> np.ndarray:
     """normFor of each cell (with compute[c] = 1): the emission phase's
-    forbidden-line total [1e-25 erg/s per gas density]."""
+    forbidden-line total [1e-25 erg/s per gas density]; the cells are shared
+    among `nthreads` threads."""
     C1 = tables.info.n_cells + 1
     te = np.ascontiguousarray(te, dtype=np.float32)
     ne = np.ascontiguousarray(ne, dtype=np.float32)
     ionden = np.ascontiguousarray(ionden, dtype=np.float32).reshape(-1)
-    comp = None if compute is None else np.ascontiguousarray(compute, dtype=np.uint8)
+    comp = np.ones(C1, np.uint8) if compute is None else np.ascontiguousarray(compute, dtype=np.uint8)
     out = np.zeros(C1, dtype=np.float64)
-    _balance_lib().orc_for_lines_emission(C.byref(tables.s), _p(te), _p(ne), _p(ionden), _p(comp), _p(out))
+    masks = _split_mask(comp, nthreads)
+
+    def run(mask):
+        o = np.zeros(C1, dtype=np.float64)
+        _balance_lib().orc_for_lines_emission(C.byref(tables.s), _p(te), _p(ne), _p(ionden), _p(mask), _p(o))
+        return mask, o
+
+    for mask, o in _threads(run, masks):
+        out[mask > 0] = o[mask > 0]
     return out
 
 

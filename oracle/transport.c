@@ -93,10 +93,16 @@ typedef struct {
     int origin;         /* origin cell id */
 } packet_t;
 
+/* J entries are merged across threads in chunks of this many; a thread marks
+ * the chunks it deposits into, so the merge visits only those */
+#define JCHUNK 512
+
 typedef struct {
     const orc_transport_in* in;
     double* jste;
     double* jlo;        /* the exact rounding errors of the jste additions (TwoSum) */
+    uint8_t* touched;   /* [nj / JCHUNK + 1] chunks of jste this thread deposited into */
+    uint8_t* touched_e; /* [ne / JCHUNK + 1] chunks of escaped this thread added to */
     double* escaped;
     double* h_est;
     orc_transport_stats st;
@@ -179,7 +185,9 @@ static void init_packet(tctx_t* c, packet_t* p, int nuP, vec3 pos, int lgLine, i
 }
 
 static void escape_tally(tctx_t* c, const packet_t* p) {
-    c->escaped[(size_t)p->origin + c->C1 * (size_t)p->nuP] += c->in->delta_e;
+    const size_t idx = (size_t)p->origin + c->C1 * (size_t)p->nuP;
+    c->escaped[idx] += c->in->delta_e;
+    c->touched_e[idx / JCHUNK] = 1;
     c->st.escaped++;
 }
 
@@ -192,6 +200,7 @@ static inline void deposit(tctx_t* c, int cell, int nuP, double dl, double dV, d
     const double v = dl * c->in->delta_e / dV, old = c->jste[idx], sum = old + v;
     c->jlo[idx] += mcx_fm_two_sum_err(old, v, sum);
     c->jste[idx] = sum;
+    c->touched[idx / JCHUNK] = 1;
     if (c->h_est) c->h_est[idx] += (dl * c->in->delta_e) * costheta / dV;
 }
 
@@ -522,6 +531,51 @@ static void* thread_main(void* arg) {
     return NULL;
 }
 
+/* Per-thread accumulators kept between calls, cleared chunk by chunk after
+ * each merge: their pages are faulted in once instead of on every call (the
+ * reference's MPI ranks likewise keep their full-grid arrays for the run).
+ * A mutex serialises orc_transport calls, which share the pool. */
+#define MAX_POOL 256
+typedef struct {
+    double *jste, *jlo, *esc, *h;
+    uint8_t *tj, *te;
+    size_t nj, ne;
+} acc_t;
+static acc_t g_pool[MAX_POOL];
+static pthread_mutex_t g_pool_lock = PTHREAD_MUTEX_INITIALIZER;
+
+static void pool_free(acc_t* a) {
+    free(a->jste); free(a->jlo); free(a->esc); free(a->h); free(a->tj); free(a->te);
+    memset(a, 0, sizeof(*a));
+}
+
+static int pool_ready(acc_t* a, size_t nj, size_t ne, int want_h) {
+    if (a->nj != nj || a->ne != ne) {
+        pool_free(a);
+        a->jste = (double*)calloc(nj, sizeof(double));
+        a->jlo = (double*)calloc(nj, sizeof(double));
+        a->esc = (double*)calloc(ne, sizeof(double));
+        a->tj = (uint8_t*)calloc(nj / JCHUNK + 1, 1);
+        a->te = (uint8_t*)calloc(ne / JCHUNK + 1, 1);
+        a->nj = nj; a->ne = ne;
+        if (!a->jste || !a->jlo || !a->esc || !a->tj || !a->te) { pool_free(a); return 0; }
+    }
+    if (want_h && !a->h) {
+        a->h = (double*)calloc(nj, sizeof(double));
+        if (!a->h) return 0;
+    }
+    return 1;
+}
+
+/* zero the chunks of a marked in `mark` (and the marks) */
+static void clear_chunks(double* v, uint8_t* mark, size_t n) {
+    for (size_t ch = 0; ch < n / JCHUNK + 1; ++ch) {
+        if (!mark[ch]) continue;
+        const size_t k1 = (ch + 1) * JCHUNK < n ? (ch + 1) * JCHUNK : n;
+        if (v) memset(v + ch * JCHUNK, 0, (k1 - ch * JCHUNK) * sizeof(double));
+    }
+}
+
 int orc_transport(const orc_transport_in* in, uint64_t seed, uint64_t counter_base, int64_t n,
                   int32_t nthreads, orc_transport_out* out, orc_transport_stats* stats) {
     if (!in || !out || !out->jste || !out->escaped || n < 0) return 2;
@@ -529,10 +583,13 @@ int orc_transport(const orc_transport_in* in, uint64_t seed, uint64_t counter_ba
     const size_t C1 = (size_t)in->n_cells + 1;
     const size_t nj = C1 * (size_t)in->nbins, ne = C1 * (size_t)(in->nbins + 1);
     if (nthreads < 1) nthreads = 1;
+    if (nthreads > MAX_POOL) nthreads = MAX_POOL;
     if ((int64_t)nthreads > n) nthreads = n > 0 ? (int32_t)n : 1;
+    const int want_h = in->rad_press && out->h_est;
     job_t* jobs = (job_t*)calloc((size_t)nthreads, sizeof(job_t));
     pthread_t* th = (pthread_t*)calloc((size_t)nthreads, sizeof(pthread_t));
     if (!jobs || !th) { free(jobs); free(th); return 3; }
+    pthread_mutex_lock(&g_pool_lock);
     int rc = 0;
     uint64_t per = (uint64_t)n / (uint64_t)nthreads, rest = (uint64_t)n % (uint64_t)nthreads, first = counter_base;
     for (int t = 0; t < nthreads; ++t) {
@@ -543,16 +600,15 @@ int orc_transport(const orc_transport_in* in, uint64_t seed, uint64_t counter_ba
         jb->first = first;
         jb->count = per + ((uint64_t)t < rest ? 1 : 0);
         first += jb->count;
-        jb->c.jlo = (double*)calloc(nj, sizeof(double));
-        if (!jb->c.jlo) rc = 3;
+        acc_t* a = &g_pool[t];
+        if (!pool_ready(a, nj, ne, want_h && t > 0)) { rc = 3; continue; }
+        jb->c.jlo = a->jlo; jb->c.touched = a->tj; jb->c.touched_e = a->te;
         if (t == 0) {
             jb->c.jste = out->jste; jb->c.escaped = out->escaped;
-            jb->c.h_est = (in->rad_press && out->h_est) ? out->h_est : NULL;
+            jb->c.h_est = want_h ? out->h_est : NULL;
         } else {
-            jb->c.jste = (double*)calloc(nj, sizeof(double));
-            jb->c.escaped = (double*)calloc(ne, sizeof(double));
-            jb->c.h_est = (in->rad_press && out->h_est) ? (double*)calloc(nj, sizeof(double)) : NULL;
-            if (!jb->c.jste || !jb->c.escaped) rc = 3;
+            jb->c.jste = a->jste; jb->c.escaped = a->esc;
+            jb->c.h_est = want_h ? a->h : NULL;
         }
     }
     if (rc == 0) {
@@ -561,26 +617,48 @@ int orc_transport(const orc_transport_in* in, uint64_t seed, uint64_t counter_ba
         for (int t = 1; t < nthreads; ++t) pthread_join(th[t], NULL);
     }
     memset(stats, 0, sizeof(*stats));
-    /* J: the compensated sum of every thread's (jste, jlo) pair, rounded once */
+    /* J: the compensated sum of every thread's (jste, jlo) pair, rounded once,
+     * over the chunks some thread deposited into */
     if (rc == 0) {
-        for (size_t k = 0; k < nj; ++k) {
-            double s = out->jste[k], e = jobs[0].c.jlo[k];
-            for (int t = 1; t < nthreads; ++t) {
-                const double h = jobs[t].c.jste[k], s2 = s + h;
-                e += mcx_fm_two_sum_err(s, h, s2) + jobs[t].c.jlo[k];
-                s = s2;
+        const size_t nch = nj / JCHUNK + 1;
+        for (size_t ch = 0; ch < nch; ++ch) {
+            int any = 0;
+            for (int t = 0; t < nthreads && !any; ++t) any = jobs[t].c.touched[ch];
+            if (!any) continue;
+            const size_t k1 = (ch + 1) * JCHUNK < nj ? (ch + 1) * JCHUNK : nj;
+            for (size_t k = ch * JCHUNK; k < k1; ++k) {
+                double s = out->jste[k], e = jobs[0].c.jlo[k];
+                for (int t = 1; t < nthreads; ++t) {
+                    if (!jobs[t].c.touched[ch]) continue;
+                    const double h = jobs[t].c.jste[k], s2 = s + h;
+                    e += mcx_fm_two_sum_err(s, h, s2) + jobs[t].c.jlo[k];
+                    s = s2;
+                }
+                out->jste[k] = s + e;
             }
-            out->jste[k] = s + e;
         }
     }
     for (int t = 0; t < nthreads; ++t) {
         job_t* jb = &jobs[t];
         if (t > 0 && rc == 0) {
-            for (size_t k = 0; k < ne; ++k) out->escaped[k] += jb->c.escaped[k];
+            for (size_t ch = 0; ch < ne / JCHUNK + 1; ++ch) {
+                if (!jb->c.touched_e[ch]) continue;
+                const size_t k1 = (ch + 1) * JCHUNK < ne ? (ch + 1) * JCHUNK : ne;
+                for (size_t k = ch * JCHUNK; k < k1; ++k) out->escaped[k] += jb->c.escaped[k];
+            }
             if (jb->c.h_est) for (size_t k = 0; k < nj; ++k) out->h_est[k] += jb->c.h_est[k];
         }
-        free(jb->c.jlo);
-        if (t > 0) { free(jb->c.jste); free(jb->c.escaped); free(jb->c.h_est); }
+        if (jb->c.touched) {
+            /* leave the pooled accumulators zero for the next call */
+            clear_chunks(jb->c.jlo, jb->c.touched, nj);
+            if (t > 0) {
+                clear_chunks(jb->c.jste, jb->c.touched, nj);
+                clear_chunks(jb->c.escaped, jb->c.touched_e, ne);
+                if (jb->c.h_est) memset(jb->c.h_est, 0, nj * sizeof(double));
+            }
+            memset(jb->c.touched, 0, nj / JCHUNK + 1);
+            memset(jb->c.touched_e, 0, ne / JCHUNK + 1);
+        }
         stats->crossings += jb->c.st.crossings;
         stats->interactions += jb->c.st.interactions;
         stats->absorptions += jb->c.st.absorptions;
@@ -592,6 +670,7 @@ int orc_transport(const orc_transport_in* in, uint64_t seed, uint64_t counter_ba
         stats->q_phot += jb->c.st.q_phot;
         if (jb->err) { stats->error = 1; rc = 1; }
     }
+    pthread_mutex_unlock(&g_pool_lock);
     free(jobs); free(th);
     return rc;
 }

@@ -216,3 +216,36 @@ def test_state_save_restore(decks, data_dir):
     ctx.state_restore()
     np.testing.assert_array_equal(ctx.get(abi.ARR_TE), te0)
     ctx.close()
+
+
+def test_state_slots_rerun_iterations(decks, data_dir):
+    """A slot holds everything an iteration hands to the next (gas state and the
+    skip rule's kept opacity and CDF): rerunning iterations 2 and 3 from their
+    slots reproduces them bit for bit (FP64 path: compensated J, deterministic
+    phases)."""
+    s = Setup(decks["lognormal_small"], data_dir)
+    ctx = Context(0)
+    ctx.load(s)
+
+    def iterate(it):
+        ctx.opacity(it)
+        ctx.emission(it)
+        ctx.transport(20000, seed=3, counter_base=it << 40, precision=abi.PREC_FP64)
+        ctx.normalize_j()
+        ctx.balance()
+        return [ctx.get(a) for a in (abi.ARR_TE, abi.ARR_NE, abi.ARR_IONDEN, abi.ARR_OPACITY, abi.ARR_RECPDF)]
+
+    iterate(1)
+    ctx.state_save(2)
+    first2 = iterate(2)
+    ctx.state_save(3)
+    first3 = iterate(3)
+    ctx.state_restore(2)
+    for a, b in zip(iterate(2), first2):
+        np.testing.assert_array_equal(a, b)
+    ctx.state_restore(3)
+    for a, b in zip(iterate(3), first3):
+        np.testing.assert_array_equal(a, b)
+    with pytest.raises(abi.McxError):
+        ctx.state_restore(7)
+    ctx.close()

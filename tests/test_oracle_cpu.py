@@ -150,3 +150,22 @@ def test_optically_thin_mean_intensity(tmp_path, data_dir, oracle_lib):
     # transported packets fly radially (octant fold) to the edge of the active
     # sphere of radius Rout = 6e18 cm, overshooting by up to a cell
     assert path / n == pytest.approx(transported * 6.1e18, rel=0.05)
+
+
+def test_threaded_phases_match_serial(decks, data_dir, oracle_lib):
+    """The oracle's per-cell phases shared among threads (the CPU baseline's
+    setting) give the serial results bit for bit."""
+    from mocassin_xray_gb300 import Setup, abi
+    s = Setup(decks["xray_small"], data_dir)
+    op1 = oracle_lib.opacity(s)
+    op4 = oracle_lib.opacity(s, nthreads=4)
+    np.testing.assert_array_equal(op1, op4)
+    T = oracle_lib.BalanceTables(s)
+    te, ne, ion = s.get(abi.ARR_TE), s.get(abi.ARR_NE), s.get(abi.ARR_IONDEN)
+    fl1 = oracle_lib.for_lines_emission(T, te, ne, ion)
+    fl4 = oracle_lib.for_lines_emission(T, te, ne, ion, nthreads=4)
+    np.testing.assert_array_equal(fl1, fl4)
+    r1, t1 = oracle_lib.emission(s, 10000.0, for_lines=fl1)
+    r4, t4 = oracle_lib.emission(s, 10000.0, for_lines=fl1, nthreads=4)
+    np.testing.assert_array_equal(r1, r4)
+    np.testing.assert_array_equal(t1, t4)
