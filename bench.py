@@ -38,7 +38,7 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
-DATA_DIR = ROOT / "tests" / "golden" / "atomic_data"
+DATA_DIR = ROOT / "mocassin_xray_gb300" / "data"
 METRIC = "MC packets/s"
 UNIT = "packets/s"
 # kernels of one step: opacity 1; emission 7 (Gaunt table, the cells' places on

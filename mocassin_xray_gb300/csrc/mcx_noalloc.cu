@@ -65,13 +65,16 @@ __global__ void noallocTranspose(const float* __restrict__ in, float* __restrict
 }
 
 // Volumes of the active cells [e45 cm^3], getVolume (source/grid_mod.f90:2887-2986) in FP64 and FP32.
+// The caller's active map is checked on the way: an id above nCells is
+// counted in *badIds and its voxel skipped (the transport is then refused).
 __global__ void noallocVolumes(const float* X, const float* Y, const float* Z, const int32_t* active, int nx, int ny,
-                               int nz, int sym, double* volD, float* volF) {
-  const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= nx * ny * nz) return;
+                               int nz, int nCells, int sym, double* volD, float* volF, unsigned int* badIds) {
+  const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= (size_t)nx * ny * nz) return;
   const int cell = active[v];
   if (cell <= 0) return;
-  const int xP = v % nx + 1, yP = (v / nx) % ny + 1, zP = v / (nx * ny) + 1;
+  if (cell > nCells) { atomicAdd(badIds, 1u); return; }
+  const int xP = (int)(v % nx) + 1, yP = (int)((v / nx) % ny) + 1, zP = (int)(v / ((size_t)nx * ny)) + 1;
   double d[3];
   const float* A[3] = {X, Y, Z};
   const int P[3] = {xP, yP, zP}, N[3] = {nx, ny, nz};
@@ -114,9 +117,12 @@ extern "C" int mcx_transport_noalloc(const mcx_noalloc_transport_args* a, mcx_tr
     if (a->star_idx[d] < 1 || a->star_idx[d] > n) return fail(MCX_ERR_INPUT, "mcx_transport_noalloc: the source must lie inside the grid");
   }
   const size_t C1 = (size_t)a->n_cells + 1, nb = (size_t)a->nbins;
-  // scratch layout: counters | volD | volF | rec CDF rows | KN CDF rows | Pcomp rows
+  const size_t nvox = (size_t)a->nx * (size_t)a->ny * (size_t)a->nz;
+  if (nvox > (size_t)0x7fffffff) return fail(MCX_ERR_INPUT, "mcx_transport_noalloc: grid above 2^31 - 1 voxels");
+  // scratch layout: counters | active-map check | volD | volF | rec CDF rows | KN CDF rows | Pcomp rows
   const size_t offCnt = 0;
-  const size_t offVolD = roundUp(sizeof(DevTransportCounters));
+  const size_t offBad = roundUp(sizeof(DevTransportCounters));
+  const size_t offVolD = offBad + roundUp(sizeof(unsigned int));
   const size_t offVolF = offVolD + roundUp(C1 * sizeof(double));
   const size_t offRec = offVolF + roundUp(C1 * sizeof(float));
   const size_t offKn = offRec + roundUp(C1 * nb * sizeof(float));
@@ -131,30 +137,37 @@ extern "C" int mcx_transport_noalloc(const mcx_noalloc_transport_args* a, mcx_tr
   if (rc != MCX_OK) return rc;
   unsigned char* sb = static_cast<unsigned char*>(base);
   auto* cnt = reinterpret_cast<DevTransportCounters*>(sb + offCnt);
+  auto* badIds = reinterpret_cast<unsigned int*>(sb + offBad);
   auto* volD = reinterpret_cast<double*>(sb + offVolD);
   auto* volF = reinterpret_cast<float*>(sb + offVolF);
   auto* recT = reinterpret_cast<float*>(sb + offRec);
   auto* knT = reinterpret_cast<float*>(sb + offKn);
   auto* pcT = reinterpret_cast<float*>(sb + offPc);
   cudaStream_t s = static_cast<cudaStream_t>(a->stream);
-  int dev = 0, numSMs = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, dev);
-
   cudaError_t e;
 #define NA_CK(call, what) \
   if ((e = (call)) != cudaSuccess) return fail(MCX_ERR_CUDA, std::string("mcx_transport_noalloc: ") + what + ": " + cudaGetErrorString(e))
+  int dev = 0, numSMs = 0;
+  NA_CK(cudaGetDevice(&dev), "cudaGetDevice");
+  NA_CK(cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, dev), "multiprocessor count");
   NA_CK(cudaMemsetAsync(cnt, 0, sizeof(DevTransportCounters), s), "clear counters");
+  NA_CK(cudaMemsetAsync(badIds, 0, sizeof(unsigned int), s), "clear the active-map check");
   NA_CK(cudaMemsetAsync(volD, 0, C1 * sizeof(double), s), "clear volumes");
   NA_CK(cudaMemsetAsync(volF, 0, C1 * sizeof(float), s), "clear volumes");
   if (a->zero_estimators) {
     NA_CK(cudaMemsetAsync(a->jste, 0, C1 * nb * sizeof(double), s), "clear jste");
     NA_CK(cudaMemsetAsync(a->escaped, 0, C1 * (nb + 1) * sizeof(double), s), "clear escaped");
   }
-  const int nvox = a->nx * a->ny * a->nz;
-  noallocVolumes<<<(nvox + 255) / 256, 256, 0, s>>>(a->x_axis, a->y_axis, a->z_axis, a->active, a->nx, a->ny, a->nz,
-                                                    a->symmetric_xyz, volD, volF);
+  noallocVolumes<<<(unsigned)((nvox + 255) / 256), 256, 0, s>>>(a->x_axis, a->y_axis, a->z_axis, a->active, a->nx,
+                                                                 a->ny, a->nz, a->n_cells, a->symmetric_xyz, volD,
+                                                                 volF, badIds);
   NA_CK(cudaGetLastError(), "volumes");
+  unsigned int bad = 0;
+  NA_CK(cudaMemcpyAsync(&bad, badIds, sizeof(bad), cudaMemcpyDeviceToHost, s), "read the active-map check");
+  NA_CK(cudaStreamSynchronize(s), "synchronize");
+  if (bad)
+    return fail(MCX_ERR_INPUT, "mcx_transport_noalloc: " + std::to_string(bad) +
+                                   " voxel(s) of the active map name a cell above n_cells");
   dim3 tb(32, 8);
   noallocTranspose<<<dim3((unsigned)((C1 + 31) / 32), (unsigned)((nb + 31) / 32)), tb, 0, s>>>(a->rec_pdf, recT, (int)nb, (int)C1);
   NA_CK(cudaGetLastError(), "transpose recPDF");

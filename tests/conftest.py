@@ -8,7 +8,7 @@ import pytest
 ROOT = Path(__file__).resolve().parents[1]
 sys.path.insert(0, str(ROOT))
 
-DATA_DIR = ROOT / "tests" / "golden" / "atomic_data"
+DATA_DIR = ROOT / "mocassin_xray_gb300" / "data"
 
 
 def pytest_configure(config):

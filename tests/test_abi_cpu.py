@@ -87,3 +87,56 @@ def test_struct_layouts_match_the_header(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(cls), cname
         for field, _ in cls._fields_:
             assert got[(cname, field)] == getattr(cls, field).offset, f"{cname}.{field}"
+
+
+def _fortran_types(text: str) -> dict:
+    """The `type, bind(c)` blocks of INTEGRATION.md's Fortran module: name ->
+    [(field, bytes)] in order, arrays expanded to their element count."""
+    import re
+    kinds = {"c_int32_t": 4, "c_int": 4, "c_int64_t": 8, "c_double": 8, "c_float": 4, "c_size_t": 8}
+    out = {}
+    for m in re.finditer(r"type, bind\(c\) :: (\w+)\n(.*?)\n\s*end type", text, re.S):
+        fields = []
+        for line in m.group(2).splitlines():
+            line = line.split("!")[0].strip()
+            if not line:
+                continue
+            decl, names = line.split("::")
+            size = 8 if "c_ptr" in decl else kinds[re.search(r"\((c_\w+)\)", decl).group(1)]
+            for nm in names.split(","):
+                nm = nm.strip()
+                a = re.match(r"(\w+)\((\d+)\)", nm)
+                fields.append((a.group(1), size * int(a.group(2))) if a else (nm, size))
+        out[m.group(1)] = fields
+    return out
+
+
+def _c_struct(text: str, name: str) -> list:
+    import re
+    sizes = {"int32_t": 4, "int64_t": 8, "uint64_t": 8, "double": 8, "float": 4}
+    body = re.search(r"typedef struct " + name + r" \{(.*?)\} " + name + ";", text, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    fields = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        m = re.match(r"(\w+)\s*(\*?)\s*(.*)", decl)
+        base, ptr, rest = m.groups()
+        for nm in rest.split(","):
+            nm = nm.strip()
+            a = re.match(r"(\w+)\[(\d+)\]", nm)
+            size = 8 if ptr or nm.startswith("*") else sizes[base]
+            nm = nm.lstrip("*")
+            fields.append((a.group(1), size * int(a.group(2))) if a else (nm, size))
+    return fields
+
+
+def test_fortran_binding_matches_header():
+    """INTEGRATION.md's ISO_C_BINDING types have the header's fields, in order and of the same sizes."""
+    root = Path(__file__).resolve().parents[1]
+    ftypes = _fortran_types((root / "INTEGRATION.md").read_text())
+    header = (root / "include" / "mcx.h").read_text()
+    assert {"mcx_balance_opts", "mcx_transport_opts", "mcx_lines"} <= set(ftypes)
+    for name, ffields in ftypes.items():
+        assert ffields == _c_struct(header, name), name

@@ -18,7 +18,7 @@ import pytest
 
 from mocassin_xray_gb300 import abi, Setup
 
-DATA = Path(__file__).resolve().parent / "golden" / "atomic_data"
+DATA = Path(__file__).resolve().parents[1] / "mocassin_xray_gb300" / "data"
 
 
 def fnum(tok: str) -> float:

@@ -1,7 +1,8 @@
-"""The reference's own benchmark decks (benchmarks/gas) read by the deck grammar of libmcx, when the
-reference tree is present on the machine running the tests (it is not on every machine): the
+"""The reference's own benchmark decks (benchmarks/gas) read by the deck grammar of libmcx, when a
+MOCASSIN source tree is named by MCX_REFERENCE_DIR on the machine running the tests: the
 photoionisation benchmarks parse into grids of the expected shape, and the decks that select paths
 outside this library (plane-parallel illumination) are rejected with a message, not misread."""
+import os
 import shutil
 from pathlib import Path
 
@@ -9,8 +10,11 @@ import pytest
 
 from mocassin_xray_gb300 import abi, Setup
 
-BENCH = Path("/root/reference/benchmarks/gas")
-pytestmark = pytest.mark.skipif(not BENCH.is_dir(), reason="the reference's benchmark decks are not on this machine")
+# the root of a MOCASSIN source tree, when one is on the machine
+REF = os.environ.get("MCX_REFERENCE_DIR", "")
+BENCH = Path(REF) / "benchmarks" / "gas"
+pytestmark = pytest.mark.skipif(not REF or not BENCH.is_dir(),
+                                reason="no MOCASSIN tree (MCX_REFERENCE_DIR) with its benchmark decks on this machine")
 
 
 def _deck(tmp_path, name):

@@ -96,3 +96,29 @@ def test_noalloc_rejects_problems_beyond_its_scratch():
     rc = abi.lib().mcx_transport_noalloc(ctypes.byref(a), ctypes.byref(st))
     assert rc == 1
     assert b"scratch" in abi.lib().mcx_noalloc_last_error()
+
+
+def test_noalloc_rejects_an_active_map_beyond_n_cells(decks, data_dir, oracle_lib):
+    """The caller's active map is checked on the device before any packet
+    moves: a voxel naming a cell above n_cells is refused (the allocating entry
+    point validates the map at load time; this one never sees a load)."""
+    torch = pytest.importorskip("torch")
+    s = Setup(decks["h_small"], data_dir)
+    op = oracle_lib.opacity(s)
+    rec = synthetic_recpdf(s.get(abi.ARR_NU), s.n_cells)
+    tl = np.full(s.n_cells + 1, 0.3, np.float32)
+    keep = []
+    a, j_dev, e_dev = _noalloc_args(torch, s, op, rec, tl, keep)
+    act = s.get(abi.ARR_ACTIVE).copy()
+    act.reshape(-1)[np.argmax(act.reshape(-1) > 0)] = s.n_cells + 5
+    bad = _dev(torch, act)
+    keep.append(bad)
+    a.active = bad.data_ptr()
+    torch.cuda.synchronize()
+    a.n_packets, a.seed, a.counter_base, a.precision = 1000, 1, 0, abi.PREC_FP64
+    a.zero_estimators, a.delta_e = 1, 1.0
+    st = abi.TransportStats()
+    rc = abi.lib().mcx_transport_noalloc(ctypes.byref(a), ctypes.byref(st))
+    assert rc == 1                                 # MCX_ERR_INPUT
+    assert b"active map" in abi.lib().mcx_noalloc_last_error()
+    assert float(j_dev.abs().sum()) == 0.0        # nothing was transported
