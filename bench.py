@@ -581,9 +581,11 @@ def run_gpu(args, dist, ws, rank, local):
 
 def run_batch(args, dist, ws, rank, local):
     """256 H + He nebulae (edges 9..33 cells, n_H 10..1e4, 30-60 kK, 1e5..1e7 packets each) as one
-    batched context: a step is one MC iteration of every nebula (mcx_iterate_batched).  Reported:
-    aggregate packets/s, p50 / p99 of the step time, and the same nebulae run one context after
-    another (the single-nebula path) for comparison."""
+    batched context: a step is one MC iteration of every nebula (mcx_iterate_batched), with the
+    transport launch chosen by the autotuner beforehand (untimed).  Reported: aggregate packets/s,
+    p50 / p99 over the nebulae of the per-nebula iteration time (the shared per-cell phases plus the
+    moment the nebula's last packet finished in the batched launch), p50 / p99 of the step time, and
+    the same nebulae run one context after another (the single-nebula path) for comparison."""
     import torch
     from mocassin_xray_gb300 import Context, Setup, abi, configs
     torch.cuda.set_device(local)
@@ -598,12 +600,26 @@ def run_batch(args, dist, ws, rank, local):
     nb = setups[0].nbins
     cells = int(ctx.cell_offsets[-1])
 
+    # the transport launch measured once on this batch (untimed)
+    from mocassin_xray_gb300 import autotune
+    ctx.opacity(1)
+    ctx.emission(1, precision=abi.PHASE_MIXED)
+    tuned = autotune.tune_transport(
+        lambda L: ctx.transport_batched(packets, seeds, block_size=L["block_size"], grid_mult=L["grid_mult"],
+                                        emit_batch=L["emit_batch"]).kernel_ms, reps=1)
+    launch = autotune.launch_of(tuned)
+    per_neb = []
+
     def step(i: int):
         ctx.state_restore()
-        return ctx.iterate_batched(packets, seeds + np.uint64(i), 0, n_iterate_mc=1)
+        st = ctx.iterate_batched(packets, seeds + np.uint64(i), 0, n_iterate_mc=1, launch=launch)
+        done = ctx.batch_transport_ms()
+        per_neb.append(st.opacity.kernel_ms + st.emission.kernel_ms + done + st.balance.kernel_ms)
+        return st
 
     for i in range(args.warmup):
         step(i)
+    per_neb.clear()
     ctx.sync()
     barrier(dist)
     clocks = ClockSampler(local)
@@ -682,6 +698,13 @@ def run_batch(args, dist, ws, rank, local):
                    "precision": "fp32 geometry, fp64 estimators, mixed balance",
                    "l2": "inputs larger than L2 (Jste fp64 of the batch)", "parallelism": "single GPU"},
         "iteration_ms": {"p50": float(np.percentile(per_step, 50)), "p99": float(np.percentile(per_step, 99))},
+        "nebula_iteration_ms": {"p50": float(np.percentile(np.concatenate(per_neb), 50)),
+                                "p99": float(np.percentile(np.concatenate(per_neb), 99)),
+                                "max": float(np.max(np.concatenate(per_neb))),
+                                "what": "per nebula: opacity + emission + the moment its last packet finished in "
+                                        "the batched transport + balance (the per-cell phases run once for the "
+                                        "whole batch)"},
+        "autotuned_launch": {**launch, "speedup_over_defaults": tuned["speedup"], "tuning_s": tuned["tuning_s"]},
         "e2e": {"value": ws * total_packets / (ms_e2e_step / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": h2d},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

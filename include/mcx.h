@@ -394,7 +394,10 @@ typedef struct mcx_iterate_opts {
     int64_t n_packets;              /* nPhotons(1)                                         */
     uint64_t seed;                  /* Philox key                                          */
     uint64_t counter_base;          /* global id of the iteration's first packet           */
-    int32_t reserved[8];
+    int32_t transport_block_size;   /* the transport launch (mcx_transport_opts' fields of the */
+    int32_t transport_grid_mult;    /* same names); 0 = library defaults                   */
+    int32_t transport_emit_batch;
+    int32_t reserved[5];
 } mcx_iterate_opts;
 
 typedef struct mcx_iterate_stats {
@@ -545,6 +548,13 @@ int  mcx_line_luminosities(mcx_ctx* ctx, mcx_lines* out);
 /* The same for nebula b of a batch (mcx_load_batched): its cells only, its
  * octant factor. */
 int  mcx_line_luminosities_nebula(mcx_ctx* ctx, int32_t nebula, mcx_lines* out);
+
+/* When each nebula's last packet of the latest mcx_transport_batched (or
+ * mcx_iterate_batched) call finished, in ms after the launch began
+ * (ms[nebula], n = the batch size; 0 for a nebula without packets).  The
+ * batched kernel stamps the GPU's global timer as a lane finishes a packet.
+ * No counterpart in the reference (one nebula per job). */
+int  mcx_batch_transport_ms(mcx_ctx* ctx, double* ms, int32_t n);
 
 
 /* ------------------------------------------- transport without allocation */

@@ -75,7 +75,9 @@ class BalanceStats(C.Structure):
 class IterateOpts(C.Structure):
     _fields_ = [("n_iterate_mc", C.c_int32), ("transport_precision", C.c_int32), ("balance_precision", C.c_int32),
                 ("emission_precision", C.c_int32), ("n_packets", C.c_int64), ("seed", C.c_uint64),
-                ("counter_base", C.c_uint64), ("reserved", C.c_int32 * 8)]
+                ("counter_base", C.c_uint64), ("transport_block_size", C.c_int32),
+                ("transport_grid_mult", C.c_int32), ("transport_emit_batch", C.c_int32),
+                ("reserved", C.c_int32 * 5)]
 
 
 class PhaseOpts(C.Structure):
@@ -182,6 +184,7 @@ SIGNATURES = [
     ("mcx_iterate", C.c_int, [_P, C.POINTER(IterateOpts), C.POINTER(IterateStats)]),
     ("mcx_line_luminosities", C.c_int, [_P, C.POINTER(Lines)]),
     ("mcx_line_luminosities_nebula", C.c_int, [_P, C.c_int32, C.POINTER(Lines)]),
+    ("mcx_batch_transport_ms", C.c_int, [_P, C.POINTER(C.c_double), C.c_int32]),
     ("mcx_line_sensitivities", C.c_int, [_P, C.POINTER(SensOpts), C.POINTER(SensOut)]),
     ("mcx_load_batched", C.c_int, [_P, _P, C.c_int32]),
     ("mcx_batch_info", C.c_int, [_P, C.POINTER(C.c_int32), _P]),

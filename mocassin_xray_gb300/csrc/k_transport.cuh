@@ -619,12 +619,22 @@ transportKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportC
 // that nebula's geometry with its own deltaE = L*/nPhotons and its own Philox
 // key and counter base, so every nebula's histories are those of a run of the
 // nebula alone.
+__device__ __forceinline__ unsigned long long globalTimerNs() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// The GPU's global timer when the batched launch begins (one thread, launched
+// on the same stream just before it).
+static __global__ void stampStartKernel(unsigned long long* startNs) { *startNs = globalTimerNs(); }
+
 template <typename R>
 __global__ void __launch_bounds__(256)
 transportKernelBatched(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportCounters* cnt,
                        const NebulaDesc* __restrict__ neb, const unsigned long long* __restrict__ pktBegin, int nNeb,
                        const float* __restrict__ axes, const int32_t* __restrict__ active,
-                       const float* __restrict__ cdfs, int emitBatch) {
+                       const float* __restrict__ cdfs, int emitBatch, unsigned long long* __restrict__ doneNs) {
   extern __shared__ float smem[];
   float* sNu = smem;
   for (int i = threadIdx.x; i < g.nbins; i += blockDim.x) sNu[i] = g.nu[i];
@@ -642,8 +652,22 @@ transportKernelBatched(DevGrid g, DevTransportIn in, DevTransportOut out, DevTra
   double deltaE = 0.;
   R deltaER = R(0);
   int state = ST_IDLE;
+  int mine = -1;              // the nebula of the lane's packet in flight
+  // the latest finish among this lane's packets of nebula stampNeb, published
+  // with one atomic when the lane moves on to another nebula (packet ids, and
+  // so the nebulae, are handed out in order) or leaves
+  int stampNeb = -1;
+  unsigned long long stampNs = 0ull;
 
   for (;;) {
+    if (state == ST_IDLE && mine >= 0) {
+      if (mine != stampNeb) {
+        if (stampNeb >= 0) atomicMax(doneNs + stampNeb, stampNs);
+        stampNeb = mine;
+      }
+      stampNs = globalTimerNs();
+      mine = -1;
+    }
     const unsigned need = __ballot_sync(FULL, state == ST_IDLE);
     if (need) {
       const unsigned long long id = refill(need, cnt);
@@ -663,6 +687,7 @@ transportKernelBatched(DevGrid g, DevTransportIn in, DevTransportOut out, DevTra
           deltaE = d.deltaE;
           deltaER = (R)deltaE;
           p.rng.init(d.seed, d.counterBase + (id - __ldg(pktBegin + lo)));
+          mine = lo;
           p.type = PT_STELLAR;
           p.nEmit = 0;
           state = ST_EMIT;
@@ -678,6 +703,7 @@ transportKernelBatched(DevGrid g, DevTransportIn in, DevTransportOut out, DevTra
       state = stepPacket<R>(g, q, in, out, sh, p, deltaER, deltaE, lc, pj);
     }
   }
+  if (stampNeb >= 0) atomicMax(doneNs + stampNeb, stampNs);
   flushJ(out, pj);
   flushCounters(lc, cnt);
 }

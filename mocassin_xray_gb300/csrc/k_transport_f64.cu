@@ -19,13 +19,16 @@ cudaError_t launchTransportBatchedF64(const DevGrid& g, const DevTransportIn& in
                                       DevTransportCounters* cnt, const NebulaDesc* neb,
                                       const unsigned long long* pktBegin, int nNeb, const float* axes,
                                       const int32_t* active, const float* cdfs, const TransportLaunch& L,
-                                      cudaStream_t s) {
+                                      unsigned long long* stamps, cudaStream_t s) {
   const size_t smem = packetStateOffset(L.smem) + packetStateBytes<double>(L.threads);
   cudaError_t e =
       cudaFuncSetAttribute(transportKernelBatched<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  // stamps[0]: the global timer at the start; stamps[1 + b]: when nebula b's last packet finished
+  stampStartKernel<<<1, 1, 0, s>>>(stamps);
   transportKernelBatched<double><<<L.blocks, L.threads, smem, s>>>(g, in, out, cnt, neb, pktBegin, nNeb, axes, active,
-                                                                  cdfs, L.emitBatch > 0 ? L.emitBatch : kEmitBatch);
+                                                                  cdfs, L.emitBatch > 0 ? L.emitBatch : kEmitBatch,
+                                                                  stamps + 1);
   return cudaGetLastError();
 }
 

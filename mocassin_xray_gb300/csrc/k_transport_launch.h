@@ -23,12 +23,12 @@ cudaError_t launchTransportBatchedF32(const DevGrid& g, const DevTransportIn& in
                                       DevTransportCounters* cnt, const NebulaDesc* neb,
                                       const unsigned long long* pktBegin, int nNeb, const float* axes,
                                       const int32_t* active, const float* cdfs, const TransportLaunch& L,
-                                      cudaStream_t s);
+                                      unsigned long long* stamps, cudaStream_t s);
 cudaError_t launchTransportBatchedF64(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,
                                       DevTransportCounters* cnt, const NebulaDesc* neb,
                                       const unsigned long long* pktBegin, int nNeb, const float* axes,
                                       const int32_t* active, const float* cdfs, const TransportLaunch& L,
-                                      cudaStream_t s);
+                                      unsigned long long* stamps, cudaStream_t s);
 cudaError_t transportOccupancyBatchedF32(int threads, size_t smem, int* blocksPerSM);
 cudaError_t transportOccupancyBatchedF64(int threads, size_t smem, int* blocksPerSM);
 

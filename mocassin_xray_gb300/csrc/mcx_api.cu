@@ -407,6 +407,7 @@ struct mcx_ctx {
   DBuf<float> nebGauntTeDev;
   DBuf<NebulaDesc> nebDescDev;
   DBuf<unsigned long long> nebPktBegin;
+  DBuf<unsigned long long> nebStamps;             // [0] launch start, [1 + b] nebula b's last packet (global timer, ns)
   DBuf<float> nebAxes, nebCdf, nebFfK, jDiv;
   DBuf<int32_t> nebActiveDev;
   DBuf<int16_t> nebFfIdx;
@@ -966,6 +967,8 @@ extern "C" int mcx_load_batched(mcx_ctx* c, const mcx_setup* const* setups, int3
   CK(c->nebGauntTeDev.alloc(n), "alloc batch Gaunt temperatures");
   CK(c->nebDescDev.alloc(n), "alloc batch descriptors");
   CK(c->nebPktBegin.alloc((size_t)n + 1), "alloc batch packet offsets");
+  CK(c->nebStamps.alloc((size_t)n + 1), "alloc batch timers");
+  CK(cudaMemset(c->nebStamps.p, 0, c->nebStamps.bytes()), "memset");
   CK(cudaDeviceSynchronize(), "mcx_load_batched");
   c->nebGauntTeOld.assign(n, -1.f);
   c->nebCellOff = off;
@@ -1390,17 +1393,34 @@ extern "C" int mcx_transport_batched(mcx_ctx* c, const mcx_transport_opts* o, co
     const unsigned long long maxBlocks = (total + L.threads - 1) / L.threads;
     if ((unsigned long long)L.blocks > maxBlocks) L.blocks = (int)maxBlocks;
   }
+  CK(cudaMemsetAsync(c->nebStamps.p, 0, c->nebStamps.bytes(), c->stream), "memset batch timers");
   CK(cudaEventRecord(c->ev0, c->stream), "event");
   if (total > 0) {
     cudaError_t e = fp64 ? launchTransportBatchedF64(g, in, out, c->counters.p, c->nebDescDev.p, c->nebPktBegin.p, n,
-                                                     c->nebAxes.p, c->nebActiveDev.p, c->nebCdf.p, L, c->stream)
+                                                     c->nebAxes.p, c->nebActiveDev.p, c->nebCdf.p, L,
+                                                     c->nebStamps.p, c->stream)
                          : launchTransportBatchedF32(g, in, out, c->counters.p, c->nebDescDev.p, c->nebPktBegin.p, n,
-                                                     c->nebAxes.p, c->nebActiveDev.p, c->nebCdf.p, L, c->stream);
+                                                     c->nebAxes.p, c->nebActiveDev.p, c->nebCdf.p, L,
+                                                     c->nebStamps.p, c->stream);
     if (e != cudaSuccess) return cudaFail(c, e, "batched transport kernel");
   }
   CK(cudaEventRecord(c->ev1, c->stream), "event");
   if (total > 0) CK(foldJ(c), "fold J compensation");
   return transportFinish(c, stats, "mcx_transport_batched");
+}
+
+extern "C" int mcx_batch_transport_ms(mcx_ctx* c, double* ms, int32_t n) {
+  if (!c || !ms) return fail(c, MCX_ERR_INPUT, "mcx_batch_transport_ms: null argument");
+  if (!c->loaded || c->nNeb <= 0) return fail(c, MCX_ERR_STATE, "mcx_batch_transport_ms: the context holds no batch");
+  if (n != c->nNeb) return fail(c, MCX_ERR_INPUT, "mcx_batch_transport_ms: n must be the batch size");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  std::vector<unsigned long long> t((size_t)n + 1);
+  CK(cudaMemcpyAsync(t.data(), c->nebStamps.p, t.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                     c->stream), "d2h batch timers");
+  CK(cudaStreamSynchronize(c->stream), "mcx_batch_transport_ms");
+  for (int b = 0; b < n; ++b)
+    ms[b] = (t[b + 1] > t[0]) ? (double)(t[b + 1] - t[0]) * 1e-6 : 0.;
+  return MCX_OK;
 }
 
 extern "C" int mcx_normalize_j(mcx_ctx* c) {
@@ -1527,6 +1547,9 @@ static int iterateImpl(mcx_ctx* c, const mcx_iterate_opts* o, const mcx_batch_pa
     to.counter_base = o->counter_base;
     to.n_photons_norm = o->n_packets;
     to.zero_estimators = 1;
+    to.block_size = o->transport_block_size;
+    to.grid_mult = o->transport_grid_mult;
+    to.emit_batch = o->transport_emit_batch;
     rc = pk ? mcx_transport_batched(c, &to, pk, &st.transport) : mcx_transport(c, &to, &st.transport);
   }
   if (rc == MCX_OK) rc = mcx_normalize_j(c);

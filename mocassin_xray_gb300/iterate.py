@@ -25,6 +25,7 @@ import numpy as np
 
 from . import abi
 from .model import Context, Setup
+from .shard import transport_sharded
 
 COUNTER_STRIDE = 1 << 40
 
@@ -47,11 +48,15 @@ class IterationReport:
 def iterate_mc(setup: Setup, ctx: Context | None = None, seed: int = 0, n_photons: int | None = None,
                max_iterations: int | None = None, precision: int = abi.PREC_FP32_GEOM,
                min_convergence: float | None = None, auto_packets: tuple[float, float, int] | None = None,
-               callback=None) -> list[IterationReport]:
+               callback=None, group=None, counter_base: int = 0) -> list[IterationReport]:
     """Runs MC iterations until totPercent >= minConvergence or maxIterateMC.
 
     auto_packets = (convIncPercent, nPhotIncrease, maxPhotons) enables the
-    reference's packet increase when convergence stalls (autoPackets)."""
+    reference's packet increase when convergence stalls (autoPackets).
+    group: a torch.distributed process group (or True for the default one)
+    whose ranks share each iteration's packets (shard.transport_sharded: one
+    sum of Jste and the escape tallies per iteration); every rank runs the
+    per-cell phases of every cell."""
     own = ctx is None
     if own:
         ctx = Context(0)
@@ -70,8 +75,12 @@ def iterate_mc(setup: Setup, ctx: Context | None = None, seed: int = 0, n_photon
             ms = {}
             ms["opacity"] = ctx.opacity(it).kernel_ms
             ms["emission"] = ctx.emission(it).kernel_ms
-            st = ctx.transport(n, seed=seed, counter_base=(it - 1) * COUNTER_STRIDE, precision=precision,
-                               zero=True, n_photons_norm=n)
+            if group is not None:
+                st = transport_sharded(ctx, n, seed, counter_base + (it - 1) * COUNTER_STRIDE, precision,
+                                       group=None if group is True else group)
+            else:
+                st = ctx.transport(n, seed=seed, counter_base=counter_base + (it - 1) * COUNTER_STRIDE,
+                                   precision=precision, zero=True, n_photons_norm=n)
             ms["transport"] = st.kernel_ms
             ctx.normalize_j()
             bs = ctx.balance()

@@ -136,25 +136,35 @@ class Context:
 
     def transport_batched(self, n_packets, seeds, counter_bases=None, precision: int = abi.PREC_FP32_GEOM,
                           zero: bool = True, n_photons_norm=None, block_size: int = 0,
-                          grid_mult: int = 0) -> abi.TransportStats:
+                          grid_mult: int = 0, emit_batch: int = 0) -> abi.TransportStats:
         """Every nebula's packets in one launch: n_packets, seeds, counter_bases per nebula (scalars broadcast)."""
         pk, keep = self._batch_packets(n_packets, seeds, counter_bases, n_photons_norm)
         o = abi.TransportOpts(istar=1, precision=precision, zero_estimators=1 if zero else 0, block_size=block_size,
-                              grid_mult=grid_mult)
+                              grid_mult=grid_mult, emit_batch=emit_batch)
         st = abi.TransportStats()
         self._check(lib().mcx_transport_batched(self._h, C.byref(o), C.byref(pk), C.byref(st)))
         return st
 
     def iterate_batched(self, n_packets, seeds, counter_bases=None, n_iterate_mc: int = 1,
                         transport_precision: int = abi.PREC_FP32_GEOM, balance_precision: int = abi.BAL_MIXED,
-                        emission_precision: int = abi.PHASE_MIXED) -> abi.IterateStats:
-        """One MC iteration of every nebula of the batch in one ABI call."""
+                        emission_precision: int = abi.PHASE_MIXED, launch: dict | None = None) -> abi.IterateStats:
+        """One MC iteration of every nebula of the batch in one ABI call; `launch` = the transport's
+        block_size / grid_mult / emit_batch (e.g. from autotune.tune_transport), library defaults if None."""
         pk, keep = self._batch_packets(n_packets, seeds, counter_bases, None)
+        L = launch or {}
         o = abi.IterateOpts(n_iterate_mc=n_iterate_mc, transport_precision=transport_precision,
-                            balance_precision=balance_precision, emission_precision=emission_precision)
+                            balance_precision=balance_precision, emission_precision=emission_precision,
+                            transport_block_size=L.get("block_size", 0), transport_grid_mult=L.get("grid_mult", 0),
+                            transport_emit_batch=L.get("emit_batch", 0))
         st = abi.IterateStats()
         self._check(lib().mcx_iterate_batched(self._h, C.byref(o), C.byref(pk), C.byref(st)))
         return st
+
+    def batch_transport_ms(self) -> np.ndarray:
+        """When each nebula's last packet of the latest batched transport finished, ms after its launch began."""
+        out = np.zeros(len(self.cell_offsets) - 1, dtype=np.float64)
+        self._check(lib().mcx_batch_transport_ms(self._h, out.ctypes.data_as(C.POINTER(C.c_double)), out.size))
+        return out
 
     def _shape(self, arr_id: int) -> tuple[tuple, type]:
         s = self.setup.info

@@ -10,7 +10,12 @@ the sum over ranks of their estimators equals the single-rank run packet for
 packet; the only exchange is the sum of J.
 
 ``shard_packets`` gives a rank its range; ``allreduce_sum`` sums an estimator
-array over the process group (NCCL on device tensors, gloo on host tensors).
+array over the process group (NCCL on device tensors, gloo on host tensors);
+``transport_sharded`` is one rank's transport phase of a sharded iteration
+through libmcx: its share of the packets, then the sum of Jste and of the
+escape tallies over the group, written back into the rank's context (every
+rank then balances every cell, as each MPI rank of the reference holds the
+whole grid).
 """
 from __future__ import annotations
 
@@ -37,3 +42,32 @@ def allreduce_sum(a, group=None):
         return t.numpy()
     dist.all_reduce(a, op=dist.ReduceOp.SUM, group=group)
     return a
+
+
+def transport_sharded(ctx, n_total: int, seed: int, counter_base: int, precision: int, group=None, **opts):
+    """The transport phase of one iteration sharded over the ranks of `group`
+    (source/iteration_mod.f90:729-753 and the MPI_Allreduce of Jste and
+    escapedPackets at :953): this rank transports packets
+    [counter_base + first, + count) of the iteration's n_total (deltaE =
+    Lstar / n_total on every rank), then Jste and the escape tallies are summed
+    over the group and put back into the context, and the returned statistics
+    are the group's totals."""
+    import torch
+    import torch.distributed as dist
+    from . import abi
+    rank, world = dist.get_rank(group), dist.get_world_size(group)
+    first, count = shard_packets(n_total, rank, world)
+    st = ctx.transport(count, seed=seed, counter_base=counter_base + first, precision=precision, zero=True,
+                       n_photons_norm=n_total, **opts)
+    for arr in (abi.ARR_JSTE, abi.ARR_ESCAPED):
+        ctx.put(arr, allreduce_sum(ctx.get(arr), group))
+    names = ("crossings", "interactions", "absorptions", "scatterings", "escaped", "line_escapes", "trapped",
+             "emissions")
+    t = torch.tensor([getattr(st, k) for k in names], dtype=torch.int64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+    for k, v in zip(names, t.tolist()):
+        setattr(st, k, v)
+    q = torch.tensor([st.q_phot], dtype=torch.float64)
+    dist.all_reduce(q, op=dist.ReduceOp.SUM, group=group)
+    st.q_phot = float(q.item())
+    return st

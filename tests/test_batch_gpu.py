@@ -95,3 +95,32 @@ def test_line_luminosities_per_nebula(batch_setups):
     with pytest.raises(RuntimeError, match="batch"):
         bc.line_luminosities()
     bc.close()
+
+
+def test_batch_timers_and_tuned_launch(data_dir, tmp_path):
+    """Each nebula's finishing time within the batched launch lies inside the
+    launch, and the autotuned launch shape gives the same J bits as the default
+    one (the shape changes the schedule, never a history)."""
+    from mocassin_xray_gb300 import autotune
+    decks = configs.nebula_batch(tmp_path, n=6, seed=3, max_edge=13, packets_range=(5e3, 2e4))
+    setups = [Setup(d, data_dir, mesh_mode=abi.MESH_LOG_EDGES) for d, _ in decks]
+    packets = np.array([pk for _, pk in decks], dtype=np.int64)
+    seeds = np.arange(len(decks), dtype=np.uint64) + np.uint64(40)
+    ctx = Context(0)
+    ctx.load_batched(setups)
+    ctx.opacity(1)
+    ctx.emission(1)
+    st = ctx.transport_batched(packets, seeds)
+    j0 = ctx.get(abi.ARR_JSTE)
+    ms = ctx.batch_transport_ms()
+    assert ms.shape == (len(setups),)
+    assert np.all(ms > 0) and ms.max() <= st.kernel_ms * 1.05 + 0.05
+
+    def run(L):
+        return ctx.transport_batched(packets, seeds, block_size=L["block_size"], grid_mult=L["grid_mult"],
+                                     emit_batch=L["emit_batch"]).kernel_ms
+
+    tuned = autotune.tune_transport(run, reps=1)
+    ctx.transport_batched(packets, seeds, **autotune.launch_of(tuned))
+    np.testing.assert_array_equal(ctx.get(abi.ARR_JSTE), j0)
+    ctx.close()
