@@ -66,7 +66,7 @@ enum mcx_array_id {
     MCX_ARR_RECPDF,          /* float [nbins][nCells+1]  recPDF(0:C,1:B)          */
     MCX_ARR_TOTAL_LINES,     /* float [nCells+1]         totalLines(0:C)          */
     MCX_ARR_JSTE,            /* double[nbins][nCells+1]  Jste(0:C,1:B)            */
-    MCX_ARR_ESCAPED,         /* double[nbins+1][nCells+1] escapedPackets(0:C,0:B,0) */
+    MCX_ARR_ESCAPED,         /* double[nAngleBins+1][nbins+1][nCells+1] escapedPackets(0:C,0:B,0:nAngleBins) */
     MCX_ARR_VOLUME,          /* float [nCells+1]      getVolume per active cell    */
     MCX_ARR_ELEM_ABUN,       /* float [30]            elemAbun(1,1:30)             */
     MCX_ARR_GAUNT_TE,        /* float [nCells+1]      Te at which the ff Gaunt factor
@@ -183,7 +183,11 @@ typedef struct mcx_setup_info {
     float   te_start;
     float   min_convergence;    /* minConvergence [%]                                 */
     float   xhi_limit;          /* XHILimit                                           */
-    int32_t reserved[8];
+    int32_t n_angle_bins;       /* nAngleBins: viewing angles of the 'inclination' keyword
+                                   (0..2); MCX_ARR_ESCAPED then holds 1 + n_angle_bins planes */
+    float   view_theta[2];      /* viewPointTheta(1:2) [rad]                           */
+    float   view_phi[2];        /* viewPointPhi(1:2) [rad]; < 0: no phi dependence     */
+    int32_t reserved[3];
 } mcx_setup_info;
 
 int  mcx_setup_from_input(const char* input_file, const char* data_dir,

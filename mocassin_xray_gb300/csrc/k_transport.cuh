@@ -181,10 +181,36 @@ __device__ __forceinline__ void initPacket(const Geo& q, const TransportShared<R
   p.origin = (xP > 0 && yP > 0 && zP > 0) ? activeAt(q, xP, yP, zP) : 0;
 }
 
+// The escape tally (e.g. source/photon_mod.f90:2293-2378): plane 0 of
+// escapedPackets always; with viewing angles also plane k when the direction's
+// (theta, phi) bin belongs to view k, where theta bins cover [0, pi] in 20 and
+// phi bins [0, 2 pi) in totAngleBinsPhi, phi = atan(vy / vx) truncated toward
+// zero and taken as 0 for vx < 1e-35 (the reference's own binning: every
+// packet leaving with vx <= 0 lands in phi bin 1, and since atan spans
+// (-pi/2, pi/2) the bins between pi/2 and 3 pi/2 receive nothing).  Directions in no view's
+// bins have viewPointPtheta = viewPointPphi = 0, which the reference's test
+// counts as a match of view 0, adding deltaE to plane 0 a second time; both
+// are reproduced.
 template <typename R>
 __device__ __forceinline__ void escapeTally(const DevGrid& g, const DevTransportOut& out, const Packet<R>& p,
                                             double deltaE, LocalCounters& lc) {
-  atomicAdd(out.escaped + (size_t)p.origin + ((size_t)g.nCells + 1) * (size_t)p.nuP, deltaE);
+  const size_t plane = ((size_t)g.nCells + 1) * ((size_t)g.nbins + 1);
+  const size_t at = (size_t)p.origin + ((size_t)g.nCells + 1) * (size_t)p.nuP;
+  if (g.nAngle > 0) {
+    const R dTheta = R(3.141592654) / R(20);
+    const R dPhi = (R(2) * R(3.141592654)) / (R)g.totPhi;
+    int idirT = (int)(acos(p.vz) / dTheta) + 1;
+    if (idirT > 20) idirT = 20;
+    if (idirT < 1) idirT = 1;
+    int idirP = p.vx < R(1.e-35) ? 0 : (int)(atan(p.vy / p.vx) / dPhi);
+    if (idirP < 0) idirP = g.totPhi + idirP;
+    idirP = idirP + 1;
+    if (idirP > g.totPhi) idirP = g.totPhi;
+    const int k = g.viewPTheta[idirT];
+    if ((g.totPhi > 1 && k == g.viewPPhi[idirP]) || (g.totPhi == 1 && k > 0))
+      atomicAdd(out.escaped + plane * (size_t)k + at, deltaE);
+  }
+  atomicAdd(out.escaped + at, deltaE);
   ++lc.escaped;
 }
 

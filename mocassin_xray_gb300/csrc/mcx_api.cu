@@ -107,6 +107,8 @@ extern "C" int mcx_setup_info_get(const mcx_setup* m, mcx_setup_info* info) {
   const Setup& s = m->s;
   std::memset(info, 0, sizeof(*info));
   info->nx = s.nx; info->ny = s.ny; info->nz = s.nz;
+  info->n_angle_bins = s.p.nAngleBins;
+  for (int j = 0; j < 2; ++j) { info->view_theta[j] = s.p.viewTheta[j]; info->view_phi[j] = s.p.viewPhi[j]; }
   info->n_cells = s.nCells;
   info->nbins = s.nbins;
   info->n_xsec = (int32_t)s.xSec.size();
@@ -375,6 +377,9 @@ struct mcx_ctx {
   // phase arrays
   DBuf<float> opacity, recPDF, recCDFT, totalLines, scaOpac, dustPDF, dustCDFT;
   DBuf<double> jste, jlo, escaped, hEst;   // jlo: the compensation of jste during a transport call
+  // viewing angles (source/grid_mod.f90:570-601): escapedPackets' planes 1..nAngle
+  int nAngle = 0, totPhi = 20;
+  int8_t viewPTheta[21] = {}, viewPPhi[21] = {};
   // scratch
   DBuf<float> gauntTe;
   DBuf<uint8_t> computeMask;
@@ -723,6 +728,25 @@ static int loadSetup(mcx_ctx* c, const Setup& s) {
   if (s.starIdx[0] < 1 || s.starIdx[0] > s.nx || s.starIdx[1] < 1 || s.starIdx[1] > s.ny || s.starIdx[2] < 1 || s.starIdx[2] > s.nz)
     return fail(c, MCX_ERR_INPUT, "mcx_load: the source must lie inside the grid");
   c->activeHost = s.active;
+  // viewing-angle bins (initCartesianGrid, source/grid_mod.f90:570-601): theta in 20 bins over
+  // [0, pi], phi in 20 over [0, 2 pi) unless a view's phi is negative (no phi dependence)
+  c->nAngle = s.p.nAngleBins;
+  c->totPhi = 20;
+  std::memset(c->viewPTheta, 0, sizeof c->viewPTheta);
+  std::memset(c->viewPPhi, 0, sizeof c->viewPPhi);
+  if (c->nAngle > 0) {
+    float vphi[2] = {s.p.viewPhi[0], s.p.viewPhi[1]};
+    for (int i = 0; i < c->nAngle; ++i)
+      if (vphi[i] < 0.f) { c->totPhi = 1; vphi[0] = vphi[1] = -1.f; break; }
+    const float pi = 3.141592654f, dTheta = pi / 20.f, dPhi = (2.f * pi) / (float)c->totPhi;
+    for (int i = 0; i < c->nAngle; ++i) {
+      const int kt = (int)(s.p.viewTheta[i] / dTheta) + 1, kp = (int)(vphi[i] / dPhi) + 1;
+      if (kt < 0 || kt > 20 || kp < 0 || kp > c->totPhi)
+        return fail(c, MCX_ERR_INPUT, "mcx_load: an inclination angle lies outside [0, pi] x [0, 2 pi)");
+      c->viewPTheta[kt] = (int8_t)(i + 1);
+      c->viewPPhi[kp] = (int8_t)(i + 1);
+    }
+  }
 
   const int nb = s.nbins;
   const size_t C1 = (size_t)s.nCells + 1;
@@ -779,7 +803,7 @@ static int loadSetup(mcx_ctx* c, const Setup& s) {
   CK(c->totalLines.alloc(C1), "alloc totalLines");
   CK(c->jste.alloc(C1 * nb), "alloc Jste");
   CK(c->jlo.alloc(C1 * nb), "alloc Jste compensation");
-  CK(c->escaped.alloc(C1 * (nb + 1)), "alloc escaped");
+  CK(c->escaped.alloc(C1 * (nb + 1) * (size_t)(c->nAngle + 1)), "alloc escaped");
   if (c->radPress) CK(c->hEst.alloc(C1 * nb), "alloc H");
   if (c->lgDust) {
     CK(c->scaOpac.alloc(C1 * nb), "alloc scaOpac");
@@ -866,6 +890,7 @@ extern "C" int mcx_load_batched(mcx_ctx* c, const mcx_setup* const* setups, int3
   for (int b = 0; b < n; ++b) {
     const Setup& s = setups[b]->s;
     if (!s.p.lgGas || s.p.lgDust) return fail(c, MCX_ERR_INPUT, "mcx_load_batched: a batch holds gas-only nebulae");
+    if (s.p.nAngleBins > 0) return fail(c, MCX_ERR_INPUT, "mcx_load_batched: viewing angles (inclination) are not batched");
     if (s.p.lgRadPress) return fail(c, MCX_ERR_INPUT, "mcx_load_batched: radiation pressure is not supported in a batch");
     if (s.nbins != s0.nbins || s.nu != s0.nu || s.widFlx != s0.widFlx) return bad(b, "the frequency mesh");
     if (s.p.nstages != s0.p.nstages || s.nElemUsed != s0.nElemUsed) return bad(b, "nstages or the elements");
@@ -1299,6 +1324,9 @@ extern "C" int mcx_transport(mcx_ctx* c, const mcx_transport_opts* o, mcx_transp
   g.xAxis = c->xAxis.p; g.yAxis = c->yAxis.p; g.zAxis = c->zAxis.p; g.active = c->active.p;
   g.nu = c->nu.p; g.srcCDF = c->srcCDF.p; g.KNsigmaT = c->KNsigmaT.p; g.KNcdfT = c->KNcdfT.p;
   g.PcompT = c->PcompT.p; g.volD = c->volD.p; g.volF = c->volF.p;
+  g.nAngle = c->nAngle; g.totPhi = c->totPhi;
+  std::memcpy(g.viewPTheta, c->viewPTheta, sizeof g.viewPTheta);
+  std::memcpy(g.viewPPhi, c->viewPPhi, sizeof g.viewPPhi);
   DevTransportIn in{};
   in.opacity = c->opacity.p; in.scaOpac = c->scaOpac.p; in.recCDFT = c->recCDFT.p; in.dustCDFT = c->dustCDFT.p;
   in.totalLines = c->totalLines.p; in.ne = c->ne.p;

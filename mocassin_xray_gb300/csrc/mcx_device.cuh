@@ -24,6 +24,11 @@ struct DevGrid {
   const float* PcompT;       // [nbins][180]
   const double* volD;        // [nCells+1] cell volume [e45 cm^3] (FP64)
   const float* volF;         // [nCells+1] the same in FP32
+  // viewing angles (the 'inclination' keyword): escapes are also binned into
+  // plane k of escapedPackets when their direction falls in view k's bins
+  int32_t nAngle, totPhi;            // nAngleBins; totAngleBinsPhi (20, or 1 without phi dependence)
+  int8_t viewPTheta[21];             // viewPointPtheta(0:20)
+  int8_t viewPPhi[21];               // viewPointPphi(0:totPhi)
 };
 
 // Per-cell fields the transport reads.

@@ -161,6 +161,17 @@ void parseInput(Params& p, const std::string& path) {
       else fail("readInput: Ndust needs 'constant' or 'file'");
     }
     else if (kw == "noScattering") p.lgDustScattering = false;
+    else if (kw == "inclination") {
+      // source/set_input_mod.f90:472-495: nAngleBins, then (theta, phi) [rad] per viewing angle
+      p.nAngleBins = (int)toI(t, 1, kw);
+      if (p.nAngleBins > 2)
+        fail("readInput: only two inclination angles are allowed per simulation");
+      if (p.nAngleBins < 0) fail("readInput: negative number of inclination angles");
+      for (int j = 0; j < p.nAngleBins; ++j) {
+        p.viewTheta[j] = toF(t, 2 + 2 * j, kw);
+        p.viewPhi[j] = toF(t, 3 + 2 * j, kw);
+      }
+    }
     else if (kw == "H0Start" || kw == "NeStart" || kw == "debug" || kw == "traceHeating" ||
              kw == "noPhotoelectric" || kw == "separateSED") {
       // accepted; these do not change the transport + balance path built here
@@ -168,7 +179,7 @@ void parseInput(Params& p, const std::string& path) {
     else if (kw == "planeIonization" || kw == "multiGrids" || kw == "multiChemistry" ||
              kw == "2D" || kw == "diffuseSource" || kw == "multiPhotoSources" ||
              kw == "quantumHeatGrain" || kw == "resLinesTransfer" || kw == "MdMg" || kw == "MdMh" ||
-             kw == "inclination" || kw == "fluorescence" || kw == "nahar") {
+             kw == "fluorescence" || kw == "nahar") {
       fail("readInput: keyword '" + kw + "' selects a reference path outside this library's scope");
     }
     else fail("readInput: invalid keyword in model parameter input file: " + kw);

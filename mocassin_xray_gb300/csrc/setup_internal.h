@@ -38,6 +38,8 @@ struct Params {
   float NdustValue = 0.f, MdMgValue = 0.f;
   float pwlIndex = 0.f, pwlMin = 0.f, pwlMax = 0.f;
   float starPos[3] = {0.f, 0.f, 0.f};
+  int nAngleBins = 0;             // 'inclination': viewing angles (at most 2)
+  float viewTheta[2] = {0.f, 0.f}, viewPhi[2] = {0.f, 0.f};
   bool haveStarPos = false, haveLStar = false, haveTStellar = false;
   bool haveContShape = false, haveNPhotons = false, haveAbundance = false;
   std::string contShape;          // "blackbody" | "powerlaw"

@@ -173,7 +173,7 @@ class Context:
         shapes = {
             abi.ARR_OPACITY: ((nb, C1), f32), abi.ARR_RECPDF: ((nb, C1), f32), abi.ARR_SCAOPAC: ((nb, C1), f32),
             abi.ARR_DUSTPDF: ((nb, C1), f32), abi.ARR_JSTE: ((nb, C1), f64), abi.ARR_H_EST: ((nb, C1), f64),
-            abi.ARR_ESCAPED: ((nb + 1, C1), f64), abi.ARR_TOTAL_LINES: ((C1,), f32), abi.ARR_HDEN: ((C1,), f32),
+            abi.ARR_ESCAPED: (((nb + 1, C1) if s.n_angle_bins == 0 else (s.n_angle_bins + 1, nb + 1, C1)), f64), abi.ARR_TOTAL_LINES: ((C1,), f32), abi.ARR_HDEN: ((C1,), f32),
             abi.ARR_TE: ((C1,), f32), abi.ARR_NE: ((C1,), f32), abi.ARR_TEOLD: ((C1,), f32),
             abi.ARR_NEOLD: ((C1,), f32), abi.ARR_VOLUME: ((C1,), f32), abi.ARR_GAUNT_TE: ((C1,), f32),
             abi.ARR_NDUST: ((C1,), f32), abi.ARR_LG_CONVERGED: ((C1,), np.int32),

@@ -126,34 +126,52 @@ def _radio_pointer(nu: np.ndarray) -> int:
 
 
 def sed(setup: Setup, escaped: np.ndarray) -> tuple[np.ndarray, float]:
-    """SED(freq) of writeSED (source/output_mod.f90:2984-3015): escapedPackets summed over the cells,
-    times 8 in symmetricXYZ mode; returns (SED [nbins] in e36 erg/s per bin, total energy)."""
-    nb = setup.info.nbins
-    esc = np.asarray(escaped, dtype=np.float64).reshape(nb + 1, -1)
-    s = esc[1:, :].sum(axis=1)
-    if setup.info.symmetric_xyz:
-        s = s * 8.0
-    return s, float(s.sum())
+    """SED(freq, imu) of writeSED (source/output_mod.f90:2984-3015): escapedPackets summed over the
+    cells for frequencies 1..nbins and every viewing-angle plane imu = 0..nAngleBins, plane imu >= 1
+    divided by dTheta (view theta > 0) and dPhi (view phi > 0), and in symmetricXYZ mode every plane
+    replaced by plane 0 x 8 (the reference's assignment); returns (SED [nbins] of plane 0, or
+    [nbins][nAngleBins+1] with viewing angles, in e36 erg/s per bin; the total energy of plane 0)."""
+    i = setup.info
+    nb, na = i.nbins, i.n_angle_bins
+    esc = np.asarray(escaped, dtype=np.float64).reshape(na + 1, nb + 1, -1)
+    s = esc[:, 1:, :].sum(axis=2).T                 # [nbins][nAngleBins+1]
+    if na:
+        pi = 3.141592654
+        tot_phi = 1 if any(i.view_phi[k] < 0 for k in range(na)) else 20
+        d_theta, d_phi = pi / 20, 2 * pi / tot_phi
+        for k in range(1, na + 1):
+            if i.view_theta[k - 1] > 0:
+                s[:, k] /= d_theta
+            if i.view_phi[k - 1] > 0 and tot_phi > 1:
+                s[:, k] /= d_phi
+    if i.symmetric_xyz:
+        s = np.repeat(s[:, :1] * 8.0, na + 1, axis=1)
+    total = float(s[:, 0].sum())
+    return (s[:, 0] if na == 0 else s), total
 
 
 def write_sed(path: str | Path, setup: Setup, escaped: np.ndarray) -> float:
-    """SED.out (source/output_mod.f90:2947-3064) for the integrated direction (no viewing angles):
-    nu [Ryd], lambda [um] and nu*F(nu) per row, the total energy and, where the mesh reaches
-    4.9 GHz, the radio flux.  Returns the total energy radiated [e36 erg/s]."""
+    """SED.out (source/output_mod.f90:2947-3064): nu [Ryd], lambda [um] and nu*F(nu) of the
+    integrated direction and of each viewing angle per row, the total energy and, where the mesh
+    reaches 4.9 GHz, the radio flux.  Returns the total energy radiated [e36 erg/s]."""
     nu = setup.get(abi.ARR_NU).astype(np.float64)
     wid = setup.get(abi.ARR_WIDFLX).astype(np.float64)
+    i = setup.info
     s, total = sed(setup, escaped)
-    out = [" Spectral energy distribution at the surface of the nebula: ", "   viewPoints = ",
+    s = s.reshape(nu.size, -1)
+    views = "".join(f" {i.view_theta[k]:12.6g} {i.view_phi[k]:12.6g}  , " for k in range(i.n_angle_bins))
+    out = [" Spectral energy distribution at the surface of the nebula: ", "   viewPoints = " + views,
            "    nu [Ryd]        lambda [um]        nu*F(nu)            ",
            " to obtain [E36 erg/sec/cm^2/str] divide column 3 by 4*Pi*D^2 or column 4 and higher by the "
            "emitting surface"]
     for f in range(nu.size):
         lam = _C_LIGHT / (nu[f] * _FR1RYD) * 1.e4
-        out.append(f" {nu[f]:16.8g} {lam:16.8g} {s[f] * nu[f] / wid[f]:16.8g}")
+        cols = " ".join(f"{s[f, k] * nu[f] / wid[f]:16.8g}" for k in range(s.shape[1]))
+        out.append(f" {nu[f]:16.8g} {lam:16.8g} {cols}")
     out += [" ", f" Total energy radiated out of the nebula [e36 erg/s]: {total:16.8g}", " "]
     p = _radio_pointer(setup.get(abi.ARR_NU))
     if p > 0:
-        flux = s[p - 1] * 3.141592654 * 1.e23 / (nu[p - 1] * _FR1RYD)
+        flux = s[p - 1, 0] * 3.141592654 * 1.e23 / (nu[p - 1] * _FR1RYD)
         out.append(f" Flux at 4.9GHz (must multiply by 1./(4 Pi D[cm]^2 to obtain units of [Jy]) : {flux:16.8g}")
     Path(path).write_text("\n".join(out) + "\n")
     return total

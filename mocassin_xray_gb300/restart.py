@@ -120,7 +120,7 @@ def write_grid(out_dir: str | Path, setup: Setup, state: dict) -> None:
           "0.0 0.0 dxSlit,dySlit", f"{_logical(i.lg_dust)} F lgDust, lgDustConstant", '"none" dustFile',
           '"none" dustFile', f"{_logical(i.lg_gas)} lgGas", "F lgRecombination",
           f"{i.n_species} {i.n_sizes} nSpecies, nSizes", "101 resLinesTransfer", "T lgDustScattering",
-          "0 nAngleBins", "0 0 continuumCube", "F lgPhotoelectric", "F lgTraceHeating", "0.0 Ldiffuse",
+          f"{i.n_angle_bins} nAngleBins", "0 0 continuumCube", "F lgPhotoelectric", "F lgTraceHeating", "0.0 Ldiffuse",
           "0.0 Tdiffuse", "none shapeDiffuse", "0 nPhotonsDiffuse", "0 emittingGrid", f"{i.nstages} nstages",
           "F lgMultiStars", f"{_logical(i.lg_compton)} compton?", "0.0 0.0 pwlMin, pwlMax", "F nahar?",
           "T badnell?", "F lgSeparateSED", "F 2D geometry?"]

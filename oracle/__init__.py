@@ -41,7 +41,25 @@ class TransportIn(C.Structure):
                 ("kn_sigma_t", _P), ("kn_cdf", _P), ("pcomp", _P), ("opacity", _P), ("sca_opac", _P),
                 ("rec_pdf", _P), ("dust_pdf", _P), ("total_lines", _P), ("ne", _P),
                 ("ion_edge1", C.c_float), ("r_out", C.c_float), ("star_pos", C.c_float * 3),
-                ("star_idx", C.c_int32 * 3), ("delta_e", C.c_double)]
+                ("star_idx", C.c_int32 * 3), ("delta_e", C.c_double), ("n_angle", C.c_int32),
+                ("tot_phi", C.c_int32), ("view_p_theta", C.c_int32 * 21), ("view_p_phi", C.c_int32 * 21)]
+
+
+def view_bins(n_angle: int, theta, phi) -> tuple[int, list, list]:
+    """totAngleBinsPhi, viewPointPtheta(0:20) and viewPointPphi(0:20) of initCartesianGrid
+    (source/grid_mod.f90:570-601): 20 theta bins over [0, pi], 20 phi bins over [0, 2 pi), or one
+    phi bin when a view's phi is negative (every view's phi is then taken as -1)."""
+    pi = 3.141592654
+    tot_phi = 20
+    phi = [float(phi[k]) for k in range(n_angle)]
+    if any(v < 0 for v in phi):
+        tot_phi, phi = 1, [-1.0] * n_angle
+    d_theta, d_phi = pi / 20, 2 * pi / tot_phi
+    pt, pp = [0] * 21, [0] * 21
+    for k in range(n_angle):
+        pt[int(float(theta[k]) / d_theta) + 1] = k + 1
+        pp[int(phi[k] / d_phi) + 1] = k + 1
+    return tot_phi, pt, pp
 
 
 class TransportOut(C.Structure):
@@ -237,8 +255,12 @@ def transport(setup, opacity_arr, rec_pdf, total_lines, ne=None, n: int = 1000, 
                     delta_e=float(np.float32(i.l_star)) / norm)
     s.star_pos[:] = list(i.star_pos)
     s.star_idx[:] = list(i.star_idx)
+    s.n_angle = i.n_angle_bins
+    s.tot_phi, pt, pp = view_bins(i.n_angle_bins, i.view_theta, i.view_phi)
+    s.view_p_theta[:] = pt
+    s.view_p_phi[:] = pp
     j = np.zeros((nb, C1), dtype=np.float64)
-    e = np.zeros((nb + 1, C1), dtype=np.float64)
+    e = np.zeros((nb + 1, C1) if i.n_angle_bins == 0 else (i.n_angle_bins + 1, nb + 1, C1), dtype=np.float64)
     o = TransportOut(jste=_p(j), escaped=_p(e), h_est=None)
     st = TransportStats()
     rc = lib().orc_transport(C.byref(s), seed, counter_base, n, nthreads, C.byref(o), C.byref(st))

@@ -59,11 +59,15 @@ typedef struct orc_transport_in {
     float star_pos[3];
     int32_t star_idx[3];        /* 1-based */
     double delta_e;             /* Lstar/nPhotons */
+    int32_t n_angle;            /* nAngleBins (0: escapes into plane 0 only)           */
+    int32_t tot_phi;            /* totAngleBinsPhi                                     */
+    int32_t view_p_theta[21];   /* viewPointPtheta(0:20)                               */
+    int32_t view_p_phi[21];     /* viewPointPphi(0:tot_phi)                            */
 } orc_transport_in;
 
 typedef struct orc_transport_out {
     double* jste;               /* [nbins][C+1], accumulated (not cleared) */
-    double* escaped;            /* [nbins+1][C+1], accumulated */
+    double* escaped;            /* [n_angle+1][nbins+1][C+1], accumulated */
     double* h_est;              /* [nbins][C+1] or NULL */
 } orc_transport_out;
 

@@ -97,6 +97,8 @@ typedef struct {
  * the chunks it deposits into, so the merge visits only those */
 #define JCHUNK 512
 
+#define R_PI 3.141592654     /* pi of source/constants_mod.f90 */
+
 typedef struct {
     const orc_transport_in* in;
     double* jste;
@@ -184,9 +186,29 @@ static void init_packet(tctx_t* c, packet_t* p, int nuP, vec3 pos, int lgLine, i
     else p->origin = 0;
 }
 
+/* the escape tally (source/photon_mod.f90:2293-2378): plane 0 of
+ * escapedPackets, and with viewing angles the plane of the view whose theta
+ * and phi bins hold the escape direction; viewPointPtheta == viewPointPphi
+ * == 0 (a direction in no view) passes the reference's test as view 0 */
 static void escape_tally(tctx_t* c, const packet_t* p) {
+    const orc_transport_in* in = c->in;
     const size_t idx = (size_t)p->origin + c->C1 * (size_t)p->nuP;
-    c->escaped[idx] += c->in->delta_e;
+    if (in->n_angle > 0) {
+        const size_t plane = c->C1 * (size_t)(in->nbins + 1);
+        const double dTheta = R_PI / 20., dPhi = (2. * R_PI) / (double)in->tot_phi;
+        int idirT = (int)(acos(p->dir.z) / dTheta) + 1;
+        if (idirT > 20) idirT = 20;
+        int idirP = p->dir.x < 1.e-35 ? 0 : (int)(atan(p->dir.y / p->dir.x) / dPhi);
+        if (idirP < 0) idirP = in->tot_phi + idirP;
+        idirP = idirP + 1;
+        if (idirP > in->tot_phi) idirP = in->tot_phi;
+        const int k = in->view_p_theta[idirT];
+        if ((in->tot_phi > 1 && k == in->view_p_phi[idirP]) || (in->tot_phi == 1 && k > 0)) {
+            c->escaped[plane * (size_t)k + idx] += in->delta_e;
+            c->touched_e[(plane * (size_t)k + idx) / JCHUNK] = 1;
+        }
+    }
+    c->escaped[idx] += in->delta_e;
     c->touched_e[idx / JCHUNK] = 1;
     c->st.escaped++;
 }
@@ -581,7 +603,7 @@ int orc_transport(const orc_transport_in* in, uint64_t seed, uint64_t counter_ba
     if (!in || !out || !out->jste || !out->escaped || n < 0) return 2;
     if (in->star_idx[0] < 1 || in->star_idx[1] < 1 || in->star_idx[2] < 1) return 2;
     const size_t C1 = (size_t)in->n_cells + 1;
-    const size_t nj = C1 * (size_t)in->nbins, ne = C1 * (size_t)(in->nbins + 1);
+    const size_t nj = C1 * (size_t)in->nbins, ne = C1 * (size_t)(in->nbins + 1) * (size_t)(in->n_angle + 1);
     if (nthreads < 1) nthreads = 1;
     if (nthreads > MAX_POOL) nthreads = MAX_POOL;
     if ((int64_t)nthreads > n) nthreads = n > 0 ? (int32_t)n : 1;

@@ -122,3 +122,35 @@ def test_block_shapes_give_identical_results(decks, data_dir, oracle_lib):
     j2 = ctx.get(abi.ARR_JSTE)
     np.testing.assert_array_equal(j2, j1)
     ctx.close()
+
+
+@pytest.mark.parametrize("views", ["2 0.5 1.0 2.0 5.5", "2 0.8 -1 2.2 -1"])
+def test_viewing_angle_planes_match_oracle(tmp_path, data_dir, oracle_lib, views):
+    """Escapes binned into the viewing-angle planes of escapedPackets
+    (source/photon_mod.f90:2293-2378), FP64 path against the oracle: the
+    same totals per plane (a packet on a bin boundary may land one bin over
+    on either side, so to a few deltaE), plane 0 included.  The reference's
+    phi = atan(vy / vx) spans (-pi/2, pi/2) only, so the views take phi bins
+    it reaches (1.0 and 5.5 rad)."""
+    deck = configs.lognormal_gas(tmp_path / "ln", n=13, packets=20000, half_width=1.5e19)
+    deck.write_text(deck.read_text() + f"inclination {views}\n")
+    s = Setup(deck, data_dir)
+    op = oracle_lib.opacity(s)
+    rec = synthetic_recpdf(s.get(abi.ARR_NU), s.n_cells)
+    tl = np.full(s.n_cells + 1, 0.3, np.float32)
+    ctx = Context(0)
+    ctx.load(s)
+    ctx.put(abi.ARR_OPACITY, op)
+    ctx.put(abi.ARR_RECPDF, rec)
+    ctx.put(abi.ARR_TOTAL_LINES, tl)
+    n = 40000
+    st = ctx.transport(n, seed=5, precision=abi.PREC_FP64)
+    esc = ctx.get(abi.ARR_ESCAPED)
+    assert esc.shape == (3, s.nbins + 1, s.n_cells + 1)
+    jo, eo, so = oracle_lib.transport(s, op, rec, tl, n=n, seed=5, nthreads=4)
+    de = float(np.float32(s.info.l_star)) / n
+    assert st.escaped == so.escaped
+    for k in range(3):
+        assert esc[k].sum() == pytest.approx(eo[k].sum(), abs=4 * de), k
+    assert esc[1].sum() > 0 and esc[2].sum() > 0
+    ctx.close()
