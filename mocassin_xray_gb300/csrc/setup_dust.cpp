@@ -4,12 +4,14 @@
 //                    frequency mesh, cross sections pi a^2 Q)
 //   dustEmissionInt  source/dust_mod.f90:141-184 (emission integral of every
 //                    species and size for T = 1..nTemps K)
-// Files of the 'nk' type (optical constants, which need a Mie calculation)
-// are rejected.
+//   getQs            source/ph_mod.f90:1601-1650 ('nk'-type files: optical
+//                    constants, the efficiencies of every size and bin from a
+//                    Mie calculation or geometric optics)
 #include "list_reader.h"
 #include "setup_internal.h"
 
 #include <cmath>
+#include <complex>
 #include <fstream>
 #include <sstream>
 #include <stdexcept>
@@ -81,6 +83,123 @@ float blackbodyFlux(float energy, float temperature) {
   return constant * energy * energy * energy / denominator;
 }
 
+// Extinction, scattering and backscattering efficiencies of a homogeneous
+// sphere of size parameter x and complex refractive index m: the series of
+// Mie coefficients a_n, b_n as organised by Bohren & Huffman (1983,
+// Absorption and Scattering of Light by Small Particles, appendix A):
+// D_n(mx) = d/dz ln psi_n(z) by downward recurrence from n = max(nstop,
+// |mx|) + 15, the Riccati-Bessel functions psi_n and chi_n of x by upward
+// recurrence, summed to nstop = x + 4 x^(1/3) + 2 terms.
+void mieEfficiencies(double x, std::complex<double> m, double& qext, double& qsca, double& qback) {
+  using cd = std::complex<double>;
+  const cd y = m * x;
+  const double xstop = x + 4.0 * std::cbrt(x) + 2.0;
+  const int nstop = (int)xstop;
+  const int nmx = (int)std::max(xstop, std::abs(y)) + 15;
+  std::vector<cd> D((size_t)nmx + 1, cd(0., 0.));
+  for (int n = nmx; n >= 1; --n) {
+    const double en = n;
+    D[(size_t)n - 1] = en / y - 1.0 / (D[(size_t)n] + en / y);
+  }
+  double psi0 = std::cos(x), psi1 = std::sin(x);
+  double chi0 = -std::sin(x), chi1 = std::cos(x);
+  cd xi1(psi1, -chi1);
+  double sumExt = 0., sumSca = 0.;
+  cd sumBack(0., 0.);
+  double sign = -1.;
+  for (int n = 1; n <= nstop; ++n) {
+    const double en = n, fn = 2. * en + 1.;
+    const double psi = (2. * en - 1.) * psi1 / x - psi0;
+    const double chi = (2. * en - 1.) * chi1 / x - chi0;
+    const cd xi(psi, -chi);
+    const cd da = D[(size_t)n] / m + en / x, db = m * D[(size_t)n] + en / x;
+    const cd an = (da * psi - psi1) / (da * xi - xi1);
+    const cd bn = (db * psi - psi1) / (db * xi - xi1);
+    sumSca += fn * (std::norm(an) + std::norm(bn));
+    sumExt += fn * (an.real() + bn.real());
+    sumBack += fn * sign * (an - bn);
+    sign = -sign;
+    psi0 = psi1; psi1 = psi;
+    chi0 = chi1; chi1 = chi;
+    xi1 = cd(psi1, -chi1);
+  }
+  qsca = 2. / (x * x) * sumSca;
+  qext = 2. / (x * x) * sumExt;
+  qback = std::norm(sumBack) / (x * x);
+}
+
+// geometricOptics (source/ph_mod.f90:1700-1750): absorption by a sphere much
+// larger than the wavelength, from the Fresnel reflectivities over 45
+// incidence angles, and scattering from the Rayleigh-Gans efficiency
+// saturated as Qrg / sqrt(1 + Qrg^2 / 4), minus the absorption.  The
+// reference reads the refraction angle psi before the first angle sets it
+// (taken as 0 here) and takes 1/m's permittivity as (epsre, -epsre) / |eps|^2.
+void geometricOptics(float x, float a, float mre, float mim, float lambda, float& qa, float& qs) {
+  const float pi = 3.141592654f;
+  const float absmm1sq = (mre - 1.f) * (mre - 1.f) + mim * mim;
+  const float epsre = mre * mre - mim * mim, epsim = mre * mim;
+  const float epsrem1 = epsre / (epsre * epsre + epsim * epsim);
+  const float epsimm1 = -(epsre / (epsre * epsre + epsim * epsim));
+  qa = 0.f;
+  float psi = 0.f;
+  for (int i = 1; i <= 45; ++i) {
+    const float t0 = (float)i * pi / 180.f, s0 = std::sin(t0), c0 = std::cos(t0);
+    const float p20 = 0.5f * (s0 * s0 - epsre + std::sqrt((2.f * epsim) * (2.f * epsim) + (epsre - s0 * s0)));
+    const float q20 = 0.5f * (-s0 * s0 + epsre + std::sqrt((2.f * epsim) * (2.f * epsim) + (epsre - s0 * s0)));
+    const float sp = std::sin(psi);
+    const float p21 = 0.5f * (sp * sp - epsrem1 + std::sqrt((2.f * epsimm1) * (2.f * epsimm1) + (epsrem1 - sp * sp)));
+    const float q21 = 0.5f * (-sp * sp + epsrem1 + std::sqrt((2.f * epsimm1) * (2.f * epsimm1) + (epsrem1 - sp * sp)));
+    const float rq20 = std::sqrt(q20);
+    const float rperp0 = ((rq20 - c0) * (rq20 - c0) + p20) / ((rq20 + c0) * (rq20 + c0) + p20);
+    const float rpara0 = rperp0 * ((rq20 - s0 * std::tan(t0)) * (rq20 - s0 * std::tan(t0)) + p20) /
+                         ((rq20 + s0 * std::tan(t0)) * (rq20 + s0 * std::tan(t0)) + p20);
+    psi = std::asin(s0 / ((q20 + s0 * s0) * (q20 + s0 * s0)));
+    const float sps = std::sin(psi), cps = std::cos(psi), rq21 = std::sqrt(q21);
+    const float rperp1 = ((rq21 - cps) * (rq21 - cps) + p21) / ((rq21 + cps) * (rq21 + cps) + p21);
+    const float rpara1 = rperp1 * ((rq21 - sps * std::tan(psi)) * (rq21 - sps * std::tan(psi)) + p21) /
+                         ((rq21 + sps * std::tan(psi)) * (rq21 + sps * std::tan(psi)) + p21);
+    const float at = std::exp(-8.f * pi * a * mim * cps / lambda);
+    qa = qa + s0 * c0 * (pi / 180.f) * (1.f - at) *
+                  ((1.f - rperp0) / (1.f - at * rperp1) + (1.f - rpara0) / (1.f - at * rpara1));
+  }
+  const float qrg = (32.f * absmm1sq * x * x * x * x) / (27.f + 16.f * x * x) + (8.f / 3.f) * mim * x;
+  qs = qrg / std::sqrt(1.f + 0.25f * qrg * qrg) - qa;
+}
+
+// getQs (source/ph_mod.f90:1601-1650): absorption and scattering efficiencies
+// of every grain size in every frequency bin from the refractive index
+// mapped onto the mesh.  Mie below |m| x = 1000 (x capped at 100), the
+// Rayleigh-Gans limit when also |m - 1| x < 1e-3, geometric optics above.
+void efficienciesFromIndex(const Setup& s, const std::vector<float>& ere, const std::vector<float>& eim,
+                           float* qabs, float* qsca) {
+  const DustTables& d = s.dust;
+  const int nb = s.nbins;
+  for (int i = 0; i < nb; ++i) {
+    const float absM = std::sqrt(ere[i] * ere[i] + eim[i] * eim[i]);
+    const float absMm1 = std::sqrt((ere[i] - 1.f) * (ere[i] - 1.f) + eim[i] * eim[i]);
+    const float lam = 2.9979250e14f / (s.nu[i] * kFr1Ryd);
+    for (int ai = 0; ai < d.nSizes; ++ai) {
+      float x = 2.0f * 3.14159265f * d.grainRadius[ai] / lam;
+      float qa, qs;
+      if (absM * x < 1000.f) {
+        if (x > 100.f) x = 100.f;
+        double qe, qsc, qb;
+        mieEfficiencies((double)x, std::complex<double>(ere[i], eim[i]), qe, qsc, qb);
+        qa = (float)(qe - qsc);
+        qs = (float)qsc;
+      } else if (absMm1 * x < 0.001f) {
+        qa = (8.f / 3.f) * eim[i] * x;
+        qs = 32.f * absMm1 * absMm1 * x * x * x * x / (27.f + 16.f * x * x);
+      } else {
+        geometricOptics(x, d.grainRadius[ai], ere[i], eim[i], lam, qa, qs);
+      }
+      if (!s.p.lgDustScattering) qs = 0.f;
+      qabs[(size_t)ai * nb + i] = qa;
+      qsca[(size_t)ai * nb + i] = qs;
+    }
+  }
+}
+
 void buildDustTables(Setup& s) {
   DustTables& d = s.dust;
   const int nb = s.nbins;
@@ -129,9 +248,36 @@ void buildDustTables(Setup& s) {
     ListReader q(qfile);
     auto head = tokensOf(q.record());
     if (head.empty()) dfail("makeDustXsec: empty extinction file " + qfile);
-    if (head[0] == "nk")
-      dfail("makeDustXsec: 'nk' optical-constant files need a Mie calculation, outside this library's scope (" +
-            qfile + "); use 'Q' efficiency files");
+    if (head[0] == "nk") {
+      // makeDustXsec's 'nk' branch (source/ph_mod.f90:1088-1230): label line, then
+      // wavelength [um], n, k per record, wavelengths ascending
+      auto lab = tokensOf(q.record());
+      if (lab.size() < 5) dfail("makeDustXsec: species header of " + qfile + " needs label, Tsub, rho, Vn, Msurf");
+      d.grainLabel[n] = lab[0];
+      d.TdustSublime[n] = (float)num(lab[1], qfile);
+      std::vector<float> wav, re, im;
+      std::vector<double> v;
+      while (!q.eof()) {
+        const int got = q.readRecord(3, v);
+        if (got < 0) break;
+        if (v.size() < 3) continue;
+        wav.push_back((float)v[0]); re.push_back((float)v[1]); im.push_back((float)v[2]);
+      }
+      const int nWav = (int)wav.size();
+      if (nWav < 2) dfail("makeDustXsec: no optical constants in " + qfile);
+      // wavelength [um] to energy [Ryd], reversed into ascending energy
+      std::vector<float> e(nWav), r(nWav), k(nWav);
+      for (int i = 0; i < nWav; ++i) {
+        e[nWav - 1 - i] = kC / (wav[i] * kFr1Ryd * 1.e-4f);
+        r[nWav - 1 - i] = re[i];
+        k[nWav - 1 - i] = im[i];
+      }
+      std::vector<float> ere(nb), eim(nb);
+      linearMap(r, e, nu, nb, ere.data());
+      linearMap(k, e, nu, nb, eim.data());
+      efficienciesFromIndex(s, ere, eim, &d.Cabs[(size_t)n * per], &d.Csca[(size_t)n * per]);
+      continue;
+    }
     if (head[0] != "Q") dfail("makeDustXsec: invalid dustFileType in " + qfile);
     auto lab = tokensOf(q.record());
     if (lab.size() < 5) dfail("makeDustXsec: species header of " + qfile + " needs label, Tsub, rho, Vn, Msurf");

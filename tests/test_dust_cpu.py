@@ -108,11 +108,12 @@ def test_emission_integral(dust):
         assert em[1, 3, int(T) - 1] == pytest.approx(ref, rel=2e-4)
 
 
-def test_nk_files_rejected(tmp_path, dust, data_dir):
+def test_nk_file_without_constants_rejected(tmp_path, dust, data_dir):
+    """An 'nk' file needs at least two (wavelength, n, k) records to interpolate."""
     deck, _ = dust
     bad = tmp_path / "run"
     import shutil
     shutil.copytree(deck.parent.parent, bad)
     (bad / "input" / "Sil_syn.Q").write_text("nk\n Ssil 1400. 3.6 0.588 20.077\n1.0 1.5 0.1\n")
-    with pytest.raises(abi.McxError, match="Mie"):
+    with pytest.raises(abi.McxError, match="no optical constants"):
         Setup(bad / "input" / "input.in", data_dir)
