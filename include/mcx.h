@@ -359,7 +359,10 @@ typedef struct mcx_transport_opts {
     int32_t chunk;              /* packets handed out per queue grab; 0 = default       */
     int32_t emit_batch;         /* lanes of a warp that wait for an emission before the
                                    warp runs the emission code; 0 = library default (12) */
-    int32_t reserved[3];
+    int32_t handoff_emissions;  /* re-emissions after which a history is continued by the
+                                   trapped-packet kernel; 0 = library default (256),
+                                   -1 = never (every history stays in the main kernel) */
+    int32_t reserved[2];
 } mcx_transport_opts;
 
 typedef struct mcx_transport_stats {
@@ -372,9 +375,10 @@ typedef struct mcx_transport_stats {
     int64_t trapped;            /* histories that hit recursionLimit / safeLimit              */
     int64_t emissions;          /* frequency draws from a CDF (source + re-emission)          */
     double  q_phot;             /* Qphot (e36 photons/s above 1 Ryd emitted by the source)    */
-    float   kernel_ms;          /* CUDA-event time of the transport kernel                    */
+    float   kernel_ms;          /* CUDA-event time of the transport kernels                   */
     float   reserved_f[3];
-    int64_t reserved[4];
+    int64_t handed_off;         /* histories continued by the trapped-packet kernel          */
+    int64_t reserved[3];
 } mcx_transport_stats;
 
 int  mcx_transport(mcx_ctx* ctx, const mcx_transport_opts* opts, mcx_transport_stats* stats);

@@ -1,8 +1,9 @@
 """Builds libmcx.so (the CUDA hot path for sm_103a) in-tree.
 
 Every translation unit is compiled in parallel with one -gencode for
-sm_103a; the FP64 transport and balance code is compiled with --fmad=false
-so that its arithmetic rounds operation by operation.
+sm_103a; the transport (both precisions) and the FP64 balance code are
+compiled with --fmad=false so that their arithmetic rounds operation by
+operation.
 """
 from __future__ import annotations
 
@@ -49,7 +50,10 @@ def build_lib(verbose: bool = False) -> Path:
         ("k_emission.cu", []),
         ("mcx_api.cu", []),
         ("k_opacity.cu", []),
-        ("k_transport_f32.cu", []),
+        # no FMA contraction in the FP32 geometry either: the persistent and the
+        # trapped-packet kernels inline the same step code in different contexts,
+        # and must round every operation the same way to follow the same histories
+        ("k_transport_f32.cu", ["--fmad=false"]),
         ("k_transport_f64.cu", ["--fmad=false"]),
         ("k_balance.cu", []),
         ("k_balance_f64.cu", ["--fmad=false"]),

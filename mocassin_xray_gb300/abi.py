@@ -94,14 +94,14 @@ class TransportOpts(C.Structure):
     _fields_ = [("istar", C.c_int32), ("precision", C.c_int32), ("n_packets", C.c_int64), ("seed", C.c_uint64),
                 ("counter_base", C.c_uint64), ("n_photons_norm", C.c_int64), ("zero_estimators", C.c_int32),
                 ("block_size", C.c_int32), ("grid_mult", C.c_int32), ("chunk", C.c_int32),
-                ("emit_batch", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("emit_batch", C.c_int32), ("handoff_emissions", C.c_int32), ("reserved", C.c_int32 * 2)]
 
 
 class TransportStats(C.Structure):
     _fields_ = [("crossings", C.c_int64), ("interactions", C.c_int64), ("absorptions", C.c_int64),
                 ("scatterings", C.c_int64), ("escaped", C.c_int64), ("line_escapes", C.c_int64),
                 ("trapped", C.c_int64), ("emissions", C.c_int64), ("q_phot", C.c_double), ("kernel_ms", C.c_float),
-                ("reserved_f", C.c_float * 3), ("reserved", C.c_int64 * 4)]
+                ("reserved_f", C.c_float * 3), ("handed_off", C.c_int64), ("reserved", C.c_int64 * 3)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("reserved")}

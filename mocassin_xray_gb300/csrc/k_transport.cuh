@@ -25,6 +25,7 @@
 // Jste(0,:), the dump row the reference fills for inactive cells and never
 // reads, is not accumulated.
 #pragma once
+#include "k_transport_launch.h"
 #include "mcx_device.cuh"
 #include "mcx_fmath.h"
 
@@ -61,12 +62,70 @@ template <> struct RMath<double> {
 
 template <typename R>
 struct Packet {
+  using Real = R;
+  static constexpr bool kWarp = false;   // one lane per history
   R x, y, z, vx, vy, vz;
   R nu, absTau, passProb;
   int xP, yP, zP, nuP, origin;
   int type, lgStellar, nEmit, nStep;
   PacketRng rng;
 };
+
+// A history run by a whole warp (the trapped-packet kernel): every lane holds
+// the same state and executes the same scalar arithmetic, so every lane
+// computes the same values; the lanes split only the data-parallel parts.
+// Here the Philox stream: lane l keeps block blk0 + l (4 draws), so one
+// refill covers the next 128 draws and a draw is a select and a shuffle.  The
+// draws are those of PacketRng, position for position.
+struct WarpRng {
+  uint32_t k0, k1, p0, p1;
+  uint32_t k;              // draws taken so far
+  uint32_t blk0;           // first Philox block held by the warp
+  uint32_t b0, b1, b2, b3; // this lane's block, blk0 + lane
+  // out of line: inlined at every draw site it would fill the instruction
+  // cache with copies of Philox that run once per 128 draws
+  __device__ __noinline__ void fill(uint32_t first) {
+    uint32_t o[4];
+    blk0 = first;
+    philox4x32_10(p0, p1, first + (threadIdx.x & 31u), 0u, k0, k1, o);
+    b0 = o[0]; b1 = o[1]; b2 = o[2]; b3 = o[3];
+  }
+  __device__ __forceinline__ void start(const PacketRng& r) {
+    k0 = r.k0; k1 = r.k1; p0 = r.p0; p1 = r.p1; k = r.k;
+    fill(k >> 2);
+  }
+  __device__ __forceinline__ uint32_t next() {
+    const uint32_t blk = k >> 2;
+    if (blk - blk0 >= 32u) fill(blk);
+    const uint32_t sel = k & 3u;
+    const uint32_t mine = sel == 0u ? b0 : (sel == 1u ? b1 : (sel == 2u ? b2 : b3));
+    ++k;
+    return __shfl_sync(0xffffffffu, mine, (int)(blk - blk0));
+  }
+};
+
+template <typename R>
+struct WarpPacket {
+  using Real = R;
+  static constexpr bool kWarp = true;
+  R x, y, z, vx, vy, vz;
+  R nu, absTau, passProb;
+  int xP, yP, zP, nuP, origin;
+  int type, lgStellar, nEmit, nStep;
+  WarpRng rng;
+  __device__ __forceinline__ void from(const Packet<R>& a) {
+    x = a.x; y = a.y; z = a.z; vx = a.vx; vy = a.vy; vz = a.vz;
+    nu = a.nu; absTau = a.absTau; passProb = a.passProb;
+    xP = a.xP; yP = a.yP; zP = a.zP; nuP = a.nuP; origin = a.origin;
+    type = a.type; lgStellar = a.lgStellar; nEmit = a.nEmit; nStep = a.nStep;
+    rng.start(a.rng);
+  }
+};
+
+// Whether this lane performs the history's side effects (atomics): every lane
+// of a one-lane history, lane 0 of a warp history.
+template <typename P>
+__device__ __forceinline__ bool effectLane() { return !P::kWarp || (threadIdx.x & 31u) == 0u; }
 
 // Shared memory of a transport block after its tables: each thread's packet
 // state (one Packet per thread; its address goes to the out-of-line emission
@@ -104,6 +163,7 @@ struct OneGrid {
   __device__ __forceinline__ const float* Y() const { return sY; }
   __device__ __forceinline__ const float* Z() const { return sZ; }
   __device__ __forceinline__ const int32_t* active() const { return g.active; }
+  __device__ __forceinline__ bool activeFull() const { return g.activeFull != 0; }
   __device__ __forceinline__ const float* cdf() const { return sCdf; }
   __device__ __forceinline__ int starIdx(int d) const { return g.starIdx[d]; }
   __device__ __forceinline__ float starPos(int d) const { return g.starPos[d]; }
@@ -126,6 +186,7 @@ struct NebulaGeo {
   __device__ __forceinline__ const float* Y() const { return Y_; }
   __device__ __forceinline__ const float* Z() const { return Z_; }
   __device__ __forceinline__ const int32_t* active() const { return active_; }
+  __device__ __forceinline__ bool activeFull() const { return false; }
   __device__ __forceinline__ const float* cdf() const { return cdf_; }
   __device__ __forceinline__ int starIdx(int d) const { return starIdx_[d]; }
   __device__ __forceinline__ float starPos(int d) const { return starPos_[d]; }
@@ -133,7 +194,26 @@ struct NebulaGeo {
 
 template <typename Geo>
 __device__ __forceinline__ int activeAt(const Geo& q, int i, int j, int k) {
+  if (q.activeFull()) return ((i - 1) * q.ny() + (j - 1)) * q.nz() + k;
   return __ldg(q.active() + (size_t)(i - 1) + (size_t)q.nx() * ((size_t)(j - 1) + (size_t)q.ny() * (size_t)(k - 1)));
+}
+
+// Packets re-emitted this many times are taken to be trapped in optically thick
+// cells: their lane runs on, often alone in its warp, long after the others
+// are done, so each dependent global load of its events is paid in full.  For
+// these lanes the emission prefetches the cell's whole CDF row into L1 before
+// the bisection, and the step prefetches the scattering inputs with the
+// opacity.  Prefetches change no value read, only when it arrives.
+constexpr int kTrappedHint = 8;
+
+__device__ __forceinline__ void prefetchL1(const void* a) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(a));
+}
+
+// every 128-byte line of the n floats at row
+__device__ __forceinline__ void prefetchRowL1(const float* row, int n) {
+  for (int i = 0; i < n; i += 32) prefetchL1(row + i);
+  prefetchL1(row + (n - 1));
 }
 
 // getNu2 on a monotone CDF: the reference's linear scan "last i with u >= cdf(i)"
@@ -150,14 +230,50 @@ __device__ __forceinline__ int sampleCDF(const float* cdf, int len, int nbins, R
   return nuP;
 }
 
+// sampleCDF's count for a warp history, the 32 lanes comparing in parallel:
+// first the last entry of each of up to 32 segments (issued by warpCdfIssue
+// as soon as the row is known, before u is drawn), then the entries of the
+// one segment that holds the answer.  On a monotone row the count of entries
+// <= u does not depend on the order of the comparisons, so the result equals
+// the bisection's.
+struct WarpCdf {
+  float v;          // this lane's segment end
+  int seg, segs;    // segment length (a multiple of 32) and segments probed
+};
+
+__device__ __forceinline__ void warpCdfIssue(WarpCdf& c, const float* __restrict__ row, int m) {
+  const int lane = threadIdx.x & 31;
+  c.seg = 32 * ((m + 1023) / 1024);
+  c.segs = m / c.seg;
+  c.v = lane < c.segs ? __ldg(row + (size_t)(lane + 1) * c.seg - 1) : 0.f;
+}
+
 template <typename R>
-__device__ __forceinline__ R draw(Packet<R>& p) { return uniformFrom<R>(p.rng.next()); }
+__device__ __forceinline__ int warpCdfFinish(const WarpCdf& c, const float* __restrict__ row, int m, int nbins, R u) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int s = __popc(__ballot_sync(FULL, lane < c.segs && u >= (R)c.v));
+  const int base = s * c.seg;
+  const int end = base + c.seg < m ? base + c.seg : m;
+  int lo = base;
+  for (int b = base; b < end; b += 32) {
+    const bool in = b + lane < end;
+    const float w = in ? __ldg(row + b + lane) : 0.f;
+    lo += __popc(__ballot_sync(FULL, in && u >= (R)w));
+  }
+  int nuP = lo < 1 ? 1 : lo;
+  if (nuP < nbins) ++nuP;
+  return nuP;
+}
+
+template <typename P>
+__device__ __forceinline__ typename P::Real draw(P& p) { return uniformFrom<typename P::Real>(p.rng.next()); }
 
 // initPhotonPacket (source/photon_mod.f90:744-896): position, frequency, an
 // isotropic direction (re-drawn while a component is exactly zero) and the
 // octant fold for stellar packets.
-template <typename R, typename Geo>
-__device__ __forceinline__ void initPacket(const Geo& q, const TransportShared<R>& sh, Packet<R>& p, int nuP,
+template <typename R, typename Geo, typename P>
+__device__ __forceinline__ void initPacket(const Geo& q, const TransportShared<R>& sh, P& p, int nuP,
                                            bool line, bool stellar, int xP, int yP, int zP) {
   using M = RMath<R>;
   p.nuP = nuP;
@@ -191,9 +307,11 @@ __device__ __forceinline__ void initPacket(const Geo& q, const TransportShared<R
 // bins have viewPointPtheta = viewPointPphi = 0, which the reference's test
 // counts as a match of view 0, adding deltaE to plane 0 a second time; both
 // are reproduced.
-template <typename R>
-__device__ __forceinline__ void escapeTally(const DevGrid& g, const DevTransportOut& out, const Packet<R>& p,
+template <typename R, typename P>
+__device__ __forceinline__ void escapeTally(const DevGrid& g, const DevTransportOut& out, const P& p,
                                             double deltaE, LocalCounters& lc) {
+  ++lc.escaped;
+  if (!effectLane<P>()) return;
   const size_t plane = ((size_t)g.nCells + 1) * ((size_t)g.nbins + 1);
   const size_t at = (size_t)p.origin + ((size_t)g.nCells + 1) * (size_t)p.nuP;
   if (g.nAngle > 0) {
@@ -211,7 +329,6 @@ __device__ __forceinline__ void escapeTally(const DevGrid& g, const DevTransport
       atomicAdd(out.escaped + plane * (size_t)k + at, deltaE);
   }
   atomicAdd(out.escaped + at, deltaE);
-  ++lc.escaped;
 }
 
 // A J deposit whose rounding error is still to be added to Jlo.  The FP64
@@ -232,10 +349,10 @@ __device__ __forceinline__ void flushJ(const DevTransportOut& out, PendingJ& pj)
   }
 }
 
-template <typename R>
+template <typename R, bool kWarp>
 __device__ __forceinline__ void deposit(const DevGrid& g, const DevTransportOut& out, int cell, int nuP, R dl,
                                         R dV, R deltaE, R costheta, PendingJ& pj) {
-  if (cell <= 0) return;
+  if (cell <= 0 || (kWarp && (threadIdx.x & 31u) != 0u)) return;
   size_t idx = (size_t)cell + ((size_t)g.nCells + 1) * (size_t)(nuP - 1);
   const double v = (double)RMath<R>::div_(dl * deltaE, dV);
   if (out.jlo) {
@@ -267,8 +384,8 @@ __device__ __forceinline__ int locateNu(const float* xa, int n, R x) {
 }
 
 // comptonScatter (source/photon_mod.f90:6805-6848)
-template <typename R>
-__device__ __forceinline__ void comptonScatter(const DevGrid& g, const TransportShared<R>& sh, Packet<R>& p) {
+template <typename R, typename P>
+__device__ __forceinline__ void comptonScatter(const DevGrid& g, const TransportShared<R>& sh, P& p) {
   using M = RMath<R>;
   const float* row = g.KNcdfT + (size_t)(p.nuP - 1) * 180;
   int th = sampleCDF<R>(row, 180, g.nbins, draw(p));
@@ -296,9 +413,11 @@ template <> __device__ __forceinline__ double cellVolume<double>(const DevGrid& 
 // at (p.x,p.y,p.z; p.xP,p.yP,p.zP).  Returns the next state.  Kept out of line:
 // with the step code inlined beside it the loop body overflows the
 // instruction cache (measured: 11.9 -> 9.5 ms for 1e7 packets at 41^3).
-template <typename R, typename Geo>
-__device__ __noinline__ int emitPacket(const DevGrid& g, const Geo& q, const DevTransportIn& in, const DevTransportOut& out,
-                          const TransportShared<R>& sh, Packet<R>& p, double deltaE, LocalCounters& lc) {
+// For a warp history (P::kWarp) the re-emission CDF search is the warp's,
+// its first round issued before the line draw; the same draws, the same result.
+template <typename R, typename Geo, typename P>
+__device__ __forceinline__ int emitBody(const DevGrid& g, const Geo& q, const DevTransportIn& in, const DevTransportOut& out,
+                                        const TransportShared<R>& sh, P& p, double deltaE, LocalCounters& lc) {
   using M = RMath<R>;
   if (p.nEmit >= kRecursionLimit) { ++lc.trapped; return ST_IDLE; }
   ++p.nEmit;
@@ -313,18 +432,27 @@ __device__ __noinline__ int emitPacket(const DevGrid& g, const Geo& q, const Dev
     if (p.xP < 1 || p.xP > q.nx() || p.yP < 1 || p.yP > q.ny() || p.zP < 1 || p.zP > q.nz()) { ++lc.errors; return ST_IDLE; }
     int cell = activeAt(q, p.xP, p.yP, p.zP);
     if (cell <= 0) { ++lc.errors; return ST_IDLE; }
+    const float* cdfTab = p.type == PT_DIFFUSE ? in.recCDFT : in.dustCDFT;
+    const float* row = cdfTab ? cdfTab + (size_t)cell * g.nbins : nullptr;
+    WarpCdf wc;
+    if constexpr (P::kWarp) { if (row) warpCdfIssue(wc, row, g.nbins); }
+    else if (p.nEmit > kTrappedHint && row) prefetchRowL1(row, g.nbins);
+    auto sample = [&](R u) {
+      if constexpr (P::kWarp) return warpCdfFinish<R>(wc, row, g.nbins, g.nbins, u);
+      else return sampleCDF<R>(row, g.nbins, g.nbins, u);
+    };
     if (p.type == PT_DIFFUSE) {
       R rnd = R(1) - draw(p);
       if (rnd <= (R)__ldg(in.totalLines + cell)) {
         initPacket<R>(q, sh, p, 0, true, false, p.xP, p.yP, p.zP);
         line = true;
       } else {
-        int nuP = sampleCDF<R>(in.recCDFT + (size_t)cell * g.nbins, g.nbins, g.nbins, draw(p));
+        int nuP = sample(draw(p));
         ++lc.emissions;
         initPacket<R>(q, sh, p, nuP, false, false, p.xP, p.yP, p.zP);
       }
     } else {
-      int nuP = sampleCDF<R>(in.dustCDFT + (size_t)cell * g.nbins, g.nbins, g.nbins, draw(p));
+      int nuP = sample(draw(p));
       ++lc.emissions;
       initPacket<R>(q, sh, p, nuP, false, false, p.xP, p.yP, p.zP);
     }
@@ -347,10 +475,16 @@ __device__ __noinline__ int emitPacket(const DevGrid& g, const Geo& q, const Dev
   return ST_STEP;
 }
 
-// One iteration of pathSegment's main loop (source/photon_mod.f90:1880-4036).
 template <typename R, typename Geo>
+__device__ __noinline__ int emitPacket(const DevGrid& g, const Geo& q, const DevTransportIn& in, const DevTransportOut& out,
+                                       const TransportShared<R>& sh, Packet<R>& p, double deltaE, LocalCounters& lc) {
+  return emitBody<R, Geo>(g, q, in, out, sh, p, deltaE, lc);
+}
+
+// One iteration of pathSegment's main loop (source/photon_mod.f90:1880-4036).
+template <typename R, typename Geo, typename P>
 __device__ __forceinline__ int stepPacket(const DevGrid& g, const Geo& q, const DevTransportIn& in,
-                                          const DevTransportOut& out, const TransportShared<R>& sh, Packet<R>& p,
+                                          const DevTransportOut& out, const TransportShared<R>& sh, P& p,
                                           R deltaER, double deltaE, LocalCounters& lc, PendingJ& pj) {
   using M = RMath<R>;
   const int nx = q.nx(), ny = q.ny(), nz = q.nz();
@@ -368,6 +502,19 @@ __device__ __forceinline__ int stepPacket(const DevGrid& g, const Geo& q, const 
   if (yP > 1)  { R m = (AXR(Y, yP) + AXR(Y, yP - 1)) / R(2); if (vy < R(0) && M::div_(M::abs_(ry - m), m) < R(2.e-2)) yP = yP - 1; }
   if (zP < nz) { R m = (AXR(Z, zP) + AXR(Z, zP + 1)) / R(2); if (vz > R(0) && M::div_(M::abs_(rz - m), m) < R(2.e-2)) zP = zP + 1; }
   if (zP > 1)  { R m = (AXR(Z, zP) + AXR(Z, zP - 1)) / R(2); if (vz < R(0) && M::div_(M::abs_(rz - m), m) < R(2.e-2)) zP = zP - 1; }
+
+  // the opacity and volume of the cell the snap leaves the packet in, loaded
+  // here so that their latency overlaps the wall-distance arithmetic; loaded
+  // again below in the rare case that a distance snap moves the index
+  const size_t C1 = (size_t)g.nCells + 1;
+  int cell = activeAt(q, xP, yP, zP);
+  R kap = (R)__ldg(in.opacity + (size_t)cell + C1 * (size_t)(p.nuP - 1));
+  R dV = cell > 0 ? cellVolume<R>(g, cell) : R(1);
+  const int xS = xP, yS = yP, zS = zP;
+  if (p.nEmit > kTrappedHint) {
+    if (g.lgDust) prefetchL1(in.scaOpac + (size_t)cell + C1 * (size_t)(p.nuP - 1));
+    else if (g.lgCompton) { prefetchL1(g.KNsigmaT + p.nuP - 1); prefetchL1(in.ne + cell); }
+  }
 
   // distances from the walls (source/photon_mod.f90:1933-2084); with one
   // mother grid the reference's inner loop runs exactly once
@@ -422,11 +569,12 @@ __device__ __forceinline__ int stepPacket(const DevGrid& g, const Geo& q, const 
   else { dS = M::min_(dSx, dSy); dS = M::min_(dS, dSz); }
   if (!(dS > R(0))) { ++lc.errors; return ST_IDLE; }
 
-  const int cell = activeAt(q, xP, yP, zP);
-  const size_t C1 = (size_t)g.nCells + 1;
-  const R kap = (R)__ldg(in.opacity + (size_t)cell + C1 * (size_t)(p.nuP - 1));
+  if (xP != xS || yP != yS || zP != zS) {
+    cell = activeAt(q, xP, yP, zP);
+    kap = (R)__ldg(in.opacity + (size_t)cell + C1 * (size_t)(p.nuP - 1));
+    dV = cell > 0 ? cellVolume<R>(g, cell) : R(1);
+  }
   const R tauCell = dS * kap;
-  const R dV = cell > 0 ? cellVolume<R>(g, cell) : R(1);
   R costheta = R(1);
   if (g.radPress && !(rx == R(0) && ry == R(0) && rz == R(0))) {
     costheta = ((rx * vx) + (ry * vy) + (rz * vz)) /
@@ -444,11 +592,12 @@ __device__ __forceinline__ int stepPacket(const DevGrid& g, const Geo& q, const 
       if (ry <= AXR(Y, 1)) { if (vy < R(0)) vy = -vy; ry = AXR(Y, 1); }
       if (rz <= AXR(Z, 1)) { if (vz < R(0)) vz = -vz; rz = AXR(Z, 1); }
     }
-    deposit<R>(g, out, cell, p.nuP, dlLoc, dV, deltaER, costheta, pj);
+    deposit<R, P::kWarp>(g, out, cell, p.nuP, dlLoc, dV, deltaER, costheta, pj);
     ++lc.interactions;
-    R rad = M::sqrt_((rx / R(1.e10)) * (rx / R(1.e10)) + (ry / R(1.e10)) * (ry / R(1.e10)) +
-                     (rz / R(1.e10)) * (rz / R(1.e10))) * R(1.e10);
-    if (rad >= (R)q.rOut() && q.rOut() > 0.f) {
+    // the radius only matters against an outer radius R_out > 0
+    if (q.rOut() > 0.f &&
+        M::sqrt_((rx / R(1.e10)) * (rx / R(1.e10)) + (ry / R(1.e10)) * (ry / R(1.e10)) +
+                 (rz / R(1.e10)) * (rz / R(1.e10))) * R(1.e10) >= (R)q.rOut()) {
       escapeTally<R>(g, out, p, deltaE, lc);
       if (p.nEmit >= kRecursionLimit) ++lc.trapped;
       return ST_IDLE;
@@ -485,7 +634,7 @@ __device__ __forceinline__ int stepPacket(const DevGrid& g, const Geo& q, const 
     }
   } else {
     // the packet crosses the cell (source/photon_mod.f90:2703-2881)
-    deposit<R>(g, out, cell, p.nuP, dS, dV, deltaER, costheta, pj);
+    deposit<R, P::kWarp>(g, out, cell, p.nuP, dS, dV, deltaER, costheta, pj);
     ++lc.crossings;
     p.absTau = p.absTau + tauCell;
     rx = rx + dS * vx; ry = ry + dS * vy; rz = rz + dS * vz;
@@ -586,7 +735,8 @@ __device__ __forceinline__ unsigned long long refill(unsigned need, DevTransport
 template <typename R>
 __global__ void __launch_bounds__(256)
 transportKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportCounters* cnt,
-                uint64_t seed, uint64_t base, unsigned long long n, double deltaE, int emitBatch) {
+                uint64_t seed, uint64_t base, unsigned long long n, double deltaE, int emitBatch,
+                Packet<R>* __restrict__ parked, unsigned long long parkedCap, int handoffAt) {
   extern __shared__ float smem[];
   float* sX = smem;
   float* sY = sX + g.nx;
@@ -628,12 +778,61 @@ transportKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportC
     }
     if (__ballot_sync(FULL, state != ST_DONE) == 0u) break;
     if (emitTurn(state, emitBatch)) {
-      if (state == ST_EMIT) state = emitPacket<R>(g, q, in, out, sh, p, deltaE, lc);
+      if (state == ST_EMIT) {
+        bool moved = false;
+        if (handoffAt > 0 && p.nEmit >= handoffAt && p.nEmit < kRecursionLimit) {
+          // trapped: park the history here, as it stands before this emission,
+          // for the trapped-packet kernel, and take the next packet
+          const unsigned long long slot = atomicAdd(&cnt->handoff, 1ull);
+          if (slot < parkedCap) { parked[slot] = p; state = ST_IDLE; moved = true; }
+        }
+        if (!moved) state = emitPacket<R>(g, q, in, out, sh, p, deltaE, lc);
+      }
     } else if (state == ST_STEP) {
       state = stepPacket<R>(g, q, in, out, sh, p, deltaER, deltaE, lc, pj);
     }
   }
   flushJ(out, pj);
+  flushCounters(lc, cnt);
+}
+
+// The trapped-packet kernel, launched after transportKernel on the same stream:
+// continues every parked history to its end, one history per warp (one warp
+// per block, as many blocks as are resident at once, histories handed out
+// round-robin).  A trapped history is a serial chain of up to recursionLimit
+// emission + step events whose length sets the launch's; a lone lane runs that
+// chain at one instruction per several cycles, so the warp's other lanes are
+// put to work on its data-parallel parts (the Philox stream, the CDF search)
+// while all lanes run the scalar physics in lockstep.  No shared memory: axes
+// and frequencies are read through L1, which keeps its full size.
+template <typename R>
+__global__ void __launch_bounds__(32)
+transportTrappedKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportCounters* cnt, double deltaE,
+                       const Packet<R>* __restrict__ parked, unsigned long long parkedCap) {
+  const unsigned long long written = *reinterpret_cast<volatile unsigned long long*>(&cnt->handoff);
+  const unsigned long long count = written < parkedCap ? written : parkedCap;
+  TransportShared<R> sh{g.nu};
+  const OneGrid q{g, g.xAxis, g.yAxis, g.zAxis, g.srcCDF};
+  const R deltaER = (R)deltaE;
+  LocalCounters lc;
+  PendingJ pj{0., 0., 0, false};
+  // the first gridDim.x histories one per warp, the rest from a queue as
+  // warps finish (most parked histories end within a few hundred events; a
+  // trapped one runs to recursionLimit)
+  for (unsigned long long i = blockIdx.x; i < count;) {
+    WarpPacket<R> p;
+    p.from(parked[i]);
+    int state = ST_EMIT;
+    while (state == ST_EMIT || state == ST_STEP) {
+      if (state == ST_EMIT) state = emitBody<R, OneGrid>(g, q, in, out, sh, p, deltaE, lc);
+      else state = stepPacket<R>(g, q, in, out, sh, p, deltaER, deltaE, lc, pj);
+    }
+    unsigned long long nxt = 0;
+    if ((threadIdx.x & 31u) == 0u) nxt = gridDim.x + atomicAdd(&cnt->parkedNext, 1ull);
+    i = __shfl_sync(0xffffffffu, nxt, 0);
+  }
+  flushJ(out, pj);
+  if ((threadIdx.x & 31u) != 0u) lc = LocalCounters{};   // every lane counted the same events
   flushCounters(lc, cnt);
 }
 
@@ -732,6 +931,32 @@ transportKernelBatched(DevGrid g, DevTransportIn in, DevTransportOut out, DevTra
   if (stampNeb >= 0) atomicMax(doneNs + stampNeb, stampNs);
   flushJ(out, pj);
   flushCounters(lc, cnt);
+}
+
+// The single-grid launch: the persistent kernel, then, when hand-off is on,
+// the trapped-packet kernel with one warp per block on every SM (as many
+// blocks as are resident at once, so every parked history starts at once).
+template <typename R>
+cudaError_t launchTransportImpl(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,
+                                DevTransportCounters* cnt, uint64_t seed, uint64_t base, unsigned long long n,
+                                double deltaE, const TransportLaunch& L, cudaStream_t s) {
+  const size_t smem = packetStateOffset(L.smem) + packetStateBytes<R>(L.threads);
+  cudaError_t e = cudaFuncSetAttribute(transportKernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const bool hand = L.parked != nullptr && L.parkedCap > 0 && L.handoffAt > 0 && L.numSMs > 0;
+  transportKernel<R><<<L.blocks, L.threads, smem, s>>>(g, in, out, cnt, seed, base, n, deltaE,
+                                                       L.emitBatch > 0 ? L.emitBatch : kEmitBatch,
+                                                       hand ? static_cast<Packet<R>*>(L.parked) : nullptr,
+                                                       hand ? L.parkedCap : 0ull, hand ? L.handoffAt : 0);
+  e = cudaGetLastError();
+  if (e != cudaSuccess || !hand) return e;
+  int perSM = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, transportTrappedKernel<R>, 32, 0);
+  if (e != cudaSuccess) return e;
+  if (perSM < 1) perSM = 1;
+  transportTrappedKernel<R><<<L.numSMs * perSM, 32, 0, s>>>(g, in, out, cnt, deltaE,
+                                                            static_cast<const Packet<R>*>(L.parked), L.parkedCap);
+  return cudaGetLastError();
 }
 
 }  // namespace mcx

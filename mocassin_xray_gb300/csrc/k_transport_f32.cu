@@ -7,13 +7,10 @@ namespace mcx {
 cudaError_t launchTransportF32(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,
                                DevTransportCounters* cnt, uint64_t seed, uint64_t base, unsigned long long n,
                                double deltaE, const TransportLaunch& L, cudaStream_t s) {
-  const size_t smem = packetStateOffset(L.smem) + packetStateBytes<float>(L.threads);
-  cudaError_t e = cudaFuncSetAttribute(transportKernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  transportKernel<float><<<L.blocks, L.threads, smem, s>>>(g, in, out, cnt, seed, base, n, deltaE,
-                                                         L.emitBatch > 0 ? L.emitBatch : kEmitBatch);
-  return cudaGetLastError();
+  return launchTransportImpl<float>(g, in, out, cnt, seed, base, n, deltaE, L, s);
 }
+
+size_t parkedPacketBytesF32() { return sizeof(Packet<float>); }
 
 cudaError_t launchTransportBatchedF32(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,
                                       DevTransportCounters* cnt, const NebulaDesc* neb,

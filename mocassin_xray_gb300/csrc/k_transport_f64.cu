@@ -7,13 +7,10 @@ namespace mcx {
 cudaError_t launchTransportF64(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,
                                DevTransportCounters* cnt, uint64_t seed, uint64_t base, unsigned long long n,
                                double deltaE, const TransportLaunch& L, cudaStream_t s) {
-  const size_t smem = packetStateOffset(L.smem) + packetStateBytes<double>(L.threads);
-  cudaError_t e = cudaFuncSetAttribute(transportKernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  transportKernel<double><<<L.blocks, L.threads, smem, s>>>(g, in, out, cnt, seed, base, n, deltaE,
-                                                         L.emitBatch > 0 ? L.emitBatch : kEmitBatch);
-  return cudaGetLastError();
+  return launchTransportImpl<double>(g, in, out, cnt, seed, base, n, deltaE, L, s);
 }
+
+size_t parkedPacketBytesF64() { return sizeof(Packet<double>); }
 
 cudaError_t launchTransportBatchedF64(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,
                                       DevTransportCounters* cnt, const NebulaDesc* neb,

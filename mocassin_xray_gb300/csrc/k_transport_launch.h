@@ -10,6 +10,14 @@ struct TransportLaunch {
   int threads;
   size_t smem;
   int emitBatch;   // 0 = the kernel's default
+  // Trapped-packet hand-off (single-grid kernel only): a packet about to be
+  // re-emitted for the handoffAt-th time is parked in `parked` (room for
+  // parkedCap packets) and continued by the trapped-packet kernel launched
+  // right after; handoffAt = 0 or parked = null keeps every packet in place.
+  void* parked;
+  unsigned long long parkedCap;
+  int handoffAt;
+  int numSMs;
 };
 
 cudaError_t launchTransportF32(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,
@@ -31,6 +39,10 @@ cudaError_t launchTransportBatchedF64(const DevGrid& g, const DevTransportIn& in
                                       unsigned long long* stamps, cudaStream_t s);
 cudaError_t transportOccupancyBatchedF32(int threads, size_t smem, int* blocksPerSM);
 cudaError_t transportOccupancyBatchedF64(int threads, size_t smem, int* blocksPerSM);
+
+// Bytes of one parked packet of the FP32 / FP64 kernel.
+size_t parkedPacketBytesF32();
+size_t parkedPacketBytesF64();
 
 // Resident blocks per SM of the FP64 (fp64 = true) or FP32 instantiation.
 cudaError_t transportOccupancy(bool fp64, int threads, size_t smem, int* blocksPerSM);

@@ -316,6 +316,13 @@ extern "C" int mcx_setup_set(mcx_setup* m, int32_t id, const void* src, size_t n
 // ------------------------------------------------------------------ context
 namespace {
 
+// Trapped-packet hand-off: a history is parked for the trapped-packet kernel
+// when it is about to be re-emitted for the kHandoffAt-th time (bulk histories
+// end after a handful of emissions; a trapped one runs on to recursionLimit),
+// in a buffer with room for kParkedCap histories (beyond it they stay in place).
+constexpr int kHandoffAt = 256;
+constexpr unsigned long long kParkedCap = 1ull << 16;
+
 template <typename T>
 struct DBuf {
   T* p = nullptr;
@@ -362,6 +369,7 @@ struct mcx_ctx {
   int starIdx[3] = {0, 0, 0};
   float starPos[3] = {0.f, 0.f, 0.f};
   std::vector<int32_t> activeHost;
+  int activeFull = 0;        // active(i,j,k) == (i-1) ny nz + (j-1) nz + k for every cell
   float gauntTeOld = -1.f;   // BoltGaunt's saved TeOld2
 
   // tables
@@ -384,6 +392,9 @@ struct mcx_ctx {
   DBuf<float> gauntTe;
   DBuf<uint8_t> computeMask;
   DBuf<DevTransportCounters> counters;
+  // histories parked by the transport kernel for the trapped-packet kernel
+  // (kParkedCap packets of the FP64 kernel, the larger of the two)
+  DBuf<unsigned char> parked;
   std::unique_ptr<EmissionData> emission;
   std::unique_ptr<BalanceData> balance;
   std::unique_ptr<DustData> dust;
@@ -728,6 +739,14 @@ static int loadSetup(mcx_ctx* c, const Setup& s) {
   if (s.starIdx[0] < 1 || s.starIdx[0] > s.nx || s.starIdx[1] < 1 || s.starIdx[1] > s.ny || s.starIdx[2] < 1 || s.starIdx[2] > s.nz)
     return fail(c, MCX_ERR_INPUT, "mcx_load: the source must lie inside the grid");
   c->activeHost = s.active;
+  c->activeFull = 1;
+  for (int k = 0; k < s.nz && c->activeFull; ++k)
+    for (int j = 0; j < s.ny && c->activeFull; ++j)
+      for (int i = 0; i < s.nx; ++i)
+        if (s.active[(size_t)i + (size_t)s.nx * ((size_t)j + (size_t)s.ny * k)] != (i * s.ny + j) * s.nz + k + 1) {
+          c->activeFull = 0;
+          break;
+        }
   // viewing-angle bins (initCartesianGrid, source/grid_mod.f90:570-601): theta in 20 bins over
   // [0, pi], phi in 20 over [0, 2 pi) unless a view's phi is negative (no phi dependence)
   c->nAngle = s.p.nAngleBins;
@@ -803,6 +822,7 @@ static int loadSetup(mcx_ctx* c, const Setup& s) {
   CK(c->totalLines.alloc(C1), "alloc totalLines");
   CK(c->jste.alloc(C1 * nb), "alloc Jste");
   CK(c->jlo.alloc(C1 * nb), "alloc Jste compensation");
+  CK(c->parked.alloc(kParkedCap * std::max(parkedPacketBytesF32(), parkedPacketBytesF64())), "alloc parked packets");
   CK(c->escaped.alloc(C1 * (nb + 1) * (size_t)(c->nAngle + 1)), "alloc escaped");
   if (c->radPress) CK(c->hEst.alloc(C1 * nb), "alloc H");
   if (c->lgDust) {
@@ -1285,6 +1305,7 @@ static int transportFinish(mcx_ctx* c, mcx_transport_stats* stats, const char* w
     stats->trapped = (int64_t)h.trapped;
     stats->emissions = (int64_t)h.emissions;
     stats->q_phot = h.qPhot;
+    stats->handed_off = (int64_t)std::min<unsigned long long>(h.handoff, c->parked.p ? kParkedCap : 0);
     cudaEventElapsedTime(&stats->kernel_ms, c->ev0, c->ev1);
   }
   if (h.errors)
@@ -1318,7 +1339,7 @@ extern "C" int mcx_transport(mcx_ctx* c, const mcx_transport_opts* o, mcx_transp
   DevGrid g{};
   g.nx = c->nx; g.ny = c->ny; g.nz = c->nz; g.nCells = c->nCells; g.nbins = c->nbins;
   g.symmetric = c->symmetric; g.lgDust = c->lgDust; g.lgGas = c->lgGas; g.lgCompton = c->lgCompton;
-  g.radPress = c->radPress;
+  g.radPress = c->radPress; g.activeFull = c->activeFull;
   for (int d = 0; d < 3; ++d) { g.starIdx[d] = c->starIdx[d]; g.starPos[d] = c->starPos[d]; }
   g.ionEdge1 = c->ionEdge1; g.rOut = c->rOut;
   g.xAxis = c->xAxis.p; g.yAxis = c->yAxis.p; g.zAxis = c->zAxis.p; g.active = c->active.p;
@@ -1343,6 +1364,10 @@ extern "C" int mcx_transport(mcx_ctx* c, const mcx_transport_opts* o, mcx_transp
   if (perSM < 1) perSM = 1;
   int mult = o->grid_mult > 0 ? std::min(o->grid_mult, perSM) : perSM;
   L.blocks = c->numSMs * mult;
+  L.parked = c->parked.p;
+  L.parkedCap = c->parked.p ? kParkedCap : 0;
+  L.handoffAt = o->handoff_emissions < 0 ? 0 : (o->handoff_emissions > 0 ? o->handoff_emissions : kHandoffAt);
+  L.numSMs = c->numSMs;
   const unsigned long long n = (unsigned long long)o->n_packets;
   if (n > 0) {
     const unsigned long long maxBlocks = (n + L.threads - 1) / L.threads;

@@ -10,6 +10,10 @@ namespace mcx {
 struct DevGrid {
   int32_t nx, ny, nz, nCells, nbins;
   int32_t symmetric, lgDust, lgGas, lgCompton, radPress;
+  // 1 when active(i,j,k) numbers every cell of the full grid in the
+  // reference's order, (i-1) ny nz + (j-1) nz + k: the cell id is then
+  // computed instead of loaded (one dependent global load less per event)
+  int32_t activeFull;
   int32_t starIdx[3];
   float starPos[3];
   float ionEdge1, rOut;
@@ -68,7 +72,9 @@ struct DevTransportCounters {
   unsigned long long errors;
   unsigned long long queue;            // work-queue head (next packet index)
   double qPhot;
-  unsigned long long pad[5];
+  unsigned long long handoff;          // packets parked for the trapped-packet kernel (may exceed the capacity)
+  unsigned long long parkedNext;       // the trapped-packet kernel's queue head (beyond its first wave)
+  unsigned long long pad[3];
 };
 
 // Philox4x32-10 (Salmon et al., SC'11), round constants of the published algorithm.

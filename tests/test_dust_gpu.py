@@ -10,10 +10,17 @@ from mocassin_xray_gb300 import abi, Context, Setup
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module")
-def dust_deck(tmp_path_factory):
-    from mocassin_xray_gb300 import configs
-    return configs.dust_shell(tmp_path_factory.mktemp("dust") / "d", n=15, packets=40000)
+@pytest.fixture(scope="module", params=["q", "nk"])
+def dust_deck(request, tmp_path_factory):
+    """The synthetic shell with grains from efficiency ('Q') files, and the
+    same shell with the reference's silicate optical constants ('nk' file,
+    cross sections from the Mie series)."""
+    from mocassin_xray_gb300 import DATA_DIR, configs
+    deck = configs.dust_shell(tmp_path_factory.mktemp("dust") / "d", n=15, packets=40000)
+    if request.param == "nk":
+        nk = DATA_DIR.parent / "dustData" / "sil-dlee.nk"
+        (deck.parent / "grainspecies.dat").write_text(f"1\n'{nk}' 1.0\n")
+    return deck
 
 
 def test_dust_phases_match_oracle(dust_deck, data_dir, oracle_lib):

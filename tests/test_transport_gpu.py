@@ -52,6 +52,44 @@ def test_fp64_transport_matches_oracle(decks, data_dir, oracle_lib, name):
     ctx.close()
 
 
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_FP32_GEOM])
+def test_trapped_handoff_changes_nothing(decks, data_dir, oracle_lib, precision):
+    """Histories moved to the trapped-packet kernel (after 1 or 3
+    re-emissions here, so that every re-emitted history moves) give the same J
+    bits, the same event counts and the same escapes as histories kept in the
+    main kernel, also when more histories qualify than the 65536 the parking
+    buffer holds (the rest stay in place); the FP64 path also equals the oracle."""
+    s, op, rec, tl, ctx = _case(decks, data_dir, oracle_lib, "lognormal_small")
+    n, seed = 100000, 4321
+    ref = ctx.transport(n, seed=seed, precision=precision, handoff_emissions=-1)
+    assert ref.handed_off == 0
+    j0, e0 = ctx.get(abi.ARR_JSTE), ctx.get(abi.ARR_ESCAPED)
+    keys = ("crossings", "interactions", "absorptions", "scatterings", "escaped", "line_escapes", "emissions", "trapped")
+    for at in (1, 3):
+        st = ctx.transport(n, seed=seed, precision=precision, handoff_emissions=at)
+        assert st.handed_off > 0
+        for k in keys:
+            assert getattr(st, k) == getattr(ref, k), (at, k)
+        assert st.q_phot == pytest.approx(ref.q_phot, rel=1e-12)
+        np.testing.assert_array_equal(ctx.get(abi.ARR_JSTE), j0)
+        np.testing.assert_allclose(ctx.get(abi.ARR_ESCAPED), e0, rtol=1e-12, atol=0)
+    if precision == abi.PREC_FP64:
+        jo, _, so = oracle_lib.transport(s, op, rec, tl, n=n, seed=seed, nthreads=8)
+        np.testing.assert_array_equal(j0, jo)
+        for k in keys:
+            assert getattr(ref, k) == getattr(so, k), k
+    # more qualifying histories than parking room
+    big = 800000
+    ref = ctx.transport(big, seed=seed, precision=precision, handoff_emissions=-1)
+    j0 = ctx.get(abi.ARR_JSTE)
+    st = ctx.transport(big, seed=seed, precision=precision, handoff_emissions=1)
+    assert st.handed_off == 65536
+    for k in keys:
+        assert getattr(st, k) == getattr(ref, k), k
+    np.testing.assert_array_equal(ctx.get(abi.ARR_JSTE), j0)
+    ctx.close()
+
+
 def test_fp32_transport_is_reproducible(decks, data_dir, oracle_lib):
     """The production path's J does not depend on the order in which the
     atomics land (scheduling, block shape): the same seed gives the same bits."""
