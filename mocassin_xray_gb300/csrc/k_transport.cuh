@@ -82,13 +82,10 @@ struct WarpRng {
   uint32_t k;              // draws taken so far
   uint32_t blk0;           // first Philox block held by the warp
   uint32_t b0, b1, b2, b3; // this lane's block, blk0 + lane
-  // out of line: inlined at every draw site it would fill the instruction
-  // cache with copies of Philox that run once per 128 draws
-  __device__ __noinline__ void fill(uint32_t first) {
-    uint32_t o[4];
+  __device__ __forceinline__ void fill(uint32_t first) {
     blk0 = first;
-    philox4x32_10(p0, p1, first + (threadIdx.x & 31u), 0u, k0, k1, o);
-    b0 = o[0]; b1 = o[1]; b2 = o[2]; b3 = o[3];
+    const uint4 b = philoxBlock(p0, p1, first + (threadIdx.x & 31u), k0, k1);
+    b0 = b.x; b1 = b.y; b2 = b.z; b3 = b.w;
   }
   __device__ __forceinline__ void start(const PacketRng& r) {
     k0 = r.k0; k1 = r.k1; p0 = r.p0; p1 = r.p1; k = r.k;
@@ -269,6 +266,18 @@ __device__ __forceinline__ int warpCdfFinish(const WarpCdf& c, const float* __re
 template <typename P>
 __device__ __forceinline__ typename P::Real draw(P& p) { return uniformFrom<typename P::Real>(p.rng.next()); }
 
+// t cos(a) and t sin(a), out of line: the accurate sine and cosine are long,
+// and inlined at each direction draw they would crowd the transport loop out
+// of the instruction cache.
+template <typename R>
+struct CosSin { R c, s; };
+
+template <typename R>
+__device__ __noinline__ CosSin<R> scaledCosSin(R t, R a) {
+  using M = RMath<R>;
+  return CosSin<R>{t * M::cos_(a), t * M::sin_(a)};
+}
+
 // initPhotonPacket (source/photon_mod.f90:744-896): position, frequency, an
 // isotropic direction (re-drawn while a component is exactly zero) and the
 // octant fold for stellar packets.
@@ -286,7 +295,8 @@ __device__ __forceinline__ void initPacket(const Geo& q, const TransportShared<R
     R t = M::sqrt_(R(1) - w * w);
     R r2 = draw(p);
     R ang = R(3.141592654) * (R(2) * r2 - R(1));
-    p.vx = t * M::cos_(ang); p.vy = t * M::sin_(ang); p.vz = w;
+    const CosSin<R> cs = scaledCosSin<R>(t, ang);
+    p.vx = cs.c; p.vy = cs.s; p.vz = w;
     if (p.vx != R(0) && p.vy != R(0) && p.vz != R(0)) break;
   }
   if (q.symmetric() && stellar) {
@@ -307,6 +317,22 @@ __device__ __forceinline__ void initPacket(const Geo& q, const TransportShared<R
 // bins have viewPointPtheta = viewPointPphi = 0, which the reference's test
 // counts as a match of view 0, adding deltaE to plane 0 a second time; both
 // are reproduced.
+// The (theta, phi) bins of a direction, out of line (acos and atan are long
+// and run once per escaping packet).
+template <typename R>
+__device__ __noinline__ int2 viewBins(R vx, R vy, R vz, int totPhi) {
+  const R dTheta = R(3.141592654) / R(20);
+  const R dPhi = (R(2) * R(3.141592654)) / (R)totPhi;
+  int idirT = (int)(acos(vz) / dTheta) + 1;
+  if (idirT > 20) idirT = 20;
+  if (idirT < 1) idirT = 1;
+  int idirP = vx < R(1.e-35) ? 0 : (int)(atan(vy / vx) / dPhi);
+  if (idirP < 0) idirP = totPhi + idirP;
+  idirP = idirP + 1;
+  if (idirP > totPhi) idirP = totPhi;
+  return make_int2(idirT, idirP);
+}
+
 template <typename R, typename P>
 __device__ __forceinline__ void escapeTally(const DevGrid& g, const DevTransportOut& out, const P& p,
                                             double deltaE, LocalCounters& lc) {
@@ -315,15 +341,8 @@ __device__ __forceinline__ void escapeTally(const DevGrid& g, const DevTransport
   const size_t plane = ((size_t)g.nCells + 1) * ((size_t)g.nbins + 1);
   const size_t at = (size_t)p.origin + ((size_t)g.nCells + 1) * (size_t)p.nuP;
   if (g.nAngle > 0) {
-    const R dTheta = R(3.141592654) / R(20);
-    const R dPhi = (R(2) * R(3.141592654)) / (R)g.totPhi;
-    int idirT = (int)(acos(p.vz) / dTheta) + 1;
-    if (idirT > 20) idirT = 20;
-    if (idirT < 1) idirT = 1;
-    int idirP = p.vx < R(1.e-35) ? 0 : (int)(atan(p.vy / p.vx) / dPhi);
-    if (idirP < 0) idirP = g.totPhi + idirP;
-    idirP = idirP + 1;
-    if (idirP > g.totPhi) idirP = g.totPhi;
+    const int2 bins = viewBins<R>(p.vx, p.vy, p.vz, g.totPhi);
+    const int idirT = bins.x, idirP = bins.y;
     const int k = g.viewPTheta[idirT];
     if ((g.totPhi > 1 && k == g.viewPPhi[idirP]) || (g.totPhi == 1 && k > 0))
       atomicAdd(out.escaped + plane * (size_t)k + at, deltaE);
@@ -393,8 +412,9 @@ __device__ __forceinline__ void comptonScatter(const DevGrid& g, const Transport
   R u = draw(p);
   R w = R(2) * u - R(1);
   R t = M::sqrt_(R(1) - w * w);
-  p.vx = t * M::cos_(newTheta);
-  p.vy = t * M::sin_(newTheta);
+  const CosSin<R> cs = scaledCosSin<R>(t, newTheta);
+  p.vx = cs.c;
+  p.vy = cs.s;
   p.vz = w;
   int thc = th > 180 ? 180 : th;
   R newNu = p.nu * (R)__ldg(g.PcompT + (size_t)(p.nuP - 1) * 180 + (thc - 1));
@@ -855,7 +875,7 @@ __device__ __forceinline__ unsigned long long globalTimerNs() {
 static __global__ void stampStartKernel(unsigned long long* startNs) { *startNs = globalTimerNs(); }
 
 template <typename R>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
 transportKernelBatched(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportCounters* cnt,
                        const NebulaDesc* __restrict__ neb, const unsigned long long* __restrict__ pktBegin, int nNeb,
                        const float* __restrict__ axes, const int32_t* __restrict__ active,

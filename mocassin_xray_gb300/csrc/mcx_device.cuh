@@ -96,6 +96,18 @@ __host__ __device__ inline void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t
   out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
+#ifdef __CUDACC__
+// One Philox block, out of line and by value: inlined at every draw site the
+// ten rounds would crowd the transport loop out of the instruction cache (a
+// draw needs a new block once in four), and a value result keeps the caller's
+// state in registers.
+__device__ __noinline__ inline uint4 philoxBlock(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t k0, uint32_t k1) {
+  uint32_t o[4];
+  philox4x32_10(c0, c1, c2, 0u, k0, k1, o);
+  return make_uint4(o[0], o[1], o[2], o[3]);
+}
+#endif
+
 // Per-packet counter-based stream: draw k of packet pid is word k%4 of
 // philox(key, (pid_lo, pid_hi, k/4, k>>34)).
 struct PacketRng {
@@ -109,7 +121,10 @@ struct PacketRng {
     k = 0;
   }
   __device__ __forceinline__ uint32_t next() {
-    if ((k & 3u) == 0) philox4x32_10(p0, p1, k >> 2, 0u, k0, k1, buf);
+    if ((k & 3u) == 0) {
+      const uint4 b = philoxBlock(p0, p1, k >> 2, k0, k1);
+      buf[0] = b.x; buf[1] = b.y; buf[2] = b.z; buf[3] = b.w;
+    }
     uint32_t x;
     switch (k & 3u) { case 0: x = buf[0]; break; case 1: x = buf[1]; break; case 2: x = buf[2]; break; default: x = buf[3]; }
     ++k;
