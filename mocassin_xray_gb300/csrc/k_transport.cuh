@@ -60,6 +60,34 @@ template <> struct RMath<double> {
   static __device__ __forceinline__ double div_(double a, double b) { return a / b; }
 };
 
+// t cos(a) and t sin(a), out of line: the accurate sine and cosine are long,
+// and inlined at each direction draw they would crowd the transport loop out
+// of the instruction cache.
+template <typename R>
+struct CosSin { R c, s; };
+
+template <typename R>
+__device__ __noinline__ CosSin<R> scaledCosSin(R t, R a) {
+  using M = RMath<R>;
+  return CosSin<R>{t * M::cos_(a), t * M::sin_(a)};
+}
+
+// The isotropic direction initPhotonPacket draws from the uniforms r1, r2
+// (source/photon_mod.f90:858-878): w = 2 r1 - 1, t = sqrt(1 - w^2),
+// phi = pi (2 r2 - 1), (t cos phi, t sin phi, w).
+template <typename R>
+struct Dir3 { R x, y, z; };
+
+template <typename R>
+__device__ __forceinline__ Dir3<R> isoDirection(R r1, R r2) {
+  using M = RMath<R>;
+  const R w = R(2) * r1 - R(1);
+  const R t = M::sqrt_(R(1) - w * w);
+  const R ang = R(3.141592654) * (R(2) * r2 - R(1));
+  const CosSin<R> cs = scaledCosSin<R>(t, ang);
+  return Dir3<R>{cs.c, cs.s, w};
+}
+
 template <typename R>
 struct Packet {
   using Real = R;
@@ -74,30 +102,81 @@ struct Packet {
 // A history run by a whole warp (the trapped-packet kernel): every lane holds
 // the same state and executes the same scalar arithmetic, so every lane
 // computes the same values; the lanes split only the data-parallel parts.
-// Here the Philox stream: lane l keeps block blk0 + l (4 draws), so one
-// refill covers the next 128 draws and a draw is a select and a shuffle.  The
-// draws are those of PacketRng, position for position.
+// Here the Philox stream: lane l keeps block blk0 + l (draws 4 (blk0 + l) ..
+// 4 (blk0 + l) + 3), so one refill covers the next 128 draws and a draw is a
+// select and a shuffle.  At a refill each lane also evaluates, for each of its
+// four positions i, what a history drawing there would compute: the isotropic
+// direction from draws i and i + 1 and -ln(1 - u_i) (a path's optical depth),
+// so that the history's chain of events takes them with a shuffle instead of a
+// square root, a sine, a cosine and a logarithm.  Lookups go by the draw index
+// the history has reached, so any sequence of draws finds its own values; the
+// values are those of the same expressions, bit for bit.
+template <typename R>
 struct WarpRng {
   uint32_t k0, k1, p0, p1;
   uint32_t k;              // draws taken so far
   uint32_t blk0;           // first Philox block held by the warp
   uint32_t b0, b1, b2, b3; // this lane's block, blk0 + lane
+  R dx0, dx1, dx2, dx3, dy0, dy1, dy2, dy3, dz0, dz1, dz2, dz3;   // direction starting at position c
+  R nl0, nl1, nl2, nl3;                                           // -ln(1 - u) at position c
   __device__ __forceinline__ void fill(uint32_t first) {
+    using M = RMath<R>;
     blk0 = first;
     const uint4 b = philoxBlock(p0, p1, first + (threadIdx.x & 31u), k0, k1);
     b0 = b.x; b1 = b.y; b2 = b.z; b3 = b.w;
+    // the next lane's first draw completes the direction starting at position 3
+    // (lane 31's lies beyond the window; it is never looked up)
+    const uint32_t after = __shfl_down_sync(0xffffffffu, b0, 1);
+    const R u0 = uniformFrom<R>(b0), u1 = uniformFrom<R>(b1), u2 = uniformFrom<R>(b2), u3 = uniformFrom<R>(b3);
+    const R u4 = uniformFrom<R>(after);
+    Dir3<R> d;
+    d = isoDirection<R>(u0, u1); dx0 = d.x; dy0 = d.y; dz0 = d.z;
+    d = isoDirection<R>(u1, u2); dx1 = d.x; dy1 = d.y; dz1 = d.z;
+    d = isoDirection<R>(u2, u3); dx2 = d.x; dy2 = d.y; dz2 = d.z;
+    d = isoDirection<R>(u3, u4); dx3 = d.x; dy3 = d.y; dz3 = d.z;
+    nl0 = -M::log_(R(1) - u0); nl1 = -M::log_(R(1) - u1);
+    nl2 = -M::log_(R(1) - u2); nl3 = -M::log_(R(1) - u3);
   }
   __device__ __forceinline__ void start(const PacketRng& r) {
     k0 = r.k0; k1 = r.k1; p0 = r.p0; p1 = r.p1; k = r.k;
     fill(k >> 2);
   }
+  template <typename T>
+  static __device__ __forceinline__ T pick(uint32_t c, T a0, T a1, T a2, T a3) {
+    return c == 0u ? a0 : (c == 1u ? a1 : (c == 2u ? a2 : a3));
+  }
+  // the lane holding position k, refilling the window first if k has left it
+  __device__ __forceinline__ int lane() {
+    if ((k >> 2) - blk0 >= 32u) fill(k >> 2);
+    return (int)((k >> 2) - blk0);
+  }
   __device__ __forceinline__ uint32_t next() {
-    const uint32_t blk = k >> 2;
-    if (blk - blk0 >= 32u) fill(blk);
-    const uint32_t sel = k & 3u;
-    const uint32_t mine = sel == 0u ? b0 : (sel == 1u ? b1 : (sel == 2u ? b2 : b3));
+    const int src = lane();
+    const uint32_t c = k & 3u;
     ++k;
-    return __shfl_sync(0xffffffffu, mine, (int)(blk - blk0));
+    return __shfl_sync(0xffffffffu, pick(c, b0, b1, b2, b3), src);
+  }
+  // -ln(1 - u) of the next draw
+  __device__ __forceinline__ R negLog1m() {
+    const int src = lane();
+    const uint32_t c = k & 3u;
+    ++k;
+    return __shfl_sync(0xffffffffu, pick(c, nl0, nl1, nl2, nl3), src);
+  }
+  // the isotropic direction from the next two draws
+  __device__ __forceinline__ Dir3<R> direction() {
+    const int src = lane();
+    const uint32_t c = k & 3u;
+    if (src == 31 && c == 3u) {   // its second draw is in the next window
+      const R r1 = uniformFrom<R>(next());
+      const R r2 = uniformFrom<R>(next());
+      return isoDirection<R>(r1, r2);
+    }
+    k += 2;
+    const unsigned FULL = 0xffffffffu;
+    return Dir3<R>{__shfl_sync(FULL, pick(c, dx0, dx1, dx2, dx3), src),
+                   __shfl_sync(FULL, pick(c, dy0, dy1, dy2, dy3), src),
+                   __shfl_sync(FULL, pick(c, dz0, dz1, dz2, dz3), src)};
   }
 };
 
@@ -109,7 +188,7 @@ struct WarpPacket {
   R nu, absTau, passProb;
   int xP, yP, zP, nuP, origin;
   int type, lgStellar, nEmit, nStep;
-  WarpRng rng;
+  WarpRng<R> rng;
   __device__ __forceinline__ void from(const Packet<R>& a) {
     x = a.x; y = a.y; z = a.z; vx = a.vx; vy = a.vy; vz = a.vz;
     nu = a.nu; absTau = a.absTau; passProb = a.passProb;
@@ -266,16 +345,12 @@ __device__ __forceinline__ int warpCdfFinish(const WarpCdf& c, const float* __re
 template <typename P>
 __device__ __forceinline__ typename P::Real draw(P& p) { return uniformFrom<typename P::Real>(p.rng.next()); }
 
-// t cos(a) and t sin(a), out of line: the accurate sine and cosine are long,
-// and inlined at each direction draw they would crowd the transport loop out
-// of the instruction cache.
-template <typename R>
-struct CosSin { R c, s; };
-
-template <typename R>
-__device__ __noinline__ CosSin<R> scaledCosSin(R t, R a) {
-  using M = RMath<R>;
-  return CosSin<R>{t * M::cos_(a), t * M::sin_(a)};
+// a path's optical depth to the next interaction, -ln(1 - u)
+template <typename P>
+__device__ __forceinline__ typename P::Real drawPassProb(P& p) {
+  using R = typename P::Real;
+  if constexpr (P::kWarp) return p.rng.negLog1m();
+  else return -RMath<R>::log_(R(1) - draw(p));
 }
 
 // initPhotonPacket (source/photon_mod.f90:744-896): position, frequency, an
@@ -290,13 +365,15 @@ __device__ __forceinline__ void initPacket(const Geo& q, const TransportShared<R
   p.nu = line ? R(0) : (R)sh.nu[nuP - 1];
   p.xP = xP; p.yP = yP; p.zP = zP;
   for (int rep = 0; rep < 1000000; ++rep) {
-    R r1 = draw(p);
-    R w = R(2) * r1 - R(1);
-    R t = M::sqrt_(R(1) - w * w);
-    R r2 = draw(p);
-    R ang = R(3.141592654) * (R(2) * r2 - R(1));
-    const CosSin<R> cs = scaledCosSin<R>(t, ang);
-    p.vx = cs.c; p.vy = cs.s; p.vz = w;
+    Dir3<R> d;
+    if constexpr (P::kWarp) {
+      d = p.rng.direction();
+    } else {
+      const R r1 = draw(p);
+      const R r2 = draw(p);
+      d = isoDirection<R>(r1, r2);
+    }
+    p.vx = d.x; p.vy = d.y; p.vz = d.z;
     if (p.vx != R(0) && p.vy != R(0) && p.vz != R(0)) break;
   }
   if (q.symmetric() && stellar) {
@@ -490,7 +567,7 @@ __device__ __forceinline__ int emitBody(const DevGrid& g, const Geo& q, const De
   // pathSegment entry (source/photon_mod.f90:1813-1878)
   if (p.xP <= 0 || p.xP > q.nx() || p.yP <= 0 || p.yP > q.ny() || p.zP <= 0 || p.zP > q.nz()) { ++lc.errors; return ST_IDLE; }
   p.absTau = R(0);
-  p.passProb = -M::log_(R(1) - draw(p));
+  p.passProb = drawPassProb(p);
   p.nStep = 0;
   return ST_STEP;
 }
@@ -499,6 +576,66 @@ template <typename R, typename Geo>
 __device__ __noinline__ int emitPacket(const DevGrid& g, const Geo& q, const DevTransportIn& in, const DevTransportOut& out,
                                        const TransportShared<R>& sh, Packet<R>& p, double deltaE, LocalCounters& lc) {
   return emitBody<R, Geo>(g, q, in, out, sh, p, deltaE, lc);
+}
+
+// One axis of a step's wall geometry (pathSegment, source/photon_mod.f90:
+// 1882-2084), written without branches so that the three axes' arithmetic
+// interleaves; every value is the reference's expression, so the results are
+// those of its branch-by-branch form.  A holds the axis (cell centres) as
+// A[0] .. A[n-1], the reference's A(1) .. A(n); a is a 1-based cell index.
+template <typename R>
+struct AxisVals { R m2, m1, c0, p1, p2, first, last; };   // A(a-2) .. A(a+2) (clamped), A(1), A(n)
+
+template <typename R>
+__device__ __forceinline__ AxisVals<R> axisLoad(const float* A, int n, int a) {
+  auto at = [&](int i) { i = i < 1 ? 1 : (i > n ? n : i); return (R)A[i - 1]; };
+  return AxisVals<R>{at(a - 2), at(a - 1), at(a), at(a + 1), at(a + 2), (R)A[0], (R)A[n - 1]};
+}
+
+// The wall snap: a packet moving toward the wall ahead whose coordinate is
+// within 2 % of it (relative to the signed wall coordinate, as in the
+// reference) is given the next cell index.
+template <typename R>
+__device__ __forceinline__ int axisSnap(const AxisVals<R>& A, int n, int a, R r, R v) {
+  using M = RMath<R>;
+  const R mUp = (A.c0 + A.p1) / R(2);
+  const R mDn = (A.c0 + A.m1) / R(2);
+  const bool up = a < n && v > R(0) && M::div_(M::abs_(r - mUp), mUp) < R(2.e-2);
+  const bool dn = a > 1 && v < R(0) && M::div_(M::abs_(r - mDn), mDn) < R(2.e-2);
+  return up ? a + 1 : (dn ? a - 1 : a);
+}
+
+template <typename R>
+struct AxisStep { R r, v, dS; int a; bool lost; };
+
+// The reflection at the first plane of a symmetric grid, then the distance to
+// the wall ahead; a distance below 1e-5 puts the packet on that wall and in
+// the next cell (lost beyond the grid's last plane).  a0 is the index the step
+// started from (AxisVals holds the axis around it), a the index after the snap.
+template <typename R>
+__device__ __forceinline__ AxisStep<R> axisDistance(const AxisVals<R>& A, int n, int a0, int a, R r, R v,
+                                                    bool symmetric) {
+  using M = RMath<R>;
+  const bool refl = symmetric && r <= A.first;
+  v = (refl && v < R(0)) ? -v : v;
+  r = refl ? A.first : r;
+  const int d = a - a0;                                        // -1, 0 or 1
+  const R ca = d < 0 ? A.m1 : (d > 0 ? A.p1 : A.c0);           // A(a)
+  const R cp = d < 0 ? A.c0 : (d > 0 ? A.p2 : A.p1);           // A(a+1)
+  const R cm = d < 0 ? A.m2 : (d > 0 ? A.c0 : A.m1);           // A(a-1)
+  const R wUp = (cp + ca) / R(2);
+  const R wDn = (ca + cm) / R(2);
+  const bool pos = v > R(0), neg = v < R(0);
+  const R target = pos ? (a < n ? wUp : A.last) : (a > 1 ? wDn : A.first);
+  const R dS = (pos || neg) ? M::div_(target - r, v) : A.last;
+  const bool snap = (pos || neg) && M::abs_(dS) < R(1.e-5);
+  AxisStep<R> o;
+  o.r = snap ? target : r;
+  o.v = v;
+  o.dS = dS;
+  o.a = snap ? (pos ? (a < n ? a + 1 : a) : (a > 1 ? a - 1 : a)) : a;
+  o.lost = snap && pos && a >= n;
+  return o;
 }
 
 // One iteration of pathSegment's main loop (source/photon_mod.f90:1880-4036).
@@ -515,13 +652,13 @@ __device__ __forceinline__ int stepPacket(const DevGrid& g, const Geo& q, const 
   if (xP < 1 || xP > nx || yP < 1 || yP > ny || zP < 1 || zP > nz) { ++lc.errors; return ST_IDLE; }
   R rx = p.x, ry = p.y, rz = p.z, vx = p.vx, vy = p.vy, vz = p.vz;
 
-  // wall-snap heuristics (source/photon_mod.f90:1882-1919), signed divisor as in the reference
-  if (xP < nx) { R m = (AXR(X, xP) + AXR(X, xP + 1)) / R(2); if (vx > R(0) && M::div_(M::abs_(rx - m), m) < R(2.e-2)) xP = xP + 1; }
-  if (xP > 1)  { R m = (AXR(X, xP) + AXR(X, xP - 1)) / R(2); if (vx < R(0) && M::div_(M::abs_(rx - m), m) < R(2.e-2)) xP = xP - 1; }
-  if (yP < ny) { R m = (AXR(Y, yP) + AXR(Y, yP + 1)) / R(2); if (vy > R(0) && M::div_(M::abs_(ry - m), m) < R(2.e-2)) yP = yP + 1; }
-  if (yP > 1)  { R m = (AXR(Y, yP) + AXR(Y, yP - 1)) / R(2); if (vy < R(0) && M::div_(M::abs_(ry - m), m) < R(2.e-2)) yP = yP - 1; }
-  if (zP < nz) { R m = (AXR(Z, zP) + AXR(Z, zP + 1)) / R(2); if (vz > R(0) && M::div_(M::abs_(rz - m), m) < R(2.e-2)) zP = zP + 1; }
-  if (zP > 1)  { R m = (AXR(Z, zP) + AXR(Z, zP - 1)) / R(2); if (vz < R(0) && M::div_(M::abs_(rz - m), m) < R(2.e-2)) zP = zP - 1; }
+  // wall snap (source/photon_mod.f90:1882-1919), one axis at a time without
+  // branches so that the three axes' arithmetic interleaves
+  const int x0 = xP, y0 = yP, z0 = zP;
+  const AxisVals<R> AX = axisLoad<R>(X, nx, xP), AY = axisLoad<R>(Y, ny, yP), AZ = axisLoad<R>(Z, nz, zP);
+  xP = axisSnap<R>(AX, nx, xP, rx, vx);
+  yP = axisSnap<R>(AY, ny, yP, ry, vy);
+  zP = axisSnap<R>(AZ, nz, zP, rz, vz);
 
   // the opacity and volume of the cell the snap leaves the packet in, loaded
   // here so that their latency overlaps the wall-distance arithmetic; loaded
@@ -536,45 +673,17 @@ __device__ __forceinline__ int stepPacket(const DevGrid& g, const Geo& q, const 
     else if (g.lgCompton) { prefetchL1(g.KNsigmaT + p.nuP - 1); prefetchL1(in.ne + cell); }
   }
 
-  // distances from the walls (source/photon_mod.f90:1933-2084); with one
-  // mother grid the reference's inner loop runs exactly once
-  if (q.symmetric()) {
-    if (rx <= AXR(X, 1)) { if (vx < R(0)) vx = -vx; rx = AXR(X, 1); }
-    if (ry <= AXR(Y, 1)) { if (vy < R(0)) vy = -vy; ry = AXR(Y, 1); }
-    if (rz <= AXR(Z, 1)) { if (vz < R(0)) vz = -vz; rz = AXR(Z, 1); }
-  }
-  R dSx, dSy, dSz;
-  bool lost = false;
-  if (vx > R(0)) {
-    if (xP < nx) { dSx = M::div_((AXR(X, xP + 1) + AXR(X, xP)) / R(2) - rx, vx);
-                   if (M::abs_(dSx) < R(1.e-5)) { rx = (AXR(X, xP + 1) + AXR(X, xP)) / R(2); xP = xP + 1; } }
-    else { dSx = M::div_(AXR(X, nx) - rx, vx); if (M::abs_(dSx) < R(1.e-5)) { rx = AXR(X, nx); lost = true; } }
-  } else if (vx < R(0)) {
-    if (xP > 1) { dSx = M::div_((AXR(X, xP) + AXR(X, xP - 1)) / R(2) - rx, vx);
-                  if (M::abs_(dSx) < R(1.e-5)) { rx = (AXR(X, xP) + AXR(X, xP - 1)) / R(2); xP = xP - 1; } }
-    else { dSx = M::div_(AXR(X, 1) - rx, vx); if (M::abs_(dSx) < R(1.e-5)) rx = AXR(X, 1); }
-  } else dSx = AXR(X, nx);
-  if (lost) { if (p.nEmit >= kRecursionLimit) ++lc.trapped; return ST_IDLE; }
-  if (vy > R(0)) {
-    if (yP < ny) { dSy = M::div_((AXR(Y, yP + 1) + AXR(Y, yP)) / R(2) - ry, vy);
-                   if (M::abs_(dSy) < R(1.e-5)) { ry = (AXR(Y, yP + 1) + AXR(Y, yP)) / R(2); yP = yP + 1; } }
-    else { dSy = M::div_(AXR(Y, ny) - ry, vy); if (M::abs_(dSy) < R(1.e-5)) { ry = AXR(Y, ny); lost = true; } }
-  } else if (vy < R(0)) {
-    if (yP > 1) { dSy = M::div_((AXR(Y, yP) + AXR(Y, yP - 1)) / R(2) - ry, vy);
-                  if (M::abs_(dSy) < R(1.e-5)) { ry = (AXR(Y, yP) + AXR(Y, yP - 1)) / R(2); yP = yP - 1; } }
-    else { dSy = M::div_(AXR(Y, 1) - ry, vy); if (M::abs_(dSy) < R(1.e-5)) ry = AXR(Y, 1); }
-  } else dSy = AXR(Y, ny);
-  if (lost) { if (p.nEmit >= kRecursionLimit) ++lc.trapped; return ST_IDLE; }
-  if (vz > R(0)) {
-    if (zP < nz) { dSz = M::div_((AXR(Z, zP + 1) + AXR(Z, zP)) / R(2) - rz, vz);
-                   if (M::abs_(dSz) < R(1.e-5)) { rz = (AXR(Z, zP + 1) + AXR(Z, zP)) / R(2); zP = zP + 1; } }
-    else { dSz = M::div_(AXR(Z, nz) - rz, vz); if (M::abs_(dSz) < R(1.e-5)) { rz = AXR(Z, nz); lost = true; } }
-  } else if (vz < R(0)) {
-    if (zP > 1) { dSz = M::div_((AXR(Z, zP) + AXR(Z, zP - 1)) / R(2) - rz, vz);
-                  if (M::abs_(dSz) < R(1.e-5)) { rz = (AXR(Z, zP) + AXR(Z, zP - 1)) / R(2); zP = zP - 1; } }
-    else { dSz = M::div_(AXR(Z, 1) - rz, vz); if (M::abs_(dSz) < R(1.e-5)) rz = AXR(Z, 1); }
-  } else dSz = AXR(Z, nz);
-  if (lost) { if (p.nEmit >= kRecursionLimit) ++lc.trapped; return ST_IDLE; }
+  // the symmetric grid's reflection and the distances from the walls
+  // (source/photon_mod.f90:1921-2084); with one mother grid the reference's
+  // inner loop runs exactly once
+  const AxisStep<R> sx = axisDistance<R>(AX, nx, x0, xP, rx, vx, q.symmetric() != 0);
+  const AxisStep<R> sy = axisDistance<R>(AY, ny, y0, yP, ry, vy, q.symmetric() != 0);
+  const AxisStep<R> sz = axisDistance<R>(AZ, nz, z0, zP, rz, vz, q.symmetric() != 0);
+  if (sx.lost || sy.lost || sz.lost) { if (p.nEmit >= kRecursionLimit) ++lc.trapped; return ST_IDLE; }
+  rx = sx.r; vx = sx.v; xP = sx.a;
+  ry = sy.r; vy = sy.v; yP = sy.a;
+  rz = sz.r; vz = sz.v; zP = sz.a;
+  R dSx = sx.dS, dSy = sy.dS, dSz = sz.dS;
   if (xP > nx || xP < 1 || yP > ny || yP < 1 || zP > nz || zP < 1) { ++lc.errors; return ST_IDLE; }
 
   // nearest wall (source/photon_mod.f90:2087-2137)
@@ -634,7 +743,7 @@ __device__ __forceinline__ int stepPacket(const DevGrid& g, const Geo& q, const 
         initPacket<R>(q, sh, p, p.nuP, false, false, xP, yP, zP);
         vx = p.vx; vy = p.vy; vz = p.vz;
         p.absTau = R(0);
-        p.passProb = -M::log_(R(1) - draw(p));
+        p.passProb = drawPassProb(p);
       }
     } else {
       R probSca = g.lgCompton ? (R)__ldg(g.KNsigmaT + p.nuP - 1) * (R)__ldg(in.ne + cell) / kap : R(0);
@@ -645,7 +754,7 @@ __device__ __forceinline__ int stepPacket(const DevGrid& g, const Geo& q, const 
         p.origin = cell;
         vx = p.vx; vy = p.vy; vz = p.vz;
         p.absTau = R(0);
-        p.passProb = -M::log_(R(1) - draw(p));
+        p.passProb = drawPassProb(p);
       } else {
         ++lc.absorptions;
         p.type = PT_DIFFUSE;
@@ -826,7 +935,7 @@ transportKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportC
 // while all lanes run the scalar physics in lockstep.  No shared memory: axes
 // and frequencies are read through L1, which keeps its full size.
 template <typename R>
-__global__ void __launch_bounds__(32)
+__global__ void __launch_bounds__(32, 16)   // 16 histories per SM, 2432 at once on 152 SMs: no spills at 128 registers
 transportTrappedKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportCounters* cnt, double deltaE,
                        const Packet<R>* __restrict__ parked, unsigned long long parkedCap) {
   const unsigned long long written = *reinterpret_cast<volatile unsigned long long*>(&cnt->handoff);
