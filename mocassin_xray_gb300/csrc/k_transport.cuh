@@ -88,6 +88,12 @@ __device__ __forceinline__ Dir3<R> isoDirection(R r1, R r2) {
   return Dir3<R>{cs.c, cs.s, w};
 }
 
+// One lane's share of a warp history's CDF search (see warpCdfIssue).
+struct WarpCdf {
+  float v;          // this lane's segment end
+  int seg, segs;    // segment length (a multiple of 32) and segments probed
+};
+
 template <typename R>
 struct Packet {
   using Real = R;
@@ -189,6 +195,7 @@ struct WarpPacket {
   int xP, yP, zP, nuP, origin;
   int type, lgStellar, nEmit, nStep;
   WarpRng<R> rng;
+  int2 cdfShape;     // warpCdfShape(nbins), computed once per launch
   __device__ __forceinline__ void from(const Packet<R>& a) {
     x = a.x; y = a.y; z = a.z; vx = a.vx; vy = a.vy; vz = a.vz;
     nu = a.nu; absTau = a.absTau; passProb = a.passProb;
@@ -312,15 +319,16 @@ __device__ __forceinline__ int sampleCDF(const float* cdf, int len, int nbins, R
 // one segment that holds the answer.  On a monotone row the count of entries
 // <= u does not depend on the order of the comparisons, so the result equals
 // the bisection's.
-struct WarpCdf {
-  float v;          // this lane's segment end
-  int seg, segs;    // segment length (a multiple of 32) and segments probed
-};
+// the segmentation of an m-entry row (fixed for a launch)
+__device__ __forceinline__ int2 warpCdfShape(int m) {
+  const int seg = 32 * ((m + 1023) / 1024);
+  return make_int2(seg, m / seg);
+}
 
-__device__ __forceinline__ void warpCdfIssue(WarpCdf& c, const float* __restrict__ row, int m) {
+__device__ __forceinline__ void warpCdfIssue(WarpCdf& c, const float* __restrict__ row, int2 shape) {
   const int lane = threadIdx.x & 31;
-  c.seg = 32 * ((m + 1023) / 1024);
-  c.segs = m / c.seg;
+  c.seg = shape.x;
+  c.segs = shape.y;
   c.v = lane < c.segs ? __ldg(row + (size_t)(lane + 1) * c.seg - 1) : 0.f;
 }
 
@@ -437,10 +445,16 @@ struct PendingJ {
   bool on;
 };
 
+// The exact rounding error of old + v by Fast2Sum (Dekker): with |a| >= |b|,
+// b - ((a + b) - a) is exact, three dependent operations where TwoSum takes
+// five; the error of a rounded sum is unique, so it is TwoSum's value.  Added
+// without a test for zero (adding zero leaves the entry as it is).
 __device__ __forceinline__ void flushJ(const DevTransportOut& out, PendingJ& pj) {
   if (pj.on) {
-    const double err = mcx_fm_two_sum_err(pj.old, pj.v, pj.old + pj.v);
-    if (err != 0.) atomicAdd(out.jlo + pj.idx, err);
+    const double s = pj.old + pj.v;
+    const bool ord = fabs(pj.old) >= fabs(pj.v);
+    const double big = ord ? pj.old : pj.v, small = ord ? pj.v : pj.old;
+    atomicAdd(out.jlo + pj.idx, small - (s - big));
     pj.on = false;
   }
 }
@@ -532,7 +546,7 @@ __device__ __forceinline__ int emitBody(const DevGrid& g, const Geo& q, const De
     const float* cdfTab = p.type == PT_DIFFUSE ? in.recCDFT : in.dustCDFT;
     const float* row = cdfTab ? cdfTab + (size_t)cell * g.nbins : nullptr;
     WarpCdf wc;
-    if constexpr (P::kWarp) { if (row) warpCdfIssue(wc, row, g.nbins); }
+    if constexpr (P::kWarp) { if (row) warpCdfIssue(wc, row, p.cdfShape); }
     else if (p.nEmit > kTrappedHint && row) prefetchRowL1(row, g.nbins);
     auto sample = [&](R u) {
       if constexpr (P::kWarp) return warpCdfFinish<R>(wc, row, g.nbins, g.nbins, u);
@@ -668,7 +682,14 @@ __device__ __forceinline__ int stepPacket(const DevGrid& g, const Geo& q, const 
   R kap = (R)__ldg(in.opacity + (size_t)cell + C1 * (size_t)(p.nuP - 1));
   R dV = cell > 0 ? cellVolume<R>(g, cell) : R(1);
   const int xS = xP, yS = yP, zS = zP;
-  if (p.nEmit > kTrappedHint) {
+  // the scattering inputs: for a warp history loaded here with the opacity
+  // (registers are plentiful there), for a trapped lane of the main kernel
+  // prefetched into L1
+  R scaIn = R(0), knIn = R(0), neIn = R(0);
+  if constexpr (P::kWarp) {
+    if (g.lgDust) scaIn = (R)__ldg(in.scaOpac + (size_t)cell + C1 * (size_t)(p.nuP - 1));
+    else if (g.lgCompton) { knIn = (R)__ldg(g.KNsigmaT + p.nuP - 1); neIn = (R)__ldg(in.ne + cell); }
+  } else if (p.nEmit > kTrappedHint) {
     if (g.lgDust) prefetchL1(in.scaOpac + (size_t)cell + C1 * (size_t)(p.nuP - 1));
     else if (g.lgCompton) { prefetchL1(g.KNsigmaT + p.nuP - 1); prefetchL1(in.ne + cell); }
   }
@@ -702,6 +723,10 @@ __device__ __forceinline__ int stepPacket(const DevGrid& g, const Geo& q, const 
     cell = activeAt(q, xP, yP, zP);
     kap = (R)__ldg(in.opacity + (size_t)cell + C1 * (size_t)(p.nuP - 1));
     dV = cell > 0 ? cellVolume<R>(g, cell) : R(1);
+    if constexpr (P::kWarp) {
+      if (g.lgDust) scaIn = (R)__ldg(in.scaOpac + (size_t)cell + C1 * (size_t)(p.nuP - 1));
+      else if (g.lgCompton) neIn = (R)__ldg(in.ne + cell);
+    }
   }
   const R tauCell = dS * kap;
   R costheta = R(1);
@@ -732,7 +757,7 @@ __device__ __forceinline__ int stepPacket(const DevGrid& g, const Geo& q, const 
       return ST_IDLE;
     }
     if (g.lgDust) {
-      R probSca = (R)__ldg(in.scaOpac + (size_t)cell + C1 * (size_t)(p.nuP - 1)) / kap;
+      R probSca = (P::kWarp ? scaIn : (R)__ldg(in.scaOpac + (size_t)cell + C1 * (size_t)(p.nuP - 1))) / kap;
       R rnd = R(1) - draw(p);
       if (rnd > probSca) {
         ++lc.absorptions;
@@ -746,7 +771,11 @@ __device__ __forceinline__ int stepPacket(const DevGrid& g, const Geo& q, const 
         p.passProb = drawPassProb(p);
       }
     } else {
-      R probSca = g.lgCompton ? (R)__ldg(g.KNsigmaT + p.nuP - 1) * (R)__ldg(in.ne + cell) / kap : R(0);
+      R probSca = R(0);
+      if (g.lgCompton) {
+        if constexpr (P::kWarp) probSca = knIn * neIn / kap;
+        else probSca = (R)__ldg(g.KNsigmaT + p.nuP - 1) * (R)__ldg(in.ne + cell) / kap;
+      }
       R rnd = R(1) - draw(p);
       if (rnd <= probSca) {
         ++lc.scatterings;
@@ -948,9 +977,11 @@ transportTrappedKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTra
   // the first gridDim.x histories one per warp, the rest from a queue as
   // warps finish (most parked histories end within a few hundred events; a
   // trapped one runs to recursionLimit)
+  const int2 cdfShape = warpCdfShape(g.nbins);
   for (unsigned long long i = blockIdx.x; i < count;) {
     WarpPacket<R> p;
     p.from(parked[i]);
+    p.cdfShape = cdfShape;
     int state = ST_EMIT;
     while (state == ST_EMIT || state == ST_STEP) {
       if (state == ST_EMIT) state = emitBody<R, OneGrid>(g, q, in, out, sh, p, deltaE, lc);
