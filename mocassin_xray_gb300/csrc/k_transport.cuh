@@ -32,7 +32,7 @@
 namespace mcx {
 
 enum : int { PT_STELLAR = 0, PT_DIFFUSE = 1, PT_DUSTEMI = 2 };
-enum : int { ST_IDLE = 0, ST_EMIT = 1, ST_STEP = 2, ST_DONE = 3 };
+enum : int { ST_IDLE = 0, ST_EMIT = 1, ST_STEP = 2, ST_DONE = 3, ST_ESCAPE = 4 };
 
 constexpr int kSafeLimit = 500000;        // pathSegment (source/photon_mod.f90:1873-1878)
 constexpr int kRecursionLimit = 100000;   // recursionLimit (source/constants_mod.f90:70)
@@ -533,12 +533,15 @@ __device__ __forceinline__ int emitBody(const DevGrid& g, const Geo& q, const De
   if (p.nEmit >= kRecursionLimit) { ++lc.trapped; return ST_IDLE; }
   ++p.nEmit;
   bool line = false;
-  if (p.type == PT_STELLAR) {
-    int nuP = sampleCDF<R>(q.cdf(), g.nbins, g.nbins, draw(p));
+  const bool stellar = p.type == PT_STELLAR;
+  // the frequency first, then one initPacket for every kind of emission (one
+  // copy of the direction code keeps the loop within the instruction cache)
+  int nuP = 0, ix = p.xP, iy = p.yP, iz = p.zP;
+  if (stellar) {
+    nuP = sampleCDF<R>(q.cdf(), g.nbins, g.nbins, draw(p));
     ++lc.emissions;
     p.x = (R)q.starPos(0); p.y = (R)q.starPos(1); p.z = (R)q.starPos(2);
-    initPacket<R>(q, sh, p, nuP, false, true, q.starIdx(0), q.starIdx(1), q.starIdx(2));
-    if (p.nu >= R(1)) lc.qPhot += deltaE / (2.1799153e-11 * (double)p.nu);
+    ix = q.starIdx(0); iy = q.starIdx(1); iz = q.starIdx(2);
   } else {
     if (p.xP < 1 || p.xP > q.nx() || p.yP < 1 || p.yP > q.ny() || p.zP < 1 || p.zP > q.nz()) { ++lc.errors; return ST_IDLE; }
     int cell = activeAt(q, p.xP, p.yP, p.zP);
@@ -555,19 +558,18 @@ __device__ __forceinline__ int emitBody(const DevGrid& g, const Geo& q, const De
     if (p.type == PT_DIFFUSE) {
       R rnd = R(1) - draw(p);
       if (rnd <= (R)__ldg(in.totalLines + cell)) {
-        initPacket<R>(q, sh, p, 0, true, false, p.xP, p.yP, p.zP);
         line = true;
       } else {
-        int nuP = sample(draw(p));
+        nuP = sample(draw(p));
         ++lc.emissions;
-        initPacket<R>(q, sh, p, nuP, false, false, p.xP, p.yP, p.zP);
       }
     } else {
-      int nuP = sample(draw(p));
+      nuP = sample(draw(p));
       ++lc.emissions;
-      initPacket<R>(q, sh, p, nuP, false, false, p.xP, p.yP, p.zP);
     }
   }
+  initPacket<R>(q, sh, p, nuP, line, stellar, ix, iy, iz);
+  if (stellar && p.nu >= R(1)) lc.qPhot += deltaE / (2.1799153e-11 * (double)p.nu);
   if (line) {
     ++lc.lineEscapes;
     if (p.nEmit >= kRecursionLimit) ++lc.trapped;
@@ -652,9 +654,10 @@ __device__ __forceinline__ AxisStep<R> axisDistance(const AxisVals<R>& A, int n,
   return o;
 }
 
-// One iteration of pathSegment's main loop (source/photon_mod.f90:1880-4036).
+// One iteration of pathSegment's main loop (source/photon_mod.f90:1880-4036);
+// ST_ESCAPE when the packet leaves the grid or R_out (tallied by stepPacket).
 template <typename R, typename Geo, typename P>
-__device__ __forceinline__ int stepPacket(const DevGrid& g, const Geo& q, const DevTransportIn& in,
+__device__ __forceinline__ int stepCore(const DevGrid& g, const Geo& q, const DevTransportIn& in,
                                           const DevTransportOut& out, const TransportShared<R>& sh, P& p,
                                           R deltaER, double deltaE, LocalCounters& lc, PendingJ& pj) {
   using M = RMath<R>;
@@ -752,9 +755,7 @@ __device__ __forceinline__ int stepPacket(const DevGrid& g, const Geo& q, const 
     if (q.rOut() > 0.f &&
         M::sqrt_((rx / R(1.e10)) * (rx / R(1.e10)) + (ry / R(1.e10)) * (ry / R(1.e10)) +
                  (rz / R(1.e10)) * (rz / R(1.e10))) * R(1.e10) >= (R)q.rOut()) {
-      escapeTally<R>(g, out, p, deltaE, lc);
-      if (p.nEmit >= kRecursionLimit) ++lc.trapped;
-      return ST_IDLE;
+      return ST_ESCAPE;
     }
     if (g.lgDust) {
       R probSca = (P::kWarp ? scaIn : (R)__ldg(in.scaOpac + (size_t)cell + C1 * (size_t)(p.nuP - 1))) / kap;
@@ -817,9 +818,7 @@ __device__ __forceinline__ int stepPacket(const DevGrid& g, const Geo& q, const 
                  rx >= AXR(X, nx) || ry >= AXR(Y, ny) || rz >= AXR(Z, nz) || xP > nx || yP > ny || zP > nz))
       esc = true;
     if (esc) {
-      escapeTally<R>(g, out, p, deltaE, lc);
-      if (p.nEmit >= kRecursionLimit) ++lc.trapped;
-      return ST_IDLE;
+      return ST_ESCAPE;
     }
     if (q.symmetric()) {
       if (rx <= AXR(X, 1) || xP < 1) { if (vx < R(0)) vx = -vx; xP = 1; rx = AXR(X, 1); }
@@ -829,14 +828,24 @@ __device__ __forceinline__ int stepPacket(const DevGrid& g, const Geo& q, const 
   }
   // source/photon_mod.f90:3951-4036
   if (next == ST_STEP && (xP > nx || yP > ny || zP > nz)) {
-    escapeTally<R>(g, out, p, deltaE, lc);
-    if (p.nEmit >= kRecursionLimit) ++lc.trapped;
-    return ST_IDLE;
+    return ST_ESCAPE;
   }
   p.x = rx; p.y = ry; p.z = rz; p.vx = vx; p.vy = vy; p.vz = vz;
   p.xP = xP; p.yP = yP; p.zP = zP;
   return next;
 #undef AXR
+}
+
+// A step and, for a packet that leaves, its escape tally (one copy of it).
+template <typename R, typename Geo, typename P>
+__device__ __forceinline__ int stepPacket(const DevGrid& g, const Geo& q, const DevTransportIn& in,
+                                          const DevTransportOut& out, const TransportShared<R>& sh, P& p,
+                                          R deltaER, double deltaE, LocalCounters& lc, PendingJ& pj) {
+  const int st = stepCore<R>(g, q, in, out, sh, p, deltaER, deltaE, lc, pj);
+  if (st != ST_ESCAPE) return st;
+  escapeTally<R>(g, out, p, deltaE, lc);
+  if (p.nEmit >= kRecursionLimit) ++lc.trapped;
+  return ST_IDLE;
 }
 
 // one atomic per counter per warp
