@@ -975,9 +975,12 @@ transportKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportC
 template <typename R>
 __global__ void __launch_bounds__(32, 16)   // 16 histories per SM, 2432 at once on 152 SMs: no spills at 128 registers
 transportTrappedKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportCounters* cnt, double deltaE,
-                       const Packet<R>* __restrict__ parked, unsigned long long parkedCap) {
+                       const Packet<R>* __restrict__ parked, unsigned long long parkedCap,
+                       unsigned long long warpMax) {
   const unsigned long long written = *reinterpret_cast<volatile unsigned long long*>(&cnt->handoff);
   const unsigned long long count = written < parkedCap ? written : parkedCap;
+  // many more histories than resident warps: transportTrappedLanesKernel runs them
+  if (count > warpMax) return;
   TransportShared<R> sh{g.nu};
   const OneGrid q{g, g.xAxis, g.yAxis, g.zAxis, g.srcCDF};
   const R deltaER = (R)deltaE;
@@ -1002,6 +1005,54 @@ transportTrappedKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTra
   }
   flushJ(out, pj);
   if ((threadIdx.x & 31u) != 0u) lc = LocalCounters{};   // every lane counted the same events
+  flushCounters(lc, cnt);
+}
+
+// The trapped-packet kernel for many parked histories (more than the warp
+// kernel holds resident at once, e.g. tens of thousands on an X-ray-heated
+// grid): one history per lane, taken from the parked queue as lanes free up,
+// with the main kernel's emission batching; the warp kernel's single-history
+// latency matters less here than running every history at once.  Histories
+// in registers, event code inlined, no shared memory.
+template <typename R>
+__global__ void __launch_bounds__(128)
+transportTrappedLanesKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportCounters* cnt,
+                            double deltaE, const Packet<R>* __restrict__ parked, unsigned long long parkedCap,
+                            unsigned long long warpMax, int emitBatch) {
+  const unsigned long long written = *reinterpret_cast<volatile unsigned long long*>(&cnt->handoff);
+  const unsigned long long count = written < parkedCap ? written : parkedCap;
+  if (count <= warpMax) return;   // transportTrappedKernel has them, one per warp
+  TransportShared<R> sh{g.nu};
+  const OneGrid q{g, g.xAxis, g.yAxis, g.zAxis, g.srcCDF};
+  const R deltaER = (R)deltaE;
+  const unsigned FULL = 0xffffffffu;
+  const unsigned lane = threadIdx.x & 31u;
+  LocalCounters lc;
+  PendingJ pj{0., 0., 0, false};
+  Packet<R> p;
+  p.nEmit = 0;
+  int state = ST_IDLE;
+  for (;;) {
+    const unsigned need = __ballot_sync(FULL, state == ST_IDLE);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long first = 0;
+      if ((int)lane == leader) first = atomicAdd(&cnt->parkedNext, (unsigned long long)__popc(need));
+      first = __shfl_sync(FULL, first, leader);
+      const unsigned long long id = first + (unsigned long long)__popc(need & ((1u << lane) - 1u));
+      if (state == ST_IDLE) {
+        if (id < count) { p = parked[id]; state = ST_EMIT; }
+        else state = ST_DONE;
+      }
+    }
+    if (__ballot_sync(FULL, state != ST_DONE) == 0u) break;
+    if (emitTurn(state, emitBatch)) {
+      if (state == ST_EMIT) state = emitBody<R, OneGrid>(g, q, in, out, sh, p, deltaE, lc);
+    } else if (state == ST_STEP) {
+      state = stepPacket<R>(g, q, in, out, sh, p, deltaER, deltaE, lc, pj);
+    }
+  }
+  flushJ(out, pj);
   flushCounters(lc, cnt);
 }
 
@@ -1119,12 +1170,29 @@ cudaError_t launchTransportImpl(const DevGrid& g, const DevTransportIn& in, cons
                                                        hand ? L.parkedCap : 0ull, hand ? L.handoffAt : 0);
   e = cudaGetLastError();
   if (e != cudaSuccess || !hand) return e;
-  int perSM = 0;
+  // both continuation kernels; each reads the parked count and only one works:
+  // one history per warp up to three times the resident warps (most parked
+  // histories end within a few hundred events, so the queue keeps the
+  // trapped ones running in the first waves; measured on the 41^3 lognormal
+  // run), one per lane beyond (the 41^3 X-ray run parks ~2e4 trapped histories,
+  // which would take ten waves one per warp)
+  int perSM = 0, lanesPerSM = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, transportTrappedKernel<R>, 32, 0);
   if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lanesPerSM, transportTrappedLanesKernel<R>, 128, 0);
+  if (e != cudaSuccess) return e;
   if (perSM < 1) perSM = 1;
-  transportTrappedKernel<R><<<L.numSMs * perSM, 32, 0, s>>>(g, in, out, cnt, deltaE,
-                                                            static_cast<const Packet<R>*>(L.parked), L.parkedCap);
+  if (lanesPerSM < 1) lanesPerSM = 1;
+  const unsigned long long warpSlots = (unsigned long long)L.numSMs * perSM;
+  const unsigned long long warpMax = 3 * warpSlots;
+  transportTrappedKernel<R><<<(unsigned)warpSlots, 32, 0, s>>>(g, in, out, cnt, deltaE,
+                                                               static_cast<const Packet<R>*>(L.parked), L.parkedCap,
+                                                               warpMax);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  transportTrappedLanesKernel<R><<<L.numSMs * lanesPerSM, 128, 0, s>>>(
+      g, in, out, cnt, deltaE, static_cast<const Packet<R>*>(L.parked), L.parkedCap, warpMax,
+      L.emitBatch > 0 ? L.emitBatch : kEmitBatch);
   return cudaGetLastError();
 }
 

@@ -54,11 +54,13 @@ def test_fp64_transport_matches_oracle(decks, data_dir, oracle_lib, name):
 
 @pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_FP32_GEOM])
 def test_trapped_handoff_changes_nothing(decks, data_dir, oracle_lib, precision):
-    """Histories moved to the trapped-packet kernel (after 1 or 3
-    re-emissions here, so that every re-emitted history moves) give the same J
-    bits, the same event counts and the same escapes as histories kept in the
-    main kernel, also when more histories qualify than the 65536 the parking
-    buffer holds (the rest stay in place); the FP64 path also equals the oracle."""
+    """Histories moved to the trapped-packet kernels (after 1 or 3
+    re-emissions here, so that every re-emitted history moves: ~1e4 of 1e5
+    packets, run one per warp, and at 8e5 packets more than 7300, run one per
+    lane) give the same J bits, the same event counts and the same escapes as
+    histories kept in the main kernel, also when more histories qualify than
+    the 65536 the parking buffer holds (the rest stay in place); the FP64 path
+    also equals the oracle."""
     s, op, rec, tl, ctx = _case(decks, data_dir, oracle_lib, "lognormal_small")
     n, seed = 100000, 4321
     ref = ctx.transport(n, seed=seed, precision=precision, handoff_emissions=-1)
