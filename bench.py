@@ -43,10 +43,12 @@ METRIC = "MC packets/s"
 UNIT = "packets/s"
 # kernels of one step: opacity 1; emission 7 (Gaunt table, the cells' places on
 # the surfaces, forbidden lines per ion and their sum, the two passes of the
-# emissivity, CDF transpose); transport 1; J normalisation 1; balance 64 (hit
-# test + Compton sums, shell integrals, state load, 20 rounds x (rates, line
-# cooling from the cooling surfaces, secant), store)
-KERNELS_PER_STEP = 1 + 7 + 1 + 1 + 64
+# emissivity, CDF transpose); transport 3 (the persistent kernel, then the two
+# trapped-packet kernels, of which one runs the parked histories and the other
+# returns at once); J normalisation 1; balance 64 (hit test + Compton sums,
+# shell integrals, state load, 20 rounds x (rates, line cooling from the
+# cooling surfaces, secant), store)
+KERNELS_PER_STEP = 1 + 7 + 3 + 1 + 64
 
 
 def parse():
@@ -564,11 +566,16 @@ def run_gpu(args, dist, ws, rank, local):
                 "d2h_bytes_per_step": h2d},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None if not tr else tr["dram_bytes_per_update"] * upd,
-                     "kernel": "transportKernel<float>", "peak_kind": peak_kind, "alg_bytes_per_launch": alg,
-                     "kernel_ms": kms,
+                     "kernel": "transport: transportKernel<float> + transportTrappedKernel<float> (or "
+                               "transportTrappedLanesKernel<float>), one launch sequence per iteration",
+                     "peak_kind": peak_kind, "alg_bytes_per_launch": alg, "kernel_ms": kms,
+                     "traffic_is": "DRAM bytes per estimator update of the three transport kernels of iteration 4 "
+                                   "(profiles/transport_traffic.json) x the updates of the mean timed launch",
                      "note": "mean over the timed steps; from the 4th iteration on, packets re-emitted in "
-                             "optically thick cold cells run up to the reference's 100000 re-emissions, a "
-                             "serial chain of events on one lane that sets the launch's length"},
+                             "optically thick cold cells run up to the reference's 100000 re-emissions: each "
+                             "such history is a serial chain of emission + step events (one warp per history "
+                             "in the trapped-packet kernel), which sets the launch's length; latency-bound, "
+                             "not bandwidth-bound"},
         "roofline_first_iteration": {"achieved": alg1 / (kms1 / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
                                      "frac": alg1 / (kms1 / 1e3) / 1e9 / peak, "alg_bytes_per_launch": alg1,
                                      "kernel_ms": kms1,
@@ -596,7 +603,10 @@ def run_gpu(args, dist, ws, rank, local):
                        "emissions", "trapped", "kernel_ms")},
         "transport_per_iteration": {str(it): {"kernel_ms": float(np.mean([s.kernel_ms for s, _, _ in per_it[it]])),
                                               "trapped": int(per_it[it][0][0].trapped),
-                                              "interactions": int(per_it[it][0][0].interactions)} for it in its},
+                                              "handed_off": int(per_it[it][0][0].handed_off),
+                                              "updates": int(per_it[it][0][0].crossings + per_it[it][0][0].interactions)}
+                                    for it in its},
+        "untimed_run_updates": {str(k + 1): int(st.crossings + st.interactions) for k, (st, _, _) in enumerate(prep)},
     }
     if clk:
         line["clocks"] = clk
@@ -821,8 +831,8 @@ def run_dust(args, dist, ws, rank, local):
                    "timing": "each step timed alone (CUDA events); the opacity and Tdust reloads between steps "
                              "are outside", "parallelism": "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "transportKernel<float>", "peak_kind": peak_kind,
-                     "alg_bytes_per_launch": alg_bytes, "kernel_ms": kms},
+                     "traffic": None, "kernel": "transport: transportKernel<float> + the trapped-packet kernels",
+                     "peak_kind": peak_kind, "alg_bytes_per_launch": alg_bytes, "kernel_ms": kms},
         "phase_ms": {k: float(np.mean([r[2][k] for r in runs])) for k in runs[0][2]},
         "plain_fp64_gpu": None if not plain else {
             "ms_per_step": float(np.mean([r[0] for r in plain])),
@@ -830,7 +840,9 @@ def run_dust(args, dist, ws, rank, local):
             "speedup_of_production": float(np.mean([r[0] for r in plain])) / ms_step},
         "transport": {k: float(np.mean([getattr(t, k) for t in tst])) for k in
                       ("crossings", "interactions", "absorptions", "scatterings", "escaped", "emissions",
-                       "trapped", "kernel_ms")},
+                       "trapped", "handed_off", "kernel_ms")},
+        # grain opacity 1; grain emission CDF 2 (PDF, transpose); transport 3; J normalisation 1; grain T 1
+        "gpu_launches": (1 + 2 + 3 + 1 + 1) * args.steps,
     }
     if clk:
         line["clocks"] = clk
