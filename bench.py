@@ -685,7 +685,6 @@ def run_batch(args, dist, ws, rank, local):
     alg_bytes = upd * 20.0 + emis * math.ceil(math.log2(nb)) * 4.0
     achieved = alg_bytes / (kms / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
-    tr = profiled_traffic()
 
     # e2e: the batched step with the state of every nebula uploaded from pinned host memory and read back
     te = torch.from_numpy(ctx.get(abi.ARR_TE)).pin_memory()
@@ -750,8 +749,7 @@ def run_batch(args, dist, ws, rank, local):
         "e2e": {"value": ws * total_packets / (ms_e2e_step / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": h2d},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None if not tr else tr["dram_bytes_per_update"] * upd,
-                     "kernel": "transportKernelBatched<float>", "peak_kind": peak_kind,
+                     "traffic": None, "kernel": "transportKernelBatched<float>", "peak_kind": peak_kind,
                      "alg_bytes_per_launch": alg_bytes, "kernel_ms": kms},
         "gpu_launches": (KERNELS_PER_STEP + len(setups)) * args.steps,
         "phase_ms": {"opacity": float(np.mean([st.opacity.kernel_ms for st in stats])),
