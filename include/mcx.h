@@ -187,7 +187,9 @@ typedef struct mcx_setup_info {
                                    (0..2); MCX_ARR_ESCAPED then holds 1 + n_angle_bins planes */
     float   view_theta[2];      /* viewPointTheta(1:2) [rad]                           */
     float   view_phi[2];        /* viewPointPhi(1:2) [rad]; < 0: no phi dependence     */
-    int32_t reserved[3];
+    int32_t plane_ionization;   /* 1: lgPlaneIonization (the source is the plane y = 0,
+                                   l_star = transferred flux x the x-z extent)         */
+    int32_t reserved[2];
 } mcx_setup_info;
 
 int  mcx_setup_from_input(const char* input_file, const char* data_dir,

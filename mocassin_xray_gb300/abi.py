@@ -59,7 +59,8 @@ class SetupInfo(C.Structure):
                 ("n_sizes", C.c_int32), ("star_pos", C.c_float * 3), ("r_out", C.c_float), ("r_in", C.c_float),
                 ("l_star", C.c_float), ("l_phot", C.c_float), ("ion_edge1", C.c_float), ("te_start", C.c_float),
                 ("min_convergence", C.c_float), ("xhi_limit", C.c_float), ("n_angle_bins", C.c_int32),
-                ("view_theta", C.c_float * 2), ("view_phi", C.c_float * 2), ("reserved", C.c_int32 * 3)]
+                ("view_theta", C.c_float * 2), ("view_phi", C.c_float * 2), ("plane_ionization", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
 
 
 class BalanceOpts(C.Structure):

@@ -35,6 +35,7 @@ enum : int { PT_STELLAR = 0, PT_DIFFUSE = 1, PT_DUSTEMI = 2 };
 enum : int { ST_IDLE = 0, ST_EMIT = 1, ST_STEP = 2, ST_DONE = 3, ST_ESCAPE = 4 };
 
 constexpr int kSafeLimit = 500000;        // pathSegment (source/photon_mod.f90:1873-1878)
+constexpr int kSafeLimitPlane = 5000;     // the same, plane-parallel ionisation
 constexpr int kRecursionLimit = 100000;   // recursionLimit (source/constants_mod.f90:70)
 
 template <typename R> struct RMath;
@@ -99,6 +100,7 @@ struct Packet {
   using Real = R;
   static constexpr bool kWarp = false;   // one lane per history
   R x, y, z, vx, vy, vz;
+  R ex, ey, ez;     // the direction the current path segment started with (the escape tally's)
   R nu, absTau, passProb;
   int xP, yP, zP, nuP, origin;
   int type, lgStellar, nEmit, nStep;
@@ -191,6 +193,7 @@ struct WarpPacket {
   using Real = R;
   static constexpr bool kWarp = true;
   R x, y, z, vx, vy, vz;
+  R ex, ey, ez;
   R nu, absTau, passProb;
   int xP, yP, zP, nuP, origin;
   int type, lgStellar, nEmit, nStep;
@@ -198,6 +201,7 @@ struct WarpPacket {
   int2 cdfShape;     // warpCdfShape(nbins), computed once per launch
   __device__ __forceinline__ void from(const Packet<R>& a) {
     x = a.x; y = a.y; z = a.z; vx = a.vx; vy = a.vy; vz = a.vz;
+    ex = a.ex; ey = a.ey; ez = a.ez;
     nu = a.nu; absTau = a.absTau; passProb = a.passProb;
     xP = a.xP; yP = a.yP; zP = a.zP; nuP = a.nuP; origin = a.origin;
     type = a.type; lgStellar = a.lgStellar; nEmit = a.nEmit; nStep = a.nStep;
@@ -247,6 +251,7 @@ struct OneGrid {
   __device__ __forceinline__ const float* Z() const { return sZ; }
   __device__ __forceinline__ const int32_t* active() const { return g.active; }
   __device__ __forceinline__ bool activeFull() const { return g.activeFull != 0; }
+  __device__ __forceinline__ bool plane() const { return g.plane != 0; }
   __device__ __forceinline__ const float* cdf() const { return sCdf; }
   __device__ __forceinline__ int starIdx(int d) const { return g.starIdx[d]; }
   __device__ __forceinline__ float starPos(int d) const { return g.starPos[d]; }
@@ -270,6 +275,7 @@ struct NebulaGeo {
   __device__ __forceinline__ const float* Z() const { return Z_; }
   __device__ __forceinline__ const int32_t* active() const { return active_; }
   __device__ __forceinline__ bool activeFull() const { return false; }
+  __device__ __forceinline__ bool plane() const { return false; }
   __device__ __forceinline__ const float* cdf() const { return cdf_; }
   __device__ __forceinline__ int starIdx(int d) const { return starIdx_[d]; }
   __device__ __forceinline__ float starPos(int d) const { return starPos_[d]; }
@@ -361,6 +367,22 @@ __device__ __forceinline__ typename P::Real drawPassProb(P& p) {
   else return -RMath<R>::log_(R(1) - draw(p));
 }
 
+// locate (source/interpolation_mod.f90:49-106) on the frequency mesh or an axis
+template <typename R>
+__device__ __forceinline__ int locateNu(const float* xa, int n, R x) {
+  if (x > (R)xa[n - 1]) return n;
+  if (x < (R)xa[0]) return 0;
+  int jlow = 0, jup = n + 1;
+  for (int it = 0; it < 64; ++it) {
+    if (jup - jlow < 1) break;
+    int jm = (jup + jlow) >> 1;
+    R v = (R)xa[jm - 1];
+    if (v == x) return jm;
+    if (x > v) { if (jlow == jm) break; jlow = jm; } else jup = jm;
+  }
+  return jlow;
+}
+
 // initPhotonPacket (source/photon_mod.f90:744-896): position, frequency, an
 // isotropic direction (re-drawn while a component is exactly zero) and the
 // octant fold for stellar packets.
@@ -371,24 +393,46 @@ __device__ __forceinline__ void initPacket(const Geo& q, const TransportShared<R
   p.nuP = nuP;
   p.lgStellar = stellar;
   p.nu = line ? R(0) : (R)sh.nu[nuP - 1];
-  p.xP = xP; p.yP = yP; p.zP = zP;
-  for (int rep = 0; rep < 1000000; ++rep) {
-    Dir3<R> d;
-    if constexpr (P::kWarp) {
-      d = p.rng.direction();
-    } else {
-      const R r1 = draw(p);
-      const R r2 = draw(p);
-      d = isoDirection<R>(r1, r2);
+  if (stellar && q.plane()) {
+    // the ionising plane (source/photon_mod.f90:795-856): born on y = 0 at a
+    // uniform (x, z) within the axes' span, in the cell whose walls bracket it,
+    // moving along +y
+    const float* X = q.X(); const float* Z = q.Z();
+    const int nx = q.nx(), nz = q.nz();
+    R rnd = R(1) - draw(p);
+    p.x = (R)X[0] + rnd * ((R)X[nx - 1] - (R)X[0]);
+    xP = locateNu<R>(X, nx, p.x);
+    if (xP < nx && xP > 0 && p.x >= ((R)X[xP - 1] + (R)X[xP]) / R(2)) xP = xP + 1;
+    p.y = R(0);
+    yP = 1;
+    rnd = R(1) - draw(p);
+    p.z = (R)Z[0] + rnd * ((R)Z[nz - 1] - (R)Z[0]);
+    zP = locateNu<R>(Z, nz, p.z);
+    if (zP < nz && zP > 0 && p.z >= ((R)Z[zP - 1] + (R)Z[zP]) / R(2)) zP = zP + 1;
+    if (xP < 1) xP = 1;
+    if (zP < 1) zP = 1;
+    p.vx = R(0); p.vy = R(1); p.vz = R(0);
+  } else {
+    for (int rep = 0; rep < 1000000; ++rep) {
+      Dir3<R> d;
+      if constexpr (P::kWarp) {
+        d = p.rng.direction();
+      } else {
+        const R r1 = draw(p);
+        const R r2 = draw(p);
+        d = isoDirection<R>(r1, r2);
+      }
+      p.vx = d.x; p.vy = d.y; p.vz = d.z;
+      if (p.vx != R(0) && p.vy != R(0) && p.vz != R(0)) break;
     }
-    p.vx = d.x; p.vy = d.y; p.vz = d.z;
-    if (p.vx != R(0) && p.vy != R(0) && p.vz != R(0)) break;
+    if (q.symmetric() && stellar) {
+      if (p.vx < R(0)) p.vx = -p.vx;
+      if (p.vy < R(0)) p.vy = -p.vy;
+      if (p.vz < R(0)) p.vz = -p.vz;
+    }
   }
-  if (q.symmetric() && stellar) {
-    if (p.vx < R(0)) p.vx = -p.vx;
-    if (p.vy < R(0)) p.vy = -p.vy;
-    if (p.vz < R(0)) p.vz = -p.vz;
-  }
+  p.xP = xP; p.yP = yP; p.zP = zP;
+  p.ex = p.vx; p.ey = p.vy; p.ez = p.vz;
   p.origin = (xP > 0 && yP > 0 && zP > 0) ? activeAt(q, xP, yP, zP) : 0;
 }
 
@@ -426,7 +470,9 @@ __device__ __forceinline__ void escapeTally(const DevGrid& g, const DevTransport
   const size_t plane = ((size_t)g.nCells + 1) * ((size_t)g.nbins + 1);
   const size_t at = (size_t)p.origin + ((size_t)g.nCells + 1) * (size_t)p.nuP;
   if (g.nAngle > 0) {
-    const int2 bins = viewBins<R>(p.vx, p.vy, p.vz, g.totPhi);
+    // the direction the segment started with: pathSegment tallies
+    // enPacket%direction, not the reflected vHat (source/photon_mod.f90:1837)
+    const int2 bins = viewBins<R>(p.ex, p.ey, p.ez, g.totPhi);
     const int idirT = bins.x, idirP = bins.y;
     const int k = g.viewPTheta[idirT];
     if ((g.totPhi > 1 && k == g.viewPPhi[idirP]) || (g.totPhi == 1 && k > 0))
@@ -477,22 +523,6 @@ __device__ __forceinline__ void deposit(const DevGrid& g, const DevTransportOut&
   if (out.hEst) atomicAdd(out.hEst + idx, (double)((dl * deltaE) * costheta / dV));
 }
 
-// locate (source/interpolation_mod.f90:49-106) on the frequency mesh
-template <typename R>
-__device__ __forceinline__ int locateNu(const float* xa, int n, R x) {
-  if (x > (R)xa[n - 1]) return n;
-  if (x < (R)xa[0]) return 0;
-  int jlow = 0, jup = n + 1;
-  for (int it = 0; it < 64; ++it) {
-    if (jup - jlow < 1) break;
-    int jm = (jup + jlow) >> 1;
-    R v = (R)xa[jm - 1];
-    if (v == x) return jm;
-    if (x > v) { if (jlow == jm) break; jlow = jm; } else jup = jm;
-  }
-  return jlow;
-}
-
 // comptonScatter (source/photon_mod.f90:6805-6848)
 template <typename R, typename P>
 __device__ __forceinline__ void comptonScatter(const DevGrid& g, const TransportShared<R>& sh, P& p) {
@@ -507,6 +537,7 @@ __device__ __forceinline__ void comptonScatter(const DevGrid& g, const Transport
   p.vx = cs.c;
   p.vy = cs.s;
   p.vz = w;
+  p.ex = p.vx; p.ey = p.vy; p.ez = p.vz;
   int thc = th > 180 ? 180 : th;
   R newNu = p.nu * (R)__ldg(g.PcompT + (size_t)(p.nuP - 1) * 180 + (thc - 1));
   int newNuP = locateNu<R>(sh.nu, g.nbins, newNu);
@@ -630,7 +661,7 @@ struct AxisStep { R r, v, dS; int a; bool lost; };
 // started from (AxisVals holds the axis around it), a the index after the snap.
 template <typename R>
 __device__ __forceinline__ AxisStep<R> axisDistance(const AxisVals<R>& A, int n, int a0, int a, R r, R v,
-                                                    bool symmetric) {
+                                                    bool symmetric, bool plane) {
   using M = RMath<R>;
   const bool refl = symmetric && r <= A.first;
   v = (refl && v < R(0)) ? -v : v;
@@ -650,7 +681,7 @@ __device__ __forceinline__ AxisStep<R> axisDistance(const AxisVals<R>& A, int n,
   o.v = v;
   o.dS = dS;
   o.a = snap ? (pos ? (a < n ? a + 1 : a) : (a > 1 ? a - 1 : a)) : a;
-  o.lost = snap && pos && a >= n;
+  o.lost = snap && pos && a >= n && !plane;   // a plane-parallel slab keeps it (source/photon_mod.f90:2003)
   return o;
 }
 
@@ -664,7 +695,12 @@ __device__ __forceinline__ int stepCore(const DevGrid& g, const Geo& q, const De
   const int nx = q.nx(), ny = q.ny(), nz = q.nz();
   const float* X = q.X(); const float* Y = q.Y(); const float* Z = q.Z();
 #define AXR(A, i) ((R)(A)[(i) - 1])
-  if (++p.nStep > kSafeLimit) { ++lc.trapped; if (p.nEmit >= kRecursionLimit) ++lc.trapped; return ST_IDLE; }
+  // safeLimit: 5000 steps per segment for a plane-parallel slab (source/photon_mod.f90:1873-1878)
+  if (++p.nStep > (q.plane() ? kSafeLimitPlane : kSafeLimit)) {
+    ++lc.trapped;
+    if (p.nEmit >= kRecursionLimit) ++lc.trapped;
+    return ST_IDLE;
+  }
   int xP = p.xP, yP = p.yP, zP = p.zP;
   if (xP < 1 || xP > nx || yP < 1 || yP > ny || zP < 1 || zP > nz) { ++lc.errors; return ST_IDLE; }
   R rx = p.x, ry = p.y, rz = p.z, vx = p.vx, vy = p.vy, vz = p.vz;
@@ -700,9 +736,10 @@ __device__ __forceinline__ int stepCore(const DevGrid& g, const Geo& q, const De
   // the symmetric grid's reflection and the distances from the walls
   // (source/photon_mod.f90:1921-2084); with one mother grid the reference's
   // inner loop runs exactly once
-  const AxisStep<R> sx = axisDistance<R>(AX, nx, x0, xP, rx, vx, q.symmetric() != 0);
-  const AxisStep<R> sy = axisDistance<R>(AY, ny, y0, yP, ry, vy, q.symmetric() != 0);
-  const AxisStep<R> sz = axisDistance<R>(AZ, nz, z0, zP, rz, vz, q.symmetric() != 0);
+  const bool sym = q.symmetric() != 0, plane = q.plane();
+  const AxisStep<R> sx = axisDistance<R>(AX, nx, x0, xP, rx, vx, sym, plane);
+  const AxisStep<R> sy = axisDistance<R>(AY, ny, y0, yP, ry, vy, sym, plane);
+  const AxisStep<R> sz = axisDistance<R>(AZ, nz, z0, zP, rz, vz, sym, plane);
   if (sx.lost || sy.lost || sz.lost) { if (p.nEmit >= kRecursionLimit) ++lc.trapped; return ST_IDLE; }
   rx = sx.r; vx = sx.v; xP = sx.a;
   ry = sy.r; vy = sy.v; yP = sy.a;
@@ -804,30 +841,41 @@ __device__ __forceinline__ int stepCore(const DevGrid& g, const Geo& q, const De
     else if (dS == dSz && vz > R(0)) zP = zP + 1;
     else if (dS == dSz && vz < R(0)) zP = zP - 1;
     bool esc = false;
-    if (!q.symmetric()) {
-      // full-grid escape (source/photon_mod.f90:2884-3244)
-      if (ry < AXR(Y, 1) || yP < 1) esc = true;
-      if (ry > AXR(Y, ny) || yP > ny) esc = true;
-      if (rx <= AXR(X, 1) || xP < 1) esc = true;
-      if (rx >= AXR(X, nx) || xP > nx) esc = true;
-      if (rz <= AXR(Z, 1) || zP < 1) esc = true;
-      if (rz >= AXR(Z, nz) || zP > nz) esc = true;
-    }
-    // grid boundary and mirror planes (source/photon_mod.f90:3607-3890)
-    if (!esc && ((!q.symmetric() && (rx <= AXR(X, 1) || ry <= AXR(Y, 1) || rz <= AXR(Z, 1))) ||
-                 rx >= AXR(X, nx) || ry >= AXR(Y, ny) || rz >= AXR(Z, nz) || xP > nx || yP > ny || zP > nz))
-      esc = true;
-    if (esc) {
-      return ST_ESCAPE;
-    }
-    if (q.symmetric()) {
-      if (rx <= AXR(X, 1) || xP < 1) { if (vx < R(0)) vx = -vx; xP = 1; rx = AXR(X, 1); }
-      if (ry <= AXR(Y, 1) || yP < 1) { if (vy < R(0)) vy = -vy; yP = 1; ry = AXR(Y, 1); }
-      if (rz <= AXR(Z, 1) || zP < 1) { if (vz < R(0)) vz = -vz; zP = 1; rz = AXR(Z, 1); }
+    if (q.plane()) {
+      // plane-parallel slab (source/photon_mod.f90:3249-3611): out through the
+      // y planes only, reflected at the x and z planes (the lower z plane puts
+      // z at yAxis(1), as the reference does)
+      if (ry < AXR(Y, 1) || yP < 1) { yP = 1; esc = true; }
+      if (ry > AXR(Y, ny) || yP > ny) { yP = ny; esc = true; }
+      if (rx <= AXR(X, 1) || xP < 1) { xP = 1; rx = AXR(X, 1); vx = -vx; }
+      if (rx >= AXR(X, nx) || xP > nx) { xP = nx; rx = AXR(X, nx); vx = -vx; }
+      if (rz <= AXR(Z, 1) || zP < 1) { zP = 1; rz = AXR(Y, 1); vz = -vz; }
+      if (rz >= AXR(Z, nz) || zP > nz) { zP = nz; rz = AXR(Z, nz); vz = -vz; }
+      if (esc) return ST_ESCAPE;
+    } else {
+      if (!q.symmetric()) {
+        // full-grid escape (source/photon_mod.f90:2884-3244)
+        if (ry < AXR(Y, 1) || yP < 1) esc = true;
+        if (ry > AXR(Y, ny) || yP > ny) esc = true;
+        if (rx <= AXR(X, 1) || xP < 1) esc = true;
+        if (rx >= AXR(X, nx) || xP > nx) esc = true;
+        if (rz <= AXR(Z, 1) || zP < 1) esc = true;
+        if (rz >= AXR(Z, nz) || zP > nz) esc = true;
+      }
+      // grid boundary and mirror planes (source/photon_mod.f90:3607-3890)
+      if (!esc && ((!q.symmetric() && (rx <= AXR(X, 1) || ry <= AXR(Y, 1) || rz <= AXR(Z, 1))) ||
+                   rx >= AXR(X, nx) || ry >= AXR(Y, ny) || rz >= AXR(Z, nz) || xP > nx || yP > ny || zP > nz))
+        esc = true;
+      if (esc) return ST_ESCAPE;
+      if (q.symmetric()) {
+        if (rx <= AXR(X, 1) || xP < 1) { if (vx < R(0)) vx = -vx; xP = 1; rx = AXR(X, 1); }
+        if (ry <= AXR(Y, 1) || yP < 1) { if (vy < R(0)) vy = -vy; yP = 1; ry = AXR(Y, 1); }
+        if (rz <= AXR(Z, 1) || zP < 1) { if (vz < R(0)) vz = -vz; zP = 1; rz = AXR(Z, 1); }
+      }
     }
   }
   // source/photon_mod.f90:3951-4036
-  if (next == ST_STEP && (xP > nx || yP > ny || zP > nz)) {
+  if (next == ST_STEP && !q.plane() && (xP > nx || yP > ny || zP > nz)) {
     return ST_ESCAPE;
   }
   p.x = rx; p.y = ry; p.z = rz; p.vx = vx; p.vy = vy; p.vz = vz;

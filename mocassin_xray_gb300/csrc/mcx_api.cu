@@ -63,17 +63,19 @@ int copyIn(std::vector<T>& v, const void* src, size_t nbytes) {
 // (source/grid_mod.f90:2887-2986) evaluated in double.
 double volumeD(const Setup& s, int xP, int yP, int zP) {
   auto A = [](const std::vector<float>& a, int i) { return (double)a[i - 1]; };
-  const bool sym = s.p.lgSymmetricXYZ;
+  // half-width first cells with symmetric axes, first and last ones with a plane source
+  const bool lo = s.p.lgSymmetricXYZ || s.p.lgPlaneIonization, hi = s.p.lgPlaneIonization;
+  auto edge = [](double w, bool half) { return half ? w / 2. : w; };
   double dx = 0., dy = 0., dz = 0.;
   if (xP > 1 && xP < s.nx) dx = std::fabs(A(s.xAxis, xP + 1) - A(s.xAxis, xP - 1)) / 2.;
-  else if (xP == 1) dx = sym ? std::fabs(A(s.xAxis, 2) - A(s.xAxis, 1)) / 2. : std::fabs(A(s.xAxis, 2) - A(s.xAxis, 1));
-  else if (xP == s.nx) dx = std::fabs(A(s.xAxis, xP) - A(s.xAxis, xP - 1));
+  else if (xP == 1) dx = edge(std::fabs(A(s.xAxis, 2) - A(s.xAxis, 1)), lo);
+  else if (xP == s.nx) dx = edge(std::fabs(A(s.xAxis, xP) - A(s.xAxis, xP - 1)), hi);
   if (yP > 1 && yP < s.ny) dy = std::fabs(A(s.yAxis, yP + 1) - A(s.yAxis, yP - 1)) / 2.;
-  else if (yP == 1) dy = sym ? std::fabs(A(s.yAxis, 2) - A(s.yAxis, 1)) / 2. : std::fabs(A(s.yAxis, 2) - A(s.yAxis, 1));
-  else if (yP == s.ny) dy = std::fabs(A(s.yAxis, yP) - A(s.yAxis, yP - 1));
+  else if (yP == 1) dy = edge(std::fabs(A(s.yAxis, 2) - A(s.yAxis, 1)), lo);
+  else if (yP == s.ny) dy = edge(std::fabs(A(s.yAxis, yP) - A(s.yAxis, yP - 1)), hi);
   if (zP > 1 && zP < s.nz) dz = std::fabs(A(s.zAxis, zP + 1) - A(s.zAxis, zP - 1)) / 2.;
-  else if (zP == 1) dz = sym ? std::fabs(A(s.zAxis, 2) - A(s.zAxis, 1)) / 2. : std::fabs(A(s.zAxis, 2) - A(s.zAxis, 1));
-  else if (zP == s.nz) dz = std::fabs(A(s.zAxis, zP) - A(s.zAxis, zP - 1));
+  else if (zP == 1) dz = edge(std::fabs(A(s.zAxis, 2) - A(s.zAxis, 1)), lo);
+  else if (zP == s.nz) dz = edge(std::fabs(A(s.zAxis, zP) - A(s.zAxis, zP - 1)), hi);
   dx = dx / 1.e15; dy = dy / 1.e15; dz = dz / 1.e15;
   return dx * dy * dz;
 }
@@ -108,6 +110,7 @@ extern "C" int mcx_setup_info_get(const mcx_setup* m, mcx_setup_info* info) {
   std::memset(info, 0, sizeof(*info));
   info->nx = s.nx; info->ny = s.ny; info->nz = s.nz;
   info->n_angle_bins = s.p.nAngleBins;
+  info->plane_ionization = s.p.lgPlaneIonization ? 1 : 0;
   for (int j = 0; j < 2; ++j) { info->view_theta[j] = s.p.viewTheta[j]; info->view_phi[j] = s.p.viewPhi[j]; }
   info->n_cells = s.nCells;
   info->nbins = s.nbins;
@@ -370,6 +373,7 @@ struct mcx_ctx {
   float starPos[3] = {0.f, 0.f, 0.f};
   std::vector<int32_t> activeHost;
   int activeFull = 0;        // active(i,j,k) == (i-1) ny nz + (j-1) nz + k for every cell
+  int plane = 0;             // plane-parallel ionisation (lgPlaneIonization)
   float gauntTeOld = -1.f;   // BoltGaunt's saved TeOld2
 
   // tables
@@ -736,8 +740,11 @@ static int loadSetup(mcx_ctx* c, const Setup& s) {
   for (int32_t a : s.active)
     if (a < 0 || a > s.nCells) return fail(c, MCX_ERR_INPUT, "mcx_load: active() holds ids outside [0, nCells] (sub-grids are not supported)");
   if (s.nbins < 2 || s.nCells < 1) return fail(c, MCX_ERR_INPUT, "mcx_load: empty grid or frequency mesh");
-  if (s.starIdx[0] < 1 || s.starIdx[0] > s.nx || s.starIdx[1] < 1 || s.starIdx[1] > s.ny || s.starIdx[2] < 1 || s.starIdx[2] > s.nz)
+  if (!s.p.lgPlaneIonization &&
+      (s.starIdx[0] < 1 || s.starIdx[0] > s.nx || s.starIdx[1] < 1 || s.starIdx[1] > s.ny || s.starIdx[2] < 1 ||
+       s.starIdx[2] > s.nz))
     return fail(c, MCX_ERR_INPUT, "mcx_load: the source must lie inside the grid");
+  c->plane = s.p.lgPlaneIonization ? 1 : 0;
   c->activeHost = s.active;
   c->activeFull = 1;
   for (int k = 0; k < s.nz && c->activeFull; ++k)
@@ -911,6 +918,7 @@ extern "C" int mcx_load_batched(mcx_ctx* c, const mcx_setup* const* setups, int3
     const Setup& s = setups[b]->s;
     if (!s.p.lgGas || s.p.lgDust) return fail(c, MCX_ERR_INPUT, "mcx_load_batched: a batch holds gas-only nebulae");
     if (s.p.nAngleBins > 0) return fail(c, MCX_ERR_INPUT, "mcx_load_batched: viewing angles (inclination) are not batched");
+    if (s.p.lgPlaneIonization) return fail(c, MCX_ERR_INPUT, "mcx_load_batched: plane-parallel models are not batched");
     if (s.p.lgRadPress) return fail(c, MCX_ERR_INPUT, "mcx_load_batched: radiation pressure is not supported in a batch");
     if (s.nbins != s0.nbins || s.nu != s0.nu || s.widFlx != s0.widFlx) return bad(b, "the frequency mesh");
     if (s.p.nstages != s0.p.nstages || s.nElemUsed != s0.nElemUsed) return bad(b, "nstages or the elements");
@@ -1339,7 +1347,7 @@ extern "C" int mcx_transport(mcx_ctx* c, const mcx_transport_opts* o, mcx_transp
   DevGrid g{};
   g.nx = c->nx; g.ny = c->ny; g.nz = c->nz; g.nCells = c->nCells; g.nbins = c->nbins;
   g.symmetric = c->symmetric; g.lgDust = c->lgDust; g.lgGas = c->lgGas; g.lgCompton = c->lgCompton;
-  g.radPress = c->radPress; g.activeFull = c->activeFull;
+  g.radPress = c->radPress; g.activeFull = c->activeFull; g.plane = c->plane;
   for (int d = 0; d < 3; ++d) { g.starIdx[d] = c->starIdx[d]; g.starPos[d] = c->starPos[d]; }
   g.ionEdge1 = c->ionEdge1; g.rOut = c->rOut;
   g.xAxis = c->xAxis.p; g.yAxis = c->yAxis.p; g.zAxis = c->zAxis.p; g.active = c->active.p;

@@ -14,6 +14,10 @@ struct DevGrid {
   // reference's order, (i-1) ny nz + (j-1) nz + k: the cell id is then
   // computed instead of loaded (one dependent global load less per event)
   int32_t activeFull;
+  // 1 for plane-parallel ionisation (lgPlaneIonization): stellar packets start
+  // on the plane y = 0 moving along +y, escape through the y planes only and
+  // are reflected at the x and z planes
+  int32_t plane;
   int32_t starIdx[3];
   float starPos[3];
   float ionEdge1, rOut;

@@ -176,7 +176,12 @@ void parseInput(Params& p, const std::string& path) {
              kw == "noPhotoelectric" || kw == "separateSED") {
       // accepted; these do not change the transport + balance path built here
     }
-    else if (kw == "planeIonization" || kw == "multiGrids" || kw == "multiChemistry" ||
+    else if (kw == "planeIonization") {
+      p.meanFieldin = toF(t, 1, kw); p.nu0 = toF(t, 2, kw); p.nu0Add = toF(t, 3, kw);
+      p.lgPlaneIonization = true;
+      p.LStar = 0.f;
+    }
+    else if (kw == "multiGrids" || kw == "multiChemistry" ||
              kw == "2D" || kw == "diffuseSource" || kw == "multiPhotoSources" ||
              kw == "quantumHeatGrain" || kw == "resLinesTransfer" || kw == "MdMg" || kw == "MdMh" ||
              kw == "fluorescence" || kw == "nahar") {
@@ -188,7 +193,8 @@ void parseInput(Params& p, const std::string& path) {
   // consistency checks of source/set_input_mod.f90:560-704 (those on this path)
   if (!p.haveContShape) fail("readInput: no information about the continuum shape - contShape -");
   if (!p.haveNPhotons) fail("readInput: no information about the number of energy packets - nPhotons -");
-  if (!p.haveLStar && p.LPhot <= 0.f) fail("readInput: no information about the stellar luminosity - Lstar or Lphot -");
+  if (!p.lgPlaneIonization && !p.haveLStar && p.LPhot <= 0.f)
+    fail("readInput: no information about the stellar luminosity - Lstar or Lphot -");
   if (p.lg1D) fail("readInput: oneD is outside this library's scope");
   if (p.lgGas && !p.haveAbundance) fail("readInput: no elemental abundance file has been specified");
   if (!p.lgDust && !p.lgGas) fail("readInput: the grid is completely empty. no gas or dust present.");
@@ -197,7 +203,17 @@ void parseInput(Params& p, const std::string& path) {
     fail("readInput: invalid or missing grid edges");
   if (p.contShape == "blackbody" && p.TStellar == 0.f) fail("readInput: TStellar must be given for a blackbody");
   if (p.R_in < 0.f) fail("readInput: invalid or missing inner radius Rin");
-  if (p.LPhot == 0.f && p.LStar == 0.f) fail("readInput: Lstar or LPhot must be given");
+  if (p.LPhot == 0.f && p.LStar == 0.f && !p.lgPlaneIonization) fail("readInput: Lstar or LPhot must be given");
+  if (p.lgPlaneIonization) {
+    if (p.nx <= 2 || p.nz <= 2)
+      fail("readInput: plane parallel simulation must have cuboid sides at least 3 cells deep (nx, nz >= 3)");
+    if (!p.lgDfile)
+      fail("readInput: plane ionizing field specified - must use user defined density distribution via densityFile");
+    // the reference drops symmetricXYZ here, except where an earlier branch of its
+    // else-if chain (the warning on edges given beside a density file) was taken
+    if (p.lgSymmetricXYZ && !(p.Rnx >= 0.f || p.Rny >= 0.f || p.Rnz >= 0.f)) p.lgSymmetricXYZ = false;
+    if (p.lgSymmetricXYZ) fail("readInput: planeIonization with symmetricXYZ");
+  }
   if (p.LPhot != 0.f && p.LStar != 0.f) fail("readInput: Lstar and LPhot are mutually exclusive");
   if (p.maxIterateMC < 1) fail("readInput: invalid maxIterateMC");
   if (p.minConvergence < 0.f || p.minConvergence > 100.f) fail("readInput: invalid minConvergence");
@@ -710,9 +726,12 @@ void setContinuum(Setup& s) {
   float nce = 0.f, ncp = 0.f;
   for (int i = 0; i < nb; ++i) nce += sumErg[i] * s.widFlx[i];
   for (int i = s.lymanP; i <= nb; ++i) ncp += sumPhot[i - 1] * s.widFlx[i - 1];
+  // a plane source emits nothing below nu0Add (source/continuum_mod.f90:472-483)
+  int nu0AddP = 1;
+  if (s.p.lgPlaneIonization && s.p.nu0Add > 0.f) nu0AddP = std::max(1, locate(s.nu.data(), nb, s.p.nu0Add));
   s.srcCDF.assign(nb, 0.f);
-  s.srcCDF[0] = sumErg[0] * s.widFlx[0];
-  for (int i = 2; i <= nb; ++i) s.srcCDF[i - 1] = s.srcCDF[i - 2] + sumErg[i - 1] * s.widFlx[i - 1];
+  s.srcCDF[nu0AddP - 1] = sumErg[nu0AddP - 1] * s.widFlx[nu0AddP - 1];
+  for (int i = nu0AddP + 1; i <= nb; ++i) s.srcCDF[i - 1] = s.srcCDF[i - 2] + sumErg[i - 1] * s.widFlx[i - 1];
   float last = s.srcCDF[nb - 1];
   for (int i = 0; i < nb; ++i) s.srcCDF[i] /= last;
   float maxp = 0.f;
@@ -737,17 +756,19 @@ void setContinuum(Setup& s) {
 // ---------------------------------------------------------------------- grid
 float getVolume(const Setup& s, int xP, int yP, int zP) {
   const auto& X = s.xAxis; const auto& Y = s.yAxis; const auto& Z = s.zAxis;
-  const bool sym = s.p.lgSymmetricXYZ;
+  // half-width first cells for a symmetric grid, half-width first and last
+  // cells for a plane-parallel one (source/grid_mod.f90:2925-2981)
+  const bool lo = s.p.lgSymmetricXYZ || s.p.lgPlaneIonization, hi = s.p.lgPlaneIonization;
   float dx = 0.f, dy = 0.f, dz = 0.f;
   if (xP > 1 && xP < s.nx) dx = fabsf(X[xP] - X[xP - 2]) / 2.f;
-  else if (xP == 1) dx = sym ? fabsf(X[1] - X[0]) / 2.f : fabsf(X[1] - X[0]);
-  else if (xP == s.nx) dx = fabsf(X[xP - 1] - X[xP - 2]);
+  else if (xP == 1) dx = lo ? fabsf(X[1] - X[0]) / 2.f : fabsf(X[1] - X[0]);
+  else if (xP == s.nx) dx = hi ? fabsf(X[xP - 1] - X[xP - 2]) / 2.f : fabsf(X[xP - 1] - X[xP - 2]);
   if (yP > 1 && yP < s.ny) dy = fabsf(Y[yP] - Y[yP - 2]) / 2.f;
-  else if (yP == 1) dy = sym ? fabsf(Y[1] - Y[0]) / 2.f : fabsf(Y[1] - Y[0]);
-  else if (yP == s.ny) dy = fabsf(Y[yP - 1] - Y[yP - 2]);
+  else if (yP == 1) dy = lo ? fabsf(Y[1] - Y[0]) / 2.f : fabsf(Y[1] - Y[0]);
+  else if (yP == s.ny) dy = hi ? fabsf(Y[yP - 1] - Y[yP - 2]) / 2.f : fabsf(Y[yP - 1] - Y[yP - 2]);
   if (zP > 1 && zP < s.nz) dz = fabsf(Z[zP] - Z[zP - 2]) / 2.f;
-  else if (zP == 1) dz = sym ? fabsf(Z[1] - Z[0]) / 2.f : fabsf(Z[1] - Z[0]);
-  else if (zP == s.nz) dz = fabsf(Z[zP - 1] - Z[zP - 2]);
+  else if (zP == 1) dz = lo ? fabsf(Z[1] - Z[0]) / 2.f : fabsf(Z[1] - Z[0]);
+  else if (zP == s.nz) dz = hi ? fabsf(Z[zP - 1] - Z[zP - 2]) / 2.f : fabsf(Z[zP - 1] - Z[zP - 2]);
   dx /= 1.e15f; dy /= 1.e15f; dz /= 1.e15f;
   return dx * dy * dz;
 }
@@ -814,8 +835,10 @@ void fillGrid(Setup& s) {
         float radius = 1.e10f * sqrtf((s.xAxis[i - 1] / 1.e10f) * (s.xAxis[i - 1] / 1.e10f) +
                                       (s.yAxis[j - 1] / 1.e10f) * (s.yAxis[j - 1] / 1.e10f) +
                                       (s.zAxis[k - 1] / 1.e10f) * (s.zAxis[k - 1] / 1.e10f));
-        if (radius < p.R_in) s.active[v] = 0;
-        else if (radius > p.R_out && p.R_out > 0.f) s.active[v] = 0;
+        if (!p.lgPlaneIonization) {   // no radial cuts for a plane-parallel slab (source/grid_mod.f90:1258)
+          if (radius < p.R_in) s.active[v] = 0;
+          else if (radius > p.R_out && p.R_out > 0.f) s.active[v] = 0;
+        }
         if (s.active[v] <= 0) { NdustTemp[v] = 0.f; HdenTemp[v] = 0.f; }
         bool on;
         if (p.lgDust && p.lgGas) on = HdenTemp[v] > 0.f || NdustTemp[v] > 0.f;
@@ -858,6 +881,45 @@ void fillGrid(Setup& s) {
               else ID(c, s.elemXref[elem - 1], ion) = (1.f - ID(c, s.elemXref[0] > 0 ? s.elemXref[0] : 1, 1)) / (float)std::min(elem, S - 1);
             }
       }
+}
+
+// The ionising plane of a plane-parallel model (setMotherGrid,
+// source/grid_mod.f90:1761-1822; fillGrid :852): the photon flux meanField
+// above nu0 scales the spectrum, the part below nu0Add is cut, and the
+// transferred energy flux times the x-z extent of the grid is the source's
+// luminosity; R_out becomes the grid's largest extent.  REAL arithmetic, as
+// in the reference.
+void setPlaneSource(Setup& s) {
+  Params& p = s.p;
+  const int nb = s.nbins;
+  const float* nu = s.nu.data();
+  float meanField = p.meanFieldin;
+  if (p.nu0 > 0.f) {
+    int nu0P = locate(nu, nb, p.nu0);
+    if (nu0P < nb && nu0P > 0 && p.nu0 > (nu[nu0P - 1] + nu[nu0P]) / 2.f) nu0P += 1;
+    int nu0AddP;
+    if (p.nu0Add != p.nu0) {
+      nu0AddP = locate(nu, nb, p.nu0Add);
+      if (nu0AddP < nb && nu0AddP > 0 && p.nu0Add > (nu[nu0AddP - 1] + nu[nu0AddP]) / 2.f) nu0AddP += 1;
+    } else {
+      nu0AddP = nu0P;
+    }
+    if (nu0P >= nb || nu0P < 1) fail("setMotherGrid: nu0 outside the frequency mesh");
+    float norm = 0.f;
+    for (int i = nu0P; i <= nb; ++i) norm = norm + (float)s.inSpectrumPhot[i - 1] * s.widFlx[i - 1];
+    const float scale = meanField / norm;
+    norm = 0.f;
+    for (int i = 1; i <= nb; ++i) {
+      if (i < nu0AddP) s.inSpectrumErg[i - 1] = 0.;
+      norm = norm + (float)s.inSpectrumErg[i - 1] * s.widFlx[i - 1];
+    }
+    meanField = norm * scale;
+  }
+  s.LStar = (meanField / 1.e36f) * (s.xAxis[s.nx - 1] - s.xAxis[0]) * (s.zAxis[s.nz - 1] - s.zAxis[0]);
+  s.LPhot = 0.f;
+  p.R_out = 1.e10f * sqrtf((s.xAxis[s.nx - 1] / 1.e10f) * (s.xAxis[s.nx - 1] / 1.e10f) +
+                           (s.yAxis[s.ny - 1] / 1.e10f) * (s.yAxis[s.ny - 1] / 1.e10f) +
+                           (s.zAxis[s.nz - 1] / 1.e10f) * (s.zAxis[s.nz - 1] / 1.e10f));
 }
 
 void setStarPosition(Setup& s) {
@@ -958,6 +1020,7 @@ void buildSetup(Setup& s, const std::string& inputFile, const std::string& dataD
   }
   setContinuum(s);
   fillGrid(s);
+  if (s.p.lgPlaneIonization) setPlaneSource(s);
   setStarPosition(s);
   if (s.p.lgDust) {   // dustDriver's initial grain temperatures (source/dust_mod.f90:66-73)
     const size_t planes = (size_t)(s.dust.nSpecies + 1) * (s.dust.nSizes + 1);

@@ -38,6 +38,10 @@ struct Params {
   float NdustValue = 0.f, MdMgValue = 0.f;
   float pwlIndex = 0.f, pwlMin = 0.f, pwlMax = 0.f;
   float starPos[3] = {0.f, 0.f, 0.f};
+  // 'planeIonization meanField nu0 nu0Add' (source/set_input_mod.f90:257-262):
+  // the ionising plane's photon flux above nu0 [Ryd], and the frequency below
+  // which the plane emits nothing
+  float meanFieldin = 0.f, nu0 = 0.f, nu0Add = 0.f;
   int nAngleBins = 0;             // 'inclination': viewing angles (at most 2)
   float viewTheta[2] = {0.f, 0.f}, viewPhi[2] = {0.f, 0.f};
   bool haveStarPos = false, haveLStar = false, haveTStellar = false;

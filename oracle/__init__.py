@@ -42,7 +42,8 @@ class TransportIn(C.Structure):
                 ("rec_pdf", _P), ("dust_pdf", _P), ("total_lines", _P), ("ne", _P),
                 ("ion_edge1", C.c_float), ("r_out", C.c_float), ("star_pos", C.c_float * 3),
                 ("star_idx", C.c_int32 * 3), ("delta_e", C.c_double), ("n_angle", C.c_int32),
-                ("tot_phi", C.c_int32), ("view_p_theta", C.c_int32 * 21), ("view_p_phi", C.c_int32 * 21)]
+                ("tot_phi", C.c_int32), ("view_p_theta", C.c_int32 * 21), ("view_p_phi", C.c_int32 * 21),
+                ("plane", C.c_int32)]
 
 
 def view_bins(n_angle: int, theta, phi) -> tuple[int, list, list]:
@@ -256,6 +257,7 @@ def transport(setup, opacity_arr, rec_pdf, total_lines, ne=None, n: int = 1000, 
     s.star_pos[:] = list(i.star_pos)
     s.star_idx[:] = list(i.star_idx)
     s.n_angle = i.n_angle_bins
+    s.plane = i.plane_ionization
     s.tot_phi, pt, pp = view_bins(i.n_angle_bins, i.view_theta, i.view_phi)
     s.view_p_theta[:] = pt
     s.view_p_phi[:] = pp

@@ -63,6 +63,7 @@ typedef struct orc_transport_in {
     int32_t tot_phi;            /* totAngleBinsPhi                                     */
     int32_t view_p_theta[21];   /* viewPointPtheta(0:20)                               */
     int32_t view_p_phi[21];     /* viewPointPphi(0:tot_phi)                            */
+    int32_t plane;              /* lgPlaneIonization                                   */
 } orc_transport_in;
 
 typedef struct orc_transport_out {

@@ -163,7 +163,7 @@ static vec3 random_unit_vector(rng_t* r) {
     return v;
 }
 
-/* initPhotonPacket (source/photon_mod.f90:744-896), non-plane-parallel */
+/* initPhotonPacket (source/photon_mod.f90:744-896) */
 static void init_packet(tctx_t* c, packet_t* p, int nuP, vec3 pos, int lgLine, int lgStellar,
                         int xP, int yP, int zP, rng_t* r) {
     const orc_transport_in* in = c->in;
@@ -172,16 +172,35 @@ static void init_packet(tctx_t* c, packet_t* p, int nuP, vec3 pos, int lgLine, i
     p->lgStellar = lgStellar;
     if (lgLine) { p->nu = 0.; p->lgLine = 1; }
     else { p->nu = (double)in->nu[nuP - 1]; p->lgLine = 0; }
+    if (lgStellar && in->plane) {
+        /* the ionising plane (:795-856): y = 0, x and z uniform over the axes'
+         * span, in the cell whose walls bracket them, moving along +y */
+        const float* X = in->x_axis; const float* Z = in->z_axis;
+        double rnd = 1. - urand(r);
+        p->pos.x = AX(X, 1) + rnd * (AX(X, in->nx) - AX(X, 1));
+        xP = locate_f(X, in->nx, p->pos.x);
+        if (xP < in->nx && xP > 0 && p->pos.x >= (AX(X, xP) + AX(X, xP + 1)) / 2.) xP = xP + 1;
+        p->pos.y = 0.;
+        yP = 1;
+        rnd = 1. - urand(r);
+        p->pos.z = AX(Z, 1) + rnd * (AX(Z, in->nz) - AX(Z, 1));
+        zP = locate_f(Z, in->nz, p->pos.z);
+        if (zP < in->nz && zP > 0 && p->pos.z >= (AX(Z, zP) + AX(Z, zP + 1)) / 2.) zP = zP + 1;
+        if (xP < 1) xP = 1;
+        if (zP < 1) zP = 1;
+        p->dir.x = 0.; p->dir.y = 1.; p->dir.z = 0.;
+    } else {
+        for (int irepeat = 0; irepeat < 1000000; ++irepeat) {
+            p->dir = random_unit_vector(r);
+            if (p->dir.x != 0. && p->dir.y != 0. && p->dir.z != 0.) break;
+        }
+        if (in->symmetric_xyz && lgStellar) {
+            if (p->dir.x < 0.) p->dir.x = -p->dir.x;
+            if (p->dir.y < 0.) p->dir.y = -p->dir.y;
+            if (p->dir.z < 0.) p->dir.z = -p->dir.z;
+        }
+    }
     p->xP = xP; p->yP = yP; p->zP = zP;
-    for (int irepeat = 0; irepeat < 1000000; ++irepeat) {
-        p->dir = random_unit_vector(r);
-        if (p->dir.x != 0. && p->dir.y != 0. && p->dir.z != 0.) break;
-    }
-    if (in->symmetric_xyz && lgStellar) {
-        if (p->dir.x < 0.) p->dir.x = -p->dir.x;
-        if (p->dir.y < 0.) p->dir.y = -p->dir.y;
-        if (p->dir.z < 0.) p->dir.z = -p->dir.z;
-    }
     if (xP > 0 && yP > 0 && zP > 0) p->origin = active_at(in, xP, yP, zP);
     else p->origin = 0;
 }
@@ -228,16 +247,19 @@ static inline void deposit(tctx_t* c, int cell, int nuP, double dl, double dV, d
 
 double orc_cell_volume(const orc_transport_in* in, int32_t xP, int32_t yP, int32_t zP) {
     const float* X = in->x_axis; const float* Y = in->y_axis; const float* Z = in->z_axis;
+    /* half-width first cells with symmetric axes, first and last with a plane
+     * source (source/photon_mod.f90:2160-2215) */
+    const int lo = in->symmetric_xyz || in->plane, hi = in->plane;
     double dx = 0., dy = 0., dz = 0.;
     if (xP > 1 && xP < in->nx) dx = fabs(AX(X, xP + 1) - AX(X, xP - 1)) / 2.;
-    else if (xP == 1) dx = in->symmetric_xyz ? fabs(AX(X, 2) - AX(X, 1)) / 2. : fabs(AX(X, 2) - AX(X, 1));
-    else if (xP == in->nx) dx = fabs(AX(X, xP) - AX(X, xP - 1));
+    else if (xP == 1) dx = lo ? fabs(AX(X, 2) - AX(X, 1)) / 2. : fabs(AX(X, 2) - AX(X, 1));
+    else if (xP == in->nx) dx = hi ? fabs(AX(X, xP) - AX(X, xP - 1)) / 2. : fabs(AX(X, xP) - AX(X, xP - 1));
     if (yP > 1 && yP < in->ny) dy = fabs(AX(Y, yP + 1) - AX(Y, yP - 1)) / 2.;
-    else if (yP == 1) dy = in->symmetric_xyz ? fabs(AX(Y, 2) - AX(Y, 1)) / 2. : fabs(AX(Y, 2) - AX(Y, 1));
-    else if (yP == in->ny) dy = fabs(AX(Y, yP) - AX(Y, yP - 1));
+    else if (yP == 1) dy = lo ? fabs(AX(Y, 2) - AX(Y, 1)) / 2. : fabs(AX(Y, 2) - AX(Y, 1));
+    else if (yP == in->ny) dy = hi ? fabs(AX(Y, yP) - AX(Y, yP - 1)) / 2. : fabs(AX(Y, yP) - AX(Y, yP - 1));
     if (zP > 1 && zP < in->nz) dz = fabs(AX(Z, zP + 1) - AX(Z, zP - 1)) / 2.;
-    else if (zP == 1) dz = in->symmetric_xyz ? fabs(AX(Z, 2) - AX(Z, 1)) / 2. : fabs(AX(Z, 2) - AX(Z, 1));
-    else if (zP == in->nz) dz = fabs(AX(Z, zP) - AX(Z, zP - 1));
+    else if (zP == 1) dz = lo ? fabs(AX(Z, 2) - AX(Z, 1)) / 2. : fabs(AX(Z, 2) - AX(Z, 1));
+    else if (zP == in->nz) dz = hi ? fabs(AX(Z, zP) - AX(Z, zP - 1)) / 2. : fabs(AX(Z, zP) - AX(Z, zP - 1));
     dx = dx / 1.e15; dy = dy / 1.e15; dz = dz / 1.e15;
     return dx * dy * dz;
 }
@@ -276,7 +298,7 @@ static int path_segment(tctx_t* c, packet_t* p, rng_t* r, int* retype) {
     double dSx = 0., dSy = 0., dSz = 0.;
     double absTau = 0.;
     double passProb = -log(1. - urand(r));
-    const int safeLimit = 500000;
+    const int safeLimit = in->plane ? 5000 : 500000;   /* :1873-1878 */
     int packetType = PT_DIFFUSE;
     int i;
     for (i = 1; i <= safeLimit; ++i) {
@@ -304,7 +326,7 @@ static int path_segment(tctx_t* c, packet_t* p, rng_t* r, int* retype) {
                     if (fabs(dSx) < 1.e-5) { rv.x = (AX(X, xP + 1) + AX(X, xP)) / 2.; xP = xP + 1; }
                 } else {
                     dSx = (AX(X, nx) - rv.x) / vh.x;
-                    if (fabs(dSx) < 1.e-5) { rv.x = AX(X, nx); return 0; }
+                    if (fabs(dSx) < 1.e-5) { rv.x = AX(X, nx); if (!in->plane) return 0; }
                 }
             } else if (vh.x < 0.) {
                 if (xP > 1) {
@@ -323,7 +345,7 @@ static int path_segment(tctx_t* c, packet_t* p, rng_t* r, int* retype) {
                     if (fabs(dSy) < 1.e-5) { rv.y = (AX(Y, yP + 1) + AX(Y, yP)) / 2.; yP = yP + 1; }
                 } else {
                     dSy = (AX(Y, ny) - rv.y) / vh.y;
-                    if (fabs(dSy) < 1.e-5) { rv.y = AX(Y, ny); return 0; }
+                    if (fabs(dSy) < 1.e-5) { rv.y = AX(Y, ny); if (!in->plane) return 0; }
                 }
             } else if (vh.y < 0.) {
                 if (yP > 1) {
@@ -342,7 +364,7 @@ static int path_segment(tctx_t* c, packet_t* p, rng_t* r, int* retype) {
                     if (fabs(dSz) < 1.e-5) { rv.z = (AX(Z, zP + 1) + AX(Z, zP)) / 2.; zP = zP + 1; }
                 } else {
                     dSz = (AX(Z, nz) - rv.z) / vh.z;
-                    if (fabs(dSz) < 1.e-5) { rv.z = AX(Z, nz); return 0; }
+                    if (fabs(dSz) < 1.e-5) { rv.z = AX(Z, nz); if (!in->plane) return 0; }
                 }
             } else if (vh.z < 0.) {
                 if (zP > 1) {
@@ -447,6 +469,19 @@ static int path_segment(tctx_t* c, packet_t* p, rng_t* r, int* retype) {
             else if (dS == dSz && vh.z > 0.) zP = zP + 1;
             else if (dS == dSz && vh.z < 0.) zP = zP - 1;
 
+            if (in->plane) {
+                /* plane-parallel slab (source/photon_mod.f90:3249-3611): out
+                 * through the y planes only, reflected at x and z (the lower z
+                 * plane puts z at yAxis(1), as the reference does) */
+                int ret = 0;
+                if (rv.y < AX(Y, 1) || yP < 1) { yP = 1; ret = 1; }
+                if (rv.y > AX(Y, ny) || yP > ny) { yP = ny; ret = 1; }
+                if (rv.x <= AX(X, 1) || xP < 1) { xP = 1; rv.x = AX(X, 1); vh.x = -vh.x; }
+                if (rv.x >= AX(X, nx) || xP > nx) { xP = nx; rv.x = AX(X, nx); vh.x = -vh.x; }
+                if (rv.z <= AX(Z, 1) || zP < 1) { zP = 1; rv.z = AX(Y, 1); vh.z = -vh.z; }
+                if (rv.z >= AX(Z, nz) || zP > nz) { zP = nz; rv.z = AX(Z, nz); vh.z = -vh.z; }
+                if (ret) { escape_tally(c, p); return 0; }
+            } else {
             if (!in->symmetric_xyz) {
                 /* full-grid escape (source/photon_mod.f90:2884-3244) */
                 int ret = 0;
@@ -470,9 +505,10 @@ static int path_segment(tctx_t* c, packet_t* p, rng_t* r, int* retype) {
                 if (rv.y <= AX(Y, 1) || yP < 1) { if (vh.y < 0.) vh.y = -vh.y; yP = 1; rv.y = AX(Y, 1); }
                 if (rv.z <= AX(Z, 1) || zP < 1) { if (vh.z < 0.) vh.z = -vh.z; zP = 1; rv.z = AX(Z, 1); }
             }
+            }
         }
         /* source/photon_mod.f90:3951-4036 */
-        if (xP > nx || yP > ny || zP > nz) { escape_tally(c, p); return 0; }
+        if (!in->plane && (xP > nx || yP > ny || zP > nz)) { escape_tally(c, p); return 0; }
     }
     if (i > safeLimit) { c->st.trapped++; return 0; }
     p->xP = xP; p->yP = yP; p->zP = zP;

@@ -1,7 +1,8 @@
 """The reference's own benchmark decks (benchmarks/gas) read by the deck grammar of libmcx, when a
 MOCASSIN source tree is named by MCX_REFERENCE_DIR on the machine running the tests: the
-photoionisation benchmarks parse into grids of the expected shape, and the decks that select paths
-outside this library (plane-parallel illumination) are rejected with a message, not misread."""
+photoionisation benchmarks parse into grids of the expected shape, the plane-parallel NLR benchmark
+parses into its slab, and the decks that select paths outside this library (the X-ray benchmarks'
+tabulated continuum file) are rejected with a message, not misread."""
 import os
 import shutil
 from pathlib import Path
@@ -36,7 +37,19 @@ def test_photoionisation_benchmarks_parse(tmp_path, data_dir, name, nbins):
     assert s.get(abi.ARR_TE)[1] > 0
 
 
-@pytest.mark.parametrize("name", ["NLR", "X1"])
-def test_plane_parallel_decks_are_rejected(tmp_path, data_dir, name):
-    with pytest.raises(RuntimeError):
-        Setup(_deck(tmp_path, name), data_dir)
+def test_plane_parallel_nlr_benchmark_parses(tmp_path, data_dir):
+    s = Setup(_deck(tmp_path, "NLR"), data_dir)
+    i = s.info
+    assert i.plane_ionization == 1 and not i.symmetric_xyz
+    assert (i.nx, i.ny, i.nz) == (3, 300, 3) and i.n_cells == 2700
+    assert i.l_star > 0 and i.lg_gas and not i.lg_dust
+    # the slab's cells tile the cuboid of the density file
+    import numpy as np
+    x, y, z = (s.get(a).astype(np.float64) for a in (abi.ARR_XAXIS, abi.ARR_YAXIS, abi.ARR_ZAXIS))
+    assert s.get(abi.ARR_VOLUME)[1:].astype(np.float64).sum() == pytest.approx(
+        (x[-1] - x[0]) * (y[-1] - y[0]) * (z[-1] - z[0]) / 1e45, rel=1e-5)
+
+
+def test_xray_benchmark_continuum_file_is_rejected(tmp_path, data_dir):
+    with pytest.raises(RuntimeError, match="continuum"):
+        Setup(_deck(tmp_path, "X1"), data_dir)

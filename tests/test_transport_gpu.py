@@ -194,3 +194,92 @@ def test_viewing_angle_planes_match_oracle(tmp_path, data_dir, oracle_lib, views
         assert esc[k].sum() == pytest.approx(eo[k].sum(), abs=4 * de), k
     assert esc[1].sum() > 0 and esc[2].sum() > 0
     ctx.close()
+
+
+@pytest.fixture(scope="module")
+def slab_deck(tmp_path_factory):
+    return configs.plane_slab(tmp_path_factory.mktemp("slab") / "s", nu_max=25.0)
+
+
+def test_plane_slab_fp64_matches_oracle(slab_deck, data_dir, oracle_lib):
+    """Plane-parallel ionisation: packets born on y = 0 moving along +y, the
+    slab's x and z faces reflecting, escapes through the y faces
+    (source/photon_mod.f90:795-856, :3249-3611): the FP64 histories equal the
+    oracle's, J bit for bit, with the hand-off to the trapped-packet kernels
+    on and off."""
+    s = Setup(slab_deck, data_dir)
+    op = oracle_lib.opacity(s)
+    rec = synthetic_recpdf(s.get(abi.ARR_NU), s.n_cells, seed=4)
+    tl = np.full(s.n_cells + 1, 0.2, np.float32)
+    ctx = Context(0)
+    ctx.load(s)
+    ctx.put(abi.ARR_OPACITY, op)
+    ctx.put(abi.ARR_RECPDF, rec)
+    ctx.put(abi.ARR_TOTAL_LINES, tl)
+    n, seed = 30000, 71
+    jo, eo, so = oracle_lib.transport(s, op, rec, tl, n=n, seed=seed, nthreads=8)
+    assert so.error == 0 and so.absorptions > 0
+    keys = ("crossings", "interactions", "absorptions", "scatterings", "escaped", "line_escapes", "emissions",
+            "trapped")
+    for at in (-1, 1):
+        st = ctx.transport(n, seed=seed, precision=abi.PREC_FP64, handoff_emissions=at)
+        for k in keys:
+            assert getattr(st, k) == getattr(so, k), (at, k)
+        np.testing.assert_array_equal(ctx.get(abi.ARR_JSTE), jo)
+        np.testing.assert_allclose(ctx.get(abi.ARR_ESCAPED), eo, rtol=1e-12, atol=0)
+    # the production precision moves histories between kernels without changing them either
+    ref = ctx.transport(n, seed=seed, precision=abi.PREC_FP32_GEOM, handoff_emissions=-1)
+    j32 = ctx.get(abi.ARR_JSTE)
+    st = ctx.transport(n, seed=seed, precision=abi.PREC_FP32_GEOM, handoff_emissions=1)
+    assert st.handed_off > 0 and all(getattr(st, k) == getattr(ref, k) for k in keys)
+    np.testing.assert_array_equal(ctx.get(abi.ARR_JSTE), j32)
+    ctx.close()
+
+
+def test_plane_slab_thin_known_answer(slab_deck, data_dir):
+    """No opacity: every transported packet crosses each y-layer once, so each
+    layer collects sum(J dV) = transported packets x deltaE x thickness."""
+    s = Setup(slab_deck, data_dir)
+    i = s.info
+    C1, nb = s.n_cells + 1, s.nbins
+    ctx = Context(0)
+    ctx.load(s)
+    ctx.put(abi.ARR_OPACITY, np.zeros((nb, C1), np.float32))
+    ctx.put(abi.ARR_RECPDF, synthetic_recpdf(s.get(abi.ARR_NU), s.n_cells))
+    ctx.put(abi.ARR_TOTAL_LINES, np.zeros(C1, np.float32))
+    n = 100000
+    st = ctx.transport(n, seed=9, precision=abi.PREC_FP64)
+    assert st.escaped == n and st.interactions == 0 and st.crossings % i.ny == 0
+    j = ctx.get(abi.ARR_JSTE)
+
+    def widths(a):
+        a = a.astype(np.float64)
+        w = np.empty_like(a)
+        w[1:-1] = (a[2:] - a[:-2]) / 2.0
+        w[0], w[-1] = (a[1] - a[0]) / 2.0, (a[-1] - a[-2]) / 2.0
+        return w / 1e15
+
+    wx, wy, wz = (widths(s.get(a)) for a in (abi.ARR_XAXIS, abi.ARR_YAXIS, abi.ARR_ZAXIS))
+    per_cell = j[:, 1:].reshape(nb, i.nx, i.ny, i.nz).sum(axis=0) * np.einsum("i,j,k->ijk", wx, wy, wz)
+    dE = float(np.float32(i.l_star)) / n
+    np.testing.assert_allclose(per_cell.sum(axis=(0, 2)), (st.crossings // i.ny) * dE * wy * 1e15, rtol=1e-9)
+    ctx.close()
+
+
+def test_plane_slab_iterates(tmp_path, data_dir):
+    """A few whole iterations of a slab through iterate_mc: at n_H = 1e4 the
+    plane's Stromgren depth (~1e17 cm) lies inside the 3e18 cm slab, so the
+    ionised layer forms at the lit face and the far side stays neutral."""
+    from mocassin_xray_gb300 import iterate_mc
+    s = Setup(configs.plane_slab(tmp_path / "dense", nh=1.0e4, nu_max=25.0), data_dir)
+    ctx = Context(0)
+    ctx.load(s)
+    reps = iterate_mc(s, ctx, seed=3, n_photons=100000, max_iterations=3)
+    assert len(reps) == 3
+    i = s.info
+    te = ctx.get(abi.ARR_TE)[1:].reshape(i.nx, i.ny, i.nz)
+    assert np.all(np.isfinite(te)) and te[:, 0, :].mean() > 3000.0
+    ion = ctx.get(abi.ARR_IONDEN).reshape(i.nstages, -1, s.n_cells + 1)
+    xh1 = ion[1, 0, 1:].reshape(i.nx, i.ny, i.nz)       # X(H+)
+    assert xh1[:, 0, :].mean() > xh1[:, -1, :].mean()
+    ctx.close()
