@@ -122,9 +122,9 @@ void parseInput(Params& p, const std::string& path) {
       p.contShape = toS(t, 1, kw);
       if (p.contShape == "powerlaw") {
         p.pwlIndex = toF(t, 2, kw); p.pwlMin = toF(t, 3, kw); p.pwlMax = toF(t, 4, kw);
-      } else if (p.contShape != "blackbody") {
-        fail("readInput: only blackbody and powerlaw continuum shapes are supported, got " + p.contShape);
       }
+      // any other shape names a spectrum file, read in the 'rauch' format
+      // (source/set_input_mod.f90:320-324)
     }
     else if (kw == "nebComposition") {
       std::string v = toS(t, 1, kw);
@@ -711,14 +711,59 @@ float getFlux(const Setup& s, float energy, float temperature) {
   return powf(energy, -s.p.pwlIndex) * expf(-energy / s.p.pwlMax) * expf(-s.p.pwlMin / energy);
 }
 
+// A tabulated spectrum in the 'rauch' format (setContinuum,
+// source/continuum_mod.f90:214-262): rows of wavelength [A] (read as REAL)
+// and H_lambda [erg/cm^2/s/A/sr] (FP64) in ascending wavelength; each row
+// becomes H_nu (FP64) and nu [Ryd] (REAL), reversed into ascending frequency,
+// and the mesh takes log-log interpolation between the rows that bracket it
+// (zero where the row's flux is not above 1e-20); the caller multiplies by 4 pi.
+void readSpectrumFile(Setup& s, std::vector<double>& erg) {
+  const int nb = s.nbins;
+  const auto rows = readNumbers(joinPath(s.p.baseDir, s.p.contShape));
+  const float c = 2.9979250e10f;
+  std::vector<double> hflux;
+  std::vector<float> en;
+  for (const auto& r : rows) {
+    if (r.size() < 2) continue;
+    const float lam = (float)r[0];
+    hflux.push_back((r[1] * (double)(1.e-8f * (lam * lam))) / (double)c / 4.);
+    en.push_back((c / (lam * 1.e-8f)) / kCRyd);
+  }
+  const int numLam = (int)en.size();
+  if (numLam < 1) fail("setContinuum: no rows in spectrum file " + s.p.contShape);
+  std::reverse(hflux.begin(), hflux.end());
+  std::reverse(en.begin(), en.end());
+  for (int i = 0; i < nb; ++i) {
+    const float nu = s.nu[i];
+    if (!(nu >= en[0] && nu <= en[numLam - 1])) continue;
+    const int enP = locate(en.data(), numLam, nu);
+    if (enP < numLam) {
+      erg[i] = std::pow(10., std::log10(hflux[enP - 1]) + std::log10(hflux[enP] / hflux[enP - 1]) *
+                                 (double)log10f(nu / en[enP - 1]) / (double)log10f(en[enP] / en[enP - 1]));
+      if (!(hflux[enP - 1] > 1.e-20)) erg[i] = 0.;
+    } else {
+      erg[i] = hflux[enP - 1] > 1.e-20 ? hflux[enP - 1] : 0.;
+    }
+  }
+}
+
 void setContinuum(Setup& s) {
   const int nb = s.nbins;
   s.lymanP = locate(s.nu.data(), nb, 1.f);
   s.inSpectrumErg.assign(nb, 0.);
   s.inSpectrumPhot.assign(nb, 0.);
-  for (int i = 0; i < nb; ++i) {
-    s.inSpectrumErg[i] = getFlux(s, s.nu[i], s.p.TStellar);
-    s.inSpectrumPhot[i] = s.inSpectrumErg[i] / ((double)s.nu[i] * (double)kHcRyd);
+  if (s.p.contShape == "blackbody" || s.p.contShape == "powerlaw") {
+    for (int i = 0; i < nb; ++i) {
+      s.inSpectrumErg[i] = getFlux(s, s.nu[i], s.p.TStellar);
+      s.inSpectrumPhot[i] = s.inSpectrumErg[i] / ((double)s.nu[i] * (double)kHcRyd);
+    }
+  } else {
+    readSpectrumFile(s, s.inSpectrumErg);
+    for (int i = 0; i < nb; ++i) {
+      s.inSpectrumPhot[i] = s.inSpectrumErg[i] / ((double)s.nu[i] * (double)kHcRyd);
+      s.inSpectrumErg[i] = (double)kFourPi * s.inSpectrumErg[i];
+      s.inSpectrumPhot[i] = (double)kFourPi * s.inSpectrumPhot[i];
+    }
   }
   // setProbDen (source/continuum_mod.f90:415-504); inSpSum* are REAL there
   std::vector<float> sumErg(nb), sumPhot(nb);

@@ -46,7 +46,7 @@ struct Params {
   float viewTheta[2] = {0.f, 0.f}, viewPhi[2] = {0.f, 0.f};
   bool haveStarPos = false, haveLStar = false, haveTStellar = false;
   bool haveContShape = false, haveNPhotons = false, haveAbundance = false;
-  std::string contShape;          // "blackbody" | "powerlaw"
+  std::string contShape;          // "blackbody" | "powerlaw" | a spectrum file (read as 'rauch')
   std::string densityFile, abundanceFile, NdustFile;
   std::string dustFile[2];
   std::string baseDir;            // directory the deck's relative paths are resolved against

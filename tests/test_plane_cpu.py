@@ -146,3 +146,27 @@ def test_slab_reflects_at_the_sides(slab, oracle_lib):
     assert st.error == 0
     assert st.escaped + st.line_escapes + st.trapped == n
     assert st.absorptions > 0 and st.crossings > 0
+
+
+def test_tabulated_spectrum_file(tmp_path, data_dir):
+    """A continuum given as a file ('rauch' format: wavelength [A], H_lambda;
+    source/continuum_mod.f90:214-262) is interpolated log-log onto the mesh:
+    a file that tabulates a power law H_nu ~ nu^-1.3 gives the source CDF of
+    the analytic power law (cut-offs far outside the mesh)."""
+    c, c_ryd = 2.9979250e10, 3.2898423e15
+    lam = np.logspace(0.5, 8.5, 400)                       # [A], ascending
+    nu = c / (lam * 1e-8) / c_ryd                          # [Ryd]
+    h_nu = nu ** -1.3
+    h_lam = 4.0 * h_nu * c / (1e-8 * lam ** 2)
+    cdfs = []
+    for shape in ("file", "powerlaw"):
+        deck = configs.plane_slab(tmp_path / shape, nu_max=25.0)
+        text = deck.read_text()
+        if shape == "file":
+            (deck.parent / "spec.in").write_text("".join(f"{a:.9e} {b:.9e}\n" for a, b in zip(lam, h_lam)))
+            text = text.replace("contShape powerlaw 1.3 7.353e-2 7351.", "contShape 'input/spec.in'")
+        else:
+            text = text.replace("contShape powerlaw 1.3 7.353e-2 7351.", "contShape powerlaw 1.3 1.e-30 1.e30")
+        deck.write_text(text)
+        cdfs.append(Setup(deck, data_dir).get(abi.ARR_SRC_CDF))
+    np.testing.assert_allclose(cdfs[0], cdfs[1], rtol=0, atol=2e-5)

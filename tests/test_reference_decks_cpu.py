@@ -1,12 +1,13 @@
 """The reference's own benchmark decks (benchmarks/gas) read by the deck grammar of libmcx, when a
 MOCASSIN source tree is named by MCX_REFERENCE_DIR on the machine running the tests: the
 photoionisation benchmarks parse into grids of the expected shape, the plane-parallel NLR benchmark
-parses into its slab, and the decks that select paths outside this library (the X-ray benchmarks'
-tabulated continuum file) are rejected with a message, not misread."""
+and X-ray benchmarks parse into their slabs, and the decks that select paths outside this library
+(resonance-line transfer) are rejected with a message, not misread."""
 import os
 import shutil
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 from mocassin_xray_gb300 import abi, Setup
@@ -44,12 +45,24 @@ def test_plane_parallel_nlr_benchmark_parses(tmp_path, data_dir):
     assert (i.nx, i.ny, i.nz) == (3, 300, 3) and i.n_cells == 2700
     assert i.l_star > 0 and i.lg_gas and not i.lg_dust
     # the slab's cells tile the cuboid of the density file
-    import numpy as np
     x, y, z = (s.get(a).astype(np.float64) for a in (abi.ARR_XAXIS, abi.ARR_YAXIS, abi.ARR_ZAXIS))
     assert s.get(abi.ARR_VOLUME)[1:].astype(np.float64).sum() == pytest.approx(
         (x[-1] - x[0]) * (y[-1] - y[0]) * (z[-1] - z[0]) / 1e45, rel=1e-5)
 
 
-def test_xray_benchmark_continuum_file_is_rejected(tmp_path, data_dir):
-    with pytest.raises(RuntimeError, match="continuum"):
-        Setup(_deck(tmp_path, "X1"), data_dir)
+@pytest.mark.parametrize("name,lstar_ratio", [("X1", 1.0), ("X10", 10.0)])
+def test_xray_plane_benchmarks_parse(tmp_path, data_dir, name, lstar_ratio):
+    """The X-ray benchmarks: plane sources with a tabulated continuum file,
+    31 stages; X10's plane flux is ten times X1's."""
+    s = Setup(_deck(tmp_path, name), data_dir)
+    i = s.info
+    assert i.plane_ionization == 1 and (i.nx, i.ny, i.nz) == (3, 30, 3) and i.nstages == 31
+    cdf = s.get(abi.ARR_SRC_CDF)
+    assert cdf[-1] == 1.0 and np.all(np.diff(cdf) >= 0)
+    ref = Setup(_deck(tmp_path / "x1", "X1"), data_dir).info.l_star
+    assert i.l_star == pytest.approx(lstar_ratio * ref, rel=1e-5)
+
+
+def test_resonance_line_transfer_deck_is_rejected(tmp_path, data_dir):
+    with pytest.raises(RuntimeError, match="resLinesTransfer"):
+        Setup(_deck(tmp_path, "X01"), data_dir)
