@@ -131,17 +131,19 @@ def lognormal_gas(root: str | Path, n: int = 41, packets: int = 10_000_000, iter
 def plane_slab(root: str | Path, nx: int = 5, ny: int = 30, nz: int = 5, packets: int = 100_000,
                iterations: int = 6, nbins: int = 400, depth: float = 3.0e18, width: float = 3.0e17,
                nh: float = 1.0e3, mean_field: float = 2.9979e12, nu0: float = 1.0, nu0_add: float = 0.56,
-               nu_max: float = 100.0) -> Path:
+               nu_max: float = 100.0, abundances: dict[str, float] | None = None, nstages: int = 3,
+               cont_shape: str = "powerlaw 1.3 7.353e-2 7351.") -> Path:
     """A plane-parallel slab lit from its y = 0 face (the reference's
-    'planeIonization' geometry, as in its NLR benchmark): a cuboid of nx x ny x
-    nz cells on the axes [0, width] x [0, depth] x [0, width] given through a
-    density file, uniform H + He gas of density nh, a nu^-1.3 power-law
-    source from 7.35e-2 to 7351 Ryd whose photon flux above nu0 Ryd is
-    mean_field [cm^-2 s^-1], nothing emitted below nu0_add Ryd."""
+    'planeIonization' geometry, as in its NLR and X-ray benchmarks): a cuboid
+    of nx x ny x nz cells on the axes [0, width] x [0, depth] x [0, width]
+    given through a density file, uniform gas of density nh (H + He unless
+    `abundances` says otherwise), a source of shape `cont_shape` (default a
+    nu^-1.3 power law from 7.35e-2 to 7351 Ryd) whose photon flux above nu0
+    Ryd is mean_field [cm^-2 s^-1], nothing emitted below nu0_add Ryd."""
     root = Path(root)
     inp = root / "input"
     inp.mkdir(parents=True, exist_ok=True)
-    _write_abundances(inp / "abun_slab.in", {"H": 1.0, "He": 0.1})
+    _write_abundances(inp / "abun_slab.in", abundances or {"H": 1.0, "He": 0.1})
     xs = np.linspace(0.0, width, nx)
     ys = np.linspace(0.0, depth, ny)
     zs = np.linspace(0.0, width, nz)
@@ -154,14 +156,14 @@ def plane_slab(root: str | Path, nx: int = 5, ny: int = 30, nz: int = 5, packets
         "Rin 0.",
         "Rout 1.e20",
         "TStellar 0.",
-        "contShape powerlaw 1.3 7.353e-2 7351.",
+        f"contShape {cont_shape}",
         f"nbins {nbins}",
         "nuMin 1.001e-5",
         f"nuMax {nu_max:g}",
         f"nPhotons {packets}",
         f"maxIterateMC {iterations} 95.",
         "TeStart 10000.",
-        "nstages 3",
+        f"nstages {nstages}",
         "nebComposition 'input/abun_slab.in'",
     ])
 

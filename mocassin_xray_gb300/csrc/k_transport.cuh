@@ -233,11 +233,12 @@ struct TransportShared {
 };
 
 // The grid a packet travels in, read through accessors so that one emit /
-// step code serves both kernels: OneGrid reads the context's single grid from
+// step code serves both kernels: OneGrid<plane> reads the context's single grid from
 // the kernel parameters (axes and source CDF staged in shared memory);
 // NebulaGeo holds, in registers, the nebula of a batch that the packet belongs
 // to (axes, active map and CDF slices of the concatenated batch arrays; the
 // active map holds batch-wide cell ids).
+template <bool kPlane>
 struct OneGrid {
   const DevGrid& g;
   const float* sX; const float* sY; const float* sZ; const float* sCdf;
@@ -251,7 +252,9 @@ struct OneGrid {
   __device__ __forceinline__ const float* Z() const { return sZ; }
   __device__ __forceinline__ const int32_t* active() const { return g.active; }
   __device__ __forceinline__ bool activeFull() const { return g.activeFull != 0; }
-  __device__ __forceinline__ bool plane() const { return g.plane != 0; }
+  // fixed per instantiation: the kernels are built with and without the
+  // plane-parallel source, so that other grids carry none of its code
+  __device__ __forceinline__ constexpr bool plane() const { return kPlane; }
   __device__ __forceinline__ const float* cdf() const { return sCdf; }
   __device__ __forceinline__ int starIdx(int d) const { return g.starIdx[d]; }
   __device__ __forceinline__ float starPos(int d) const { return g.starPos[d]; }
@@ -275,7 +278,7 @@ struct NebulaGeo {
   __device__ __forceinline__ const float* Z() const { return Z_; }
   __device__ __forceinline__ const int32_t* active() const { return active_; }
   __device__ __forceinline__ bool activeFull() const { return false; }
-  __device__ __forceinline__ bool plane() const { return false; }
+  __device__ __forceinline__ constexpr bool plane() const { return false; }
   __device__ __forceinline__ const float* cdf() const { return cdf_; }
   __device__ __forceinline__ int starIdx(int d) const { return starIdx_[d]; }
   __device__ __forceinline__ float starPos(int d) const { return starPos_[d]; }
@@ -947,7 +950,7 @@ __device__ __forceinline__ unsigned long long refill(unsigned need, DevTransport
   return first + (unsigned long long)__popc(need & ((1u << lane) - 1u));
 }
 
-template <typename R>
+template <typename R, bool kPlane>
 __global__ void __launch_bounds__(256)
 transportKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportCounters* cnt,
                 uint64_t seed, uint64_t base, unsigned long long n, double deltaE, int emitBatch,
@@ -964,7 +967,7 @@ transportKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportC
   for (int i = threadIdx.x; i < g.nbins; i += blockDim.x) { sNu[i] = g.nu[i]; sCdf[i] = g.srcCDF[i]; }
   __syncthreads();
   TransportShared<R> sh{sNu};
-  const OneGrid q{g, sX, sY, sZ, sCdf};
+  const OneGrid<kPlane> q{g, sX, sY, sZ, sCdf};
 
   const unsigned FULL = 0xffffffffu;
   const R deltaER = (R)deltaE;
@@ -1020,7 +1023,7 @@ transportKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportC
 // put to work on its data-parallel parts (the Philox stream, the CDF search)
 // while all lanes run the scalar physics in lockstep.  No shared memory: axes
 // and frequencies are read through L1, which keeps its full size.
-template <typename R>
+template <typename R, bool kPlane>
 __global__ void __launch_bounds__(32, 16)   // 16 histories per SM, 2432 at once on 152 SMs: no spills at 128 registers
 transportTrappedKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportCounters* cnt, double deltaE,
                        const Packet<R>* __restrict__ parked, unsigned long long parkedCap,
@@ -1030,7 +1033,7 @@ transportTrappedKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTra
   // many more histories than resident warps: transportTrappedLanesKernel runs them
   if (count > warpMax) return;
   TransportShared<R> sh{g.nu};
-  const OneGrid q{g, g.xAxis, g.yAxis, g.zAxis, g.srcCDF};
+  const OneGrid<kPlane> q{g, g.xAxis, g.yAxis, g.zAxis, g.srcCDF};
   const R deltaER = (R)deltaE;
   LocalCounters lc;
   PendingJ pj{0., 0., 0, false};
@@ -1044,7 +1047,7 @@ transportTrappedKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTra
     p.cdfShape = cdfShape;
     int state = ST_EMIT;
     while (state == ST_EMIT || state == ST_STEP) {
-      if (state == ST_EMIT) state = emitBody<R, OneGrid>(g, q, in, out, sh, p, deltaE, lc);
+      if (state == ST_EMIT) state = emitBody<R, OneGrid<kPlane>>(g, q, in, out, sh, p, deltaE, lc);
       else state = stepPacket<R>(g, q, in, out, sh, p, deltaER, deltaE, lc, pj);
     }
     unsigned long long nxt = 0;
@@ -1062,7 +1065,7 @@ transportTrappedKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTra
 // with the main kernel's emission batching; the warp kernel's single-history
 // latency matters less here than running every history at once.  Histories
 // in registers, event code inlined, no shared memory.
-template <typename R>
+template <typename R, bool kPlane>
 __global__ void __launch_bounds__(128)
 transportTrappedLanesKernel(DevGrid g, DevTransportIn in, DevTransportOut out, DevTransportCounters* cnt,
                             double deltaE, const Packet<R>* __restrict__ parked, unsigned long long parkedCap,
@@ -1071,7 +1074,7 @@ transportTrappedLanesKernel(DevGrid g, DevTransportIn in, DevTransportOut out, D
   const unsigned long long count = written < parkedCap ? written : parkedCap;
   if (count <= warpMax) return;   // transportTrappedKernel has them, one per warp
   TransportShared<R> sh{g.nu};
-  const OneGrid q{g, g.xAxis, g.yAxis, g.zAxis, g.srcCDF};
+  const OneGrid<kPlane> q{g, g.xAxis, g.yAxis, g.zAxis, g.srcCDF};
   const R deltaER = (R)deltaE;
   const unsigned FULL = 0xffffffffu;
   const unsigned lane = threadIdx.x & 31u;
@@ -1095,7 +1098,7 @@ transportTrappedLanesKernel(DevGrid g, DevTransportIn in, DevTransportOut out, D
     }
     if (__ballot_sync(FULL, state != ST_DONE) == 0u) break;
     if (emitTurn(state, emitBatch)) {
-      if (state == ST_EMIT) state = emitBody<R, OneGrid>(g, q, in, out, sh, p, deltaE, lc);
+      if (state == ST_EMIT) state = emitBody<R, OneGrid<kPlane>>(g, q, in, out, sh, p, deltaE, lc);
     } else if (state == ST_STEP) {
       state = stepPacket<R>(g, q, in, out, sh, p, deltaER, deltaE, lc, pj);
     }
@@ -1204,15 +1207,15 @@ transportKernelBatched(DevGrid g, DevTransportIn in, DevTransportOut out, DevTra
 // The single-grid launch: the persistent kernel, then, when hand-off is on,
 // the trapped-packet kernel with one warp per block on every SM (as many
 // blocks as are resident at once, so every parked history starts at once).
-template <typename R>
-cudaError_t launchTransportImpl(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,
+template <typename R, bool kPlane>
+cudaError_t launchTransportPlane(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,
                                 DevTransportCounters* cnt, uint64_t seed, uint64_t base, unsigned long long n,
                                 double deltaE, const TransportLaunch& L, cudaStream_t s) {
   const size_t smem = packetStateOffset(L.smem) + packetStateBytes<R>(L.threads);
-  cudaError_t e = cudaFuncSetAttribute(transportKernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(transportKernel<R, kPlane>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const bool hand = L.parked != nullptr && L.parkedCap > 0 && L.handoffAt > 0 && L.numSMs > 0;
-  transportKernel<R><<<L.blocks, L.threads, smem, s>>>(g, in, out, cnt, seed, base, n, deltaE,
+  transportKernel<R, kPlane><<<L.blocks, L.threads, smem, s>>>(g, in, out, cnt, seed, base, n, deltaE,
                                                        L.emitBatch > 0 ? L.emitBatch : kEmitBatch,
                                                        hand ? static_cast<Packet<R>*>(L.parked) : nullptr,
                                                        hand ? L.parkedCap : 0ull, hand ? L.handoffAt : 0);
@@ -1225,23 +1228,31 @@ cudaError_t launchTransportImpl(const DevGrid& g, const DevTransportIn& in, cons
   // run), one per lane beyond (the 41^3 X-ray run parks ~2e4 trapped histories,
   // which would take ten waves one per warp)
   int perSM = 0, lanesPerSM = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, transportTrappedKernel<R>, 32, 0);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, transportTrappedKernel<R, kPlane>, 32, 0);
   if (e != cudaSuccess) return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lanesPerSM, transportTrappedLanesKernel<R>, 128, 0);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lanesPerSM, transportTrappedLanesKernel<R, kPlane>, 128, 0);
   if (e != cudaSuccess) return e;
   if (perSM < 1) perSM = 1;
   if (lanesPerSM < 1) lanesPerSM = 1;
   const unsigned long long warpSlots = (unsigned long long)L.numSMs * perSM;
   const unsigned long long warpMax = 3 * warpSlots;
-  transportTrappedKernel<R><<<(unsigned)warpSlots, 32, 0, s>>>(g, in, out, cnt, deltaE,
+  transportTrappedKernel<R, kPlane><<<(unsigned)warpSlots, 32, 0, s>>>(g, in, out, cnt, deltaE,
                                                                static_cast<const Packet<R>*>(L.parked), L.parkedCap,
                                                                warpMax);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  transportTrappedLanesKernel<R><<<L.numSMs * lanesPerSM, 128, 0, s>>>(
+  transportTrappedLanesKernel<R, kPlane><<<L.numSMs * lanesPerSM, 128, 0, s>>>(
       g, in, out, cnt, deltaE, static_cast<const Packet<R>*>(L.parked), L.parkedCap, warpMax,
       L.emitBatch > 0 ? L.emitBatch : kEmitBatch);
   return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launchTransportImpl(const DevGrid& g, const DevTransportIn& in, const DevTransportOut& out,
+                                DevTransportCounters* cnt, uint64_t seed, uint64_t base, unsigned long long n,
+                                double deltaE, const TransportLaunch& L, cudaStream_t s) {
+  return g.plane ? launchTransportPlane<R, true>(g, in, out, cnt, seed, base, n, deltaE, L, s)
+                 : launchTransportPlane<R, false>(g, in, out, cnt, seed, base, n, deltaE, L, s);
 }
 
 }  // namespace mcx

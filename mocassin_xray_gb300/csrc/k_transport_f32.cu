@@ -37,11 +37,17 @@ cudaError_t transportOccupancyBatchedF32(int threads, size_t smem, int* blocksPe
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, transportKernelBatched<float>, threads, all);
 }
 
-cudaError_t transportOccupancyF32(int threads, size_t smem, int* blocksPerSM) {
+template <bool kPlane>
+static cudaError_t occupancyF32(int threads, size_t smem, int* blocksPerSM) {
   const size_t all = packetStateOffset(smem) + packetStateBytes<float>(threads);
-  cudaError_t e = cudaFuncSetAttribute(transportKernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)all);
+  cudaError_t e =
+      cudaFuncSetAttribute(transportKernel<float, kPlane>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)all);
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, transportKernel<float>, threads, all);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, transportKernel<float, kPlane>, threads, all);
+}
+
+cudaError_t transportOccupancyF32(int threads, size_t smem, int* blocksPerSM, bool plane) {
+  return plane ? occupancyF32<true>(threads, smem, blocksPerSM) : occupancyF32<false>(threads, smem, blocksPerSM);
 }
 
 }  // namespace mcx

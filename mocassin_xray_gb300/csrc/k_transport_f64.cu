@@ -37,11 +37,17 @@ cudaError_t transportOccupancyBatchedF64(int threads, size_t smem, int* blocksPe
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, transportKernelBatched<double>, threads, all);
 }
 
-cudaError_t transportOccupancyF64(int threads, size_t smem, int* blocksPerSM) {
+template <bool kPlane>
+static cudaError_t occupancyF64(int threads, size_t smem, int* blocksPerSM) {
   const size_t all = packetStateOffset(smem) + packetStateBytes<double>(threads);
-  cudaError_t e = cudaFuncSetAttribute(transportKernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)all);
+  cudaError_t e =
+      cudaFuncSetAttribute(transportKernel<double, kPlane>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)all);
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, transportKernel<double>, threads, all);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, transportKernel<double, kPlane>, threads, all);
+}
+
+cudaError_t transportOccupancyF64(int threads, size_t smem, int* blocksPerSM, bool plane) {
+  return plane ? occupancyF64<true>(threads, smem, blocksPerSM) : occupancyF64<false>(threads, smem, blocksPerSM);
 }
 
 }  // namespace mcx

@@ -44,13 +44,14 @@ cudaError_t transportOccupancyBatchedF64(int threads, size_t smem, int* blocksPe
 size_t parkedPacketBytesF32();
 size_t parkedPacketBytesF64();
 
-// Resident blocks per SM of the FP64 (fp64 = true) or FP32 instantiation.
-cudaError_t transportOccupancy(bool fp64, int threads, size_t smem, int* blocksPerSM);
-cudaError_t transportOccupancyF32(int threads, size_t smem, int* blocksPerSM);
-cudaError_t transportOccupancyF64(int threads, size_t smem, int* blocksPerSM);
+// Resident blocks per SM of the FP64 (fp64 = true) or FP32 instantiation of
+// the persistent kernel, with or without the plane-parallel source.
+cudaError_t transportOccupancyF32(int threads, size_t smem, int* blocksPerSM, bool plane);
+cudaError_t transportOccupancyF64(int threads, size_t smem, int* blocksPerSM, bool plane);
 
-inline cudaError_t transportOccupancy(bool fp64, int threads, size_t smem, int* blocksPerSM) {
-  return fp64 ? transportOccupancyF64(threads, smem, blocksPerSM) : transportOccupancyF32(threads, smem, blocksPerSM);
+inline cudaError_t transportOccupancy(bool fp64, int threads, size_t smem, int* blocksPerSM, bool plane) {
+  return fp64 ? transportOccupancyF64(threads, smem, blocksPerSM, plane)
+              : transportOccupancyF32(threads, smem, blocksPerSM, plane);
 }
 
 }  // namespace mcx

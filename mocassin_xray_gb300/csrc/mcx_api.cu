@@ -1368,7 +1368,7 @@ extern "C" int mcx_transport(mcx_ctx* c, const mcx_transport_opts* o, mcx_transp
   if (L.threads % 32 != 0 || L.threads > 256) return fail(c, MCX_ERR_INPUT, "mcx_transport: block_size must be a multiple of 32 up to 256");
   L.smem = (size_t)(c->nx + c->ny + c->nz + 2 * c->nbins) * sizeof(float);
   int perSM = 0;
-  CK(transportOccupancy(o->precision == MCX_PREC_FP64, L.threads, L.smem, &perSM), "occupancy");
+  CK(transportOccupancy(o->precision == MCX_PREC_FP64, L.threads, L.smem, &perSM, c->plane != 0), "occupancy");
   if (perSM < 1) perSM = 1;
   int mult = o->grid_mult > 0 ? std::min(o->grid_mult, perSM) : perSM;
   L.blocks = c->numSMs * mult;

@@ -194,7 +194,7 @@ extern "C" int mcx_transport_noalloc(const mcx_noalloc_transport_args* a, mcx_tr
   L.threads = 256;
   L.smem = (size_t)(a->nx + a->ny + a->nz + 2 * a->nbins) * sizeof(float);
   int perSM = 0;
-  NA_CK(transportOccupancy(a->precision == MCX_PREC_FP64, L.threads, L.smem, &perSM), "occupancy");
+  NA_CK(transportOccupancy(a->precision == MCX_PREC_FP64, L.threads, L.smem, &perSM, false), "occupancy");
   L.blocks = numSMs * (perSM < 1 ? 1 : perSM);
   const unsigned long long n = (unsigned long long)a->n_packets;
   if (n > 0) {

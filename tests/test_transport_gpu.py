@@ -283,3 +283,36 @@ def test_plane_slab_iterates(tmp_path, data_dir):
     xh1 = ion[1, 0, 1:].reshape(i.nx, i.ny, i.nz)       # X(H+)
     assert xh1[:, 0, :].mean() > xh1[:, -1, :].mean()
     ctx.close()
+
+
+def test_xray_plane_slab_iterates(tmp_path, data_dir, oracle_lib):
+    """The geometry of the reference's X-ray benchmarks: a plane-parallel slab
+    lit by a hard power law to 740 Ryd, H to Fe with 31 stages (K shells and
+    Auger yields): its FP64 transport equals the oracle's and whole
+    production iterations run."""
+    from mocassin_xray_gb300 import iterate_mc
+    deck = configs.plane_slab(tmp_path / "xslab", nh=1.0e3, mean_field=2.9979e15, nu0=7.3529, nu0_add=0.56,
+                              nu_max=740.0, abundances=configs.XRAY_ABUN, nstages=31,
+                              cont_shape="powerlaw 1.5 1. 740.")
+    s = Setup(deck, data_dir)
+    assert s.info.plane_ionization == 1 and s.info.nstages == 31
+    op = oracle_lib.opacity(s)
+    rec = synthetic_recpdf(s.get(abi.ARR_NU), s.n_cells, seed=6)
+    tl = np.full(s.n_cells + 1, 0.1, np.float32)
+    ctx = Context(0)
+    ctx.load(s)
+    ctx.put(abi.ARR_OPACITY, op)
+    ctx.put(abi.ARR_RECPDF, rec)
+    ctx.put(abi.ARR_TOTAL_LINES, tl)
+    n = 20000
+    st = ctx.transport(n, seed=11, precision=abi.PREC_FP64)
+    jo, _, so = oracle_lib.transport(s, op, rec, tl, n=n, seed=11, nthreads=8)
+    assert st.crossings == so.crossings and st.escaped == so.escaped
+    np.testing.assert_array_equal(ctx.get(abi.ARR_JSTE), jo)
+    ctx.close()
+    ctx = Context(0)
+    ctx.load(s)
+    reps = iterate_mc(s, ctx, seed=2, n_photons=50000, max_iterations=2)
+    assert len(reps) == 2
+    assert np.all(np.isfinite(ctx.get(abi.ARR_TE)[1:]))
+    ctx.close()
