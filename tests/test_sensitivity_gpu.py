@@ -132,3 +132,33 @@ def test_tight_balance_is_a_fixed_point(iterated):
     stay = np.abs(te2[1:][ok] / te1[1:][ok] - 1) <= 1e-6
     assert stay.mean() >= 0.995
     assert np.median(np.abs(te1[1:][ok] / te_ref[1:][ok] - 1)) < 0.02
+
+
+def test_autograd_wrapper(iterated):
+    """mocassin_xray_gb300.autograd.frozen_field_lines: a torch.autograd.Function whose backward
+    contracts the incoming gradient with the frozen-field derivatives; its gradient matches a
+    one-cell difference of its own forward."""
+    import torch
+    from mocassin_xray_gb300.autograd import frozen_field_lines
+    s, ctx = iterated
+    hden0 = ctx.get(abi.ARR_HDEN).astype(np.float64)
+    hden = torch.tensor(hden0, requires_grad=True)
+    abun = torch.zeros(2, dtype=torch.float64, requires_grad=True)
+    L = frozen_field_lines(ctx, hden, LINES[:2], abun=abun, abun_z=[8, 7], slot=0, precision=abi.BAL_FP64)
+    w = torch.tensor([1.0, 0.5], dtype=torch.float64)
+    (w * L).sum().backward()
+    ctx.state_restore()
+    r = ctx.line_sensitivities(LINES[:2], abun_z=[8, 7], precision=abi.BAL_FP64)
+    np.testing.assert_allclose(L.detach().numpy(), r["L"], rtol=1e-12)
+    np.testing.assert_allclose(hden.grad.numpy(), w.numpy() @ r["dL_dhden"], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(abun.grad.numpy(), w.numpy() @ r["dL_dabun"], rtol=1e-12, atol=0)
+    # a one-cell difference through the forward
+    g = hden.grad.numpy()
+    c = int(np.argmax(np.abs(g[1:]))) + 1
+    step = np.float32(hden0[c] * 1e-3)
+    hp = hden0.copy()
+    hp[c] = float(np.float32(hden0[c]) + step)
+    Lp = frozen_field_lines(ctx, torch.tensor(hp), LINES[:2], slot=0, precision=abi.BAL_FP64)
+    fd = float((w * (Lp - L.detach())).sum()) / float(hp[c] - np.float32(hden0[c]))
+    assert fd == pytest.approx(g[c], rel=0.05)
+    ctx.put(abi.ARR_HDEN, hden0.astype(np.float32))
