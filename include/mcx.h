@@ -80,6 +80,8 @@ enum mcx_array_id {
     MCX_ARR_N_ITER_T,        /* int32 [nCells+1] T-iterations of the last balance (0 = not updated) */
     MCX_ARR_FOR_LINES,       /* float [nCells+1] forbidden-line total of the last emission phase */
     MCX_ARR_TDUST,           /* float [nSpecies+1][nSizes+1][nCells+1] Tdust(0:nSp,0:nSz,0:C) */
+    MCX_ARR_BAL_RESID,       /* double[nCells+1] heating - cooling at the held Te of the last balance
+                                run with fix_te = 1 (thermBalance's units, erg/cm^3/s per Hden^2 scale) */
     MCX_ARR_COUNT_
 };
 
@@ -317,7 +319,13 @@ typedef struct mcx_balance_opts {
                                    (max_rounds up to 64).  The solution is then a smooth function
                                    of the inputs away from the balance's discontinuities (used for
                                    derivatives)                                           */
-    int32_t reserved[4];
+    int32_t fix_te;             /* 1 (with converge = 1) = hold every cell's Te: calcAlpha,
+                                   photoionisation, Compton and ionBalance at that Te, repeated
+                                   until ionBalance's X(H0), X(He0), X(He+) changes fall below
+                                   1e-14 (MCX_BAL_MIXED: 1e-5), then thermBalance;
+                                   heating - cooling there is left in MCX_ARR_BAL_RESID.  The
+                                   evaluations of mcx_adjoint                             */
+    int32_t reserved[3];
 } mcx_balance_opts;
 
 typedef struct mcx_balance_stats {
@@ -478,6 +486,38 @@ typedef struct mcx_sens_out {
 } mcx_sens_out;
 
 int  mcx_line_sensitivities(mcx_ctx* ctx, const mcx_sens_opts* opts, mcx_sens_out* out);
+
+/* ----------------------------------- adjoint of the converged per-cell balance */
+/* No counterpart in the reference.  The same derivatives as
+ * mcx_line_sensitivities (frozen J), from the implicit-function theorem on the
+ * converged balance instead of perturbed balances: at fixed J a cell's
+ * converged Te is the root of R(Te; p) = heating - cooling of its ionisation
+ * ladder converged at Te, so with L(Te; p) the cell's line luminosities
+ *     dL/dp = dL/dp|Te - dL/dTe|p (dR/dp|Te) / (dR/dTe|p),
+ * p = the cell's Hden or an element's abundance.  The call converges the
+ * balance tightly from the current state (mcx_balance_opts.converge), then
+ * evaluates R and L with every Te held (fix_te) at Te(1 +- h), Hden(1 +- h)
+ * and each listed abundance (1 +- h), all cells at once, and an adjoint kernel
+ * combines the central differences per cell.  No T-iteration is run for a
+ * perturbed p, so a cell whose perturbed balance would take another branch of
+ * the iteration still gets the derivative of its root.  A cell without a root
+ * (its bracket closed on a jump of heating - cooling, no convergence in 64
+ * T-iterations, or dR/dTe not finite and non-zero) has its Te held: dTe/dp = 0,
+ * counted in pinned_cells.  opts as for mcx_line_sensitivities
+ * (reference_stopping must be 0).  The context is left as after the converged
+ * unperturbed balance.  Gas, one nebula. */
+typedef struct mcx_adjoint_out {
+    double* L;                  /* [n_lines] line sums of the converged balance         */
+    double* dL_dhden;           /* [n_lines][nCells+1] or NULL                          */
+    double* dL_dabun;           /* [n_lines][n_abun] or NULL                            */
+    double* dte_dhden;          /* [nCells+1] or NULL: dTe/dHden of each cell's root    */
+    float   kernel_ms;          /* out: CUDA-event time of the balances, lines and adjoint kernels */
+    float   reserved_f[3];
+    int64_t pinned_cells;       /* out: cells with their Te held (no root)              */
+    int64_t reserved[3];
+} mcx_adjoint_out;
+
+int  mcx_adjoint(mcx_ctx* ctx, const mcx_sens_opts* opts, mcx_adjoint_out* out);
 
 /* ------------------------------------------------------- batches of nebulae */
 /* No counterpart in the reference, which runs one nebula per job.  A batch

@@ -21,7 +21,8 @@ ERRORS = {1: "MCX_ERR_INPUT", 2: "MCX_ERR_IO", 3: "MCX_ERR_CUDA", 4: "MCX_ERR_NO
 (ARR_NU, ARR_WIDFLX, ARR_XSEC, ARR_SRC_CDF, ARR_KN_SIGMA_T, ARR_KN_CDF, ARR_PCOMP, ARR_XAXIS, ARR_YAXIS,
  ARR_ZAXIS, ARR_ACTIVE, ARR_HDEN, ARR_TE, ARR_NE, ARR_TEOLD, ARR_NEOLD, ARR_IONDEN, ARR_OPACITY, ARR_RECPDF,
  ARR_TOTAL_LINES, ARR_JSTE, ARR_ESCAPED, ARR_VOLUME, ARR_ELEM_ABUN, ARR_GAUNT_TE, ARR_SCAOPAC, ARR_DUSTPDF,
- ARR_NDUST, ARR_LG_CONVERGED, ARR_H_EST, ARR_LG_BLACK, ARR_N_ITER_T, ARR_FOR_LINES, ARR_TDUST) = range(1, 35)
+ ARR_NDUST, ARR_LG_CONVERGED, ARR_H_EST, ARR_LG_BLACK, ARR_N_ITER_T, ARR_FOR_LINES, ARR_TDUST,
+ ARR_BAL_RESID) = range(1, 36)
 SARR_POINTERS, SARR_ELEMENT_P, SARR_N_SHELLS, SARR_ELEM_XREF, SARR_ION_EDGE, SARR_COMXSEC_H, \
     SARR_COMXSEC_C, SARR_XSEC_RECOIL = range(1001, 1009)
 (SARR_EM_DIMS, SARR_EM_TK, SARR_EM_EDGE_P, SARR_EM_LOG_GAMMA, SARR_EM_FB_HEAVY, SARR_EM_HYDRO_MAP,
@@ -65,7 +66,7 @@ class SetupInfo(C.Structure):
 
 class BalanceOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("max_rounds", C.c_int32), ("atom_solves", C.c_int32),
-                ("converge", C.c_int32), ("reserved", C.c_int32 * 4)]
+                ("converge", C.c_int32), ("fix_te", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class BalanceStats(C.Structure):
@@ -145,6 +146,11 @@ class SensOpts(C.Structure):
                 ("precision", C.c_int32), ("reference_stopping", C.c_int32), ("reserved", C.c_int32 * 4)]
 
 
+class AdjointOut(C.Structure):
+    _fields_ = [("L", _P), ("dL_dhden", _P), ("dL_dabun", _P), ("dte_dhden", _P), ("kernel_ms", C.c_float),
+                ("reserved_f", C.c_float * 3), ("pinned_cells", C.c_int64), ("reserved", C.c_int64 * 3)]
+
+
 class SensOut(C.Structure):
     _fields_ = [("L", _P), ("dL_dhden", _P), ("dL_dabun", _P), ("kernel_ms", C.c_float),
                 ("reserved_f", C.c_float * 3), ("branch_cells_hden", C.c_int64), ("branch_cells_abun", C.c_int64),
@@ -188,6 +194,7 @@ SIGNATURES = [
     ("mcx_line_luminosities_nebula", C.c_int, [_P, C.c_int32, C.POINTER(Lines)]),
     ("mcx_batch_transport_ms", C.c_int, [_P, C.POINTER(C.c_double), C.c_int32]),
     ("mcx_line_sensitivities", C.c_int, [_P, C.POINTER(SensOpts), C.POINTER(SensOut)]),
+    ("mcx_adjoint", C.c_int, [_P, C.POINTER(SensOpts), C.POINTER(AdjointOut)]),
     ("mcx_load_batched", C.c_int, [_P, _P, C.c_int32]),
     ("mcx_batch_info", C.c_int, [_P, C.POINTER(C.c_int32), _P]),
     ("mcx_transport_batched", C.c_int, [_P, C.POINTER(TransportOpts), C.POINTER(BatchPackets),

@@ -92,6 +92,7 @@ std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out)
   d.secIonP = s.secIonP; d.cRecoilHP = s.cRecoilHP; d.cRecoilHeP = s.cRecoilHeP;
   d.xhiLimit = s.p.XHILimit;
   d.converge = 0;
+  d.fixTe = 0;
   d.maxIterT = kRefRounds;
   d.resTol = (double)0.02f;
   d.stepMin = 0.2;
@@ -250,7 +251,7 @@ std::string balanceDataCreate(const Setup& s, std::unique_ptr<BalanceData>& out)
   d.heatHi = carve<double>(blocks, nSh * C1, err);
   d.comp = carve<double>(blocks, 4 * (size_t)C1, err);
   double** scal[] = {&d.te, &d.ne, &d.xOld, &d.tHigh, &d.tLow, &d.resHigh, &d.resLow, &d.heat, &d.coolA,
-                     &d.coolHex, &d.coolCollH, &d.compHeat, &d.compRecoil, &d.compCool};
+                     &d.coolHex, &d.coolCollH, &d.compHeat, &d.compRecoil, &d.compCool, &d.resid};
   for (double** p : scal) *p = carve<double>(blocks, C1, err);
   d.forSum = carve<double>(blocks, (size_t)std::max(t.nAtoms, 1) * C1, err);
   d.coolAt = carve<CoolAt>(blocks, C1, err);
@@ -343,14 +344,18 @@ bool sameGrid(const BalanceGrid& a, const BalanceGrid& b) {
 }  // namespace
 
 cudaError_t launchBalance(BalanceData& bd, const BalanceGrid& g, int maxRounds, int precision, cudaStream_t s,
-                          int atomSolves, int converge) {
+                          int atomSolves, int converge, int fixTe) {
+  // Te held only with the tight stopping rules (the ladder converged at the held Te)
+  bd.dev.fixTe = fixTe && converge ? 1 : 0;
   {
     // the stopping rules: the reference's, or tight ones at the level the precision resolves
     BalanceDev& d = bd.dev;
     const int want = converge ? 1 : 0;
     const bool mixed = precision == kBalMixed;
     const double resTol = want ? (mixed ? 1e-6 : 1e-9) : (double)0.02f;
-    const float xTol = want ? (mixed ? 1e-5f : 1e-9f) : 0.01f;
+    // with Te held the ladder is converged to the end of FP64 (the adjoint differences its results
+    // over steps of 1e-3, and its slow modes leave 1e-9-converged ladders off by up to 1e-5)
+    const float xTol = want ? (mixed ? 1e-5f : (bd.dev.fixTe ? 1e-14f : 1e-9f)) : 0.01f;
     if (d.converge != want || d.resTol != resTol || d.xTol != xTol) {
       d.converge = want;
       d.maxIterT = want ? kMaxRounds : kRefRounds;
@@ -368,7 +373,7 @@ cudaError_t launchBalance(BalanceData& bd, const BalanceGrid& g, int maxRounds, 
     return precision == kBalMixed ? bal_mixed::launch(bd, g, maxRounds, s, atomSolves)
                                   : bal_f64::launch(bd, g, maxRounds, s, 1);
   };
-  if (maxRounds != kRefRounds || atomSolves || converge) return direct();
+  if (maxRounds != kRefRounds || atomSolves || converge || bd.dev.fixTe) return direct();
   const int k = precision == kBalMixed ? 1 : 0;
   if (bd.graph[k] && !sameGrid(bd.graphGrid[k], g)) {
     cudaGraphExecDestroy(bd.graph[k]);

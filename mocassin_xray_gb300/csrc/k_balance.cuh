@@ -96,6 +96,8 @@ struct BalanceDev {
   // bracket is 1e-12 wide, and unbracketed steps that start small (a converged
   // state stays on its branch of heating = cooling) and double up to x1.2
   int32_t converge, maxIterT;
+  int32_t fixTe;               // 1: Te held (with converge = 1): the ladder converged at each cell's Te and
+                               // heating - cooling left in resid; the evaluations of the balance's adjoint
   double resTol;
   double stepMin;              // tight mode: unbracketed steps 1 + stepMin 2^n at T-iteration n, at most 1.2
   float xTol;
@@ -152,6 +154,7 @@ struct BalanceDev {
   int8_t* ibConv;
   int8_t* side;                // tight mode: bracket end replaced last (1 low, 2 high); 3 = the
                                // bracket closed on a discontinuity of heating - cooling
+  double* resid;               // fixTe: heating - cooling at the held Te
   BalanceCounters* counters;
 };
 
@@ -186,8 +189,10 @@ constexpr int kBalMixed = 1;   // FP32 rates / splines / exponentials, FP64 solv
 // BalanceDev::counters.
 // atomSolves = 1: the mixed balance solves every ion's levels per cell and
 // T-iteration instead of reading the cooling surfaces.
+// fixTe = 1 (with converge = 1): every cell's Te is held; its ladder is
+// converged at that Te and heating - cooling is left in BalanceDev::resid.
 cudaError_t launchBalance(BalanceData& b, const BalanceGrid& g, int maxRounds, int precision, cudaStream_t s,
-                          int atomSolves = 0, int converge = 0);
+                          int atomSolves = 0, int converge = 0, int fixTe = 0);
 
 // The forLines line total of every cell with compute[c] = 1 (the emission
 // phase's normFor, rec = .true., units of 1e-25 erg/s per gas density) from

@@ -1594,6 +1594,17 @@ __device__ __forceinline__ void secantCell(const BalanceDev& b, int round, int l
   // tight mode: a residual whose ionisation ladder has not converged is evaluated again at the same Te
   // (the X-iterations go on from where they stopped) rather than taken as a bracket end
   const bool xPending = tight && !b.ibConv[cell];
+  if (b.fixTe) {
+    // Te held: the ladder goes on converging at this Te; the residual there is the result
+    b.resid[cell] = res;
+    if (xPending && nIterateT < b.maxIterT && round + 1 < kMaxRounds) {
+      b.list[(size_t)((round + 1) & 1) * C1 + atomicAdd(&b.listCount[round + 1], 1u)] = cell;
+    } else {
+      b.state[cell] = 1;
+      if (!b.ibConv[cell]) atomicAdd(&b.counters->noIonBal, 1ull);
+    }
+    return;
+  }
   bool open = xPending || fabs(res) >= b.resTol * (fabs(cool) + fabs(heat)) / 2.;
   if (open && !xPending && tight && Thigh != 0. && Tlow != 0. && fabs(Thigh - Tlow) <= 1e-12 * (Thigh + Tlow)) {
     open = false;

@@ -186,7 +186,37 @@ __global__ void lineSumReduceKernel(const double* __restrict__ partial, int nGro
   out[k] = s;
 }
 
+__global__ void __launch_bounds__(128) adjointCombineKernel(AdjointArgs a) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (cell > a.nCells) return;
+  const size_t C1 = (size_t)a.nCells + 1;
+  const uint8_t hold = a.hold[cell];
+  const double dT = (double)a.teP[cell] - (double)a.teM[cell];
+  const double dp = a.pP ? (double)a.pP[cell] - (double)a.pM[cell] : a.dpScalar;
+  double dTdp = 0.;
+  if (hold != 2 && dT != 0. && dp != 0.) {
+    const double dRdT = (a.rTp[cell] - a.rTm[cell]) / dT;
+    const double dRdp = (a.rPp[cell] - a.rPm[cell]) / dp;
+    const bool root = hold == 0 && isfinite(dRdT) && dRdT != 0. && isfinite(dRdp);
+    if (root) dTdp = -dRdp / dRdT;
+    else if (a.held) atomicAdd(a.held, 1ull);
+  }
+  if (a.dTdp) a.dTdp[cell] = dTdp;
+  for (int k = 0; k < a.nL; ++k) {
+    const size_t i = (size_t)k * C1 + cell;
+    double v = 0.;
+    if (hold != 2 && dT != 0. && dp != 0.) v = (a.lPp[i] - a.lPm[i]) / dp + (a.lTp[i] - a.lTm[i]) / dT * dTdp;
+    a.dLdp[i] = v;
+  }
+}
+
 }  // namespace
+
+cudaError_t launchAdjointCombine(const AdjointArgs& a, cudaStream_t s) {
+  if (a.nCells <= 0) return cudaSuccess;
+  adjointCombineKernel<<<(a.nCells + 127) / 128, 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
 
 cudaError_t launchGasLineSums(const EmissionDev& e, const LineSumArgs& a, cudaStream_t s) {
   if (a.nGroups <= 0) return cudaSuccess;

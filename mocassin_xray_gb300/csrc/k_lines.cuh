@@ -60,6 +60,30 @@ struct LineCellArgs {
   int32_t nReq;
 };
 
+// The implicit-function adjoint of the converged balance at fixed J, one cell
+// per thread (FP64).  From evaluations with every Te held, R = heating -
+// cooling and L = the requested lines' luminosities, each at Te(1 +- h) and at
+// a parameter stepped by +-h (each cell's Hden, or one abundance for all):
+//   dR/dTe, dL/dTe, dR/dp, dL/dp   central differences (steps as stored),
+//   dTe/dp = -(dR/dp) / (dR/dTe)   the root's response (0 where Te is held),
+//   out[k][cell] = dL_k/dp + dL_k/dTe dTe/dp.
+struct AdjointArgs {
+  const double* rTp, *rTm;    // [C+1] R at Te(1+h), Te(1-h)
+  const double* lTp, *lTm;    // [nL][C+1] L there
+  const float* teP, *teM;     // [C+1] the held Te values
+  const double* rPp, *rPm;    // [C+1] R at p(1+h), p(1-h)
+  const double* lPp, *lPm;    // [nL][C+1]
+  const float* pP, *pM;       // [C+1] the stepped per-cell parameter, or null: dpScalar
+  double dpScalar;            // p(1+h) - p(1-h) of a parameter shared by all cells
+  const uint8_t* hold;        // [C+1] 0 root, 1 Te held (no root), 2 no photon hit
+  double* dLdp;               // [nL][C+1] out
+  double* dTdp;               // [C+1] out, or null
+  unsigned long long* held;   // out: cells whose Te was held (hold = 1 or dR/dTe unusable), or null
+  int32_t nCells, nL;
+};
+
+cudaError_t launchAdjointCombine(const AdjointArgs& a, cudaStream_t s);
+
 // Shuffle-tree sum over the 32 lanes; lane 0 holds the result.
 __device__ __forceinline__ double warpSumD(double v) {
 #pragma unroll

@@ -1078,6 +1078,9 @@ ArrView viewOf(mcx_ctx* c, int id) {
     case MCX_ARR_N_ITER_T: return {c->nIterT.p, c->nIterT.bytes()};
     case MCX_ARR_FOR_LINES: return {c->forLines.p, c->forLines.bytes()};
     case MCX_ARR_TDUST: return {c->tdust.p, c->tdust.bytes()};
+    case MCX_ARR_BAL_RESID:
+      if (!c->balance) return {nullptr, 0};
+      return {c->balance->dev.resid, ((size_t)c->nCells + 1) * sizeof(double)};
     default: return {nullptr, 0};
   }
 }
@@ -1536,6 +1539,8 @@ extern "C" int mcx_balance(mcx_ctx* c, const mcx_balance_opts* opts, mcx_balance
     return fail(c, MCX_ERR_INPUT, "mcx_balance: unknown precision");
   const int prec = (opts && opts->precision == MCX_BAL_MIXED) ? kBalMixed : kBalFp64;
   const int converge = opts && opts->converge ? 1 : 0;
+  const int fixTe = opts && opts->fix_te ? 1 : 0;
+  if (fixTe && !converge) return fail(c, MCX_ERR_INPUT, "mcx_balance: fix_te needs converge = 1");
   const int roundCap = converge ? kMaxRounds : kRefRounds;
   const int rounds = (opts && opts->max_rounds > 0) ? opts->max_rounds : roundCap;
   if (rounds > roundCap)
@@ -1548,7 +1553,7 @@ extern "C" int mcx_balance(mcx_ctx* c, const mcx_balance_opts* opts, mcx_balance
   CK(cudaMemcpyAsync(c->teOld.p, c->te.p, C1 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream), "TeOld");
   CK(cudaMemcpyAsync(c->neOld.p, c->ne.p, C1 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream), "NeOld");
   BalanceGrid g{c->jste.p, c->hden.p, c->te.p, c->ne.p, c->ionDen.p, c->lgConverged.p, c->lgBlack.p, c->nIterT.p};
-  CK(launchBalance(*c->balance, g, rounds, prec, c->stream, opts && opts->atom_solves ? 1 : 0, converge),
+  CK(launchBalance(*c->balance, g, rounds, prec, c->stream, opts && opts->atom_solves ? 1 : 0, converge, fixTe),
      "balance kernels");
   CK(cudaEventRecord(c->ev1, c->stream), "event");
   BalanceCounters h{};
@@ -1784,35 +1789,42 @@ int copyState(mcx_ctx* c, StateCopy& d, bool save) {
   return MCX_OK;
 }
 
-}  // namespace
-
-extern "C" int mcx_line_sensitivities(mcx_ctx* c, const mcx_sens_opts* o, mcx_sens_out* out) {
-  if (!c || !o || !out || !out->L || (o->n_lines > 0 && !o->lines) || (o->n_abun > 0 && !o->abun_z))
-    return fail(c, MCX_ERR_INPUT, "mcx_line_sensitivities: null argument");
-  if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_line_sensitivities: no model loaded");
-  if (!c->lgGas || !c->balance) return fail(c, MCX_ERR_STATE, "mcx_line_sensitivities: the grid holds no gas");
-  if (c->nNeb > 0) return fail(c, MCX_ERR_STATE, "mcx_line_sensitivities: not for a batch");
-  if (o->n_lines < 1 || o->n_abun < 0) return fail(c, MCX_ERR_INPUT, "mcx_line_sensitivities: no lines");
-  const double h = o->h != 0. ? o->h : 1.e-3;
-  const int nL = o->n_lines, C = c->nCells;
-  const size_t C1 = (size_t)C + 1;
-  // the requested lines as (atom slot, lower, upper)
-  std::vector<int32_t> req(3 * (size_t)nL);
+// The checks shared by the derivative calls and the requested lines as (atom slot, lower, upper).
+int lineRequests(mcx_ctx* c, const mcx_sens_opts* o, bool haveOut, const std::string& who, std::vector<int32_t>& req) {
+  if (!c || !o || !haveOut || (o->n_lines > 0 && !o->lines) || (o->n_abun > 0 && !o->abun_z))
+    return fail(c, MCX_ERR_INPUT, who + ": null argument");
+  if (!c->loaded) return fail(c, MCX_ERR_STATE, who + ": no model loaded");
+  if (!c->lgGas || !c->balance) return fail(c, MCX_ERR_STATE, who + ": the grid holds no gas");
+  if (c->nNeb > 0) return fail(c, MCX_ERR_STATE, who + ": not for a batch");
+  if (o->n_lines < 1 || o->n_abun < 0) return fail(c, MCX_ERR_INPUT, who + ": no lines");
+  const int nL = o->n_lines;
+  req.assign(3 * (size_t)nL, 0);
   for (int k = 0; k < nL; ++k) {
     const mcx_line_ref& l = o->lines[k];
     int slot = -1;
     for (size_t a = 0; a < c->lineAtoms.size(); ++a)
       if (c->lineAtoms[a].elem == l.elem && c->lineAtoms[a].ion == l.ion) slot = (int)a;
-    if (slot < 0) return fail(c, MCX_ERR_INPUT, "mcx_line_sensitivities: no multi-level data for line " + std::to_string(k));
+    if (slot < 0) return fail(c, MCX_ERR_INPUT, who + ": no multi-level data for line " + std::to_string(k));
     const int n = c->lineAtoms[slot].nLev;
     if (l.lower < 1 || l.upper <= l.lower || l.upper > n ||
         c->lineAtoms[slot].fac[(size_t)(l.lower - 1) * n + (l.upper - 1)] == 0.)
-      return fail(c, MCX_ERR_INPUT, "mcx_line_sensitivities: line " + std::to_string(k) + " has no transition");
+      return fail(c, MCX_ERR_INPUT, who + ": line " + std::to_string(k) + " has no transition");
     req[3 * k] = slot; req[3 * k + 1] = l.lower; req[3 * k + 2] = l.upper;
   }
   for (int q = 0; q < o->n_abun; ++q)
     if (o->abun_z[q] < 1 || o->abun_z[q] > 30 || c->xrefAll[o->abun_z[q] - 1] <= 0)
-      return fail(c, MCX_ERR_INPUT, "mcx_line_sensitivities: element " + std::to_string(o->abun_z[q]) + " is not on");
+      return fail(c, MCX_ERR_INPUT, who + ": element " + std::to_string(o->abun_z[q]) + " is not on");
+  return MCX_OK;
+}
+
+}  // namespace
+
+extern "C" int mcx_line_sensitivities(mcx_ctx* c, const mcx_sens_opts* o, mcx_sens_out* out) {
+  std::vector<int32_t> req;
+  if (int rc = lineRequests(c, o, out && out->L, "mcx_line_sensitivities", req)) return rc;
+  const double h = o->h != 0. ? o->h : 1.e-3;
+  const int nL = o->n_lines, C = c->nCells;
+  const size_t C1 = (size_t)C + 1;
   CK(cudaSetDevice(c->device), "cudaSetDevice");
   DBuf<int32_t> dReq;
   DBuf<double> cellL;
@@ -1919,6 +1931,164 @@ extern "C" int mcx_line_sensitivities(mcx_ctx* c, const mcx_sens_opts* o, mcx_se
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
   if (rc == MCX_OK) CK(cudaStreamSynchronize(c->stream), "mcx_line_sensitivities");
+  return rc;
+}
+
+extern "C" int mcx_adjoint(mcx_ctx* c, const mcx_sens_opts* o, mcx_adjoint_out* out) {
+  std::vector<int32_t> req;
+  if (int rc = lineRequests(c, o, out && out->L, "mcx_adjoint", req)) return rc;
+  if (o->reference_stopping)
+    return fail(c, MCX_ERR_INPUT, "mcx_adjoint: needs the tightly converged balance (reference_stopping = 0)");
+  const double h = o->h != 0. ? std::fabs(o->h) : 1.e-3;
+  const int nL = o->n_lines, C = c->nCells;
+  const size_t C1 = (size_t)C + 1, LC = (size_t)nL * C1;
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  cudaStream_t st = c->stream;
+  DBuf<int32_t> dReq;
+  CK(upload(dReq, req), "upload line requests");
+  // the evaluations: [0] the converged balance, [1, 2] Te(1 +- h), [3, 4] the stepped parameter
+  DBuf<double> lum[5], res[5];
+  for (int e = 0; e < 5; ++e) {
+    CK(lum[e].alloc(LC), "alloc line cells");
+    CK(res[e].alloc(C1), "alloc residuals");
+  }
+  DBuf<float> tP, tM, pP, pM;
+  DBuf<double> dLdp, dTdp;
+  DBuf<uint8_t> hold;
+  DBuf<unsigned long long> held;
+  CK(tP.alloc(C1), "alloc"); CK(tM.alloc(C1), "alloc"); CK(pP.alloc(C1), "alloc"); CK(pM.alloc(C1), "alloc");
+  CK(dLdp.alloc(LC), "alloc"); CK(dTdp.alloc(C1), "alloc"); CK(hold.alloc(C1), "alloc"); CK(held.alloc(1), "alloc");
+  CK(cudaMemsetAsync(held.p, 0, sizeof(unsigned long long), st), "memset");
+  LineCellArgs la{};
+  la.te = c->te.p; la.ne = c->ne.p; la.ionDen = c->ionDen.p; la.hden = c->hden.p; la.vol = c->volD.p;
+  la.black = c->lgBlack.p; la.req = dReq.p; la.nReq = nL;
+  mcx_balance_opts bo{};
+  bo.precision = o->precision;
+  bo.converge = 1;
+  auto lines = [&](int e) -> int {
+    la.out = lum[e].p;
+    CK(launchLineCellLuminosities(*c->balance, la, st), "line cells");
+    return MCX_OK;
+  };
+  StateCopy s1;
+  // R and L with every Te held, from the converged state; te (host) replaces its Te where given
+  auto held_eval = [&](int e, const std::vector<float>* te) -> int {
+    if (int rc = copyState(c, s1, false)) return rc;
+    if (te) CK(cudaMemcpyAsync(c->te.p, te->data(), C1 * sizeof(float), cudaMemcpyHostToDevice, st), "h2d Te");
+    bo.fix_te = 1;
+    int rc = mcx_balance(c, &bo, nullptr);
+    bo.fix_te = 0;
+    if (rc != MCX_OK) return rc;
+    if ((rc = lines(e))) return rc;
+    CK(cudaMemcpyAsync(res[e].p, c->balance->dev.resid, C1 * sizeof(double), cudaMemcpyDeviceToDevice, st), "d2d R");
+    CK(cudaStreamSynchronize(st), "mcx_adjoint");
+    return MCX_OK;
+  };
+  AdjointArgs aa{};
+  aa.rTp = res[1].p; aa.rTm = res[2].p; aa.lTp = lum[1].p; aa.lTm = lum[2].p; aa.teP = tP.p; aa.teM = tM.p;
+  aa.rPp = res[3].p; aa.rPm = res[4].p; aa.lPp = lum[3].p; aa.lPm = lum[4].p;
+  aa.hold = hold.p; aa.dLdp = dLdp.p; aa.nCells = C; aa.nL = nL;
+
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  CK(cudaEventCreate(&t0), "event");
+  CK(cudaEventCreate(&t1), "event");
+  CK(cudaEventRecord(t0, st), "event");
+  out->pinned_cells = 0;
+  // the converged balance (from the current state) and its line sums
+  int rc = mcx_balance(c, &bo, nullptr);
+  if (rc == MCX_OK) rc = lines(0);
+  if (rc == MCX_OK) rc = copyState(c, s1, true);
+  std::vector<float> te(C1), hd(C1), stepP(C1), stepM(C1);
+  std::vector<int32_t> nit(C1), black(C1);
+  std::vector<int8_t> side(C1);
+  std::vector<double> hostL(LC);
+  if (rc == MCX_OK) {
+    CK(cudaMemcpyAsync(hostL.data(), lum[0].p, LC * sizeof(double), cudaMemcpyDeviceToHost, st), "d2h L");
+    CK(cudaMemcpyAsync(te.data(), c->te.p, C1 * sizeof(float), cudaMemcpyDeviceToHost, st), "d2h Te");
+    CK(cudaMemcpyAsync(hd.data(), c->hden.p, C1 * sizeof(float), cudaMemcpyDeviceToHost, st), "d2h Hden");
+    CK(cudaMemcpyAsync(nit.data(), c->nIterT.p, C1 * sizeof(int32_t), cudaMemcpyDeviceToHost, st), "d2h");
+    CK(cudaMemcpyAsync(black.data(), c->lgBlack.p, C1 * sizeof(int32_t), cudaMemcpyDeviceToHost, st), "d2h");
+    CK(cudaMemcpyAsync(side.data(), c->balance->dev.side, C1, cudaMemcpyDeviceToHost, st), "d2h");
+    CK(cudaStreamSynchronize(st), "mcx_adjoint");
+    for (int k = 0; k < nL; ++k) {
+      double t = 0.;
+      for (size_t cell = 1; cell < C1; ++cell) t += hostL[(size_t)k * C1 + cell];
+      out->L[k] = t;
+    }
+    // a cell without a root: its bracket closed on a jump, or it did not converge
+    std::vector<uint8_t> hh(C1, 2);
+    for (size_t cell = 1; cell < C1; ++cell)
+      hh[cell] = black[cell] >= 1 ? 2 : (side[cell] == 3 || nit[cell] >= kMaxRounds) ? 1 : 0;
+    CK(cudaMemcpyAsync(hold.p, hh.data(), C1, cudaMemcpyHostToDevice, st), "h2d hold");
+    // Te(1 +- h)
+    for (size_t cell = 0; cell < C1; ++cell) {
+      stepP[cell] = (float)((double)te[cell] * (1. + h));
+      stepM[cell] = (float)((double)te[cell] * (1. - h));
+    }
+    CK(cudaMemcpyAsync(tP.p, stepP.data(), C1 * sizeof(float), cudaMemcpyHostToDevice, st), "h2d");
+    CK(cudaMemcpyAsync(tM.p, stepM.data(), C1 * sizeof(float), cudaMemcpyHostToDevice, st), "h2d");
+    rc = held_eval(1, &stepP);
+    if (rc == MCX_OK) rc = held_eval(2, &stepM);
+  }
+  // every cell's Hden (1 +- h) at once: at fixed J each cell answers for itself
+  if (rc == MCX_OK && (out->dL_dhden || out->dte_dhden)) {
+    for (size_t cell = 0; cell < C1; ++cell) {
+      stepP[cell] = (float)((double)hd[cell] * (1. + h));
+      stepM[cell] = (float)((double)hd[cell] * (1. - h));
+    }
+    CK(cudaMemcpyAsync(pP.p, stepP.data(), C1 * sizeof(float), cudaMemcpyHostToDevice, st), "h2d");
+    CK(cudaMemcpyAsync(pM.p, stepM.data(), C1 * sizeof(float), cudaMemcpyHostToDevice, st), "h2d");
+    CK(cudaMemcpyAsync(c->hden.p, stepP.data(), C1 * sizeof(float), cudaMemcpyHostToDevice, st), "h2d Hden");
+    rc = held_eval(3, nullptr);
+    if (rc == MCX_OK) {
+      CK(cudaMemcpyAsync(c->hden.p, stepM.data(), C1 * sizeof(float), cudaMemcpyHostToDevice, st), "h2d Hden");
+      rc = held_eval(4, nullptr);
+    }
+    CK(cudaMemcpyAsync(c->hden.p, hd.data(), C1 * sizeof(float), cudaMemcpyHostToDevice, st), "h2d Hden");
+    if (rc == MCX_OK) {
+      aa.pP = pP.p; aa.pM = pM.p; aa.dTdp = dTdp.p; aa.held = held.p;
+      CK(launchAdjointCombine(aa, st), "adjoint kernel");
+      if (out->dL_dhden)
+        CK(cudaMemcpyAsync(out->dL_dhden, dLdp.p, LC * sizeof(double), cudaMemcpyDeviceToHost, st), "d2h");
+      if (out->dte_dhden)
+        CK(cudaMemcpyAsync(out->dte_dhden, dTdp.p, C1 * sizeof(double), cudaMemcpyDeviceToHost, st), "d2h");
+      unsigned long long nh = 0;
+      CK(cudaMemcpyAsync(&nh, held.p, sizeof(nh), cudaMemcpyDeviceToHost, st), "d2h");
+      CK(cudaStreamSynchronize(st), "mcx_adjoint");
+      out->pinned_cells = (int64_t)nh;
+    }
+  }
+  // each abundance (1 +- h), one parameter shared by every cell
+  for (int q = 0; rc == MCX_OK && out->dL_dabun && q < o->n_abun; ++q) {
+    const int z = o->abun_z[q];
+    float& ab = c->balance->dev.abun[z];
+    const float a0 = ab, ap = (float)((double)a0 * (1. + h)), am = (float)((double)a0 * (1. - h));
+    ab = ap;
+    invalidateBalanceGraphs(*c->balance);
+    rc = held_eval(3, nullptr);
+    ab = am;
+    invalidateBalanceGraphs(*c->balance);
+    if (rc == MCX_OK) rc = held_eval(4, nullptr);
+    ab = a0;
+    invalidateBalanceGraphs(*c->balance);
+    if (rc != MCX_OK) break;
+    aa.pP = nullptr; aa.pM = nullptr; aa.dpScalar = (double)ap - (double)am; aa.dTdp = nullptr; aa.held = nullptr;
+    CK(launchAdjointCombine(aa, st), "adjoint kernel");
+    CK(cudaMemcpyAsync(hostL.data(), dLdp.p, LC * sizeof(double), cudaMemcpyDeviceToHost, st), "d2h");
+    CK(cudaStreamSynchronize(st), "mcx_adjoint");
+    for (int k = 0; k < nL; ++k) {
+      double t = 0.;
+      for (size_t cell = 1; cell < C1; ++cell) t += hostL[(size_t)k * C1 + cell];
+      out->dL_dabun[(size_t)k * o->n_abun + q] = t;
+    }
+  }
+  if (rc == MCX_OK) rc = copyState(c, s1, false);
+  cudaEventRecord(t1, st);
+  cudaEventSynchronize(t1);
+  cudaEventElapsedTime(&out->kernel_ms, t0, t1);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  if (rc == MCX_OK) CK(cudaStreamSynchronize(st), "mcx_adjoint");
   return rc;
 }
 

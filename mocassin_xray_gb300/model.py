@@ -180,6 +180,7 @@ class Context:
             abi.ARR_LG_BLACK: ((C1,), np.int32), abi.ARR_N_ITER_T: ((C1,), np.int32), abi.ARR_FOR_LINES: ((C1,), f32),
             abi.ARR_IONDEN: ((s.nstages, max(s.n_elem_used, 1), C1), f32),
             abi.ARR_TDUST: ((self._dust_planes(), C1), f32),
+            abi.ARR_BAL_RESID: ((C1,), np.float64),
         }
         return shapes[arr_id]
 
@@ -227,12 +228,14 @@ class Context:
         return st
 
     def balance(self, max_rounds: int = 0, precision: int = abi.BAL_FP64,
-                atom_solves: bool = False, converge: bool = False) -> abi.BalanceStats:
+                atom_solves: bool = False, converge: bool = False, fix_te: bool = False) -> abi.BalanceStats:
         """updateCell for every cell (Te, Ne, ionDen, lgConverged) from the normalised J.  atom_solves
         (mixed precision): solve every ion's levels per cell instead of reading the cooling surfaces;
-        converge: converge every cell tightly instead of iterateT's stopping rules."""
+        converge: converge every cell tightly instead of iterateT's stopping rules; fix_te (with
+        converge): hold every cell's Te, converge its ladder there and leave heating - cooling in
+        ARR_BAL_RESID."""
         o = abi.BalanceOpts(precision=precision, max_rounds=max_rounds, atom_solves=int(atom_solves),
-                            converge=int(converge))
+                            converge=int(converge), fix_te=int(fix_te))
         st = abi.BalanceStats()
         self._check(lib().mcx_balance(self._h, C.byref(o), C.byref(st)))
         return st
@@ -298,6 +301,29 @@ class Context:
         self._check(lib().mcx_line_sensitivities(self._h, C.byref(o), C.byref(out)))
         return dict(L=L, dL_dhden=dh, dL_dabun=da[:, :len(z)], kernel_ms=float(out.kernel_ms),
                     branch_cells_hden=int(out.branch_cells_hden), branch_cells_abun=int(out.branch_cells_abun))
+
+    def adjoint(self, lines, abun_z=(), h: float = 1e-3, precision: int = abi.BAL_MIXED,
+                per_cell: bool = True) -> dict:
+        """The implicit-function adjoint of the converged balance at the context's J (mcx_adjoint): the
+        outputGas volume sums L of the forbidden lines `lines` [(elem, ion, lower, upper), ...] after a
+        tightly converged balance, dL/dHden per cell ([n_lines, nCells+1]), dTe/dHden of each cell's root
+        ([nCells+1]) and dL/d(elemAbun) of the elements `abun_z` ([n_lines, len(abun_z)]), from central
+        differences (relative step h) of evaluations with every Te held."""
+        n = len(lines)
+        refs = (abi.LineRef * n)(*[abi.LineRef(*map(int, l)) for l in lines])
+        z = np.ascontiguousarray(np.asarray(abun_z, dtype=np.int32))
+        L = np.zeros(n)
+        dh = np.zeros((n, self._cells + 1)) if per_cell else None
+        dt = np.zeros(self._cells + 1) if per_cell else None
+        da = np.zeros((n, max(len(z), 1)))
+        o = abi.SensOpts(n_lines=n, n_abun=len(z), lines=C.cast(refs, C.c_void_p),
+                         abun_z=z.ctypes.data if len(z) else None, h=h, precision=precision)
+        out = abi.AdjointOut(L=L.ctypes.data, dL_dhden=dh.ctypes.data if per_cell else None,
+                             dL_dabun=da.ctypes.data if len(z) else None,
+                             dte_dhden=dt.ctypes.data if per_cell else None)
+        self._check(lib().mcx_adjoint(self._h, C.byref(o), C.byref(out)))
+        return dict(L=L, dL_dhden=dh, dte_dhden=dt, dL_dabun=da[:, :len(z)], kernel_ms=float(out.kernel_ms),
+                    pinned_cells=int(out.pinned_cells))
 
     def state_save(self, slot: int = 0) -> None:
         """Device-side snapshot, in slot `slot`, of everything an iteration

@@ -370,6 +370,8 @@ def _balance_lib():
         l.orc_for_lines_emission.argtypes = [C.POINTER(BalanceIn), _P, _P, _P, _P, _P]
         l.orc_balance_trace.argtypes = [C.POINTER(BalanceIn), C.POINTER(BalanceState), C.c_int32, _P]
         l.orc_balance_trace.restype = C.c_int
+        l.orc_balance_fixed_te.argtypes = [C.POINTER(BalanceIn), C.POINTER(BalanceState), C.c_int32, C.c_double, _P]
+        l.orc_balance_fixed_te.restype = C.c_int
         l.orc_for_lines_emission.restype = C.c_int
         l._balance_ready = True
     return l
@@ -441,6 +443,51 @@ def balance(tables: BalanceTables, jste, te, ne, ionden, nthreads: int = 1):
     if rc != 0:
         raise RuntimeError(f"orc_balance failed: {rc}")
     return te, ne, ionden, conv, black, nit, stats
+
+
+class _Swap:
+    """Points fields of a ctypes struct at other arrays for the length of a with-block."""
+
+    def __init__(self, struct, **arrays):
+        self.struct, self.arrays, self.saved = struct, arrays, {}
+
+    def __enter__(self):
+        for f, a in self.arrays.items():
+            if a is not None:
+                self.saved[f] = getattr(self.struct, f)
+                setattr(self.struct, f, _p(a))
+        return self
+
+    def __exit__(self, *exc):
+        for f, v in self.saved.items():
+            setattr(self.struct, f, v)
+
+
+def balance_fixed_te(tables: BalanceTables, jste, te, ne, ionden, x_tol=float(np.float32(1e-14)), hden=None,
+                     abun=None, nthreads: int = 1):
+    """The balance of every cell with its Te held (orc_balance_fixed_te): ionBalance converged to x_tol at
+    the given Te, then heating - cooling.  hden [C+1] and abun [30] replace the set-up's densities and
+    abundances.  Returns (ne, ionden, resid, converged, black, rounds)."""
+    i = tables.info
+    C1 = i.n_cells + 1
+    jste = np.ascontiguousarray(jste, dtype=np.float64)
+    te = np.array(te, dtype=np.float32, copy=True)
+    ne = np.array(ne, dtype=np.float32, copy=True)
+    ionden = np.array(ionden, dtype=np.float32, copy=True).reshape(-1)
+    conv = np.zeros(C1, dtype=np.int32)
+    black = np.zeros(C1, dtype=np.int32)
+    rounds = np.zeros(C1, dtype=np.int32)
+    resid = np.zeros(C1, dtype=np.float64)
+    hd = None if hden is None else np.ascontiguousarray(hden, dtype=np.float32)
+    ab = None if abun is None else np.ascontiguousarray(abun, dtype=np.float32)
+    st = BalanceState(te=_p(te), ne=_p(ne), ionden=_p(ionden), converged=_p(conv), black=_p(black),
+                      n_iter_t=_p(rounds))
+    with _Swap(tables.s, jste=jste, hden=hd, elem_abun=ab):
+        rc = _balance_lib().orc_balance_fixed_te(C.byref(tables.s), C.byref(st), nthreads, float(x_tol), _p(resid))
+    tables.s.jste = None
+    if rc != 0:
+        raise RuntimeError(f"orc_balance_fixed_te failed: {rc}")
+    return ne, ionden, resid, conv, black, rounds
 
 
 def for_lines_emission(tables: BalanceTables, te, ne, ionden, compute=None, nthreads: int = 1) -> np.ndarray:
@@ -623,6 +670,100 @@ def line_luminosities(setup, tables: BalanceTables, te, ne, ionden, black, vol=N
         hbv = 8.0 * hbv
     return dict(hbeta_vol=hbv, relative=bool(rel), n_cells=int(out.n_cells), hydro=hydro / d, hei=hei / d,
                 forb=forb_full, te_vol=te_vol, ion_vol=ion_vol)
+
+
+def line_cell_luminosities(setup, tables: BalanceTables, te, ne, ionden, cells, lines, hden=None, abun=None,
+                           vol=None) -> np.ndarray:
+    """[len(lines), len(cells)]: each listed cell's luminosity of the forbidden lines (elem, ion, lower,
+    upper), outputGas's forbVol term of that cell alone before the division by HbetaVol
+    (source/output_mod.f90:410-432), x8 in symmetricXYZ mode; hden and abun replace the set-up's."""
+    i = setup.info
+    C1 = i.n_cells + 1
+    em, keep = _emission_struct(setup, te, ne, ionden)
+    if vol is None:
+        vol = cell_volumes(setup)
+    vol = np.ascontiguousarray(vol, dtype=np.float64)
+    n_atoms = max(tables.s.n_atoms, 1)
+    hydro, hei = np.zeros((30, 14, 8)), np.zeros(34)
+    forb = np.zeros((n_atoms, 30, 30))
+    num, den = np.zeros((30, i.nstages)), np.zeros((30, i.nstages))
+    out = LinesOut(hydro=_p(hydro), hei=_p(hei), forb=_p(forb), ion_num=_p(num), ion_den=_p(den))
+    l = lib()
+    l.orc_line_sums.argtypes = [C.POINTER(EmissionIn), C.POINTER(BalanceIn), _P, _P, C.POINTER(LinesOut)]
+    l.orc_line_sums.restype = C.c_int
+    slots = [(tables.atom(z, ion), lo - 1, up - 1) for z, ion, lo, up in lines]
+    hd = None if hden is None else np.ascontiguousarray(hden, dtype=np.float32)
+    ab = None if abun is None else np.ascontiguousarray(abun, dtype=np.float32)
+    res = np.zeros((len(lines), len(cells)))
+    black = np.ones(C1, np.int32)
+    with _Swap(tables.s, hden=hd), _Swap(em, elem_abun=ab):
+        for n, cell in enumerate(cells):
+            black[:] = 1
+            black[int(cell)] = 0
+            rc = l.orc_line_sums(C.byref(em), C.byref(tables.s), _p(vol), _p(black), C.byref(out))
+            if rc != 0:
+                raise RuntimeError(f"orc_line_sums failed: {rc}")
+            for k, (a, lo, up) in enumerate(slots):
+                res[k, n] = forb[a, lo, up]
+    del keep
+    return res * (8.0 if i.symmetric_xyz else 1.0)
+
+
+def ift_line_gradient(setup, tables: BalanceTables, jste, te, ne, ionden, lines, cells, abun_z=(), h: float = 1e-3,
+                      x_tol=float(np.float32(1e-14)), nthreads: int = 4) -> dict:
+    """The implicit-function adjoint of the converged balance at fixed J, in FP64 on the CPU, for the
+    listed cells: with R(Te; p) = heating - cooling of the ladder converged at Te (balance_fixed_te) and
+    L(Te; p) the cell's line luminosities, the balance's root Te*(p) gives
+        dL/dp = dL/dp|Te - dL/dTe|p * (dR/dp|Te) / (dR/dTe|p),
+    each partial a central difference (relative step h, the stepped values rounded to FP32 as the grid
+    holds them) of evaluations at Te held, started from the given converged state, their ladders
+    converged to x_tol (the slow modes of the X-iteration leave a ladder stopped at 1e-9 off by up to
+    1e-5, enough to spoil differences over steps of 1e-3 where dL/dp is a small difference of larger
+    terms).  p is every cell's
+    Hden (each cell's own; they do not interact at fixed J) and the abundances of the elements abun_z.
+    Returns dL_dhden [lines, cells], dL_dabun [lines, len(abun_z), cells] (each cell's share of
+    dL/d(abundance)), dte_dhden [cells], dR_dte [cells] and dL_dhden_te_held [lines, cells] (the
+    partial derivative with Te held, the gradient of a cell whose Te has no root)."""
+    cells = np.asarray(cells, dtype=np.int64)
+    te = np.asarray(te, np.float32)
+    hden0 = tables.k["hden"].astype(np.float32)
+    abun0 = tables.k["abun"].astype(np.float32)
+
+    def evaluate(te_s, hden=None, abun=None):
+        ne_s, ion_s, r, _, _, _ = balance_fixed_te(tables, jste, te_s, ne, ionden, x_tol, hden, abun, nthreads)
+        lum = line_cell_luminosities(setup, tables, te_s, ne_s, ion_s, cells, lines, hden=hden, abun=abun)
+        return r[cells], lum
+
+    def central(make):
+        (rp, lp, xp), (rm, lm, xm) = make(1.0 + h), make(1.0 - h)
+        dx = xp - xm
+        return (rp - rm) / dx, (lp - lm) / dx
+
+    te_p = (te.astype(np.float64) * (1.0 + h)).astype(np.float32)
+    te_m = (te.astype(np.float64) * (1.0 - h)).astype(np.float32)
+    rt = {"p": evaluate(te_p), "m": evaluate(te_m)}
+    dT = te_p[cells].astype(np.float64) - te_m[cells].astype(np.float64)
+    dR_dT = (rt["p"][0] - rt["m"][0]) / dT
+    dL_dT = (rt["p"][1] - rt["m"][1]) / dT
+
+    def hden_step(f):
+        hd = (hden0.astype(np.float64) * f).astype(np.float32)
+        r, lum = evaluate(te, hden=hd)
+        return r, lum, hd[cells].astype(np.float64)
+
+    dR_dH, dL_dH = central(hden_step)
+    dte_dh = -dR_dH / dR_dT
+    out = dict(dL_dhden=dL_dH + dL_dT * dte_dh, dte_dhden=dte_dh, dR_dte=dR_dT, dL_dhden_te_held=dL_dH,
+               dL_dabun=np.zeros((len(lines), len(abun_z), cells.size)))
+    for q, z in enumerate(abun_z):
+        def abun_step(f, z=z):
+            ab = abun0.copy()
+            ab[z - 1] = np.float32(float(abun0[z - 1]) * f)
+            r, lum = evaluate(te, abun=ab)
+            return r, lum, np.full(cells.size, float(ab[z - 1]))
+        dR_dA, dL_dA = central(abun_step)
+        out["dL_dabun"][:, q, :] = dL_dA - dL_dT * dR_dA / dR_dT
+    return out
 
 
 def iterate_chain(setup, n_photons: int, iterations: int, seed: int, nthreads: int = 8, tables=None):

@@ -402,8 +402,10 @@ static void compton(const orc_balance_in* in, const double* J, cell_t* c) {
     c->comptonRecoilHeat = (rhH * c->ion[1][1] * abun(in, 1) + he) * kRyd2erg;
 }
 
-/* ionBalance, source/update_mod.f90:1575-1992 (recursion as a loop); returns lgConv */
-static int ion_balance(const orc_balance_in* in, cell_t* c) {
+/* ionBalance, source/update_mod.f90:1575-1992 (recursion as a loop); returns
+ * lgConv.  x_tol is the limit on the relative X(H0), X(He0), X(He+) changes
+ * that ends the X-iterations (the reference's 0.01). */
+static int ion_balance(const orc_balance_in* in, cell_t* c, double x_tol) {
     const int ns = in->nstages;
     double chexRaw[NEL + 1][MAXST][4];
     chex_table(chexRaw);
@@ -507,7 +509,7 @@ static int ion_balance(const orc_balance_in* in, cell_t* c) {
         double dHI = (c->ion[1][1] - HIOld) / HIOld;
         double dHeI = on(in, 2) ? (c->ion[2][1] - HeIOld) / HeIOld : 0.;
         double dHeII = on(in, 2) ? (c->ion[2][2] - HeIIOld) / HeIIOld : 0.;
-        int big = fabs(dHI) > R(0.01) || fabs(dHeI) > R(0.01) || fabs(dHeII) > R(0.01);
+        int big = fabs(dHI) > x_tol || fabs(dHeI) > x_tol || fabs(dHeII) > x_tol;
         if (big && c->nIterateX < 15) {
             c->nIterateX = c->nIterateX + 1;
             continue;
@@ -787,22 +789,15 @@ static void update_cell(const orc_balance_in* in, orc_balance_state* st, int cel
 }
 
 /* the same with a record of each T-iteration: Te, heating, cooling, Ne, X(H0) */
-static void update_cell_tr(const orc_balance_in* in, orc_balance_state* st, int cell, cell_t* c, double* J,
-                           orc_balance_stats* s, double* trace) {
+/* a cell's J and grid state into c; returns 0 for a cell no photon reached */
+static int load_cell(const orc_balance_in* in, const orc_balance_state* st, int cell, cell_t* c, double* J) {
     const int C1 = in->n_cells + 1, nb = in->nbins, ns = in->nstages, E = in->n_elem_used;
     int hit = 0;
     for (int b = 0; b < nb; ++b) {
         J[b] = in->jste[(size_t)b * C1 + cell];
         if (J[b] > 0.) hit = 1;
     }
-    st->black[cell] = 0;
-    st->converged[cell] = 0;
-    st->n_iter_t[cell] = 0;
-    if (!hit) {
-        st->black[cell] = 1;
-        s->no_hit += 1.;
-        return;
-    }
+    if (!hit) return 0;
     memset(c->ion, 0, sizeof(c->ion));
     for (int elem = 1; elem <= NEL; ++elem) {
         if (!on(in, elem)) continue;
@@ -812,6 +807,30 @@ static void update_cell_tr(const orc_balance_in* in, orc_balance_state* st, int 
     c->te = st->te[cell];
     c->ne = st->ne[cell];
     c->hden = in->hden[cell];
+    return 1;
+}
+
+/* Ne and the ion fractions of c into the grid state (FP32, as the grid holds them) */
+static void store_cell(const orc_balance_in* in, orc_balance_state* st, int cell, const cell_t* c) {
+    const int C1 = in->n_cells + 1, ns = in->nstages, E = in->n_elem_used;
+    st->ne[cell] = (float)c->ne;
+    for (int elem = 1; elem <= NEL; ++elem) {
+        if (!on(in, elem)) continue;
+        for (int ion = 1; ion <= ns; ++ion)
+            st->ionden[((size_t)(ion - 1) * E + (xref(in, elem) - 1)) * C1 + cell] = (float)c->ion[elem][ion];
+    }
+}
+
+static void update_cell_tr(const orc_balance_in* in, orc_balance_state* st, int cell, cell_t* c, double* J,
+                           orc_balance_stats* s, double* trace) {
+    st->black[cell] = 0;
+    st->converged[cell] = 0;
+    st->n_iter_t[cell] = 0;
+    if (!load_cell(in, st, cell, c, J)) {
+        st->black[cell] = 1;
+        s->no_hit += 1.;
+        return;
+    }
     const double XOldHI = c->ion[1][1];
     const double thLimit = R(0.02);
     int nIterateT = 0, lgIBConv = 1;
@@ -823,7 +842,7 @@ static void update_cell_tr(const orc_balance_in* in, orc_balance_state* st, int 
         collisional_ionisation(in, c);
         c->nIterateX = 1;
         if (in->lg_compton) compton(in, J, c);
-        lgIBConv = ion_balance(in, c);
+        lgIBConv = ion_balance(in, c, R(0.01));
         double heat, cool;
         therm_balance(in, c, &heat, &cool);
         if (trace && nIterateT <= 20) {
@@ -865,12 +884,39 @@ static void update_cell_tr(const orc_balance_in* in, orc_balance_state* st, int 
     if (st->converged[cell]) s->converged += 1;
     st->n_iter_t[cell] = nIterateT;
     st->te[cell] = (float)c->te;
-    st->ne[cell] = (float)c->ne;
-    for (int elem = 1; elem <= NEL; ++elem) {
-        if (!on(in, elem)) continue;
-        for (int ion = 1; ion <= ns; ++ion)
-            st->ionden[((size_t)(ion - 1) * E + (xref(in, elem) - 1)) * C1 + cell] = (float)c->ion[elem][ion];
+    store_cell(in, st, cell, c);
+}
+
+/* The balance of one cell with its Te held: calcAlpha, photoionisation,
+ * collisional ionisation, Compton and ionBalance at that Te, repeated from
+ * where ionBalance stopped until its X changes fall within x_tol (at most 64
+ * times, as the tight device balance does), then thermBalance; returns
+ * heating - cooling (0 for a cell no photon reached, which is marked black). */
+static double fixed_te_cell(const orc_balance_in* in, orc_balance_state* st, int cell, cell_t* c, double* J,
+                            double x_tol) {
+    st->black[cell] = 0;
+    st->n_iter_t[cell] = 0;
+    st->converged[cell] = 0;
+    if (!load_cell(in, st, cell, c, J)) {
+        st->black[cell] = 1;
+        return 0.;
     }
+    int round = 0, lgIBConv = 0;
+    while (!lgIBConv && round < 64) {
+        round = round + 1;
+        calc_alpha(in, c);
+        photoionisation(in, J, c);
+        collisional_ionisation(in, c);
+        c->nIterateX = 1;
+        if (in->lg_compton) compton(in, J, c);
+        lgIBConv = ion_balance(in, c, x_tol);
+    }
+    double heat, cool;
+    therm_balance(in, c, &heat, &cool);
+    st->n_iter_t[cell] = round;
+    st->converged[cell] = lgIBConv;
+    store_cell(in, st, cell, c);
+    return heat - cool;
 }
 
 typedef struct {
@@ -878,6 +924,8 @@ typedef struct {
     orc_balance_state* st;
     int c0, c1;
     orc_balance_stats stats;
+    double x_tol;
+    double* resid;              /* non-NULL: the balance with Te held */
 } job_t;
 
 static void* worker(void* arg) {
@@ -885,13 +933,17 @@ static void* worker(void* arg) {
     cell_t* c = (cell_t*)malloc(sizeof(cell_t));
     double* J = (double*)malloc(sizeof(double) * (size_t)j->in->nbins);
     memset(&j->stats, 0, sizeof(j->stats));
-    for (int cell = j->c0; cell < j->c1; ++cell) update_cell(j->in, j->st, cell, c, J, &j->stats);
+    for (int cell = j->c0; cell < j->c1; ++cell) {
+        if (j->resid) j->resid[cell] = fixed_te_cell(j->in, j->st, cell, c, J, j->x_tol);
+        else update_cell(j->in, j->st, cell, c, J, &j->stats);
+    }
     free(J);
     free(c);
     return NULL;
 }
 
-int orc_balance(const orc_balance_in* in, orc_balance_state* st, int32_t nthreads, orc_balance_stats* stats) {
+static void run_jobs(const orc_balance_in* in, orc_balance_state* st, int32_t nthreads, double x_tol,
+                     double* resid, orc_balance_stats* stats) {
     if (nthreads < 1) nthreads = 1;
     if (nthreads > 256) nthreads = 256;
     job_t jobs[256];
@@ -902,16 +954,31 @@ int orc_balance(const orc_balance_in* in, orc_balance_state* st, int32_t nthread
         jobs[t].st = st;
         jobs[t].c0 = 1 + (int)((int64_t)C * t / nthreads);
         jobs[t].c1 = 1 + (int)((int64_t)C * (t + 1) / nthreads);
+        jobs[t].x_tol = x_tol;
+        jobs[t].resid = resid;
         pthread_create(&th[t], NULL, worker, &jobs[t]);
     }
-    memset(stats, 0, sizeof(*stats));
+    if (stats) memset(stats, 0, sizeof(*stats));
     for (int t = 0; t < nthreads; ++t) {
         pthread_join(th[t], NULL);
+        if (!stats) continue;
         stats->no_hit += jobs[t].stats.no_hit;
         stats->no_ion_bal += jobs[t].stats.no_ion_bal;
         stats->no_te_bal += jobs[t].stats.no_te_bal;
         stats->converged += jobs[t].stats.converged;
     }
+}
+
+int orc_balance(const orc_balance_in* in, orc_balance_state* st, int32_t nthreads, orc_balance_stats* stats) {
+    run_jobs(in, st, nthreads, 0., NULL, stats);
+    return 0;
+}
+
+int orc_balance_fixed_te(const orc_balance_in* in, orc_balance_state* st, int32_t nthreads, double x_tol,
+                         double* resid) {
+    if (!resid) return 1;
+    resid[0] = 0.;
+    run_jobs(in, st, nthreads, x_tol, resid, NULL);
     return 0;
 }
 

@@ -232,6 +232,17 @@ typedef struct orc_balance_stats {
  * Gas only (no grains).  Returns 0. */
 int orc_balance(const orc_balance_in* in, orc_balance_state* st, int32_t nthreads, orc_balance_stats* stats);
 
+/* The balance of every cell with its Te held (the evaluations of the
+ * implicit-function adjoint of the converged balance): calcAlpha,
+ * photoionisation, collisional ionisation, Compton and ionBalance at the
+ * state's Te, repeated from where ionBalance stopped until its X(H0), X(He0),
+ * X(He+) changes fall within x_tol (at most 64 times), then thermBalance.
+ * Writes Ne and the ion fractions, n_iter_t = the repetitions, converged = 1
+ * where ionBalance met x_tol, black = 1 where no photon reached the cell, and
+ * resid[cell] = heating - cooling (resid[C+1]).  Returns 0. */
+int orc_balance_fixed_te(const orc_balance_in* in, orc_balance_state* st, int32_t nthreads, double x_tol,
+                         double* resid);
+
 /* updateCell of one cell recording each T-iteration in trace[20][5] (Te,
  * heating, cooling, Ne, X(H0)); returns the number of T-iterations. */
 int orc_balance_trace(const orc_balance_in* in, orc_balance_state* st, int32_t cell, double* trace);

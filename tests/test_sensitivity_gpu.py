@@ -144,7 +144,8 @@ def test_autograd_wrapper(iterated):
     hden0 = ctx.get(abi.ARR_HDEN).astype(np.float64)
     hden = torch.tensor(hden0, requires_grad=True)
     abun = torch.zeros(2, dtype=torch.float64, requires_grad=True)
-    L = frozen_field_lines(ctx, hden, LINES[:2], abun=abun, abun_z=[8, 7], slot=0, precision=abi.BAL_FP64)
+    L = frozen_field_lines(ctx, hden, LINES[:2], abun=abun, abun_z=[8, 7], slot=0, precision=abi.BAL_FP64,
+                           method="differences")
     w = torch.tensor([1.0, 0.5], dtype=torch.float64)
     (w * L).sum().backward()
     ctx.state_restore()
@@ -158,7 +159,7 @@ def test_autograd_wrapper(iterated):
     step = np.float32(hden0[c] * 1e-3)
     hp = hden0.copy()
     hp[c] = float(np.float32(hden0[c]) + step)
-    Lp = frozen_field_lines(ctx, torch.tensor(hp), LINES[:2], slot=0, precision=abi.BAL_FP64)
+    Lp = frozen_field_lines(ctx, torch.tensor(hp), LINES[:2], slot=0, precision=abi.BAL_FP64, method="differences")
     fd = float((w * (Lp - L.detach())).sum()) / float(hp[c] - np.float32(hden0[c]))
     assert fd == pytest.approx(g[c], rel=0.05)
     ctx.put(abi.ARR_HDEN, hden0.astype(np.float32))
