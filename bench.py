@@ -71,6 +71,8 @@ def parse():
                          "inner shells); batch256: 256 small H+He nebulae in one batched context; dust81: the "
                          "81^3 dust-only shell (1e8 packets)")
     ap.add_argument("--tau", type=float, default=1.0, help="tau_V of the dust81 shell")
+    ap.add_argument("--no-adjoint", dest="adjoint", action="store_false",
+                    help="xray41: skip the adjoint measurement (mcx_adjoint and its check)")
     ap.add_argument("--nebulae", type=int, default=256, help="nebulae of the batch256 workload")
     ap.add_argument("--converge-iterations", type=int, default=12,
                     help="iteration limit of the time-to-converged-grid runs (0 = skip them)")
@@ -413,6 +415,48 @@ def line_agreement(a: dict, b: dict, floor: float = 0.01) -> dict:
 # algorithmic bytes: 4 B kappa read + 16 B FP64 J read-modify-write per estimator update, ceil(log2 B) * 4 B
 # per CDF search (transport); 16 B per (cell, frequency) of J read, opacity and CDF written, per balanced
 # cell (balance)
+# the X-ray configuration's adjoint: five forbidden lines against every cell's density and ten abundances
+ADJ_LINES = [(8, 3, 3, 4), (8, 2, 1, 3), (7, 2, 3, 4), (10, 3, 1, 4), (16, 2, 1, 2)]
+ADJ_ABUN = [1, 2, 6, 7, 8, 10, 12, 14, 16, 26]
+
+
+def adjoint_check(ctx, setup, slot: int, h: float = 1e-3, n_cells: int = 64, seed: int = 64) -> dict:
+    """mcx_adjoint (FP64) at the J and gas state left by the last iteration (saved in `slot`), timed, and
+    checked against central differences of tightly converged balances (mcx_line_sensitivities at +h and
+    -h) on n_cells random cells that both differences keep, and on the abundance derivatives."""
+    from mocassin_xray_gb300 import abi
+    ctx.state_save(slot)
+    t0 = time.perf_counter()
+    a = ctx.adjoint(ADJ_LINES, abun_z=ADJ_ABUN, h=h, precision=abi.BAL_FP64)
+    wall = time.perf_counter() - t0
+    ctx.state_restore(slot)
+    fwd = ctx.line_sensitivities(ADJ_LINES, abun_z=ADJ_ABUN, h=h, precision=abi.BAL_FP64)
+    ctx.state_restore(slot)
+    bwd = ctx.line_sensitivities(ADJ_LINES, abun_z=ADJ_ABUN, h=-h, precision=abi.BAL_FP64)
+    ctx.state_restore(slot)
+    central = 0.5 * (fwd["dL_dhden"] + bwd["dL_dhden"])
+    lit = ctx.get(abi.ARR_LG_BLACK) < 1
+    lit[0] = False
+    keep = np.nonzero(lit & (fwd["dL_dhden"][0] != 0) & (bwd["dL_dhden"][0] != 0))[0]
+    cells = np.random.default_rng(seed).choice(keep, size=min(n_cells, keep.size), replace=False)
+    scale = np.abs(central[:, keep]).max(axis=1, keepdims=True)
+    err = np.abs(a["dL_dhden"][:, cells] - central[:, cells])
+    rel = err / np.maximum(np.abs(central[:, cells]), 1e-3 * scale)
+    ca = 0.5 * (fwd["dL_dabun"] + bwd["dL_dabun"])
+    rel_ab = np.abs(a["dL_dabun"] - ca) / np.maximum(np.abs(ca), 1e-3 * np.abs(ca).max())
+    return {"what": f"dL/dHden of every cell and dL/d(abundance) of {len(ADJ_ABUN)} elements for "
+                    f"{len(ADJ_LINES)} forbidden lines {ADJ_LINES}, FP64, at the J and state of the run's last "
+                    "iteration",
+            "ms": float(a["kernel_ms"]), "wall_s": wall, "pinned_cells": a["pinned_cells"],
+            "no_solution_cells": a["no_solution_cells"],
+            "central_differences_ms": float(fwd["kernel_ms"] + bwd["kernel_ms"]),
+            "check_cells": int(cells.size), "h": h,
+            "dL_dhden_rel_err": {"median": float(np.median(rel)), "p90": float(np.percentile(rel, 90)),
+                                 "max": float(rel.max())},
+            "dL_dabun_rel_err": {"median": float(np.median(rel_ab)), "max": float(rel_ab.max())},
+            "cells_left_out_by_differences": int(lit.sum() - keep.size)}
+
+
 def transport_alg_bytes(updates: float, emissions: float, nbins: int) -> float:
     return updates * 20.0 + emissions * math.ceil(math.log2(nbins)) * 4.0
 
@@ -520,6 +564,13 @@ def run_gpu(args, dist, ws, rank, local):
                 "speedup": ref64["s"] / prod["s"],
                 "lines_vs_plain_fp64": line_agreement(prod["lines"], ref64["lines"])}
 
+    # the adjoint of the X-ray configuration (its config names one), at the J of the run's last iteration
+    adj = None
+    if args.workload == "xray41" and args.adjoint:
+        ctx.state_restore(nit)
+        iteration(nit)
+        adj = adjoint_check(ctx, setup, slot=nit + 1)
+
     # e2e: the same steps through the C ABI, each iteration's gas state uploaded from pinned host memory (the
     # state the run reached before it) and the updated state read back; the skip rule's kept arrays come
     # from the iteration's device slot
@@ -598,6 +649,7 @@ def run_gpu(args, dist, ws, rank, local):
             "phase_ms": {k: float(np.mean([p[k] for _, _, p in plain])) for k in plain[0][2]},
             "speedup_of_production": plain_ms / it_ms.get(1, plain_ms)},
         "time_to_converged_grid": conv,
+        "adjoint": adj,
         "transport": {k: float(np.mean([getattr(s, k) for s in tst])) for k in
                       ("crossings", "interactions", "absorptions", "scatterings", "escaped", "line_escapes",
                        "emissions", "trapped", "kernel_ms")},

@@ -501,9 +501,12 @@ int  mcx_line_sensitivities(mcx_ctx* ctx, const mcx_sens_opts* opts, mcx_sens_ou
  * combines the central differences per cell.  No T-iteration is run for a
  * perturbed p, so a cell whose perturbed balance would take another branch of
  * the iteration still gets the derivative of its root.  A cell without a root
- * (its bracket closed on a jump of heating - cooling, no convergence in 64
- * T-iterations, or dR/dTe not finite and non-zero) has its Te held: dTe/dp = 0,
- * counted in pinned_cells.  opts as for mcx_line_sensitivities
+ * (its bracket closed on a jump of heating - cooling, or dR/dTe not finite and
+ * non-zero) has its Te held: dTe/dp = 0, counted in pinned_cells.  A cell whose
+ * balance did not converge in 64 T-iterations has no converged state: its
+ * derivatives are 0, counted in no_solution_cells, and it is left out of the
+ * evaluations (as are the held cells from those at Te(1 +- h)).  opts as for
+ * mcx_line_sensitivities
  * (reference_stopping must be 0).  The context is left as after the converged
  * unperturbed balance.  Gas, one nebula. */
 typedef struct mcx_adjoint_out {
@@ -514,7 +517,8 @@ typedef struct mcx_adjoint_out {
     float   kernel_ms;          /* out: CUDA-event time of the balances, lines and adjoint kernels */
     float   reserved_f[3];
     int64_t pinned_cells;       /* out: cells with their Te held (no root)              */
-    int64_t reserved[3];
+    int64_t no_solution_cells;  /* out: cells without a converged balance (derivatives 0) */
+    int64_t reserved[2];
 } mcx_adjoint_out;
 
 int  mcx_adjoint(mcx_ctx* ctx, const mcx_sens_opts* opts, mcx_adjoint_out* out);

@@ -148,7 +148,8 @@ class SensOpts(C.Structure):
 
 class AdjointOut(C.Structure):
     _fields_ = [("L", _P), ("dL_dhden", _P), ("dL_dabun", _P), ("dte_dhden", _P), ("kernel_ms", C.c_float),
-                ("reserved_f", C.c_float * 3), ("pinned_cells", C.c_int64), ("reserved", C.c_int64 * 3)]
+                ("reserved_f", C.c_float * 3), ("pinned_cells", C.c_int64), ("no_solution_cells", C.c_int64),
+                ("reserved", C.c_int64 * 2)]
 
 
 class SensOut(C.Structure):

@@ -345,8 +345,10 @@ bool sameGrid(const BalanceGrid& a, const BalanceGrid& b) {
 
 cudaError_t launchBalance(BalanceData& bd, const BalanceGrid& g, int maxRounds, int precision, cudaStream_t s,
                           int atomSolves, int converge, int fixTe) {
-  // Te held only with the tight stopping rules (the ladder converged at the held Te)
+  // Te held only with the tight stopping rules (the ladder converged at the held Te); a cell mask
+  // only for those evaluations
   bd.dev.fixTe = fixTe && converge ? 1 : 0;
+  if (!bd.dev.fixTe) bd.dev.evalMask = nullptr;
   {
     // the stopping rules: the reference's, or tight ones at the level the precision resolves
     BalanceDev& d = bd.dev;

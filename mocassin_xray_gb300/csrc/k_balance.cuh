@@ -155,6 +155,8 @@ struct BalanceDev {
   int8_t* side;                // tight mode: bracket end replaced last (1 low, 2 high); 3 = the
                                // bracket closed on a discontinuity of heating - cooling
   double* resid;               // fixTe: heating - cooling at the held Te
+  const uint8_t* evalMask;     // fixTe: 0 leaves the cell out of the evaluation (as if no photon reached
+                               // it); null: every cell
   BalanceCounters* counters;
 };
 

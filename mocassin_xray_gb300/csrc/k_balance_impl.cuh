@@ -263,6 +263,7 @@ __global__ void __launch_bounds__(128) hitComptonKernel(BalanceDev b, const doub
 #pragma unroll
     for (int k = 0; k < 8; ++k) hit = hit || v[k] > 0.;
   }
+  if (b.evalMask && !b.evalMask[cell]) hit = false;
   b.state[cell] = hit ? 0 : 2;
   if (!hit) return;
   b.list[atomicAdd(&b.listCount[0], 1u)] = cell;   // the cells of the first T-iteration
@@ -1247,11 +1248,19 @@ __device__ double equilibriumLines(const BalanceDev& b, int atom, double Te, dou
 }
 
 // forLines of update_mod: one thread per (cell, ion with data)
-__global__ void __launch_bounds__(128) atomsKernel(BalanceDev b, int round) {
+// Tight mode: a cell whose ladder has not converged in this round goes on at the same Te and its
+// residual is not used (the secant step skips it), so its line cooling is not solved; the last round
+// a cell can have still gets it (with Te held, the residual of that round is the result).
+__device__ __forceinline__ bool coolingUnused(const BalanceDev& b, int round, int lastRound, int cell) {
+  return b.converge && !b.ibConv[cell] && b.nIterT[cell] < b.maxIterT && round + 1 < kMaxRounds && !lastRound;
+}
+
+__global__ void __launch_bounds__(128) atomsKernel(BalanceDev b, int round, int lastRound) {
   const int li = blockIdx.x * blockDim.x + threadIdx.x;
   const int atom = blockIdx.y;
   if ((unsigned)li >= b.listCount[round]) return;
   const int cell = b.list[(size_t)(round & 1) * (b.nCells + 1) + li];
+  if (coolingUnused(b, round, lastRound, cell)) return;
   const CellIdx c{cell, b.nCells + 1};
   const int32_t* h = b.atomHdr + (size_t)atom * kAtHdrSize;
   const int elem = h[kAtElem], ion = h[kAtIon];
@@ -1564,11 +1573,12 @@ __device__ __forceinline__ void surfaceAtom(const BalanceDev& b, int round, int 
   *out = w * RD(1.9865e-16) * g;
 }
 
-__global__ void __launch_bounds__(128) surfaceAtomsKernel(BalanceDev b, int round) {
+__global__ void __launch_bounds__(128) surfaceAtomsKernel(BalanceDev b, int round, int lastRound) {
   const int atom = blockIdx.y;
   const unsigned cnt = b.listCount[round];
+  const int C1 = b.nCells + 1;
   for (unsigned li = blockIdx.x * blockDim.x + threadIdx.x; li < cnt; li += gridDim.x * blockDim.x)
-    surfaceAtom(b, round, (int)li, atom);
+    if (!coolingUnused(b, round, lastRound, b.list[(size_t)(round & 1) * C1 + li])) surfaceAtom(b, round, (int)li, atom);
 }
 #endif
 
@@ -1654,7 +1664,9 @@ __device__ __forceinline__ void secantCell(const BalanceDev& b, int round, int l
       if (te <= 0.) te = 1.;
       done = lastRound != 0;   // a caller-imposed round limit ends the cell here
     } else {
-      if (Thigh == 0.) te = Tlow;
+      // (tight mode: a cell whose ladder never converged was never bracketed and keeps its Te)
+      if (Thigh == 0. && Tlow == 0.) {
+      } else if (Thigh == 0.) te = Tlow;
       else if (Tlow == 0.) te = Thigh;
       else te = (Thigh + Tlow) * 0.5;
       atomicAdd(&b.counters->noTeBal, 1ull);
@@ -1736,13 +1748,14 @@ cudaError_t launch(BalanceData& bd, const BalanceGrid& g, int maxRounds, cudaStr
   // round r works on the cells listed for it (the first list holds every cell
   // a packet reached; each secant step lists the cells that go on)
   for (int r = 1; r <= rounds; ++r) {
+    const int last = r == rounds && rounds < b.maxIterT ? 1 : 0;
     ratesKernel<<<rGrid, 32 * b.ratesWarps[kBuildL], ratesSmem(b), s>>>(b, g.hden, r - 1);
 #if !MCX_BAL_EXACT
-    if (b.nAtoms > 0 && useSurfaces) surfaceAtomsKernel<<<dim3(aGrid, b.nAtoms), T, 0, s>>>(b, r - 1);
+    if (b.nAtoms > 0 && useSurfaces) surfaceAtomsKernel<<<dim3(aGrid, b.nAtoms), T, 0, s>>>(b, r - 1, last);
     else
 #endif
-    if (b.nAtoms > 0) atomsKernel<<<dim3(nb, b.nAtoms), T, 0, s>>>(b, r - 1);
-    secantKernel<<<sGrid, T, 0, s>>>(b, r - 1, r == rounds && rounds < b.maxIterT ? 1 : 0);
+    if (b.nAtoms > 0) atomsKernel<<<dim3(nb, b.nAtoms), T, 0, s>>>(b, r - 1, last);
+    secantKernel<<<sGrid, T, 0, s>>>(b, r - 1, last);
   }
   storeKernel<<<nb, T, 0, s>>>(b, g);
   return cudaGetLastError();

@@ -193,8 +193,9 @@ __global__ void __launch_bounds__(128) adjointCombineKernel(AdjointArgs a) {
   const uint8_t hold = a.hold[cell];
   const double dT = (double)a.teP[cell] - (double)a.teM[cell];
   const double dp = a.pP ? (double)a.pP[cell] - (double)a.pM[cell] : a.dpScalar;
+  const bool some = hold < 2 && dT != 0. && dp != 0.;   // a cell with a derivative
   double dTdp = 0.;
-  if (hold != 2 && dT != 0. && dp != 0.) {
+  if (some) {
     const double dRdT = (a.rTp[cell] - a.rTm[cell]) / dT;
     const double dRdp = (a.rPp[cell] - a.rPm[cell]) / dp;
     const bool root = hold == 0 && isfinite(dRdT) && dRdT != 0. && isfinite(dRdp);
@@ -205,7 +206,7 @@ __global__ void __launch_bounds__(128) adjointCombineKernel(AdjointArgs a) {
   for (int k = 0; k < a.nL; ++k) {
     const size_t i = (size_t)k * C1 + cell;
     double v = 0.;
-    if (hold != 2 && dT != 0. && dp != 0.) v = (a.lPp[i] - a.lPm[i]) / dp + (a.lTp[i] - a.lTm[i]) / dT * dTdp;
+    if (some) v = (a.lPp[i] - a.lPm[i]) / dp + (dTdp != 0. ? (a.lTp[i] - a.lTm[i]) / dT * dTdp : 0.);
     a.dLdp[i] = v;
   }
 }

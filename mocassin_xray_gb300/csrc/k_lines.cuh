@@ -75,7 +75,7 @@ struct AdjointArgs {
   const double* lPp, *lPm;    // [nL][C+1]
   const float* pP, *pM;       // [C+1] the stepped per-cell parameter, or null: dpScalar
   double dpScalar;            // p(1+h) - p(1-h) of a parameter shared by all cells
-  const uint8_t* hold;        // [C+1] 0 root, 1 Te held (no root), 2 no photon hit
+  const uint8_t* hold;        // [C+1] 0 root, 1 Te held (no root), 2 no photon hit, 3 no converged balance
   double* dLdp;               // [nL][C+1] out
   double* dTdp;               // [C+1] out, or null
   unsigned long long* held;   // out: cells whose Te was held (hold = 1 or dR/dTe unusable), or null

@@ -1954,10 +1954,11 @@ extern "C" int mcx_adjoint(mcx_ctx* c, const mcx_sens_opts* o, mcx_adjoint_out* 
   }
   DBuf<float> tP, tM, pP, pM;
   DBuf<double> dLdp, dTdp;
-  DBuf<uint8_t> hold;
+  DBuf<uint8_t> hold, maskRoot, maskSome;
   DBuf<unsigned long long> held;
   CK(tP.alloc(C1), "alloc"); CK(tM.alloc(C1), "alloc"); CK(pP.alloc(C1), "alloc"); CK(pM.alloc(C1), "alloc");
   CK(dLdp.alloc(LC), "alloc"); CK(dTdp.alloc(C1), "alloc"); CK(hold.alloc(C1), "alloc"); CK(held.alloc(1), "alloc");
+  CK(maskRoot.alloc(C1), "alloc"); CK(maskSome.alloc(C1), "alloc");
   CK(cudaMemsetAsync(held.p, 0, sizeof(unsigned long long), st), "memset");
   LineCellArgs la{};
   la.te = c->te.p; la.ne = c->ne.p; la.ionDen = c->ionDen.p; la.hden = c->hden.p; la.vol = c->volD.p;
@@ -1971,12 +1972,15 @@ extern "C" int mcx_adjoint(mcx_ctx* c, const mcx_sens_opts* o, mcx_adjoint_out* 
     return MCX_OK;
   };
   StateCopy s1;
-  // R and L with every Te held, from the converged state; te (host) replaces its Te where given
-  auto held_eval = [&](int e, const std::vector<float>* te) -> int {
+  // R and L with every Te held, from the converged state, for the cells of `mask`; te (host) replaces
+  // its Te where given
+  auto held_eval = [&](int e, const std::vector<float>* te, const uint8_t* mask) -> int {
     if (int rc = copyState(c, s1, false)) return rc;
     if (te) CK(cudaMemcpyAsync(c->te.p, te->data(), C1 * sizeof(float), cudaMemcpyHostToDevice, st), "h2d Te");
     bo.fix_te = 1;
+    c->balance->dev.evalMask = mask;
     int rc = mcx_balance(c, &bo, nullptr);
+    c->balance->dev.evalMask = nullptr;
     bo.fix_te = 0;
     if (rc != MCX_OK) return rc;
     if ((rc = lines(e))) return rc;
@@ -1994,6 +1998,7 @@ extern "C" int mcx_adjoint(mcx_ctx* c, const mcx_sens_opts* o, mcx_adjoint_out* 
   CK(cudaEventCreate(&t1), "event");
   CK(cudaEventRecord(t0, st), "event");
   out->pinned_cells = 0;
+  out->no_solution_cells = 0;
   // the converged balance (from the current state) and its line sums
   int rc = mcx_balance(c, &bo, nullptr);
   if (rc == MCX_OK) rc = lines(0);
@@ -2015,11 +2020,19 @@ extern "C" int mcx_adjoint(mcx_ctx* c, const mcx_sens_opts* o, mcx_adjoint_out* 
       for (size_t cell = 1; cell < C1; ++cell) t += hostL[(size_t)k * C1 + cell];
       out->L[k] = t;
     }
-    // a cell without a root: its bracket closed on a jump, or it did not converge
-    std::vector<uint8_t> hh(C1, 2);
-    for (size_t cell = 1; cell < C1; ++cell)
-      hh[cell] = black[cell] >= 1 ? 2 : (side[cell] == 3 || nit[cell] >= kMaxRounds) ? 1 : 0;
+    // a cell without a root: its bracket closed on a jump (Te held); a cell whose balance did not
+    // converge in 64 T-iterations has no converged state to differentiate (no derivative).  The
+    // evaluations at Te(1 +- h) need the cells with a root, those at p(1 +- h) these and the held ones
+    std::vector<uint8_t> hh(C1, 2), mr(C1, 0), ms(C1, 0);
+    for (size_t cell = 1; cell < C1; ++cell) {
+      hh[cell] = black[cell] >= 1 ? 2 : nit[cell] >= kMaxRounds ? 3 : side[cell] == 3 ? 1 : 0;
+      mr[cell] = hh[cell] == 0;
+      ms[cell] = hh[cell] <= 1;
+      out->no_solution_cells += hh[cell] == 3;
+    }
     CK(cudaMemcpyAsync(hold.p, hh.data(), C1, cudaMemcpyHostToDevice, st), "h2d hold");
+    CK(cudaMemcpyAsync(maskRoot.p, mr.data(), C1, cudaMemcpyHostToDevice, st), "h2d mask");
+    CK(cudaMemcpyAsync(maskSome.p, ms.data(), C1, cudaMemcpyHostToDevice, st), "h2d mask");
     // Te(1 +- h)
     for (size_t cell = 0; cell < C1; ++cell) {
       stepP[cell] = (float)((double)te[cell] * (1. + h));
@@ -2027,8 +2040,8 @@ extern "C" int mcx_adjoint(mcx_ctx* c, const mcx_sens_opts* o, mcx_adjoint_out* 
     }
     CK(cudaMemcpyAsync(tP.p, stepP.data(), C1 * sizeof(float), cudaMemcpyHostToDevice, st), "h2d");
     CK(cudaMemcpyAsync(tM.p, stepM.data(), C1 * sizeof(float), cudaMemcpyHostToDevice, st), "h2d");
-    rc = held_eval(1, &stepP);
-    if (rc == MCX_OK) rc = held_eval(2, &stepM);
+    rc = held_eval(1, &stepP, maskRoot.p);
+    if (rc == MCX_OK) rc = held_eval(2, &stepM, maskRoot.p);
   }
   // every cell's Hden (1 +- h) at once: at fixed J each cell answers for itself
   if (rc == MCX_OK && (out->dL_dhden || out->dte_dhden)) {
@@ -2039,10 +2052,10 @@ extern "C" int mcx_adjoint(mcx_ctx* c, const mcx_sens_opts* o, mcx_adjoint_out* 
     CK(cudaMemcpyAsync(pP.p, stepP.data(), C1 * sizeof(float), cudaMemcpyHostToDevice, st), "h2d");
     CK(cudaMemcpyAsync(pM.p, stepM.data(), C1 * sizeof(float), cudaMemcpyHostToDevice, st), "h2d");
     CK(cudaMemcpyAsync(c->hden.p, stepP.data(), C1 * sizeof(float), cudaMemcpyHostToDevice, st), "h2d Hden");
-    rc = held_eval(3, nullptr);
+    rc = held_eval(3, nullptr, maskSome.p);
     if (rc == MCX_OK) {
       CK(cudaMemcpyAsync(c->hden.p, stepM.data(), C1 * sizeof(float), cudaMemcpyHostToDevice, st), "h2d Hden");
-      rc = held_eval(4, nullptr);
+      rc = held_eval(4, nullptr, maskSome.p);
     }
     CK(cudaMemcpyAsync(c->hden.p, hd.data(), C1 * sizeof(float), cudaMemcpyHostToDevice, st), "h2d Hden");
     if (rc == MCX_OK) {
@@ -2065,10 +2078,10 @@ extern "C" int mcx_adjoint(mcx_ctx* c, const mcx_sens_opts* o, mcx_adjoint_out* 
     const float a0 = ab, ap = (float)((double)a0 * (1. + h)), am = (float)((double)a0 * (1. - h));
     ab = ap;
     invalidateBalanceGraphs(*c->balance);
-    rc = held_eval(3, nullptr);
+    rc = held_eval(3, nullptr, maskSome.p);
     ab = am;
     invalidateBalanceGraphs(*c->balance);
-    if (rc == MCX_OK) rc = held_eval(4, nullptr);
+    if (rc == MCX_OK) rc = held_eval(4, nullptr, maskSome.p);
     ab = a0;
     invalidateBalanceGraphs(*c->balance);
     if (rc != MCX_OK) break;

@@ -323,7 +323,7 @@ class Context:
                              dte_dhden=dt.ctypes.data if per_cell else None)
         self._check(lib().mcx_adjoint(self._h, C.byref(o), C.byref(out)))
         return dict(L=L, dL_dhden=dh, dte_dhden=dt, dL_dabun=da[:, :len(z)], kernel_ms=float(out.kernel_ms),
-                    pinned_cells=int(out.pinned_cells))
+                    pinned_cells=int(out.pinned_cells), no_solution_cells=int(out.no_solution_cells))
 
     def state_save(self, slot: int = 0) -> None:
         """Device-side snapshot, in slot `slot`, of everything an iteration

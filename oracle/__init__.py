@@ -722,8 +722,8 @@ def ift_line_gradient(setup, tables: BalanceTables, jste, te, ne, ionden, lines,
     terms).  p is every cell's
     Hden (each cell's own; they do not interact at fixed J) and the abundances of the elements abun_z.
     Returns dL_dhden [lines, cells], dL_dabun [lines, len(abun_z), cells] (each cell's share of
-    dL/d(abundance)), dte_dhden [cells], dR_dte [cells] and dL_dhden_te_held [lines, cells] (the
-    partial derivative with Te held, the gradient of a cell whose Te has no root)."""
+    dL/d(abundance)), dte_dhden [cells], dR_dte [cells], and dL_dhden_te_held, dL_dabun_te_held (the
+    partial derivatives with Te held, the gradient of a cell whose Te has no root)."""
     cells = np.asarray(cells, dtype=np.int64)
     te = np.asarray(te, np.float32)
     hden0 = tables.k["hden"].astype(np.float32)
@@ -754,7 +754,8 @@ def ift_line_gradient(setup, tables: BalanceTables, jste, te, ne, ionden, lines,
     dR_dH, dL_dH = central(hden_step)
     dte_dh = -dR_dH / dR_dT
     out = dict(dL_dhden=dL_dH + dL_dT * dte_dh, dte_dhden=dte_dh, dR_dte=dR_dT, dL_dhden_te_held=dL_dH,
-               dL_dabun=np.zeros((len(lines), len(abun_z), cells.size)))
+               dL_dabun=np.zeros((len(lines), len(abun_z), cells.size)),
+               dL_dabun_te_held=np.zeros((len(lines), len(abun_z), cells.size)))
     for q, z in enumerate(abun_z):
         def abun_step(f, z=z):
             ab = abun0.copy()
@@ -763,6 +764,7 @@ def ift_line_gradient(setup, tables: BalanceTables, jste, te, ne, ionden, lines,
             return r, lum, np.full(cells.size, float(ab[z - 1]))
         dR_dA, dL_dA = central(abun_step)
         out["dL_dabun"][:, q, :] = dL_dA - dL_dT * dR_dA / dR_dT
+        out["dL_dabun_te_held"][:, q, :] = dL_dA
     return out
 
 

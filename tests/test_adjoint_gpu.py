@@ -73,13 +73,15 @@ def test_adjoint_matches_oracle_gradient(field, oracle_lib):
     T = oracle_lib.BalanceTables(s)
     o = oracle_lib.ift_line_gradient(s, T, j, te, ne, ion, LINES, cells, h=1e-3, nthreads=8)
     # a cell whose converged balance found no root keeps its Te (dTe/dHden = 0): the partial
-    # derivative with Te held is its gradient
+    # derivative with Te held is its gradient; a cell without a converged balance has none (0)
     held = a["dte_dhden"][cells] == 0.0
-    assert held.sum() <= 2
-    np.testing.assert_allclose(a["dte_dhden"][cells][~held], o["dte_dhden"][~held], rtol=1e-4,
+    nosol = ctx.get(abi.ARR_N_ITER_T)[cells] >= 64
+    assert held.sum() <= 2 and a["no_solution_cells"] == np.count_nonzero(ctx.get(abi.ARR_N_ITER_T) >= 64)
+    ok = ~held
+    np.testing.assert_allclose(a["dte_dhden"][cells][ok], o["dte_dhden"][ok], rtol=1e-4,
                                atol=1e-6 * np.abs(o["dte_dhden"]).max())
     for k in range(len(LINES)):
-        want = np.where(held, o["dL_dhden_te_held"][k], o["dL_dhden"][k])
+        want = np.where(nosol, 0.0, np.where(held, o["dL_dhden_te_held"][k], o["dL_dhden"][k]))
         np.testing.assert_allclose(a["dL_dhden"][k, cells], want, rtol=1e-4, atol=1e-6 * np.abs(want).max())
     # the line sums are those of the converged balance
     lum = oracle_lib.line_cell_luminosities(s, T, te, ne, ion, cells, LINES)
@@ -115,7 +117,8 @@ def test_adjoint_matches_central_differences(field):
     # cells the differences leave out still get the derivative of their root
     left_out = ~both & lit
     assert np.all(np.isfinite(a["dL_dhden"][:, left_out]))
-    assert np.count_nonzero(a["dL_dhden"][0, left_out]) >= left_out.sum() - a["pinned_cells"]
+    assert np.count_nonzero(a["dL_dhden"][0, left_out]) >= \
+        left_out.sum() - a["pinned_cells"] - a["no_solution_cells"]
 
 
 def test_adjoint_abundance_gradient(field):
@@ -148,3 +151,41 @@ def test_adjoint_autograd(field):
     np.testing.assert_allclose(hden.grad.numpy(), w.numpy() @ a["dL_dhden"], rtol=1e-12, atol=0)
     np.testing.assert_allclose(abun.grad.numpy(), w.numpy() @ a["dL_dabun"], rtol=1e-12, atol=0)
     ctx.put(abi.ARR_HDEN, hden0)
+
+
+XLINES = [(8, 3, 3, 4), (8, 2, 1, 3), (7, 2, 3, 4), (10, 3, 1, 4), (16, 2, 1, 2)]
+
+
+def test_adjoint_xray_chemistry_matches_oracle(decks, data_dir, oracle_lib):
+    """The X-ray chemistry (Mg, Si, Fe with inner shells and Auger electrons, 27 stages, the power-law
+    source to 740 Ryd): five lines, every cell's density and three abundances against the oracle's FP64
+    gradient, the densities on 64 random cells, the abundances summed over every cell."""
+    s = Setup(decks["xray_small"], data_dir)
+    ctx = Context(0)
+    ctx.load(s)
+    ctx.opacity(1)
+    ctx.emission(1)
+    ctx.transport(20000, seed=5, precision=abi.PREC_FP64)
+    ctx.normalize_j()
+    z = [8, 26, 14]
+    a = ctx.adjoint(XLINES, abun_z=z, precision=abi.BAL_FP64, h=1e-3)
+    te, ne, ion, j = (ctx.get(x) for x in (abi.ARR_TE, abi.ARR_NE, abi.ARR_IONDEN, abi.ARR_JSTE))
+    lit = np.nonzero(ctx.get(abi.ARR_LG_BLACK)[1:] < 1)[0] + 1
+    # from the deck's first J a fifth of these cells have no converged balance (their ladders do not
+    # settle in 64 T-iterations): no derivative; the others are compared
+    nosol = ctx.get(abi.ARR_N_ITER_T)[lit] >= 64
+    ctx.close()
+    assert a["no_solution_cells"] == nosol.sum() and nosol.sum() < 0.5 * lit.size
+    assert np.all(a["dL_dhden"][:, lit[nosol]] == 0.0)
+    lit = lit[~nosol]
+    T = oracle_lib.BalanceTables(s)
+    o = oracle_lib.ift_line_gradient(s, T, j, te, ne, ion, XLINES, lit, abun_z=z, h=1e-3, nthreads=8)
+    held = a["dte_dhden"][lit] == 0.0
+    assert a["pinned_cells"] <= held.sum() <= a["pinned_cells"] + 0.05 * lit.size
+    cells = np.sort(np.random.default_rng(9).choice(lit.size, size=min(64, lit.size), replace=False))
+    for k in range(len(XLINES)):
+        want = np.where(held, o["dL_dhden_te_held"][k], o["dL_dhden"][k])[cells]
+        np.testing.assert_allclose(a["dL_dhden"][k, lit[cells]], want, rtol=1e-4, atol=1e-6 * np.abs(want).max())
+    total = np.where(held[None, None, :], o["dL_dabun_te_held"], o["dL_dabun"]).sum(axis=2)
+    np.testing.assert_allclose(a["dL_dabun"], total, rtol=1e-4, atol=1e-6 * np.abs(total).max())
+    assert np.all(a["L"] > 0)
