@@ -118,7 +118,7 @@ def _c_struct(text: str, name: str) -> list:
     body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
     fields = []
     for decl in body.split(";"):
-        decl = decl.strip()
+        decl = re.sub(r"^const\s+", "", decl.strip())
         if not decl:
             continue
         m = re.match(r"(\w+)\s*(\*?)\s*(.*)", decl)
@@ -137,6 +137,7 @@ def test_fortran_binding_matches_header():
     root = Path(__file__).resolve().parents[1]
     ftypes = _fortran_types((root / "INTEGRATION.md").read_text())
     header = (root / "include" / "mcx.h").read_text()
-    assert {"mcx_balance_opts", "mcx_transport_opts", "mcx_lines"} <= set(ftypes)
+    assert {"mcx_balance_opts", "mcx_transport_opts", "mcx_lines", "mcx_line_ref", "mcx_sens_opts",
+            "mcx_adjoint_out"} <= set(ftypes)
     for name, ffields in ftypes.items():
         assert ffields == _c_struct(header, name), name
