@@ -140,6 +140,10 @@ enum mcx_array_id {
 #define MCX_SARR_DUST_RADIUS   1046  /* float[nSizes] grainRadius [um]                                  */
 #define MCX_SARR_DUST_WEIGHT   1047  /* float[nSizes] normalised grainWeight                            */
 #define MCX_SARR_DUST_EMINT    1048  /* float[nSpecies][nSizes][nTemps] dustEmIntegral                  */
+#define MCX_SARR_STARS         1049  /* float[nStars][8] per source: Lstar [e36 erg/s], TStellar [K],
+                                        starPosition x, y, z [cm], its cell's x, y, z indices
+                                        (1-based, -1 outside the grid)                            */
+#define MCX_SARR_SRC_CDFS      1050  /* float[nStars][nbins] inSpectrumProbDen(1:nStars,:)          */
 #define MCX_SARR_ATOM_DATA     1038  /* double[n] packed atom data: log10 T[nTemp]; qom and its natural-
                                         spline second derivatives [pair (l<u) row-major][nTemp];
                                         a(j,i) at [j-1][i-1]; g; e [1/cm]; recombination fits; atp    */
@@ -191,7 +195,10 @@ typedef struct mcx_setup_info {
     float   view_phi[2];        /* viewPointPhi(1:2) [rad]; < 0: no phi dependence     */
     int32_t plane_ionization;   /* 1: lgPlaneIonization (the source is the plane y = 0,
                                    l_star = transferred flux x the x-z extent)         */
-    int32_t reserved[2];
+    int32_t n_stars;            /* nStars: ionising sources (multiPhotoSources; else 1); star_*,
+                                   l_star and MCX_ARR_SRC_CDF are source 1's, n_photons is
+                                   nPhotons(1) = nPhotons / nStars                      */
+    int32_t reserved[1];
 } mcx_setup_info;
 
 int  mcx_setup_from_input(const char* input_file, const char* data_dir,
@@ -409,7 +416,8 @@ typedef struct mcx_iterate_opts {
     int32_t transport_precision;    /* MCX_PREC_*                                          */
     int32_t balance_precision;      /* MCX_BAL_*                                           */
     int32_t emission_precision;     /* MCX_PHASE_*                                         */
-    int64_t n_packets;              /* nPhotons(1)                                         */
+    int64_t n_packets;              /* nPhotons: every source's packets (each of nStars
+                                       sources sends n_packets / nStars)                   */
     uint64_t seed;                  /* Philox key                                          */
     uint64_t counter_base;          /* global id of the iteration's first packet           */
     int32_t transport_block_size;   /* the transport launch (mcx_transport_opts' fields of the */

@@ -33,6 +33,7 @@ SARR_POINTERS, SARR_ELEMENT_P, SARR_N_SHELLS, SARR_ELEM_XREF, SARR_ION_EDGE, SAR
  SARR_ATOM_INDEX, SARR_ATOM_HDR, SARR_ATOM_DATA) = range(1024, 1039)
 (SARR_DUST_DIMS, SARR_DUST_CABS, SARR_DUST_CSCA, SARR_DUST_CTABS, SARR_DUST_CTSCA, SARR_DUST_ABUN, SARR_DUST_TSUB,
  SARR_DUST_RADIUS, SARR_DUST_WEIGHT, SARR_DUST_EMINT) = range(1039, 1049)
+SARR_STARS, SARR_SRC_CDFS = 1049, 1050
 INT_SARR = {SARR_POINTERS, SARR_ELEMENT_P, SARR_N_SHELLS, SARR_ELEM_XREF, SARR_EM_DIMS, SARR_EM_EDGE_P,
             SARR_EM_FB_HEAVY, SARR_EM_HYDRO_MAP, SARR_NAUGER, SARR_OUTER_SHELL, SARR_ATOM_INDEX, SARR_ATOM_HDR,
             SARR_DUST_DIMS}
@@ -61,7 +62,7 @@ class SetupInfo(C.Structure):
                 ("l_star", C.c_float), ("l_phot", C.c_float), ("ion_edge1", C.c_float), ("te_start", C.c_float),
                 ("min_convergence", C.c_float), ("xhi_limit", C.c_float), ("n_angle_bins", C.c_int32),
                 ("view_theta", C.c_float * 2), ("view_phi", C.c_float * 2), ("plane_ionization", C.c_int32),
-                ("reserved", C.c_int32 * 2)]
+                ("n_stars", C.c_int32), ("reserved", C.c_int32 * 1)]
 
 
 class BalanceOpts(C.Structure):

@@ -91,6 +91,52 @@ def h_sphere(root: str | Path, n: int = 19, packets: int = 100_000, iterations: 
     ])
 
 
+def multi_source(root: str | Path, sources, n: int = 11, packets: int = 40_000, iterations: int = 4,
+                 nbins: int = 300, edge: float = 6.0e18, hden: float = 200.0) -> Path:
+    """An H + He nebula lit by several sources (the 'multiPhotoSources' file of
+    source/set_input_mod.f90:741-800): `sources` are rows (TStellar [K], Lstar
+    [1e36 erg/s], contShape, (x, y, z) as fractions of the axes' last values,
+    spID, tStep); a spectrum file named in contShape is relative to the run
+    directory.  The grid is the full cube [-edge, edge]^3."""
+    root = Path(root)
+    inp = root / "input"
+    inp.mkdir(parents=True, exist_ok=True)
+    _write_abundances(inp / "abun_hhe.in", {"H": 1.0, "He": 0.1})
+    rows = [f"{len(sources)}"]
+    for t, l, shape, (x, y, z), sp, ts in sources:
+        rows.append(f"{t:.6e} {l:.6e} '{shape}' {x:.6e} {y:.6e} {z:.6e} '{sp}' {ts:.6e}")
+    (inp / "sources.in").write_text("\n".join(rows) + "\n")
+    return _deck(root, [
+        f"nx {n}", f"ny {n}", f"nz {n}",
+        f"Hdensity {hden}",
+        f"edges {edge:.6e} {edge:.6e} {edge:.6e}",
+        "Rin 0.",
+        "multiPhotoSources 'input/sources.in'",
+        f"nbins {nbins}",
+        "nuMin 1.e-4",
+        "nuMax 100.",
+        f"nPhotons {packets}",
+        f"maxIterateMC {iterations} 95.",
+        "TeStart 10000.",
+        "nstages 4",
+        "nebComposition 'input/abun_hhe.in'",
+    ])
+
+
+def write_sb99(path: str | Path, blocks) -> Path:
+    """A Starburst99 spectrum file as setContinuum reads it
+    (source/continuum_mod.f90:129-170): 7 comment records, then for each (time,
+    log10 L_lambda [erg/s/A] at 1221 ascending wavelengths [A]) block its
+    records of time, wavelength, a third column and log L_lambda."""
+    path = Path(path)
+    out = [f"# synthetic Starburst99 spectrum, comment record {k}" for k in range(1, 8)]
+    for time, lam, logl in blocks:
+        assert len(lam) == 1221 and len(logl) == 1221
+        out += [f"{time:.6e} {a:.6e} {b - 0.5:.6e} {b:.6e}" for a, b in zip(lam, logl)]
+    path.write_text("\n".join(out) + "\n")
+    return path
+
+
 LOGNORMAL_ABUN = {"H": 1.0, "He": 0.1, "C": 3e-4, "N": 1e-4, "O": 5e-4, "Ne": 1e-4, "S": 1e-5}
 
 

@@ -111,6 +111,7 @@ extern "C" int mcx_setup_info_get(const mcx_setup* m, mcx_setup_info* info) {
   info->nx = s.nx; info->ny = s.ny; info->nz = s.nz;
   info->n_angle_bins = s.p.nAngleBins;
   info->plane_ionization = s.p.lgPlaneIonization ? 1 : 0;
+  info->n_stars = (int32_t)std::max<size_t>(s.stars.size(), 1);
   for (int j = 0; j < 2; ++j) { info->view_theta[j] = s.p.viewTheta[j]; info->view_phi[j] = s.p.viewPhi[j]; }
   info->n_cells = s.nCells;
   info->nbins = s.nbins;
@@ -121,7 +122,7 @@ extern "C" int mcx_setup_info_get(const mcx_setup* m, mcx_setup_info* info) {
   info->lg_gas = s.p.lgGas; info->lg_dust = s.p.lgDust; info->lg_compton = s.p.lgCompton;
   for (int d = 0; d < 3; ++d) { info->star_idx[d] = s.starIdx[d]; info->star_pos[d] = s.starPos[d]; }
   info->lyman_p = s.lymanP;
-  info->n_photons = s.p.nPhotons;
+  info->n_photons = s.p.nPhotons / std::max<int64_t>((int64_t)s.stars.size(), 1);
   info->max_iterate_mc = s.p.maxIterateMC;
   info->r_out = s.p.R_out; info->r_in = s.p.R_in;
   info->l_star = s.LStar; info->l_phot = s.LPhot;
@@ -140,6 +141,31 @@ static std::vector<int32_t> packedPointers(const Setup& s) {
   p[8] = s.KshellLimitP; p[9] = s.secIonP; p[10] = s.cRecoilHP; p[11] = s.cRecoilHeP;
   p[12] = s.xrayP; p[13] = s.BjumpP;
   return p;
+}
+
+// The sources as MCX_SARR_STARS lays them out; source 1 from the single-source fields (which
+// mcx_setup_set may have changed)
+static std::vector<float> starTable(const Setup& s) {
+  const size_t n = std::max<size_t>(s.stars.size(), 1);
+  std::vector<float> t(8 * n, 0.f);
+  for (size_t i = 0; i < n; ++i) {
+    float* r = t.data() + 8 * i;
+    const bool one = i == 0 || s.stars.size() <= i;
+    r[0] = one ? s.LStar : s.stars[i].LStar;
+    r[1] = one ? s.p.TStellar : s.stars[i].TStellar;
+    for (int d = 0; d < 3; ++d) {
+      r[2 + d] = one ? s.starPos[d] : s.stars[i].pos[d];
+      r[5 + d] = (float)(one ? s.starIdx[d] : s.stars[i].idx[d]);
+    }
+  }
+  return t;
+}
+
+// Every source's CDF, [nStars][nbins]; source 1's from srcCDF
+static std::vector<float> sourceCDFs(const Setup& s) {
+  std::vector<float> c(s.srcCDF);
+  for (size_t i = 1; i < s.stars.size(); ++i) c.insert(c.end(), s.stars[i].cdf.begin(), s.stars[i].cdf.end());
+  return c;
 }
 
 extern "C" int mcx_setup_get(const mcx_setup* m, int32_t id, void* dst, size_t nbytes) {
@@ -234,6 +260,8 @@ extern "C" int mcx_setup_get(const mcx_setup* m, int32_t id, void* dst, size_t n
     case MCX_SARR_DUST_WEIGHT: return copyOut(s.dust.grainWeight, dst, nbytes);
     case MCX_SARR_DUST_EMINT: return copyOut(s.dust.emIntegral, dst, nbytes);
     case MCX_ARR_TDUST: return copyOut(s.Tdust, dst, nbytes);
+    case MCX_SARR_STARS: return copyOut(starTable(s), dst, nbytes);
+    case MCX_SARR_SRC_CDFS: return copyOut(sourceCDFs(s), dst, nbytes);
     default: g_setupError = "mcx_setup_get: unknown array id " + std::to_string(id); return MCX_ERR_INPUT;
   }
 }
@@ -295,6 +323,8 @@ extern "C" int mcx_setup_len(const mcx_setup* m, int32_t id, int64_t* count) {
     case MCX_SARR_DUST_RADIUS: case MCX_SARR_DUST_WEIGHT: *count = s.dust.nSizes; break;
     case MCX_SARR_DUST_EMINT: *count = (int64_t)s.dust.emIntegral.size(); break;
     case MCX_ARR_TDUST: *count = (int64_t)s.Tdust.size(); break;
+    case MCX_SARR_STARS: *count = 8 * (int64_t)std::max<size_t>(s.stars.size(), 1); break;
+    case MCX_SARR_SRC_CDFS: *count = nb * (int64_t)std::max<size_t>(s.stars.size(), 1); break;
 
     default: g_setupError = "mcx_setup_len: unknown array id " + std::to_string(id); return MCX_ERR_INPUT;
   }
@@ -371,6 +401,8 @@ struct mcx_ctx {
   int64_t nPhotons = 0;
   int starIdx[3] = {0, 0, 0};
   float starPos[3] = {0.f, 0.f, 0.f};
+  int nStars = 1;                  // ionising sources; srcCDF holds their CDFs, [nStars][nbins]
+  std::vector<float> stars;        // [nStars][8] as MCX_SARR_STARS
   std::vector<int32_t> activeHost;
   int activeFull = 0;        // active(i,j,k) == (i-1) ny nz + (j-1) nz + k for every cell
   int plane = 0;             // plane-parallel ionisation (lgPlaneIonization)
@@ -735,15 +767,18 @@ static int loadSetup(mcx_ctx* c, const Setup& s) {
   c->lStar = s.LStar; c->ionEdge1 = s.ionEdge.empty() ? 0.f : s.ionEdge[0]; c->rOut = s.p.R_out;
   c->nPhotons = s.p.nPhotons;
   for (int d = 0; d < 3; ++d) { c->starIdx[d] = s.starIdx[d]; c->starPos[d] = s.starPos[d]; }
+  c->stars = starTable(s);
+  c->nStars = (int)(c->stars.size() / 8);
   c->gauntTeOld = -1.f;
   // validate what the kernels index with
   for (int32_t a : s.active)
     if (a < 0 || a > s.nCells) return fail(c, MCX_ERR_INPUT, "mcx_load: active() holds ids outside [0, nCells] (sub-grids are not supported)");
   if (s.nbins < 2 || s.nCells < 1) return fail(c, MCX_ERR_INPUT, "mcx_load: empty grid or frequency mesh");
-  if (!s.p.lgPlaneIonization &&
-      (s.starIdx[0] < 1 || s.starIdx[0] > s.nx || s.starIdx[1] < 1 || s.starIdx[1] > s.ny || s.starIdx[2] < 1 ||
-       s.starIdx[2] > s.nz))
-    return fail(c, MCX_ERR_INPUT, "mcx_load: the source must lie inside the grid");
+  for (int i = 0; i < c->nStars && !s.p.lgPlaneIonization; ++i) {
+    const float* r = c->stars.data() + 8 * i;
+    if (r[5] < 1.f || r[5] > (float)s.nx || r[6] < 1.f || r[6] > (float)s.ny || r[7] < 1.f || r[7] > (float)s.nz)
+      return fail(c, MCX_ERR_INPUT, "mcx_load: source " + std::to_string(i + 1) + " must lie inside the grid");
+  }
   c->plane = s.p.lgPlaneIonization ? 1 : 0;
   c->activeHost = s.active;
   c->activeFull = 1;
@@ -798,7 +833,7 @@ static int loadSetup(mcx_ctx* c, const Setup& s) {
   CK(upload(c->KNsigmaT, s.KNsigmaT), "upload KNsigmaT");
   CK(upload(c->KNcdfT, knT), "upload KN cdf");
   CK(upload(c->PcompT, pcT), "upload Pcomp");
-  CK(upload(c->srcCDF, s.srcCDF), "upload srcCDF");
+  CK(upload(c->srcCDF, sourceCDFs(s)), "upload srcCDF");
   CK(upload(c->xAxis, s.xAxis), "upload xAxis");
   CK(upload(c->yAxis, s.yAxis), "upload yAxis");
   CK(upload(c->zAxis, s.zAxis), "upload zAxis");
@@ -931,6 +966,7 @@ extern "C" int mcx_load_batched(mcx_ctx* c, const mcx_setup* const* setups, int3
     if (s.starIdx[0] < 1 || s.starIdx[0] > s.nx || s.starIdx[1] < 1 || s.starIdx[1] > s.ny || s.starIdx[2] < 1 ||
         s.starIdx[2] > s.nz)
       return fail(c, MCX_ERR_INPUT, "mcx_load_batched: a source lies outside its grid");
+    if (s.stars.size() > 1) return fail(c, MCX_ERR_INPUT, "mcx_load_batched: one ionising source per nebula");
     total += s.nCells;
   }
   if (total > (int64_t)INT32_MAX - 1) return fail(c, MCX_ERR_INPUT, "mcx_load_batched: too many cells");
@@ -1050,7 +1086,7 @@ ArrView viewOf(mcx_ctx* c, int id) {
   switch (id) {
     case MCX_ARR_NU: return {c->nu.p, c->nu.bytes()};
     case MCX_ARR_XSEC: return {c->xsec.p, c->xsec.bytes()};
-    case MCX_ARR_SRC_CDF: return {c->srcCDF.p, c->srcCDF.bytes()};
+    case MCX_ARR_SRC_CDF: return {c->srcCDF.p, (size_t)c->nbins * sizeof(float)};   // source 1's
     case MCX_ARR_KN_SIGMA_T: return {c->KNsigmaT.p, c->KNsigmaT.bytes()};
     case MCX_ARR_XAXIS: return {c->xAxis.p, c->xAxis.bytes()};
     case MCX_ARR_YAXIS: return {c->yAxis.p, c->yAxis.bytes()};
@@ -1328,7 +1364,9 @@ static int transportFinish(mcx_ctx* c, mcx_transport_stats* stats, const char* w
 extern "C" int mcx_transport(mcx_ctx* c, const mcx_transport_opts* o, mcx_transport_stats* stats) {
   if (!c || !o) return fail(c, MCX_ERR_INPUT, "mcx_transport: null argument");
   if (!c->loaded) return fail(c, MCX_ERR_STATE, "mcx_transport: no model loaded");
-  if (o->istar != 1) return fail(c, MCX_ERR_INPUT, "mcx_transport: only source 1 is supported");
+  if (o->istar < 1 || o->istar > c->nStars)
+    return fail(c, MCX_ERR_INPUT, "mcx_transport: source " + std::to_string(o->istar) + " of " +
+                                      std::to_string(c->nStars));
   if (o->n_packets < 0) return fail(c, MCX_ERR_INPUT, "mcx_transport: negative packet count");
   if (!c->haveOpacity) return fail(c, MCX_ERR_STATE, "mcx_transport: no opacity (call mcx_opacity or mcx_put(MCX_ARR_OPACITY))");
   if (c->lgGas && !c->haveRecPDF) return fail(c, MCX_ERR_STATE, "mcx_transport: no re-emission CDF (recPDF)");
@@ -1338,7 +1376,10 @@ extern "C" int mcx_transport(mcx_ctx* c, const mcx_transport_opts* o, mcx_transp
   if (c->nNeb > 0) return fail(c, MCX_ERR_STATE, "mcx_transport: the context holds a batch (use mcx_transport_batched)");
   CK(cudaSetDevice(c->device), "cudaSetDevice");
   const int64_t norm = o->n_photons_norm > 0 ? o->n_photons_norm : o->n_packets;
-  const double deltaE = norm > 0 ? (double)c->lStar / (double)norm : 0.;
+  // source istar: its luminosity, position and CDF row (source 1: the context's, which mcx_put may change)
+  const int si = o->istar - 1;
+  const float* star = c->stars.data() + 8 * si;
+  const double deltaE = norm > 0 ? (double)(si == 0 ? c->lStar : star[0]) / (double)norm : 0.;
   if (o->zero_estimators) {
     CK(cudaMemsetAsync(c->jste.p, 0, c->jste.bytes(), c->stream), "memset Jste");
     CK(cudaMemsetAsync(c->jlo.p, 0, c->jlo.bytes(), c->stream), "memset Jste compensation");
@@ -1351,10 +1392,14 @@ extern "C" int mcx_transport(mcx_ctx* c, const mcx_transport_opts* o, mcx_transp
   g.nx = c->nx; g.ny = c->ny; g.nz = c->nz; g.nCells = c->nCells; g.nbins = c->nbins;
   g.symmetric = c->symmetric; g.lgDust = c->lgDust; g.lgGas = c->lgGas; g.lgCompton = c->lgCompton;
   g.radPress = c->radPress; g.activeFull = c->activeFull; g.plane = c->plane;
-  for (int d = 0; d < 3; ++d) { g.starIdx[d] = c->starIdx[d]; g.starPos[d] = c->starPos[d]; }
+  for (int d = 0; d < 3; ++d) {
+    g.starIdx[d] = si == 0 ? c->starIdx[d] : (int)star[5 + d];
+    g.starPos[d] = si == 0 ? c->starPos[d] : star[2 + d];
+  }
   g.ionEdge1 = c->ionEdge1; g.rOut = c->rOut;
   g.xAxis = c->xAxis.p; g.yAxis = c->yAxis.p; g.zAxis = c->zAxis.p; g.active = c->active.p;
-  g.nu = c->nu.p; g.srcCDF = c->srcCDF.p; g.KNsigmaT = c->KNsigmaT.p; g.KNcdfT = c->KNcdfT.p;
+  g.nu = c->nu.p; g.srcCDF = c->srcCDF.p + (size_t)si * c->nbins; g.KNsigmaT = c->KNsigmaT.p;
+  g.KNcdfT = c->KNcdfT.p;
   g.PcompT = c->PcompT.p; g.volD = c->volD.p; g.volF = c->volF.p;
   g.nAngle = c->nAngle; g.totPhi = c->totPhi;
   std::memcpy(g.viewPTheta, c->viewPTheta, sizeof g.viewPTheta);
@@ -1616,7 +1661,31 @@ static int iterateImpl(mcx_ctx* c, const mcx_iterate_opts* o, const mcx_batch_pa
     to.block_size = o->transport_block_size;
     to.grid_mult = o->transport_grid_mult;
     to.emit_batch = o->transport_emit_batch;
-    rc = pk ? mcx_transport_batched(c, &to, pk, &st.transport) : mcx_transport(c, &to, &st.transport);
+    if (pk) {
+      rc = mcx_transport_batched(c, &to, pk, &st.transport);
+    } else {
+      // the sources one after another (source/iteration_mod.f90:729-753): nPhotons / nStars packets each,
+      // on consecutive counter ranges; J adds up, the escape tallies keep the last source's (the reference
+      // zeroes escapedPackets before each source)
+      const int64_t per = c->nStars > 1 ? o->n_packets / c->nStars : o->n_packets;
+      mcx_transport_stats& ts = st.transport;
+      for (int i = 1; i <= c->nStars && rc == MCX_OK; ++i) {
+        to.istar = i;
+        to.n_packets = per;
+        to.n_photons_norm = per;
+        to.counter_base = o->counter_base + (uint64_t)(i - 1) * (uint64_t)per;
+        to.zero_estimators = i == 1 ? 1 : 0;
+        if (i > 1) CK(cudaMemsetAsync(c->escaped.p, 0, c->escaped.bytes(), c->stream), "memset escaped");
+        mcx_transport_stats one{};
+        rc = mcx_transport(c, &to, &one);
+        if (rc != MCX_OK) break;
+        if (i == 1) { ts = one; continue; }
+        ts.crossings += one.crossings; ts.interactions += one.interactions; ts.absorptions += one.absorptions;
+        ts.scatterings += one.scatterings; ts.escaped += one.escaped; ts.line_escapes += one.line_escapes;
+        ts.trapped += one.trapped; ts.emissions += one.emissions; ts.q_phot += one.q_phot;
+        ts.kernel_ms += one.kernel_ms; ts.handed_off += one.handed_off;
+      }
+    }
   }
   if (rc == MCX_OK) rc = mcx_normalize_j(c);
   if (rc == MCX_OK) {

@@ -91,6 +91,50 @@ std::string toS(const std::vector<std::string>& t, size_t k, const std::string& 
   return t[k];
 }
 
+// setMultiPhotoSources (source/set_input_mod.f90:741-800): the number of
+// sources, then one list-directed READ per source of Tstellar, Lstar,
+// contShape, x, y, z (fractions of the axes' last values), spID and tStep.
+// A READ starts a new record and takes its values across records.
+void readMultiPhotoSources(Params& p) {
+  const std::string path = joinPath(p.baseDir, p.multiPhotoSources);
+  std::ifstream in(path);
+  if (!in) fail("setMultiPhotoSources: can't open ionising sources file " + path);
+  auto readValues = [&](size_t n) {
+    std::vector<std::string> v;
+    std::string line;
+    while (v.size() < n && std::getline(in, line))
+      for (auto& x : splitRecord(line))
+        if (v.size() < n) v.push_back(x);
+    if (v.size() < n) fail("setMultiPhotoSources: " + path + " ends before its last source");
+    return v;
+  };
+  const int64_t n = toI(readValues(1), 0, "nStars");
+  if (n < 1 || n > 4096) fail("setMultiPhotoSources: invalid number of sources in " + path);
+  p.starsIn.clear();
+  for (int64_t i = 0; i < n; ++i) {
+    const auto v = readValues(8);
+    StarIn st;
+    st.TStellar = toF(v, 0, "Tstellar");
+    st.LStar = toF(v, 1, "Lstar");
+    st.contShape = v[2];
+    for (int d = 0; d < 3; ++d) st.pos[d] = toF(v, 3 + d, "starPosition");
+    st.spID = v[6];
+    st.tStep = toF(v, 7, "tStep");
+    p.starsIn.push_back(st);
+  }
+}
+
+// The deck's single-source fields set to source `st` (each source's spectrum
+// and position are built with them).
+void useStar(Params& p, const StarIn& st) {
+  p.contShape = st.contShape;
+  p.spID = (st.contShape == "blackbody" || st.contShape == "powerlaw") ? st.contShape : st.spID;
+  p.tStep = st.tStep;
+  p.TStellar = st.TStellar;
+  p.LStar = st.LStar;
+  for (int d = 0; d < 3; ++d) p.starPos[d] = st.pos[d];
+}
+
 // readInput (source/set_input_mod.f90:140-500): one keyword per record.
 void parseInput(Params& p, const std::string& path) {
   std::ifstream in(path);
@@ -181,13 +225,33 @@ void parseInput(Params& p, const std::string& path) {
       p.lgPlaneIonization = true;
       p.LStar = 0.f;
     }
+    else if (kw == "multiPhotoSources") p.multiPhotoSources = toS(t, 1, kw);
     else if (kw == "multiGrids" || kw == "multiChemistry" ||
-             kw == "2D" || kw == "diffuseSource" || kw == "multiPhotoSources" ||
+             kw == "2D" || kw == "diffuseSource" ||
              kw == "quantumHeatGrain" || kw == "resLinesTransfer" || kw == "MdMg" || kw == "MdMh" ||
              kw == "fluorescence" || kw == "nahar") {
       fail("readInput: keyword '" + kw + "' selects a reference path outside this library's scope");
     }
     else fail("readInput: invalid keyword in model parameter input file: " + kw);
+  }
+
+  if (!p.multiPhotoSources.empty()) {
+    // the sources come from the file (the deck's contShape, TStellar, Lstar and starPosition are not
+    // used); the checks below see source 1
+    readMultiPhotoSources(p);
+    if (p.lgPlaneIonization) fail("readInput: planeIonization with multiPhotoSources");
+    if (p.LPhot != 0.f) fail("readInput: LPhot with multiPhotoSources (each source's Lstar is in its file)");
+    for (size_t i = 0; i < p.starsIn.size(); ++i) {
+      const StarIn& st = p.starsIn[i];
+      const std::string at = "setMultiPhotoSources: source " + std::to_string(i + 1);
+      if (st.contShape == "powerlaw") fail(at + ": a powerlaw source needs pwlIndex, which the file does not carry");
+      if (st.contShape == "blackbody" && st.TStellar <= 0.f) fail(at + ": TStellar must be given for a blackbody");
+      if (st.contShape != "blackbody" && st.spID != "rauch" && st.spID != "sb99")
+        fail(at + ": unsupported spectrum ID '" + st.spID + "'");
+      if (st.LStar <= 0.f) fail(at + ": Lstar must be positive");
+    }
+    useStar(p, p.starsIn[0]);
+    p.haveContShape = p.haveLStar = p.haveTStellar = true;
   }
 
   // consistency checks of source/set_input_mod.f90:560-704 (those on this path)
@@ -747,6 +811,77 @@ void readSpectrumFile(Setup& s, std::vector<double>& erg) {
   }
 }
 
+// A Starburst99 spectrum (setContinuum, source/continuum_mod.f90:129-222): 7
+// comment records, then records of time, wavelength [A], a skipped column and
+// log L_lambda [erg/s/A]; the 1221 records that start at the first one of time
+// tStep become L_nu [erg/s/Hz] (FP64) at nu [Ryd] (REAL) in ascending
+// frequency.  Each is added to the mesh bin whose edges (the midpoints between
+// mesh points; half widths at both ends) hold it, the bins are averaged, the
+// photon spectrum is taken, and only then are the empty bins between filled
+// ones interpolated linearly in the energy spectrum (so the photon spectrum
+// stays 0 there, as in the reference).
+void readSB99(Setup& s) {
+  const int nb = s.nbins;
+  constexpr int kSb99NuLim = 1221;
+  const std::string path = joinPath(s.p.baseDir, s.p.contShape);
+  std::ifstream in(path);
+  if (!in) fail("setContinuum: can't open spectrum file " + path);
+  std::string line;
+  for (int j = 0; j < 7 && std::getline(in, line); ++j) {}
+  std::vector<std::vector<std::string>> block;
+  while (std::getline(in, line)) {
+    auto t = splitRecord(line);
+    if (t.empty()) continue;
+    if (block.empty() && toF(t, 0, "sb99 time") != s.p.tStep) continue;
+    block.push_back(t);
+    if ((int)block.size() == kSb99NuLim) break;
+  }
+  if ((int)block.size() < kSb99NuLim)
+    fail("setContinuum: " + path + " has no 1221 records at time step " + std::to_string(s.p.tStep));
+  const float c = 2.9979250e10f;
+  std::vector<double> hflux(kSb99NuLim);
+  std::vector<float> en(kSb99NuLim);
+  for (int k = 0; k < kSb99NuLim; ++k) {
+    const float lam = toF(block[k], 1, "sb99 wavelength");
+    const double logL = std::strtod(toS(block[k], 3, "sb99 log L").c_str(), nullptr);
+    // reversed into ascending frequency
+    hflux[kSb99NuLim - 1 - k] = (std::pow(10., logL) * (double)(1.e-8f * (lam * lam))) / (double)c;
+    en[kSb99NuLim - 1 - k] = (c / (lam * 1.e-8f)) / kCRyd;
+  }
+  std::vector<int> count(nb, 0);
+  for (int j = 0; j < kSb99NuLim; ++j) {
+    const float e = en[j];
+    if (e >= s.nu[0] - s.widFlx[0] / 2.f && e < s.nu[0] + s.widFlx[0] / 2.f) {
+      s.inSpectrumErg[0] += hflux[j];
+      ++count[0];
+    }
+    for (int i = 1; i < nb - 1; ++i)
+      if (e >= (s.nu[i - 1] + s.nu[i]) / 2.f && e < (s.nu[i + 1] + s.nu[i]) / 2.f) {
+        s.inSpectrumErg[i] += hflux[j];
+        ++count[i];
+      }
+    if (e >= s.nu[nb - 1] - s.widFlx[nb - 1] / 2.f && e < s.nu[nb - 1] + s.widFlx[nb - 1] / 2.f) {
+      s.inSpectrumErg[nb - 1] += hflux[j];
+      ++count[nb - 1];
+    }
+  }
+  for (int i = 0; i < nb; ++i) {
+    if (count[i] > 0) s.inSpectrumErg[i] = s.inSpectrumErg[i] / (double)(float)count[i];
+    s.inSpectrumPhot[i] = s.inSpectrumErg[i] / (double)(s.nu[i] * kHcRyd);
+  }
+  for (int i = 1; i < nb - 1; ++i) {
+    if (s.inSpectrumErg[i] <= 0. && s.inSpectrumErg[i - 1] > 0.) {
+      for (int j = i + 1; j < nb; ++j)
+        if (s.inSpectrumErg[j] > 0.) {
+          s.inSpectrumErg[i] = s.inSpectrumErg[i - 1] - (double)(s.nu[i] - s.nu[i - 1]) *
+                                                            (s.inSpectrumErg[i - 1] - s.inSpectrumErg[j]) /
+                                                            (double)(s.nu[j] - s.nu[i - 1]);
+          break;
+        }
+    }
+  }
+}
+
 void setContinuum(Setup& s) {
   const int nb = s.nbins;
   s.lymanP = locate(s.nu.data(), nb, 1.f);
@@ -757,6 +892,8 @@ void setContinuum(Setup& s) {
       s.inSpectrumErg[i] = getFlux(s, s.nu[i], s.p.TStellar);
       s.inSpectrumPhot[i] = s.inSpectrumErg[i] / ((double)s.nu[i] * (double)kHcRyd);
     }
+  } else if (s.p.spID == "sb99") {
+    readSB99(s);
   } else {
     readSpectrumFile(s, s.inSpectrumErg);
     for (int i = 0; i < nb; ++i) {
@@ -784,8 +921,9 @@ void setContinuum(Setup& s) {
   for (int i = 0; i < nb; ++i) if (s.srcCDF[i] >= maxp) s.srcCDF[i] = 1.f;
   if (s.p.contShape == "blackbody") { nce = kPi * nce * kHPlanck; ncp = kPi * ncp * kHPlanck; }
   s.normConstantErg = nce; s.normConstantPhot = ncp;
-  // Lstar <-> LPhot (source/continuum_mod.f90:308-335)
+  // Lstar <-> LPhot (source/continuum_mod.f90:308-335), for one source only
   s.LPhot = s.p.LPhot; s.LStar = s.p.LStar;
+  if (s.p.starsIn.size() > 1) return;
   if (s.LPhot > 0.f) {
     if (s.p.contShape == "powerlaw") fail("setContinuum: powerlaw does not allow Lphot; use Lstar");
     s.RStar = sqrtf(s.LPhot / (kFourPi * ncp * kCRyd));
@@ -1063,10 +1201,26 @@ void buildSetup(Setup& s, const std::string& inputFile, const std::string& dataD
     buildEmissionTables(s);
     buildBalanceTables(s);
   }
-  setContinuum(s);
+  // every source's spectrum and position (multiPhotoSources), source 1 last so that the
+  // single-source fields hold it
+  const int nStars = s.p.starsIn.empty() ? 1 : (int)s.p.starsIn.size();
+  s.stars.assign(nStars, Setup::Star{});
+  for (int i = nStars - 1; i >= 0; --i) {
+    if (!s.p.starsIn.empty()) useStar(s.p, s.p.starsIn[i]);
+    setContinuum(s);
+    s.stars[i].cdf = s.srcCDF;
+  }
   fillGrid(s);
   if (s.p.lgPlaneIonization) setPlaneSource(s);
-  setStarPosition(s);
+  for (int i = nStars - 1; i >= 0; --i) {
+    if (!s.p.starsIn.empty()) useStar(s.p, s.p.starsIn[i]);
+    setStarPosition(s);
+    Setup::Star& st = s.stars[i];
+    for (int d = 0; d < 3; ++d) { st.pos[d] = s.starPos[d]; st.idx[d] = s.starIdx[d]; }
+    st.TStellar = s.p.TStellar;
+    st.LStar = s.p.starsIn.empty() ? s.LStar : s.p.starsIn[i].LStar;
+  }
+  s.stars[0].cdf = s.srcCDF;   // (a plane source's luminosity and CDF cut are set above)
   if (s.p.lgDust) {   // dustDriver's initial grain temperatures (source/dust_mod.f90:66-73)
     const size_t planes = (size_t)(s.dust.nSpecies + 1) * (s.dust.nSizes + 1);
     s.Tdust.assign(planes * ((size_t)s.nCells + 1), 50.f);

@@ -14,6 +14,17 @@ constexpr int kNHeIlevel = 9;       // nHeIlevel
 constexpr int kNHeIIlevel = 9;      // nHeIIlevel
 constexpr int kNAngles = 180;       // Compton theta bins (source/ph_mod.f90:1889)
 
+// One ionising source of a multiPhotoSources file (setMultiPhotoSources,
+// source/set_input_mod.f90:741-800): a row of Tstellar, Lstar, contShape,
+// position (fractions of the axes' last values) and, for a spectrum file, its
+// reader (spID 'rauch' or 'sb99') and the Starburst99 time step.
+struct StarIn {
+  float TStellar = 0.f, LStar = 0.f;
+  std::string contShape, spID;
+  float pos[3] = {0.f, 0.f, 0.f};
+  float tStep = 0.f;
+};
+
 // Parsed input deck (keyword grammar of source/set_input_mod.f90:140-500,
 // defaults of :33-117).
 struct Params {
@@ -46,7 +57,11 @@ struct Params {
   float viewTheta[2] = {0.f, 0.f}, viewPhi[2] = {0.f, 0.f};
   bool haveStarPos = false, haveLStar = false, haveTStellar = false;
   bool haveContShape = false, haveNPhotons = false, haveAbundance = false;
-  std::string contShape;          // "blackbody" | "powerlaw" | a spectrum file (read as 'rauch')
+  std::string contShape;          // "blackbody" | "powerlaw" | a spectrum file (read by spID)
+  std::string spID = "rauch";     // reader of a spectrum file: 'rauch' or 'sb99'
+  float tStep = 0.f;              // the Starburst99 time step a 'sb99' file is read at
+  std::string multiPhotoSources;  // the file of several ionising sources
+  std::vector<StarIn> starsIn;    // its rows (empty: one source from the deck's keywords)
   std::string densityFile, abundanceFile, NdustFile;
   std::string dustFile[2];
   std::string baseDir;            // directory the deck's relative paths are resolved against
@@ -187,6 +202,14 @@ struct Setup {
   std::vector<float> Tdust;                          // [nSpecies+1][nSizes+1][nCells+1]
   int starIdx[3] = {-1, -1, -1};
   float starPos[3] = {0.f, 0.f, 0.f};
+  // every ionising source (source 1 first; its values are also the scalars above)
+  struct Star {
+    float LStar = 0.f, TStellar = 0.f;
+    float pos[3] = {0.f, 0.f, 0.f};       // [cm]
+    int idx[3] = {-1, -1, -1};            // its cell, 1-based; -1 outside the grid
+    std::vector<float> cdf;               // inSpectrumProbDen(i,:)
+  };
+  std::vector<Star> stars;
 
   inline int activeAt(int i, int j, int k) const {   // 1-based Fortran indices
     return active[(size_t)(i - 1) + (size_t)nx * ((size_t)(j - 1) + (size_t)ny * (size_t)(k - 1))];

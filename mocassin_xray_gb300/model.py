@@ -215,11 +215,12 @@ class Context:
 
     def transport(self, n_packets: int, seed: int = 0, counter_base: int = 0, precision: int = abi.PREC_FP32_GEOM,
                   zero: bool = True, n_photons_norm: int = 0, block_size: int = 0, grid_mult: int = 0,
-                  emit_batch: int = 0, handoff_emissions: int = 0) -> abi.TransportStats:
-        """handoff_emissions: re-emissions after which a history moves to the
-        trapped-packet kernel (0 = library default, -1 = never); it changes
-        only where a history runs, never its result."""
-        o = abi.TransportOpts(istar=1, precision=precision, n_packets=n_packets, seed=seed, counter_base=counter_base,
+                  emit_batch: int = 0, handoff_emissions: int = 0, istar: int = 1) -> abi.TransportStats:
+        """Packets of ionising source `istar` (1-based).  handoff_emissions:
+        re-emissions after which a history moves to the trapped-packet kernel
+        (0 = library default, -1 = never); it changes only where a history
+        runs, never its result."""
+        o = abi.TransportOpts(istar=istar, precision=precision, n_packets=n_packets, seed=seed, counter_base=counter_base,
                               n_photons_norm=n_photons_norm, zero_estimators=1 if zero else 0,
                               block_size=block_size, grid_mult=grid_mult, emit_batch=emit_batch,
                               handoff_emissions=handoff_emissions)

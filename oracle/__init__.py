@@ -229,14 +229,18 @@ def opacity(setup, te=None, ne=None, ionden=None, hden=None, gaunt_te=None, comp
 
 def transport(setup, opacity_arr, rec_pdf, total_lines, ne=None, n: int = 1000, seed: int = 0,
               counter_base: int = 0, nthreads: int = 1, n_photons_norm: int = 0,
-              sca_opac=None, dust_pdf=None):
-    """Oracle transport of packets [counter_base, counter_base+n); returns (Jste, escaped, stats)."""
+              sca_opac=None, dust_pdf=None, istar: int = 1):
+    """Oracle transport of packets [counter_base, counter_base+n) of ionising source `istar` (its
+    luminosity, position and CDF: energyPacketDriver(iStar, ...), source/photon_mod.f90:28-416);
+    returns (Jste, escaped, stats)."""
     from mocassin_xray_gb300 import abi
     i = setup.info
     C1, nb = i.n_cells + 1, i.nbins
+    star = setup.get(abi.SARR_STARS).reshape(-1, 8)[istar - 1]
     keep = dict(
         x=setup.get(abi.ARR_XAXIS), y=setup.get(abi.ARR_YAXIS), z=setup.get(abi.ARR_ZAXIS),
-        act=setup.get(abi.ARR_ACTIVE), nu=setup.get(abi.ARR_NU), cdf=setup.get(abi.ARR_SRC_CDF),
+        act=setup.get(abi.ARR_ACTIVE), nu=setup.get(abi.ARR_NU),
+        cdf=np.ascontiguousarray(setup.get(abi.SARR_SRC_CDFS).reshape(-1, nb)[istar - 1]),
         kn=setup.get(abi.ARR_KN_SIGMA_T), kncdf=setup.get(abi.ARR_KN_CDF), pc=setup.get(abi.ARR_PCOMP),
         op=np.ascontiguousarray(opacity_arr, dtype=np.float32),
         rec=np.ascontiguousarray(rec_pdf, dtype=np.float32),
@@ -253,9 +257,9 @@ def transport(setup, opacity_arr, rec_pdf, total_lines, ne=None, n: int = 1000, 
                     kn_cdf=_p(keep["kncdf"]), pcomp=_p(keep["pc"]), opacity=_p(keep["op"]),
                     sca_opac=_p(keep["sca"]), rec_pdf=_p(keep["rec"]), dust_pdf=_p(keep["dust"]),
                     total_lines=_p(keep["tl"]), ne=_p(keep["ne"]), ion_edge1=i.ion_edge1, r_out=i.r_out,
-                    delta_e=float(np.float32(i.l_star)) / norm)
-    s.star_pos[:] = list(i.star_pos)
-    s.star_idx[:] = list(i.star_idx)
+                    delta_e=float(np.float32(star[0])) / norm)
+    s.star_pos[:] = [float(v) for v in star[2:5]]
+    s.star_idx[:] = [int(v) for v in star[5:8]]
     s.n_angle = i.n_angle_bins
     s.plane = i.plane_ionization
     s.tot_phi, pt, pp = view_bins(i.n_angle_bins, i.view_theta, i.view_phi)
