@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(128) adjointCombineKernel(AdjointArgs a) {
     const double dRdp = (a.rPp[cell] - a.rPm[cell]) / dp;
     const bool root = hold == 0 && isfinite(dRdT) && dRdT != 0. && isfinite(dRdp);
     if (root) dTdp = -dRdp / dRdT;
-    else if (a.held) atomicAdd(a.held, 1ull);
+    else if (hold == 0 && a.held) atomicAdd(a.held, 1ull);   // a root whose dR/dTe is unusable
   }
   if (a.dTdp) a.dTdp[cell] = dTdp;
   for (int k = 0; k < a.nL; ++k) {

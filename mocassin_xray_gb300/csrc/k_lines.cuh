@@ -78,7 +78,7 @@ struct AdjointArgs {
   const uint8_t* hold;        // [C+1] 0 root, 1 Te held (no root), 2 no photon hit, 3 no converged balance
   double* dLdp;               // [nL][C+1] out
   double* dTdp;               // [C+1] out, or null
-  unsigned long long* held;   // out: cells whose Te was held (hold = 1 or dR/dTe unusable), or null
+  unsigned long long* held;   // out: cells with hold = 0 whose dR/dTe or dR/dp is unusable (Te held), or null
   int32_t nCells, nL;
 };
 

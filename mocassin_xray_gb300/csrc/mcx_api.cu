@@ -2057,6 +2057,7 @@ extern "C" int mcx_adjoint(mcx_ctx* c, const mcx_sens_opts* o, mcx_adjoint_out* 
     CK(cudaStreamSynchronize(st), "mcx_adjoint");
     return MCX_OK;
   };
+  bool countHeld = true;   // the first combination counts the roots it cannot use
   AdjointArgs aa{};
   aa.rTp = res[1].p; aa.rTm = res[2].p; aa.lTp = lum[1].p; aa.lTm = lum[2].p; aa.teP = tP.p; aa.teM = tM.p;
   aa.rPp = res[3].p; aa.rPm = res[4].p; aa.lPp = lum[3].p; aa.lPm = lum[4].p;
@@ -2098,6 +2099,7 @@ extern "C" int mcx_adjoint(mcx_ctx* c, const mcx_sens_opts* o, mcx_adjoint_out* 
       mr[cell] = hh[cell] == 0;
       ms[cell] = hh[cell] <= 1;
       out->no_solution_cells += hh[cell] == 3;
+      out->pinned_cells += hh[cell] == 1;
     }
     CK(cudaMemcpyAsync(hold.p, hh.data(), C1, cudaMemcpyHostToDevice, st), "h2d hold");
     CK(cudaMemcpyAsync(maskRoot.p, mr.data(), C1, cudaMemcpyHostToDevice, st), "h2d mask");
@@ -2128,16 +2130,14 @@ extern "C" int mcx_adjoint(mcx_ctx* c, const mcx_sens_opts* o, mcx_adjoint_out* 
     }
     CK(cudaMemcpyAsync(c->hden.p, hd.data(), C1 * sizeof(float), cudaMemcpyHostToDevice, st), "h2d Hden");
     if (rc == MCX_OK) {
-      aa.pP = pP.p; aa.pM = pM.p; aa.dTdp = dTdp.p; aa.held = held.p;
+      aa.pP = pP.p; aa.pM = pM.p; aa.dTdp = dTdp.p; aa.held = countHeld ? held.p : nullptr;
+      countHeld = false;
       CK(launchAdjointCombine(aa, st), "adjoint kernel");
       if (out->dL_dhden)
         CK(cudaMemcpyAsync(out->dL_dhden, dLdp.p, LC * sizeof(double), cudaMemcpyDeviceToHost, st), "d2h");
       if (out->dte_dhden)
         CK(cudaMemcpyAsync(out->dte_dhden, dTdp.p, C1 * sizeof(double), cudaMemcpyDeviceToHost, st), "d2h");
-      unsigned long long nh = 0;
-      CK(cudaMemcpyAsync(&nh, held.p, sizeof(nh), cudaMemcpyDeviceToHost, st), "d2h");
       CK(cudaStreamSynchronize(st), "mcx_adjoint");
-      out->pinned_cells = (int64_t)nh;
     }
   }
   // each abundance (1 +- h), one parameter shared by every cell
@@ -2154,7 +2154,9 @@ extern "C" int mcx_adjoint(mcx_ctx* c, const mcx_sens_opts* o, mcx_adjoint_out* 
     ab = a0;
     invalidateBalanceGraphs(*c->balance);
     if (rc != MCX_OK) break;
-    aa.pP = nullptr; aa.pM = nullptr; aa.dpScalar = (double)ap - (double)am; aa.dTdp = nullptr; aa.held = nullptr;
+    aa.pP = nullptr; aa.pM = nullptr; aa.dpScalar = (double)ap - (double)am; aa.dTdp = nullptr;
+    aa.held = countHeld ? held.p : nullptr;
+    countHeld = false;
     CK(launchAdjointCombine(aa, st), "adjoint kernel");
     CK(cudaMemcpyAsync(hostL.data(), dLdp.p, LC * sizeof(double), cudaMemcpyDeviceToHost, st), "d2h");
     CK(cudaStreamSynchronize(st), "mcx_adjoint");
@@ -2164,7 +2166,14 @@ extern "C" int mcx_adjoint(mcx_ctx* c, const mcx_sens_opts* o, mcx_adjoint_out* 
       out->dL_dabun[(size_t)k * o->n_abun + q] = t;
     }
   }
-  if (rc == MCX_OK) rc = copyState(c, s1, false);
+  if (rc == MCX_OK) {
+    // roots whose dR/dTe (or dR/dp) the first combination found unusable also keep their Te
+    unsigned long long nh = 0;
+    CK(cudaMemcpyAsync(&nh, held.p, sizeof(nh), cudaMemcpyDeviceToHost, st), "d2h");
+    CK(cudaStreamSynchronize(st), "mcx_adjoint");
+    out->pinned_cells += (int64_t)nh;
+    rc = copyState(c, s1, false);
+  }
   cudaEventRecord(t1, st);
   cudaEventSynchronize(t1);
   cudaEventElapsedTime(&out->kernel_ms, t0, t1);
