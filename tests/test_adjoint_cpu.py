@@ -101,3 +101,39 @@ def test_ift_abundance_gradient_equals_root_differences(converged, oracle_lib):
         lum[sign] = (oracle_lib.line_cell_luminosities(s, T, t, n, x, cells, LINES[:1], abun=ab), float(ab[z - 1]))
     fd = (lum[1.0][0] - lum[-1.0][0]) / (lum[1.0][1] - lum[-1.0][1])
     np.testing.assert_allclose(g["dL_dabun"][:, 0, :], fd, rtol=1e-2, atol=1e-3 * np.abs(fd).max())
+
+
+def test_ift_xray_chemistry_equals_root_differences(tmp_path, oracle_lib, data_dir):
+    """The same on the X-ray chemistry (Mg, Si, Fe with inner shells and Auger electrons, 27 stages):
+    J is kept only in a dozen cells, so that the balances run on those alone."""
+    s = Setup(configs.xray_gas(tmp_path / "xr", n=7, packets=4000), data_dir)
+    T = oracle_lib.BalanceTables(s)
+    te0, ne0, ion0 = s.get(abi.ARR_TE), s.get(abi.ARR_NE), s.get(abi.ARR_IONDEN)
+    op = oracle_lib.opacity(s)
+    rec, tl = oracle_lib.emission(s, 10000.0, for_lines=oracle_lib.for_lines_emission(T, te0, ne0, ion0))
+    j, _, _ = oracle_lib.transport(s, op, rec, tl, n=20000, seed=3, nthreads=4)
+    j *= 1e-9
+    lit = np.nonzero(j.sum(axis=0)[1:] > 0)[0] + 1
+    cells = np.sort(np.random.default_rng(3).choice(lit, size=min(12, lit.size), replace=False))
+    keep = np.zeros(j.shape[1], bool)
+    keep[cells] = True
+    j = np.where(keep[None, :], j, 0.0)
+    te, ne, ion, _, _, _, _ = oracle_lib.balance(T, j, te0, ne0, ion0, nthreads=4)
+    te, ne, ion, ok = _roots(oracle_lib, T, j, te, ne, ion, cells)
+    cells = cells[ok[cells]]
+    assert cells.size >= 6
+    lines = [(8, 3, 3, 4), (10, 3, 1, 4)]
+    g = oracle_lib.ift_line_gradient(s, T, j, te, ne, ion, lines, cells, abun_z=[26], h=H)
+    hden = T.k["hden"].astype(np.float64)
+    lum = {}
+    for sign in (1.0, -1.0):
+        hd = (hden * (1.0 + sign * H)).astype(np.float32)
+        t, n, x, ok2 = _roots(oracle_lib, T, j, te, ne, ion, cells, hden=hd)
+        assert ok2[cells].all()
+        lum[sign] = (oracle_lib.line_cell_luminosities(s, T, t, n, x, cells, lines, hden=hd),
+                     hd[cells].astype(np.float64))
+    fd = (lum[1.0][0] - lum[-1.0][0]) / (lum[1.0][1] - lum[-1.0][1])
+    for k in range(len(lines)):
+        assert np.count_nonzero(fd[k]) >= cells.size // 2
+        np.testing.assert_allclose(g["dL_dhden"][k], fd[k], rtol=1e-2, atol=1e-3 * np.abs(fd[k]).max())
+    assert np.all(np.isfinite(g["dL_dabun"])) and np.abs(g["dte_dhden"]).max() > 0
