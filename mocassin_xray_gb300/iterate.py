@@ -5,7 +5,7 @@ Each iteration runs, for the single mother grid of the deck:
 
 1. ``mcx_opacity``   - ionizationDriver for every cell (skip rule from the 2nd iteration)
 2. ``mcx_emission``  - emissionDriver for every cell (same skip rule)
-3. ``mcx_transport`` - energyPacketDriver for the stellar source: nPhotons packets
+3. ``mcx_transport`` - energyPacketDriver for each ionising source: nPhotons(i) packets
 4. ``mcx_normalize_j`` - J x 1e-9 (and / 8 for an octant grid)
 5. ``mcx_balance``   - updateCell for every cell (TeOld/NeOld saved first)
 
@@ -45,12 +45,21 @@ class IterationReport:
     transport: dict
 
 
+def _add_transport_stats(a: abi.TransportStats, b: abi.TransportStats) -> abi.TransportStats:
+    for k in ("crossings", "interactions", "absorptions", "scatterings", "escaped", "line_escapes", "trapped",
+              "emissions", "q_phot", "kernel_ms", "handed_off"):
+        setattr(a, k, getattr(a, k) + getattr(b, k))
+    return a
+
+
 def iterate_mc(setup: Setup, ctx: Context | None = None, seed: int = 0, n_photons: int | None = None,
                max_iterations: int | None = None, precision: int = abi.PREC_FP32_GEOM,
                min_convergence: float | None = None, auto_packets: tuple[float, float, int] | None = None,
                callback=None, group=None, counter_base: int = 0) -> list[IterationReport]:
     """Runs MC iterations until totPercent >= minConvergence or maxIterateMC.
 
+    n_photons: packets of each ionising source per iteration (default: the
+    set-up's nPhotons / nStars).
     auto_packets = (convIncPercent, nPhotIncrease, maxPhotons) enables the
     reference's packet increase when convergence stalls (autoPackets).
     group: a torch.distributed process group (or True for the default one)
@@ -62,6 +71,8 @@ def iterate_mc(setup: Setup, ctx: Context | None = None, seed: int = 0, n_photon
         ctx = Context(0)
         ctx.load(setup)
     info = setup.info
+    n_stars = max(int(info.n_stars), 1)
+    # packets per source: nPhotons(i) = nPhotons / nStars (the set-up's n_photons is already per source)
     n = int(n_photons if n_photons is not None else info.n_photons)
     if n <= 0:
         raise ValueError("nPhotons must be positive")
@@ -75,12 +86,21 @@ def iterate_mc(setup: Setup, ctx: Context | None = None, seed: int = 0, n_photon
             ms = {}
             ms["opacity"] = ctx.opacity(it).kernel_ms
             ms["emission"] = ctx.emission(it).kernel_ms
-            if group is not None:
-                st = transport_sharded(ctx, n, seed, counter_base + (it - 1) * COUNTER_STRIDE, precision,
-                                       group=None if group is True else group)
-            else:
-                st = ctx.transport(n, seed=seed, counter_base=counter_base + (it - 1) * COUNTER_STRIDE,
-                                   precision=precision, zero=True, n_photons_norm=n)
+            st = None
+            for istar in range(1, n_stars + 1):
+                # the sources one after another on consecutive counter ranges (source/iteration_mod.f90:729-753)
+                base = counter_base + (it - 1) * COUNTER_STRIDE + (istar - 1) * n
+                if istar > 1:
+                    # the reference zeroes escapedPackets before each source (:736)
+                    shape, dt = ctx._shape(abi.ARR_ESCAPED)
+                    ctx.put(abi.ARR_ESCAPED, np.zeros(shape, dt))
+                if group is not None:
+                    one = transport_sharded(ctx, n, seed, base, precision, group=None if group is True else group,
+                                            istar=istar, zero=istar == 1, reduce=istar == n_stars)
+                else:
+                    one = ctx.transport(n, seed=seed, counter_base=base, precision=precision, zero=istar == 1,
+                                        n_photons_norm=n, istar=istar)
+                st = one if st is None else _add_transport_stats(st, one)
             ms["transport"] = st.kernel_ms
             ctx.normalize_j()
             bs = ctx.balance()
@@ -92,7 +112,7 @@ def iterate_mc(setup: Setup, ctx: Context | None = None, seed: int = 0, n_photon
             C = setup.n_cells
             tot = 100.0 * bs.converged / C
             rep = IterationReport(
-                iteration=it, n_photons=n, conv_percent=tot, no_hit_percent=100.0 * bs.no_hit / C,
+                iteration=it, n_photons=n * n_stars, conv_percent=tot, no_hit_percent=100.0 * bs.no_hit / C,
                 no_ion_bal_percent=100.0 * bs.no_ion_bal / C, no_te_bal_percent=100.0 * bs.no_te_bal / C,
                 te_change_max=float(dte[upd].max()) if upd.any() else 0.0,
                 te_change_mean=float(dte[upd].mean()) if upd.any() else 0.0,

@@ -44,22 +44,25 @@ def allreduce_sum(a, group=None):
     return a
 
 
-def transport_sharded(ctx, n_total: int, seed: int, counter_base: int, precision: int, group=None, **opts):
+def transport_sharded(ctx, n_total: int, seed: int, counter_base: int, precision: int, group=None, istar: int = 1,
+                      zero: bool = True, reduce: bool = True, **opts):
     """The transport phase of one iteration sharded over the ranks of `group`
     (source/iteration_mod.f90:729-753 and the MPI_Allreduce of Jste and
     escapedPackets at :953): this rank transports packets
-    [counter_base + first, + count) of the iteration's n_total (deltaE =
-    Lstar / n_total on every rank), then Jste and the escape tallies are summed
-    over the group and put back into the context, and the returned statistics
-    are the group's totals."""
+    [counter_base + first, + count) of source `istar`'s n_total (deltaE =
+    Lstar(istar) / n_total on every rank), then (with `reduce`) Jste and the
+    escape tallies are summed over the group and put back into the context; the
+    returned statistics are the group's totals.  Several sources: `zero` for
+    the first only and `reduce` after the last, so that each rank's estimators
+    hold its share of every source before the one sum."""
     import torch
     import torch.distributed as dist
     from . import abi
     rank, world = dist.get_rank(group), dist.get_world_size(group)
     first, count = shard_packets(n_total, rank, world)
-    st = ctx.transport(count, seed=seed, counter_base=counter_base + first, precision=precision, zero=True,
-                       n_photons_norm=n_total, **opts)
-    for arr in (abi.ARR_JSTE, abi.ARR_ESCAPED):
+    st = ctx.transport(count, seed=seed, counter_base=counter_base + first, precision=precision, zero=zero,
+                       n_photons_norm=n_total, istar=istar, **opts)
+    for arr in ((abi.ARR_JSTE, abi.ARR_ESCAPED) if reduce else ()):
         ctx.put(arr, allreduce_sum(ctx.get(arr), group))
     names = ("crossings", "interactions", "absorptions", "scatterings", "escaped", "line_escapes", "trapped",
              "emissions")

@@ -66,3 +66,26 @@ def test_iteration_runs_every_source(two, data_dir):
     assert tr.escaped + tr.line_escapes + tr.trapped == 40000
     assert st.balance.cells_updated > 0.5 * s.n_cells
     ctx.close()
+
+
+def test_python_loop_equals_the_abi_iteration(two):
+    """iterate_mc's source loop (one transport per source, nPhotons / nStars each on consecutive counter
+    ranges, the escape tallies zeroed before each source) gives the same iteration as mcx_iterate."""
+    from mocassin_xray_gb300 import iterate_mc
+    s, _, _, _, _ = two
+    a = Context(0)
+    a.load(s)
+    rep = iterate_mc(s, a, seed=7, n_photons=15000, max_iterations=1, precision=abi.PREC_FP64,
+                     min_convergence=101.0)
+    assert rep[0].n_photons == 30000
+    b = Context(0)
+    b.load(s)
+    st = b.iterate(30000, seed=7, transport_precision=abi.PREC_FP64, balance_precision=abi.BAL_FP64,
+                   emission_precision=abi.PHASE_EXACT)
+    assert rep[0].transport["escaped"] == st.transport.escaped
+    assert rep[0].transport["emissions"] == st.transport.emissions
+    np.testing.assert_array_equal(a.get(abi.ARR_JSTE), b.get(abi.ARR_JSTE))
+    np.testing.assert_array_equal(a.get(abi.ARR_ESCAPED), b.get(abi.ARR_ESCAPED))
+    np.testing.assert_array_equal(a.get(abi.ARR_TE), b.get(abi.ARR_TE))
+    a.close()
+    b.close()
