@@ -107,10 +107,14 @@ def write_grid(out_dir: str | Path, setup: Setup, state: dict) -> None:
         (d / "grid2.out").write_text("\n".join(g2) + "\n")
     if i.lg_dust:
         (d / "dustGrid.out").write_text("\n".join(gd) + "\n \n")
-    sp = [_f(i.star_pos[k] / ax[k][-1]) if ax[k][-1] != 0 else "0.0" for k in range(3)]
-    (d / "photoSource.out").write_text(
-        f"1  number of photon sources\n'blackbody' 0.0 {_f(i.l_star)} {int(i.n_photons)} {' '.join(sp)} 'none' 0.0\n"
-        "(contShape, T_eff[K], L_* [E36 erg/s], nPackets, (x,y,z) position, spID, tstep)\n")
+    # every ionising source: T_eff, L*, its packets and its position as fractions of the axes' last values
+    stars = setup.get(abi.SARR_STARS).reshape(-1, 8)
+    rows = [f"{len(stars)}  number of photon sources"]
+    for st in stars:
+        sp = [_f(st[2 + k] / ax[k][-1]) if ax[k][-1] != 0 else "0.0" for k in range(3)]
+        rows.append(f"'blackbody' {_f(st[1])} {_f(st[0])} {int(i.n_photons)} {' '.join(sp)} 'none' 0.0")
+    rows.append("(contShape, T_eff[K], L_* [E36 erg/s], nPackets, (x,y,z) position, spID, tstep)")
+    (d / "photoSource.out").write_text("\n".join(rows) + "\n")
     nu = setup.get(abi.ARR_NU)
     g3 = ["1", "0.0 convWriteGrid", "F 0.0 0 0 lgAutoPackets", f"{_logical(i.symmetric_xyz)} lgSymmetricXYZ",
           "F lgTalk", "F lg1D", f"{i.nbins} nbins", "0.0 nuStepSize", f"{_f(nu[-1])} nuMax",
@@ -122,7 +126,7 @@ def write_grid(out_dir: str | Path, setup: Setup, state: dict) -> None:
           f"{i.n_species} {i.n_sizes} nSpecies, nSizes", "101 resLinesTransfer", "T lgDustScattering",
           f"{i.n_angle_bins} nAngleBins", "0 0 continuumCube", "F lgPhotoelectric", "F lgTraceHeating", "0.0 Ldiffuse",
           "0.0 Tdiffuse", "none shapeDiffuse", "0 nPhotonsDiffuse", "0 emittingGrid", f"{i.nstages} nstages",
-          "F lgMultiStars", f"{_logical(i.lg_compton)} compton?", "0.0 0.0 pwlMin, pwlMax", "F nahar?",
+          f"{_logical(i.n_stars > 1)} lgMultiStars", f"{_logical(i.lg_compton)} compton?", "0.0 0.0 pwlMin, pwlMax", "F nahar?",
           "T badnell?", "F lgSeparateSED", "F 2D geometry?"]
     (d / "grid3.out").write_text("\n".join(g3) + "\n")
 
