@@ -66,3 +66,21 @@ def test_xray_plane_benchmarks_parse(tmp_path, data_dir, name, lstar_ratio):
 def test_resonance_line_transfer_deck_is_rejected(tmp_path, data_dir):
     with pytest.raises(RuntimeError, match="resLinesTransfer"):
         Setup(_deck(tmp_path, "X01"), data_dir)
+
+
+def test_multistar_example_parses(tmp_path, data_dir):
+    """The reference's multistar example (examples/multistar): 30 sources with Starburst99 spectra at
+    t = 1e6 yr, spread over an octant shell; every source gets the spectrum of its file and its cell."""
+    src = Path(REF) / "examples" / "multistar" / "input"
+    if not src.is_dir():
+        pytest.skip("examples/multistar is not in the reference tree")
+    shutil.copytree(src, tmp_path / "input")
+    s = Setup(tmp_path / "input" / "input.in", data_dir)
+    i = s.info
+    assert i.n_stars == 30 and i.symmetric_xyz and (i.nx, i.ny, i.nz) == (52, 52, 52)
+    assert i.n_photons == 1000000 // 30
+    stars = s.get(abi.SARR_STARS).reshape(-1, 8)
+    assert np.all(stars[:, 0] == np.float32(1000.0))
+    assert np.all((stars[:, 5:8] >= 1) & (stars[:, 5:8] <= 52))
+    cdfs = s.get(abi.SARR_SRC_CDFS).reshape(30, -1)
+    assert np.all(cdfs[:, -1] == 1.0) and np.all(np.diff(cdfs, axis=1) >= 0)
