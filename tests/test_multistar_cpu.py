@@ -135,3 +135,29 @@ def test_oracle_sources_conserve_energy(two, oracle_lib):
         assert esc.sum() == pytest.approx(float(stars[i - 1, 0]), rel=1e-9)
         fields.append(j)
     assert not np.array_equal(fields[0], fields[1])
+
+
+def test_ragged_source_files(tmp_path, data_dir):
+    """A file that ends before its last source, one with no sources, and a missing file are refused; a
+    source's record may run over two lines (list-directed READ)."""
+    deck = configs.multi_source(tmp_path / "cut", SOURCES)
+    src = deck.parent / "sources.in"
+    lines = src.read_text().splitlines()
+    src.write_text("\n".join(lines[:2] + [lines[2].rsplit(" ", 3)[0]]) + "\n")
+    with pytest.raises(RuntimeError, match="ends before its last source"):
+        Setup(deck, data_dir)
+    src.write_text("0\n")
+    with pytest.raises(RuntimeError, match="invalid number of sources"):
+        Setup(deck, data_dir)
+    src.unlink()
+    with pytest.raises(RuntimeError, match="can't open"):
+        Setup(deck, data_dir)
+    # the second source's record split over two lines reads as one
+    deck2 = configs.multi_source(tmp_path / "split", SOURCES)
+    src2 = deck2.parent / "sources.in"
+    lines = src2.read_text().splitlines()
+    head, tail = lines[2].split(" ", 3)[:3], lines[2].split(" ", 3)[3]
+    src2.write_text("\n".join(lines[:2] + [" ".join(head), tail]) + "\n")
+    s = Setup(deck2, data_dir)
+    ref = Setup(configs.multi_source(tmp_path / "ref", SOURCES), data_dir)
+    np.testing.assert_array_equal(s.get(abi.SARR_STARS), ref.get(abi.SARR_STARS))
