@@ -843,7 +843,9 @@ void readSB99(Setup& s) {
   std::vector<float> en(kSb99NuLim);
   for (int k = 0; k < kSb99NuLim; ++k) {
     const float lam = toF(block[k], 1, "sb99 wavelength");
-    const double logL = std::strtod(toS(block[k], 3, "sb99 log L").c_str(), nullptr);
+    std::string v = toS(block[k], 3, "sb99 log L");
+    for (auto& ch : v) if (ch == 'd' || ch == 'D') ch = 'e';   // Fortran double exponent
+    const double logL = std::strtod(v.c_str(), nullptr);
     // reversed into ascending frequency
     hflux[kSb99NuLim - 1 - k] = (std::pow(10., logL) * (double)(1.e-8f * (lam * lam))) / (double)c;
     en[kSb99NuLim - 1 - k] = (c / (lam * 1.e-8f)) / kCRyd;
