@@ -20,6 +20,7 @@ from __future__ import annotations
 
 import dataclasses
 import time
+from pathlib import Path
 
 import numpy as np
 
@@ -55,7 +56,8 @@ def _add_transport_stats(a: abi.TransportStats, b: abi.TransportStats) -> abi.Tr
 def iterate_mc(setup: Setup, ctx: Context | None = None, seed: int = 0, n_photons: int | None = None,
                max_iterations: int | None = None, precision: int = abi.PREC_FP32_GEOM,
                min_convergence: float | None = None, auto_packets: tuple[float, float, int] | None = None,
-               callback=None, group=None, counter_base: int = 0) -> list[IterationReport]:
+               callback=None, group=None, counter_base: int = 0,
+               out_dir: str | None = None) -> list[IterationReport]:
     """Runs MC iterations until totPercent >= minConvergence or maxIterateMC.
 
     n_photons: packets of each ionising source per iteration (default: the
@@ -65,7 +67,8 @@ def iterate_mc(setup: Setup, ctx: Context | None = None, seed: int = 0, n_photon
     group: a torch.distributed process group (or True for the default one)
     whose ranks share each iteration's packets (shard.transport_sharded: one
     sum of Jste and the escape tallies per iteration); every rank runs the
-    per-cell phases of every cell."""
+    per-cell phases of every cell.
+    out_dir: a directory to write summary.out into after every iteration."""
     own = ctx is None
     if own:
         ctx = Context(0)
@@ -120,6 +123,9 @@ def iterate_mc(setup: Setup, ctx: Context | None = None, seed: int = 0, n_photon
                 transport={k: getattr(st, k) for k in ("crossings", "interactions", "absorptions", "scatterings",
                                                        "escaped", "line_escapes", "trapped", "emissions")})
             reports.append(rep)
+            if out_dir is not None:
+                from .output import write_summary
+                write_summary(Path(out_dir) / "summary.out", rep)
             if callback:
                 callback(rep)
             if auto_packets and it > 1 and tot < 95.0 and tot_old > 0.0:

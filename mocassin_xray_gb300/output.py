@@ -5,7 +5,10 @@ from Context.line_luminosities():
   hydrogenic recombination lines, the 34 HeI recombination lines and the
   forbidden lines of the ions with multi-level data;
 * ``temperature.out`` - the mean ionic temperatures Te(elem, ion);
-* ``ionratio.out``    - the mean ionic fractions <ion> (Harrington et al. 1982).
+* ``ionratio.out``    - the mean ionic fractions <ion> (Harrington et al. 1982);
+
+and iterateMC's ``summary.out`` (source/iteration_mod.f90:1316-1350) from the
+iteration reports of ``iterate_mc``.
 
 Column order and line numbering (iLine) follow the reference's writers; the
 number formatting is plain whitespace-separated text rather than Fortran's
@@ -175,3 +178,19 @@ def write_sed(path: str | Path, setup: Setup, escaped: np.ndarray) -> float:
         out.append(f" Flux at 4.9GHz (must multiply by 1./(4 Pi D[cm]^2 to obtain units of [Jy]) : {flux:16.8g}")
     Path(path).write_text("\n".join(out) + "\n")
     return total
+
+
+def write_summary(path: str | Path, report, grid: int = 1) -> None:
+    """summary.out (iterateMC, source/iteration_mod.f90:1316-1350): four records per iteration, the
+    percentages of the grid's active cells that converged, that no packet reached, whose ionisation
+    balance and whose Te balance were not reached, each truncated to an integer; the file is rewritten
+    at the first iteration and appended to after it.  The records keep the reference's wording
+    (spelling included) so that scripts that parse it find their text."""
+    recs = [(report.conv_percent, "% conveged cells in grid "),
+            (report.no_hit_percent, "% no hit cells in grid "),
+            (report.no_ion_bal_percent, "% Ion balance not reached in grid "),
+            (report.no_te_bal_percent, "% Te balance not reached in grid")]
+    text = "".join(f" ! iterateMC: [Summary] Iteration {report.iteration:12d} ; {int(p):12d} {what}{grid:12d}\n"
+                   for p, what in recs)
+    with open(path, "w" if report.iteration == 1 else "a") as f:
+        f.write(text)
