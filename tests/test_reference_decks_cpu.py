@@ -84,3 +84,15 @@ def test_multistar_example_parses(tmp_path, data_dir):
     assert np.all((stars[:, 5:8] >= 1) & (stars[:, 5:8] <= 52))
     cdfs = s.get(abi.SARR_SRC_CDFS).reshape(30, -1)
     assert np.all(cdfs[:, -1] == 1.0) and np.all(np.diff(cdfs, axis=1) >= 0)
+
+
+@pytest.mark.parametrize("name", ["multigridgas", "multigridgasdust"])
+def test_multigrid_examples_rejected(tmp_path, data_dir, name):
+    """The reference's nested-grid examples (multiGrids) select a path outside this library: the
+    set-up refuses them with a message naming the keyword, instead of misreading them."""
+    src = Path(REF) / "examples" / name
+    if not (src / "input.in").is_file():
+        pytest.skip(f"examples/{name} is not in the reference tree")
+    shutil.copytree(src, tmp_path / "input")
+    with pytest.raises(RuntimeError, match="multiGrids"):
+        Setup(tmp_path / "input" / "input.in", data_dir)
